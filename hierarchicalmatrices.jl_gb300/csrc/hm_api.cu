@@ -1,0 +1,643 @@
+// C ABI of libhmgpu.so: KernelMatrix build (host planner + GPU compression)
+// and the hierarchical matvec.  See include/hmgpu.h for the contract.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "hm_kernels.cuh"
+#include "hm_plan.h"
+#include "hmgpu.h"
+
+using namespace hm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+int cuda_status(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return HM_OK;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? HM_ERR_ALLOC : HM_ERR_CUDA;
+}
+
+#define HM_CK(call)                                             \
+    do {                                                        \
+        int st_ = cuda_status((call), #call);                   \
+        if (st_) return st_;                                    \
+    } while (0)
+
+#define HM_TRY(call)                                            \
+    do {                                                        \
+        int st_ = (call);                                       \
+        if (st_) return st_;                                    \
+    } while (0)
+
+#define HM_CK_LAUNCH(what)                                      \
+    do {                                                        \
+        int st_ = cuda_status(cudaGetLastError(), what);        \
+        if (st_) return st_;                                    \
+    } while (0)
+
+constexpr int kSegRows = 64;
+#define HM_NSTAGES 5   // leaf_up, xfer_up, m2l, xfer_down, expand
+constexpr int kWarpCta = 256;
+
+inline unsigned warp_grid(int64_t warps) { return (unsigned)((warps * 32 + kWarpCta - 1) / kWarpCta); }
+
+// sin(pi t) in extended precision, rounded once; t is formed in double like
+// the reference's (n-2k+1)/2n.
+double sinpi_ext(double t)
+{
+    const long double pi = 3.141592653589793238462643383279502884L;
+    return (double)sinl(pi * (long double)t);
+}
+
+// chebyshevpoints(T, n) and chebyshevbarycentricweights(T, n), first kind
+// (src/BarycentricMatrix.jl:92-136).
+void chebyshev_first_kind(int n, std::vector<double> &x, std::vector<double> &w)
+{
+    x.assign(n, 0.0);
+    w.assign(n, 0.0);
+    const int nd2 = n / 2;
+    for (int k = 1; k <= nd2; ++k) x[k - 1] = sinpi_ext(((double)(n - 2 * k) + 1.0) / (double)(2 * n));
+    for (int k = 1; k <= nd2; ++k) x[n - k] = -x[k - 1];
+    for (int k = 1; k <= nd2 + 1 && k <= n; ++k) w[k - 1] = sinpi_ext(((double)(2 * k) - 1.0) / (double)(2 * n));
+    for (int k = 1; k <= nd2; ++k) w[n - k] = w[k - 1];
+    for (int k = 2; k <= n; k += 2) w[k - 1] *= -1.0;
+}
+
+// Transfer matrices between a box and its two halves, in the box's
+// normalised coordinate: T_c[m' * r + m] = L_m(u_m'), u = -1/2 + x_m'/2 for
+// the first half and 1/2 + x_m'/2 for the second, L_m the barycentric Lagrange
+// basis on the first-kind nodes.
+void transfer_matrices(int r, const std::vector<double> &x, const std::vector<double> &w,
+                       std::vector<double> &T)
+{
+    T.assign(2 * r * r, 0.0);
+    for (int c = 0; c < 2; ++c) {
+        for (int mp = 0; mp < r; ++mp) {
+            const long double u = (c == 0 ? -0.5L : 0.5L) + 0.5L * (long double)x[mp];
+            int hit = -1;
+            for (int m = 0; m < r; ++m)
+                if (u == (long double)x[m]) hit = m;
+            long double vals[HM_RMAX];
+            long double sum = 0.0L;
+            for (int m = 0; m < r; ++m) {
+                vals[m] = (hit >= 0) ? (m == hit ? 1.0L : 0.0L) : (long double)w[m] / (u - (long double)x[m]);
+                sum += vals[m];
+            }
+            for (int m = 0; m < r; ++m) T[c * r * r + mp * r + m] = (double)(vals[m] / sum);
+        }
+    }
+}
+
+}  // namespace
+
+struct hm_handle {
+    int kernel = 0, storage = HM_F64, r = 0;
+    int64_t nx = 0, ny = 0;
+    PlanStats stats;
+    int n_xslots = 0, n_yslots = 0, max_width = 0;
+    std::vector<void *> allocs;
+    int64_t device_bytes = 0;
+
+    double *d_x = nullptr, *d_y = nullptr, *d_cheb = nullptr, *d_lam = nullptr;
+    void *d_T = nullptr;               // transfer matrices in the storage type
+    void *d_V = nullptr, *d_F = nullptr, *d_P = nullptr;
+    hm_vpanel *d_vp = nullptr;
+    int n_vp = 0;
+    hm_xfer *d_up = nullptr;
+    std::vector<int> up_ptr;
+    hm_m2l_row *d_m2l_rows = nullptr;
+    int n_m2l_rows = 0;
+    hm_m2l_ent *d_m2l_ents = nullptr;
+    hm_xfer *d_down = nullptr;
+    std::vector<int> down_ptr;
+    hm_seg *d_segs = nullptr;
+    int n_segs = 0;
+    hm_piece *d_pieces = nullptr;
+
+    std::mutex mu;
+    struct Scratch { void *p = nullptr; size_t bytes = 0; };
+    std::map<void *, Scratch> scratch;   // per stream, grown stream-ordered
+    void *d_stage = nullptr;
+    size_t stage_bytes = 0;
+    cudaStream_t host_stream = nullptr;
+
+    // Optional per-stage timing: CUDA events recorded on the launching stream
+    // around each stage of hm_mul.
+    unsigned profile_mask = 0;      // bit i: time stage i
+    struct StageEvent { int stage; cudaEvent_t a, b; };
+    std::vector<StageEvent> events;
+    double stage_ms[HM_NSTAGES] = {0};
+    int64_t stage_launches[HM_NSTAGES] = {0};
+    int launches_per_mul = 0;
+
+    template <typename T>
+    int alloc(T **p, size_t count)
+    {
+        *p = nullptr;
+        if (count == 0) return HM_OK;
+        void *q = nullptr;
+        HM_CK(cudaMalloc(&q, count * sizeof(T)));
+        allocs.push_back(q);
+        device_bytes += (int64_t)(count * sizeof(T));
+        *p = static_cast<T *>(q);
+        return HM_OK;
+    }
+    template <typename T>
+    int upload(T **p, const std::vector<T> &v, cudaStream_t st)
+    {
+        int e = alloc(p, v.size());
+        if (e) return e;
+        if (!v.empty()) HM_CK(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+        return HM_OK;
+    }
+};
+
+namespace {
+
+int check_points(const double *x, int64_t n, const char *name)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        if (std::isnan(x[i])) { set_error("%s[%lld] is NaN", name, (long long)i); return HM_ERR_NAN; }
+        if (i > 0 && x[i] > x[i - 1]) {
+            set_error("%s is not in non-increasing order at index %lld (KernelMatrix needs descending points)",
+                      name, (long long)i);
+            return HM_ERR_UNSORTED;
+        }
+    }
+    return HM_OK;
+}
+
+template <typename S>
+int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, const std::vector<double> &lam,
+                 const std::vector<double> &T, const double *x, const double *y, cudaStream_t st)
+{
+    HM_TRY(h->alloc(&h->d_x, (size_t)h->nx));
+    HM_TRY(h->alloc(&h->d_y, (size_t)h->ny));
+    HM_CK(cudaMemcpyAsync(h->d_x, x, sizeof(double) * h->nx, cudaMemcpyHostToDevice, st));
+    HM_CK(cudaMemcpyAsync(h->d_y, y, sizeof(double) * h->ny, cudaMemcpyHostToDevice, st));
+    HM_TRY(h->upload(&h->d_cheb, cheb, st));
+    HM_TRY(h->upload(&h->d_lam, lam, st));
+    std::vector<S> Ts(T.begin(), T.end());
+    S *dT = nullptr;
+    HM_TRY(h->upload(&dT, Ts, st));
+    h->d_T = dT;
+
+    hm_vpanel *vp = nullptr; hm_fill_vpanel *vpf = nullptr;
+    HM_TRY(h->upload(&vp, P.vpanels, st));
+    HM_TRY(h->upload(&vpf, P.vpanel_fill, st));
+    h->d_vp = vp; h->n_vp = (int)P.vpanels.size();
+    HM_TRY(h->upload(&h->d_up, P.up, st));
+    h->up_ptr = P.up_level_ptr;
+    HM_TRY(h->upload(&h->d_m2l_rows, P.m2l_rows, st));
+    h->n_m2l_rows = (int)P.m2l_rows.size();
+    HM_TRY(h->upload(&h->d_m2l_ents, P.m2l_ents, st));
+    hm_fill_f *ff = nullptr;
+    HM_TRY(h->upload(&ff, P.f_fill, st));
+    HM_TRY(h->upload(&h->d_down, P.down, st));
+    h->down_ptr = P.down_level_ptr;
+    HM_TRY(h->upload(&h->d_segs, P.segs, st));
+    h->n_segs = (int)P.segs.size();
+    HM_TRY(h->upload(&h->d_pieces, P.pieces, st));
+    hm_fill_seg *sf = nullptr;
+    HM_TRY(h->upload(&sf, P.seg_fill, st));
+
+    S *V = nullptr, *F = nullptr, *Pn = nullptr;
+    HM_TRY(h->alloc(&V, (size_t)P.vstore_elems));
+    HM_TRY(h->alloc(&F, (size_t)P.fstore_elems));
+    HM_TRY(h->alloc(&Pn, (size_t)P.pstore_elems));
+    if (Pn) HM_CK(cudaMemsetAsync(Pn, 0, sizeof(S) * P.pstore_elems, st));
+    h->d_V = V; h->d_F = F; h->d_P = Pn;
+
+    FillArgs fa;
+    fa.x = h->d_x; fa.y = h->d_y; fa.cheb = h->d_cheb; fa.lam = h->d_lam; fa.r = h->r; fa.kernel = h->kernel;
+    if (h->n_vp) {
+        fill_vpanels<S><<<h->n_vp, 128, 0, st>>>(fa, vp, vpf, h->n_vp, V);
+        HM_CK_LAUNCH("fill_vpanels");
+    }
+    if (!P.f_fill.empty()) {
+        fill_f<S><<<(unsigned)P.f_fill.size(), 128, 0, st>>>(fa, ff, (int)P.f_fill.size(), F);
+        HM_CK_LAUNCH("fill_f");
+    }
+    if (h->n_segs) {
+        fill_segments<S><<<h->n_segs, 128, 0, st>>>(fa, h->d_segs, h->d_pieces, sf, h->n_segs, Pn);
+        HM_CK_LAUNCH("fill_segments");
+    }
+    HM_CK(cudaStreamSynchronize(st));
+    return HM_OK;
+}
+
+struct StageTimer {
+    hm_handle *h;
+    int stage;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr, b = nullptr;
+    StageTimer(hm_handle *h_, int stage_, cudaStream_t st_) : h(h_), stage(stage_), st(st_)
+    {
+        if (!(h->profile_mask & (1u << stage))) return;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, st);
+    }
+    ~StageTimer()
+    {
+        if (!a) return;
+        cudaEventRecord(b, st);
+        h->events.push_back({stage, a, b});
+    }
+};
+
+template <typename S, typename A>
+int get_scratch(hm_handle *h, cudaStream_t st, size_t bytes, A **out)
+{
+    std::lock_guard<std::mutex> lk(h->mu);
+    auto &sc = h->scratch[(void *)st];
+    if (sc.bytes < bytes) {
+        if (sc.p) HM_CK(cudaFreeAsync(sc.p, st));
+        sc.p = nullptr; sc.bytes = 0;
+        HM_CK(cudaMallocAsync(&sc.p, bytes, st));
+        sc.bytes = bytes;
+    }
+    *out = static_cast<A *>(sc.p);
+    return HM_OK;
+}
+
+template <typename S, typename A, int KT>
+int launch_expand(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+{
+    const size_t smem = (size_t)std::max(h->max_width, 1) * KT * sizeof(A);
+    if (smem > 48 * 1024) {
+        if (smem > 227 * 1024) { set_error("panel width %d too large", h->max_width); return HM_ERR_UNSUPPORTED; }
+        HM_CK(cudaFuncSetAttribute(expand<S, A, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    expand<S, A, KT><<<h->n_segs, kSegRows, smem, st>>>(ma, h->d_segs, h->d_pieces,
+                                                          static_cast<const S *>(h->d_P), s, h->r);
+    HM_CK_LAUNCH("expand");
+    return HM_OK;
+}
+
+template <typename S, typename A>
+int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st)
+{
+    if (ma.k <= 0) return HM_OK;
+    const int r = h->r, k = ma.k;
+    const size_t nt = (size_t)h->n_yslots * k * r, ns = (size_t)h->n_xslots * k * r;
+    A *t = nullptr;
+    if (nt + ns) {
+        int e = get_scratch<S, A>(h, st, (nt + ns) * sizeof(A), &t);
+        if (e) return e;
+    }
+    A *s = t + nt;
+    const A *T = static_cast<const A *>(h->d_T);
+    if (h->n_vp) {
+        StageTimer tm(h, 0, st);
+        leaf_up<S, A><<<warp_grid((int64_t)h->n_vp * k), kWarpCta, 0, st>>>(
+            ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
+        HM_CK_LAUNCH("leaf_up");
+    }
+    for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
+        const int b = h->up_ptr[l], n = h->up_ptr[l + 1] - b;
+        StageTimer tm(h, 1, st);
+        xfer_up<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_up + b, n, T, t, r, k);
+        HM_CK_LAUNCH("xfer_up");
+    }
+    if (h->n_m2l_rows) {
+        StageTimer tm(h, 2, st);
+        m2l<S, A><<<warp_grid((int64_t)h->n_m2l_rows * k), kWarpCta, 0, st>>>(
+            h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), t, s, r, k);
+        HM_CK_LAUNCH("m2l");
+    }
+    for (size_t l = 0; l + 1 < h->down_ptr.size(); ++l) {
+        const int b = h->down_ptr[l], n = h->down_ptr[l + 1] - b;
+        StageTimer tm(h, 3, st);
+        xfer_down<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_down + b, n, T, s, r, k);
+        HM_CK_LAUNCH("xfer_down");
+    }
+    if (h->n_segs) {
+        StageTimer tm(h, 4, st);
+        if (k == 1) return launch_expand<S, A, 1>(h, ma, s, st);
+        if (sizeof(A) == 8) return launch_expand<S, A, 4>(h, ma, s, st);
+        return launch_expand<S, A, 8>(h, ma, s, st);
+    }
+    return HM_OK;
+}
+
+int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
+                 int k, int accumulate, cudaStream_t st)
+{
+    if (h->storage == HM_F64) {
+        MulArgs<double> ma{static_cast<const double *>(x), static_cast<double *>(y), incx, ldx, incy, ldy, k, accumulate};
+        return run_mul<double, double>(h, ma, st);
+    }
+    MulArgs<float> ma{static_cast<const float *>(x), static_cast<float *>(y), incx, ldx, incy, ldy, k, accumulate};
+    return run_mul<float, float>(h, ma, st);
+}
+
+}  // namespace
+
+struct hm_plan {
+    Plan P;
+    std::vector<double> cheb, lam, T;
+};
+
+extern "C" {
+
+int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b, double c,
+                   double d, int rank, int64_t blocksize, hm_plan **out)
+{
+    if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
+    *out = nullptr;
+    if (!x || !y || nx < 1 || ny < 1) { set_error("empty or NULL point list"); return HM_ERR_INVALID_ARG; }
+    if (nx >= (int64_t)1 << 31 || ny >= (int64_t)1 << 31) { set_error("more than 2^31 points"); return HM_ERR_UNSUPPORTED; }
+    if (rank == 0) rank = 20;
+    if (rank < 1 || rank > HM_RMAX) { set_error("rank %d outside 1..%d", rank, HM_RMAX); return HM_ERR_UNSUPPORTED; }
+    if (blocksize == 0) blocksize = 4 * (int64_t)rank;
+    if (blocksize < 1) { set_error("blocksize %lld < 1", (long long)blocksize); return HM_ERR_INVALID_ARG; }
+    if (std::isnan(a) || std::isnan(b) || std::isnan(c) || std::isnan(d)) { set_error("NaN box end"); return HM_ERR_NAN; }
+    if (!(a > b) || !(c > d)) { set_error("box ends must satisfy a > b and c > d"); return HM_ERR_BOX; }
+    int st = check_points(x, nx, "x");
+    if (!st) st = check_points(y, ny, "y");
+    if (st) return st;
+    hm_plan *pl = new hm_plan();
+    chebyshev_first_kind(rank, pl->cheb, pl->lam);
+    transfer_matrices(rank, pl->cheb, pl->lam, pl->T);
+    st = build_plan(x, nx, y, ny, a, b, c, d, rank, blocksize, kSegRows, pl->P);
+    if (st == PLAN_ERR_BOUNDS) {
+        set_error("indsplit would read past the end of the point list");
+        delete pl;
+        return HM_ERR_BOUNDS;
+    }
+    if (st) { set_error("degenerate partition (status %d)", st); delete pl; return HM_ERR_DEGENERATE; }
+    *out = pl;
+    return HM_OK;
+}
+
+int hm_plan_table(const hm_plan *pl, int which, const void **data, int64_t *count, int64_t *elem_bytes)
+{
+    if (!pl || !data || !count || !elem_bytes) return HM_ERR_INVALID_ARG;
+    const Plan &P = pl->P;
+#define HM_TAB(vec) { *data = (vec).data(); *count = (int64_t)(vec).size(); *elem_bytes = (int64_t)sizeof((vec)[0]); return HM_OK; }
+    switch (which) {
+    case 0: HM_TAB(P.vpanels)
+    case 1: HM_TAB(P.vpanel_fill)
+    case 2: HM_TAB(P.up)
+    case 3: HM_TAB(P.up_level_ptr)
+    case 4: HM_TAB(P.m2l_rows)
+    case 5: HM_TAB(P.m2l_ents)
+    case 6: HM_TAB(P.f_fill)
+    case 7: HM_TAB(P.down)
+    case 8: HM_TAB(P.down_level_ptr)
+    case 9: HM_TAB(P.segs)
+    case 10: HM_TAB(P.pieces)
+    case 11: HM_TAB(P.seg_fill)
+    case 12: HM_TAB(pl->T)
+    case 13: HM_TAB(pl->cheb)
+    case 14: HM_TAB(pl->lam)
+    default: return HM_ERR_INVALID_ARG;
+    }
+#undef HM_TAB
+}
+
+int hm_plan_sizes(const hm_plan *pl, int64_t *out, int nout)
+{
+    if (!pl || !out) return 0;
+    const Plan &P = pl->P;
+    const int64_t v[] = {P.r, P.nx, P.ny, P.n_xslots, P.n_yslots, P.vstore_elems, P.fstore_elems,
+                         P.pstore_elems, P.max_width, P.stats.n_bary, P.stats.n_dense, P.stats.depth,
+                         P.stats.canonical_values, P.stats.reference_values, P.stats.stored_values,
+                         P.stats.dense_values, P.stats.n_segments};
+    const int nv = (int)(sizeof(v) / sizeof(v[0]));
+    const int w = std::min(nv, nout);
+    for (int i = 0; i < w; ++i) out[i] = v[i];
+    return w;
+}
+
+void hm_plan_free(hm_plan *pl) { delete pl; }
+
+const char *hm_status_string(int status)
+{
+    switch (status) {
+    case HM_OK: return "ok";
+    case HM_ERR_INVALID_ARG: return "invalid argument";
+    case HM_ERR_UNSORTED: return "points are not in non-increasing order";
+    case HM_ERR_BOUNDS: return "index out of bounds";
+    case HM_ERR_NAN: return "NaN input";
+    case HM_ERR_CUDA: return "CUDA error";
+    case HM_ERR_ALLOC: return "device allocation failed";
+    case HM_ERR_UNSUPPORTED: return "unsupported parameter";
+    case HM_ERR_BOX: return "box ends must satisfy a > b and c > d";
+    case HM_ERR_DEGENERATE: return "degenerate partition";
+    default: return "unknown status";
+    }
+}
+
+const char *hm_last_error(void) { return g_last_error.c_str(); }
+
+int hm_version(void) { return 100; }
+
+int hm_blockrank(double eps)
+{
+    if (!(eps > 0.0) || !(eps < 1.0)) return 0;
+    const double v = 0.5 * (std::log(1.0 / eps) / std::log(3.0 + std::sqrt(8.0)));
+    return 2 * (int)std::llround(v);
+}
+
+int hm_indsplit(const double *x, int64_t n, int64_t start, int64_t len, double a, double b, int64_t *out4)
+{
+    if (!x || !out4 || n < 0 || start < 0 || len < 0) { set_error("hm_indsplit: bad arguments"); return HM_ERR_INVALID_ARG; }
+    const double mid = 0.5 * (a + b);
+    int64_t i = start;
+    // The reference's scan (src/BarycentricMatrix.jl:299-307), first element
+    // read even for an empty range.
+    for (;;) {
+        if (i >= n) { set_error("indsplit: index %lld past the end (%lld)", (long long)i, (long long)n); return HM_ERR_BOUNDS; }
+        if (!(x[i] >= mid)) break;
+        i += 1;
+        if (i > start + len - 1) break;
+    }
+    out4[0] = start; out4[1] = i - start;
+    out4[2] = i; out4[3] = std::max<int64_t>(0, start + len - i);
+    return HM_OK;
+}
+
+int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double *y, int64_t ny,
+                          double a, double b, double c, double d, int rank, int64_t blocksize,
+                          int storage, void *stream, hm_handle **out)
+{
+    g_last_error.clear();
+    if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
+    *out = nullptr;
+    if (kernel < HM_KERNEL_CAUCHY || kernel > HM_KERNEL_LOG) { set_error("unknown kernel %d", kernel); return HM_ERR_UNSUPPORTED; }
+    if (storage != HM_F64 && storage != HM_F32) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
+    hm_plan *pl = nullptr;
+    int st = hm_plan_create(x, nx, y, ny, a, b, c, d, rank, blocksize, &pl);
+    if (st) return st;
+    const Plan &P = pl->P;
+    rank = P.r;
+    const std::vector<double> &cheb = pl->cheb, &lam = pl->lam, &T = pl->T;
+
+    hm_handle *h = new hm_handle();
+    h->kernel = kernel; h->storage = storage; h->r = rank; h->nx = nx; h->ny = ny;
+    h->stats = P.stats;
+    h->n_xslots = P.n_xslots; h->n_yslots = P.n_yslots; h->max_width = P.max_width;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    st = (storage == HM_F64) ? build_device<double>(h, P, cheb, lam, T, x, y, cs)
+                             : build_device<float>(h, P, cheb, lam, T, x, y, cs);
+    hm_plan_free(pl);
+    h->launches_per_mul = (h->n_vp > 0) + (int)std::max<size_t>(h->up_ptr.size(), 1) - 1 + (h->n_m2l_rows > 0) +
+                          (int)std::max<size_t>(h->down_ptr.size(), 1) - 1 + (h->n_segs > 0);
+    if (st) { hm_free(h); return st; }
+    *out = h;
+    return HM_OK;
+}
+
+int hm_size(const hm_handle *h, int64_t *m, int64_t *n)
+{
+    if (!h || !m || !n) return HM_ERR_INVALID_ARG;
+    *m = h->nx; *n = h->ny;
+    return HM_OK;
+}
+
+int hm_storage(const hm_handle *h) { return h ? h->storage : -1; }
+
+int hm_stats(const hm_handle *h, int64_t *out, int nout)
+{
+    if (!h || !out) return 0;
+    const int64_t v[] = {h->stats.n_bary, h->stats.n_dense, h->stats.depth, h->stats.n_xslots,
+                         h->stats.n_yslots, h->stats.canonical_values, h->stats.reference_values,
+                         h->stats.stored_values, h->stats.dense_values, h->stats.n_segments,
+                         h->stats.max_width, h->device_bytes, h->launches_per_mul};
+    const int nv = (int)(sizeof(v) / sizeof(v[0]));
+    const int w = std::min(nv, nout);
+    for (int i = 0; i < w; ++i) out[i] = v[i];
+    return w;
+}
+
+int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs, int accumulate,
+           void *stream)
+{
+    g_last_error.clear();
+    if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
+    if (nrhs < 0) { set_error("nrhs < 0"); return HM_ERR_INVALID_ARG; }
+    if (nrhs > 1 && (ldv < h->ny || ldu < h->nx)) { set_error("leading dimension too small"); return HM_ERR_BOUNDS; }
+    return dispatch_mul(h, v, 1, ldv, u, 1, ldu, nrhs, accumulate ? 1 : 0, static_cast<cudaStream_t>(stream));
+}
+
+int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, int64_t incx, void *y,
+                   int64_t leny, int64_t istart, int64_t incy, void *stream)
+{
+    g_last_error.clear();
+    if (!h || !x || !y) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
+    if (istart < 1 || jstart < 1 || incx < 1 || incy < 1) { set_error("istart/jstart/INCX/INCY must be >= 1"); return HM_ERR_INVALID_ARG; }
+    if ((jstart - 1) + (h->ny - 1) * incx >= lenx || (istart - 1) + (h->nx - 1) * incy >= leny) {
+        set_error("strided access past the end of x or y");
+        return HM_ERR_BOUNDS;
+    }
+    const size_t es = h->storage == HM_F64 ? 8 : 4;
+    const char *xb = static_cast<const char *>(x) + (size_t)(jstart - 1) * es;
+    char *yb = static_cast<char *>(y) + (size_t)(istart - 1) * es;
+    return dispatch_mul(h, xb, incx, 0, yb, incy, 0, 1, 1, static_cast<cudaStream_t>(stream));
+}
+
+int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
+{
+    g_last_error.clear();
+    if (!h || !v || !u || nrhs < 0) { set_error("bad argument"); return HM_ERR_INVALID_ARG; }
+    if (nrhs == 0) return HM_OK;
+    const size_t es = h->storage == HM_F64 ? 8 : 4;
+    const size_t bv = (size_t)h->ny * nrhs * es, bu = (size_t)h->nx * nrhs * es;
+    if (!h->host_stream) HM_CK(cudaStreamCreateWithFlags(&h->host_stream, cudaStreamNonBlocking));
+    cudaStream_t st = h->host_stream;
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        if (h->stage_bytes < bv + bu) {
+            if (h->d_stage) HM_CK(cudaFree(h->d_stage));
+            h->d_stage = nullptr; h->stage_bytes = 0;
+            HM_CK(cudaMalloc(&h->d_stage, bv + bu));
+            h->stage_bytes = bv + bu;
+        }
+    }
+    char *dv = static_cast<char *>(h->d_stage), *du = dv + bv;
+    HM_CK(cudaMemcpyAsync(dv, v, bv, cudaMemcpyHostToDevice, st));
+    if (accumulate) HM_CK(cudaMemcpyAsync(du, u, bu, cudaMemcpyHostToDevice, st));
+    int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, accumulate ? 1 : 0, st);
+    if (e) return e;
+    HM_CK(cudaMemcpyAsync(u, du, bu, cudaMemcpyDeviceToHost, st));
+    HM_CK(cudaStreamSynchronize(st));
+    return HM_OK;
+}
+
+int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t nrows, double *out, void *stream)
+{
+    g_last_error.clear();
+    if (!h || !b || !rows || !out || nrows < 0) { set_error("bad argument"); return HM_ERR_INVALID_ARG; }
+    if (nrows == 0) return HM_OK;
+    direct_rows<<<(unsigned)nrows, 256, 0, static_cast<cudaStream_t>(stream)>>>(h->kernel, h->d_x, h->nx, h->d_y, h->ny,
+                                                                              b, rows, nrows, out);
+    HM_CK_LAUNCH("direct_rows");
+    return HM_OK;
+}
+
+int hm_profile(hm_handle *h, int stage_mask)
+{
+    if (!h) return HM_ERR_INVALID_ARG;
+    h->profile_mask = (unsigned)stage_mask & ((1u << HM_NSTAGES) - 1);
+    return HM_OK;
+}
+
+int hm_profile_read(hm_handle *h, double *ms, int64_t *launches, int n, int reset)
+{
+    if (!h) return HM_ERR_INVALID_ARG;
+    for (auto &e : h->events) {
+        HM_CK(cudaEventSynchronize(e.b));
+        float t = 0.f;
+        HM_CK(cudaEventElapsedTime(&t, e.a, e.b));
+        h->stage_ms[e.stage] += t;
+        h->stage_launches[e.stage] += 1;
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    h->events.clear();
+    for (int i = 0; i < n && i < HM_NSTAGES; ++i) {
+        if (ms) ms[i] = h->stage_ms[i];
+        if (launches) launches[i] = h->stage_launches[i];
+    }
+    if (reset)
+        for (int i = 0; i < HM_NSTAGES; ++i) { h->stage_ms[i] = 0; h->stage_launches[i] = 0; }
+    return HM_OK;
+}
+
+void hm_free(hm_handle *h)
+{
+    if (!h) return;
+    cudaDeviceSynchronize();
+    for (auto &kv : h->scratch)
+        if (kv.second.p) cudaFree(kv.second.p);
+    for (auto &e : h->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    if (h->d_stage) cudaFree(h->d_stage);
+    if (h->host_stream) cudaStreamDestroy(h->host_stream);
+    for (void *p : h->allocs) cudaFree(p);
+    delete h;
+}
+
+}  // extern "C"

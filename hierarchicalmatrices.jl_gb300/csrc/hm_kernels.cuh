@@ -1,0 +1,122 @@
+// CUDA kernels of the KernelMatrix compression and matrix-vector product.
+// Written for sm_103a.  All kernels are launched from hm_api.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hm_types.h"
+
+#define HM_RMAX 32
+
+namespace hm {
+
+// ---------------------------------------------------------------- numerics
+
+// Kernels of examples/Kernel.jl:34-37, evaluated in FP64 with every operation
+// separately rounded (no contraction), as Julia evaluates them.
+__device__ __forceinline__ double kernel_eval(int kid, double x, double y)
+{
+    double d = __dsub_rn(x, y);
+    switch (kid) {
+    case 0: return 1.0 / d;
+    case 1: return 1.0 / __dmul_rn(d, d);
+    case 2: return 1.0 / __dmul_rn(__dmul_rn(d, d), d);
+    default: return log(fabs(d));
+    }
+}
+
+// Chebyshev node m mapped to the box [a, b]  (src/BarycentricMatrix.jl:156-164)
+__device__ __forceinline__ double box_node(double a, double b, double cheb)
+{
+    double ab2 = __dmul_rn(0.5, __dadd_rn(a, b));
+    double ba2 = __dmul_rn(0.5, __dsub_rn(b, a));
+    return __dadd_rn(ab2, __dmul_rn(ba2, cheb));
+}
+
+// Error-free transformations for the compensated FP32 dot products.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    float bp = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+template <typename A>
+struct Acc;   // accumulator: plain FMA for FP64, compensated (Dot2) for FP32
+
+template <>
+struct Acc<double> {
+    double s;
+    __device__ __forceinline__ void zero() { s = 0.0; }
+    __device__ __forceinline__ void add(double p, double g) { s = fma(p, g, s); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct Acc<float> {
+    float s, c;
+    __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
+    __device__ __forceinline__ void add(float p, float g)
+    {
+        float h = __fmul_rn(p, g);
+        float l = __fmaf_rn(p, g, -h);      // exact product error
+        float t, e;
+        two_sum(s, h, t, e);
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(e, l));
+    }
+    __device__ __forceinline__ float value() const { return __fadd_rn(s, c); }
+};
+
+struct FillArgs {
+    const double *x, *y;     // device copies of the points
+    const double *cheb, *lam;
+    int r, kernel;
+};
+
+template <typename S>
+struct MulArgs {
+    const S *x;      // x[(j * incx) + q * ldx]
+    S *y;            // y[(i * incy) + q * ldy]
+    int64_t incx, ldx, incy, ldy;
+    int k;           // right-hand sides
+    int accumulate;  // 1: y += H x (the reference's mul!), 0: y = H x
+};
+
+// ---------------------------------------------------------------- fill (build)
+
+template <typename S>
+__global__ void fill_vpanels(FillArgs fa, const hm_vpanel *vp, const hm_fill_vpanel *vf, int npanels, S *V);
+
+template <typename S>
+__global__ void fill_f(FillArgs fa, const hm_fill_f *ff, int nblocks, S *F);
+
+template <typename S>
+__global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *pieces,
+                              const hm_fill_seg *sf, int nsegs, S *P);
+
+// ---------------------------------------------------------------- matvec
+
+template <typename S, typename A>
+__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
+
+template <typename A>
+__global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k);
+
+template <typename S, typename A>
+__global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F,
+                    const A *t, A *s, int r, int k);
+
+template <typename A>
+__global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k);
+
+template <typename S, typename A, int KT>
+__global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P,
+                       const A *s, int r);
+
+// ---------------------------------------------------------------- direct sums
+
+__global__ void direct_rows(int kid, const double *x, int64_t nx, const double *y, int64_t ny,
+                           const double *b, const int64_t *rows, int64_t nrows, double *out);
+
+}  // namespace hm

@@ -1,0 +1,344 @@
+// Host planner for KernelMatrix: block tree + nested cluster bases.
+//
+// The block tree is the reference's (src/KernelMatrix.jl:49-116): a pair of
+// clusters is split at the box midpoints (indsplit, src/BarycentricMatrix.jl:
+// 299-307, points >= midpoint go first); diagonal pairs recurse, off-diagonal
+// pairs produce three barycentric children and recurse on the child whose
+// boxes touch; a pair becomes a leaf when all four halves hold fewer than
+// BLOCKSIZE points.
+//
+// The representation differs from the reference's: each barycentric block
+// of the reference stores its own U = Lagrange basis of its row box at the
+// row points and V likewise.  Because the boxes are nested halvings and the
+// basis is degree r-1 polynomial interpolation at Chebyshev points, the basis
+// of a box restricted to a child box equals the child's basis times one of two
+// fixed r x r transfer matrices.  So only the deepest boxes store explicit
+// bases; coarser coefficients move through the transfer matrices.  The
+// product is the same matrix up to rounding (the tests bound the difference).
+#include "hm_plan.h"
+
+#include <algorithm>
+
+namespace hm {
+
+static Node make_node(int64_t lo, int64_t hi, double a, double b, int level, int parent)
+{
+    Node n;
+    n.lo = lo; n.hi = hi; n.a = a; n.b = b; n.level = level; n.parent = parent;
+    n.child[0] = n.child[1] = -1;
+    n.used = n.sub_used = false;
+    n.kind = 0; n.slot = -1;
+    return n;
+}
+
+void Tree::init(const double *pts, int64_t npts, double a, double b)
+{
+    x = pts; n = npts;
+    nodes.clear();
+    nodes.push_back(make_node(0, npts, a, b, 0, -1));
+}
+
+int Tree::split(int id)
+{
+    if (nodes[id].child[0] >= 0) return PLAN_OK;
+    const int64_t lo = nodes[id].lo, hi = nodes[id].hi;
+    const double a = nodes[id].a, b = nodes[id].b;
+    const double mid = 0.5 * (a + b);
+    int64_t s;
+    if (lo >= hi) {
+        // An empty range: the reference still reads x[first(ir)].
+        if (lo >= n) return PLAN_ERR_BOUNDS;
+        if (x[lo] >= mid) return PLAN_ERR_DEGENERATE;
+        s = lo;
+    } else {
+        // First index with !(x[i] >= mid); x is non-increasing, so the
+        // reference's linear scan and this binary search agree.
+        int64_t L = lo, R = hi;
+        while (L < R) {
+            int64_t M = L + (R - L) / 2;
+            if (x[M] >= mid) L = M + 1; else R = M;
+        }
+        s = L;
+    }
+    const int lev = nodes[id].level + 1;
+    int c0 = (int)nodes.size();
+    nodes.push_back(make_node(lo, s, a, mid, lev, id));
+    nodes.push_back(make_node(s, std::max(s, hi), mid, b, lev, id));
+    nodes[id].child[0] = c0;
+    nodes[id].child[1] = c0 + 1;
+    return PLAN_OK;
+}
+
+namespace {
+
+struct Builder {
+    Plan &P;
+    int64_t leaf;
+    int err = 0;
+    int64_t depth = 0;
+
+    void rec(int kind, int xn, int yn)
+    {
+        if (err) return;
+        int e = P.X.split(xn);
+        if (!e) e = P.Y.split(yn);
+        if (e) { err = e; return; }
+        depth = std::max<int64_t>(depth, P.X.nodes[xn].level);
+        const int x1 = P.X.nodes[xn].child[0], x2 = P.X.nodes[xn].child[1];
+        const int y1 = P.Y.nodes[yn].child[0], y2 = P.Y.nodes[yn].child[1];
+        const bool lf = P.X.size(x1) < leaf && P.X.size(x2) < leaf &&
+                        P.Y.size(y1) < leaf && P.Y.size(y2) < leaf;
+        if (kind == 0) {            // KernelMatrix, src/KernelMatrix.jl:49-70
+            if (lf) {
+                P.dense.push_back({x1, y1}); P.dense.push_back({x1, y2});
+                P.dense.push_back({x2, y1}); P.dense.push_back({x2, y2});
+            } else {
+                rec(0, x1, y1); rec(1, x1, y2); rec(2, x2, y1); rec(0, x2, y2);
+            }
+        } else if (kind == 1) {     // KernelMatrix1, src/KernelMatrix.jl:72-93
+            P.bary.push_back({x1, y1}); P.bary.push_back({x1, y2});
+            if (lf) P.dense.push_back({x2, y1}); else rec(1, x2, y1);
+            P.bary.push_back({x2, y2});
+        } else {                    // KernelMatrix2, src/KernelMatrix.jl:95-116
+            P.bary.push_back({x1, y1});
+            if (lf) P.dense.push_back({x1, y2}); else rec(2, x1, y2);
+            P.bary.push_back({x2, y1}); P.bary.push_back({x2, y2});
+        }
+    }
+};
+
+void mark_sub_used(Tree &T)
+{
+    for (size_t i = 0; i < T.nodes.size(); ++i) {
+        if (!T.nodes[i].used) continue;
+        int p = T.nodes[i].parent;
+        while (p >= 0 && !T.nodes[p].sub_used) {
+            T.nodes[p].sub_used = true;
+            p = T.nodes[p].parent;
+        }
+    }
+}
+
+void assign_basis(Tree &T, int id, bool above)
+{
+    const bool inb = above || T.nodes[id].used;
+    if (T.nodes[id].sub_used) {
+        assign_basis(T, T.nodes[id].child[0], inb);
+        assign_basis(T, T.nodes[id].child[1], inb);
+        if (inb) T.nodes[id].kind = 1;
+    } else if (inb) {
+        T.nodes[id].kind = 2;
+    }
+}
+
+// Slots in (level, lo) order; returns the slot count.
+int assign_slots(Tree &T)
+{
+    std::vector<int> ids;
+    for (size_t i = 0; i < T.nodes.size(); ++i)
+        if (T.nodes[i].kind) ids.push_back((int)i);
+    std::sort(ids.begin(), ids.end(), [&](int u, int v) {
+        if (T.nodes[u].level != T.nodes[v].level) return T.nodes[u].level < T.nodes[v].level;
+        if (T.nodes[u].lo != T.nodes[v].lo) return T.nodes[u].lo < T.nodes[v].lo;
+        return u < v;
+    });
+    for (size_t k = 0; k < ids.size(); ++k) T.nodes[ids[k]].slot = (int)k;
+    return (int)ids.size();
+}
+
+// Transfer steps for the internal basis nodes, grouped by level.
+void transfer_steps(const Tree &T, bool deepest_first, std::vector<hm_xfer> &out,
+                    std::vector<int> &ptr)
+{
+    int maxlev = 0;
+    for (const Node &n : T.nodes) if (n.kind == 1) maxlev = std::max(maxlev, n.level);
+    std::vector<std::vector<hm_xfer>> by(maxlev + 1);
+    for (const Node &n : T.nodes)
+        if (n.kind == 1)
+            by[n.level].push_back({n.slot, T.nodes[n.child[0]].slot, T.nodes[n.child[1]].slot, 0});
+    out.clear(); ptr.clear();
+    ptr.push_back(0);
+    for (int k = 0; k <= maxlev; ++k) {
+        int lev = deepest_first ? maxlev - k : k;
+        auto &v = by[lev];
+        if (v.empty()) continue;
+        std::sort(v.begin(), v.end(), [](const hm_xfer &p, const hm_xfer &q) { return p.slot < q.slot; });
+        out.insert(out.end(), v.begin(), v.end());
+        ptr.push_back((int)out.size());
+    }
+}
+
+inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b,
+               double c, double d, int r, int64_t leaf, int seg_rows, Plan &P)
+{
+    P = Plan();
+    P.r = r; P.nx = nx; P.ny = ny;
+    P.X.init(x, nx, a, b);
+    P.Y.init(y, ny, c, d);
+    Builder B{P, leaf};
+    B.rec(0, 0, 0);
+    if (B.err) return B.err;
+
+    for (auto &e : P.bary) { P.X.nodes[e.first].used = true; P.Y.nodes[e.second].used = true; }
+    mark_sub_used(P.X);
+    mark_sub_used(P.Y);
+    assign_basis(P.X, 0, false);
+    assign_basis(P.Y, 0, false);
+    P.n_xslots = assign_slots(P.X);
+    P.n_yslots = assign_slots(P.Y);
+    transfer_steps(P.Y, true, P.up, P.up_level_ptr);
+    transfer_steps(P.X, false, P.down, P.down_level_ptr);
+
+    // Explicit column bases at the deepest basis nodes of the column tree.
+    {
+        std::vector<int> leaves;
+        for (size_t i = 0; i < P.Y.nodes.size(); ++i)
+            if (P.Y.nodes[i].kind == 2) leaves.push_back((int)i);
+        std::sort(leaves.begin(), leaves.end(),
+                  [&](int u, int v) { return P.Y.nodes[u].slot < P.Y.nodes[v].slot; });
+        int64_t off = 0;
+        for (int id : leaves) {
+            const Node &n = P.Y.nodes[id];
+            hm_vpanel vp;
+            vp.row0 = n.lo;
+            vp.nrows = (int32_t)(n.hi - n.lo);
+            vp.ld = r;                         // row-major: r values per point
+            vp.width = r;
+            vp.slot = n.slot;
+            vp.off = off;
+            off += round_up((int64_t)vp.nrows * r, 32);
+            P.vpanels.push_back(vp);
+            P.vpanel_fill.push_back({n.a, n.b});
+        }
+        P.vstore_elems = off;
+    }
+
+    // M2L rows: barycentric blocks grouped by row cluster.
+    {
+        std::vector<std::pair<int, int>> bs;   // (xslot, index into bary)
+        for (size_t i = 0; i < P.bary.size(); ++i)
+            bs.push_back({P.X.nodes[P.bary[i].first].slot, (int)i});
+        std::sort(bs.begin(), bs.end(), [&](const std::pair<int, int> &p, const std::pair<int, int> &q) {
+            if (p.first != q.first) return p.first < q.first;
+            return P.Y.nodes[P.bary[p.second].second].slot < P.Y.nodes[P.bary[q.second].second].slot;
+        });
+        // One row per row-basis slot (slots without blocks get empty ranges, so
+        // the far-field pass writes every coefficient).
+        for (int sl = 0; sl < P.n_xslots; ++sl) P.m2l_rows.push_back({sl, 0, 0, 0});
+        for (size_t k = 0; k < bs.size(); ++k) {
+            const int xn = P.bary[bs[k].second].first, yn = P.bary[bs[k].second].second;
+            hm_m2l_row &row = P.m2l_rows[bs[k].first];
+            if (row.end == 0) row.begin = (int32_t)k;
+            row.end = (int32_t)(k + 1);
+            hm_m2l_ent e;
+            e.foff = (int64_t)k * r * r;
+            e.yslot = P.Y.nodes[yn].slot;
+            e.pad = 0;
+            P.m2l_ents.push_back(e);
+            P.f_fill.push_back({P.X.nodes[xn].a, P.X.nodes[xn].b, P.Y.nodes[yn].a, P.Y.nodes[yn].b});
+        }
+        P.fstore_elems = (int64_t)bs.size() * r * r;
+    }
+
+    // Row segments: elementary row intervals of {row-basis leaves, dense rows}.
+    {
+        std::vector<int> xleaves;
+        for (size_t i = 0; i < P.X.nodes.size(); ++i)
+            if (P.X.nodes[i].kind == 2 && P.X.size((int)i) > 0) xleaves.push_back((int)i);
+        std::sort(xleaves.begin(), xleaves.end(),
+                  [&](int u, int v) { return P.X.nodes[u].lo < P.X.nodes[v].lo; });
+        std::vector<int64_t> cuts = {0, nx};
+        for (int id : xleaves) { cuts.push_back(P.X.nodes[id].lo); cuts.push_back(P.X.nodes[id].hi); }
+        for (auto &e : P.dense) {
+            if (P.X.size(e.first) == 0 || P.Y.size(e.second) == 0) continue;
+            cuts.push_back(P.X.nodes[e.first].lo);
+            cuts.push_back(P.X.nodes[e.first].hi);
+        }
+        std::sort(cuts.begin(), cuts.end());
+        cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+        const size_t nint = cuts.size() - 1;
+        std::vector<std::vector<int>> dl(nint);
+        for (size_t k = 0; k < P.dense.size(); ++k) {
+            const Node &xn = P.X.nodes[P.dense[k].first];
+            if (xn.hi <= xn.lo || P.Y.size(P.dense[k].second) == 0) continue;
+            size_t i0 = std::lower_bound(cuts.begin(), cuts.end(), xn.lo) - cuts.begin();
+            size_t i1 = std::lower_bound(cuts.begin(), cuts.end(), xn.hi) - cuts.begin();
+            for (size_t i = i0; i < i1; ++i) dl[i].push_back((int)k);
+        }
+        size_t lp = 0;
+        int64_t poff = 0;
+        for (size_t iv = 0; iv < nint; ++iv) {
+            const int64_t p = cuts[iv], q = cuts[iv + 1];
+            if (q <= p) continue;
+            while (lp < xleaves.size() && P.X.nodes[xleaves[lp]].hi <= p) ++lp;
+            int leafid = -1;
+            if (lp < xleaves.size() && P.X.nodes[xleaves[lp]].lo <= p) leafid = xleaves[lp];
+            auto &ds = dl[iv];
+            std::sort(ds.begin(), ds.end(), [&](int u, int v) {
+                return P.Y.nodes[P.dense[u].second].lo < P.Y.nodes[P.dense[v].second].lo;
+            });
+            for (int64_t r0 = p; r0 < q; r0 += seg_rows) {
+                hm_seg s;
+                s.row0 = r0;
+                s.nrows = (int32_t)std::min<int64_t>(seg_rows, q - r0);
+                s.ld = (int32_t)round_up(s.nrows, 4);
+                s.piece0 = (int32_t)P.pieces.size();
+                s.width = 0;
+                hm_fill_seg f;
+                f.has_basis = 0; f.basis_w = 0; f.a = 0; f.b = 0;
+                if (leafid >= 0) {
+                    hm_piece pc;
+                    pc.kind = HM_PIECE_COEF; pc.src = P.X.nodes[leafid].slot; pc.width = r;
+                    P.pieces.push_back(pc);
+                    s.width += r;
+                    f.has_basis = 1; f.basis_w = r;
+                    f.a = P.X.nodes[leafid].a; f.b = P.X.nodes[leafid].b;
+                }
+                for (int k : ds) {
+                    const Node &yn = P.Y.nodes[P.dense[k].second];
+                    hm_piece pc;
+                    pc.kind = HM_PIECE_X; pc.src = yn.lo; pc.width = (int32_t)(yn.hi - yn.lo);
+                    P.pieces.push_back(pc);
+                    s.width += pc.width;
+                }
+                s.npieces = (int32_t)P.pieces.size() - s.piece0;
+                s.poff = poff;
+                s.pad = 0;
+                poff += round_up((int64_t)s.ld * std::max(s.width, 1), 32);
+                P.max_width = std::max(P.max_width, s.width);
+                P.segs.push_back(s);
+                P.seg_fill.push_back(f);
+            }
+        }
+        P.pstore_elems = poff;
+    }
+
+    // Statistics.
+    PlanStats &S = P.stats;
+    S.n_bary = (int64_t)P.bary.size();
+    S.n_dense = (int64_t)P.dense.size();
+    S.depth = B.depth;
+    S.n_xslots = P.n_xslots; S.n_yslots = P.n_yslots;
+    int64_t ux = 0, uy = 0;
+    for (const Node &n : P.X.nodes) if (n.used) ux += n.hi - n.lo;
+    for (const Node &n : P.Y.nodes) if (n.used) uy += n.hi - n.lo;
+    int64_t dv = 0, refv = 0;
+    for (auto &e : P.dense) dv += P.X.size(e.first) * P.Y.size(e.second);
+    for (auto &e : P.bary) refv += (P.X.size(e.first) + P.Y.size(e.second)) * r + (int64_t)r * r;
+    S.dense_values = dv;
+    S.canonical_values = (ux + uy) * r + S.n_bary * r * r + dv;
+    S.reference_values = refv + dv;
+    int64_t st = P.fstore_elems;
+    for (auto &v : P.vpanels) st += (int64_t)v.nrows * v.width;
+    for (auto &s : P.segs) st += (int64_t)s.nrows * s.width;
+    S.stored_values = st;
+    S.n_segments = (int64_t)P.segs.size();
+    S.max_width = P.max_width;
+    return PLAN_OK;
+}
+
+}  // namespace hm

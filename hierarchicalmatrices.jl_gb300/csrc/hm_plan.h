@@ -1,0 +1,84 @@
+// Host planner: reproduces the KernelMatrix block tree of HierarchicalMatrices.jl
+// (src/KernelMatrix.jl:47-116 with indsplit, src/BarycentricMatrix.jl:299-307)
+// and flattens it into the device tables of hm_types.h.
+#pragma once
+#include <stdint.h>
+#include <vector>
+
+#include "hm_types.h"
+
+namespace hm {
+
+enum PlanStatus {
+    PLAN_OK = 0,
+    PLAN_ERR_BOUNDS = 3,        // the reference would raise BoundsError in indsplit
+    PLAN_ERR_DEGENERATE = 9,    // a partition the reference builds inconsistently
+};
+
+struct Node {
+    int64_t lo, hi;     // [lo, hi) 0-based indices into the point list
+    double a, b;        // box; children are [a, (a+b)/2] and [(a+b)/2, b]
+    int level;
+    int parent;
+    int child[2];
+    bool used;          // cluster of at least one barycentric block
+    bool sub_used;      // some strict descendant is used
+    int kind;           // 0 none, 1 internal basis node, 2 basis leaf
+    int slot;           // coefficient slot, -1 if none
+};
+
+struct Tree {
+    const double *x = nullptr;
+    int64_t n = 0;
+    std::vector<Node> nodes;
+    void init(const double *pts, int64_t npts, double a, double b);
+    // Computes the children of node id once (indsplit semantics).
+    int split(int id);
+    int64_t size(int id) const { return nodes[id].hi - nodes[id].lo; }
+};
+
+struct PlanStats {
+    int64_t n_bary = 0, n_dense = 0, depth = 0;
+    int64_t n_xslots = 0, n_yslots = 0;
+    int64_t canonical_values = 0;   // cluster-deduplicated U, V + F + dense leaves
+    int64_t reference_values = 0;   // per-block U, V, F + dense (the reference's layout)
+    int64_t stored_values = 0;      // what this plan stores (nested bases)
+    int64_t dense_values = 0;
+    int64_t n_segments = 0;
+    int64_t max_width = 0;
+};
+
+struct Plan {
+    int r = 0;
+    int64_t nx = 0, ny = 0;
+    Tree X, Y;
+    std::vector<std::pair<int, int>> bary;    // (x node, y node)
+    std::vector<std::pair<int, int>> dense;   // (x node, y node)
+
+    // flattened tables
+    std::vector<hm_vpanel> vpanels;           // y-side explicit bases
+    std::vector<hm_fill_vpanel> vpanel_fill;
+    int64_t vstore_elems = 0;
+    std::vector<hm_xfer> up;                  // y tree, deepest level first
+    std::vector<int> up_level_ptr;            // ranges of `up` per level step
+    std::vector<hm_m2l_row> m2l_rows;
+    std::vector<hm_m2l_ent> m2l_ents;
+    std::vector<hm_fill_f> f_fill;
+    int64_t fstore_elems = 0;
+    std::vector<hm_xfer> down;                // x tree, top level first
+    std::vector<int> down_level_ptr;
+    std::vector<hm_seg> segs;
+    std::vector<hm_piece> pieces;
+    std::vector<hm_fill_seg> seg_fill;
+    int64_t pstore_elems = 0;
+    int n_xslots = 0, n_yslots = 0;
+    int max_width = 0;
+    PlanStats stats;
+};
+
+// Builds the plan.  x, y must be non-increasing (validated by the caller);
+// leaf = BLOCKSIZE, r = rank, seg_rows = maximum rows per row segment.
+int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b,
+               double c, double d, int r, int64_t leaf, int seg_rows, Plan &out);
+
+}  // namespace hm

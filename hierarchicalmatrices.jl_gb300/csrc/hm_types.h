@@ -1,0 +1,69 @@
+// Device-table records shared by the host planner and the CUDA kernels.
+//
+// A KernelMatrix (src/KernelMatrix.jl:47-116) is flattened into:
+//   * coefficient "slots": one per node of the row (x) and column (y) cluster
+//     trees that carries Chebyshev coefficients, each `width` values per
+//     right-hand side;
+//   * V panels: explicit column-cluster bases (y side) whose transpose times
+//     x gives the coefficients of a leaf slot;
+//   * transfer steps: parent <- children moves of coefficients between tree
+//     levels (upward on the column tree, downward on the row tree);
+//   * M2L rows: for each row cluster, the barycentric blocks
+//     (src/BarycentricMatrix.jl:208-297) of that row, each an r x r sample
+//     matrix F applied to the coefficients of its column cluster;
+//   * row segments: a contiguous run of rows whose near-field dense blocks and
+//     row basis are the same, stored as one column-major panel
+//     [U rows | dense block rows ...] that multiplies a gathered right-hand
+//     side [s coefficients ; x segments ...].
+#pragma once
+#include <stdint.h>
+
+struct hm_vpanel {      // explicit basis panel: coef[slot] = P^T x[row0 : row0+nrows)
+    int64_t row0;       // first row of x (element index before stride)
+    int64_t off;        // element offset of the panel in the V store
+    int32_t nrows;
+    int32_t ld;         // leading dimension of the column-major panel
+    int32_t width;      // number of basis columns (<= slot width)
+    int32_t slot;
+};
+
+struct hm_xfer {        // coefficient transfer between a node and its two children
+    int32_t slot, c0, c1, pad;
+};
+
+struct hm_m2l_row {     // s[slot] = sum_{e in [begin,end)} F_e t[yslot_e]
+    int32_t slot, begin, end, pad;
+};
+
+struct hm_m2l_ent {
+    int64_t foff;       // element offset of F_e (r x r column-major)
+    int32_t yslot, pad;
+};
+
+struct hm_seg {         // y[row0 : row0+nrows) (+)= panel * gathered rhs
+    int64_t row0;
+    int64_t poff;       // element offset of the panel in the panel store
+    int32_t nrows;
+    int32_t ld;
+    int32_t width;      // total panel columns
+    int32_t piece0;     // first piece record
+    int32_t npieces;
+    int32_t pad;
+};
+
+enum { HM_PIECE_COEF = 0, HM_PIECE_X = 1 };
+
+struct hm_piece {       // one block column run of a segment panel
+    int64_t src;        // coefficient slot (COEF) or first x element (X)
+    int32_t kind;
+    int32_t width;
+};
+
+// Build-time only: geometry needed to fill factors on the device.
+struct hm_fill_vpanel { double a, b; };          // box of an explicit basis panel
+struct hm_fill_f { double xa, xb, ya, yb; };     // boxes of one F block
+struct hm_fill_seg {                              // what the panel columns hold
+    double a, b;        // row-basis box (when has_basis)
+    int32_t has_basis;  // first `basis_w` columns are the row basis
+    int32_t basis_w;
+};

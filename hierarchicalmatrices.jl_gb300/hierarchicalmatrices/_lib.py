@@ -1,0 +1,175 @@
+"""ctypes binding of libhmgpu.so (the C ABI declared in include/hmgpu.h).
+
+The library is built in-tree by ``csrc/build.py``; importing this module never
+falls back to anything else: a missing library raises ``ImportError`` with
+the build command.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG_ROOT, "lib", "libhmgpu.so")
+
+HM_OK = 0
+HM_ERR_INVALID_ARG = 1
+HM_ERR_UNSORTED = 2
+HM_ERR_BOUNDS = 3
+HM_ERR_NAN = 4
+HM_ERR_CUDA = 5
+HM_ERR_ALLOC = 6
+HM_ERR_UNSUPPORTED = 7
+HM_ERR_BOX = 8
+HM_ERR_DEGENERATE = 9
+
+HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
+HM_F64, HM_F32 = 0, 1
+
+# Records of csrc/hm_types.h.
+VPANEL = np.dtype([("row0", "<i8"), ("off", "<i8"), ("nrows", "<i4"), ("ld", "<i4"),
+                   ("width", "<i4"), ("slot", "<i4")])
+XFER = np.dtype([("slot", "<i4"), ("c0", "<i4"), ("c1", "<i4"), ("pad", "<i4")])
+M2L_ROW = np.dtype([("slot", "<i4"), ("begin", "<i4"), ("end", "<i4"), ("pad", "<i4")])
+M2L_ENT = np.dtype([("foff", "<i8"), ("yslot", "<i4"), ("pad", "<i4")])
+SEG = np.dtype([("row0", "<i8"), ("poff", "<i8"), ("nrows", "<i4"), ("ld", "<i4"), ("width", "<i4"),
+                ("piece0", "<i4"), ("npieces", "<i4"), ("pad", "<i4")])
+PIECE = np.dtype([("src", "<i8"), ("kind", "<i4"), ("width", "<i4")])
+FILL_VPANEL = np.dtype([("a", "<f8"), ("b", "<f8")])
+FILL_F = np.dtype([("xa", "<f8"), ("xb", "<f8"), ("ya", "<f8"), ("yb", "<f8")])
+FILL_SEG = np.dtype([("a", "<f8"), ("b", "<f8"), ("has_basis", "<i4"), ("basis_w", "<i4")])
+PLAN_TABLES = {
+    "vpanels": (0, VPANEL), "vpanel_fill": (1, FILL_VPANEL), "up": (2, XFER),
+    "up_level_ptr": (3, np.dtype("<i4")), "m2l_rows": (4, M2L_ROW), "m2l_ents": (5, M2L_ENT),
+    "f_fill": (6, FILL_F), "down": (7, XFER), "down_level_ptr": (8, np.dtype("<i4")),
+    "segs": (9, SEG), "pieces": (10, PIECE), "seg_fill": (11, FILL_SEG),
+    "T": (12, np.dtype("<f8")), "cheb": (13, np.dtype("<f8")), "lam": (14, np.dtype("<f8")),
+}
+PLAN_SIZES = ("r", "nx", "ny", "n_xslots", "n_yslots", "vstore", "fstore", "pstore", "max_width",
+              "n_bary", "n_dense", "depth", "canonical_values", "reference_values", "stored_values",
+              "dense_values", "n_segments")
+STATS = ("n_bary", "n_dense", "depth", "n_xslots", "n_yslots", "canonical_values",
+         "reference_values", "stored_values", "dense_values", "n_segments", "max_width",
+         "device_bytes", "launches_per_mul")
+STAGES = ("leaf_up", "xfer_up", "m2l", "xfer_down", "expand")
+
+EXPORTED = (
+    "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
+    "hm_kernelmatrix_build", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
+    "hm_mul_host", "hm_direct_rows", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
+    "hm_plan_free",
+)
+
+_d = ctypes.POINTER(ctypes.c_double)
+_i64 = ctypes.c_int64
+_pi64 = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+
+
+class HMError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with "
+            "`python hierarchicalmatrices.jl_gb300/csrc/build.py` (no CPU fallback exists)")
+    L = ctypes.CDLL(LIB_PATH)
+    L.hm_status_string.restype = ctypes.c_char_p
+    L.hm_status_string.argtypes = [ctypes.c_int]
+    L.hm_last_error.restype = ctypes.c_char_p
+    L.hm_last_error.argtypes = []
+    L.hm_version.restype = ctypes.c_int
+    L.hm_blockrank.restype = ctypes.c_int
+    L.hm_blockrank.argtypes = [ctypes.c_double]
+    L.hm_indsplit.restype = ctypes.c_int
+    L.hm_indsplit.argtypes = [_d, _i64, _i64, _i64, ctypes.c_double, ctypes.c_double, _pi64]
+    L.hm_kernelmatrix_build.restype = ctypes.c_int
+    L.hm_kernelmatrix_build.argtypes = [ctypes.c_int, _d, _i64, _d, _i64, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, _i64, ctypes.c_int, _vp,
+                                        ctypes.POINTER(_vp)]
+    L.hm_size.restype = ctypes.c_int
+    L.hm_size.argtypes = [_vp, _pi64, _pi64]
+    L.hm_storage.restype = ctypes.c_int
+    L.hm_storage.argtypes = [_vp]
+    L.hm_stats.restype = ctypes.c_int
+    L.hm_stats.argtypes = [_vp, _pi64, ctypes.c_int]
+    L.hm_mul.restype = ctypes.c_int
+    L.hm_mul.argtypes = [_vp, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
+    L.hm_mul_strided.restype = ctypes.c_int
+    L.hm_mul_strided.argtypes = [_vp, _vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, _vp]
+    L.hm_mul_host.restype = ctypes.c_int
+    L.hm_mul_host.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
+    L.hm_direct_rows.restype = ctypes.c_int
+    L.hm_direct_rows.argtypes = [_vp, _vp, _vp, _i64, _vp, _vp]
+    L.hm_profile.restype = ctypes.c_int
+    L.hm_profile.argtypes = [_vp, ctypes.c_int]
+    L.hm_profile_read.restype = ctypes.c_int
+    L.hm_profile_read.argtypes = [_vp, _d, _pi64, ctypes.c_int, ctypes.c_int]
+    L.hm_free.restype = None
+    L.hm_free.argtypes = [_vp]
+    L.hm_plan_create.restype = ctypes.c_int
+    L.hm_plan_create.argtypes = [_d, _i64, _d, _i64, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, ctypes.c_int, _i64,
+                                 ctypes.POINTER(_vp)]
+    L.hm_plan_table.restype = ctypes.c_int
+    L.hm_plan_table.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(_vp), _pi64, _pi64]
+    L.hm_plan_sizes.restype = ctypes.c_int
+    L.hm_plan_sizes.argtypes = [_vp, _pi64, ctypes.c_int]
+    L.hm_plan_free.restype = None
+    L.hm_plan_free.argtypes = [_vp]
+    return L
+
+
+lib = _load()
+
+
+def check(status):
+    """Raise HMError for a non-zero status (IndexError for HM_ERR_BOUNDS, as the
+    reference raises BoundsError)."""
+    if status == HM_OK:
+        return
+    msg = lib.hm_last_error().decode() or lib.hm_status_string(status).decode()
+    text = f"{lib.hm_status_string(status).decode()}: {msg}"
+    if status == HM_ERR_BOUNDS:
+        raise IndexError(text)
+    raise HMError(status, text)
+
+
+def f64_ptr(a):
+    return a.ctypes.data_as(_d)
+
+
+class Plan:
+    """Host-side plan (block tree + flattened tables) without a GPU."""
+
+    def __init__(self, x, y, a, b, c, d, rank=20, blocksize=0):
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+        self.y = np.ascontiguousarray(y, dtype=np.float64)
+        h = _vp()
+        check(lib.hm_plan_create(f64_ptr(self.x), len(self.x), f64_ptr(self.y), len(self.y),
+                                 a, b, c, d, rank, blocksize, ctypes.byref(h)))
+        self._h = h
+        out = np.zeros(len(PLAN_SIZES), dtype=np.int64)
+        n = lib.hm_plan_sizes(self._h, out.ctypes.data_as(_pi64), len(out))
+        self.sizes = dict(zip(PLAN_SIZES[:n], (int(v) for v in out[:n])))
+
+    def table(self, name):
+        which, dt = PLAN_TABLES[name]
+        data, count, es = _vp(), _i64(), _i64()
+        check(lib.hm_plan_table(self._h, which, ctypes.byref(data), ctypes.byref(count),
+                                ctypes.byref(es)))
+        assert es.value == dt.itemsize, (name, es.value, dt.itemsize)
+        if count.value == 0:
+            return np.zeros(0, dtype=dt)
+        buf = (ctypes.c_char * (count.value * es.value)).from_address(data.value)
+        return np.frombuffer(bytes(buf), dtype=dt).copy()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib.hm_plan_free(self._h)
+            self._h = None

@@ -1,0 +1,267 @@
+"""KernelMatrix: the reference's compressed kernel matrix, built and applied on the GPU.
+
+Mirrors src/KernelMatrix.jl of HierarchicalMatrices.jl:
+  * ``KernelMatrix(f, x, y, a, b, c, d)``   (src/KernelMatrix.jl:47)
+  * ``H @ v`` / ``H * v``                   (src/KernelMatrix.jl:5-12)
+  * ``mul_(u, H, v, istart, jstart)``       (src/KernelMatrix.jl:14-45; accumulates into u)
+
+Device arrays are torch CUDA tensors; host arrays are numpy arrays (copied to
+the GPU and back inside the call).  Every product runs the CUDA kernels of
+libhmgpu.so; there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+_vp = ctypes.c_void_p
+
+
+class _Kernel:
+    """A kernel the GPU library knows, callable like the reference's closures."""
+
+    def __init__(self, name, kid, fn):
+        self.__name__ = name
+        self.hm_id = kid
+        self._fn = fn
+
+    def __call__(self, x, y):
+        return self._fn(np.asarray(x, dtype=np.float64), np.asarray(y, dtype=np.float64))
+
+    def __repr__(self):
+        return self.__name__
+
+
+# examples/Kernel.jl:34-37
+cauchykernel = _Kernel("cauchykernel", _lib.HM_KERNEL_CAUCHY, lambda x, y: 1.0 / (x - y))
+coulombkernel = _Kernel("coulombkernel", _lib.HM_KERNEL_COULOMB, lambda x, y: 1.0 / ((x - y) * (x - y)))
+coulombprimekernel = _Kernel("coulombprimekernel", _lib.HM_KERNEL_COULOMB_PRIME,
+                             lambda x, y: 1.0 / (((x - y) * (x - y)) * (x - y)))
+logkernel = _Kernel("logkernel", _lib.HM_KERNEL_LOG, lambda x, y: np.log(np.abs(x - y)))
+KERNELS = {k.__name__: k for k in (cauchykernel, coulombkernel, coulombprimekernel, logkernel)}
+
+
+def _kernel_id(f):
+    if isinstance(f, _Kernel):
+        return f.hm_id
+    if isinstance(f, str) and f in KERNELS:
+        return KERNELS[f].hm_id
+    if isinstance(f, int) and 0 <= f <= 3:
+        return f
+    raise ValueError(f"kernel {f!r} is not one of {sorted(KERNELS)}; the GPU library evaluates "
+                     "a fixed kernel set")
+
+
+def _storage_of(dtype):
+    dt = np.dtype(dtype)
+    if dt == np.float64:
+        return _lib.HM_F64
+    if dt == np.float32:
+        return _lib.HM_F32
+    raise ValueError(f"unsupported storage dtype {dt}")
+
+
+def _host_f64(a):
+    try:
+        import torch
+        if isinstance(a, torch.Tensor):
+            a = a.detach().cpu().numpy()
+    except ImportError:
+        pass
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.current_stream().cuda_stream
+        except ImportError:
+            pass
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def BLOCKRANK(T=np.float64):
+    """BLOCKRANK(T) (src/HierarchicalMatrices.jl:5)."""
+    return lib.hm_blockrank(float(np.finfo(T).eps))
+
+
+def BLOCKSIZE(T=np.float64):
+    """BLOCKSIZE(T) = 4 BLOCKRANK(T) (src/HierarchicalMatrices.jl:7)."""
+    return 4 * BLOCKRANK(T)
+
+
+def indsplit(x, ir, a, b):
+    """indsplit(x, ir, a, b) (src/BarycentricMatrix.jl:299-307) with 0-based
+    Python ranges: returns the two halves of ``ir`` split at (a+b)/2."""
+    x = _host_f64(x)
+    out = np.zeros(4, dtype=np.int64)
+    check(lib.hm_indsplit(_lib.f64_ptr(x), len(x), ir.start, len(ir), float(a), float(b),
+                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+    return range(out[0], out[0] + out[1]), range(out[2], out[2] + out[3])
+
+
+class KernelMatrix:
+    """KernelMatrix(f, x, y, a, b, c, d) compressed on the GPU.
+
+    ``x``, ``y`` must be in non-increasing order with ``a > b`` and ``c > d``
+    (the reference's convention).  ``dtype`` is the storage type of factors,
+    leaves and vectors (float64, or float32 from FP64 compression);
+    ``rank`` defaults to BLOCKRANK(Float64) = 20 and ``blocksize`` to 4 rank.
+    """
+
+    def __init__(self, f, x, y, a, b, c, d, *, dtype=np.float64, rank=None, blocksize=None,
+                 stream=None):
+        self.kernel = _kernel_id(f)
+        self.f = f
+        self.x = _host_f64(x)
+        self.y = _host_f64(y)
+        self.box = (float(a), float(b), float(c), float(d))
+        self.dtype = np.dtype(dtype)
+        self.rank = int(rank) if rank else BLOCKRANK(np.float64)
+        self.blocksize = int(blocksize) if blocksize else 4 * self.rank
+        h = _vp()
+        check(lib.hm_kernelmatrix_build(self.kernel, _lib.f64_ptr(self.x), len(self.x),
+                                        _lib.f64_ptr(self.y), len(self.y), *self.box, self.rank,
+                                        self.blocksize, _storage_of(self.dtype),
+                                        _stream_ptr(stream), ctypes.byref(h)))
+        self._h = h
+        self.shape = (len(self.x), len(self.y))
+
+    # -- reference surface -------------------------------------------------
+    def size(self, dim=None):
+        return self.shape if dim is None else self.shape[dim - 1]
+
+    def stats(self):
+        out = np.zeros(len(_lib.STATS), dtype=np.int64)
+        n = lib.hm_stats(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(out))
+        return dict(zip(_lib.STATS[:n], (int(v) for v in out[:n])))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check_dev(self, t, rows, name):
+        import torch
+        if not isinstance(t, torch.Tensor) or not t.is_cuda:
+            raise TypeError(f"{name} must be a CUDA tensor")
+        if t.dtype != (torch.float64 if self.dtype == np.float64 else torch.float32):
+            raise TypeError(f"{name} must have dtype {self.dtype}")
+        if t.dim() == 1:
+            if not t.is_contiguous():
+                raise ValueError(f"{name} must be contiguous")
+            if t.shape[0] < rows:
+                raise IndexError(f"{name} has {t.shape[0]} entries, needs {rows}")
+            return 1, rows
+        if t.dim() == 2:
+            # column-major (n x k) storage: stride (1, ld)
+            if t.stride(0) != 1:
+                raise ValueError(f"{name} must be column-major (t.stride(0) == 1)")
+            if t.shape[0] < rows:
+                raise IndexError(f"{name} has {t.shape[0]} rows, needs {rows}")
+            return t.shape[1], max(t.stride(1), rows)
+        raise ValueError(f"{name} must be 1-D or 2-D")
+
+    def mul(self, u, v, *, accumulate=True, stream=None):
+        """u (+)= H v on device tensors (1-D, or column-major 2-D for many
+        right-hand sides).  accumulate=True is the reference's mul!."""
+        ku, ldu = self._check_dev(u, self.shape[0], "u")
+        kv, ldv = self._check_dev(v, self.shape[1], "v")
+        if ku != kv:
+            raise ValueError("u and v have different numbers of columns")
+        check(lib.hm_mul(self._h, v.data_ptr(), ldv, u.data_ptr(), ldu, kv, 1 if accumulate else 0,
+                         _stream_ptr(stream)))
+        return u
+
+    def mul_strided(self, y, x, istart=1, jstart=1, incx=1, incy=1, *, stream=None):
+        """mul!(y, H, x, istart, jstart, INCX, INCY) on device vectors (1-based)."""
+        self._check_dev(y, 0, "y")
+        self._check_dev(x, 0, "x")
+        check(lib.hm_mul_strided(self._h, x.data_ptr(), x.numel(), jstart, incx, y.data_ptr(),
+                                 y.numel(), istart, incy, _stream_ptr(stream)))
+        return y
+
+    def mul_host(self, u, v, *, accumulate=True):
+        """u (+)= H v on host numpy arrays (column-major (n, k) for k > 1)."""
+        u_ = np.asarray(u)
+        v_ = np.asfortranarray(v, dtype=self.dtype)
+        if u_.dtype != self.dtype or not (u_.flags.f_contiguous or u_.ndim == 1):
+            raise TypeError(f"u must be a Fortran-ordered {self.dtype} array")
+        k = 1 if v_.ndim == 1 else v_.shape[1]
+        if v_.shape[0] != self.shape[1] or u_.shape[0] != self.shape[0]:
+            raise IndexError("dimension mismatch")
+        check(lib.hm_mul_host(self._h, v_.ctypes.data, u_.ctypes.data, k, 1 if accumulate else 0))
+        return u_
+
+    def __matmul__(self, v):
+        """H * v (src/KernelMatrix.jl:5-12): a new result, on the device for a
+        CUDA tensor, on the host for a numpy array."""
+        try:
+            import torch
+            if isinstance(v, torch.Tensor):
+                shape = (self.shape[0],) if v.dim() == 1 else (v.shape[1], self.shape[0])
+                u = torch.zeros(shape, dtype=v.dtype, device=v.device)
+                if v.dim() == 2:
+                    u = u.t()                        # column-major view
+                return self.mul(u, v, accumulate=False)
+        except ImportError:
+            pass
+        v = np.asfortranarray(v, dtype=self.dtype)
+        u = np.zeros(v.shape[:1] and ((self.shape[0],) + v.shape[1:]), dtype=self.dtype, order="F")
+        return self.mul_host(u, v, accumulate=False)
+
+    __mul__ = __matmul__
+
+    def direct_rows(self, b, rows, *, stream=None):
+        """Exact FP64 dense rows sum_j f(x_i, y_j) b_j (device b float64, rows int64)."""
+        import torch
+        b = b.to(torch.float64).contiguous()
+        rows = rows.to(torch.int64).contiguous()
+        out = torch.empty(rows.numel(), dtype=torch.float64, device=b.device)
+        check(lib.hm_direct_rows(self._h, b.data_ptr(), rows.data_ptr(), rows.numel(),
+                                 out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def profile(self, stages=_lib.STAGES):
+        """Record CUDA events around the launches of the named matvec stages
+        (see stage_times); an empty list turns timing off."""
+        mask = 0
+        for name in stages or ():
+            mask |= 1 << _lib.STAGES.index(name)
+        check(lib.hm_profile(self._h, mask))
+
+    def stage_times(self, reset=True):
+        """{stage: (total ms, launches)} accumulated since the last reset."""
+        n = len(_lib.STAGES)
+        ms = np.zeros(n)
+        cnt = np.zeros(n, dtype=np.int64)
+        check(lib.hm_profile_read(self._h, _lib.f64_ptr(ms),
+                                  cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n,
+                                  1 if reset else 0))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(_lib.STAGES)}
+
+    def free(self):
+        if getattr(self, "_h", None):
+            lib.hm_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def mul_(u, H, v, istart=1, jstart=1, incx=None, incy=None, **kw):
+    """mul!(u, H, v[, istart, jstart[, INCX, INCY]]): accumulates H v into u."""
+    if incx is None and incy is None and istart == 1 and jstart == 1:
+        if isinstance(u, np.ndarray):
+            return H.mul_host(u, v, accumulate=True)
+        return H.mul(u, v, accumulate=True, **kw)
+    return H.mul_strided(u, v, istart, jstart, incx or 1, incy or 1, **kw)

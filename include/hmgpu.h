@@ -1,0 +1,148 @@
+/*
+ * hmgpu.h -- C ABI of the GB300-native hierarchical-matrix library (libhmgpu.so).
+ *
+ * Drop-in boundary for the hot path of HierarchicalMatrices.jl v0.2.2: the
+ * KernelMatrix compression of Cauchy-type kernels and the hierarchical
+ * matrix-vector product.  Plain pointers and sizes only; every call returns a
+ * status code (HM_OK = 0) and never falls back to the CPU.  "device" pointers
+ * are CUDA device memory of the current device; "host" pointers are ordinary
+ * process memory.  Streams are cudaStream_t passed as void* (NULL = legacy
+ * default stream).
+ *
+ * Each entry point names the reference function it stands in for
+ * (file:line within HierarchicalMatrices.jl).
+ */
+#ifndef HMGPU_H
+#define HMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hm_handle hm_handle;
+
+/* Status codes.  The reference reports failures as Julia exceptions; the
+   mapping is given per code. */
+enum {
+    HM_OK = 0,
+    HM_ERR_INVALID_ARG = 1,   /* ArgumentError / DimensionMismatch */
+    HM_ERR_UNSORTED = 2,      /* points not non-increasing (the reference needs descending order) */
+    HM_ERR_BOUNDS = 3,        /* BoundsError (indsplit past the end, vector too short) */
+    HM_ERR_NAN = 4,           /* NaN point or box end */
+    HM_ERR_CUDA = 5,          /* a CUDA runtime call failed (see hm_last_error) */
+    HM_ERR_ALLOC = 6,         /* device allocation failed */
+    HM_ERR_UNSUPPORTED = 7,   /* rank above 32, unknown kernel or storage type */
+    HM_ERR_BOX = 8,           /* box ends not strictly decreasing (a > b, c > d) */
+    HM_ERR_DEGENERATE = 9     /* a partition the reference itself builds inconsistently */
+};
+
+/* Kernels of examples/Kernel.jl:34-37. */
+enum {
+    HM_KERNEL_CAUCHY = 0,         /* 1/(x-y) */
+    HM_KERNEL_COULOMB = 1,        /* 1/(x-y)^2 */
+    HM_KERNEL_COULOMB_PRIME = 2,  /* 1/(x-y)^3 */
+    HM_KERNEL_LOG = 3             /* log|x-y| */
+};
+
+/* Storage / arithmetic type of factors, leaves and vectors. */
+enum { HM_F64 = 0, HM_F32 = 1 };
+
+const char *hm_status_string(int status);
+/* Message of the last failing call on this thread ("" if none). */
+const char *hm_last_error(void);
+int hm_version(void);
+
+/* BLOCKRANK(T) (src/HierarchicalMatrices.jl:5): rank for machine epsilon eps. */
+int hm_blockrank(double eps);
+
+/* indsplit(x, ir, a, b) (src/BarycentricMatrix.jl:299-307) on a host point
+   list: splits the 0-based range [start, start+len) at the first point below
+   (a+b)/2.  out4 = (start1, len1, start2, len2). */
+int hm_indsplit(const double *x, int64_t n, int64_t start, int64_t len, double a, double b,
+                int64_t *out4);
+
+/* KernelMatrix(f, x, y, a, b, c, d) (src/KernelMatrix.jl:47-116).
+   x (nx) and y (ny) are HOST arrays in non-increasing order with a > b, c > d,
+   as the reference requires.  rank = BLOCKRANK (0 selects 20), blocksize =
+   BLOCKSIZE leaf threshold (0 selects 4*rank).  Compression runs on the GPU in
+   FP64; factors and leaves are stored as `storage` (HM_F64 or HM_F32). */
+int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double *y, int64_t ny,
+                          double a, double b, double c, double d, int rank, int64_t blocksize,
+                          int storage, void *stream, hm_handle **out);
+
+/* size(H) (src/hierarchical.jl:33-47). */
+int hm_size(const hm_handle *h, int64_t *m, int64_t *n);
+/* Storage type of h (HM_F64 / HM_F32). */
+int hm_storage(const hm_handle *h);
+
+/* Statistics: out[0..] = barycentric blocks, dense blocks, tree depth, row slots,
+   column slots, canonical stored values, reference-layout values, values this
+   build stores, dense values, row segments, max panel width, device bytes,
+   kernel launches per single-RHS hm_mul.
+   Returns the number of values written (<= nout). */
+int hm_stats(const hm_handle *h, int64_t *out, int nout);
+
+/* mul!(u, H, v, istart, jstart) (src/KernelMatrix.jl:14-45), generalised to
+   nrhs right-hand sides: for q < nrhs,
+     u[:, q] += H * v[:, q]   (accumulate = 1, the reference's semantics)
+     u[:, q]  = H * v[:, q]   (accumulate = 0)
+   u, v are DEVICE arrays of the handle's storage type, column q at u + q*ldu.
+   Stream-ordered; returns before the work completes. */
+int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs,
+           int accumulate, void *stream);
+
+/* mul!(y, H, x, istart, jstart, INCX, INCY) (src/HierarchicalMatrix.jl:24-52):
+   y[istart-1 + i*incy] += (H x)[i] with x read at x[jstart-1 + j*incx]
+   (1-based istart/jstart, positive strides).  lenx/leny are the array
+   lengths, checked like the reference's BoundsError.  DEVICE arrays. */
+int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, int64_t incx,
+                   void *y, int64_t leny, int64_t istart, int64_t incy, void *stream);
+
+/* H * v with HOST arrays (u = H v or u += H v): copies v to the device, runs
+   hm_mul and copies the result back; synchronous. */
+int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate);
+
+/* Exact dense rows: out[q] = sum_j f(x[rows[q]], y[j]) b[j] evaluated in FP64
+   with double-double accumulation, on the handle's points (DEVICE b, rows,
+   out).  Used to state the error of a compressed product. */
+int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t nrows, double *out,
+                   void *stream);
+
+/* Per-stage timing of hm_mul (the reference prints @time per call,
+   examples/Kernel.jl:73-76): for each stage whose bit is set in stage_mask
+   (0 leaf bases, 1 upward transfers, 2 far field, 3 downward transfers,
+   4 row segments), CUDA events are recorded on the launching stream around
+   its launches.  hm_profile_read synchronises on them and returns accumulated
+   milliseconds and launch counts per stage; reset = 1 clears the totals.
+   stage_mask = 0 turns timing off. */
+int hm_profile(hm_handle *h, int stage_mask);
+int hm_profile_read(hm_handle *h, double *ms, int64_t *launches, int n, int reset);
+
+void hm_free(hm_handle *h);
+
+/* --- host planner (no GPU needed) ------------------------------------------
+   The block tree and the flattened tables that hm_kernelmatrix_build uploads,
+   for inspection and host-side tests.  Same validation and status codes as
+   hm_kernelmatrix_build. */
+typedef struct hm_plan hm_plan;
+int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b,
+                   double c, double d, int rank, int64_t blocksize, hm_plan **out);
+/* Table `which` (0 vpanels, 1 vpanel boxes, 2 upward steps, 3 upward level
+   offsets, 4 far-field rows, 5 far-field entries, 6 F boxes, 7 downward steps,
+   8 downward level offsets, 9 row segments, 10 pieces, 11 segment fill info,
+   12 transfer matrices, 13 Chebyshev nodes, 14 barycentric weights):
+   pointer, element count and element size (records of hm_types.h). */
+int hm_plan_table(const hm_plan *p, int which, const void **data, int64_t *count, int64_t *elem_bytes);
+/* r, nx, ny, row slots, column slots, V/F/panel store elements, max panel
+   width, barycentric blocks, dense blocks, depth, canonical values,
+   reference-layout values, stored values, dense values, row segments. */
+int hm_plan_sizes(const hm_plan *p, int64_t *out, int nout);
+void hm_plan_free(hm_plan *p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HMGPU_H */

@@ -1,0 +1,93 @@
+"""numpy executor of the product's plan tables (test infrastructure).
+
+Runs the fill and matvec stages of csrc/hm_kernels.cu on the host tables
+returned by hm_plan_create, in FP64, so the planner and the nested-basis
+algebra can be checked against the oracle without a GPU.
+"""
+import numpy as np
+
+
+def box_nodes(a, b, cheb):
+    ab2 = 0.5 * (a + b)
+    ba2 = 0.5 * (b - a)
+    return ab2 + ba2 * cheb
+
+
+def kernel_np(kernel, x, y):
+    d = x - y
+    if kernel == 0:
+        return 1.0 / d
+    if kernel == 1:
+        return 1.0 / (d * d)
+    if kernel == 2:
+        return 1.0 / ((d * d) * d)
+    return np.log(np.abs(d))
+
+
+def basis(pts, a, b, cheb, lam):
+    nodes = box_nodes(a, b, cheb)
+    w = lam[None, :] * (1.0 / (pts[:, None] - nodes[None, :]))
+    return w / w.sum(axis=1, keepdims=True)
+
+
+def emulate(plan, kernel, b):
+    """Returns H @ b (b: (ny,) or (ny, k)) computed from the plan tables."""
+    S = plan.sizes
+    r = S["r"]
+    x, y = plan.x, plan.y
+    b = np.asarray(b, dtype=np.float64)
+    squeeze = b.ndim == 1
+    B = b[:, None] if squeeze else b
+    k = B.shape[1]
+    cheb, lam = plan.table("cheb"), plan.table("lam")
+    T = plan.table("T").reshape(2, r, r)           # T[c][m', m]
+    t = np.zeros((S["n_yslots"], r, k))
+    s = np.zeros((S["n_xslots"], r, k))
+    # explicit column bases -> leaf coefficients
+    for vp, vf in zip(plan.table("vpanels"), plan.table("vpanel_fill")):
+        rows = slice(vp["row0"], vp["row0"] + vp["nrows"])
+        V = basis(y[rows], vf["a"], vf["b"], cheb, lam)
+        t[vp["slot"]] = V.T @ B[rows]
+    # upward transfers, level by level
+    up, ptr = plan.table("up"), plan.table("up_level_ptr")
+    for l in range(len(ptr) - 1):
+        for e in up[ptr[l]:ptr[l + 1]]:
+            t[e["slot"]] = T[0].T @ t[e["c0"]] + T[1].T @ t[e["c1"]]
+    # far field
+    ents, ff = plan.table("m2l_ents"), plan.table("f_fill")
+    for row in plan.table("m2l_rows"):
+        acc = np.zeros((r, k))
+        for e in range(row["begin"], row["end"]):
+            f = ff[e]
+            F = kernel_np(kernel, box_nodes(f["xa"], f["xb"], cheb)[:, None],
+                          box_nodes(f["ya"], f["yb"], cheb)[None, :])
+            acc += F @ t[ents[e]["yslot"]]
+        s[row["slot"]] = acc
+    # downward transfers
+    down, ptr = plan.table("down"), plan.table("down_level_ptr")
+    for l in range(len(ptr) - 1):
+        for e in down[ptr[l]:ptr[l + 1]]:
+            s[e["c0"]] += T[0] @ s[e["slot"]]
+            s[e["c1"]] += T[1] @ s[e["slot"]]
+    # row segments
+    out = np.zeros((S["nx"], k))
+    covered = np.zeros(S["nx"], dtype=np.int64)
+    pieces, sf = plan.table("pieces"), plan.table("seg_fill")
+    for sg, fi in zip(plan.table("segs"), sf):
+        rows = slice(sg["row0"], sg["row0"] + sg["nrows"])
+        covered[rows] += 1
+        cols, g = [], []
+        for p in pieces[sg["piece0"]:sg["piece0"] + sg["npieces"]]:
+            if p["kind"] == 0:
+                cols.append(basis(x[rows], fi["a"], fi["b"], cheb, lam))
+                g.append(s[p["src"]])
+            else:
+                yy = y[p["src"]:p["src"] + p["width"]]
+                cols.append(kernel_np(kernel, x[rows][:, None], yy[None, :]))
+                g.append(B[p["src"]:p["src"] + p["width"]])
+        if cols:
+            P = np.concatenate(cols, axis=1)
+            assert P.shape[1] == sg["width"]
+            out[rows] = P @ np.concatenate(g, axis=0)
+    assert np.all(covered == 1), "every row must be in exactly one segment"
+    return out[:, 0] if squeeze else out

@@ -1,0 +1,247 @@
+"""GPU parity of the KernelMatrix build + matvec (CUDA kernels through the C ABI)
+against the CPU oracle.
+
+Tolerances (the benchmark spec): FP64 storage <= 1e-12 relative 2-norm error against
+the oracle's reference-order product; FP32 storage <= 1e-6 against the FP64
+dense product.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import hierarchicalmatrices as hm  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL64 = 1e-12
+TOL32 = 1e-6
+KFUN = {O.CAUCHY: hm.cauchykernel, O.COULOMB: hm.coulombkernel,
+        O.COULOMB_PRIME: hm.coulombprimekernel, O.LOG: hm.logkernel}
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def dev(a, dtype=torch.float64):
+    return torch.tensor(np.asarray(a), device="cuda", dtype=dtype)
+
+
+@pytest.mark.parametrize("n", [128, 2048, 65536])
+def test_grid_fp64_matches_oracle(n):
+    x, y = O.grid_points(n)
+    b = np.random.default_rng(n).standard_normal(n)
+    ref = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0) @ b
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    u = (H @ dev(b)).cpu().numpy()
+    assert rel(u, ref) <= TOL64
+
+
+def test_beta_fp64_matches_oracle():
+    x, y = O.beta_points(65536, 21)
+    b = np.random.default_rng(1).standard_normal(65536)
+    ref = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0) @ b
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    assert rel((H @ dev(b)).cpu().numpy(), ref) <= TOL64
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))),
+                         ids=lambda p: os.path.basename(p)[:-4])
+def test_golden_fp64(path):
+    d = np.load(path)
+    kname = os.path.basename(path)[:-4].split("_")[1]
+    f = {"cauchy": hm.cauchykernel, "coulomb": hm.coulombkernel,
+         "coulombprime": hm.coulombprimekernel, "log": hm.logkernel}[kname]
+    H = hm.KernelMatrix(f, d["x"], d["y"], *d["box"])
+    st = H.stats()
+    assert [st["n_bary"], st["n_dense"], st["depth"]] == d["stats"][:3].tolist()
+    u = (H @ dev(d["b"])).cpu().numpy()
+    assert rel(u, d["u"]) <= TOL64
+    assert rel(u, d["u_dense"]) <= 1e-12
+
+
+@pytest.mark.parametrize("kernel", [O.CAUCHY, O.COULOMB, O.COULOMB_PRIME, O.LOG])
+def test_example_chebyshev_10000(kernel):
+    # examples/Kernel.jl:58-78 at N = 10000
+    x, y, box = O.example_points("chebyshev", 10000)
+    b = np.random.default_rng(3).standard_normal(10000)
+    ref = O.OracleKernelMatrix(kernel, x, y, *box) @ b
+    H = hm.KernelMatrix(KFUN[kernel], x, y, *box)
+    assert rel((H @ dev(b)).cpu().numpy(), ref) <= TOL64
+
+
+def test_fp32_against_dense():
+    n = 65536
+    x, y = O.grid_points(n)
+    b = np.random.default_rng(5).standard_normal(n).astype(np.float32)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    u = (H @ dev(b, torch.float32)).cpu().numpy().astype(np.float64)
+    rows = np.arange(0, n, 61)
+    ref = O.dense_rows(O.CAUCHY, x, y, b.astype(np.float64), rows, nthreads=os.cpu_count())
+    assert rel(u[rows], ref) <= TOL32
+
+
+@pytest.mark.parametrize("dtype,k", [(np.float64, 3), (np.float64, 8), (np.float32, 5), (np.float32, 32)])
+def test_multi_rhs_matches_columns(dtype, k):
+    n = 8192
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=dtype)
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    B = torch.randn(k, n, device="cuda", dtype=tdt).t()          # column-major n x k
+    U = H @ B
+    Ho = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0)
+    Bh = B.double().cpu().numpy()
+    for q in range(k):
+        ref = Ho @ Bh[:, q].copy()
+        assert rel(U[:, q].double().cpu().numpy(), ref) <= (TOL64 if dtype == np.float64 else TOL32)
+        single = (H @ B[:, q].contiguous()).double().cpu().numpy()
+        assert rel(U[:, q].double().cpu().numpy(), single) <= (1e-14 if dtype == np.float64 else 1e-7)
+
+
+def test_mul_accumulates_like_reference():
+    # LinearAlgebra.mul!(u, H, v) = mul!(u, H, v, 1, 1) adds into u
+    n = 2048
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    b = dev(np.random.default_rng(0).standard_normal(n))
+    u0 = dev(np.random.default_rng(1).standard_normal(n))
+    u = u0.clone()
+    hm.mul_(u, H, b)
+    Hb = H @ b
+    assert torch.allclose(u, u0 + Hb, rtol=1e-14, atol=1e-9)
+
+
+def test_strided_mul():
+    # mul!(y, H, x, istart, jstart, INCX, INCY) semantics
+    n = 2048
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    rng = np.random.default_rng(2)
+    xs = rng.standard_normal(3 + 2 * n)
+    ys = rng.standard_normal(5 + 3 * n)
+    xd, yd = dev(xs), dev(ys)
+    H.mul_strided(yd, xd, istart=4, jstart=2, incx=2, incy=3)
+    ref = ys.copy()
+    ref[3:3 + 3 * n:3] += O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0) @ xs[1:1 + 2 * n:2].copy()
+    got = yd.cpu().numpy()
+    assert rel(got[3:3 + 3 * n:3], ref[3:3 + 3 * n:3]) <= TOL64
+    mask = np.ones(len(ys), dtype=bool)
+    mask[3:3 + 3 * n:3] = False
+    assert np.array_equal(got[mask], ys[mask])          # untouched elements
+    with pytest.raises(IndexError):
+        H.mul_strided(yd, xd, istart=4, jstart=5, incx=2, incy=3)
+
+
+def test_host_api_and_errors():
+    n = 2048
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    b = np.random.default_rng(6).standard_normal(n)
+    u = H @ b                                              # numpy in -> host path
+    ref = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0) @ b
+    assert isinstance(u, np.ndarray) and rel(u, ref) <= TOL64
+    with pytest.raises(IndexError):
+        H.mul(torch.zeros(n - 1, device="cuda", dtype=torch.float64), dev(b))
+    with pytest.raises(TypeError):
+        H.mul(torch.zeros(n, device="cuda", dtype=torch.float32), dev(b))
+
+
+def test_direct_rows_matches_oracle():
+    n = 8192
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    b = np.random.default_rng(8).standard_normal(n)
+    rows = np.arange(0, n, 37)
+    got = H.direct_rows(dev(b), torch.tensor(rows, device="cuda")).cpu().numpy()
+    ref = O.dense_rows(O.CAUCHY, x, y, b, rows)
+    np.testing.assert_allclose(got, ref, rtol=1e-13, atol=1e-12)
+    bad = H.direct_rows(dev(b), torch.tensor([0, n, -1], device="cuda")).cpu().numpy()
+    assert np.isfinite(bad[0]) and np.isnan(bad[1]) and np.isnan(bad[2])
+
+
+def test_small_dense_only():
+    # fewer points than BLOCKSIZE: four dense blocks, no far field
+    x, y = O.grid_points(100)
+    b = np.random.default_rng(1).standard_normal(100)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    assert H.stats()["n_bary"] == 0
+    ref = O.kernel_dense(O.CAUCHY, x, y) @ b
+    assert rel((H @ dev(b)).cpu().numpy(), ref) <= 1e-14
+
+
+def test_rectangular_uniform():
+    rng = np.random.default_rng(12)
+    x = np.sort(rng.random(30000))[::-1].copy()
+    y = np.sort(rng.random(17000))[::-1].copy()
+    b = rng.standard_normal(17000)
+    ref = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0) @ b
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    assert rel((H @ dev(b)).cpu().numpy(), ref) <= TOL64
+
+
+def test_profile_stage_times():
+    n = 65536
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    b = dev(np.random.default_rng(0).standard_normal(n), torch.float32)
+    u = torch.empty(n, device="cuda", dtype=torch.float32)
+    H.profile()
+    for _ in range(3):
+        H.mul(u, b, accumulate=False)
+    st = H.stage_times()
+    H.profile([])
+    assert st["expand"][1] == 3 and st["expand"][0] > 0
+    assert st["m2l"][1] == 3
+
+
+# ---- full size (n = 2^20): size-independent properties ---------------------
+
+@pytest.fixture(scope="module")
+def big():
+    n = 1 << 20
+    x, y = O.grid_points(n)
+    H64 = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    H32 = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    yield n, x, y, H64, H32
+    H64.free()
+    H32.free()
+
+
+def test_2pow20_tree(big):
+    n, x, y, H64, H32 = big
+    st = H64.stats()
+    assert (st["n_bary"], st["n_dense"], st["depth"]) == (98214, 49150, 13)
+    assert st["canonical_values"] == 785863520
+
+
+def test_2pow20_linearity_and_sampled_rows(big):
+    n, x, y, H64, H32 = big
+    g = torch.Generator(device="cuda").manual_seed(0)
+    b1 = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    b2 = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    u1, u2 = H64 @ b1, H64 @ b2
+    u12 = H64 @ (2.0 * b1 - 0.5 * b2)
+    assert float(torch.linalg.norm(u12 - (2.0 * u1 - 0.5 * u2)) / torch.linalg.norm(u12)) <= 1e-14
+    rows_np = np.sort(np.random.default_rng(4).choice(n, 64, replace=False))
+    ref = O.dense_rows(O.CAUCHY, x, y, b1.cpu().numpy(), rows_np, nthreads=os.cpu_count())
+    assert rel(u1.cpu().numpy()[rows_np], ref) <= TOL64
+    rows = torch.tensor(rows_np, device="cuda")
+    assert rel(H64.direct_rows(b1, rows).cpu().numpy(), ref) <= 1e-14
+
+
+def test_2pow20_fp32_error(big):
+    n, x, y, H64, H32 = big
+    g = torch.Generator(device="cuda").manual_seed(1)
+    b = torch.randn(n, device="cuda", dtype=torch.float32, generator=g)
+    u32 = H32 @ b
+    rows = torch.tensor(np.sort(np.random.default_rng(5).choice(n, 4096, replace=False)), device="cuda")
+    ref = H64.direct_rows(b.double(), rows)
+    err = float(torch.linalg.norm(u32.double()[rows] - ref) / torch.linalg.norm(ref))
+    assert err <= TOL32
+    u64 = H64 @ b.double()
+    assert float(torch.linalg.norm(u32.double() - u64) / torch.linalg.norm(u64)) <= TOL32
