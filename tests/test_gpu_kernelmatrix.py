@@ -134,7 +134,7 @@ def test_strided_mul():
     mask[3:3 + 3 * n:3] = False
     assert np.array_equal(got[mask], ys[mask])          # untouched elements
     with pytest.raises(IndexError):
-        H.mul_strided(yd, xd, istart=4, jstart=5, incx=2, incy=3)
+        H.mul_strided(yd, xd, istart=4, jstart=10, incx=2, incy=3)
 
 
 def test_host_api_and_errors():
