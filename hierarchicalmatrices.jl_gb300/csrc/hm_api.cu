@@ -353,6 +353,75 @@ int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y
     return run_mul<float, float>(h, ma, st);
 }
 
+// ---- allocation-free single right-hand-side product ------------------------
+//
+// Some callers cannot let the library allocate device memory during a
+// product: processes whose device memory is entirely reserved up front by
+// another allocator (a framework memory pool that takes most of HBM at
+// start-up), and loops that must not call cudaMalloc/cudaFree after
+// initialisation because those calls can synchronise the device and take an
+// unbounded time.  hm_mul_noalloc serves them: its coefficient scratch is
+// this file-scope device array, fixed at load time and held by every GPU
+// that loads the library until the process exits.
+#define HM_NOALLOC_SCRATCH_BYTES (16u << 20)
+static __device__ __align__(256) unsigned char hm_noalloc_scratch[HM_NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[256];   // device address of hm_noalloc_scratch, per device
+
+// On host, `hm_noalloc_scratch` names a host-side stand-in, not device memory;
+// the device address is looked up once per device, with that device current.
+int noalloc_scratch(void **out)
+{
+    int dev = -1;
+    HM_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) { set_error("device ordinal %d out of range", dev); return HM_ERR_UNSUPPORTED; }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, hm_noalloc_scratch);
+        if (e != cudaSuccess) {
+            set_error("cudaGetSymbolAddress(hm_noalloc_scratch): %s", cudaGetErrorString(e));
+            return HM_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return HM_OK;
+}
+
+// The launch sequence of run_mul with the caller-provided scratch t (and s
+// after it); no allocation, no timing events.
+template <typename S, typename A>
+int run_mul_static(hm_handle *h, MulArgs<S> ma, cudaStream_t st, A *t)
+{
+    const int r = h->r, k = ma.k;
+    A *s = t + (size_t)h->n_yslots * k * r;
+    const A *T = static_cast<const A *>(h->d_T);
+    if (h->n_vp) {
+        leaf_up<S, A><<<warp_grid((int64_t)h->n_vp * k), kWarpCta, 0, st>>>(
+            ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
+        HM_CK_LAUNCH("leaf_up");
+    }
+    for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
+        const int b = h->up_ptr[l], n = h->up_ptr[l + 1] - b;
+        xfer_up<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_up + b, n, T, t, r, k);
+        HM_CK_LAUNCH("xfer_up");
+    }
+    if (h->n_m2l_rows) {
+        m2l<S, A><<<warp_grid((int64_t)h->n_m2l_rows * k), kWarpCta, 0, st>>>(
+            h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), t, s, r, k);
+        HM_CK_LAUNCH("m2l");
+    }
+    for (size_t l = 0; l + 1 < h->down_ptr.size(); ++l) {
+        const int b = h->down_ptr[l], n = h->down_ptr[l + 1] - b;
+        xfer_down<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_down + b, n, T, s, r, k);
+        HM_CK_LAUNCH("xfer_down");
+    }
+    if (h->n_segs) return launch_expand<S, A, 1>(h, ma, s, st);
+    return HM_OK;
+}
+
 }  // namespace
 
 struct hm_plan {
@@ -596,6 +665,30 @@ int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t n
                                                                               b, rows, nrows, out);
     HM_CK_LAUNCH("direct_rows");
     return HM_OK;
+}
+
+int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *stream)
+{
+    g_last_error.clear();
+    if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
+    const size_t es = h->storage == HM_F64 ? sizeof(double) : sizeof(float);
+    const size_t need = (size_t)(h->n_xslots + h->n_yslots) * h->r * es;
+    if (need > HM_NOALLOC_SCRATCH_BYTES) {
+        set_error("hm_mul_noalloc: this matrix needs %zu bytes of coefficient scratch; the static scratch "
+                  "holds %u bytes (use hm_mul)", need, (unsigned)HM_NOALLOC_SCRATCH_BYTES);
+        return HM_ERR_UNSUPPORTED;
+    }
+    void *scratch = nullptr;
+    HM_TRY(noalloc_scratch(&scratch));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (h->storage == HM_F64) {
+        MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, h->ny, 1, h->nx, 1,
+                           accumulate ? 1 : 0};
+        return run_mul_static<double, double>(h, ma, st, static_cast<double *>(scratch));
+    }
+    MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, h->ny, 1, h->nx, 1,
+                      accumulate ? 1 : 0};
+    return run_mul_static<float, float>(h, ma, st, static_cast<float *>(scratch));
 }
 
 int hm_profile(hm_handle *h, int stage_mask)

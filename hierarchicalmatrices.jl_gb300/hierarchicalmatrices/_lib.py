@@ -56,7 +56,7 @@ STAGES = ("leaf_up", "xfer_up", "m2l", "xfer_down", "expand")
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
     "hm_kernelmatrix_build", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
-    "hm_mul_host", "hm_direct_rows", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
+    "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free",
 )
 
@@ -104,6 +104,8 @@ def _load():
     L.hm_mul_strided.argtypes = [_vp, _vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, _vp]
     L.hm_mul_host.restype = ctypes.c_int
     L.hm_mul_host.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
+    L.hm_mul_noalloc.restype = ctypes.c_int
+    L.hm_mul_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp]
     L.hm_direct_rows.restype = ctypes.c_int
     L.hm_direct_rows.argtypes = [_vp, _vp, _vp, _i64, _vp, _vp]
     L.hm_profile.restype = ctypes.c_int

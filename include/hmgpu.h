@@ -110,6 +110,26 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate);
 int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t nrows, double *out,
                    void *stream);
 
+/* Allocation-free single right-hand-side product (no counterpart in the
+   reference).  For callers that cannot let a library allocate device memory
+   during a product: processes whose GPU memory is reserved up front by
+   another allocator, and loops that must not call cudaMalloc/cudaFree after
+   start-up because those calls can synchronise the device.
+     u (+)= H v   (accumulate = 1 adds, as the reference's mul!; 0 overwrites)
+   u, v: DEVICE vectors of the handle's storage type (lengths nx, ny).
+   The coefficient scratch is a 16 MiB array compiled into the library
+   (every GPU that loads the library holds it until the process exits);
+   matrices needing more (n_xslots + n_yslots) * rank * element size bytes
+   are rejected with HM_ERR_UNSUPPORTED.  Nothing in the array needs to
+   start at zero: each call writes every coefficient before reading it, so
+   a call never depends on what the previous call left there.  All calls
+   share the one array: calls that overlap on the GPU (different streams,
+   or different handles, at the same time) race and give wrong results.
+   The first call on each device looks up the array's device address
+   (cudaGetSymbolAddress) with that device current; make that first call
+   before any stream capture.  Calls no cudaMalloc/cudaFree. */
+int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *stream);
+
 /* Per-stage timing of hm_mul (the reference prints @time per call,
    examples/Kernel.jl:73-76): for each stage whose bit is set in stage_mask
    (0 leaf bases, 1 upward transfers, 2 far field, 3 downward transfers,
