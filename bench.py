@@ -65,6 +65,7 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
+        time.sleep(0.4)                     # let the sampler start before the timed region
         return self
 
     def __exit__(self, *a):
@@ -202,8 +203,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-variants", action="store_true")
@@ -263,6 +264,7 @@ def main():
         ms = float(t.item())
     value = world * 1e3 / ms
     err32 = rel_err_sampled(H32, u32, b64, rows, torch)
+    H32.check_errors()
 
     # dominant kernel: row-segment panels (stage "expand")
     hbm_peak, peak_kind = peaks()

@@ -57,7 +57,7 @@ int cuda_status(cudaError_t e, const char *what)
     } while (0)
 
 constexpr int kSegRows = 64;
-#define HM_NSTAGES 5   // leaf_up, xfer_up, m2l, xfer_down, expand
+#define HM_NSTAGES 3   // up_pass, down_pass, expand
 constexpr int kWarpCta = 256;
 
 inline unsigned warp_grid(int64_t warps) { return (unsigned)((warps * 32 + kWarpCta - 1) / kWarpCta); }
@@ -131,6 +131,9 @@ struct hm_handle {
     hm_m2l_ent *d_m2l_ents = nullptr;
     hm_xfer *d_down = nullptr;
     std::vector<int> down_ptr;
+    int32_t *d_yparent = nullptr, *d_xparent = nullptr;
+    int n_up = 0, fstride = 0;
+    size_t err_off = 0;             // error word offset in a per-call scratch
     hm_seg *d_segs = nullptr;
     int n_segs = 0;
     hm_piece *d_pieces = nullptr;
@@ -216,6 +219,10 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     HM_TRY(h->upload(&ff, P.f_fill, st));
     HM_TRY(h->upload(&h->d_down, P.down, st));
     h->down_ptr = P.down_level_ptr;
+    HM_TRY(h->upload(&h->d_yparent, P.y_up_parent, st));
+    HM_TRY(h->upload(&h->d_xparent, P.x_parent, st));
+    h->n_up = (int)P.up.size();
+    h->fstride = P.fstride;
     HM_TRY(h->upload(&h->d_segs, P.segs, st));
     h->n_segs = (int)P.segs.size();
     HM_TRY(h->upload(&h->d_pieces, P.pieces, st));
@@ -236,7 +243,7 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
         HM_CK_LAUNCH("fill_vpanels");
     }
     if (!P.f_fill.empty()) {
-        fill_f<S><<<(unsigned)P.f_fill.size(), 128, 0, st>>>(fa, ff, (int)P.f_fill.size(), F);
+        fill_f<S><<<(unsigned)P.f_fill.size(), 128, 0, st>>>(fa, ff, h->d_m2l_ents, (int)P.f_fill.size(), F);
         HM_CK_LAUNCH("fill_f");
     }
     if (h->n_segs) {
@@ -254,7 +261,7 @@ struct StageTimer {
     cudaEvent_t a = nullptr, b = nullptr;
     StageTimer(hm_handle *h_, int stage_, cudaStream_t st_) : h(h_), stage(stage_), st(st_)
     {
-        if (!(h->profile_mask & (1u << stage))) return;
+        if (stage < 0 || !(h->profile_mask & (1u << stage))) return;
         cudaEventCreate(&a);
         cudaEventCreate(&b);
         cudaEventRecord(a, st);
@@ -267,8 +274,33 @@ struct StageTimer {
     }
 };
 
-template <typename S, typename A>
-int get_scratch(hm_handle *h, cudaStream_t st, size_t bytes, A **out)
+// Per-call scratch.  First the synchronisation words of the single-launch
+// passes (upward counters, row-slot flags, the ticket counter, an error
+// word) at offsets that do not depend on the number of right-hand sides,
+// then the coefficients t (column slots) and s (row slots).  The words must
+// be zero before the first call; every complete call leaves them zero again
+// (the error word stays set until read).
+struct ScratchLayout {
+    size_t cnt_off, flag_off, ticket_off, err_off, t_off, s_off, bytes;
+};
+
+inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+template <typename A>
+ScratchLayout scratch_layout(const hm_handle *h, int k)
+{
+    ScratchLayout L;
+    L.cnt_off = 0;
+    L.flag_off = (size_t)h->n_up * sizeof(int);
+    L.ticket_off = L.flag_off + (size_t)h->n_xslots * sizeof(int);
+    L.err_off = L.ticket_off + sizeof(int);
+    L.t_off = align256(L.err_off + sizeof(int));
+    L.s_off = L.t_off + align256((size_t)h->n_yslots * k * h->r * sizeof(A));
+    L.bytes = L.s_off + align256((size_t)h->n_xslots * k * h->r * sizeof(A));
+    return L;
+}
+
+int get_scratch(hm_handle *h, cudaStream_t st, size_t bytes, void **out)
 {
     std::lock_guard<std::mutex> lk(h->mu);
     auto &sc = h->scratch[(void *)st];
@@ -276,23 +308,80 @@ int get_scratch(hm_handle *h, cudaStream_t st, size_t bytes, A **out)
         if (sc.p) HM_CK(cudaFreeAsync(sc.p, st));
         sc.p = nullptr; sc.bytes = 0;
         HM_CK(cudaMallocAsync(&sc.p, bytes, st));
+        HM_CK(cudaMemsetAsync(sc.p, 0, bytes, st));
         sc.bytes = bytes;
     }
-    *out = static_cast<A *>(sc.p);
+    *out = sc.p;
     return HM_OK;
 }
 
 template <typename S, typename A, int KT>
-int launch_expand(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+int launch_expand(hm_handle *h, const MulArgs<S> &ma, const A *s, int *flags, int *ticket, cudaStream_t st)
 {
     const size_t smem = (size_t)std::max(h->max_width, 1) * KT * sizeof(A);
     if (smem > 48 * 1024) {
         if (smem > 227 * 1024) { set_error("panel width %d too large", h->max_width); return HM_ERR_UNSUPPORTED; }
         HM_CK(cudaFuncSetAttribute(expand<S, A, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
-    expand<S, A, KT><<<h->n_segs, kSegRows, smem, st>>>(ma, h->d_segs, h->d_pieces,
-                                                          static_cast<const S *>(h->d_P), s, h->r);
+    expand<S, A, KT><<<h->n_segs, kSegRows, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(h->d_P),
+                                                          s, h->r, flags, h->n_xslots, ticket);
     HM_CK_LAUNCH("expand");
+    return HM_OK;
+}
+
+constexpr int kPassWarps = 4;   // warps per CTA of up_pass / down_pass / expand1
+
+// The three launches of one product on stream st, using `scratch` laid out
+// by scratch_layout<A>(h, ma.k).  timing = false records no events.
+template <typename S, typename A>
+int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, void *scratch, bool timing)
+{
+    const int r = h->r, k = ma.k;
+    const ScratchLayout L = scratch_layout<A>(h, k);
+    char *base = static_cast<char *>(scratch);
+    int *cnt = reinterpret_cast<int *>(base + L.cnt_off);
+    int *flags = reinterpret_cast<int *>(base + L.flag_off);
+    int *ticket = reinterpret_cast<int *>(base + L.ticket_off);
+    int *err = reinterpret_cast<int *>(base + L.err_off);
+    A *t = reinterpret_cast<A *>(base + L.t_off);
+    A *s = reinterpret_cast<A *>(base + L.s_off);
+    const A *T = static_cast<const A *>(h->d_T);
+    const size_t tsm = align256(2 * (size_t)r * r * sizeof(A));
+    if (h->n_vp) {
+        StageTimer tm(h, timing ? 0 : -1, st);
+        const unsigned grid = (unsigned)((h->n_vp + kPassWarps - 1) / kPassWarps);
+        up_pass<S, A><<<grid, 32 * kPassWarps, tsm, st>>>(ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V),
+                                                           h->d_up, h->d_yparent, T, t, cnt, r);
+        HM_CK_LAUNCH("up_pass");
+    }
+    if (h->n_m2l_rows) {
+        StageTimer tm(h, timing ? 1 : -1, st);
+        const size_t smem = tsm + (size_t)kPassWarps * h->fstride * sizeof(S);
+        const int want = (h->n_m2l_rows + kPassWarps - 1) / kPassWarps;
+        const unsigned grid = (unsigned)std::min(want, 152 * 16);
+        down_pass<S, A><<<grid, 32 * kPassWarps, smem, st>>>(
+            h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, h->d_xparent,
+            T, t, s, flags, ticket, err, r, k);
+        HM_CK_LAUNCH("down_pass");
+    }
+    if (h->n_segs) {
+        StageTimer tm(h, timing ? 2 : -1, st);
+        if (k == 1) {
+            const size_t smem = (size_t)kPassWarps * std::max(h->max_width, 1) * sizeof(A);
+            if (smem > 48 * 1024) {
+                if (smem > 227 * 1024) { set_error("panel width %d too large", h->max_width); return HM_ERR_UNSUPPORTED; }
+                HM_CK(cudaFuncSetAttribute(expand1<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            }
+            const unsigned grid = (unsigned)((h->n_segs + kPassWarps - 1) / kPassWarps);
+            expand1<S, A><<<grid, 32 * kPassWarps, smem, st>>>(ma, h->d_segs, h->n_segs, h->d_pieces,
+                                                               static_cast<const S *>(h->d_P), s, r,
+                                                               std::max(h->max_width, 1), flags, h->n_xslots, ticket);
+            HM_CK_LAUNCH("expand1");
+            return HM_OK;
+        }
+        if (sizeof(A) == 8) return launch_expand<S, A, 4>(h, ma, s, flags, ticket, st);
+        return launch_expand<S, A, 8>(h, ma, s, flags, ticket, st);
+    }
     return HM_OK;
 }
 
@@ -300,46 +389,9 @@ template <typename S, typename A>
 int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st)
 {
     if (ma.k <= 0) return HM_OK;
-    const int r = h->r, k = ma.k;
-    const size_t nt = (size_t)h->n_yslots * k * r, ns = (size_t)h->n_xslots * k * r;
-    A *t = nullptr;
-    if (nt + ns) {
-        int e = get_scratch<S, A>(h, st, (nt + ns) * sizeof(A), &t);
-        if (e) return e;
-    }
-    A *s = t + nt;
-    const A *T = static_cast<const A *>(h->d_T);
-    if (h->n_vp) {
-        StageTimer tm(h, 0, st);
-        leaf_up<S, A><<<warp_grid((int64_t)h->n_vp * k), kWarpCta, 0, st>>>(
-            ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
-        HM_CK_LAUNCH("leaf_up");
-    }
-    for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
-        const int b = h->up_ptr[l], n = h->up_ptr[l + 1] - b;
-        StageTimer tm(h, 1, st);
-        xfer_up<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_up + b, n, T, t, r, k);
-        HM_CK_LAUNCH("xfer_up");
-    }
-    if (h->n_m2l_rows) {
-        StageTimer tm(h, 2, st);
-        m2l<S, A><<<warp_grid((int64_t)h->n_m2l_rows * k), kWarpCta, 0, st>>>(
-            h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), t, s, r, k);
-        HM_CK_LAUNCH("m2l");
-    }
-    for (size_t l = 0; l + 1 < h->down_ptr.size(); ++l) {
-        const int b = h->down_ptr[l], n = h->down_ptr[l + 1] - b;
-        StageTimer tm(h, 3, st);
-        xfer_down<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_down + b, n, T, s, r, k);
-        HM_CK_LAUNCH("xfer_down");
-    }
-    if (h->n_segs) {
-        StageTimer tm(h, 4, st);
-        if (k == 1) return launch_expand<S, A, 1>(h, ma, s, st);
-        if (sizeof(A) == 8) return launch_expand<S, A, 4>(h, ma, s, st);
-        return launch_expand<S, A, 8>(h, ma, s, st);
-    }
-    return HM_OK;
+    void *scratch = nullptr;
+    HM_TRY(get_scratch(h, st, scratch_layout<A>(h, ma.k).bytes, &scratch));
+    return launch_pipeline<S, A>(h, ma, st, scratch, true);
 }
 
 int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
@@ -387,38 +439,6 @@ int noalloc_scratch(void **out)
         g_noalloc_addr[dev] = p;
     }
     *out = g_noalloc_addr[dev];
-    return HM_OK;
-}
-
-// The launch sequence of run_mul with the caller-provided scratch t (and s
-// after it); no allocation, no timing events.
-template <typename S, typename A>
-int run_mul_static(hm_handle *h, MulArgs<S> ma, cudaStream_t st, A *t)
-{
-    const int r = h->r, k = ma.k;
-    A *s = t + (size_t)h->n_yslots * k * r;
-    const A *T = static_cast<const A *>(h->d_T);
-    if (h->n_vp) {
-        leaf_up<S, A><<<warp_grid((int64_t)h->n_vp * k), kWarpCta, 0, st>>>(
-            ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
-        HM_CK_LAUNCH("leaf_up");
-    }
-    for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
-        const int b = h->up_ptr[l], n = h->up_ptr[l + 1] - b;
-        xfer_up<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_up + b, n, T, t, r, k);
-        HM_CK_LAUNCH("xfer_up");
-    }
-    if (h->n_m2l_rows) {
-        m2l<S, A><<<warp_grid((int64_t)h->n_m2l_rows * k), kWarpCta, 0, st>>>(
-            h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), t, s, r, k);
-        HM_CK_LAUNCH("m2l");
-    }
-    for (size_t l = 0; l + 1 < h->down_ptr.size(); ++l) {
-        const int b = h->down_ptr[l], n = h->down_ptr[l + 1] - b;
-        xfer_down<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_down + b, n, T, s, r, k);
-        HM_CK_LAUNCH("xfer_down");
-    }
-    if (h->n_segs) return launch_expand<S, A, 1>(h, ma, s, st);
     return HM_OK;
 }
 
@@ -516,6 +536,7 @@ const char *hm_status_string(int status)
     case HM_ERR_UNSUPPORTED: return "unsupported parameter";
     case HM_ERR_BOX: return "box ends must satisfy a > b and c > d";
     case HM_ERR_DEGENERATE: return "degenerate partition";
+    case HM_ERR_TIMEOUT: return "a bounded device-side wait gave up";
     default: return "unknown status";
     }
 }
@@ -573,8 +594,8 @@ int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double 
     st = (storage == HM_F64) ? build_device<double>(h, P, cheb, lam, T, x, y, cs)
                              : build_device<float>(h, P, cheb, lam, T, x, y, cs);
     hm_plan_free(pl);
-    h->launches_per_mul = (h->n_vp > 0) + (int)std::max<size_t>(h->up_ptr.size(), 1) - 1 + (h->n_m2l_rows > 0) +
-                          (int)std::max<size_t>(h->down_ptr.size(), 1) - 1 + (h->n_segs > 0);
+    h->launches_per_mul = (h->n_vp > 0) + (h->n_m2l_rows > 0) + (h->n_segs > 0);
+    h->err_off = scratch_layout<double>(h, 1).err_off;
     if (st) { hm_free(h); return st; }
     *out = h;
     return HM_OK;
@@ -671,10 +692,9 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
 {
     g_last_error.clear();
     if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
-    const size_t es = h->storage == HM_F64 ? sizeof(double) : sizeof(float);
-    const size_t need = (size_t)(h->n_xslots + h->n_yslots) * h->r * es;
+    const size_t need = h->storage == HM_F64 ? scratch_layout<double>(h, 1).bytes : scratch_layout<float>(h, 1).bytes;
     if (need > HM_NOALLOC_SCRATCH_BYTES) {
-        set_error("hm_mul_noalloc: this matrix needs %zu bytes of coefficient scratch; the static scratch "
+        set_error("hm_mul_noalloc: this matrix needs %zu bytes of scratch; the static scratch "
                   "holds %u bytes (use hm_mul)", need, (unsigned)HM_NOALLOC_SCRATCH_BYTES);
         return HM_ERR_UNSUPPORTED;
     }
@@ -684,11 +704,30 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
     if (h->storage == HM_F64) {
         MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, h->ny, 1, h->nx, 1,
                            accumulate ? 1 : 0};
-        return run_mul_static<double, double>(h, ma, st, static_cast<double *>(scratch));
+        return launch_pipeline<double, double>(h, ma, st, scratch, false);
     }
     MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, h->ny, 1, h->nx, 1,
                       accumulate ? 1 : 0};
-    return run_mul_static<float, float>(h, ma, st, static_cast<float *>(scratch));
+    return launch_pipeline<float, float>(h, ma, st, scratch, false);
+}
+
+int hm_stream_errors(hm_handle *h, void *stream, int clear)
+{
+    if (!h) return HM_ERR_INVALID_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    void *p = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        auto it = h->scratch.find((void *)st);
+        if (it == h->scratch.end() || !it->second.p) return HM_OK;
+        p = it->second.p;
+    }
+    HM_CK(cudaStreamSynchronize(st));
+    int v = 0;
+    HM_CK(cudaMemcpy(&v, static_cast<char *>(p) + h->err_off, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v && clear) HM_CK(cudaMemset(static_cast<char *>(p) + h->err_off, 0, sizeof(int)));
+    if (v) { set_error("a bounded wait in the far-field pass gave up"); return HM_ERR_TIMEOUT; }
+    return HM_OK;
 }
 
 int hm_profile(hm_handle *h, int stage_mask)

@@ -50,6 +50,9 @@ struct Acc<double> {
     __device__ __forceinline__ void zero() { s = 0.0; }
     __device__ __forceinline__ void add(double p, double g) { s = fma(p, g, s); }
     __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ double s_hi() const { return s; }
+    __device__ __forceinline__ double s_lo() const { return 0.0; }
+    __device__ __forceinline__ double merged(double so, double) const { return s + so; }
 };
 
 template <>
@@ -66,6 +69,15 @@ struct Acc<float> {
         c = __fadd_rn(c, __fadd_rn(e, l));
     }
     __device__ __forceinline__ float value() const { return __fadd_rn(s, c); }
+    __device__ __forceinline__ float s_hi() const { return s; }
+    __device__ __forceinline__ float s_lo() const { return c; }
+    // value of this accumulator plus another (so, co) one
+    __device__ __forceinline__ float merged(float so, float co) const
+    {
+        float t, e;
+        two_sum(s, so, t, e);
+        return __fadd_rn(t, __fadd_rn(e, __fadd_rn(c, co)));
+    }
 };
 
 struct FillArgs {
@@ -89,7 +101,7 @@ template <typename S>
 __global__ void fill_vpanels(FillArgs fa, const hm_vpanel *vp, const hm_fill_vpanel *vf, int npanels, S *V);
 
 template <typename S>
-__global__ void fill_f(FillArgs fa, const hm_fill_f *ff, int nblocks, S *F);
+__global__ void fill_f(FillArgs fa, const hm_fill_f *ff, const hm_m2l_ent *ents, int nblocks, S *F);
 
 template <typename S>
 __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *pieces,
@@ -98,21 +110,21 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
 // ---------------------------------------------------------------- matvec
 
 template <typename S, typename A>
-__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
-
-template <typename A>
-__global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k);
+__global__ void up_pass(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, const hm_xfer *up,
+                        const int32_t *yparent, const A *T, A *t, int *cnt, int r);
 
 template <typename S, typename A>
-__global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F,
-                    const A *t, A *s, int r, int k);
+__global__ void down_pass(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
+                          const int32_t *xparent, const A *T, const A *t, A *s, int *flags, int *ticket,
+                          int *err, int r, int k);
 
-template <typename A>
-__global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k);
+template <typename S, typename A>
+__global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
+                        const A *s, int r, int maxw, int *flags, int nflags, int *ticket);
 
 template <typename S, typename A, int KT>
 __global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P,
-                       const A *s, int r);
+                       const A *s, int r, int *flags, int nflags, int *ticket);
 
 // ---------------------------------------------------------------- direct sums
 

@@ -217,7 +217,20 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
         P.vstore_elems = off;
     }
 
+    // Parent links for the single-launch upward and downward passes.
+    P.y_up_parent.assign(P.n_yslots, -1);
+    for (size_t i = 0; i < P.up.size(); ++i) {
+        P.y_up_parent[P.up[i].c0] = (int32_t)i;
+        P.y_up_parent[P.up[i].c1] = (int32_t)i;
+    }
+    P.x_parent.assign(P.n_xslots, -1);
+    for (const hm_xfer &e : P.down) {
+        P.x_parent[e.c0] = 2 * e.slot;
+        P.x_parent[e.c1] = 2 * e.slot + 1;
+    }
+
     // M2L rows: barycentric blocks grouped by row cluster.
+    P.fstride = (int)round_up((int64_t)r * r, 4);
     {
         std::vector<std::pair<int, int>> bs;   // (xslot, index into bary)
         for (size_t i = 0; i < P.bary.size(); ++i)
@@ -235,13 +248,13 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
             if (row.end == 0) row.begin = (int32_t)k;
             row.end = (int32_t)(k + 1);
             hm_m2l_ent e;
-            e.foff = (int64_t)k * r * r;
+            e.foff = (int64_t)k * P.fstride;
             e.yslot = P.Y.nodes[yn].slot;
             e.pad = 0;
             P.m2l_ents.push_back(e);
             P.f_fill.push_back({P.X.nodes[xn].a, P.X.nodes[xn].b, P.Y.nodes[yn].a, P.Y.nodes[yn].b});
         }
-        P.fstore_elems = (int64_t)bs.size() * r * r;
+        P.fstore_elems = (int64_t)bs.size() * P.fstride;
     }
 
     // Row segments: elementary row intervals of {row-basis leaves, dense rows}.
@@ -332,7 +345,7 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
     S.dense_values = dv;
     S.canonical_values = (ux + uy) * r + S.n_bary * r * r + dv;
     S.reference_values = refv + dv;
-    int64_t st = P.fstore_elems;
+    int64_t st = (int64_t)P.bary.size() * r * r;
     for (auto &v : P.vpanels) st += (int64_t)v.nrows * v.width;
     for (auto &s : P.segs) st += (int64_t)s.nrows * s.width;
     S.stored_values = st;

@@ -65,6 +65,9 @@ struct Plan {
     std::vector<hm_m2l_ent> m2l_ents;
     std::vector<hm_fill_f> f_fill;
     int64_t fstore_elems = 0;
+    int fstride = 0;                          // elements between F blocks (r*r rounded to 4)
+    std::vector<int32_t> y_up_parent;         // per column slot: index of its parent's upward step, -1 at a root
+    std::vector<int32_t> x_parent;            // per row slot: 2*parent slot + child index, -1 at a root
     std::vector<hm_xfer> down;                // x tree, top level first
     std::vector<int> down_level_ptr;
     std::vector<hm_seg> segs;

@@ -196,7 +196,8 @@ def test_profile_stage_times():
     st = H.stage_times()
     H.profile([])
     assert st["expand"][1] == 3 and st["expand"][0] > 0
-    assert st["m2l"][1] == 3
+    assert st["down"][1] == 3 and st["up"][1] == 3
+    H.check_errors()
 
 
 # ---- full size (n = 2^20): size-independent properties ---------------------
@@ -245,3 +246,23 @@ def test_2pow20_fp32_error(big):
     assert err <= TOL32
     u64 = H64 @ b.double()
     assert float(torch.linalg.norm(u32.double() - u64) / torch.linalg.norm(u64)) <= TOL32
+
+
+def test_repeated_calls_and_streams():
+    # the single-launch passes reset their synchronisation words: repeated
+    # products, and products on a second stream, give identical results
+    n = 65536
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    b = torch.randn(n, device="cuda", dtype=torch.float64)
+    u1 = H @ b
+    for _ in range(5):
+        u2 = H @ b
+        assert torch.equal(u1, u2)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        u3 = H @ b
+    s.synchronize()
+    assert torch.equal(u1, u3)
+    H.check_errors()
+    H.check_errors(stream=s)
