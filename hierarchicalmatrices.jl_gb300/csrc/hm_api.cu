@@ -57,7 +57,7 @@ int cuda_status(cudaError_t e, const char *what)
     } while (0)
 
 constexpr int kSegRows = 64;
-#define HM_NSTAGES 3   // up_pass, down_pass, expand
+#define HM_NSTAGES 4   // upward pass, far field + downward pass, near-field panels, far-field panels
 constexpr int kWarpCta = 256;
 
 inline unsigned warp_grid(int64_t warps) { return (unsigned)((warps * 32 + kWarpCta - 1) / kWarpCta); }
@@ -133,14 +133,20 @@ struct hm_handle {
     std::vector<int> down_ptr;
     int32_t *d_yparent = nullptr, *d_xparent = nullptr;
     int n_up = 0, fstride = 0;
-    size_t err_off = 0;             // error word offset in a per-call scratch
     hm_seg *d_segs = nullptr;
     int n_segs = 0;
     hm_piece *d_pieces = nullptr;
 
     std::mutex mu;
-    struct Scratch { void *p = nullptr; size_t bytes = 0; };
-    std::map<void *, Scratch> scratch;   // per stream, grown stream-ordered
+    // Per caller stream: coefficient scratch (grown stream-ordered), the side
+    // stream of the tree passes and the fork/join events.
+    struct StreamCtx {
+        void *p = nullptr;
+        size_t bytes = 0;
+        cudaStream_t side = nullptr;
+        cudaEvent_t fork = nullptr, join = nullptr;
+    };
+    std::map<void *, StreamCtx> streams;
     void *d_stage = nullptr;
     size_t stage_bytes = 0;
     cudaStream_t host_stream = nullptr;
@@ -274,14 +280,9 @@ struct StageTimer {
     }
 };
 
-// Per-call scratch.  First the synchronisation words of the single-launch
-// passes (upward counters, row-slot flags, the ticket counter, an error
-// word) at offsets that do not depend on the number of right-hand sides,
-// then the coefficients t (column slots) and s (row slots).  The words must
-// be zero before the first call; every complete call leaves them zero again
-// (the error word stays set until read).
+// Per-call scratch: coefficients t (column slots) then s (row slots).
 struct ScratchLayout {
-    size_t cnt_off, flag_off, ticket_off, err_off, t_off, s_off, bytes;
+    size_t t_off, s_off, bytes;
 };
 
 inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
@@ -290,33 +291,91 @@ template <typename A>
 ScratchLayout scratch_layout(const hm_handle *h, int k)
 {
     ScratchLayout L;
-    L.cnt_off = 0;
-    L.flag_off = (size_t)h->n_up * sizeof(int);
-    L.ticket_off = L.flag_off + (size_t)h->n_xslots * sizeof(int);
-    L.err_off = L.ticket_off + sizeof(int);
-    L.t_off = align256(L.err_off + sizeof(int));
-    L.s_off = L.t_off + align256((size_t)h->n_yslots * k * h->r * sizeof(A));
+    L.t_off = 0;
+    L.s_off = align256((size_t)h->n_yslots * k * h->r * sizeof(A));
     L.bytes = L.s_off + align256((size_t)h->n_xslots * k * h->r * sizeof(A));
     return L;
 }
 
-int get_scratch(hm_handle *h, cudaStream_t st, size_t bytes, void **out)
+// Scratch, side stream and fork/join events for products issued on stream st.
+int stream_ctx(hm_handle *h, cudaStream_t st, size_t bytes, hm_handle::StreamCtx **out)
 {
     std::lock_guard<std::mutex> lk(h->mu);
-    auto &sc = h->scratch[(void *)st];
+    auto &sc = h->streams[(void *)st];
+    if (!sc.side) {
+        int least = 0, greatest = 0;
+        HM_CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        HM_CK(cudaStreamCreateWithPriority(&sc.side, cudaStreamNonBlocking, greatest));
+        HM_CK(cudaEventCreateWithFlags(&sc.fork, cudaEventDisableTiming));
+        HM_CK(cudaEventCreateWithFlags(&sc.join, cudaEventDisableTiming));
+    }
     if (sc.bytes < bytes) {
         if (sc.p) HM_CK(cudaFreeAsync(sc.p, st));
         sc.p = nullptr; sc.bytes = 0;
         HM_CK(cudaMallocAsync(&sc.p, bytes, st));
-        HM_CK(cudaMemsetAsync(sc.p, 0, bytes, st));
         sc.bytes = bytes;
     }
-    *out = sc.p;
+    *out = &sc;
+    return HM_OK;
+}
+
+constexpr int kWarpsPerCta = 4;
+
+inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
+
+// Tree passes on stream st: leaf bases, upward transfers level by level, far
+// field, downward transfers level by level.
+template <typename S, typename A>
+int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
+{
+    const int r = h->r, k = ma.k;
+    const A *T = static_cast<const A *>(h->d_T);
+    {
+        StageTimer tm(h, timing ? 0 : -1, st);
+        if (h->n_vp) {
+            leaf_up<S, A><<<warp_grid(h->n_vp), kWarpCta, 0, st>>>(ma, h->d_vp, h->n_vp,
+                                                                   static_cast<const S *>(h->d_V), t, r);
+            HM_CK_LAUNCH("leaf_up");
+        }
+        for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
+            const int b = h->up_ptr[l], n = h->up_ptr[l + 1] - b;
+            xfer_up<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_up + b, n, T, t, r, k);
+            HM_CK_LAUNCH("xfer_up");
+        }
+    }
+    {
+        StageTimer tm(h, timing ? 1 : -1, st);
+        if (h->n_m2l_rows) {
+            const size_t smem = (size_t)kWarpsPerCta * h->fstride * sizeof(S);
+            m2l<S, A><<<warp_ctas(h->n_m2l_rows), 32 * kWarpsPerCta, smem, st>>>(
+                h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
+            HM_CK_LAUNCH("m2l");
+        }
+        for (size_t l = 0; l + 1 < h->down_ptr.size(); ++l) {
+            const int b = h->down_ptr[l], n = h->down_ptr[l + 1] - b;
+            xfer_down<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_down + b, n, T, s, r, k);
+            HM_CK_LAUNCH("xfer_down");
+        }
+    }
+    return HM_OK;
+}
+
+template <typename S, typename A, bool FAR>
+int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+{
+    const size_t smem = (size_t)kWarpsPerCta * std::max(h->max_width, 1) * sizeof(A);
+    if (smem > 48 * 1024) {
+        if (smem > 227 * 1024) { set_error("panel width %d too large", h->max_width); return HM_ERR_UNSUPPORTED; }
+        HM_CK(cudaFuncSetAttribute(expand_part<S, A, FAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    expand_part<S, A, FAR><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
+        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(h->d_P), s, h->r, std::max(h->max_width, 1));
+    HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
     return HM_OK;
 }
 
 template <typename S, typename A, int KT>
-int launch_expand(hm_handle *h, const MulArgs<S> &ma, const A *s, int *flags, int *ticket, cudaStream_t st)
+int launch_expand(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
 {
     const size_t smem = (size_t)std::max(h->max_width, 1) * KT * sizeof(A);
     if (smem > 48 * 1024) {
@@ -324,74 +383,61 @@ int launch_expand(hm_handle *h, const MulArgs<S> &ma, const A *s, int *flags, in
         HM_CK(cudaFuncSetAttribute(expand<S, A, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     expand<S, A, KT><<<h->n_segs, kSegRows, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(h->d_P),
-                                                          s, h->r, flags, h->n_xslots, ticket);
+                                                          s, h->r);
     HM_CK_LAUNCH("expand");
     return HM_OK;
 }
 
-constexpr int kPassWarps = 4;   // warps per CTA of up_pass / down_pass / expand1
-
-// The three launches of one product on stream st, using `scratch` laid out
-// by scratch_layout<A>(h, ma.k).  timing = false records no events.
+// One product.  With a side stream the tree passes run there, concurrently
+// with the near-field panels on the caller's stream; the far field U s is
+// added after the join.  side == st runs everything in order on st.
 template <typename S, typename A>
-int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, void *scratch, bool timing)
+int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStream_t side, cudaEvent_t fork,
+                    cudaEvent_t join, void *scratch, bool timing)
 {
-    const int r = h->r, k = ma.k;
+    const int k = ma.k;
     const ScratchLayout L = scratch_layout<A>(h, k);
-    char *base = static_cast<char *>(scratch);
-    int *cnt = reinterpret_cast<int *>(base + L.cnt_off);
-    int *flags = reinterpret_cast<int *>(base + L.flag_off);
-    int *ticket = reinterpret_cast<int *>(base + L.ticket_off);
-    int *err = reinterpret_cast<int *>(base + L.err_off);
-    A *t = reinterpret_cast<A *>(base + L.t_off);
-    A *s = reinterpret_cast<A *>(base + L.s_off);
-    const A *T = static_cast<const A *>(h->d_T);
-    const size_t tsm = align256(2 * (size_t)r * r * sizeof(A));
-    if (h->n_vp) {
-        StageTimer tm(h, timing ? 0 : -1, st);
-        const unsigned grid = (unsigned)((h->n_vp + kPassWarps - 1) / kPassWarps);
-        up_pass<S, A><<<grid, 32 * kPassWarps, tsm, st>>>(ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V),
-                                                           h->d_up, h->d_yparent, T, t, cnt, r);
-        HM_CK_LAUNCH("up_pass");
-    }
-    if (h->n_m2l_rows) {
-        StageTimer tm(h, timing ? 1 : -1, st);
-        const size_t smem = tsm + (size_t)kPassWarps * h->fstride * sizeof(S);
-        const int want = (h->n_m2l_rows + kPassWarps - 1) / kPassWarps;
-        const unsigned grid = (unsigned)std::min(want, 152 * 16);
-        down_pass<S, A><<<grid, 32 * kPassWarps, smem, st>>>(
-            h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, h->d_xparent,
-            T, t, s, flags, ticket, err, r, k);
-        HM_CK_LAUNCH("down_pass");
-    }
-    if (h->n_segs) {
-        StageTimer tm(h, timing ? 2 : -1, st);
-        if (k == 1) {
-            const size_t smem = (size_t)kPassWarps * std::max(h->max_width, 1) * sizeof(A);
-            if (smem > 48 * 1024) {
-                if (smem > 227 * 1024) { set_error("panel width %d too large", h->max_width); return HM_ERR_UNSUPPORTED; }
-                HM_CK(cudaFuncSetAttribute(expand1<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            }
-            const unsigned grid = (unsigned)((h->n_segs + kPassWarps - 1) / kPassWarps);
-            expand1<S, A><<<grid, 32 * kPassWarps, smem, st>>>(ma, h->d_segs, h->n_segs, h->d_pieces,
-                                                               static_cast<const S *>(h->d_P), s, r,
-                                                               std::max(h->max_width, 1), flags, h->n_xslots, ticket);
-            HM_CK_LAUNCH("expand1");
-            return HM_OK;
+    A *t = reinterpret_cast<A *>(static_cast<char *>(scratch) + L.t_off);
+    A *s = reinterpret_cast<A *>(static_cast<char *>(scratch) + L.s_off);
+    const bool split = side != st;
+    const bool tree = h->n_vp || h->n_m2l_rows;
+    if (tree) {
+        if (split) {
+            HM_CK(cudaEventRecord(fork, st));
+            HM_CK(cudaStreamWaitEvent(side, fork, 0));
         }
-        if (sizeof(A) == 8) return launch_expand<S, A, 4>(h, ma, s, flags, ticket, st);
-        return launch_expand<S, A, 8>(h, ma, s, flags, ticket, st);
+        HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing)));
+        if (split) HM_CK(cudaEventRecord(join, side));
     }
-    return HM_OK;
+    if (!h->n_segs) {
+        if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
+        return HM_OK;
+    }
+    if (k == 1) {
+        {
+            StageTimer tm(h, timing ? 2 : -1, st);
+            HM_TRY((launch_part<S, A, false>(h, ma, s, st)));
+        }
+        if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
+        if (tree) {
+            StageTimer tm(h, timing ? 3 : -1, st);
+            HM_TRY((launch_part<S, A, true>(h, ma, s, st)));
+        }
+        return HM_OK;
+    }
+    if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
+    StageTimer tm(h, timing ? 2 : -1, st);
+    if (sizeof(A) == 8) return launch_expand<S, A, 4>(h, ma, s, st);
+    return launch_expand<S, A, 8>(h, ma, s, st);
 }
 
 template <typename S, typename A>
 int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st)
 {
     if (ma.k <= 0) return HM_OK;
-    void *scratch = nullptr;
-    HM_TRY(get_scratch(h, st, scratch_layout<A>(h, ma.k).bytes, &scratch));
-    return launch_pipeline<S, A>(h, ma, st, scratch, true);
+    hm_handle::StreamCtx *sc = nullptr;
+    HM_TRY(stream_ctx(h, st, scratch_layout<A>(h, ma.k).bytes, &sc));
+    return launch_pipeline<S, A>(h, ma, st, sc->side, sc->fork, sc->join, sc->p, true);
 }
 
 int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
@@ -536,7 +582,6 @@ const char *hm_status_string(int status)
     case HM_ERR_UNSUPPORTED: return "unsupported parameter";
     case HM_ERR_BOX: return "box ends must satisfy a > b and c > d";
     case HM_ERR_DEGENERATE: return "degenerate partition";
-    case HM_ERR_TIMEOUT: return "a bounded device-side wait gave up";
     default: return "unknown status";
     }
 }
@@ -594,8 +639,9 @@ int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double 
     st = (storage == HM_F64) ? build_device<double>(h, P, cheb, lam, T, x, y, cs)
                              : build_device<float>(h, P, cheb, lam, T, x, y, cs);
     hm_plan_free(pl);
-    h->launches_per_mul = (h->n_vp > 0) + (h->n_m2l_rows > 0) + (h->n_segs > 0);
-    h->err_off = scratch_layout<double>(h, 1).err_off;
+    h->launches_per_mul = (h->n_vp > 0) + (int)std::max<size_t>(h->up_ptr.size(), 1) - 1 + (h->n_m2l_rows > 0) +
+                          (int)std::max<size_t>(h->down_ptr.size(), 1) - 1 +
+                          (h->n_segs > 0) * (1 + ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
     if (st) { hm_free(h); return st; }
     *out = h;
     return HM_OK;
@@ -704,30 +750,11 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
     if (h->storage == HM_F64) {
         MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, h->ny, 1, h->nx, 1,
                            accumulate ? 1 : 0};
-        return launch_pipeline<double, double>(h, ma, st, scratch, false);
+        return launch_pipeline<double, double>(h, ma, st, st, nullptr, nullptr, scratch, false);
     }
     MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, h->ny, 1, h->nx, 1,
                       accumulate ? 1 : 0};
-    return launch_pipeline<float, float>(h, ma, st, scratch, false);
-}
-
-int hm_stream_errors(hm_handle *h, void *stream, int clear)
-{
-    if (!h) return HM_ERR_INVALID_ARG;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    void *p = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(h->mu);
-        auto it = h->scratch.find((void *)st);
-        if (it == h->scratch.end() || !it->second.p) return HM_OK;
-        p = it->second.p;
-    }
-    HM_CK(cudaStreamSynchronize(st));
-    int v = 0;
-    HM_CK(cudaMemcpy(&v, static_cast<char *>(p) + h->err_off, sizeof(int), cudaMemcpyDeviceToHost));
-    if (v && clear) HM_CK(cudaMemset(static_cast<char *>(p) + h->err_off, 0, sizeof(int)));
-    if (v) { set_error("a bounded wait in the far-field pass gave up"); return HM_ERR_TIMEOUT; }
-    return HM_OK;
+    return launch_pipeline<float, float>(h, ma, st, st, nullptr, nullptr, scratch, false);
 }
 
 int hm_profile(hm_handle *h, int stage_mask)
@@ -763,8 +790,12 @@ void hm_free(hm_handle *h)
 {
     if (!h) return;
     cudaDeviceSynchronize();
-    for (auto &kv : h->scratch)
+    for (auto &kv : h->streams) {
         if (kv.second.p) cudaFree(kv.second.p);
+        if (kv.second.side) cudaStreamDestroy(kv.second.side);
+        if (kv.second.fork) cudaEventDestroy(kv.second.fork);
+        if (kv.second.join) cudaEventDestroy(kv.second.join);
+    }
     for (auto &e : h->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     if (h->d_stage) cudaFree(h->d_stage);
     if (h->host_stream) cudaStreamDestroy(h->host_stream);

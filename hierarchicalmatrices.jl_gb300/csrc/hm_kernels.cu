@@ -121,201 +121,160 @@ template __global__ void fill_segments<float>(FillArgs, const hm_seg *, const hm
 // ============================================================== matvec kernels
 //
 // Coefficients of slot `sl` for right-hand side q live at coef[(sl*k + q)*r + m].
-// A product is three launches: up_pass, down_pass, then expand1/expand.
+// A product runs the tree passes (leaf_up, xfer_up per level, m2l, xfer_down
+// per level) on a side stream while expand_part<.., false> streams the
+// near-field dense panels on the caller's stream; after the join
+// expand_part<.., true> adds the far field U s.
 
-// Upward pass in one launch.  One warp per explicit column basis panel:
-// t[leaf] = V^T x (lane m owns basis column m of the row-major panel, so
-// loads are coalesced and need no cross-lane reduction), then the warp
-// climbs the column tree: at each parent the second child to arrive (an
-// atomic counter) computes t[parent] = sum_c T_c^T t[child_c] and climbs on,
-// the first simply stops.  Nothing waits, so the launch always completes.
-// The second arrival resets the counter, leaving it zero for the next call.
+// t[leaf] = V^T x for each explicit column basis panel.  One warp per panel;
+// lane m owns basis column m of the row-major panel (coalesced, no cross-lane
+// reduction).
 template <typename S, typename A>
-__global__ void up_pass(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, const hm_xfer *up,
-                        const int32_t *yparent, const A *T, A *t, int *cnt, int r)
+__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r)
 {
-    extern __shared__ unsigned char smem_raw[];
-    A *Ts = reinterpret_cast<A *>(smem_raw);
-    for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) Ts[i] = T[i];
-    __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (w >= npanels) return;
     const hm_vpanel P = vp[w];
-    const int k = ma.k;
-    for (int q = 0; q < k; ++q) {
+    if (lane >= r) return;
+    const S *col = V + P.off + lane;
+    for (int q = 0; q < ma.k; ++q) {
         const S *xq = ma.x + (int64_t)q * ma.ldx + P.row0 * ma.incx;
         Acc<A> acc;
         acc.zero();
-        if (lane < r) {
-            const S *col = V + P.off + lane;
-            int j = 0;
-            for (; j + 4 <= P.nrows; j += 4) {
-                const A x0 = (A)xq[(int64_t)j * ma.incx], x1 = (A)xq[(int64_t)(j + 1) * ma.incx];
-                const A x2 = (A)xq[(int64_t)(j + 2) * ma.incx], x3 = (A)xq[(int64_t)(j + 3) * ma.incx];
-                const A v0 = (A)col[(int64_t)j * P.ld], v1 = (A)col[(int64_t)(j + 1) * P.ld];
-                const A v2 = (A)col[(int64_t)(j + 2) * P.ld], v3 = (A)col[(int64_t)(j + 3) * P.ld];
-                acc.add(v0, x0); acc.add(v1, x1); acc.add(v2, x2); acc.add(v3, x3);
-            }
-            for (; j < P.nrows; ++j) acc.add((A)col[(int64_t)j * P.ld], (A)xq[(int64_t)j * ma.incx]);
-            t[((int64_t)P.slot * k + q) * r + lane] = acc.value();
+        int j = 0;
+        for (; j + 4 <= P.nrows; j += 4) {
+            const A x0 = (A)xq[(int64_t)j * ma.incx], x1 = (A)xq[(int64_t)(j + 1) * ma.incx];
+            const A x2 = (A)xq[(int64_t)(j + 2) * ma.incx], x3 = (A)xq[(int64_t)(j + 3) * ma.incx];
+            const A v0 = (A)col[(int64_t)j * P.ld], v1 = (A)col[(int64_t)(j + 1) * P.ld];
+            const A v2 = (A)col[(int64_t)(j + 2) * P.ld], v3 = (A)col[(int64_t)(j + 3) * P.ld];
+            acc.add(v0, x0); acc.add(v1, x1); acc.add(v2, x2); acc.add(v3, x3);
         }
-    }
-    int slot = P.slot;
-    for (;;) {
-        const int p = yparent[slot];
-        if (p < 0) break;
-        __syncwarp();
-        int old = 0;
-        if (lane == 0) {
-            __threadfence();
-            old = atomicAdd(&cnt[p], 1);
-        }
-        old = __shfl_sync(0xffffffffu, old, 0);
-        if (old == 0) break;                    // first child here: the sibling climbs on
-        if (lane == 0) cnt[p] = 0;
-        __threadfence();
-        const hm_xfer X = up[p];
-        for (int q = 0; q < k; ++q) {
-            if (lane < r) {
-                const A *t0 = t + ((int64_t)X.c0 * k + q) * r;
-                const A *t1 = t + ((int64_t)X.c1 * k + q) * r;
-                A a = 0;
-                for (int mp = 0; mp < r; ++mp) {
-                    a += Ts[mp * r + lane] * __ldcg(t0 + mp);
-                    a += Ts[r * r + mp * r + lane] * __ldcg(t1 + mp);
-                }
-                t[((int64_t)X.slot * k + q) * r + lane] = a;
-            }
-        }
-        slot = X.slot;
+        for (; j < P.nrows; ++j) acc.add((A)col[(int64_t)j * P.ld], (A)xq[(int64_t)j * ma.incx]);
+        t[((int64_t)P.slot * ma.k + q) * r + lane] = acc.value();
     }
 }
 
-// Far field and downward pass in one launch.  Warps take row slots in
-// level order from a ticket counter.  For its slot a warp forms
-//   s[slot] = sum_e F_e t[yslot_e]            (the F stage of src/algebra.jl:258-265)
-// staging each r x r block in shared memory with 16-byte loads, then waits
-// for its parent slot's flag and adds T_c s[parent] (the downward transfer),
-// and publishes its own flag.  A parent always holds a lower ticket than its
-// children, so it was taken by a running warp: every wait ends.  Waits are
-// still bounded; on the bound the warp records an error in err[0] and goes on.
-#define HM_SPIN_LIMIT (1 << 22)
+// Upward transfer of one level: t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m'].
+// One warp per (parent, rhs); the children's coefficients are loaded once,
+// one per lane, and broadcast with shuffles.  T holds T_0 then T_1, each
+// r x r with T_c[m' * r + m].
+template <typename A>
+__global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k)
+{
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (int64_t)nx * k) return;
+    const hm_xfer X = xf[w / k];
+    const int q = (int)(w % k);
+    A v0 = 0, v1 = 0;
+    if (lane < r) {
+        v0 = t[((int64_t)X.c0 * k + q) * r + lane];
+        v1 = t[((int64_t)X.c1 * k + q) * r + lane];
+    }
+    A acc = 0;
+    for (int mp = 0; mp < r; ++mp) {
+        const A a0 = __shfl_sync(0xffffffffu, v0, mp), a1 = __shfl_sync(0xffffffffu, v1, mp);
+        if (lane < r) acc += __ldg(T + mp * r + lane) * a0 + __ldg(T + r * r + mp * r + lane) * a1;
+    }
+    if (lane < r) t[((int64_t)X.slot * k + q) * r + lane] = acc;
+}
+
+// Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
+// (the F stage of src/algebra.jl:258-265, grouped by row cluster).  One warp
+// per (row slot, rhs chunk); each r x r block is staged in shared memory with
+// 16-byte loads by all lanes, the column coefficients are loaded one per lane
+// and broadcast with shuffles.
 template <typename S, typename A>
-__global__ void down_pass(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
-                          const int32_t *xparent, const A *T, const A *t, A *s, int *flags, int *ticket,
-                          int *err, int r, int k)
+__global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
+                    const A *t, A *s, int r, int k)
 {
     extern __shared__ unsigned char smem_raw[];
-    A *Ts = reinterpret_cast<A *>(smem_raw);
-    S *Fb = reinterpret_cast<S *>(smem_raw + sizeof(A) * 2 * r * r) + (threadIdx.x >> 5) * fstride;
-    for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) Ts[i] = T[i];
-    __syncthreads();
+    constexpr int VE = 16 / sizeof(S);
+    S *Fb = reinterpret_cast<S *>(smem_raw) + (threadIdx.x >> 5) * fstride;
     const int lane = threadIdx.x & 31;
-    constexpr int QC = 8;
-    constexpr int VE = 16 / sizeof(S);         // elements per 16-byte load
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(ticket, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= nrows) break;
-        const hm_m2l_row R = rows[item];
-        const int slot = R.slot;
-        for (int q0 = 0; q0 < k; q0 += QC) {
-            const int qc = min(QC, k - q0);
-            A acc[QC];
-#pragma unroll
-            for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
-            for (int e = R.begin; e < R.end; ++e) {
-                const hm_m2l_ent E = ents[e];
-                const float4 *src = reinterpret_cast<const float4 *>(F + E.foff);
-                float4 *dst = reinterpret_cast<float4 *>(Fb);
-                for (int i = lane; i < fstride / VE; i += 32) dst[i] = __ldg(src + i);
-                __syncwarp();
-                if (lane < r) {
-                    const A *te = t + ((int64_t)E.yslot * k + q0) * r;
-                    for (int n = 0; n < r; ++n) {
-                        const A f = (A)Fb[lane + r * n];
-#pragma unroll
-                        for (int qq = 0; qq < QC; ++qq)
-                            if (qq < qc) acc[qq] += f * te[qq * r + n];
-                    }
-                }
-                __syncwarp();
-            }
-            if (lane < r) {
-#pragma unroll
-                for (int qq = 0; qq < QC; ++qq)
-                    if (qq < qc) s[((int64_t)slot * k + q0 + qq) * r + lane] = acc[qq];
-            }
-        }
-        const int pp = xparent[slot];
-        if (pp >= 0) {
-            const int ps = pp >> 1, c = pp & 1;
-            if (lane == 0) {
-                int it = 0;
-                while (*(volatile int *)(flags + ps) == 0) {
-                    if (++it > HM_SPIN_LIMIT) { atomicExch(err, 1); break; }
-                    __nanosleep(64);
-                }
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= nrows) return;
+    const hm_m2l_row R = rows[w];
+    for (int q = 0; q < k; ++q) {
+        A acc = 0;
+        for (int e = R.begin; e < R.end; ++e) {
+            const hm_m2l_ent E = ents[e];
+            const float4 *src = reinterpret_cast<const float4 *>(F + E.foff);
+            float4 *dst = reinterpret_cast<float4 *>(Fb);
+            for (int i = lane; i < fstride / VE; i += 32) dst[i] = __ldg(src + i);
+            const A tv = (lane < r) ? t[((int64_t)E.yslot * k + q) * r + lane] : (A)0;
+            __syncwarp();
+            for (int n = 0; n < r; ++n) {
+                const A tn = __shfl_sync(0xffffffffu, tv, n);
+                if (lane < r) acc += (A)Fb[lane + r * n] * tn;
             }
             __syncwarp();
-            __threadfence();
-            if (lane < r) {
-                const A *Tc = Ts + c * r * r + lane * r;
-                for (int q = 0; q < k; ++q) {
-                    const A *sp = s + ((int64_t)ps * k + q) * r;
-                    A a = 0;
-                    for (int m = 0; m < r; ++m) a += Tc[m] * __ldcg(sp + m);
-                    s[((int64_t)slot * k + q) * r + lane] += a;
-                }
-            }
         }
-        __syncwarp();
-        if (lane == 0) {
-            __threadfence();
-            atomicExch(flags + slot, 1);
-        }
+        if (lane < r) s[((int64_t)R.slot * k + q) * r + lane] = acc;
     }
 }
 
-// Clears the flags and the ticket of down_pass so the next call starts from
-// zero (runs in the launch that follows down_pass).
-__device__ __forceinline__ void clear_sync(int *flags, int nflags, int *ticket)
+// Downward transfer of one level: s[child_c][m'] += sum_m T_c[m', m] s[parent][m].
+template <typename A>
+__global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k)
 {
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = tid; i < nflags; i += nth) flags[i] = 0;
-    if (tid == 0 && ticket) *ticket = 0;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (int64_t)nx * k) return;
+    const hm_xfer X = xf[w / k];
+    const int q = (int)(w % k);
+    const A sp = (lane < r) ? s[((int64_t)X.slot * k + q) * r + lane] : (A)0;
+    A a0 = 0, a1 = 0;
+    for (int m = 0; m < r; ++m) {
+        const A v = __shfl_sync(0xffffffffu, sp, m);
+        if (lane < r) {
+            a0 += __ldg(T + lane * r + m) * v;
+            a1 += __ldg(T + r * r + lane * r + m) * v;
+        }
+    }
+    if (lane < r) {
+        s[((int64_t)X.c0 * k + q) * r + lane] += a0;
+        s[((int64_t)X.c1 * k + q) * r + lane] += a1;
+    }
 }
 
 // Row segments, one right-hand side: one warp per segment (<= 64 rows).
+// FAR = false: the near-field dense columns, y (+)= D x (written with the
+// caller's accumulate flag); FAR = true: the row-basis columns, y += U s.
 // FP32: lanes 0-15 and 16-31 take alternate panel columns, each lane four
 // consecutive rows through one 16-byte load per column; FP64: each lane two
-// rows per 16-byte load.  The gathered right-hand side [s ; x pieces] is
-// staged per warp in shared memory.  FP32 products accumulate with
-// compensated (TwoProd/TwoSum) sums.
-template <typename S, typename A>
-__global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                        const A *s, int r, int maxw, int *flags, int nflags, int *ticket)
+// rows per 16-byte load.  The gathered right-hand side is staged per warp in
+// shared memory.  FP32 products accumulate with compensated (TwoProd/TwoSum)
+// sums.
+template <typename S, typename A, bool FAR>
+__global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
+                            const A *s, int r, int maxw)
 {
     extern __shared__ unsigned char smem_raw[];
-    clear_sync(flags, nflags, ticket);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int seg = blockIdx.x * (blockDim.x >> 5) + wib;
     if (seg >= nsegs) return;
     A *g = reinterpret_cast<A *>(smem_raw) + (int64_t)wib * maxw;
     const hm_seg G = segs[seg];
-    int col = 0;
+    // columns [c0, c1) of the panel
+    int c0 = 0, c1 = 0, col = 0;
     for (int pc = 0; pc < G.npieces; ++pc) {
         const hm_piece Q = pieces[G.piece0 + pc];
-        for (int c = lane; c < Q.width; c += 32)
-            g[col + c] = (Q.kind == HM_PIECE_COEF) ? s[Q.src * r + c] : (A)ma.x[(Q.src + c) * ma.incx];
+        const bool take = FAR ? (Q.kind == HM_PIECE_COEF) : (Q.kind == HM_PIECE_X);
+        if (take) {
+            if (c1 == c0) c0 = col;
+            for (int c = lane; c < Q.width; c += 32)
+                g[col + c] = FAR ? s[Q.src * r + c] : (A)ma.x[(Q.src + c) * ma.incx];
+            c1 = col + Q.width;
+        }
         col += Q.width;
     }
+    if (FAR && c1 == c0) return;          // no far field on these rows
     __syncwarp();
     const S *Pg = P + G.poff;
+    const bool acc_y = FAR || ma.accumulate;
     if (sizeof(S) == 4) {
         const int rg = lane & 15, h = lane >> 4;
         Acc<A> acc[4];
@@ -324,8 +283,8 @@ __global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_p
         if (4 * rg < G.ld) {
             const float4 *base = reinterpret_cast<const float4 *>(Pg + 4 * rg);
             const int64_t ld4 = G.ld / 4;
-            int c = h;
-            for (; c + 6 < G.width; c += 8) {
+            int c = c0 + h;
+            for (; c + 6 < c1; c += 8) {
                 const float4 p0 = __ldcs(base + ld4 * c), p1 = __ldcs(base + ld4 * (c + 2));
                 const float4 p2 = __ldcs(base + ld4 * (c + 4)), p3 = __ldcs(base + ld4 * (c + 6));
                 const A g0 = g[c], g1 = g[c + 2], g2 = g[c + 4], g3 = g[c + 6];
@@ -334,13 +293,12 @@ __global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_p
                 acc[0].add(p2.x, g2); acc[1].add(p2.y, g2); acc[2].add(p2.z, g2); acc[3].add(p2.w, g2);
                 acc[0].add(p3.x, g3); acc[1].add(p3.y, g3); acc[2].add(p3.z, g3); acc[3].add(p3.w, g3);
             }
-            for (; c < G.width; c += 2) {
+            for (; c < c1; c += 2) {
                 const float4 p0 = __ldcs(base + ld4 * c);
                 const A g0 = g[c];
                 acc[0].add(p0.x, g0); acc[1].add(p0.y, g0); acc[2].add(p0.z, g0); acc[3].add(p0.w, g0);
             }
         }
-        // fold the two column halves: (s, c) pairs combined with TwoSum
         A val[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -355,7 +313,7 @@ __global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_p
                 if (row < G.nrows) {
                     S *yp = ma.y + (G.row0 + row) * ma.incy;
                     A v = val[j];
-                    if (ma.accumulate) v += (A)(*yp);
+                    if (acc_y) v += (A)(*yp);
                     *yp = (S)v;
                 }
             }
@@ -366,8 +324,8 @@ __global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_p
         if (2 * lane < G.ld) {
             const double2 *base = reinterpret_cast<const double2 *>(Pg + 2 * lane);
             const int64_t ld2 = G.ld / 2;
-            int c = 0;
-            for (; c + 4 <= G.width; c += 4) {
+            int c = c0;
+            for (; c + 4 <= c1; c += 4) {
                 const double2 p0 = __ldcs(base + ld2 * c), p1 = __ldcs(base + ld2 * (c + 1));
                 const double2 p2 = __ldcs(base + ld2 * (c + 2)), p3 = __ldcs(base + ld2 * (c + 3));
                 a0.add(p0.x, g[c]); a1.add(p0.y, g[c]);
@@ -375,7 +333,7 @@ __global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_p
                 a0.add(p2.x, g[c + 2]); a1.add(p2.y, g[c + 2]);
                 a0.add(p3.x, g[c + 3]); a1.add(p3.y, g[c + 3]);
             }
-            for (; c < G.width; ++c) {
+            for (; c < c1; ++c) {
                 const double2 p0 = __ldcs(base + ld2 * c);
                 a0.add(p0.x, g[c]); a1.add(p0.y, g[c]);
             }
@@ -387,7 +345,7 @@ __global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_p
             if (row < G.nrows) {
                 S *yp = ma.y + (G.row0 + row) * ma.incy;
                 A v = v2[j];
-                if (ma.accumulate) v += (A)(*yp);
+                if (acc_y) v += (A)(*yp);
                 *yp = (S)v;
             }
         }
@@ -398,11 +356,10 @@ __global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_p
 // row; the gathered right-hand sides are staged in shared memory, KT at a time.
 template <typename S, typename A, int KT>
 __global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P,
-                       const A *s, int r, int *flags, int nflags, int *ticket)
+                       const A *s, int r)
 {
     extern __shared__ unsigned char smem_raw[];
     A *g = reinterpret_cast<A *>(smem_raw);
-    clear_sync(flags, nflags, ticket);
     const hm_seg G = segs[blockIdx.x];
     const S *Pg = P + G.poff;
     for (int q0 = 0; q0 < ma.k; q0 += KT) {
@@ -461,19 +418,23 @@ __global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces
 }
 
 #define HM_INST_MV(S, A)                                                                             \
-    template __global__ void up_pass<S, A>(MulArgs<S>, const hm_vpanel *, int, const S *, const hm_xfer *, \
-                                           const int32_t *, const A *, A *, int *, int);                \
-    template __global__ void down_pass<S, A>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int, \
-                                             const int32_t *, const A *, const A *, A *, int *, int *,  \
-                                             int *, int, int);                                          \
-    template __global__ void expand1<S, A>(MulArgs<S>, const hm_seg *, int, const hm_piece *, const S *, \
-                                           const A *, int, int, int *, int, int *);                     \
+    template __global__ void leaf_up<S, A>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);      \
+    template __global__ void m2l<S, A>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,       \
+                                       const A *, A *, int, int);                                       \
+    template __global__ void expand_part<S, A, false>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
+                                                      const S *, const A *, int, int);                  \
+    template __global__ void expand_part<S, A, true>(MulArgs<S>, const hm_seg *, int, const hm_piece *,   \
+                                                     const S *, const A *, int, int);                   \
     template __global__ void expand<S, A, 4>(MulArgs<S>, const hm_seg *, const hm_piece *,            \
-                                             const S *, const A *, int, int *, int, int *);             \
+                                             const S *, const A *, int);                                \
     template __global__ void expand<S, A, 8>(MulArgs<S>, const hm_seg *, const hm_piece *,            \
-                                             const S *, const A *, int, int *, int, int *);
+                                             const S *, const A *, int);
 HM_INST_MV(double, double)
 HM_INST_MV(float, float)
+template __global__ void xfer_up<double>(const hm_xfer *, int, const double *, double *, int, int);
+template __global__ void xfer_up<float>(const hm_xfer *, int, const float *, float *, int, int);
+template __global__ void xfer_down<double>(const hm_xfer *, int, const double *, double *, int, int);
+template __global__ void xfer_down<float>(const hm_xfer *, int, const float *, float *, int, int);
 
 // ============================================================== direct sums
 

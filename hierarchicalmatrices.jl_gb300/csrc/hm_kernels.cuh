@@ -110,21 +110,25 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
 // ---------------------------------------------------------------- matvec
 
 template <typename S, typename A>
-__global__ void up_pass(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, const hm_xfer *up,
-                        const int32_t *yparent, const A *T, A *t, int *cnt, int r);
+__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
+
+template <typename A>
+__global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k);
 
 template <typename S, typename A>
-__global__ void down_pass(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
-                          const int32_t *xparent, const A *T, const A *t, A *s, int *flags, int *ticket,
-                          int *err, int r, int k);
+__global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
+                    const A *t, A *s, int r, int k);
 
-template <typename S, typename A>
-__global__ void expand1(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                        const A *s, int r, int maxw, int *flags, int nflags, int *ticket);
+template <typename A>
+__global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k);
+
+template <typename S, typename A, bool FAR>
+__global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
+                            const A *s, int r, int maxw);
 
 template <typename S, typename A, int KT>
 __global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P,
-                       const A *s, int r, int *flags, int nflags, int *ticket);
+                       const A *s, int r);
 
 // ---------------------------------------------------------------- direct sums
 

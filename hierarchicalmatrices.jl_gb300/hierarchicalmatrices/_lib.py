@@ -22,7 +22,6 @@ HM_ERR_ALLOC = 6
 HM_ERR_UNSUPPORTED = 7
 HM_ERR_BOX = 8
 HM_ERR_DEGENERATE = 9
-HM_ERR_TIMEOUT = 10
 
 HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
 HM_F64, HM_F32 = 0, 1
@@ -52,12 +51,12 @@ PLAN_SIZES = ("r", "nx", "ny", "n_xslots", "n_yslots", "vstore", "fstore", "psto
 STATS = ("n_bary", "n_dense", "depth", "n_xslots", "n_yslots", "canonical_values",
          "reference_values", "stored_values", "dense_values", "n_segments", "max_width",
          "device_bytes", "launches_per_mul")
-STAGES = ("up", "down", "expand")
+STAGES = ("up", "down", "expand", "far")
 
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
     "hm_kernelmatrix_build", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
-    "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_stream_errors", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
+    "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free",
 )
 
@@ -109,8 +108,6 @@ def _load():
     L.hm_mul_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp]
     L.hm_direct_rows.restype = ctypes.c_int
     L.hm_direct_rows.argtypes = [_vp, _vp, _vp, _i64, _vp, _vp]
-    L.hm_stream_errors.restype = ctypes.c_int
-    L.hm_stream_errors.argtypes = [_vp, _vp, ctypes.c_int]
     L.hm_profile.restype = ctypes.c_int
     L.hm_profile.argtypes = [_vp, ctypes.c_int]
     L.hm_profile_read.restype = ctypes.c_int

@@ -246,11 +246,6 @@ class KernelMatrix:
                                   1 if reset else 0))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(_lib.STAGES)}
 
-    def check_errors(self, stream=None, clear=True):
-        """Synchronise the stream and raise HMError(HM_ERR_TIMEOUT) if a
-        bounded device-side wait of a product on it gave up."""
-        check(lib.hm_stream_errors(self._h, _stream_ptr(stream), 1 if clear else 0))
-
     def free(self):
         if getattr(self, "_h", None):
             lib.hm_free(self._h)

@@ -35,8 +35,7 @@ enum {
     HM_ERR_ALLOC = 6,         /* device allocation failed */
     HM_ERR_UNSUPPORTED = 7,   /* rank above 32, unknown kernel or storage type */
     HM_ERR_BOX = 8,           /* box ends not strictly decreasing (a > b, c > d) */
-    HM_ERR_DEGENERATE = 9,    /* a partition the reference itself builds inconsistently */
-    HM_ERR_TIMEOUT = 10       /* a bounded device-side wait gave up (see hm_stream_errors) */
+    HM_ERR_DEGENERATE = 9     /* a partition the reference itself builds inconsistently */
 };
 
 /* Kernels of examples/Kernel.jl:34-37. */
@@ -90,7 +89,8 @@ int hm_stats(const hm_handle *h, int64_t *out, int nout);
      u[:, q] += H * v[:, q]   (accumulate = 1, the reference's semantics)
      u[:, q]  = H * v[:, q]   (accumulate = 0)
    u, v are DEVICE arrays of the handle's storage type, column q at u + q*ldu.
-   Stream-ordered; returns before the work completes. */
+   Stream-ordered; returns before the work completes.  Internally the tree
+   passes run on a side stream forked from and joined back into `stream`. */
 int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs,
            int accumulate, void *stream);
 
@@ -120,9 +120,8 @@ int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t n
    u, v: DEVICE vectors of the handle's storage type (lengths nx, ny).
    The coefficient scratch is a 16 MiB array compiled into the library
    (every GPU that loads the library holds it until the process exits);
-   matrices needing more ((n_xslots + n_yslots) * rank * element size
-   bytes of coefficients plus 4 bytes per transfer step and row slot) are
-   rejected with HM_ERR_UNSUPPORTED.  Besides coefficients (each call
+   matrices needing more than (n_xslots + n_yslots) * rank * element size
+   bytes (each part rounded up to 256) are rejected with HM_ERR_UNSUPPORTED.  Besides coefficients (each call
    writes them before reading them) the array holds synchronisation words
    that must start at zero: they are zero when the library loads and every
    complete call leaves them at zero again.  All calls
@@ -133,15 +132,10 @@ int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t n
    before any stream capture.  Calls no cudaMalloc/cudaFree. */
 int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *stream);
 
-/* Synchronises `stream` and reports whether a product on it hit the bound of
-   a device-side wait (HM_ERR_TIMEOUT; the product's result is then not to be
-   trusted).  clear = 1 resets the record.  HM_OK when none occurred. */
-int hm_stream_errors(hm_handle *h, void *stream, int clear);
-
 /* Per-stage timing of hm_mul (the reference prints @time per call,
    examples/Kernel.jl:73-76): for each stage whose bit is set in stage_mask
    (0 upward pass: leaf bases and transfers, 1 far field and downward
-   transfers, 2 row segments), CUDA events are recorded on the launching stream around
+   transfers, 2 near-field panels, 3 far-field panel columns), CUDA events are recorded on the launching stream around
    its launches.  hm_profile_read synchronises on them and returns accumulated
    milliseconds and launch counts per stage; reset = 1 clears the totals.
    stage_mask = 0 turns timing off. */
