@@ -333,8 +333,9 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
-            leaf_up<S, A><<<warp_grid(h->n_vp), kWarpCta, 0, st>>>(ma, h->d_vp, h->n_vp,
-                                                                   static_cast<const S *>(h->d_V), t, r);
+            const size_t smem = (size_t)kWarpsPerCta * 64 * r * sizeof(S);
+            leaf_up<S, A><<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(ma, h->d_vp, h->n_vp,
+                                                                                static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
         }
         for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
@@ -347,7 +348,8 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
             const size_t smem = (size_t)kWarpsPerCta * h->fstride * sizeof(S);
-            m2l<S, A><<<warp_ctas(h->n_m2l_rows), 32 * kWarpsPerCta, smem, st>>>(
+            const int64_t nw = (int64_t)h->n_m2l_rows * ((k + 7) / 8);
+            m2l<S, A><<<warp_ctas(nw), 32 * kWarpsPerCta, smem, st>>>(
                 h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
             HM_CK_LAUNCH("m2l");
         }
@@ -374,17 +376,18 @@ int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
     return HM_OK;
 }
 
-template <typename S, typename A, int KT>
-int launch_expand(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+template <typename S, typename A>
+int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
 {
-    const size_t smem = (size_t)std::max(h->max_width, 1) * KT * sizeof(A);
-    if (smem > 48 * 1024) {
-        if (smem > 227 * 1024) { set_error("panel width %d too large", h->max_width); return HM_ERR_UNSUPPORTED; }
-        HM_CK(cudaFuncSetAttribute(expand<S, A, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
-    expand<S, A, KT><<<h->n_segs, kSegRows, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(h->d_P),
-                                                          s, h->r);
-    HM_CK_LAUNCH("expand");
+    const int maxw = std::max(h->max_width, 1);
+    const int qc = sizeof(A) == 8 ? 16 : 32;
+    const size_t smem = ((size_t)64 * maxw * sizeof(S) + 15) / 16 * 16 + (size_t)maxw * qc * sizeof(A);
+    if (smem > 227 * 1024) { set_error("panel width %d too large for the multi-RHS kernel", maxw); return HM_ERR_UNSUPPORTED; }
+    if (smem > 48 * 1024)
+        HM_CK(cudaFuncSetAttribute(expand_k<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    expand_k<S, A><<<h->n_segs, 128, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(h->d_P), s,
+                                                  h->r, maxw);
+    HM_CK_LAUNCH("expand_k");
     return HM_OK;
 }
 
@@ -427,8 +430,7 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
     }
     if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
     StageTimer tm(h, timing ? 2 : -1, st);
-    if (sizeof(A) == 8) return launch_expand<S, A, 4>(h, ma, s, st);
-    return launch_expand<S, A, 8>(h, ma, s, st);
+    return launch_expand_k<S, A>(h, ma, s, st);
 }
 
 template <typename S, typename A>

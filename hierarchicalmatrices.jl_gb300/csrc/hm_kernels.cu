@@ -127,17 +127,47 @@ template __global__ void fill_segments<float>(FillArgs, const hm_seg *, const hm
 // expand_part<.., true> adds the far field U s.
 
 // t[leaf] = V^T x for each explicit column basis panel.  One warp per panel;
-// lane m owns basis column m of the row-major panel (coalesced, no cross-lane
-// reduction).
+// lane m owns basis column m of the row-major panel.  Panels of up to 64
+// rows are staged once in shared memory (16-byte loads by all lanes) and
+// reused for every right-hand side; the x values of a right-hand side are
+// loaded two per lane and broadcast with shuffles.
 template <typename S, typename A>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r)
 {
+    extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
     if (w >= npanels) return;
     const hm_vpanel P = vp[w];
+    const S *Vp = V + P.off;
+    if (P.nrows <= 64) {
+        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * 64 * r;
+        const int nel = P.nrows * r;
+        if (sizeof(S) * nel % 16 == 0) {
+            const float4 *src = reinterpret_cast<const float4 *>(Vp);
+            float4 *dst = reinterpret_cast<float4 *>(Vs);
+            for (int i = lane; i < (int)(nel * sizeof(S) / 16); i += 32) dst[i] = __ldcs(src + i);
+        } else {
+            for (int i = lane; i < nel; i += 32) Vs[i] = Vp[i];
+        }
+        __syncwarp();
+        for (int q = 0; q < ma.k; ++q) {
+            const S *xq = ma.x + (int64_t)q * ma.ldx + P.row0 * ma.incx;
+            const A xa = lane < P.nrows ? (A)xq[(int64_t)lane * ma.incx] : (A)0;
+            const A xb = lane + 32 < P.nrows ? (A)xq[(int64_t)(lane + 32) * ma.incx] : (A)0;
+            Acc<A> acc;
+            acc.zero();
+            for (int j = 0; j < P.nrows; ++j) {
+                const A xj = __shfl_sync(0xffffffffu, j < 32 ? xa : xb, j & 31);
+                if (lane < r) acc.add((A)Vs[j * r + lane], xj);
+            }
+            if (lane < r) t[((int64_t)P.slot * ma.k + q) * r + lane] = acc.value();
+        }
+        return;
+    }
     if (lane >= r) return;
-    const S *col = V + P.off + lane;
+    const S *col = Vp + lane;
     for (int q = 0; q < ma.k; ++q) {
         const S *xq = ma.x + (int64_t)q * ma.ldx + P.row0 * ma.incx;
         Acc<A> acc;
@@ -182,8 +212,9 @@ __global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int 
 
 // Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
 // (the F stage of src/algebra.jl:258-265, grouped by row cluster).  One warp
-// per (row slot, rhs chunk); each r x r block is staged in shared memory with
-// 16-byte loads by all lanes, the column coefficients are loaded one per lane
+// per (row slot, chunk of up to 8 right-hand sides); each r x r block is
+// staged in shared memory with 16-byte loads by all lanes and used for every
+// right-hand side of the chunk; column coefficients are loaded one per lane
 // and broadcast with shuffles.
 template <typename S, typename A>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
@@ -191,27 +222,38 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
 {
     extern __shared__ unsigned char smem_raw[];
     constexpr int VE = 16 / sizeof(S);
+    constexpr int QC = 8;
     S *Fb = reinterpret_cast<S *>(smem_raw) + (threadIdx.x >> 5) * fstride;
     const int lane = threadIdx.x & 31;
+    const int nq = (k + QC - 1) / QC;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= nrows) return;
-    const hm_m2l_row R = rows[w];
-    for (int q = 0; q < k; ++q) {
-        A acc = 0;
-        for (int e = R.begin; e < R.end; ++e) {
-            const hm_m2l_ent E = ents[e];
-            const float4 *src = reinterpret_cast<const float4 *>(F + E.foff);
-            float4 *dst = reinterpret_cast<float4 *>(Fb);
-            for (int i = lane; i < fstride / VE; i += 32) dst[i] = __ldg(src + i);
-            const A tv = (lane < r) ? t[((int64_t)E.yslot * k + q) * r + lane] : (A)0;
-            __syncwarp();
-            for (int n = 0; n < r; ++n) {
-                const A tn = __shfl_sync(0xffffffffu, tv, n);
-                if (lane < r) acc += (A)Fb[lane + r * n] * tn;
-            }
-            __syncwarp();
+    if (w >= (int64_t)nrows * nq) return;
+    const hm_m2l_row R = rows[w / nq];
+    const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+    A acc[QC];
+#pragma unroll
+    for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
+    for (int e = R.begin; e < R.end; ++e) {
+        const hm_m2l_ent E = ents[e];
+        const float4 *src = reinterpret_cast<const float4 *>(F + E.foff);
+        float4 *dst = reinterpret_cast<float4 *>(Fb);
+        for (int i = lane; i < fstride / VE; i += 32) dst[i] = __ldg(src + i);
+        A tv[QC];
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq)
+            tv[qq] = (lane < r && qq < qc) ? t[((int64_t)E.yslot * k + q0 + qq) * r + lane] : (A)0;
+        __syncwarp();
+        for (int n = 0; n < r; ++n) {
+            const A f = lane < r ? (A)Fb[lane + r * n] : (A)0;
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq) acc[qq] += f * __shfl_sync(0xffffffffu, tv[qq], n);
         }
-        if (lane < r) s[((int64_t)R.slot * k + q) * r + lane] = acc;
+        __syncwarp();
+    }
+    if (lane < r) {
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq)
+            if (qq < qc) s[((int64_t)R.slot * k + q0 + qq) * r + lane] = acc[qq];
     }
 }
 
@@ -352,68 +394,109 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
     }
 }
 
-// Row segments, several right-hand sides: one CTA per segment, one thread per
-// row; the gathered right-hand sides are staged in shared memory, KT at a time.
-template <typename S, typename A, int KT>
-__global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P,
-                       const A *s, int r)
+// Row segments, several right-hand sides.  One CTA (128 threads) per
+// segment: the whole column-major panel is staged once in shared memory
+// (16-byte streaming loads), then right-hand sides are processed in chunks
+// of QC: the gathered [s ; x pieces] chunk goes to shared memory and each
+// thread accumulates an RB-row x QB-column register tile.  Each piece is
+// summed in plain FMA and folded into the output with a compensated
+// (TwoSum) addition.
+template <typename A>
+struct KTile;
+template <> struct KTile<float> { static constexpr int RB = 4, QB = 4, RG = 16, QG = 8; };   // 64 rows x 32 rhs
+template <> struct KTile<double> { static constexpr int RB = 2, QB = 4, RG = 32, QG = 4; };  // 64 rows x 16 rhs
+
+template <typename A>
+__device__ __forceinline__ void comp_add(A &hi, A &lo, A v)
 {
-    extern __shared__ unsigned char smem_raw[];
-    A *g = reinterpret_cast<A *>(smem_raw);
+    const A t = hi + v;
+    const A bp = t - hi;
+    lo += (hi - (t - bp)) + (v - bp);
+    hi = t;
+}
+
+template <typename S, typename A>
+__global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s, int r,
+                         int maxw)
+{
+    constexpr int RB = KTile<A>::RB, QB = KTile<A>::QB, RG = KTile<A>::RG, QG = KTile<A>::QG;
+    constexpr int QC = QB * QG;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const hm_seg G = segs[blockIdx.x];
-    const S *Pg = P + G.poff;
-    for (int q0 = 0; q0 < ma.k; q0 += KT) {
-        const int kt = min(KT, ma.k - q0);
+    S *Ps = reinterpret_cast<S *>(smem_raw);                              // ld x width
+    A *Gs = reinterpret_cast<A *>(smem_raw + (((size_t)64 * maxw * sizeof(S) + 15) / 16) * 16);  // width x QC
+    {
+        const int64_t n16 = (int64_t)G.ld * G.width * sizeof(S) / 16;
+        const float4 *src = reinterpret_cast<const float4 *>(P + G.poff);
+        float4 *dst = reinterpret_cast<float4 *>(Ps);
+        for (int64_t i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = __ldcs(src + i);
+    }
+    const int rg = threadIdx.x % RG, qg = threadIdx.x / RG;
+    for (int q0 = 0; q0 < ma.k; q0 += QC) {
+        const int qc = min(QC, ma.k - q0);
+        __syncthreads();
         int col = 0;
         for (int pc = 0; pc < G.npieces; ++pc) {
             const hm_piece Q = pieces[G.piece0 + pc];
-            for (int idx = threadIdx.x; idx < Q.width * KT; idx += blockDim.x) {
-                const int c = idx / KT, qq = idx % KT;
+            for (int idx = threadIdx.x; idx < Q.width * QC; idx += blockDim.x) {
+                const int c = idx / QC, qq = idx % QC;
                 A v = 0;
-                if (qq < kt) {
+                if (qq < qc) {
                     if (Q.kind == HM_PIECE_COEF)
                         v = s[((int64_t)Q.src * ma.k + q0 + qq) * r + c];
                     else
                         v = (A)ma.x[(Q.src + c) * ma.incx + (int64_t)(q0 + qq) * ma.ldx];
                 }
-                g[(col + c) * KT + qq] = v;
+                Gs[(col + c) * QC + qq] = v;
             }
             col += Q.width;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < G.nrows; i += blockDim.x) {
-            Acc<A> acc[KT];
+        A hi[RB][QB], lo[RB][QB];
 #pragma unroll
-            for (int qq = 0; qq < KT; ++qq) acc[qq].zero();
-            const S *pr = Pg + i;
+        for (int i = 0; i < RB; ++i)
+#pragma unroll
+            for (int j = 0; j < QB; ++j) { hi[i][j] = 0; lo[i][j] = 0; }
+        if (rg * RB < G.ld) {
             int c = 0;
-            for (; c + 4 <= G.width; c += 4) {
-                A p0 = (A)pr[(int64_t)G.ld * c], p1 = (A)pr[(int64_t)G.ld * (c + 1)];
-                A p2 = (A)pr[(int64_t)G.ld * (c + 2)], p3 = (A)pr[(int64_t)G.ld * (c + 3)];
+            for (int pc = 0; pc < G.npieces; ++pc) {
+                const int cend = c + pieces[G.piece0 + pc].width;
+                A part[RB][QB];
 #pragma unroll
-                for (int qq = 0; qq < KT; ++qq) {
-                    acc[qq].add(p0, g[c * KT + qq]);
-                    acc[qq].add(p1, g[(c + 1) * KT + qq]);
-                    acc[qq].add(p2, g[(c + 2) * KT + qq]);
-                    acc[qq].add(p3, g[(c + 3) * KT + qq]);
+                for (int i = 0; i < RB; ++i)
+#pragma unroll
+                    for (int j = 0; j < QB; ++j) part[i][j] = 0;
+                for (; c < cend; ++c) {
+                    A pv[RB], gv[QB];
+#pragma unroll
+                    for (int i = 0; i < RB; ++i) pv[i] = (A)Ps[(int64_t)c * G.ld + rg * RB + i];
+#pragma unroll
+                    for (int j = 0; j < QB; ++j) gv[j] = Gs[c * QC + qg * QB + j];
+#pragma unroll
+                    for (int i = 0; i < RB; ++i)
+#pragma unroll
+                        for (int j = 0; j < QB; ++j) part[i][j] = fma(pv[i], gv[j], part[i][j]);
                 }
-            }
-            for (; c < G.width; ++c) {
-                A p0 = (A)pr[(int64_t)G.ld * c];
 #pragma unroll
-                for (int qq = 0; qq < KT; ++qq) acc[qq].add(p0, g[c * KT + qq]);
-            }
+                for (int i = 0; i < RB; ++i)
 #pragma unroll
-            for (int qq = 0; qq < KT; ++qq) {
-                if (qq < kt) {
-                    S *yp = ma.y + (G.row0 + i) * ma.incy + (int64_t)(q0 + qq) * ma.ldy;
-                    A v = acc[qq].value();
-                    if (ma.accumulate) v += (A)(*yp);
-                    *yp = (S)v;
-                }
+                    for (int j = 0; j < QB; ++j) comp_add(hi[i][j], lo[i][j], part[i][j]);
             }
         }
-        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+            const int row = rg * RB + i;
+            if (row >= G.nrows) continue;
+#pragma unroll
+            for (int j = 0; j < QB; ++j) {
+                const int q = qg * QB + j;
+                if (q >= qc) continue;
+                S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)(q0 + q) * ma.ldy;
+                A v = hi[i][j] + lo[i][j];
+                if (ma.accumulate) v += (A)(*yp);
+                *yp = (S)v;
+            }
+        }
     }
 }
 
@@ -425,10 +508,8 @@ __global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces
                                                       const S *, const A *, int, int);                  \
     template __global__ void expand_part<S, A, true>(MulArgs<S>, const hm_seg *, int, const hm_piece *,   \
                                                      const S *, const A *, int, int);                   \
-    template __global__ void expand<S, A, 4>(MulArgs<S>, const hm_seg *, const hm_piece *,            \
-                                             const S *, const A *, int);                                \
-    template __global__ void expand<S, A, 8>(MulArgs<S>, const hm_seg *, const hm_piece *,            \
-                                             const S *, const A *, int);
+    template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
+                                            const A *, int, int);
 HM_INST_MV(double, double)
 HM_INST_MV(float, float)
 template __global__ void xfer_up<double>(const hm_xfer *, int, const double *, double *, int, int);

@@ -126,9 +126,9 @@ template <typename S, typename A, bool FAR>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
                             const A *s, int r, int maxw);
 
-template <typename S, typename A, int KT>
-__global__ void expand(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P,
-                       const A *s, int r);
+template <typename S, typename A>
+__global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s, int r,
+                         int maxw);
 
 // ---------------------------------------------------------------- direct sums
 
