@@ -100,7 +100,7 @@ def test_multi_rhs_matches_columns(dtype, k):
         ref = Ho @ Bh[:, q].copy()
         assert rel(U[:, q].double().cpu().numpy(), ref) <= (TOL64 if dtype == np.float64 else TOL32)
         single = (H @ B[:, q].contiguous()).double().cpu().numpy()
-        assert rel(U[:, q].double().cpu().numpy(), single) <= (1e-14 if dtype == np.float64 else 1e-7)
+        assert rel(U[:, q].double().cpu().numpy(), single) <= (1e-14 if dtype == np.float64 else 5e-7)
 
 
 def test_mul_accumulates_like_reference():
