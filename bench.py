@@ -120,6 +120,19 @@ def time_device(fn, steps, warmup, torch, barrier=None, after_warmup=None):
     return e0.elapsed_time(e1) / steps
 
 
+def serial_stages(H, fn, steps, torch):
+    """Per-stage milliseconds per call with the tree passes run in order on
+    the caller's stream (so stage times do not overlap)."""
+    H.set_overlap(False)
+    H.profile()
+    time_device(fn, steps, 2, torch, after_warmup=lambda: H.stage_times(reset=True))
+    st = H.stage_times(reset=True)
+    H.profile([])
+    H.set_overlap(True)
+    n = max(1, max(v[1] for v in st.values()))
+    return {k: v[0] / n for k, v in st.items()}
+
+
 def rel_err_sampled(H, u, b64, rows, torch):
     ref = H.direct_rows(b64, rows)
     got = u.index_select(0, rows).to(torch.float64)
@@ -251,12 +264,8 @@ def main():
         ms = time_device(lambda: H32.mul(u32, b32, accumulate=False), args.steps, args.warmup,
                          torch, barrier, after_warmup=lambda: H32.stage_times(reset=True))
     exp_total, exp_launches = H32.stage_times(reset=True)["expand"]
-    # all stages, in a separate pass of the same steps (per-stage breakdown)
-    H32.profile()
-    time_device(lambda: H32.mul(u32, b32, accumulate=False), args.steps, 0, torch,
-                after_warmup=lambda: H32.stage_times(reset=True))
-    stages = H32.stage_times(reset=True)
-    H32.profile([])
+    # per-stage breakdown: every stage timed in order on one stream (no overlap)
+    stages = serial_stages(H32, lambda: H32.mul(u32, b32, accumulate=False), args.steps, torch)
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device=dev)
@@ -268,7 +277,6 @@ def main():
     # dominant kernel: row-segment panels (stage "expand")
     hbm_peak, peak_kind = peaks()
     exp_ms = exp_total / max(1, exp_launches)
-    n_mv = max(1, stages["expand"][1])
     # near-field panel kernel: streams the dense leaf values once, reads x
     # once and writes y once
     exp_bytes = st["dense_values"] * 4 + 2 * n * 4
@@ -301,24 +309,27 @@ def main():
         build64_s = time.perf_counter() - t0
         u64 = torch.empty(n, device=dev, dtype=torch.float64)
         ms64 = time_device(lambda: H64.mul(u64, b64, accumulate=False), k_steps, 3, torch)
+        st64s = serial_stages(H64, lambda: H64.mul(u64, b64, accumulate=False), 10, torch)
         err64 = rel_err_sampled(H64, u64, b64, rows, torch)
         st64 = H64.stats()
         variants["fp64_k1"] = {
             "matvec_per_s": 1e3 / ms64, "ms": ms64, "rel_err_vs_dense_fp64": err64,
             "stored_GBs": (st64["stored_values"] * 8 + 2 * n * 8) / (ms64 * 1e-3) / 1e9,
             "effective_canonical_GBs": (st64["canonical_values"] * 8 + 2 * n * 8) / (ms64 * 1e-3) / 1e9,
-            "build_s": build64_s}
+            "build_s": build64_s, "stage_ms_serial": st64s}
         del H64, u64
         torch.cuda.empty_cache()
         for k in (32, 256):
             B = torch.randn(k, n, device=dev, dtype=torch.float32).t()    # column-major n x k
             U = torch.empty(k, n, device=dev, dtype=torch.float32).t()
             msk = time_device(lambda: H32.mul(U, B, accumulate=False), max(3, k_steps // 2), 2, torch)
+            stk = serial_stages(H32, lambda: H32.mul(U, B, accumulate=False), 3, torch)
             errk = rel_err_sampled(H32, U[:, k - 1].contiguous(), B[:, k - 1].to(torch.float64).contiguous(),
                                    rows, torch)
             variants[f"fp32_k{k}"] = {
                 "matvec_per_s": k * 1e3 / msk, "ms_per_block": msk, "rel_err_vs_dense_fp64": errk,
-                "stored_GBs": (st["stored_values"] * 4 + 2 * n * k * 4) / (msk * 1e-3) / 1e9}
+                "stored_GBs": (st["stored_values"] * 4 + 2 * n * k * 4) / (msk * 1e-3) / 1e9,
+                "stage_ms_serial": stk}
             del B, U
             torch.cuda.empty_cache()
 
@@ -352,7 +363,7 @@ def main():
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": None,
                 "peak_source": peak_kind, "kernel_ms": exp_ms, "kernel_bytes": exp_bytes,
-                "stage_ms_per_step": {k: v[0] / n_mv for k, v in stages.items()},
+                "stage_ms_serial": stages,
             },
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 4,
                     "d2h_bytes_per_step": n * 4},

@@ -159,6 +159,7 @@ struct hm_handle {
     double stage_ms[HM_NSTAGES] = {0};
     int64_t stage_launches[HM_NSTAGES] = {0};
     int launches_per_mul = 0;
+    bool overlap = true;            // tree passes on a side stream
 
     template <typename T>
     int alloc(T **p, size_t count)
@@ -324,23 +325,25 @@ constexpr int kWarpsPerCta = 4;
 inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
 
 // Tree passes on stream st: leaf bases, upward transfers level by level, far
-// field, downward transfers level by level.
-template <typename S, typename A>
-int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
+// field, downward transfers level by level.  QC right-hand sides per warp.
+template <typename S, typename A, int QC>
+int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
 {
     const int r = h->r, k = ma.k;
+    const int64_t nq = (k + QC - 1) / QC;
     const A *T = static_cast<const A *>(h->d_T);
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
-            const size_t smem = (size_t)kWarpsPerCta * 64 * r * sizeof(S);
-            leaf_up<S, A><<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(ma, h->d_vp, h->n_vp,
-                                                                                static_cast<const S *>(h->d_V), t, r);
+            const size_t smem = (size_t)kWarpsPerCta * 64 * (r + QC) * sizeof(S);
+            leaf_up<S, A, QC><<<warp_ctas(h->n_vp * nq), 32 * kWarpsPerCta, smem, st>>>(
+                ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
         }
+        const size_t xsm = (size_t)(kWarpCta / 32) * 2 * QC * HM_RMAX * sizeof(A);
         for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
             const int b = h->up_ptr[l], n = h->up_ptr[l + 1] - b;
-            xfer_up<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_up + b, n, T, t, r, k);
+            xfer_up<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, xsm, st>>>(h->d_up + b, n, T, t, r, k);
             HM_CK_LAUNCH("xfer_up");
         }
     }
@@ -348,18 +351,25 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
             const size_t smem = (size_t)kWarpsPerCta * h->fstride * sizeof(S);
-            const int64_t nw = (int64_t)h->n_m2l_rows * ((k + 7) / 8);
-            m2l<S, A><<<warp_ctas(nw), 32 * kWarpsPerCta, smem, st>>>(
+            m2l<S, A, QC><<<warp_ctas((int64_t)h->n_m2l_rows * nq), 32 * kWarpsPerCta, smem, st>>>(
                 h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
             HM_CK_LAUNCH("m2l");
         }
+        const size_t xsm = (size_t)(kWarpCta / 32) * QC * HM_RMAX * sizeof(A);
         for (size_t l = 0; l + 1 < h->down_ptr.size(); ++l) {
             const int b = h->down_ptr[l], n = h->down_ptr[l + 1] - b;
-            xfer_down<A><<<warp_grid((int64_t)n * k), kWarpCta, 0, st>>>(h->d_down + b, n, T, s, r, k);
+            xfer_down<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, xsm, st>>>(h->d_down + b, n, T, s, r, k);
             HM_CK_LAUNCH("xfer_down");
         }
     }
     return HM_OK;
+}
+
+template <typename S, typename A>
+int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
+{
+    if (ma.k == 1) return launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing);
+    return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing);
 }
 
 template <typename S, typename A, bool FAR>
@@ -381,7 +391,7 @@ int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t
 {
     const int maxw = std::max(h->max_width, 1);
     const int qc = sizeof(A) == 8 ? 16 : 32;
-    const size_t smem = ((size_t)64 * maxw * sizeof(S) + 15) / 16 * 16 + (size_t)maxw * qc * sizeof(A);
+    const size_t smem = ((size_t)64 * maxw * sizeof(S) + 31) / 32 * 32 + (size_t)maxw * qc * sizeof(A);
     if (smem > 227 * 1024) { set_error("panel width %d too large for the multi-RHS kernel", maxw); return HM_ERR_UNSUPPORTED; }
     if (smem > 48 * 1024)
         HM_CK(cudaFuncSetAttribute(expand_k<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -439,7 +449,7 @@ int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st)
     if (ma.k <= 0) return HM_OK;
     hm_handle::StreamCtx *sc = nullptr;
     HM_TRY(stream_ctx(h, st, scratch_layout<A>(h, ma.k).bytes, &sc));
-    return launch_pipeline<S, A>(h, ma, st, sc->side, sc->fork, sc->join, sc->p, true);
+    return launch_pipeline<S, A>(h, ma, st, h->overlap ? sc->side : st, sc->fork, sc->join, sc->p, true);
 }
 
 int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
@@ -757,6 +767,15 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
     MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, h->ny, 1, h->nx, 1,
                       accumulate ? 1 : 0};
     return launch_pipeline<float, float>(h, ma, st, st, nullptr, nullptr, scratch, false);
+}
+
+int hm_configure(hm_handle *h, int option, int64_t value)
+{
+    if (!h) return HM_ERR_INVALID_ARG;
+    switch (option) {
+    case HM_OPT_OVERLAP: h->overlap = value != 0; return HM_OK;
+    default: set_error("unknown option %d", option); return HM_ERR_INVALID_ARG;
+    }
 }
 
 int hm_profile(hm_handle *h, int stage_mask)

@@ -1,6 +1,8 @@
 // CUDA kernels: batched compression (fill) and the hierarchical matvec.
 #include "hm_kernels.cuh"
 
+#include <type_traits>
+
 namespace hm {
 
 // ============================================================== fill kernels
@@ -126,23 +128,31 @@ template __global__ void fill_segments<float>(FillArgs, const hm_seg *, const hm
 // near-field dense panels on the caller's stream; after the join
 // expand_part<.., true> adds the far field U s.
 
-// t[leaf] = V^T x for each explicit column basis panel.  One warp per panel;
-// lane m owns basis column m of the row-major panel.  Panels of up to 64
-// rows are staged once in shared memory (16-byte loads by all lanes) and
-// reused for every right-hand side; the x values of a right-hand side are
-// loaded two per lane and broadcast with shuffles.
-template <typename S, typename A>
+// t[leaf] = V^T x for each explicit column basis panel.  One warp per
+// (panel, chunk of QC right-hand sides); lane m owns basis column m of the
+// row-major panel.  Panels of up to 64 rows are staged in shared memory
+// (16-byte loads by all lanes) together with the chunk's x values; longer
+// panels are read directly.  QC = 1 accumulates with compensated sums in
+// FP32, QC > 1 with plain FMA.
+template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r)
 {
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+    const int nq = (ma.k + QC - 1) / QC;
     const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
-    if (w >= npanels) return;
-    const hm_vpanel P = vp[w];
+    if (w >= (int64_t)npanels * nq) return;
+    const hm_vpanel P = vp[w / nq];
+    const int q0 = (int)(w % nq) * QC, qc = min(QC, ma.k - q0);
     const S *Vp = V + P.off;
+    using AccT = typename std::conditional<QC == 1, Acc<A>, PlainAcc<A>>::type;
+    AccT acc[QC];
+#pragma unroll
+    for (int qq = 0; qq < QC; ++qq) acc[qq].zero();
     if (P.nrows <= 64) {
-        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * 64 * r;
+        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * (64 * r + 64 * QC);
+        A *xs = reinterpret_cast<A *>(Vs + 64 * r);          // xs[j * QC + qq]
         const int nel = P.nrows * r;
         if (sizeof(S) * nel % 16 == 0) {
             const float4 *src = reinterpret_cast<const float4 *>(Vp);
@@ -151,63 +161,68 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
         } else {
             for (int i = lane; i < nel; i += 32) Vs[i] = Vp[i];
         }
+        for (int i = lane; i < P.nrows * QC; i += 32) {
+            const int j = i / QC, qq = i % QC;
+            xs[i] = qq < qc ? (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx] : (A)0;
+        }
         __syncwarp();
-        for (int q = 0; q < ma.k; ++q) {
-            const S *xq = ma.x + (int64_t)q * ma.ldx + P.row0 * ma.incx;
-            const A xa = lane < P.nrows ? (A)xq[(int64_t)lane * ma.incx] : (A)0;
-            const A xb = lane + 32 < P.nrows ? (A)xq[(int64_t)(lane + 32) * ma.incx] : (A)0;
-            Acc<A> acc;
-            acc.zero();
+        if (lane < r) {
             for (int j = 0; j < P.nrows; ++j) {
-                const A xj = __shfl_sync(0xffffffffu, j < 32 ? xa : xb, j & 31);
-                if (lane < r) acc.add((A)Vs[j * r + lane], xj);
+                const A v = (A)Vs[j * r + lane];
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xs[j * QC + qq]);
             }
-            if (lane < r) t[((int64_t)P.slot * ma.k + q) * r + lane] = acc.value();
         }
-        return;
+    } else if (lane < r) {
+        const S *col = Vp + lane;
+        for (int j = 0; j < P.nrows; ++j) {
+            const A v = (A)col[(int64_t)j * P.ld];
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq)
+                if (qq < qc) acc[qq].add(v, (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx]);
+        }
     }
-    if (lane >= r) return;
-    const S *col = Vp + lane;
-    for (int q = 0; q < ma.k; ++q) {
-        const S *xq = ma.x + (int64_t)q * ma.ldx + P.row0 * ma.incx;
-        Acc<A> acc;
-        acc.zero();
-        int j = 0;
-        for (; j + 4 <= P.nrows; j += 4) {
-            const A x0 = (A)xq[(int64_t)j * ma.incx], x1 = (A)xq[(int64_t)(j + 1) * ma.incx];
-            const A x2 = (A)xq[(int64_t)(j + 2) * ma.incx], x3 = (A)xq[(int64_t)(j + 3) * ma.incx];
-            const A v0 = (A)col[(int64_t)j * P.ld], v1 = (A)col[(int64_t)(j + 1) * P.ld];
-            const A v2 = (A)col[(int64_t)(j + 2) * P.ld], v3 = (A)col[(int64_t)(j + 3) * P.ld];
-            acc.add(v0, x0); acc.add(v1, x1); acc.add(v2, x2); acc.add(v3, x3);
-        }
-        for (; j < P.nrows; ++j) acc.add((A)col[(int64_t)j * P.ld], (A)xq[(int64_t)j * ma.incx]);
-        t[((int64_t)P.slot * ma.k + q) * r + lane] = acc.value();
+    if (lane < r) {
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq)
+            if (qq < qc) t[((int64_t)P.slot * ma.k + q0 + qq) * r + lane] = acc[qq].value();
     }
 }
 
 // Upward transfer of one level: t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m'].
-// One warp per (parent, rhs); the children's coefficients are loaded once,
-// one per lane, and broadcast with shuffles.  T holds T_0 then T_1, each
-// r x r with T_c[m' * r + m].
-template <typename A>
+// One warp per (parent, chunk of QC right-hand sides); the children's
+// coefficients are staged in shared memory and read as broadcasts.  T holds
+// T_0 then T_1, each r x r with T_c[m' * r + m].
+template <typename A, int QC>
 __global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k)
 {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
-    if (w >= (int64_t)nx * k) return;
-    const hm_xfer X = xf[w / k];
-    const int q = (int)(w % k);
-    A v0 = 0, v1 = 0;
-    if (lane < r) {
-        v0 = t[((int64_t)X.c0 * k + q) * r + lane];
-        v1 = t[((int64_t)X.c1 * k + q) * r + lane];
+    const int nq = (k + QC - 1) / QC;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= (int64_t)nx * nq) return;
+    A *cs = reinterpret_cast<A *>(smem_raw) + (threadIdx.x >> 5) * 2 * QC * HM_RMAX;   // [c][qq][m']
+    const hm_xfer X = xf[w / nq];
+    const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+    for (int i = lane; i < QC * r; i += 32) {
+        const int qq = i / r, m = i % r;
+        cs[qq * HM_RMAX + m] = qq < qc ? t[((int64_t)X.c0 * k + q0 + qq) * r + m] : (A)0;
+        cs[(QC + qq) * HM_RMAX + m] = qq < qc ? t[((int64_t)X.c1 * k + q0 + qq) * r + m] : (A)0;
     }
-    A acc = 0;
+    __syncwarp();
+    if (lane >= r) return;
+    A acc[QC];
+#pragma unroll
+    for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
     for (int mp = 0; mp < r; ++mp) {
-        const A a0 = __shfl_sync(0xffffffffu, v0, mp), a1 = __shfl_sync(0xffffffffu, v1, mp);
-        if (lane < r) acc += __ldg(T + mp * r + lane) * a0 + __ldg(T + r * r + mp * r + lane) * a1;
+        const A a0 = __ldg(T + mp * r + lane), a1 = __ldg(T + r * r + mp * r + lane);
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq)
+            acc[qq] += a0 * cs[qq * HM_RMAX + mp] + a1 * cs[(QC + qq) * HM_RMAX + mp];
     }
-    if (lane < r) t[((int64_t)X.slot * k + q) * r + lane] = acc;
+#pragma unroll
+    for (int qq = 0; qq < QC; ++qq)
+        if (qq < qc) t[((int64_t)X.slot * k + q0 + qq) * r + lane] = acc[qq];
 }
 
 // Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
@@ -216,13 +231,12 @@ __global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int 
 // staged in shared memory with 16-byte loads by all lanes and used for every
 // right-hand side of the chunk; column coefficients are loaded one per lane
 // and broadcast with shuffles.
-template <typename S, typename A>
+template <typename S, typename A, int QC>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
                     const A *t, A *s, int r, int k)
 {
     extern __shared__ unsigned char smem_raw[];
     constexpr int VE = 16 / sizeof(S);
-    constexpr int QC = 8;
     S *Fb = reinterpret_cast<S *>(smem_raw) + (threadIdx.x >> 5) * fstride;
     const int lane = threadIdx.x & 31;
     const int nq = (k + QC - 1) / QC;
@@ -258,26 +272,41 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
 }
 
 // Downward transfer of one level: s[child_c][m'] += sum_m T_c[m', m] s[parent][m].
-template <typename A>
+template <typename A, int QC>
 __global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k)
 {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
-    if (w >= (int64_t)nx * k) return;
-    const hm_xfer X = xf[w / k];
-    const int q = (int)(w % k);
-    const A sp = (lane < r) ? s[((int64_t)X.slot * k + q) * r + lane] : (A)0;
-    A a0 = 0, a1 = 0;
+    const int nq = (k + QC - 1) / QC;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= (int64_t)nx * nq) return;
+    A *ps = reinterpret_cast<A *>(smem_raw) + (threadIdx.x >> 5) * QC * HM_RMAX;   // [qq][m]
+    const hm_xfer X = xf[w / nq];
+    const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+    for (int i = lane; i < QC * r; i += 32) {
+        const int qq = i / r, m = i % r;
+        ps[qq * HM_RMAX + m] = qq < qc ? s[((int64_t)X.slot * k + q0 + qq) * r + m] : (A)0;
+    }
+    __syncwarp();
+    if (lane >= r) return;
+    A a0[QC], a1[QC];
+#pragma unroll
+    for (int qq = 0; qq < QC; ++qq) { a0[qq] = 0; a1[qq] = 0; }
     for (int m = 0; m < r; ++m) {
-        const A v = __shfl_sync(0xffffffffu, sp, m);
-        if (lane < r) {
-            a0 += __ldg(T + lane * r + m) * v;
-            a1 += __ldg(T + r * r + lane * r + m) * v;
+        const A t0 = __ldg(T + lane * r + m), t1 = __ldg(T + r * r + lane * r + m);
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq) {
+            const A v = ps[qq * HM_RMAX + m];
+            a0[qq] += t0 * v;
+            a1[qq] += t1 * v;
         }
     }
-    if (lane < r) {
-        s[((int64_t)X.c0 * k + q) * r + lane] += a0;
-        s[((int64_t)X.c1 * k + q) * r + lane] += a1;
+#pragma unroll
+    for (int qq = 0; qq < QC; ++qq) {
+        if (qq < qc) {
+            s[((int64_t)X.c0 * k + q0 + qq) * r + lane] += a0[qq];
+            s[((int64_t)X.c1 * k + q0 + qq) * r + lane] += a1[qq];
+        }
     }
 }
 
@@ -406,6 +435,27 @@ struct KTile;
 template <> struct KTile<float> { static constexpr int RB = 4, QB = 4, RG = 16, QG = 8; };   // 64 rows x 32 rhs
 template <> struct KTile<double> { static constexpr int RB = 2, QB = 4, RG = 32, QG = 4; };  // 64 rows x 16 rhs
 
+// n consecutive shared-memory values (16-byte aligned) converted to A.
+template <typename S, typename A, int n>
+__device__ __forceinline__ void load_vec(const S *p, A *out)
+{
+    if (sizeof(S) * n == 16) {
+        if (sizeof(S) == 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(p);
+            out[0] = (A)v.x; out[1] = (A)v.y; out[2] = (A)v.z; out[3] = (A)v.w;
+        } else {
+            const double2 v = *reinterpret_cast<const double2 *>(p);
+            out[0] = (A)v.x; out[1] = (A)v.y;
+        }
+    } else if (sizeof(S) * n == 32 && sizeof(S) == 8) {
+        const double2 v0 = *reinterpret_cast<const double2 *>(p), v1 = *reinterpret_cast<const double2 *>(p + 2);
+        out[0] = (A)v0.x; out[1] = (A)v0.y; out[2] = (A)v1.x; out[3] = (A)v1.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < n; ++i) out[i] = (A)p[i];
+    }
+}
+
 template <typename A>
 __device__ __forceinline__ void comp_add(A &hi, A &lo, A v)
 {
@@ -424,7 +474,7 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const hm_seg G = segs[blockIdx.x];
     S *Ps = reinterpret_cast<S *>(smem_raw);                              // ld x width
-    A *Gs = reinterpret_cast<A *>(smem_raw + (((size_t)64 * maxw * sizeof(S) + 15) / 16) * 16);  // width x QC
+    A *Gs = reinterpret_cast<A *>(smem_raw + (((size_t)64 * maxw * sizeof(S) + 31) / 32) * 32);  // width x QC
     {
         const int64_t n16 = (int64_t)G.ld * G.width * sizeof(S) / 16;
         const float4 *src = reinterpret_cast<const float4 *>(P + G.poff);
@@ -468,10 +518,8 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                     for (int j = 0; j < QB; ++j) part[i][j] = 0;
                 for (; c < cend; ++c) {
                     A pv[RB], gv[QB];
-#pragma unroll
-                    for (int i = 0; i < RB; ++i) pv[i] = (A)Ps[(int64_t)c * G.ld + rg * RB + i];
-#pragma unroll
-                    for (int j = 0; j < QB; ++j) gv[j] = Gs[c * QC + qg * QB + j];
+                    load_vec<S, A, RB>(Ps + (int64_t)c * G.ld + rg * RB, pv);
+                    load_vec<A, A, QB>(Gs + c * QC + qg * QB, gv);
 #pragma unroll
                     for (int i = 0; i < RB; ++i)
 #pragma unroll
@@ -501,21 +549,24 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
 }
 
 #define HM_INST_MV(S, A)                                                                             \
-    template __global__ void leaf_up<S, A>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);      \
-    template __global__ void m2l<S, A>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,       \
-                                       const A *, A *, int, int);                                       \
+    template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
+    template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
+    template __global__ void m2l<S, A, 1>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,    \
+                                          const A *, A *, int, int);                                    \
+    template __global__ void m2l<S, A, 8>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,    \
+                                          const A *, A *, int, int);                                    \
     template __global__ void expand_part<S, A, false>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
                                                       const S *, const A *, int, int);                  \
     template __global__ void expand_part<S, A, true>(MulArgs<S>, const hm_seg *, int, const hm_piece *,   \
                                                      const S *, const A *, int, int);                   \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
-                                            const A *, int, int);
+                                            const A *, int, int);                                       \
+    template __global__ void xfer_up<A, 1>(const hm_xfer *, int, const A *, A *, int, int);             \
+    template __global__ void xfer_up<A, 8>(const hm_xfer *, int, const A *, A *, int, int);             \
+    template __global__ void xfer_down<A, 1>(const hm_xfer *, int, const A *, A *, int, int);           \
+    template __global__ void xfer_down<A, 8>(const hm_xfer *, int, const A *, A *, int, int);
 HM_INST_MV(double, double)
 HM_INST_MV(float, float)
-template __global__ void xfer_up<double>(const hm_xfer *, int, const double *, double *, int, int);
-template __global__ void xfer_up<float>(const hm_xfer *, int, const float *, float *, int, int);
-template __global__ void xfer_down<double>(const hm_xfer *, int, const double *, double *, int, int);
-template __global__ void xfer_down<float>(const hm_xfer *, int, const float *, float *, int, int);
 
 // ============================================================== direct sums
 

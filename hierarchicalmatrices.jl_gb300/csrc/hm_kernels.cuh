@@ -80,6 +80,14 @@ struct Acc<float> {
     }
 };
 
+template <typename A>
+struct PlainAcc {   // plain FMA accumulation (multi-RHS paths)
+    A s;
+    __device__ __forceinline__ void zero() { s = 0; }
+    __device__ __forceinline__ void add(A p, A g) { s = fma(p, g, s); }
+    __device__ __forceinline__ A value() const { return s; }
+};
+
 struct FillArgs {
     const double *x, *y;     // device copies of the points
     const double *cheb, *lam;
@@ -109,17 +117,17 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
 
 // ---------------------------------------------------------------- matvec
 
-template <typename S, typename A>
+template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
 
-template <typename A>
+template <typename A, int QC>
 __global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k);
 
-template <typename S, typename A>
+template <typename S, typename A, int QC>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
                     const A *t, A *s, int r, int k);
 
-template <typename A>
+template <typename A, int QC>
 __global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k);
 
 template <typename S, typename A, bool FAR>

@@ -25,6 +25,7 @@ HM_ERR_DEGENERATE = 9
 
 HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
 HM_F64, HM_F32 = 0, 1
+HM_OPT_OVERLAP = 1
 
 # Records of csrc/hm_types.h.
 VPANEL = np.dtype([("row0", "<i8"), ("off", "<i8"), ("nrows", "<i4"), ("ld", "<i4"),
@@ -56,7 +57,7 @@ STAGES = ("up", "down", "expand", "far")
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
     "hm_kernelmatrix_build", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
-    "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
+    "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free",
 )
 
@@ -108,6 +109,8 @@ def _load():
     L.hm_mul_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp]
     L.hm_direct_rows.restype = ctypes.c_int
     L.hm_direct_rows.argtypes = [_vp, _vp, _vp, _i64, _vp, _vp]
+    L.hm_configure.restype = ctypes.c_int
+    L.hm_configure.argtypes = [_vp, ctypes.c_int, _i64]
     L.hm_profile.restype = ctypes.c_int
     L.hm_profile.argtypes = [_vp, ctypes.c_int]
     L.hm_profile_read.restype = ctypes.c_int

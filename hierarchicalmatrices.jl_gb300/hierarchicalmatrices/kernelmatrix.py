@@ -228,6 +228,11 @@ class KernelMatrix:
                                  out.data_ptr(), _stream_ptr(stream)))
         return out
 
+    def set_overlap(self, enable=True):
+        """Run the tree passes on a side stream concurrently with the
+        near-field panels (default), or every stage in order."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_OVERLAP, 1 if enable else 0))
+
     def profile(self, stages=_lib.STAGES):
         """Record CUDA events around the launches of the named matvec stages
         (see stage_times); an empty list turns timing off."""

@@ -111,6 +111,12 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate);
 int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t nrows, double *out,
                    void *stream);
 
+/* Handle options.  HM_OPT_OVERLAP (default 1): run the tree passes of hm_mul
+   on a side stream concurrently with the near-field panels; 0 runs every
+   stage in order on the caller's stream. */
+enum { HM_OPT_OVERLAP = 1 };
+int hm_configure(hm_handle *h, int option, int64_t value);
+
 /* Allocation-free single right-hand-side product (no counterpart in the
    reference).  For callers that cannot let a library allocate device memory
    during a product: processes whose GPU memory is reserved up front by
