@@ -324,6 +324,16 @@ constexpr int kWarpsPerCta = 4;
 
 inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
 
+// Raises the dynamic shared-memory limit of `kernel` when `bytes` needs it.
+template <typename K>
+int ensure_smem(K kernel, size_t bytes)
+{
+    if (bytes <= 48 * 1024) return HM_OK;
+    if (bytes > 227 * 1024) { set_error("kernel needs %zu bytes of shared memory", bytes); return HM_ERR_UNSUPPORTED; }
+    HM_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return HM_OK;
+}
+
 // Tree passes on stream st: leaf bases, upward transfers level by level, far
 // field, downward transfers level by level.  QC right-hand sides per warp.
 template <typename S, typename A, int QC>
@@ -336,6 +346,7 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
             const size_t smem = (size_t)kWarpsPerCta * 64 * (r + QC) * sizeof(S);
+            HM_TRY(ensure_smem(leaf_up<S, A, QC>, smem));
             leaf_up<S, A, QC><<<warp_ctas(h->n_vp * nq), 32 * kWarpsPerCta, smem, st>>>(
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
@@ -351,6 +362,7 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
             const size_t smem = (size_t)kWarpsPerCta * h->fstride * sizeof(S);
+            HM_TRY(ensure_smem(m2l<S, A, QC>, smem));
             m2l<S, A, QC><<<warp_ctas((int64_t)h->n_m2l_rows * nq), 32 * kWarpsPerCta, smem, st>>>(
                 h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
             HM_CK_LAUNCH("m2l");
