@@ -131,8 +131,12 @@ struct hm_handle {
     hm_m2l_ent *d_m2l_ents = nullptr;
     hm_xfer *d_down = nullptr;
     std::vector<int> down_ptr;
-    int32_t *d_yparent = nullptr, *d_xparent = nullptr;
-    int n_up = 0, fstride = 0;
+    // banded transfers
+    hm_xfer *d_up_ents = nullptr, *d_down_ents = nullptr;
+    hm_step *d_up_steps = nullptr, *d_down_steps = nullptr;
+    hm_task *d_up_tasks = nullptr, *d_down_tasks = nullptr;
+    std::vector<int> up_band_ptr, down_band_ptr;
+    int fstride = 0;
     hm_seg *d_segs = nullptr;
     int n_segs = 0;
     hm_piece *d_pieces = nullptr;
@@ -226,9 +230,14 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     HM_TRY(h->upload(&ff, P.f_fill, st));
     HM_TRY(h->upload(&h->d_down, P.down, st));
     h->down_ptr = P.down_level_ptr;
-    HM_TRY(h->upload(&h->d_yparent, P.y_up_parent, st));
-    HM_TRY(h->upload(&h->d_xparent, P.x_parent, st));
-    h->n_up = (int)P.up.size();
+    HM_TRY(h->upload(&h->d_up_ents, P.up_ents, st));
+    HM_TRY(h->upload(&h->d_up_steps, P.up_steps, st));
+    HM_TRY(h->upload(&h->d_up_tasks, P.up_tasks, st));
+    HM_TRY(h->upload(&h->d_down_ents, P.down_ents, st));
+    HM_TRY(h->upload(&h->d_down_steps, P.down_steps, st));
+    HM_TRY(h->upload(&h->d_down_tasks, P.down_tasks, st));
+    h->up_band_ptr = P.up_band_ptr;
+    h->down_band_ptr = P.down_band_ptr;
     h->fstride = P.fstride;
     HM_TRY(h->upload(&h->d_segs, P.segs, st));
     h->n_segs = (int)P.segs.size();
@@ -351,11 +360,13 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
         }
-        const size_t xsm = (size_t)(kWarpCta / 32) * 2 * QC * HM_RMAX * sizeof(A);
-        for (size_t l = 0; l + 1 < h->up_ptr.size(); ++l) {
-            const int b = h->up_ptr[l], n = h->up_ptr[l + 1] - b;
-            xfer_up<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, xsm, st>>>(h->d_up + b, n, T, t, r, k);
-            HM_CK_LAUNCH("xfer_up");
+        const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * 2 * QC * HM_RMAX) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_up_band<A, QC>, xsm));
+        for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
+            const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
+            if (!n) continue;
+            xfer_up_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, r, k);
+            HM_CK_LAUNCH("xfer_up_band");
         }
     }
     {
@@ -367,11 +378,14 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
             HM_CK_LAUNCH("m2l");
         }
-        const size_t xsm = (size_t)(kWarpCta / 32) * QC * HM_RMAX * sizeof(A);
-        for (size_t l = 0; l + 1 < h->down_ptr.size(); ++l) {
-            const int b = h->down_ptr[l], n = h->down_ptr[l + 1] - b;
-            xfer_down<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, xsm, st>>>(h->d_down + b, n, T, s, r, k);
-            HM_CK_LAUNCH("xfer_down");
+        const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * QC * HM_RMAX) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_down_band<A, QC>, xsm));
+        for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
+            const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
+            if (!n) continue;
+            xfer_down_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T,
+                                                            s, r, k);
+            HM_CK_LAUNCH("xfer_down_band");
         }
     }
     return HM_OK;
@@ -572,6 +586,14 @@ int hm_plan_table(const hm_plan *pl, int which, const void **data, int64_t *coun
     case 12: HM_TAB(pl->T)
     case 13: HM_TAB(pl->cheb)
     case 14: HM_TAB(pl->lam)
+    case 15: HM_TAB(P.up_ents)
+    case 16: HM_TAB(P.up_steps)
+    case 17: HM_TAB(P.up_tasks)
+    case 18: HM_TAB(P.up_band_ptr)
+    case 19: HM_TAB(P.down_ents)
+    case 20: HM_TAB(P.down_steps)
+    case 21: HM_TAB(P.down_tasks)
+    case 22: HM_TAB(P.down_band_ptr)
     default: return HM_ERR_INVALID_ARG;
     }
 #undef HM_TAB
@@ -663,8 +685,12 @@ int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double 
     st = (storage == HM_F64) ? build_device<double>(h, P, cheb, lam, T, x, y, cs)
                              : build_device<float>(h, P, cheb, lam, T, x, y, cs);
     hm_plan_free(pl);
-    h->launches_per_mul = (h->n_vp > 0) + (int)std::max<size_t>(h->up_ptr.size(), 1) - 1 + (h->n_m2l_rows > 0) +
-                          (int)std::max<size_t>(h->down_ptr.size(), 1) - 1 +
+    auto nonempty = [](const std::vector<int> &ptr) {
+        int c = 0;
+        for (size_t i = 0; i + 1 < ptr.size(); ++i) c += ptr[i + 1] > ptr[i];
+        return c;
+    };
+    h->launches_per_mul = (h->n_vp > 0) + nonempty(h->up_band_ptr) + (h->n_m2l_rows > 0) + nonempty(h->down_band_ptr) +
                           (h->n_segs > 0) * (1 + ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
     if (st) { hm_free(h); return st; }
     *out = h;

@@ -189,40 +189,53 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
     }
 }
 
-// Upward transfer of one level: t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m'].
-// One warp per (parent, chunk of QC right-hand sides); the children's
-// coefficients are staged in shared memory and read as broadcasts.  T holds
-// T_0 then T_1, each r x r with T_c[m' * r + m].
+// Upward transfers of one band: t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m'].
+// One CTA per task (a subtree cut to the band's levels); the task's steps
+// (levels, deepest first) run in order with a CTA barrier between them, warps
+// taking (record, chunk of QC right-hand sides) pairs.  T (T_0 then T_1, each
+// r x r with T_c[m' * r + m]) and the children's coefficients are staged in
+// shared memory.
 template <typename A, int QC>
-__global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k)
+__global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
+                             int r, int k)
 {
     extern __shared__ unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31;
+    A *Ts = reinterpret_cast<A *>(smem_raw);
+    A *cs = Ts + 2 * HM_RMAX * HM_RMAX + (threadIdx.x >> 5) * 2 * QC * HM_RMAX;   // [c][qq][m']
+    for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) Ts[i] = T[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int nq = (k + QC - 1) / QC;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= (int64_t)nx * nq) return;
-    A *cs = reinterpret_cast<A *>(smem_raw) + (threadIdx.x >> 5) * 2 * QC * HM_RMAX;   // [c][qq][m']
-    const hm_xfer X = xf[w / nq];
-    const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
-    for (int i = lane; i < QC * r; i += 32) {
-        const int qq = i / r, m = i % r;
-        cs[qq * HM_RMAX + m] = qq < qc ? t[((int64_t)X.c0 * k + q0 + qq) * r + m] : (A)0;
-        cs[(QC + qq) * HM_RMAX + m] = qq < qc ? t[((int64_t)X.c1 * k + q0 + qq) * r + m] : (A)0;
+    const hm_task tk = tasks[blockIdx.x];
+    for (int st = tk.step0; st < tk.step1; ++st) {
+        const hm_step S = steps[st];
+        for (int64_t w = threadIdx.x >> 5; w < (int64_t)(S.e1 - S.e0) * nq; w += nw) {
+            const hm_xfer X = ents[S.e0 + w / nq];
+            const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+            for (int i = lane; i < QC * r; i += 32) {
+                const int qq = i / r, m = i % r;
+                cs[qq * HM_RMAX + m] = qq < qc ? t[((int64_t)X.c0 * k + q0 + qq) * r + m] : (A)0;
+                cs[(QC + qq) * HM_RMAX + m] = qq < qc ? t[((int64_t)X.c1 * k + q0 + qq) * r + m] : (A)0;
+            }
+            __syncwarp();
+            if (lane < r) {
+                A acc[QC];
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
+                for (int mp = 0; mp < r; ++mp) {
+                    const A a0 = Ts[mp * r + lane], a1 = Ts[r * r + mp * r + lane];
+#pragma unroll
+                    for (int qq = 0; qq < QC; ++qq)
+                        acc[qq] += a0 * cs[qq * HM_RMAX + mp] + a1 * cs[(QC + qq) * HM_RMAX + mp];
+                }
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq)
+                    if (qq < qc) t[((int64_t)X.slot * k + q0 + qq) * r + lane] = acc[qq];
+            }
+            __syncwarp();
+        }
+        __syncthreads();
     }
-    __syncwarp();
-    if (lane >= r) return;
-    A acc[QC];
-#pragma unroll
-    for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
-    for (int mp = 0; mp < r; ++mp) {
-        const A a0 = __ldg(T + mp * r + lane), a1 = __ldg(T + r * r + mp * r + lane);
-#pragma unroll
-        for (int qq = 0; qq < QC; ++qq)
-            acc[qq] += a0 * cs[qq * HM_RMAX + mp] + a1 * cs[(QC + qq) * HM_RMAX + mp];
-    }
-#pragma unroll
-    for (int qq = 0; qq < QC; ++qq)
-        if (qq < qc) t[((int64_t)X.slot * k + q0 + qq) * r + lane] = acc[qq];
 }
 
 // Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
@@ -271,42 +284,54 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
     }
 }
 
-// Downward transfer of one level: s[child_c][m'] += sum_m T_c[m', m] s[parent][m].
+// Downward transfers of one band: s[child_c][m'] += sum_m T_c[m', m] s[parent][m].
+// Same task/step structure as xfer_up_band, topmost level first.
 template <typename A, int QC>
-__global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k)
+__global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
+                               int r, int k)
 {
     extern __shared__ unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31;
+    A *Ts = reinterpret_cast<A *>(smem_raw);
+    A *ps = Ts + 2 * HM_RMAX * HM_RMAX + (threadIdx.x >> 5) * QC * HM_RMAX;   // [qq][m]
+    for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) Ts[i] = T[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int nq = (k + QC - 1) / QC;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= (int64_t)nx * nq) return;
-    A *ps = reinterpret_cast<A *>(smem_raw) + (threadIdx.x >> 5) * QC * HM_RMAX;   // [qq][m]
-    const hm_xfer X = xf[w / nq];
-    const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
-    for (int i = lane; i < QC * r; i += 32) {
-        const int qq = i / r, m = i % r;
-        ps[qq * HM_RMAX + m] = qq < qc ? s[((int64_t)X.slot * k + q0 + qq) * r + m] : (A)0;
-    }
-    __syncwarp();
-    if (lane >= r) return;
-    A a0[QC], a1[QC];
+    const hm_task tk = tasks[blockIdx.x];
+    for (int st = tk.step0; st < tk.step1; ++st) {
+        const hm_step S = steps[st];
+        for (int64_t w = threadIdx.x >> 5; w < (int64_t)(S.e1 - S.e0) * nq; w += nw) {
+            const hm_xfer X = ents[S.e0 + w / nq];
+            const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+            for (int i = lane; i < QC * r; i += 32) {
+                const int qq = i / r, m = i % r;
+                ps[qq * HM_RMAX + m] = qq < qc ? s[((int64_t)X.slot * k + q0 + qq) * r + m] : (A)0;
+            }
+            __syncwarp();
+            if (lane < r) {
+                A a0[QC], a1[QC];
 #pragma unroll
-    for (int qq = 0; qq < QC; ++qq) { a0[qq] = 0; a1[qq] = 0; }
-    for (int m = 0; m < r; ++m) {
-        const A t0 = __ldg(T + lane * r + m), t1 = __ldg(T + r * r + lane * r + m);
+                for (int qq = 0; qq < QC; ++qq) { a0[qq] = 0; a1[qq] = 0; }
+                for (int m = 0; m < r; ++m) {
+                    const A t0 = Ts[lane * r + m], t1 = Ts[r * r + lane * r + m];
 #pragma unroll
-        for (int qq = 0; qq < QC; ++qq) {
-            const A v = ps[qq * HM_RMAX + m];
-            a0[qq] += t0 * v;
-            a1[qq] += t1 * v;
+                    for (int qq = 0; qq < QC; ++qq) {
+                        const A v = ps[qq * HM_RMAX + m];
+                        a0[qq] += t0 * v;
+                        a1[qq] += t1 * v;
+                    }
+                }
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) {
+                    if (qq < qc) {
+                        s[((int64_t)X.c0 * k + q0 + qq) * r + lane] += a0[qq];
+                        s[((int64_t)X.c1 * k + q0 + qq) * r + lane] += a1[qq];
+                    }
+                }
+            }
+            __syncwarp();
         }
-    }
-#pragma unroll
-    for (int qq = 0; qq < QC; ++qq) {
-        if (qq < qc) {
-            s[((int64_t)X.c0 * k + q0 + qq) * r + lane] += a0[qq];
-            s[((int64_t)X.c1 * k + q0 + qq) * r + lane] += a1[qq];
-        }
+        __syncthreads();
     }
 }
 
@@ -561,10 +586,14 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                                      const S *, const A *, int, int);                   \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
                                             const A *, int, int);                                       \
-    template __global__ void xfer_up<A, 1>(const hm_xfer *, int, const A *, A *, int, int);             \
-    template __global__ void xfer_up<A, 8>(const hm_xfer *, int, const A *, A *, int, int);             \
-    template __global__ void xfer_down<A, 1>(const hm_xfer *, int, const A *, A *, int, int);           \
-    template __global__ void xfer_down<A, 8>(const hm_xfer *, int, const A *, A *, int, int);
+    template __global__ void xfer_up_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
+                                                A *, int, int);                                         \
+    template __global__ void xfer_up_band<A, 8>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
+                                                A *, int, int);                                         \
+    template __global__ void xfer_down_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *,        \
+                                                  const A *, A *, int, int);                            \
+    template __global__ void xfer_down_band<A, 8>(const hm_task *, const hm_step *, const hm_xfer *,        \
+                                                  const A *, A *, int, int);
 HM_INST_MV(double, double)
 HM_INST_MV(float, float)
 

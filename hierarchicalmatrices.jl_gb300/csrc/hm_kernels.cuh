@@ -121,14 +121,16 @@ template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
 
 template <typename A, int QC>
-__global__ void xfer_up(const hm_xfer *xf, int nx, const A *T, A *t, int r, int k);
+__global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
+                             int r, int k);
 
 template <typename S, typename A, int QC>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
                     const A *t, A *s, int r, int k);
 
 template <typename A, int QC>
-__global__ void xfer_down(const hm_xfer *xf, int nx, const A *T, A *s, int r, int k);
+__global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
+                               int r, int k);
 
 template <typename S, typename A, bool FAR>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,

@@ -170,6 +170,56 @@ void transfer_steps(const Tree &T, bool deepest_first, std::vector<hm_xfer> &out
 
 inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
+// Groups the internal basis nodes into bands of kBandLevels levels (counted
+// from the deepest internal level).  Within a band, a task is the set of
+// nodes sharing the same topmost in-band ancestor; its steps are its levels,
+// deepest first for the upward pass, topmost first for the downward pass.
+void band_transfers(const Tree &T, bool upward, std::vector<hm_xfer> &ents, std::vector<hm_step> &steps,
+                    std::vector<hm_task> &tasks, std::vector<int> &band_ptr)
+{
+    ents.clear(); steps.clear(); tasks.clear(); band_ptr.clear();
+    int maxlev = -1;
+    for (const Node &n : T.nodes) if (n.kind == 1) maxlev = std::max(maxlev, n.level);
+    band_ptr.push_back(0);
+    if (maxlev < 0) return;
+    const int nbands = maxlev / kBandLevels + 1;
+    auto band_of = [&](int level) { return (maxlev - level) / kBandLevels; };
+    // task root of every internal node: climb while the parent is internal and in the same band
+    std::vector<std::vector<std::pair<int, int>>> members(nbands);   // (root id, node id)
+    for (size_t i = 0; i < T.nodes.size(); ++i) {
+        if (T.nodes[i].kind != 1) continue;
+        int root = (int)i;
+        const int b = band_of(T.nodes[i].level);
+        while (T.nodes[root].parent >= 0 && T.nodes[T.nodes[root].parent].kind == 1 &&
+               band_of(T.nodes[T.nodes[root].parent].level) == b)
+            root = T.nodes[root].parent;
+        members[b].push_back({root, (int)i});
+    }
+    for (int k = 0; k < nbands; ++k) {
+        const int b = upward ? k : nbands - 1 - k;
+        auto &mem = members[b];
+        std::sort(mem.begin(), mem.end(), [&](const std::pair<int, int> &p, const std::pair<int, int> &q) {
+            if (p.first != q.first) return T.nodes[p.first].slot < T.nodes[q.first].slot;
+            const int lp = T.nodes[p.second].level, lq = T.nodes[q.second].level;
+            if (lp != lq) return upward ? lp > lq : lp < lq;
+            return T.nodes[p.second].slot < T.nodes[q.second].slot;
+        });
+        for (size_t i = 0; i < mem.size(); ++i) {
+            const Node &n = T.nodes[mem[i].second];
+            const bool new_task = i == 0 || mem[i].first != mem[i - 1].first;
+            const bool new_step = new_task || n.level != T.nodes[mem[i - 1].second].level;
+            if (new_task) tasks.push_back({(int32_t)steps.size(), (int32_t)steps.size()});
+            if (new_step) {
+                steps.push_back({(int32_t)ents.size(), (int32_t)ents.size()});
+                tasks.back().step1 = (int32_t)steps.size();
+            }
+            ents.push_back({n.slot, T.nodes[n.child[0]].slot, T.nodes[n.child[1]].slot, 0});
+            steps.back().e1 = (int32_t)ents.size();
+        }
+        band_ptr.push_back((int)tasks.size());
+    }
+}
+
 }  // namespace
 
 int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b,
@@ -217,17 +267,8 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
         P.vstore_elems = off;
     }
 
-    // Parent links for the single-launch upward and downward passes.
-    P.y_up_parent.assign(P.n_yslots, -1);
-    for (size_t i = 0; i < P.up.size(); ++i) {
-        P.y_up_parent[P.up[i].c0] = (int32_t)i;
-        P.y_up_parent[P.up[i].c1] = (int32_t)i;
-    }
-    P.x_parent.assign(P.n_xslots, -1);
-    for (const hm_xfer &e : P.down) {
-        P.x_parent[e.c0] = 2 * e.slot;
-        P.x_parent[e.c1] = 2 * e.slot + 1;
-    }
+    band_transfers(P.Y, true, P.up_ents, P.up_steps, P.up_tasks, P.up_band_ptr);
+    band_transfers(P.X, false, P.down_ents, P.down_steps, P.down_tasks, P.down_band_ptr);
 
     // M2L rows: barycentric blocks grouped by row cluster.
     P.fstride = (int)round_up((int64_t)r * r, 4);

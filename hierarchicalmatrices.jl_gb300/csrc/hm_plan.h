@@ -66,8 +66,11 @@ struct Plan {
     std::vector<hm_fill_f> f_fill;
     int64_t fstore_elems = 0;
     int fstride = 0;                          // elements between F blocks (r*r rounded to 4)
-    std::vector<int32_t> y_up_parent;         // per column slot: index of its parent's upward step, -1 at a root
-    std::vector<int32_t> x_parent;            // per row slot: 2*parent slot + child index, -1 at a root
+    // banded transfers (records ordered band by band, task by task, step by step)
+    std::vector<hm_xfer> up_ents, down_ents;
+    std::vector<hm_step> up_steps, down_steps;
+    std::vector<hm_task> up_tasks, down_tasks;
+    std::vector<int> up_band_ptr, down_band_ptr;   // task ranges per band, in launch order
     std::vector<hm_xfer> down;                // x tree, top level first
     std::vector<int> down_level_ptr;
     std::vector<hm_seg> segs;
@@ -83,5 +86,7 @@ struct Plan {
 // leaf = BLOCKSIZE, r = rank, seg_rows = maximum rows per row segment.
 int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b,
                double c, double d, int r, int64_t leaf, int seg_rows, Plan &out);
+
+constexpr int kBandLevels = 4;   // tree levels per transfer band
 
 }  // namespace hm

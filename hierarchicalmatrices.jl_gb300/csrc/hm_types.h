@@ -31,6 +31,13 @@ struct hm_xfer {        // coefficient transfer between a node and its two child
     int32_t slot, c0, c1, pad;
 };
 
+// Transfer bands: the upward (downward) transfers are grouped into bands of a
+// few tree levels; a band is one launch, each of its tasks (a subtree cut to
+// the band's levels) one CTA, which walks the task's steps (one level each)
+// in order with a CTA barrier between steps.
+struct hm_task { int32_t step0, step1; };     // range of steps
+struct hm_step { int32_t e0, e1; };           // range of transfer records
+
 struct hm_m2l_row {     // s[slot] = sum_{e in [begin,end)} F_e t[yslot_e]
     int32_t slot, begin, end, pad;
 };

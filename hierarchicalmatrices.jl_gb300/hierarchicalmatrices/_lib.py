@@ -31,6 +31,8 @@ HM_OPT_OVERLAP = 1
 VPANEL = np.dtype([("row0", "<i8"), ("off", "<i8"), ("nrows", "<i4"), ("ld", "<i4"),
                    ("width", "<i4"), ("slot", "<i4")])
 XFER = np.dtype([("slot", "<i4"), ("c0", "<i4"), ("c1", "<i4"), ("pad", "<i4")])
+STEP = np.dtype([("e0", "<i4"), ("e1", "<i4")])
+TASK = np.dtype([("step0", "<i4"), ("step1", "<i4")])
 M2L_ROW = np.dtype([("slot", "<i4"), ("begin", "<i4"), ("end", "<i4"), ("pad", "<i4")])
 M2L_ENT = np.dtype([("foff", "<i8"), ("yslot", "<i4"), ("pad", "<i4")])
 SEG = np.dtype([("row0", "<i8"), ("poff", "<i8"), ("nrows", "<i4"), ("ld", "<i4"), ("width", "<i4"),
@@ -45,6 +47,9 @@ PLAN_TABLES = {
     "f_fill": (6, FILL_F), "down": (7, XFER), "down_level_ptr": (8, np.dtype("<i4")),
     "segs": (9, SEG), "pieces": (10, PIECE), "seg_fill": (11, FILL_SEG),
     "T": (12, np.dtype("<f8")), "cheb": (13, np.dtype("<f8")), "lam": (14, np.dtype("<f8")),
+    "up_ents": (15, XFER), "up_steps": (16, STEP), "up_tasks": (17, TASK),
+    "up_band_ptr": (18, np.dtype("<i4")), "down_ents": (19, XFER), "down_steps": (20, STEP),
+    "down_tasks": (21, TASK), "down_band_ptr": (22, np.dtype("<i4")),
 }
 PLAN_SIZES = ("r", "nx", "ny", "n_xslots", "n_yslots", "vstore", "fstore", "pstore", "max_width",
               "n_bary", "n_dense", "depth", "canonical_values", "reference_values", "stored_values",

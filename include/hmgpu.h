@@ -160,7 +160,9 @@ int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, dou
 /* Table `which` (0 vpanels, 1 vpanel boxes, 2 upward steps, 3 upward level
    offsets, 4 far-field rows, 5 far-field entries, 6 F boxes, 7 downward steps,
    8 downward level offsets, 9 row segments, 10 pieces, 11 segment fill info,
-   12 transfer matrices, 13 Chebyshev nodes, 14 barycentric weights):
+   12 transfer matrices, 13 Chebyshev nodes, 14 barycentric weights,
+   15-18 upward band records / steps / tasks / band offsets, 19-22 the same
+   for the downward bands):
    pointer, element count and element size (records of hm_types.h). */
 int hm_plan_table(const hm_plan *p, int which, const void **data, int64_t *count, int64_t *elem_bytes);
 /* r, nx, ny, row slots, column slots, V/F/panel store elements, max panel

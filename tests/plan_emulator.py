@@ -30,6 +30,19 @@ def basis(pts, a, b, cheb, lam):
     return w / w.sum(axis=1, keepdims=True)
 
 
+def _banded(plan, which):
+    """Transfer records in launch order: band by band, task by task, step by step."""
+    ents = plan.table(f"{which}_ents")
+    steps = plan.table(f"{which}_steps")
+    tasks = plan.table(f"{which}_tasks")
+    bptr = plan.table(f"{which}_band_ptr")
+    assert len(ents) == len(plan.table(which))
+    for bd in range(len(bptr) - 1):
+        for tk in tasks[bptr[bd]:bptr[bd + 1]]:
+            for st in steps[tk["step0"]:tk["step1"]]:
+                yield from ents[st["e0"]:st["e1"]]
+
+
 def emulate(plan, kernel, b):
     """Returns H @ b (b: (ny,) or (ny, k)) computed from the plan tables."""
     S = plan.sizes
@@ -48,11 +61,14 @@ def emulate(plan, kernel, b):
         rows = slice(vp["row0"], vp["row0"] + vp["nrows"])
         V = basis(y[rows], vf["a"], vf["b"], cheb, lam)
         t[vp["slot"]] = V.T @ B[rows]
-    # upward transfers, level by level
-    up, ptr = plan.table("up"), plan.table("up_level_ptr")
-    for l in range(len(ptr) - 1):
-        for e in up[ptr[l]:ptr[l + 1]]:
-            t[e["slot"]] = T[0].T @ t[e["c0"]] + T[1].T @ t[e["c1"]]
+    # upward transfers in band / task / step order (as the GPU runs them);
+    # `done` checks that every child is final before its parent reads it
+    done = np.zeros(S["n_yslots"], dtype=bool)
+    done[[vp["slot"] for vp in plan.table("vpanels")]] = True
+    for e in _banded(plan, "up"):
+        assert done[e["c0"]] and done[e["c1"]] and not done[e["slot"]]
+        t[e["slot"]] = T[0].T @ t[e["c0"]] + T[1].T @ t[e["c1"]]
+        done[e["slot"]] = True
     # far field
     ents, ff = plan.table("m2l_ents"), plan.table("f_fill")
     for row in plan.table("m2l_rows"):
@@ -63,12 +79,17 @@ def emulate(plan, kernel, b):
                           box_nodes(f["ya"], f["yb"], cheb)[None, :])
             acc += F @ t[ents[e]["yslot"]]
         s[row["slot"]] = acc
-    # downward transfers
-    down, ptr = plan.table("down"), plan.table("down_level_ptr")
-    for l in range(len(ptr) - 1):
-        for e in down[ptr[l]:ptr[l + 1]]:
-            s[e["c0"]] += T[0] @ s[e["slot"]]
-            s[e["c1"]] += T[1] @ s[e["slot"]]
+    # downward transfers in band / task / step order; a parent is final once
+    # its own parent has pushed into it
+    pushed = np.zeros(S["n_xslots"], dtype=bool)
+    has_parent = np.zeros(S["n_xslots"], dtype=bool)
+    for e in plan.table("down"):
+        has_parent[e["c0"]] = has_parent[e["c1"]] = True
+    for e in _banded(plan, "down"):
+        assert pushed[e["slot"]] or not has_parent[e["slot"]]
+        s[e["c0"]] += T[0] @ s[e["slot"]]
+        s[e["c1"]] += T[1] @ s[e["slot"]]
+        pushed[e["c0"]] = pushed[e["c1"]] = True
     # row segments
     out = np.zeros((S["nx"], k))
     covered = np.zeros(S["nx"], dtype=np.int64)
