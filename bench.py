@@ -211,6 +211,70 @@ def run_reference(args):
     return 0
 
 
+# ----------------------------------------------------------------- batching
+
+def batch_instances(count=512, lo=1024, hi=65536, seed=0):
+    """count instances, n_k log-uniform in [lo, hi], points uniform on [0,1],
+    sorted descending."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)
+    xs = [np.sort(rng.random(int(n)))[::-1].copy() for n in ns]
+    ys = [np.sort(rng.random(int(n)))[::-1].copy() for n in ns]
+    return xs, ys, [(1.0, 0.0, 1.0, 0.0)] * count
+
+
+def run_batch(hm, torch, dev, args, count=512, nrhs=8):
+    """512 independent Cauchy KernelMatrices, 8 FP32 right-hand sides each,
+    multiplied together by one captured CUDA graph; instances/s and the
+    per-batch latency distribution over the replays."""
+    xs, ys, boxes = batch_instances(count)
+    t0 = time.perf_counter()
+    Hb = hm.KernelMatrixBatch(hm.cauchykernel, xs, ys, boxes, dtype=np.float32)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    st = Hb.stats()
+    B = torch.randn(nrhs, Hb.shape[1], device=dev, dtype=torch.float32).t()
+    U = torch.empty(nrhs, Hb.shape[0], device=dev, dtype=torch.float32).t()
+    cs = torch.cuda.Stream()
+    cs.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(cs):
+        for _ in range(3):                      # warm-up: per-stream scratch, side stream
+            Hb.mul(U, B, accumulate=False)
+    cs.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=cs):
+        Hb.mul(U, B, accumulate=False, stream=cs)
+    reps = max(10, min(200, args.steps // 5))
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    cur = torch.cuda.current_stream()
+    for a, b in evs:
+        a.record(cur)
+        g.replay()
+        b.record(cur)
+    torch.cuda.synchronize()
+    lat = np.array([a.elapsed_time(b) for a, b in evs])
+    # error of the last instance's last column against exact dense rows
+    i = count - 1
+    r0, c0 = int(Hb.row_offsets[i]), int(Hb.col_offsets[i])
+    Hi = hm.KernelMatrix(hm.cauchykernel, xs[i], ys[i], *boxes[i])
+    rows = torch.arange(0, len(xs[i]), 7, device=dev)
+    ref = Hi.direct_rows(B[c0:c0 + len(ys[i]), nrhs - 1].double().contiguous(), rows)
+    got = U[r0:r0 + len(xs[i]), nrhs - 1].double()[rows]
+    err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+    return {
+        "workload": f"{count} Cauchy KernelMatrices, n log-uniform in [1024, 65536] (sum {Hb.shape[0]}), "
+                    f"uniform sorted points, {nrhs} FP32 RHS each, one captured CUDA graph per batch",
+        "instances_per_s": count / (lat.mean() * 1e-3), "matvec_per_s": count * nrhs / (lat.mean() * 1e-3),
+        "batch_ms_mean": float(lat.mean()), "batch_ms_p50": float(np.percentile(lat, 50)),
+        "batch_ms_p99": float(np.percentile(lat, 99)), "replays": reps, "build_s": build_s,
+        "stored_GB": st["stored_values"] * 4 / 1e9, "rel_err_vs_dense_fp64_sample": err,
+        "gpu_launches_per_batch": st["launches_per_mul"],
+    }
+
+
 # ----------------------------------------------------------------- GPU arm
 
 def main():
@@ -222,6 +286,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -333,6 +398,10 @@ def main():
             del B, U
             torch.cuda.empty_cache()
 
+    batch = None
+    if not args.no_variants and not args.no_batch:
+        batch = run_batch(hm, torch, dev, args)
+
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -373,6 +442,7 @@ def main():
             "tree": {k: st[k] for k in ("n_bary", "n_dense", "depth", "canonical_values",
                                         "reference_values", "stored_values", "device_bytes")},
             "variants": variants,
+            "batch": batch,
             "cpu_baseline": cb,
         }
         print(json.dumps(line), flush=True)

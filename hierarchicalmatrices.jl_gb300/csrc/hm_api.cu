@@ -6,7 +6,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <map>
+#include <thread>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -113,7 +115,15 @@ void transfer_matrices(int r, const std::vector<double> &x, const std::vector<do
 
 struct hm_handle {
     int kernel = 0, storage = HM_F64, r = 0;
+    int swap = 0;                  // 1: this handle holds the transpose of the kernel matrix
+    int ninst = 1;                 // instances of a batched (block-diagonal) handle
     int64_t nx = 0, ny = 0;
+    // host copies of the build inputs, for the lazily built transpose
+    std::vector<double> hx, hy;
+    double box[4] = {0, 0, 0, 0};
+    int64_t blocksize = 0;
+    hm_handle *trans = nullptr;    // H^T, built on the first hm_mul_t
+    std::mutex trans_mu;
     PlanStats stats;
     int n_xslots = 0, n_yslots = 0, max_width = 0;
     std::vector<void *> allocs;
@@ -254,6 +264,7 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
 
     FillArgs fa;
     fa.x = h->d_x; fa.y = h->d_y; fa.cheb = h->d_cheb; fa.lam = h->d_lam; fa.r = h->r; fa.kernel = h->kernel;
+    fa.swap = h->swap;
     if (h->n_vp) {
         fill_vpanels<S><<<h->n_vp, 128, 0, st>>>(fa, vp, vpf, h->n_vp, V);
         HM_CK_LAUNCH("fill_vpanels");
@@ -289,6 +300,27 @@ struct StageTimer {
         h->events.push_back({stage, a, b});
     }
 };
+
+// Raises the dynamic shared-memory limit of `kernel` when `bytes` needs it.
+// The limit set per kernel is remembered, so repeated products (and stream
+// capture after a first product) make no further attribute calls.
+std::mutex g_smem_mu;
+std::map<std::pair<int, const void *>, size_t> g_smem_set;
+
+template <typename K>
+int ensure_smem(K kernel, size_t bytes)
+{
+    if (bytes <= 48 * 1024) return HM_OK;
+    if (bytes > 227 * 1024) { set_error("kernel needs %zu bytes of shared memory", bytes); return HM_ERR_UNSUPPORTED; }
+    int dev = 0;
+    HM_CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    size_t &have = g_smem_set[{dev, reinterpret_cast<const void *>(kernel)}];
+    if (have >= bytes) return HM_OK;
+    HM_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    have = bytes;
+    return HM_OK;
+}
 
 // Per-call scratch: coefficients t (column slots) then s (row slots).
 struct ScratchLayout {
@@ -332,16 +364,6 @@ int stream_ctx(hm_handle *h, cudaStream_t st, size_t bytes, hm_handle::StreamCtx
 constexpr int kWarpsPerCta = 4;
 
 inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
-
-// Raises the dynamic shared-memory limit of `kernel` when `bytes` needs it.
-template <typename K>
-int ensure_smem(K kernel, size_t bytes)
-{
-    if (bytes <= 48 * 1024) return HM_OK;
-    if (bytes > 227 * 1024) { set_error("kernel needs %zu bytes of shared memory", bytes); return HM_ERR_UNSUPPORTED; }
-    HM_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    return HM_OK;
-}
 
 // Tree passes on stream st: leaf bases, upward transfers level by level, far
 // field, downward transfers level by level.  QC right-hand sides per warp.
@@ -402,10 +424,7 @@ template <typename S, typename A, bool FAR>
 int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
 {
     const size_t smem = (size_t)kWarpsPerCta * std::max(h->max_width, 1) * sizeof(A);
-    if (smem > 48 * 1024) {
-        if (smem > 227 * 1024) { set_error("panel width %d too large", h->max_width); return HM_ERR_UNSUPPORTED; }
-        HM_CK(cudaFuncSetAttribute(expand_part<S, A, FAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
+    HM_TRY(ensure_smem(expand_part<S, A, FAR>, smem));
     expand_part<S, A, FAR><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
         ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(h->d_P), s, h->r, std::max(h->max_width, 1));
     HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
@@ -418,9 +437,7 @@ int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t
     const int maxw = std::max(h->max_width, 1);
     const int qc = sizeof(A) == 8 ? 16 : 32;
     const size_t smem = ((size_t)64 * maxw * sizeof(S) + 31) / 32 * 32 + (size_t)maxw * qc * sizeof(A);
-    if (smem > 227 * 1024) { set_error("panel width %d too large for the multi-RHS kernel", maxw); return HM_ERR_UNSUPPORTED; }
-    if (smem > 48 * 1024)
-        HM_CK(cudaFuncSetAttribute(expand_k<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    HM_TRY(ensure_smem(expand_k<S, A>, smem));
     expand_k<S, A><<<h->n_segs, 128, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(h->d_P), s,
                                                   h->r, maxw);
     HM_CK_LAUNCH("expand_k");
@@ -565,6 +582,54 @@ int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, dou
     return HM_OK;
 }
 
+int hm_batch_plan_create(int ninst, const int64_t *nx, const int64_t *ny, const double *x, const double *y,
+                         const double *boxes, int rank, int64_t blocksize, hm_plan **out)
+{
+    if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
+    *out = nullptr;
+    if (ninst < 1 || !nx || !ny || !x || !y || !boxes) { set_error("hm_batch: bad arguments"); return HM_ERR_INVALID_ARG; }
+    std::vector<int64_t> xo(ninst + 1, 0), yo(ninst + 1, 0);
+    for (int i = 0; i < ninst; ++i) {
+        if (nx[i] < 1 || ny[i] < 1) { set_error("instance %d is empty", i); return HM_ERR_INVALID_ARG; }
+        xo[i + 1] = xo[i] + nx[i];
+        yo[i + 1] = yo[i] + ny[i];
+    }
+    if (xo[ninst] >= (int64_t)1 << 31 || yo[ninst] >= (int64_t)1 << 31) { set_error("more than 2^31 points"); return HM_ERR_UNSUPPORTED; }
+    std::vector<hm_plan *> parts(ninst, nullptr);
+    std::vector<int> status(ninst, HM_OK);
+    std::vector<std::string> errs(ninst);
+    const int nth = std::max(1, std::min<int>(ninst, (int)std::thread::hardware_concurrency()));
+    std::atomic<int> next(0);
+    auto work = [&]() {
+        for (int i = next++; i < ninst; i = next++) {
+            const double *bx = boxes + 4 * (size_t)i;
+            status[i] = hm_plan_create(x + xo[i], nx[i], y + yo[i], ny[i], bx[0], bx[1], bx[2], bx[3], rank, blocksize,
+                                       &parts[i]);
+            if (status[i]) errs[i] = g_last_error;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; ++t) pool.emplace_back(work);
+    work();
+    for (auto &th : pool) th.join();
+    int st = HM_OK;
+    for (int i = 0; i < ninst && !st; ++i)
+        if (status[i]) { st = status[i]; set_error("instance %d: %s", i, errs[i].c_str()); }
+    hm_plan *pl = nullptr;
+    if (!st) {
+        pl = new hm_plan();
+        std::vector<Plan> ps;
+        ps.reserve(ninst);
+        for (int i = 0; i < ninst; ++i) ps.push_back(std::move(parts[i]->P));
+        merge_plans(ps, pl->P);
+        pl->cheb = parts[0]->cheb; pl->lam = parts[0]->lam; pl->T = parts[0]->T;
+    }
+    for (hm_plan *p : parts) delete p;
+    if (st) return st;
+    *out = pl;
+    return HM_OK;
+}
+
 int hm_plan_table(const hm_plan *pl, int which, const void **data, int64_t *count, int64_t *elem_bytes)
 {
     if (!pl || !data || !count || !elem_bytes) return HM_ERR_INVALID_ARG;
@@ -661,11 +726,19 @@ int hm_indsplit(const double *x, int64_t n, int64_t start, int64_t len, double a
     return HM_OK;
 }
 
-int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double *y, int64_t ny,
-                          double a, double b, double c, double d, int rank, int64_t blocksize,
-                          int storage, void *stream, hm_handle **out)
+}  // extern "C"
+
+namespace {
+
+int build_from_plan(int kernel, int swap, hm_plan *pl, const double *x, const double *y, int storage, void *stream,
+                    hm_handle **out);
+
+// Builds the KernelMatrix of (x, y) -- or, with swap = 1, the matrix with
+// entries f(y_j, x_i), i.e. the transpose of the KernelMatrix of (y, x).
+int build_kernelmatrix(int kernel, int swap, const double *x, int64_t nx, const double *y, int64_t ny, double a,
+                       double b, double c, double d, int rank, int64_t blocksize, int storage, void *stream,
+                       hm_handle **out)
 {
-    g_last_error.clear();
     if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
     *out = nullptr;
     if (kernel < HM_KERNEL_CAUCHY || kernel > HM_KERNEL_LOG) { set_error("unknown kernel %d", kernel); return HM_ERR_UNSUPPORTED; }
@@ -673,12 +746,30 @@ int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double 
     hm_plan *pl = nullptr;
     int st = hm_plan_create(x, nx, y, ny, a, b, c, d, rank, blocksize, &pl);
     if (st) return st;
+    st = build_from_plan(kernel, swap, pl, x, y, storage, stream, out);
+    if (*out) {
+        hm_handle *h = *out;
+        h->hx.assign(x, x + nx);
+        h->hy.assign(y, y + ny);
+        h->box[0] = a; h->box[1] = b; h->box[2] = c; h->box[3] = d;
+        h->blocksize = blocksize ? blocksize : 4 * (int64_t)h->r;
+    }
+    return st;
+}
+
+// Uploads a plan and compresses on the GPU; frees the plan.
+int build_from_plan(int kernel, int swap, hm_plan *pl, const double *x, const double *y, int storage, void *stream,
+                    hm_handle **out)
+{
+    *out = nullptr;
+    int st = HM_OK;
     const Plan &P = pl->P;
-    rank = P.r;
+    const int64_t nx = P.nx, ny = P.ny;
+    const int rank = P.r;
     const std::vector<double> &cheb = pl->cheb, &lam = pl->lam, &T = pl->T;
 
     hm_handle *h = new hm_handle();
-    h->kernel = kernel; h->storage = storage; h->r = rank; h->nx = nx; h->ny = ny;
+    h->kernel = kernel; h->storage = storage; h->r = rank; h->nx = nx; h->ny = ny; h->swap = swap;
     h->stats = P.stats;
     h->n_xslots = P.n_xslots; h->n_yslots = P.n_yslots; h->max_width = P.max_width;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
@@ -695,6 +786,52 @@ int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double 
     if (st) { hm_free(h); return st; }
     *out = h;
     return HM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double *y, int64_t ny,
+                          double a, double b, double c, double d, int rank, int64_t blocksize,
+                          int storage, void *stream, hm_handle **out)
+{
+    g_last_error.clear();
+    return build_kernelmatrix(kernel, 0, x, nx, y, ny, a, b, c, d, rank, blocksize, storage, stream, out);
+}
+
+int hm_kernelmatrix_batch_build(int kernel, int ninst, const int64_t *nx, const int64_t *ny, const double *x,
+                                const double *y, const double *boxes, int rank, int64_t blocksize, int storage,
+                                void *stream, hm_handle **out)
+{
+    g_last_error.clear();
+    if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
+    *out = nullptr;
+    if (kernel < HM_KERNEL_CAUCHY || kernel > HM_KERNEL_LOG) { set_error("unknown kernel %d", kernel); return HM_ERR_UNSUPPORTED; }
+    if (storage != HM_F64 && storage != HM_F32) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
+    hm_plan *pl = nullptr;
+    HM_TRY(hm_batch_plan_create(ninst, nx, ny, x, y, boxes, rank, blocksize, &pl));
+    const int st = build_from_plan(kernel, 0, pl, x, y, storage, stream, out);
+    if (*out) (*out)->ninst = ninst;
+    return st;
+}
+
+int hm_mul_t(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs, int accumulate,
+             void *stream)
+{
+    g_last_error.clear();
+    if (!h) { set_error("NULL handle"); return HM_ERR_INVALID_ARG; }
+    if (h->ninst > 1 || h->hx.empty()) { set_error("hm_mul_t: not available for batched handles"); return HM_ERR_UNSUPPORTED; }
+    {
+        std::lock_guard<std::mutex> lk(h->trans_mu);
+        if (!h->trans) {
+            // H^T = the matrix of f(row, col) swapped, on the tree of (y, x)
+            HM_TRY(build_kernelmatrix(h->kernel, 1 - h->swap, h->hy.data(), h->ny, h->hx.data(), h->nx, h->box[2],
+                                      h->box[3], h->box[0], h->box[1], h->r, h->blocksize, h->storage, stream,
+                                      &h->trans));
+        }
+    }
+    return hm_mul(h->trans, v, ldv, u, ldu, nrhs, accumulate, stream);
 }
 
 int hm_size(const hm_handle *h, int64_t *m, int64_t *n)
@@ -849,6 +986,7 @@ void hm_free(hm_handle *h)
 {
     if (!h) return;
     cudaDeviceSynchronize();
+    if (h->trans) hm_free(h->trans);
     for (auto &kv : h->streams) {
         if (kv.second.p) cudaFree(kv.second.p);
         if (kv.second.side) cudaStreamDestroy(kv.second.side);

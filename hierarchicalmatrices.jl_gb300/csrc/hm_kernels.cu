@@ -58,7 +58,7 @@ __global__ void fill_f(FillArgs fa, const hm_fill_f *ff, const hm_m2l_ent *ents,
     S *Fe = F + ents[e].foff;
     for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
         const int m = idx % r, n = idx / r;
-        Fe[idx] = (S)kernel_eval(fa.kernel, xh[m], yh[n]);
+        Fe[idx] = (S)fill_kernel(fa, xh[m], yh[n]);
     }
 }
 
@@ -107,7 +107,7 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
         for (int64_t idx = threadIdx.x; idx < tot; idx += blockDim.x) {
             const int i = (int)(idx % G.nrows), j = (int)(idx / G.nrows);
             Pg[i + (int64_t)G.ld * (col + j)] =
-                (S)kernel_eval(fa.kernel, fa.x[G.row0 + i], fa.y[Q.src + j]);
+                (S)fill_kernel(fa, fa.x[G.row0 + i], fa.y[Q.src + j]);
         }
         col += Q.width;
     }

@@ -92,7 +92,13 @@ struct FillArgs {
     const double *x, *y;     // device copies of the points
     const double *cheb, *lam;
     int r, kernel;
+    int swap;                // 1: entries are f(col point, row point) (the transposed matrix)
 };
+
+__device__ __forceinline__ double fill_kernel(const FillArgs &fa, double row_pt, double col_pt)
+{
+    return fa.swap ? kernel_eval(fa.kernel, col_pt, row_pt) : kernel_eval(fa.kernel, row_pt, col_pt);
+}
 
 template <typename S>
 struct MulArgs {

@@ -395,4 +395,93 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
     return PLAN_OK;
 }
 
+namespace {
+
+void merge_bands(const std::vector<Plan> &parts, bool upward, Plan &out)
+{
+    std::vector<hm_xfer> &ents = upward ? out.up_ents : out.down_ents;
+    std::vector<hm_step> &steps = upward ? out.up_steps : out.down_steps;
+    std::vector<hm_task> &tasks = upward ? out.up_tasks : out.down_tasks;
+    std::vector<int> &bptr = upward ? out.up_band_ptr : out.down_band_ptr;
+    size_t nb = 0;
+    for (const Plan &p : parts) {
+        const std::vector<int> &pb = upward ? p.up_band_ptr : p.down_band_ptr;
+        nb = std::max(nb, pb.size() ? pb.size() - 1 : 0);
+    }
+    bptr.assign(1, 0);
+    std::vector<int32_t> xs_off(parts.size()), ys_off(parts.size());
+    int32_t xo = 0, yo = 0;
+    for (size_t i = 0; i < parts.size(); ++i) { xs_off[i] = xo; ys_off[i] = yo; xo += parts[i].n_xslots; yo += parts[i].n_yslots; }
+    for (size_t b = 0; b < nb; ++b) {
+        for (size_t i = 0; i < parts.size(); ++i) {
+            const Plan &p = parts[i];
+            const std::vector<int> &pb = upward ? p.up_band_ptr : p.down_band_ptr;
+            if (b + 1 >= pb.size()) continue;
+            const std::vector<hm_task> &pt = upward ? p.up_tasks : p.down_tasks;
+            const std::vector<hm_step> &ps = upward ? p.up_steps : p.down_steps;
+            const std::vector<hm_xfer> &pe = upward ? p.up_ents : p.down_ents;
+            const int32_t so = upward ? ys_off[i] : xs_off[i];
+            for (int t = pb[b]; t < pb[b + 1]; ++t) {
+                hm_task nt{(int32_t)steps.size(), (int32_t)steps.size()};
+                for (int st = pt[t].step0; st < pt[t].step1; ++st) {
+                    hm_step ns{(int32_t)ents.size(), (int32_t)ents.size()};
+                    for (int e = ps[st].e0; e < ps[st].e1; ++e)
+                        ents.push_back({pe[e].slot + so, pe[e].c0 + so, pe[e].c1 + so, 0});
+                    ns.e1 = (int32_t)ents.size();
+                    steps.push_back(ns);
+                }
+                nt.step1 = (int32_t)steps.size();
+                tasks.push_back(nt);
+            }
+        }
+        bptr.push_back((int)tasks.size());
+    }
+}
+
+}  // namespace
+
+void merge_plans(const std::vector<Plan> &parts, Plan &P)
+{
+    P = Plan();
+    if (parts.empty()) return;
+    P.r = parts[0].r;
+    P.fstride = parts[0].fstride;
+    int64_t row0 = 0, col0 = 0, voff = 0, foff = 0, poff = 0;
+    int32_t xs = 0, ys = 0, ent0 = 0;
+    for (const Plan &p : parts) {
+        for (hm_vpanel v : p.vpanels) { v.row0 += col0; v.off += voff; v.slot += ys; P.vpanels.push_back(v); }
+        P.vpanel_fill.insert(P.vpanel_fill.end(), p.vpanel_fill.begin(), p.vpanel_fill.end());
+        for (hm_m2l_row rw : p.m2l_rows) { rw.slot += xs; rw.begin += ent0; rw.end += ent0; P.m2l_rows.push_back(rw); }
+        for (hm_m2l_ent e : p.m2l_ents) { e.foff += foff; e.yslot += ys; P.m2l_ents.push_back(e); }
+        P.f_fill.insert(P.f_fill.end(), p.f_fill.begin(), p.f_fill.end());
+        const int32_t piece0 = (int32_t)P.pieces.size();
+        for (hm_piece q : p.pieces) {
+            if (q.kind == HM_PIECE_COEF) q.src += xs; else q.src += col0;
+            P.pieces.push_back(q);
+        }
+        for (hm_seg g : p.segs) { g.row0 += row0; g.poff += poff; g.piece0 += piece0; P.segs.push_back(g); }
+        P.seg_fill.insert(P.seg_fill.end(), p.seg_fill.begin(), p.seg_fill.end());
+        for (hm_xfer e : p.up) { e.slot += ys; e.c0 += ys; e.c1 += ys; P.up.push_back(e); }
+        for (hm_xfer e : p.down) { e.slot += xs; e.c0 += xs; e.c1 += xs; P.down.push_back(e); }
+        P.max_width = std::max(P.max_width, p.max_width);
+        PlanStats &S = P.stats;
+        const PlanStats &Q = p.stats;
+        S.n_bary += Q.n_bary; S.n_dense += Q.n_dense; S.depth = std::max(S.depth, Q.depth);
+        S.canonical_values += Q.canonical_values; S.reference_values += Q.reference_values;
+        S.stored_values += Q.stored_values; S.dense_values += Q.dense_values; S.n_segments += Q.n_segments;
+        S.max_width = std::max(S.max_width, Q.max_width);
+        row0 += p.nx; col0 += p.ny; voff += p.vstore_elems; foff += p.fstore_elems; poff += p.pstore_elems;
+        xs += p.n_xslots; ys += p.n_yslots; ent0 += (int32_t)p.m2l_ents.size();
+    }
+    P.nx = row0; P.ny = col0;
+    P.vstore_elems = voff; P.fstore_elems = foff; P.pstore_elems = poff;
+    P.n_xslots = xs; P.n_yslots = ys;
+    P.stats.n_xslots = xs; P.stats.n_yslots = ys;
+    merge_bands(parts, true, P);
+    merge_bands(parts, false, P);
+    // level tables are per instance only; the merged plan keeps them empty
+    P.up_level_ptr.assign(1, 0);
+    P.down_level_ptr.assign(1, 0);
+}
+
 }  // namespace hm

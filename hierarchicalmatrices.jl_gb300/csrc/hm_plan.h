@@ -89,4 +89,10 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
 
 constexpr int kBandLevels = 4;   // tree levels per transfer band
 
+// Merges independent plans into one block-diagonal plan: instance i's rows
+// and columns follow those of instances 0..i-1, its slots, stores and records
+// are offset accordingly, and the transfer bands are merged launch by launch
+// (the k-th band launch of every instance runs together).
+void merge_plans(const std::vector<Plan> &parts, Plan &out);
+
 }  // namespace hm

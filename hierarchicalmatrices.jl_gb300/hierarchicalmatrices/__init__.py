@@ -6,10 +6,10 @@ examples/Kernel.jl): ``BLOCKRANK``, ``BLOCKSIZE``, ``indsplit``,
 All products run CUDA kernels compiled for sm_103a in libhmgpu.so.
 """
 from ._lib import HMError, Plan
-from .kernelmatrix import (BLOCKRANK, BLOCKSIZE, KERNELS, KernelMatrix, cauchykernel, coulombkernel,
-                           coulombprimekernel, indsplit, logkernel, mul_)
+from .kernelmatrix import (BLOCKRANK, BLOCKSIZE, KERNELS, KernelMatrix, KernelMatrixBatch, cauchykernel,
+                           coulombkernel, coulombprimekernel, indsplit, logkernel, mul_)
 
 __all__ = [
-    "BLOCKRANK", "BLOCKSIZE", "HMError", "KERNELS", "KernelMatrix", "Plan", "cauchykernel",
+    "BLOCKRANK", "BLOCKSIZE", "HMError", "KERNELS", "KernelMatrix", "KernelMatrixBatch", "Plan", "cauchykernel",
     "coulombkernel", "coulombprimekernel", "indsplit", "logkernel", "mul_",
 ]

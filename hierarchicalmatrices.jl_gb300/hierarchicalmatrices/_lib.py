@@ -61,9 +61,9 @@ STAGES = ("up", "down", "expand", "far")
 
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
-    "hm_kernelmatrix_build", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
+    "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
     "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
-    "hm_plan_free",
+    "hm_plan_free", "hm_batch_plan_create",
 )
 
 _d = ctypes.POINTER(ctypes.c_double)
@@ -98,6 +98,12 @@ def _load():
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_int, _i64, ctypes.c_int, _vp,
                                         ctypes.POINTER(_vp)]
+    L.hm_kernelmatrix_batch_build.restype = ctypes.c_int
+    L.hm_kernelmatrix_batch_build.argtypes = [ctypes.c_int, ctypes.c_int, _pi64, _pi64, _d, _d, _d,
+                                              ctypes.c_int, _i64, ctypes.c_int, _vp, ctypes.POINTER(_vp)]
+    L.hm_batch_plan_create.restype = ctypes.c_int
+    L.hm_batch_plan_create.argtypes = [ctypes.c_int, _pi64, _pi64, _d, _d, _d, ctypes.c_int, _i64,
+                                       ctypes.POINTER(_vp)]
     L.hm_size.restype = ctypes.c_int
     L.hm_size.argtypes = [_vp, _pi64, _pi64]
     L.hm_storage.restype = ctypes.c_int
@@ -106,6 +112,8 @@ def _load():
     L.hm_stats.argtypes = [_vp, _pi64, ctypes.c_int]
     L.hm_mul.restype = ctypes.c_int
     L.hm_mul.argtypes = [_vp, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
+    L.hm_mul_t.restype = ctypes.c_int
+    L.hm_mul_t.argtypes = [_vp, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
     L.hm_mul_strided.restype = ctypes.c_int
     L.hm_mul_strided.argtypes = [_vp, _vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, _vp]
     L.hm_mul_host.restype = ctypes.c_int
@@ -157,12 +165,15 @@ def f64_ptr(a):
 class Plan:
     """Host-side plan (block tree + flattened tables) without a GPU."""
 
-    def __init__(self, x, y, a, b, c, d, rank=20, blocksize=0):
+    def __init__(self, x, y, a, b, c, d, rank=20, blocksize=0, _handle=None):
         self.x = np.ascontiguousarray(x, dtype=np.float64)
         self.y = np.ascontiguousarray(y, dtype=np.float64)
         h = _vp()
-        check(lib.hm_plan_create(f64_ptr(self.x), len(self.x), f64_ptr(self.y), len(self.y),
-                                 a, b, c, d, rank, blocksize, ctypes.byref(h)))
+        if _handle is None:
+            check(lib.hm_plan_create(f64_ptr(self.x), len(self.x), f64_ptr(self.y), len(self.y),
+                                     a, b, c, d, rank, blocksize, ctypes.byref(h)))
+        else:
+            h = _handle
         self._h = h
         out = np.zeros(len(PLAN_SIZES), dtype=np.int64)
         n = lib.hm_plan_sizes(self._h, out.ctypes.data_as(_pi64), len(out))
@@ -183,3 +194,16 @@ class Plan:
         if getattr(self, "_h", None):
             lib.hm_plan_free(self._h)
             self._h = None
+
+
+def batch_plan(xs, ys, boxes, rank=20, blocksize=0):
+    """Merged host plan of many instances (see hm_batch_plan_create)."""
+    nx = np.array([len(v) for v in xs], dtype=np.int64)
+    ny = np.array([len(v) for v in ys], dtype=np.int64)
+    x = np.ascontiguousarray(np.concatenate(xs), dtype=np.float64)
+    y = np.ascontiguousarray(np.concatenate(ys), dtype=np.float64)
+    bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 4))
+    h = _vp()
+    check(lib.hm_batch_plan_create(len(xs), nx.ctypes.data_as(_pi64), ny.ctypes.data_as(_pi64),
+                                   f64_ptr(x), f64_ptr(y), f64_ptr(bx), rank, blocksize, ctypes.byref(h)))
+    return Plan(x, y, 0, 0, 0, 0, _handle=h)

@@ -179,6 +179,21 @@ class KernelMatrix:
                          _stream_ptr(stream)))
         return u
 
+    def mul_t(self, u, v, *, accumulate=True, stream=None):
+        """u (+)= H^T v on device tensors (u has size(H, 2) rows, v size(H, 1))."""
+        ku, ldu = self._check_dev(u, self.shape[1], "u")
+        kv, ldv = self._check_dev(v, self.shape[0], "v")
+        if ku != kv:
+            raise ValueError("u and v have different numbers of columns")
+        check(lib.hm_mul_t(self._h, v.data_ptr(), ldv, u.data_ptr(), ldu, kv, 1 if accumulate else 0,
+                           _stream_ptr(stream)))
+        return u
+
+    @property
+    def T(self):
+        """The transpose as an operator: ``H.T @ v`` runs the transposed product."""
+        return _Transposed(self)
+
     def mul_strided(self, y, x, istart=1, jstart=1, incx=1, incy=1, *, stream=None):
         """mul!(y, H, x, istart, jstart, INCX, INCY) on device vectors (1-based)."""
         self._check_dev(y, 0, "y")
@@ -261,6 +276,58 @@ class KernelMatrix:
             self.free()
         except Exception:
             pass
+
+
+class KernelMatrixBatch(KernelMatrix):
+    """Many independent KernelMatrices multiplied together (block-diagonal).
+
+    ``xs``, ``ys``: lists of point arrays (each non-increasing); ``boxes``:
+    one (a, b, c, d) per instance.  Rows/columns of instance i follow those of
+    instances 0..i-1 in the vectors given to ``mul``; ``offsets`` holds the
+    row and column starts.
+    """
+
+    def __init__(self, f, xs, ys, boxes, *, dtype=np.float64, rank=None, blocksize=None, stream=None):
+        self.kernel = _kernel_id(f)
+        self.f = f
+        self.dtype = np.dtype(dtype)
+        self.rank = int(rank) if rank else BLOCKRANK(np.float64)
+        self.blocksize = int(blocksize) if blocksize else 4 * self.rank
+        nx = np.array([len(v) for v in xs], dtype=np.int64)
+        ny = np.array([len(v) for v in ys], dtype=np.int64)
+        self.x = np.ascontiguousarray(np.concatenate([_host_f64(v) for v in xs]))
+        self.y = np.ascontiguousarray(np.concatenate([_host_f64(v) for v in ys]))
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 4))
+        if len(bx) != len(xs) or len(ys) != len(xs):
+            raise ValueError("one point list pair and one box per instance")
+        h = _vp()
+        check(lib.hm_kernelmatrix_batch_build(
+            self.kernel, len(xs), nx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            ny.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _lib.f64_ptr(self.x), _lib.f64_ptr(self.y),
+            _lib.f64_ptr(bx), self.rank, self.blocksize, _storage_of(self.dtype), _stream_ptr(stream),
+            ctypes.byref(h)))
+        self._h = h
+        self.ninst = len(xs)
+        self.row_offsets = np.concatenate([[0], np.cumsum(nx)])
+        self.col_offsets = np.concatenate([[0], np.cumsum(ny)])
+        self.shape = (int(nx.sum()), int(ny.sum()))
+
+    def mul_t(self, *a, **k):
+        raise NotImplementedError("the transposed product is not available for batched handles")
+
+
+class _Transposed:
+    def __init__(self, H):
+        self.H = H
+        self.shape = (H.shape[1], H.shape[0])
+
+    def __matmul__(self, v):
+        import torch
+        shape = (self.shape[0],) if v.dim() == 1 else (v.shape[1], self.shape[0])
+        u = torch.zeros(shape, dtype=v.dtype, device=v.device)
+        if v.dim() == 2:
+            u = u.t()
+        return self.H.mul_t(u, v, accumulate=False)
 
 
 def mul_(u, H, v, istart=1, jstart=1, incx=None, incy=None, **kw):

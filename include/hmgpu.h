@@ -72,6 +72,17 @@ int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double 
                           double a, double b, double c, double d, int rank, int64_t blocksize,
                           int storage, void *stream, hm_handle **out);
 
+/* Many independent KernelMatrices as one block-diagonal handle (no
+   counterpart in the reference, which builds one matrix per call).
+   Instance i has nx[i] rows and ny[i] columns; x (sum nx) and y (sum ny) are
+   the instances' HOST point lists concatenated, each non-increasing, and
+   boxes holds (a, b, c, d) per instance.  hm_mul on the handle multiplies
+   every instance at once: rows and columns of instance i follow those of
+   instances 0..i-1 in u and v.  Planning runs on all host cores. */
+int hm_kernelmatrix_batch_build(int kernel, int ninst, const int64_t *nx, const int64_t *ny,
+                                const double *x, const double *y, const double *boxes, int rank,
+                                int64_t blocksize, int storage, void *stream, hm_handle **out);
+
 /* size(H) (src/hierarchical.jl:33-47). */
 int hm_size(const hm_handle *h, int64_t *m, int64_t *n);
 /* Storage type of h (HM_F64 / HM_F32). */
@@ -93,6 +104,15 @@ int hm_stats(const hm_handle *h, int64_t *out, int nout);
    passes run on a side stream forked from and joined back into `stream`. */
 int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs,
            int accumulate, void *stream);
+
+/* u (+)= H^T v: the transposed product (the role of the Transpose/Adjoint
+   block mul! of src/algebra.jl:50-82 and :133-159 for the whole KernelMatrix;
+   the reference itself has no transposed KernelMatrix product).  Same
+   arguments as hm_mul with u of length ny and v of length nx.  The first
+   call builds the transposed plan (the reference's tree of (y, x) is the
+   transpose of the tree of (x, y)) and keeps it with the handle. */
+int hm_mul_t(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs,
+             int accumulate, void *stream);
 
 /* mul!(y, H, x, istart, jstart, INCX, INCY) (src/HierarchicalMatrix.jl:24-52):
    y[istart-1 + i*incy] += (H x)[i] with x read at x[jstart-1 + j*incx]
@@ -164,6 +184,10 @@ int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, dou
    15-18 upward band records / steps / tasks / band offsets, 19-22 the same
    for the downward bands):
    pointer, element count and element size (records of hm_types.h). */
+/* The merged plan of hm_kernelmatrix_batch_build (same arguments). */
+int hm_batch_plan_create(int ninst, const int64_t *nx, const int64_t *ny, const double *x,
+                         const double *y, const double *boxes, int rank, int64_t blocksize,
+                         hm_plan **out);
 int hm_plan_table(const hm_plan *p, int which, const void **data, int64_t *count, int64_t *elem_bytes);
 /* r, nx, ny, row slots, column slots, V/F/panel store elements, max panel
    width, barycentric blocks, dense blocks, depth, canonical values,

@@ -263,3 +263,57 @@ def test_repeated_calls_and_streams():
         u3 = H @ b
     s.synchronize()
     assert torch.equal(u1, u3)
+
+
+@pytest.mark.parametrize("kernel,sign", [(O.CAUCHY, -1.0), (O.COULOMB, 1.0), (O.COULOMB_PRIME, -1.0), (O.LOG, 1.0)])
+def test_transposed_product(kernel, sign):
+    # H^T = the KernelMatrix of (y, x) with the kernel's arguments swapped:
+    # f(x, y) = sign * f(y, x) for the example kernels
+    rng = np.random.default_rng(31)
+    x = np.sort(rng.random(20000))[::-1].copy()
+    y = np.sort(rng.random(13000))[::-1].copy()
+    H = hm.KernelMatrix(KFUN[kernel], x, y, 1.0, 0.0, 1.0, 0.0)
+    v = rng.standard_normal(20000)
+    ref = sign * (O.OracleKernelMatrix(kernel, y, x, 1.0, 0.0, 1.0, 0.0) @ v)
+    got = (H.T @ dev(v)).cpu().numpy()
+    assert rel(got, ref) <= TOL64
+    # <H w, v> == <w, H^T v>
+    w = dev(rng.standard_normal(13000))
+    lhs = float(torch.dot(H @ w, dev(v)))
+    rhs = float(torch.dot(w, dev(got)))
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
+
+
+def test_transposed_fp32_multi_rhs():
+    n = 65536
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    V = torch.randn(4, n, device="cuda", dtype=torch.float32).t()
+    U = H.T @ V
+    Ho = O.OracleKernelMatrix(O.CAUCHY, y, x, 1.0, 0.0, 1.0, 0.0)
+    for q in range(4):
+        ref = -(Ho @ V[:, q].double().cpu().numpy().copy())
+        assert rel(U[:, q].double().cpu().numpy(), ref) <= TOL32
+
+
+@pytest.mark.parametrize("dtype,k", [(np.float64, 1), (np.float32, 8)])
+def test_batch_matches_instances(dtype, k):
+    rng = np.random.default_rng(40)
+    xs, ys, boxes = [], [], []
+    for i in range(24):
+        n = int(np.exp(rng.uniform(np.log(1024), np.log(20000))))
+        xs.append(np.sort(rng.random(n))[::-1].copy())
+        ys.append(np.sort(rng.random(n))[::-1].copy())
+        boxes.append((1.0, 0.0, 1.0, 0.0))
+    Hb = hm.KernelMatrixBatch(hm.cauchykernel, xs, ys, boxes, dtype=dtype)
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    B = torch.randn(k, Hb.shape[1], device="cuda", dtype=tdt).t()
+    U = Hb @ B if k > 1 else Hb @ B[:, 0].contiguous()
+    U = U.reshape(Hb.shape[0], k) if k == 1 else U
+    for i in (0, 5, 23):
+        r0, r1 = Hb.row_offsets[i], Hb.row_offsets[i + 1]
+        c0, c1 = Hb.col_offsets[i], Hb.col_offsets[i + 1]
+        Ho = O.OracleKernelMatrix(O.CAUCHY, xs[i], ys[i], *boxes[i])
+        for q in range(k):
+            ref = Ho @ B[c0:c1, q].double().cpu().numpy().copy()
+            assert rel(U[r0:r1, q].double().cpu().numpy(), ref) <= (TOL64 if dtype == np.float64 else TOL32)

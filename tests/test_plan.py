@@ -128,3 +128,30 @@ def test_indsplit_matches_oracle():
         assert (r1.start, len(r1), r2.start, len(r2)) == (s1, l1, s2, l2)
     with pytest.raises(IndexError):
         hm.indsplit(x, range(50, 50), 1.0, 0.0)
+
+
+def _batch_instances(seed, count, lo=600, hi=5000):
+    rng = np.random.default_rng(seed)
+    xs, ys, boxes = [], [], []
+    for _ in range(count):
+        n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        m = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        xs.append(np.sort(rng.random(n))[::-1].copy())
+        ys.append(np.sort(rng.random(m))[::-1].copy())
+        boxes.append((1.0, 0.0, 1.0, 0.0))
+    return xs, ys, boxes
+
+
+def test_batch_plan_emulation_matches_instances():
+    xs, ys, boxes = _batch_instances(3, 9)
+    P = _lib.batch_plan(xs, ys, boxes)
+    assert P.sizes["nx"] == sum(map(len, xs)) and P.sizes["ny"] == sum(map(len, ys))
+    b = np.random.default_rng(4).standard_normal(P.sizes["ny"])
+    u = emulate(P, O.CAUCHY, b)
+    r0 = c0 = 0
+    for x, y, box in zip(xs, ys, boxes):
+        ref = O.OracleKernelMatrix(O.CAUCHY, x, y, *box) @ b[c0:c0 + len(y)]
+        got = u[r0:r0 + len(x)]
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-13
+        r0 += len(x)
+        c0 += len(y)
