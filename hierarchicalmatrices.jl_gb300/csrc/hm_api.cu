@@ -362,6 +362,7 @@ int stream_ctx(hm_handle *h, cudaStream_t st, size_t bytes, hm_handle::StreamCtx
 }
 
 constexpr int kWarpsPerCta = 4;
+constexpr int kPartMaxK = 8;    // right-hand sides handled by the streaming panel kernels
 
 inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
 
@@ -420,15 +421,26 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
     return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing);
 }
 
+template <typename S, typename A, bool FAR, int KB>
+int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+{
+    const int maxw = std::max(h->max_width, 1);
+    const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(A);
+    HM_TRY(ensure_smem(expand_part<S, A, FAR, KB>, smem));
+    expand_part<S, A, FAR, KB><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
+        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(h->d_P), s, h->r, maxw);
+    HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
+    return HM_OK;
+}
+
+// Near-field (FAR = false) or far-field (FAR = true) panel columns for k <= 8.
 template <typename S, typename A, bool FAR>
 int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
 {
-    const size_t smem = (size_t)kWarpsPerCta * std::max(h->max_width, 1) * sizeof(A);
-    HM_TRY(ensure_smem(expand_part<S, A, FAR>, smem));
-    expand_part<S, A, FAR><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
-        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(h->d_P), s, h->r, std::max(h->max_width, 1));
-    HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
-    return HM_OK;
+    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, st);
+    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, st);
+    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, st);
+    return launch_part_kb<S, A, FAR, 8>(h, ma, s, st);
 }
 
 template <typename S, typename A>
@@ -469,7 +481,7 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
         if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
         return HM_OK;
     }
-    if (k == 1) {
+    if (k <= kPartMaxK) {
         {
             StageTimer tm(h, timing ? 2 : -1, st);
             HM_TRY((launch_part<S, A, false>(h, ma, s, st)));

@@ -335,15 +335,63 @@ __global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const
     }
 }
 
-// Row segments, one right-hand side: one warp per segment (<= 64 rows).
+// Row segments, up to KB right-hand sides: one warp per segment (<= 64 rows).
 // FAR = false: the near-field dense columns, y (+)= D x (written with the
 // caller's accumulate flag); FAR = true: the row-basis columns, y += U s.
 // FP32: lanes 0-15 and 16-31 take alternate panel columns, each lane four
 // consecutive rows through one 16-byte load per column; FP64: each lane two
-// rows per 16-byte load.  The gathered right-hand side is staged per warp in
-// shared memory.  FP32 products accumulate with compensated (TwoProd/TwoSum)
-// sums.
-template <typename S, typename A, bool FAR>
+// rows per 16-byte load.  The panel streams once from HBM whatever the
+// number of right-hand sides; the gathered right-hand sides [s ; x pieces]
+// are staged per warp in shared memory (g[c * KB + q]).  KB = 1 accumulates
+// with compensated (TwoProd/TwoSum) sums, KB > 1 with FMA per piece folded
+// in with TwoSum.
+template <typename A, int KB>
+struct SegAcc;
+template <typename A>
+struct SegAcc<A, 1> {
+    Acc<A> a;
+    __device__ __forceinline__ void zero() { a.zero(); }
+    __device__ __forceinline__ void add(A p, const A *g) { a.add(p, g[0]); }
+    __device__ __forceinline__ void fold() {}
+    __device__ __forceinline__ A hi(int) const { return a.s_hi(); }
+    __device__ __forceinline__ A lo(int) const { return a.s_lo(); }
+    __device__ __forceinline__ A merged(int, A so, A co) const { return a.merged(so, co); }
+};
+template <typename A, int KB>
+struct SegAcc {
+    A part[KB], h[KB], l[KB];
+    __device__ __forceinline__ void zero()
+    {
+#pragma unroll
+        for (int q = 0; q < KB; ++q) { part[q] = 0; h[q] = 0; l[q] = 0; }
+    }
+    __device__ __forceinline__ void add(A p, const A *g)
+    {
+#pragma unroll
+        for (int q = 0; q < KB; ++q) part[q] = fma(p, g[q], part[q]);
+    }
+    __device__ __forceinline__ void fold()   // end of a piece: compensated fold of the partial sums
+    {
+#pragma unroll
+        for (int q = 0; q < KB; ++q) {
+            const A t = h[q] + part[q];
+            const A bp = t - h[q];
+            l[q] += (h[q] - (t - bp)) + (part[q] - bp);
+            h[q] = t;
+            part[q] = 0;
+        }
+    }
+    __device__ __forceinline__ A hi(int q) const { return h[q]; }
+    __device__ __forceinline__ A lo(int q) const { return l[q]; }
+    __device__ __forceinline__ A merged(int q, A so, A co) const
+    {
+        const A t = h[q] + so;
+        const A bp = t - h[q];
+        return t + (((h[q] - (t - bp)) + (so - bp)) + (l[q] + co));
+    }
+};
+
+template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
                             const A *s, int r, int maxw)
 {
@@ -352,97 +400,130 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
     const int wib = threadIdx.x >> 5;
     const int seg = blockIdx.x * (blockDim.x >> 5) + wib;
     if (seg >= nsegs) return;
-    A *g = reinterpret_cast<A *>(smem_raw) + (int64_t)wib * maxw;
+    A *g = reinterpret_cast<A *>(smem_raw) + (int64_t)wib * maxw * KB;
     const hm_seg G = segs[seg];
-    // columns [c0, c1) of the panel
-    int c0 = 0, c1 = 0, col = 0;
+    const int k = ma.k;
+    // gather the right-hand sides of the columns this part uses
+    int pcs[2] = {0, 0};          // piece range [pc0, pc1) of the part
+    int c0 = -1, c1 = 0, col = 0;
     for (int pc = 0; pc < G.npieces; ++pc) {
         const hm_piece Q = pieces[G.piece0 + pc];
         const bool take = FAR ? (Q.kind == HM_PIECE_COEF) : (Q.kind == HM_PIECE_X);
         if (take) {
-            if (c1 == c0) c0 = col;
-            for (int c = lane; c < Q.width; c += 32)
-                g[col + c] = FAR ? s[Q.src * r + c] : (A)ma.x[(Q.src + c) * ma.incx];
+            if (c0 < 0) { c0 = col; pcs[0] = pc; }
+            for (int i = lane; i < Q.width * KB; i += 32) {
+                const int c = i / KB, q = i % KB;
+                A v = 0;
+                if (q < k)
+                    v = FAR ? s[((int64_t)Q.src * k + q) * r + c]
+                            : (A)ma.x[(Q.src + c) * ma.incx + (int64_t)q * ma.ldx];
+                g[(col + c) * KB + q] = v;
+            }
             c1 = col + Q.width;
+            pcs[1] = pc + 1;
         }
         col += Q.width;
     }
-    if (FAR && c1 == c0) return;          // no far field on these rows
+    if (c0 < 0) {
+        if (FAR) return;          // no far field on these rows
+        c0 = c1 = 0;
+    }
     __syncwarp();
     const S *Pg = P + G.poff;
     const bool acc_y = FAR || ma.accumulate;
     if (sizeof(S) == 4) {
         const int rg = lane & 15, h = lane >> 4;
-        Acc<A> acc[4];
+        SegAcc<A, KB> acc[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[j].zero();
         if (4 * rg < G.ld) {
             const float4 *base = reinterpret_cast<const float4 *>(Pg + 4 * rg);
             const int64_t ld4 = G.ld / 4;
-            int c = c0 + h;
-            for (; c + 6 < c1; c += 8) {
-                const float4 p0 = __ldcs(base + ld4 * c), p1 = __ldcs(base + ld4 * (c + 2));
-                const float4 p2 = __ldcs(base + ld4 * (c + 4)), p3 = __ldcs(base + ld4 * (c + 6));
-                const A g0 = g[c], g1 = g[c + 2], g2 = g[c + 4], g3 = g[c + 6];
-                acc[0].add(p0.x, g0); acc[1].add(p0.y, g0); acc[2].add(p0.z, g0); acc[3].add(p0.w, g0);
-                acc[0].add(p1.x, g1); acc[1].add(p1.y, g1); acc[2].add(p1.z, g1); acc[3].add(p1.w, g1);
-                acc[0].add(p2.x, g2); acc[1].add(p2.y, g2); acc[2].add(p2.z, g2); acc[3].add(p2.w, g2);
-                acc[0].add(p3.x, g3); acc[1].add(p3.y, g3); acc[2].add(p3.z, g3); acc[3].add(p3.w, g3);
-            }
-            for (; c < c1; c += 2) {
-                const float4 p0 = __ldcs(base + ld4 * c);
-                const A g0 = g[c];
-                acc[0].add(p0.x, g0); acc[1].add(p0.y, g0); acc[2].add(p0.z, g0); acc[3].add(p0.w, g0);
-            }
-        }
-        A val[4];
+            int cp = c0;
+            for (int pc = pcs[0]; pc < pcs[1]; ++pc) {
+                const int ce = cp + pieces[G.piece0 + pc].width;
+                int c = cp + ((h - cp) & 1);             // this half's first column (parity h)
+                for (; c + 6 < ce; c += 8) {
+                    const float4 p0 = __ldcs(base + ld4 * c), p1 = __ldcs(base + ld4 * (c + 2));
+                    const float4 p2 = __ldcs(base + ld4 * (c + 4)), p3 = __ldcs(base + ld4 * (c + 6));
+                    const A *g0 = g + c * KB, *g1 = g + (c + 2) * KB, *g2 = g + (c + 4) * KB, *g3 = g + (c + 6) * KB;
+                    acc[0].add(p0.x, g0); acc[1].add(p0.y, g0); acc[2].add(p0.z, g0); acc[3].add(p0.w, g0);
+                    acc[0].add(p1.x, g1); acc[1].add(p1.y, g1); acc[2].add(p1.z, g1); acc[3].add(p1.w, g1);
+                    acc[0].add(p2.x, g2); acc[1].add(p2.y, g2); acc[2].add(p2.z, g2); acc[3].add(p2.w, g2);
+                    acc[0].add(p3.x, g3); acc[1].add(p3.y, g3); acc[2].add(p3.z, g3); acc[3].add(p3.w, g3);
+                }
+                for (; c < ce; c += 2) {
+                    const float4 p0 = __ldcs(base + ld4 * c);
+                    const A *g0 = g + c * KB;
+                    acc[0].add(p0.x, g0); acc[1].add(p0.y, g0); acc[2].add(p0.z, g0); acc[3].add(p0.w, g0);
+                }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const A so = __shfl_xor_sync(0xffffffffu, acc[j].s_hi(), 16);
-            const A co = __shfl_xor_sync(0xffffffffu, acc[j].s_lo(), 16);
-            val[j] = acc[j].merged(so, co);
+                for (int j = 0; j < 4; ++j) acc[j].fold();
+                cp = ce;
+            }
         }
-        if (h == 0) {
+#pragma unroll
+        for (int q = 0; q < KB; ++q) {
+            if (q >= k) break;
+            A val[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const int row = 4 * rg + j;
-                if (row < G.nrows) {
-                    S *yp = ma.y + (G.row0 + row) * ma.incy;
-                    A v = val[j];
-                    if (acc_y) v += (A)(*yp);
-                    *yp = (S)v;
+                const A so = __shfl_xor_sync(0xffffffffu, acc[j].hi(q), 16);
+                const A co = __shfl_xor_sync(0xffffffffu, acc[j].lo(q), 16);
+                val[j] = acc[j].merged(q, so, co);
+            }
+            if (h == 0) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int row = 4 * rg + j;
+                    if (row < G.nrows) {
+                        S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
+                        A v = val[j];
+                        if (acc_y) v += (A)(*yp);
+                        *yp = (S)v;
+                    }
                 }
             }
         }
     } else {
-        Acc<A> a0, a1;
+        SegAcc<A, KB> a0, a1;
         a0.zero(); a1.zero();
         if (2 * lane < G.ld) {
             const double2 *base = reinterpret_cast<const double2 *>(Pg + 2 * lane);
             const int64_t ld2 = G.ld / 2;
-            int c = c0;
-            for (; c + 4 <= c1; c += 4) {
-                const double2 p0 = __ldcs(base + ld2 * c), p1 = __ldcs(base + ld2 * (c + 1));
-                const double2 p2 = __ldcs(base + ld2 * (c + 2)), p3 = __ldcs(base + ld2 * (c + 3));
-                a0.add(p0.x, g[c]); a1.add(p0.y, g[c]);
-                a0.add(p1.x, g[c + 1]); a1.add(p1.y, g[c + 1]);
-                a0.add(p2.x, g[c + 2]); a1.add(p2.y, g[c + 2]);
-                a0.add(p3.x, g[c + 3]); a1.add(p3.y, g[c + 3]);
-            }
-            for (; c < c1; ++c) {
-                const double2 p0 = __ldcs(base + ld2 * c);
-                a0.add(p0.x, g[c]); a1.add(p0.y, g[c]);
+            int cp = c0;
+            for (int pc = pcs[0]; pc < pcs[1]; ++pc) {
+                const int ce = cp + pieces[G.piece0 + pc].width;
+                int c = cp;
+                for (; c + 4 <= ce; c += 4) {
+                    const double2 p0 = __ldcs(base + ld2 * c), p1 = __ldcs(base + ld2 * (c + 1));
+                    const double2 p2 = __ldcs(base + ld2 * (c + 2)), p3 = __ldcs(base + ld2 * (c + 3));
+                    a0.add(p0.x, g + c * KB); a1.add(p0.y, g + c * KB);
+                    a0.add(p1.x, g + (c + 1) * KB); a1.add(p1.y, g + (c + 1) * KB);
+                    a0.add(p2.x, g + (c + 2) * KB); a1.add(p2.y, g + (c + 2) * KB);
+                    a0.add(p3.x, g + (c + 3) * KB); a1.add(p3.y, g + (c + 3) * KB);
+                }
+                for (; c < ce; ++c) {
+                    const double2 p0 = __ldcs(base + ld2 * c);
+                    a0.add(p0.x, g + c * KB); a1.add(p0.y, g + c * KB);
+                }
+                a0.fold(); a1.fold();
+                cp = ce;
             }
         }
-        const A v2[2] = {a0.value(), a1.value()};
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const int row = 2 * lane + j;
-            if (row < G.nrows) {
-                S *yp = ma.y + (G.row0 + row) * ma.incy;
-                A v = v2[j];
-                if (acc_y) v += (A)(*yp);
-                *yp = (S)v;
+        for (int q = 0; q < KB; ++q) {
+            if (q >= k) break;
+            const A v2[2] = {a0.merged(q, 0, 0), a1.merged(q, 0, 0)};
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int row = 2 * lane + j;
+                if (row < G.nrows) {
+                    S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
+                    A v = v2[j];
+                    if (acc_y) v += (A)(*yp);
+                    *yp = (S)v;
+                }
             }
         }
     }
@@ -573,6 +654,11 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     }
 }
 
+#define HM_INST_PART(S, A, KB)                                                                       \
+    template __global__ void expand_part<S, A, false, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *, \
+                                                          const S *, const A *, int, int);              \
+    template __global__ void expand_part<S, A, true, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
+                                                         const S *, const A *, int, int);
 #define HM_INST_MV(S, A)                                                                             \
     template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
     template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
@@ -580,10 +666,7 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                           const A *, A *, int, int);                                    \
     template __global__ void m2l<S, A, 8>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,    \
                                           const A *, A *, int, int);                                    \
-    template __global__ void expand_part<S, A, false>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
-                                                      const S *, const A *, int, int);                  \
-    template __global__ void expand_part<S, A, true>(MulArgs<S>, const hm_seg *, int, const hm_piece *,   \
-                                                     const S *, const A *, int, int);                   \
+    HM_INST_PART(S, A, 1) HM_INST_PART(S, A, 2) HM_INST_PART(S, A, 4) HM_INST_PART(S, A, 8)               \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
                                             const A *, int, int);                                       \
     template __global__ void xfer_up_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \

@@ -138,7 +138,7 @@ template <typename A, int QC>
 __global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
                                int r, int k);
 
-template <typename S, typename A, bool FAR>
+template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
                             const A *s, int r, int maxw);
 
