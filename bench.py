@@ -275,6 +275,32 @@ def run_batch(hm, torch, dev, args, count=512, nrhs=8):
     }
 
 
+# ----------------------------------------------------------------- gradients
+
+def run_grad(hm, torch, dev, args, n=65536):
+    """L = 1/2 |H(x,y) w - t|^2 for a Cauchy KernelMatrix on n uniform sorted
+    points, FP32: loss and dL/dw, dL/dx, dL/dy (forward product, transposed
+    product and the two row-derivative products)."""
+    rng = np.random.default_rng(11)
+    x = np.sort(rng.random(n))[::-1].copy()
+    y = np.sort(rng.random(n))[::-1].copy()
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    w = torch.randn(n, device=dev, dtype=torch.float32)
+    t = torch.randn(n, device=dev, dtype=torch.float32)
+    for _ in range(3):
+        H.loss_and_grad(w, t)                 # builds the transposed and derivative panels
+    reps = max(5, min(100, args.steps // 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        H.loss_and_grad(w, t)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    return {"workload": f"Cauchy KernelMatrix n={n} uniform sorted points, FP32; loss + dL/dw + dL/dx + dL/dy "
+                        "(forward, transposed and two row-derivative products)",
+            "ms_per_grad": ms, "grads_per_s": 1e3 / ms, "reps": reps}
+
+
 # ----------------------------------------------------------------- GPU arm
 
 def main():
@@ -401,6 +427,9 @@ def main():
     batch = None
     if not args.no_variants and not args.no_batch:
         batch = run_batch(hm, torch, dev, args)
+    grad = None
+    if not args.no_variants:
+        grad = run_grad(hm, torch, dev, args)
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -443,6 +472,7 @@ def main():
                                         "reference_values", "stored_values", "device_bytes")},
             "variants": variants,
             "batch": batch,
+            "grad": grad,
             "cpu_baseline": cb,
         }
         print(json.dumps(line), flush=True)

@@ -117,6 +117,10 @@ struct hm_handle {
     int kernel = 0, storage = HM_F64, r = 0;
     int swap = 0;                  // 1: this handle holds the transpose of the kernel matrix
     int ninst = 1;                 // instances of a batched (block-diagonal) handle
+    hm_fill_seg *d_seg_fill = nullptr;
+    int64_t pstore_elems = 0;
+    void *d_dP = nullptr;          // row-derivative panels, filled on the first hm_mul_drow
+    std::mutex drow_mu;
     int64_t nx = 0, ny = 0;
     // host copies of the build inputs, for the lazily built transpose
     std::vector<double> hx, hy;
@@ -254,6 +258,8 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     HM_TRY(h->upload(&h->d_pieces, P.pieces, st));
     hm_fill_seg *sf = nullptr;
     HM_TRY(h->upload(&sf, P.seg_fill, st));
+    h->d_seg_fill = sf;
+    h->pstore_elems = P.pstore_elems;
 
     S *V = nullptr, *F = nullptr, *Pn = nullptr;
     HM_TRY(h->alloc(&V, (size_t)P.vstore_elems));
@@ -274,7 +280,7 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
         HM_CK_LAUNCH("fill_f");
     }
     if (h->n_segs) {
-        fill_segments<S><<<h->n_segs, 128, 0, st>>>(fa, h->d_segs, h->d_pieces, sf, h->n_segs, Pn);
+        fill_segments<S, false><<<h->n_segs, 128, 0, st>>>(fa, h->d_segs, h->d_pieces, sf, h->n_segs, Pn);
         HM_CK_LAUNCH("fill_segments");
     }
     HM_CK(cudaStreamSynchronize(st));
@@ -422,35 +428,35 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
 }
 
 template <typename S, typename A, bool FAR, int KB>
-int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const void *panels, cudaStream_t st)
 {
     const int maxw = std::max(h->max_width, 1);
     const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(A);
     HM_TRY(ensure_smem(expand_part<S, A, FAR, KB>, smem));
     expand_part<S, A, FAR, KB><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
-        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(h->d_P), s, h->r, maxw);
+        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(panels), s, h->r, maxw);
     HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
     return HM_OK;
 }
 
 // Near-field (FAR = false) or far-field (FAR = true) panel columns for k <= 8.
 template <typename S, typename A, bool FAR>
-int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const void *panels, cudaStream_t st)
 {
-    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, st);
-    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, st);
-    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, st);
-    return launch_part_kb<S, A, FAR, 8>(h, ma, s, st);
+    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, panels, st);
+    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, panels, st);
+    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, panels, st);
+    return launch_part_kb<S, A, FAR, 8>(h, ma, s, panels, st);
 }
 
 template <typename S, typename A>
-int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t st)
+int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const void *panels, cudaStream_t st)
 {
     const int maxw = std::max(h->max_width, 1);
     const int qc = sizeof(A) == 8 ? 16 : 32;
     const size_t smem = ((size_t)64 * maxw * sizeof(S) + 31) / 32 * 32 + (size_t)maxw * qc * sizeof(A);
     HM_TRY(ensure_smem(expand_k<S, A>, smem));
-    expand_k<S, A><<<h->n_segs, 128, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(h->d_P), s,
+    expand_k<S, A><<<h->n_segs, 128, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(panels), s,
                                                   h->r, maxw);
     HM_CK_LAUNCH("expand_k");
     return HM_OK;
@@ -461,8 +467,9 @@ int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, cudaStream_t
 // added after the join.  side == st runs everything in order on st.
 template <typename S, typename A>
 int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStream_t side, cudaEvent_t fork,
-                    cudaEvent_t join, void *scratch, bool timing)
+                    cudaEvent_t join, void *scratch, bool timing, const void *panels = nullptr)
 {
+    if (!panels) panels = h->d_P;
     const int k = ma.k;
     const ScratchLayout L = scratch_layout<A>(h, k);
     A *t = reinterpret_cast<A *>(static_cast<char *>(scratch) + L.t_off);
@@ -484,27 +491,48 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
     if (k <= kPartMaxK) {
         {
             StageTimer tm(h, timing ? 2 : -1, st);
-            HM_TRY((launch_part<S, A, false>(h, ma, s, st)));
+            HM_TRY((launch_part<S, A, false>(h, ma, s, panels, st)));
         }
         if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
         if (tree) {
             StageTimer tm(h, timing ? 3 : -1, st);
-            HM_TRY((launch_part<S, A, true>(h, ma, s, st)));
+            HM_TRY((launch_part<S, A, true>(h, ma, s, panels, st)));
         }
         return HM_OK;
     }
     if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
     StageTimer tm(h, timing ? 2 : -1, st);
-    return launch_expand_k<S, A>(h, ma, s, st);
+    return launch_expand_k<S, A>(h, ma, s, panels, st);
 }
 
 template <typename S, typename A>
-int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st)
+int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st, const void *panels = nullptr)
 {
     if (ma.k <= 0) return HM_OK;
     hm_handle::StreamCtx *sc = nullptr;
     HM_TRY(stream_ctx(h, st, scratch_layout<A>(h, ma.k).bytes, &sc));
-    return launch_pipeline<S, A>(h, ma, st, h->overlap ? sc->side : st, sc->fork, sc->join, sc->p, true);
+    return launch_pipeline<S, A>(h, ma, st, h->overlap ? sc->side : st, sc->fork, sc->join, sc->p, true, panels);
+}
+
+// Row-derivative panels (same layout as the panels), filled once.
+template <typename S>
+int ensure_drow(hm_handle *h, cudaStream_t st)
+{
+    std::lock_guard<std::mutex> lk(h->drow_mu);
+    if (h->d_dP) return HM_OK;
+    S *dP = nullptr;
+    HM_TRY(h->alloc(&dP, (size_t)h->pstore_elems));
+    if (!dP) return HM_OK;
+    HM_CK(cudaMemsetAsync(dP, 0, sizeof(S) * h->pstore_elems, st));
+    FillArgs fa;
+    fa.x = h->d_x; fa.y = h->d_y; fa.cheb = h->d_cheb; fa.lam = h->d_lam; fa.r = h->r; fa.kernel = h->kernel;
+    fa.swap = h->swap;
+    if (h->n_segs) {
+        fill_segments<S, true><<<h->n_segs, 128, 0, st>>>(fa, h->d_segs, h->d_pieces, h->d_seg_fill, h->n_segs, dP);
+        HM_CK_LAUNCH("fill_segments<drow>");
+    }
+    h->d_dP = dP;
+    return HM_OK;
 }
 
 int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
@@ -876,6 +904,35 @@ int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int n
     if (nrhs < 0) { set_error("nrhs < 0"); return HM_ERR_INVALID_ARG; }
     if (nrhs > 1 && (ldv < h->ny || ldu < h->nx)) { set_error("leading dimension too small"); return HM_ERR_BOUNDS; }
     return dispatch_mul(h, v, 1, ldv, u, 1, ldu, nrhs, accumulate ? 1 : 0, static_cast<cudaStream_t>(stream));
+}
+
+int hm_mul_drow(hm_handle *h, int transposed, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs,
+                int accumulate, void *stream)
+{
+    g_last_error.clear();
+    if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
+    if (transposed) {
+        if (h->ninst > 1 || h->hx.empty()) { set_error("transposed products are not available for batched handles"); return HM_ERR_UNSUPPORTED; }
+        {
+            std::lock_guard<std::mutex> lk(h->trans_mu);
+            if (!h->trans)
+                HM_TRY(build_kernelmatrix(h->kernel, 1 - h->swap, h->hy.data(), h->ny, h->hx.data(), h->nx, h->box[2],
+                                          h->box[3], h->box[0], h->box[1], h->r, h->blocksize, h->storage, stream,
+                                          &h->trans));
+        }
+        return hm_mul_drow(h->trans, 0, v, ldv, u, ldu, nrhs, accumulate, stream);
+    }
+    if (nrhs < 0) { set_error("nrhs < 0"); return HM_ERR_INVALID_ARG; }
+    if (nrhs > 1 && (ldv < h->ny || ldu < h->nx)) { set_error("leading dimension too small"); return HM_ERR_BOUNDS; }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (h->storage == HM_F64) {
+        HM_TRY(ensure_drow<double>(h, st));
+        MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, ldv, 1, ldu, nrhs, accumulate ? 1 : 0};
+        return run_mul<double, double>(h, ma, st, h->d_dP);
+    }
+    HM_TRY(ensure_drow<float>(h, st));
+    MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, ldv, 1, ldu, nrhs, accumulate ? 1 : 0};
+    return run_mul<float, float>(h, ma, st, h->d_dP);
 }
 
 int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, int64_t incx, void *y,

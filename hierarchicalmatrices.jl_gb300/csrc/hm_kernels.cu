@@ -65,8 +65,11 @@ __global__ void fill_f(FillArgs fa, const hm_fill_f *ff, const hm_m2l_ent *ents,
 // Segment panels: the first basis_w columns hold the row basis U[i, m] of the
 // segment's deepest row box (src/BarycentricMatrix.jl:256-267), the rest the
 // near-field dense blocks f(x_i, y_j) (src/KernelMatrix.jl:57-60).  Column-major
-// with leading dimension ld.  One CTA per segment.
-template <typename S>
+// with leading dimension ld.  One CTA per segment.  DROW = true fills the
+// derivative of every entry with respect to its row point instead: the basis
+// derivative U_m'(x) = U_m(x) (sum_k U_k(x)/(x - xh_k) - 1/(x - xh_m)) and
+// d f / d(row point) for the dense blocks.
+template <typename S, bool DROW>
 __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *pieces,
                               const hm_fill_seg *sf, int nsegs, S *P)
 {
@@ -95,9 +98,19 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
                     sum = __dadd_rn(sum, w[m]);
                 }
             }
+            if (DROW) {
+                double sd = 0.0;
 #pragma unroll
-            for (int m = 0; m < HM_RMAX; ++m)
-                if (m < r) Pg[i + (int64_t)G.ld * m] = (S)(w[m] / sum);
+                for (int m = 0; m < HM_RMAX; ++m)
+                    if (m < r) sd += (w[m] / sum) / __dsub_rn(xi, nodes[m]);
+#pragma unroll
+                for (int m = 0; m < HM_RMAX; ++m)
+                    if (m < r) Pg[i + (int64_t)G.ld * m] = (S)((w[m] / sum) * (sd - 1.0 / __dsub_rn(xi, nodes[m])));
+            } else {
+#pragma unroll
+                for (int m = 0; m < HM_RMAX; ++m)
+                    if (m < r) Pg[i + (int64_t)G.ld * m] = (S)(w[m] / sum);
+            }
         }
         col = Fi.basis_w;
     }
@@ -107,7 +120,8 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
         for (int64_t idx = threadIdx.x; idx < tot; idx += blockDim.x) {
             const int i = (int)(idx % G.nrows), j = (int)(idx / G.nrows);
             Pg[i + (int64_t)G.ld * (col + j)] =
-                (S)fill_kernel(fa, fa.x[G.row0 + i], fa.y[Q.src + j]);
+                (S)(DROW ? fill_kernel_drow(fa, fa.x[G.row0 + i], fa.y[Q.src + j])
+                         : fill_kernel(fa, fa.x[G.row0 + i], fa.y[Q.src + j]));
         }
         col += Q.width;
     }
@@ -117,8 +131,10 @@ template __global__ void fill_vpanels<double>(FillArgs, const hm_vpanel *, const
 template __global__ void fill_vpanels<float>(FillArgs, const hm_vpanel *, const hm_fill_vpanel *, int, float *);
 template __global__ void fill_f<double>(FillArgs, const hm_fill_f *, const hm_m2l_ent *, int, double *);
 template __global__ void fill_f<float>(FillArgs, const hm_fill_f *, const hm_m2l_ent *, int, float *);
-template __global__ void fill_segments<double>(FillArgs, const hm_seg *, const hm_piece *, const hm_fill_seg *, int, double *);
-template __global__ void fill_segments<float>(FillArgs, const hm_seg *, const hm_piece *, const hm_fill_seg *, int, float *);
+template __global__ void fill_segments<double, false>(FillArgs, const hm_seg *, const hm_piece *, const hm_fill_seg *, int, double *);
+template __global__ void fill_segments<float, false>(FillArgs, const hm_seg *, const hm_piece *, const hm_fill_seg *, int, float *);
+template __global__ void fill_segments<double, true>(FillArgs, const hm_seg *, const hm_piece *, const hm_fill_seg *, int, double *);
+template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, const hm_piece *, const hm_fill_seg *, int, float *);
 
 // ============================================================== matvec kernels
 //

@@ -100,6 +100,25 @@ __device__ __forceinline__ double fill_kernel(const FillArgs &fa, double row_pt,
     return fa.swap ? kernel_eval(fa.kernel, col_pt, row_pt) : kernel_eval(fa.kernel, row_pt, col_pt);
 }
 
+// d/dx of the example kernels f(x, y) = phi(x - y), in FP64.
+__device__ __forceinline__ double kernel_dx(int kid, double x, double y)
+{
+    const double d = __dsub_rn(x, y);
+    switch (kid) {
+    case 0: return -1.0 / __dmul_rn(d, d);
+    case 1: return -2.0 / __dmul_rn(__dmul_rn(d, d), d);
+    case 2: return -3.0 / __dmul_rn(__dmul_rn(d, d), __dmul_rn(d, d));
+    default: return 1.0 / d;
+    }
+}
+
+// Derivative of a matrix entry with respect to its row point.  For the
+// transposed matrix (swap) the entry is f(col, row) and d/d(row) = -phi'.
+__device__ __forceinline__ double fill_kernel_drow(const FillArgs &fa, double row_pt, double col_pt)
+{
+    return fa.swap ? -kernel_dx(fa.kernel, col_pt, row_pt) : kernel_dx(fa.kernel, row_pt, col_pt);
+}
+
 template <typename S>
 struct MulArgs {
     const S *x;      // x[(j * incx) + q * ldx]
@@ -117,7 +136,7 @@ __global__ void fill_vpanels(FillArgs fa, const hm_vpanel *vp, const hm_fill_vpa
 template <typename S>
 __global__ void fill_f(FillArgs fa, const hm_fill_f *ff, const hm_m2l_ent *ents, int nblocks, S *F);
 
-template <typename S>
+template <typename S, bool DROW>
 __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *pieces,
                               const hm_fill_seg *sf, int nsegs, S *P);
 

@@ -61,7 +61,7 @@ STAGES = ("up", "down", "expand", "far")
 
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
-    "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
+    "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
     "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create",
 )
@@ -114,6 +114,8 @@ def _load():
     L.hm_mul.argtypes = [_vp, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
     L.hm_mul_t.restype = ctypes.c_int
     L.hm_mul_t.argtypes = [_vp, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
+    L.hm_mul_drow.restype = ctypes.c_int
+    L.hm_mul_drow.argtypes = [_vp, ctypes.c_int, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
     L.hm_mul_strided.restype = ctypes.c_int
     L.hm_mul_strided.argtypes = [_vp, _vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, _vp]
     L.hm_mul_host.restype = ctypes.c_int

@@ -189,6 +189,34 @@ class KernelMatrix:
                            _stream_ptr(stream)))
         return u
 
+    def mul_drow(self, u, v, *, transposed=False, accumulate=True, stream=None):
+        """Row-derivative products on device tensors:
+        transposed=False: u (+)= D_x v with D_x[i, j] = dH[i, j]/dx_i;
+        transposed=True:  u (+)= D_y^T v with D_y[i, j] = dH[i, j]/dy_j."""
+        rows_u = self.shape[1] if transposed else self.shape[0]
+        rows_v = self.shape[0] if transposed else self.shape[1]
+        ku, ldu = self._check_dev(u, rows_u, "u")
+        kv, ldv = self._check_dev(v, rows_v, "v")
+        if ku != kv:
+            raise ValueError("u and v have different numbers of columns")
+        check(lib.hm_mul_drow(self._h, 1 if transposed else 0, v.data_ptr(), ldv, u.data_ptr(), ldu, kv,
+                              1 if accumulate else 0, _stream_ptr(stream)))
+        return u
+
+    def loss_and_grad(self, w, t):
+        """L = 1/2 |H w - t|^2 and its gradients (dL/dw, dL/dx, dL/dy) with the
+        block tree held fixed; w, t device tensors of the handle's dtype."""
+        import torch
+        r = self @ w
+        r -= t
+        loss = 0.5 * float(torch.dot(r.double(), r.double()))
+        gw = self.T @ r
+        dxw = torch.empty(self.shape[0], dtype=w.dtype, device=w.device)
+        self.mul_drow(dxw, w, accumulate=False)
+        dyr = torch.empty(self.shape[1], dtype=w.dtype, device=w.device)
+        self.mul_drow(dyr, r, transposed=True, accumulate=False)
+        return loss, gw, r * dxw, w * dyr
+
     @property
     def T(self):
         """The transpose as an operator: ``H.T @ v`` runs the transposed product."""

@@ -114,6 +114,19 @@ int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int n
 int hm_mul_t(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs,
              int accumulate, void *stream);
 
+/* Row-derivative product (no counterpart in the reference; the building
+   block of the gradients of L(x, y, w) through the kernel and the
+   barycentric factors, with the block tree held fixed):
+     transposed = 0:  u (+)= D_x v,    D_x[i, j] = d H[i, j] / d x_i
+     transposed = 1:  u (+)= D_y^T v,  D_y[i, j] = d H[i, j] / d y_j
+   Near-field entries differentiate the kernel, far-field rows the
+   barycentric basis U(x_i) (U_m' = U_m (sum_k U_k/(x - xh_k) - 1/(x - xh_m))).
+   For L = 1/2 |H w - t|^2 with r = H w - t:  dL/dx = r .* (D_x w),
+   dL/dy = w .* (D_y^T r), dL/dw = H^T r.  The derivative panels are filled
+   on the first call and kept (the same device memory as the panels). */
+int hm_mul_drow(hm_handle *h, int transposed, const void *v, int64_t ldv, void *u, int64_t ldu,
+                int nrhs, int accumulate, void *stream);
+
 /* mul!(y, H, x, istart, jstart, INCX, INCY) (src/HierarchicalMatrix.jl:24-52):
    y[istart-1 + i*incy] += (H x)[i] with x read at x[jstart-1 + j*incx]
    (1-based istart/jstart, positive strides).  lenx/leny are the array

@@ -13,6 +13,25 @@ def box_nodes(a, b, cheb):
     return ab2 + ba2 * cheb
 
 
+def kernel_dx_np(kernel, x, y):
+    d = x - y
+    if kernel == 0:
+        return -1.0 / (d * d)
+    if kernel == 1:
+        return -2.0 / ((d * d) * d)
+    if kernel == 2:
+        return -3.0 / ((d * d) * (d * d))
+    return 1.0 / d
+
+
+def basis_drow(pts, a, b, cheb, lam):
+    nodes = box_nodes(a, b, cheb)
+    diff = pts[:, None] - nodes[None, :]
+    U = basis(pts, a, b, cheb, lam)
+    sd = (U / diff).sum(axis=1, keepdims=True)
+    return U * (sd - 1.0 / diff)
+
+
 def kernel_np(kernel, x, y):
     d = x - y
     if kernel == 0:
@@ -43,11 +62,16 @@ def _banded(plan, which):
                 yield from ents[st["e0"]:st["e1"]]
 
 
-def emulate(plan, kernel, b):
-    """Returns H @ b (b: (ny,) or (ny, k)) computed from the plan tables."""
+def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
+    """Returns H @ b (b: (ny,) or (ny, k)) computed from the plan tables.
+    drow=True: the row-derivative product D b (entries differentiated with
+    respect to their row point); swap=True: entries f(col, row) (the
+    transposed matrix); x / y replace the plan's points in the entries (the
+    tree stays the plan's)."""
     S = plan.sizes
     r = S["r"]
-    x, y = plan.x, plan.y
+    x = plan.x if x is None else np.asarray(x, dtype=np.float64)
+    y = plan.y if y is None else np.asarray(y, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     squeeze = b.ndim == 1
     B = b[:, None] if squeeze else b
@@ -75,8 +99,9 @@ def emulate(plan, kernel, b):
         acc = np.zeros((r, k))
         for e in range(row["begin"], row["end"]):
             f = ff[e]
-            F = kernel_np(kernel, box_nodes(f["xa"], f["xb"], cheb)[:, None],
-                          box_nodes(f["ya"], f["yb"], cheb)[None, :])
+            xn = box_nodes(f["xa"], f["xb"], cheb)[:, None]
+            yn = box_nodes(f["ya"], f["yb"], cheb)[None, :]
+            F = kernel_np(kernel, yn, xn) if swap else kernel_np(kernel, xn, yn)
             acc += F @ t[ents[e]["yslot"]]
         s[row["slot"]] = acc
     # downward transfers in band / task / step order; a parent is final once
@@ -100,11 +125,17 @@ def emulate(plan, kernel, b):
         cols, g = [], []
         for p in pieces[sg["piece0"]:sg["piece0"] + sg["npieces"]]:
             if p["kind"] == 0:
-                cols.append(basis(x[rows], fi["a"], fi["b"], cheb, lam))
+                bf = basis_drow if drow else basis
+                cols.append(bf(x[rows], fi["a"], fi["b"], cheb, lam))
                 g.append(s[p["src"]])
             else:
                 yy = y[p["src"]:p["src"] + p["width"]]
-                cols.append(kernel_np(kernel, x[rows][:, None], yy[None, :]))
+                xr = x[rows][:, None]
+                if drow:
+                    blk = -kernel_dx_np(kernel, yy[None, :], xr) if swap else kernel_dx_np(kernel, xr, yy[None, :])
+                else:
+                    blk = kernel_np(kernel, yy[None, :], xr) if swap else kernel_np(kernel, xr, yy[None, :])
+                cols.append(blk)
                 g.append(B[p["src"]:p["src"] + p["width"]])
         if cols:
             P = np.concatenate(cols, axis=1)
