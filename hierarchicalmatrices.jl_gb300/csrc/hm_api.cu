@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
 #include <map>
 #include <thread>
@@ -307,6 +308,35 @@ struct StageTimer {
     }
 };
 
+// Uploads a flat plan (user-assembled HierarchicalMatrix) with its host-built
+// stores; nothing is computed on the device at build time.
+template <typename S>
+int build_hier_device(hm_handle *h, const Plan &P, const std::vector<double> &vs, const std::vector<double> &fs,
+                      const std::vector<double> &ps, cudaStream_t st)
+{
+    hm_vpanel *vp = nullptr;
+    HM_TRY(h->upload(&vp, P.vpanels, st));
+    h->d_vp = vp; h->n_vp = (int)P.vpanels.size();
+    HM_TRY(h->upload(&h->d_m2l_rows, P.m2l_rows, st));
+    h->n_m2l_rows = (int)P.m2l_rows.size();
+    HM_TRY(h->upload(&h->d_m2l_ents, P.m2l_ents, st));
+    HM_TRY(h->upload(&h->d_segs, P.segs, st));
+    h->n_segs = (int)P.segs.size();
+    HM_TRY(h->upload(&h->d_pieces, P.pieces, st));
+    h->up_band_ptr = P.up_band_ptr;
+    h->down_band_ptr = P.down_band_ptr;
+    h->fstride = P.fstride;
+    h->pstore_elems = P.pstore_elems;
+    std::vector<S> v(vs.begin(), vs.end()), f(fs.begin(), fs.end()), p(ps.begin(), ps.end());
+    S *dv = nullptr, *df = nullptr, *dp = nullptr;
+    HM_TRY(h->upload(&dv, v, st));
+    HM_TRY(h->upload(&df, f, st));
+    HM_TRY(h->upload(&dp, p, st));
+    h->d_V = dv; h->d_F = df; h->d_P = dp;
+    HM_CK(cudaStreamSynchronize(st));
+    return HM_OK;
+}
+
 // Raises the dynamic shared-memory limit of `kernel` when `bytes` needs it.
 // The limit set per kernel is remembered, so repeated products (and stream
 // capture after a first product) make no further attribute calls.
@@ -383,7 +413,7 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
-            const size_t smem = (size_t)kWarpsPerCta * 64 * (r + QC) * sizeof(S);
+            const size_t smem = (size_t)kWarpsPerCta * 64 * (HM_RMAX + QC) * sizeof(S);
             HM_TRY(ensure_smem(leaf_up<S, A, QC>, smem));
             leaf_up<S, A, QC><<<warp_ctas(h->n_vp * nq), 32 * kWarpsPerCta, smem, st>>>(
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
@@ -428,36 +458,36 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
 }
 
 template <typename S, typename A, bool FAR, int KB>
-int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const void *panels, cudaStream_t st)
+int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
 {
     const int maxw = std::max(h->max_width, 1);
     const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(A);
     HM_TRY(ensure_smem(expand_part<S, A, FAR, KB>, smem));
     expand_part<S, A, FAR, KB><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
-        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(panels), s, h->r, maxw);
+        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(panels), s, t, h->r, maxw);
     HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
     return HM_OK;
 }
 
 // Near-field (FAR = false) or far-field (FAR = true) panel columns for k <= 8.
 template <typename S, typename A, bool FAR>
-int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const void *panels, cudaStream_t st)
+int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
 {
-    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, panels, st);
-    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, panels, st);
-    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, panels, st);
-    return launch_part_kb<S, A, FAR, 8>(h, ma, s, panels, st);
+    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, st);
+    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, st);
+    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, st);
+    return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, st);
 }
 
 template <typename S, typename A>
-int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const void *panels, cudaStream_t st)
+int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
 {
     const int maxw = std::max(h->max_width, 1);
     const int qc = sizeof(A) == 8 ? 16 : 32;
     const size_t smem = ((size_t)64 * maxw * sizeof(S) + 31) / 32 * 32 + (size_t)maxw * qc * sizeof(A);
     HM_TRY(ensure_smem(expand_k<S, A>, smem));
     expand_k<S, A><<<h->n_segs, 128, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const S *>(panels), s,
-                                                  h->r, maxw);
+                                                  t, h->r, maxw);
     HM_CK_LAUNCH("expand_k");
     return HM_OK;
 }
@@ -491,18 +521,18 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
     if (k <= kPartMaxK) {
         {
             StageTimer tm(h, timing ? 2 : -1, st);
-            HM_TRY((launch_part<S, A, false>(h, ma, s, panels, st)));
+            HM_TRY((launch_part<S, A, false>(h, ma, s, t, panels, st)));
         }
         if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
         if (tree) {
             StageTimer tm(h, timing ? 3 : -1, st);
-            HM_TRY((launch_part<S, A, true>(h, ma, s, panels, st)));
+            HM_TRY((launch_part<S, A, true>(h, ma, s, t, panels, st)));
         }
         return HM_OK;
     }
     if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
     StageTimer tm(h, timing ? 2 : -1, st);
-    return launch_expand_k<S, A>(h, ma, s, panels, st);
+    return launch_expand_k<S, A>(h, ma, s, t, panels, st);
 }
 
 template <typename S, typename A>
@@ -856,12 +886,184 @@ int hm_kernelmatrix_batch_build(int kernel, int ninst, const int64_t *nx, const 
     return st;
 }
 
+int hm_hier_build(int storage, int64_t m, int64_t n, int nblocks, const int32_t *kinds, const int64_t *row0,
+                  const int64_t *rows, const int64_t *col0, const int64_t *cols, const int64_t *ranks,
+                  const double *values, const int64_t *offsets, void *stream, hm_handle **out)
+{
+    g_last_error.clear();
+    if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
+    *out = nullptr;
+    if (storage != HM_F64 && storage != HM_F32) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
+    if (m < 0 || n < 0 || nblocks < 0 || (nblocks && (!kinds || !row0 || !rows || !col0 || !cols || !ranks || !values || !offsets))) {
+        set_error("hm_hier_build: bad arguments");
+        return HM_ERR_INVALID_ARG;
+    }
+    if (m >= (int64_t)1 << 31 || n >= (int64_t)1 << 31) { set_error("more than 2^31 rows or columns"); return HM_ERR_UNSUPPORTED; }
+    std::vector<HierBlock> blocks(nblocks);
+    for (int i = 0; i < nblocks; ++i) {
+        HierBlock &b = blocks[i];
+        b.kind = kinds[i]; b.row0 = row0[i]; b.rows = rows[i]; b.col0 = col0[i]; b.cols = cols[i];
+        b.rank = b.kind == 0 ? 0 : ranks[i];
+        b.data = values + offsets[i];
+        if (b.kind < 0 || b.kind > 2 || b.rows < 0 || b.cols < 0 || b.rank < 0) {
+            set_error("block %d: bad kind or size", i);
+            return HM_ERR_INVALID_ARG;
+        }
+        if (b.row0 < 0 || b.col0 < 0 || b.row0 + b.rows > m || b.col0 + b.cols > n) {
+            set_error("block %d: rows [%lld, %lld) or columns [%lld, %lld) outside the %lld x %lld matrix", i,
+                      (long long)b.row0, (long long)(b.row0 + b.rows), (long long)b.col0, (long long)(b.col0 + b.cols),
+                      (long long)m, (long long)n);
+            return HM_ERR_BOUNDS;
+        }
+    }
+    Plan P;
+    std::vector<double> vs, fs, ps;
+    if (build_hier_plan(m, n, blocks, P, vs, fs, ps)) {
+        set_error("core (BarycentricMatrix2D) blocks need rank <= 32 in a matrix whose ranks are all <= 32");
+        return HM_ERR_UNSUPPORTED;
+    }
+    hm_handle *h = new hm_handle();
+    h->kernel = -1; h->storage = storage; h->r = P.r; h->nx = m; h->ny = n;
+    h->stats = P.stats;
+    h->n_xslots = P.n_xslots; h->n_yslots = P.n_yslots; h->max_width = P.max_width;
+    h->ninst = 0;       // no transposed or derivative plans for user-assembled matrices
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    const int st = storage == HM_F64 ? build_hier_device<double>(h, P, vs, fs, ps, cs)
+                                     : build_hier_device<float>(h, P, vs, fs, ps, cs);
+    h->launches_per_mul = (h->n_vp > 0) + (h->n_m2l_rows > 0) + (h->n_segs > 0) * (1 + (h->n_vp > 0));
+    if (st) { hm_free(h); return st; }
+    *out = h;
+    return HM_OK;
+}
+
+// ---- block-level products on device arrays -----------------------------------
+
+static int check_strided(int64_t len, int64_t start, int64_t inc, int64_t count, const char *name)
+{
+    if (start < 1 || inc < 1) { set_error("%s: start and increment must be >= 1", name); return HM_ERR_INVALID_ARG; }
+    if (count > 0 && (start - 1) + (count - 1) * inc >= len) {
+        set_error("%s: strided access past the end (length %lld)", name, (long long)len);
+        return HM_ERR_BOUNDS;
+    }
+    return HM_OK;
+}
+
+int hm_dense_mul(int trans, int dtype, const void *A, int64_t m, int64_t n, int64_t lda, const void *x, int64_t lenx,
+                 int64_t jstart, int64_t incx, void *y, int64_t leny, int64_t istart, int64_t incy, void *stream)
+{
+    g_last_error.clear();
+    if (!A || !x || !y || m < 0 || n < 0 || lda < std::max<int64_t>(m, 1)) { set_error("hm_dense_mul: bad arguments"); return HM_ERR_INVALID_ARG; }
+    if (dtype != HM_F64 && dtype != HM_F32) { set_error("unknown dtype %d", dtype); return HM_ERR_UNSUPPORTED; }
+    const int64_t nin = trans ? m : n, nout = trans ? n : m;
+    HM_TRY(check_strided(lenx, jstart, incx, nin, "x"));
+    HM_TRY(check_strided(leny, istart, incy, nout, "y"));
+    if (nout == 0) return HM_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t es = dtype == HM_F64 ? 8 : 4;
+    const void *xb = static_cast<const char *>(x) + (size_t)(jstart - 1) * es;
+    void *yb = static_cast<char *>(y) + (size_t)(istart - 1) * es;
+    if (!trans) {
+        const unsigned grid = (unsigned)((m + 255) / 256);
+        if (dtype == HM_F64) gemv_n<double><<<grid, 256, 0, st>>>((const double *)A, m, n, lda, (const double *)xb, incx, (double *)yb, incy);
+        else gemv_n<float><<<grid, 256, 0, st>>>((const float *)A, m, n, lda, (const float *)xb, incx, (float *)yb, incy);
+    } else {
+        const unsigned grid = (unsigned)((n * 32 + 255) / 256);
+        if (dtype == HM_F64) gemv_t<double><<<grid, 256, 0, st>>>((const double *)A, m, n, lda, (const double *)xb, incx, (double *)yb, incy);
+        else gemv_t<float><<<grid, 256, 0, st>>>((const float *)A, m, n, lda, (const float *)xb, incx, (float *)yb, incy);
+    }
+    HM_CK_LAUNCH("hm_dense_mul");
+    return HM_OK;
+}
+
+}  // extern "C"
+
+template <typename T>
+static int lowrank_mul_t(int adjoint, const T *U, const T *core, int core_diag, const T *V, int64_t m, int64_t n,
+                         int64_t r, const T *x, int64_t incx, T *y, int64_t incy, cudaStream_t st)
+{
+    // product:  t = V^T x, y += U (C t);  adjoint:  t = U^T x, y += V (C^T t)
+    const T *Win = adjoint ? U : V, *Wout = adjoint ? V : U;
+    const int64_t rin = adjoint ? m : n, rout = adjoint ? n : m;
+    if (r == 0 || rout == 0) return HM_OK;
+    T *t = nullptr;
+    HM_CK(cudaMallocAsync((void **)&t, sizeof(T) * r, st));
+    lr_project<T><<<(unsigned)((r * 32 + 255) / 256), 256, 0, st>>>(Win, rin, rin, r, x, incx, t);
+    int e = cuda_status(cudaGetLastError(), "lr_project");
+    if (!e) {
+        const size_t smem = sizeof(T) * r;
+        if (smem > 48 * 1024) e = cuda_status(cudaFuncSetAttribute(lr_expand<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(smem, 227 * 1024)), "lr_expand attribute");
+        if (!e && smem > 227 * 1024) { set_error("rank %lld too large", (long long)r); e = HM_ERR_UNSUPPORTED; }
+        if (!e) {
+            lr_expand<T><<<(unsigned)((rout + 255) / 256), 256, smem, st>>>(Wout, rout, rout, r, core, core_diag, adjoint, t, y, incy);
+            e = cuda_status(cudaGetLastError(), "lr_expand");
+        }
+    }
+    cudaError_t fe = cudaFreeAsync(t, st);
+    if (!e) e = cuda_status(fe, "cudaFreeAsync");
+    return e;
+}
+
+extern "C" {
+
+int hm_lowrank_mul(int adjoint, int dtype, const void *U, const void *core, int core_diag, const void *V, int64_t m,
+                   int64_t n, int64_t r, const void *x, int64_t lenx, int64_t jstart, int64_t incx, void *y,
+                   int64_t leny, int64_t istart, int64_t incy, void *stream)
+{
+    g_last_error.clear();
+    if (!U || !core || !V || !x || !y || m < 0 || n < 0 || r < 0) { set_error("hm_lowrank_mul: bad arguments"); return HM_ERR_INVALID_ARG; }
+    if (dtype != HM_F64 && dtype != HM_F32) { set_error("unknown dtype %d", dtype); return HM_ERR_UNSUPPORTED; }
+    const int64_t nin = adjoint ? m : n, nout = adjoint ? n : m;
+    HM_TRY(check_strided(lenx, jstart, incx, nin, "x"));
+    HM_TRY(check_strided(leny, istart, incy, nout, "y"));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dtype == HM_F64)
+        return lowrank_mul_t<double>(adjoint, (const double *)U, (const double *)core, core_diag, (const double *)V, m, n, r,
+                                     (const double *)x + (jstart - 1), incx, (double *)y + (istart - 1), incy, st);
+    return lowrank_mul_t<float>(adjoint, (const float *)U, (const float *)core, core_diag, (const float *)V, m, n, r,
+                                (const float *)x + (jstart - 1), incx, (float *)y + (istart - 1), incy, st);
+}
+
+int hm_bary_factors(int kernel, int rank, double a, double b, double c, double d, const double *x, int64_t nx,
+                    const double *y, int64_t ny, int dtype, void *U, void *F, void *V, void *stream)
+{
+    g_last_error.clear();
+    if (kernel < HM_KERNEL_CAUCHY || kernel > HM_KERNEL_LOG) { set_error("unknown kernel %d", kernel); return HM_ERR_UNSUPPORTED; }
+    if (dtype != HM_F64 && dtype != HM_F32) { set_error("unknown dtype %d", dtype); return HM_ERR_UNSUPPORTED; }
+    if (rank < 1 || rank > HM_RMAX) { set_error("rank %d outside 1..%d", rank, HM_RMAX); return HM_ERR_UNSUPPORTED; }
+    if (!x || !y || !U || !F || !V || nx < 0 || ny < 0) { set_error("hm_bary_factors: bad arguments"); return HM_ERR_INVALID_ARG; }
+    std::vector<double> cheb, lam;
+    chebyshev_first_kind(rank, cheb, lam);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double *dbuf = nullptr;
+    const size_t nbuf = 2 * (size_t)rank + nx + ny;
+    HM_CK(cudaMallocAsync((void **)&dbuf, sizeof(double) * std::max<size_t>(nbuf, 1), st));
+    int e = cuda_status(cudaMemcpyAsync(dbuf, cheb.data(), sizeof(double) * rank, cudaMemcpyHostToDevice, st), "copy");
+    if (!e) e = cuda_status(cudaMemcpyAsync(dbuf + rank, lam.data(), sizeof(double) * rank, cudaMemcpyHostToDevice, st), "copy");
+    if (!e && nx) e = cuda_status(cudaMemcpyAsync(dbuf + 2 * rank, x, sizeof(double) * nx, cudaMemcpyHostToDevice, st), "copy");
+    if (!e && ny) e = cuda_status(cudaMemcpyAsync(dbuf + 2 * rank + nx, y, sizeof(double) * ny, cudaMemcpyHostToDevice, st), "copy");
+    if (!e) {
+        const int64_t work = std::max<int64_t>({(int64_t)rank * rank, nx, ny});
+        const unsigned grid = (unsigned)((work + 127) / 128);
+        if (dtype == HM_F64)
+            bary_factors<double><<<grid, 128, 0, st>>>(kernel, rank, a, b, c, d, dbuf, dbuf + rank, dbuf + 2 * rank, nx,
+                                                       dbuf + 2 * rank + nx, ny, (double *)U, (double *)F, (double *)V);
+        else
+            bary_factors<float><<<grid, 128, 0, st>>>(kernel, rank, a, b, c, d, dbuf, dbuf + rank, dbuf + 2 * rank, nx,
+                                                      dbuf + 2 * rank + nx, ny, (float *)U, (float *)F, (float *)V);
+        e = cuda_status(cudaGetLastError(), "bary_factors");
+    }
+    cudaError_t fe = cudaFreeAsync(dbuf, st);
+    if (!e) e = cuda_status(fe, "cudaFreeAsync");
+    if (!e) e = cuda_status(cudaStreamSynchronize(st), "bary_factors sync");
+    return e;
+}
+
 int hm_mul_t(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs, int accumulate,
              void *stream)
 {
     g_last_error.clear();
     if (!h) { set_error("NULL handle"); return HM_ERR_INVALID_ARG; }
-    if (h->ninst > 1 || h->hx.empty()) { set_error("hm_mul_t: not available for batched handles"); return HM_ERR_UNSUPPORTED; }
+    if (h->ninst != 1 || h->hx.empty()) { set_error("hm_mul_t: not available for batched or user-assembled handles"); return HM_ERR_UNSUPPORTED; }
     {
         std::lock_guard<std::mutex> lk(h->trans_mu);
         if (!h->trans) {
@@ -912,7 +1114,7 @@ int hm_mul_drow(hm_handle *h, int transposed, const void *v, int64_t ldv, void *
     g_last_error.clear();
     if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
     if (transposed) {
-        if (h->ninst > 1 || h->hx.empty()) { set_error("transposed products are not available for batched handles"); return HM_ERR_UNSUPPORTED; }
+        if (h->ninst != 1 || h->hx.empty()) { set_error("transposed products are not available for batched or user-assembled handles"); return HM_ERR_UNSUPPORTED; }
         {
             std::lock_guard<std::mutex> lk(h->trans_mu);
             if (!h->trans)
@@ -922,6 +1124,7 @@ int hm_mul_drow(hm_handle *h, int transposed, const void *v, int64_t ldv, void *
         }
         return hm_mul_drow(h->trans, 0, v, ldv, u, ldu, nrhs, accumulate, stream);
     }
+    if (h->kernel < 0) { set_error("derivative products need a KernelMatrix handle"); return HM_ERR_UNSUPPORTED; }
     if (nrhs < 0) { set_error("nrhs < 0"); return HM_ERR_INVALID_ARG; }
     if (nrhs > 1 && (ldv < h->ny || ldu < h->nx)) { set_error("leading dimension too small"); return HM_ERR_BOUNDS; }
     cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -144,12 +144,13 @@ template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, co
 // near-field dense panels on the caller's stream; after the join
 // expand_part<.., true> adds the far field U s.
 
-// t[leaf] = V^T x for each explicit column basis panel.  One warp per
-// (panel, chunk of QC right-hand sides); lane m owns basis column m of the
-// row-major panel.  Panels of up to 64 rows are staged in shared memory
-// (16-byte loads by all lanes) together with the chunk's x values; longer
-// panels are read directly.  QC = 1 accumulates with compensated sums in
-// FP32, QC > 1 with plain FMA.
+// t[slot][col0 + m] = (V^T x)[m] for each explicit basis panel.  One warp
+// per (panel, chunk of QC right-hand sides); lane m owns column m of the
+// row-major panel (width <= 32, row stride ld).  Panels of up to 64 rows are
+// staged in shared memory (16-byte loads by all lanes) together with the
+// chunk's x values; longer panels are read directly.  QC = 1 accumulates with
+// compensated sums in FP32, QC > 1 with plain FMA.  Coefficients of a slot
+// are r apart per right-hand side.
 template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r)
 {
@@ -161,16 +162,17 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
     if (w >= (int64_t)npanels * nq) return;
     const hm_vpanel P = vp[w / nq];
     const int q0 = (int)(w % nq) * QC, qc = min(QC, ma.k - q0);
+    const int pw = P.width;
     const S *Vp = V + P.off;
     using AccT = typename std::conditional<QC == 1, Acc<A>, PlainAcc<A>>::type;
     AccT acc[QC];
 #pragma unroll
     for (int qq = 0; qq < QC; ++qq) acc[qq].zero();
-    if (P.nrows <= 64) {
-        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * (64 * r + 64 * QC);
-        A *xs = reinterpret_cast<A *>(Vs + 64 * r);          // xs[j * QC + qq]
-        const int nel = P.nrows * r;
-        if (sizeof(S) * nel % 16 == 0) {
+    if (P.nrows <= 64 && P.ld == pw) {
+        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * (64 * HM_RMAX + 64 * QC);
+        A *xs = reinterpret_cast<A *>(Vs + 64 * HM_RMAX);    // xs[j * QC + qq]
+        const int nel = P.nrows * pw;
+        if (sizeof(S) * nel % 16 == 0 && (P.off * sizeof(S)) % 16 == 0) {
             const float4 *src = reinterpret_cast<const float4 *>(Vp);
             float4 *dst = reinterpret_cast<float4 *>(Vs);
             for (int i = lane; i < (int)(nel * sizeof(S) / 16); i += 32) dst[i] = __ldcs(src + i);
@@ -182,14 +184,14 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
             xs[i] = qq < qc ? (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx] : (A)0;
         }
         __syncwarp();
-        if (lane < r) {
+        if (lane < pw) {
             for (int j = 0; j < P.nrows; ++j) {
-                const A v = (A)Vs[j * r + lane];
+                const A v = (A)Vs[j * pw + lane];
 #pragma unroll
                 for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xs[j * QC + qq]);
             }
         }
-    } else if (lane < r) {
+    } else if (lane < pw) {
         const S *col = Vp + lane;
         for (int j = 0; j < P.nrows; ++j) {
             const A v = (A)col[(int64_t)j * P.ld];
@@ -198,10 +200,10 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
                 if (qq < qc) acc[qq].add(v, (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx]);
         }
     }
-    if (lane < r) {
+    if (lane < pw) {
 #pragma unroll
         for (int qq = 0; qq < QC; ++qq)
-            if (qq < qc) t[((int64_t)P.slot * ma.k + q0 + qq) * r + lane] = acc[qq].value();
+            if (qq < qc) t[((int64_t)P.slot * ma.k + q0 + qq) * r + P.col0 + lane] = acc[qq].value();
     }
 }
 
@@ -409,7 +411,7 @@ struct SegAcc {
 
 template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                            const A *s, int r, int maxw)
+                            const A *s, const A *t, int r, int maxw)
 {
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -424,14 +426,15 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
     int c0 = -1, c1 = 0, col = 0;
     for (int pc = 0; pc < G.npieces; ++pc) {
         const hm_piece Q = pieces[G.piece0 + pc];
-        const bool take = FAR ? (Q.kind == HM_PIECE_COEF) : (Q.kind == HM_PIECE_X);
+        const bool take = FAR ? (Q.kind != HM_PIECE_X) : (Q.kind == HM_PIECE_X);
         if (take) {
             if (c0 < 0) { c0 = col; pcs[0] = pc; }
+            const A *coef = Q.kind == HM_PIECE_TCOEF ? t : s;
             for (int i = lane; i < Q.width * KB; i += 32) {
                 const int c = i / KB, q = i % KB;
                 A v = 0;
                 if (q < k)
-                    v = FAR ? s[((int64_t)Q.src * k + q) * r + c]
+                    v = FAR ? coef[((int64_t)Q.src * k + q) * r + c]
                             : (A)ma.x[(Q.src + c) * ma.incx + (int64_t)q * ma.ldx];
                 g[(col + c) * KB + q] = v;
             }
@@ -588,8 +591,8 @@ __device__ __forceinline__ void comp_add(A &hi, A &lo, A v)
 }
 
 template <typename S, typename A>
-__global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s, int r,
-                         int maxw)
+__global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s,
+                         const A *t, int r, int maxw)
 {
     constexpr int RB = KTile<A>::RB, QB = KTile<A>::QB, RG = KTile<A>::RG, QG = KTile<A>::QG;
     constexpr int QC = QB * QG;
@@ -614,10 +617,10 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                 const int c = idx / QC, qq = idx % QC;
                 A v = 0;
                 if (qq < qc) {
-                    if (Q.kind == HM_PIECE_COEF)
-                        v = s[((int64_t)Q.src * ma.k + q0 + qq) * r + c];
-                    else
+                    if (Q.kind == HM_PIECE_X)
                         v = (A)ma.x[(Q.src + c) * ma.incx + (int64_t)(q0 + qq) * ma.ldx];
+                    else
+                        v = (Q.kind == HM_PIECE_TCOEF ? t : s)[((int64_t)Q.src * ma.k + q0 + qq) * r + c];
                 }
                 Gs[(col + c) * QC + qq] = v;
             }
@@ -672,9 +675,9 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
 
 #define HM_INST_PART(S, A, KB)                                                                       \
     template __global__ void expand_part<S, A, false, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *, \
-                                                          const S *, const A *, int, int);              \
+                                                          const S *, const A *, const A *, int, int);   \
     template __global__ void expand_part<S, A, true, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
-                                                         const S *, const A *, int, int);
+                                                         const S *, const A *, const A *, int, int);
 #define HM_INST_MV(S, A)                                                                             \
     template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
     template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
@@ -684,7 +687,7 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                           const A *, A *, int, int);                                    \
     HM_INST_PART(S, A, 1) HM_INST_PART(S, A, 2) HM_INST_PART(S, A, 4) HM_INST_PART(S, A, 8)               \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
-                                            const A *, int, int);                                       \
+                                            const A *, const A *, int, int);                            \
     template __global__ void xfer_up_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
                                                 A *, int, int);                                         \
     template __global__ void xfer_up_band<A, 8>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \

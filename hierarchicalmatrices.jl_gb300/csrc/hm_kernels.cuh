@@ -159,11 +159,27 @@ __global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const
 
 template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                            const A *s, int r, int maxw);
+                            const A *s, const A *t, int r, int maxw);
 
 template <typename S, typename A>
-__global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s, int r,
-                         int maxw);
+__global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s,
+                         const A *t, int r, int maxw);
+
+// ---------------------------------------------------------------- block-level (hm_blocks.cu)
+
+template <typename T>
+__global__ void gemv_n(const T *A, int64_t m, int64_t n, int64_t lda, const T *x, int64_t incx, T *y, int64_t incy);
+template <typename T>
+__global__ void gemv_t(const T *A, int64_t m, int64_t n, int64_t lda, const T *x, int64_t incx, T *y, int64_t incy);
+template <typename T>
+__global__ void lr_project(const T *W, int64_t rows, int64_t ldw, int64_t r, const T *x, int64_t incx, T *t);
+template <typename T>
+__global__ void lr_expand(const T *W, int64_t rows, int64_t ldw, int64_t r, const T *core, int core_diag,
+                          int core_trans, const T *t, T *y, int64_t incy);
+template <typename T>
+__global__ void bary_factors(int kernel, int r, double a, double b, double c, double d, const double *cheb,
+                             const double *lam, const double *x, int64_t nx, const double *y, int64_t ny, T *U, T *F,
+                             T *V);
 
 // ---------------------------------------------------------------- direct sums
 

@@ -259,6 +259,8 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
             vp.ld = r;                         // row-major: r values per point
             vp.width = r;
             vp.slot = n.slot;
+            vp.col0 = 0;
+            vp.pad = 0;
             vp.off = off;
             off += round_up((int64_t)vp.nrows * r, 32);
             P.vpanels.push_back(vp);
@@ -482,6 +484,138 @@ void merge_plans(const std::vector<Plan> &parts, Plan &P)
     // level tables are per instance only; the merged plan keeps them empty
     P.up_level_ptr.assign(1, 0);
     P.down_level_ptr.assign(1, 0);
+}
+
+int build_hier_plan(int64_t m, int64_t n, const std::vector<HierBlock> &blocks, Plan &P,
+                    std::vector<double> &vstore, std::vector<double> &fstore, std::vector<double> &pstore)
+{
+    P = Plan();
+    P.nx = m; P.ny = n;
+    int R = 1;
+    bool has_core = false;
+    for (const HierBlock &b : blocks) {
+        if (b.kind != 0) R = std::max<int64_t>(R, b.rank);
+        if (b.kind == 2) has_core = true;
+    }
+    if (has_core && R > 32) return PLAN_ERR_DEGENERATE;
+    P.r = R;
+    P.fstride = (int)round_up((int64_t)R * R, 4);
+    std::vector<int> slot(blocks.size(), -1);
+    int ns = 0;
+    vstore.clear(); fstore.clear(); pstore.clear();
+    for (size_t i = 0; i < blocks.size(); ++i) {
+        const HierBlock &b = blocks[i];
+        if (b.kind == 0 || b.rank <= 0 || b.rows <= 0 || b.cols <= 0) continue;
+        slot[i] = ns++;
+        // basis panel(s): V (diag(sigma) folded in for low-rank blocks), row-major, <= 32 columns each
+        const double *V = b.kind == 1 ? b.data + b.rows * b.rank + b.rank : b.data + b.rows * b.rank + b.rank * b.rank;
+        const double *sig = b.kind == 1 ? b.data + b.rows * b.rank : nullptr;
+        for (int64_t c0 = 0; c0 < b.rank; c0 += 32) {
+            const int w = (int)std::min<int64_t>(32, b.rank - c0);
+            hm_vpanel vp;
+            vp.row0 = b.col0; vp.nrows = (int32_t)b.cols; vp.ld = w; vp.width = w; vp.slot = slot[i];
+            vp.col0 = (int32_t)c0; vp.pad = 0;
+            vp.off = (int64_t)vstore.size();
+            for (int64_t j = 0; j < b.cols; ++j)
+                for (int c = 0; c < w; ++c) {
+                    double v = V[j + b.cols * (c0 + c)];
+                    if (sig) v *= sig[c0 + c];
+                    vstore.push_back(v);
+                }
+            vstore.resize(round_up((int64_t)vstore.size(), 32), 0.0);
+            P.vpanels.push_back(vp);
+        }
+        if (b.kind == 2) {
+            hm_m2l_ent e;
+            e.foff = (int64_t)fstore.size(); e.yslot = slot[i]; e.pad = 0;
+            fstore.resize(fstore.size() + P.fstride, 0.0);
+            const double *C = b.data + b.rows * b.rank;
+            for (int64_t q = 0; q < b.rank; ++q)
+                for (int64_t p = 0; p < b.rank; ++p) fstore[e.foff + p + R * q] = C[p + b.rank * q];
+            P.m2l_rows.push_back({slot[i], (int32_t)P.m2l_ents.size(), (int32_t)P.m2l_ents.size() + 1, 0});
+            P.m2l_ents.push_back(e);
+            P.stats.n_bary += 1;
+        }
+    }
+    P.n_xslots = P.n_yslots = ns;
+    P.vstore_elems = (int64_t)vstore.size();
+    P.fstore_elems = (int64_t)fstore.size();
+    // elementary row intervals
+    std::vector<int64_t> cuts = {0, m};
+    for (const HierBlock &b : blocks)
+        if (b.rows > 0 && b.cols > 0 && (b.kind == 0 || b.rank > 0)) {
+            cuts.push_back(std::min(std::max<int64_t>(b.row0, 0), m));
+            cuts.push_back(std::min(std::max<int64_t>(b.row0 + b.rows, 0), m));
+        }
+    std::sort(cuts.begin(), cuts.end());
+    cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+    const size_t nint = cuts.size() - 1;
+    std::vector<std::vector<int>> cover(nint);
+    for (size_t i = 0; i < blocks.size(); ++i) {
+        const HierBlock &b = blocks[i];
+        if (b.rows <= 0 || b.cols <= 0 || (b.kind != 0 && b.rank <= 0)) continue;
+        const size_t i0 = std::lower_bound(cuts.begin(), cuts.end(), b.row0) - cuts.begin();
+        const size_t i1 = std::lower_bound(cuts.begin(), cuts.end(), b.row0 + b.rows) - cuts.begin();
+        for (size_t iv = i0; iv < i1; ++iv) cover[iv].push_back((int)i);
+    }
+    const int seg_rows = 64;
+    for (size_t iv = 0; iv < nint; ++iv) {
+        const int64_t p0 = cuts[iv], q0 = cuts[iv + 1];
+        if (q0 <= p0) continue;
+        // far-field pieces first, then dense pieces (each part is a contiguous column run)
+        std::vector<int> order;
+        for (int i : cover[iv]) if (blocks[i].kind != 0) order.push_back(i);
+        for (int i : cover[iv]) if (blocks[i].kind == 0) order.push_back(i);
+        for (int64_t r0 = p0; r0 < q0; r0 += seg_rows) {
+            hm_seg g;
+            g.row0 = r0;
+            g.nrows = (int32_t)std::min<int64_t>(seg_rows, q0 - r0);
+            g.ld = (int32_t)round_up(g.nrows, 4);
+            g.piece0 = (int32_t)P.pieces.size();
+            g.width = 0;
+            g.pad = 0;
+            for (int i : order) {
+                const HierBlock &b = blocks[i];
+                hm_piece pc;
+                if (b.kind == 0) { pc.kind = HM_PIECE_X; pc.src = b.col0; pc.width = (int32_t)b.cols; }
+                else { pc.kind = b.kind == 1 ? HM_PIECE_TCOEF : HM_PIECE_COEF; pc.src = slot[i]; pc.width = (int32_t)b.rank; }
+                P.pieces.push_back(pc);
+                g.width += pc.width;
+            }
+            g.npieces = (int32_t)P.pieces.size() - g.piece0;
+            g.poff = (int64_t)pstore.size();
+            pstore.resize(pstore.size() + round_up((int64_t)g.ld * std::max(g.width, 1), 32), 0.0);
+            int col = 0;
+            for (int i : order) {
+                const HierBlock &b = blocks[i];
+                const int64_t w = b.kind == 0 ? b.cols : b.rank;
+                const int64_t ldb = b.rows;          // A (rows x cols) or U (rows x r), column-major
+                for (int64_t c = 0; c < w; ++c)
+                    for (int rr = 0; rr < g.nrows; ++rr)
+                        pstore[g.poff + rr + (int64_t)g.ld * (col + c)] = b.data[(r0 + rr - b.row0) + ldb * c];
+                col += (int)w;
+            }
+            P.max_width = std::max(P.max_width, g.width);
+            P.segs.push_back(g);
+            P.seg_fill.push_back({0.0, 0.0, 0, 0});
+        }
+    }
+    P.pstore_elems = (int64_t)pstore.size();
+    P.up_band_ptr.assign(1, 0);
+    P.down_band_ptr.assign(1, 0);
+    P.up_level_ptr.assign(1, 0);
+    P.down_level_ptr.assign(1, 0);
+    PlanStats &S = P.stats;
+    S.n_xslots = S.n_yslots = ns;
+    for (const HierBlock &b : blocks) {
+        if (b.kind == 0) { S.n_dense += 1; S.dense_values += b.rows * b.cols; }
+        S.reference_values += b.kind == 0 ? b.rows * b.cols : (b.rows + b.cols) * b.rank + (b.kind == 1 ? b.rank : b.rank * b.rank);
+    }
+    S.canonical_values = S.reference_values;
+    S.stored_values = P.vstore_elems + P.fstore_elems + P.pstore_elems;
+    S.n_segments = (int64_t)P.segs.size();
+    S.max_width = P.max_width;
+    return PLAN_OK;
 }
 
 }  // namespace hm

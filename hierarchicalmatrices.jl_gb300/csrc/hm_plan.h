@@ -89,6 +89,25 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
 
 constexpr int kBandLevels = 4;   // tree levels per transfer band
 
+// A user-assembled HierarchicalMatrix flattened to leaf blocks (the block
+// walk of src/HierarchicalMatrix.jl:24-52 gives each leaf its row and column
+// offsets).  kind 0: dense A (rows x cols, column-major); kind 1: LowRankMatrix
+// U diag(sigma) V^T (src/LowRankMatrix.jl:28-33; U rows x r, sigma r, V cols x r,
+// contiguous); kind 2: U C V^T with an r x r core C (a BarycentricMatrix2D,
+// src/BarycentricMatrix.jl:208-218, r <= 32).
+struct HierBlock {
+    int kind;
+    int64_t row0, rows, col0, cols, rank;
+    const double *data;
+};
+
+// Builds the flat plan and the host stores (panels, V, F) in FP64:
+// low-rank blocks become coefficient slots whose basis panel is V diag(sigma)
+// (read back by TCOEF pieces), core blocks slots whose far-field stage applies
+// C, and rows are cut into the elementary intervals of all block row ranges.
+int build_hier_plan(int64_t m, int64_t n, const std::vector<HierBlock> &blocks, Plan &P,
+                    std::vector<double> &vstore, std::vector<double> &fstore, std::vector<double> &pstore);
+
 // Merges independent plans into one block-diagonal plan: instance i's rows
 // and columns follow those of instances 0..i-1, its slots, stores and records
 // are offset accordingly, and the transfer bands are merged launch by launch

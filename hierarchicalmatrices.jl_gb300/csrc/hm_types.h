@@ -18,13 +18,15 @@
 #pragma once
 #include <stdint.h>
 
-struct hm_vpanel {      // explicit basis panel: coef[slot] = P^T x[row0 : row0+nrows)
+struct hm_vpanel {      // explicit basis panel: coef[slot][col0 + m] = (P^T x[row0 : row0+nrows))[m]
     int64_t row0;       // first row of x (element index before stride)
     int64_t off;        // element offset of the panel in the V store
     int32_t nrows;
-    int32_t ld;         // leading dimension of the column-major panel
-    int32_t width;      // number of basis columns (<= slot width)
+    int32_t ld;         // row stride of the row-major panel
+    int32_t width;      // number of basis columns (<= 32)
     int32_t slot;
+    int32_t col0;       // first coefficient of the slot this panel produces
+    int32_t pad;
 };
 
 struct hm_xfer {        // coefficient transfer between a node and its two children
@@ -58,7 +60,11 @@ struct hm_seg {         // y[row0 : row0+nrows) (+)= panel * gathered rhs
     int32_t pad;
 };
 
-enum { HM_PIECE_COEF = 0, HM_PIECE_X = 1 };
+enum {
+    HM_PIECE_COEF = 0,   // far-field coefficients s[slot] (after the far-field stage)
+    HM_PIECE_X = 1,      // a run of x
+    HM_PIECE_TCOEF = 2   // coefficients t[slot] straight from a basis panel (low-rank blocks)
+};
 
 struct hm_piece {       // one block column run of a segment panel
     int64_t src;        // coefficient slot (COEF) or first x element (X)

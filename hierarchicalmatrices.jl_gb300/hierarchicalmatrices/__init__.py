@@ -1,15 +1,21 @@
 """GB300-native hierarchical matrices (the hot path of HierarchicalMatrices.jl).
 
 Public names follow the Julia module (src/HierarchicalMatrices.jl:22-26 and
-examples/Kernel.jl): ``BLOCKRANK``, ``BLOCKSIZE``, ``indsplit``,
-``KernelMatrix``, the example kernels and ``mul_`` (Julia's ``mul!``).
-All products run CUDA kernels compiled for sm_103a in libhmgpu.so.
+examples/Kernel.jl): ``BLOCKRANK``, ``BLOCKSIZE``, ``Block``, ``hierarchical``
+(the @hierarchical macro), ``HierarchicalMatrix``, ``LowRankMatrix``,
+``BarycentricMatrix2D``, ``KernelMatrix``, ``indsplit``, the example kernels
+and ``mul_`` (Julia's ``mul!``).  All products run CUDA kernels compiled for
+sm_103a in libhmgpu.so.
 """
 from ._lib import HMError, Plan
+from .hierarchical import (AbstractHierarchical, Adjoint, BarycentricMatrix2D, Block, HierarchicalMatrix,
+                           LowRankMatrix, Transpose, adjoint, hierarchical, mul_, transpose)
 from .kernelmatrix import (BLOCKRANK, BLOCKSIZE, KERNELS, KernelMatrix, KernelMatrixBatch, cauchykernel,
-                           coulombkernel, coulombprimekernel, indsplit, logkernel, mul_)
+                           coulombkernel, coulombprimekernel, indsplit, logkernel)
 
 __all__ = [
-    "BLOCKRANK", "BLOCKSIZE", "HMError", "KERNELS", "KernelMatrix", "KernelMatrixBatch", "Plan", "cauchykernel",
-    "coulombkernel", "coulombprimekernel", "indsplit", "logkernel", "mul_",
+    "AbstractHierarchical", "Adjoint", "BLOCKRANK", "BLOCKSIZE", "BarycentricMatrix2D", "Block", "HMError",
+    "HierarchicalMatrix", "KERNELS", "KernelMatrix", "KernelMatrixBatch", "LowRankMatrix", "Plan", "Transpose",
+    "adjoint", "cauchykernel", "coulombkernel", "coulombprimekernel", "hierarchical", "indsplit", "logkernel",
+    "mul_", "transpose",
 ]

@@ -29,7 +29,7 @@ HM_OPT_OVERLAP = 1
 
 # Records of csrc/hm_types.h.
 VPANEL = np.dtype([("row0", "<i8"), ("off", "<i8"), ("nrows", "<i4"), ("ld", "<i4"),
-                   ("width", "<i4"), ("slot", "<i4")])
+                   ("width", "<i4"), ("slot", "<i4"), ("col0", "<i4"), ("pad", "<i4")])
 XFER = np.dtype([("slot", "<i4"), ("c0", "<i4"), ("c1", "<i4"), ("pad", "<i4")])
 STEP = np.dtype([("e0", "<i4"), ("e1", "<i4")])
 TASK = np.dtype([("step0", "<i4"), ("step1", "<i4")])
@@ -63,7 +63,8 @@ EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
     "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
     "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
-    "hm_plan_free", "hm_batch_plan_create",
+    "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
+    "hm_bary_factors",
 )
 
 _d = ctypes.POINTER(ctypes.c_double)
@@ -104,6 +105,18 @@ def _load():
     L.hm_batch_plan_create.restype = ctypes.c_int
     L.hm_batch_plan_create.argtypes = [ctypes.c_int, _pi64, _pi64, _d, _d, _d, ctypes.c_int, _i64,
                                        ctypes.POINTER(_vp)]
+    L.hm_hier_build.restype = ctypes.c_int
+    L.hm_hier_build.argtypes = [ctypes.c_int, _i64, _i64, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), _pi64,
+                                _pi64, _pi64, _pi64, _pi64, _d, _pi64, _vp, ctypes.POINTER(_vp)]
+    L.hm_dense_mul.restype = ctypes.c_int
+    L.hm_dense_mul.argtypes = [ctypes.c_int, ctypes.c_int, _vp, _i64, _i64, _i64, _vp, _i64, _i64, _i64, _vp,
+                               _i64, _i64, _i64, _vp]
+    L.hm_lowrank_mul.restype = ctypes.c_int
+    L.hm_lowrank_mul.argtypes = [ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _i64, _i64, _i64, _vp,
+                                 _i64, _i64, _i64, _vp, _i64, _i64, _i64, _vp]
+    L.hm_bary_factors.restype = ctypes.c_int
+    L.hm_bary_factors.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_double, _d, _i64, _d, _i64, ctypes.c_int, _vp, _vp, _vp, _vp]
     L.hm_size.restype = ctypes.c_int
     L.hm_size.argtypes = [_vp, _pi64, _pi64]
     L.hm_storage.restype = ctypes.c_int

@@ -1,0 +1,419 @@
+"""Block types and user-assembled hierarchical matrices on the GPU.
+
+Mirrors the reference's generic layer:
+  * ``Block(K)``                               src/block.jl:8-10
+  * ``hierarchical(name, *types)``             the @hierarchical macro, src/hierarchical.jl:4-232
+  * ``HierarchicalMatrix``                     src/HierarchicalMatrix.jl:1 (LowRankMatrix, Matrix blocks)
+  * ``LowRankMatrix(U, sigma, V)``             src/LowRankMatrix.jl:28-43
+  * ``BarycentricMatrix2D(f, a, b, c, d, x, y, ir, jr)``   src/BarycentricMatrix.jl:236-297
+  * ``mul_(y, A, x, istart, jstart, INCX, INCY)`` for dense, transposed, low-rank
+    (and adjoint), barycentric and hierarchical blocks   src/algebra.jl:37-277,
+    src/HierarchicalMatrix.jl:24-52
+
+Products run on the GPU through libhmgpu.so: device vectors are torch CUDA
+tensors; a HierarchicalMatrix is flattened to its leaf blocks (with the
+reference's block-walk offsets) and uploaded once, on its first product.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+_vp = ctypes.c_void_p
+_pi64 = ctypes.POINTER(ctypes.c_int64)
+
+
+class Block:
+    """Block(K): index of a block row or column (src/block.jl:8-10)."""
+
+    def __init__(self, K):
+        self.K = int(K)
+
+    def __eq__(self, other):
+        return isinstance(other, Block) and self.K == other.K
+
+    def __hash__(self):
+        return hash(("Block", self.K))
+
+    def __repr__(self):
+        return f"Block({self.K})"
+
+
+def _np64(a):
+    try:
+        import torch
+        if isinstance(a, torch.Tensor):
+            return a.detach().cpu().numpy().astype(np.float64)
+    except ImportError:
+        pass
+    return np.asarray(a, dtype=np.float64)
+
+
+class LowRankMatrix:
+    """A = U diag(sigma) V^T (src/LowRankMatrix.jl:28-43); U is m x r, V n x r."""
+
+    def __init__(self, U, sigma, V):
+        self.U, self.sigma, self.V = U, sigma, V
+        self.shape = (int(U.shape[0]), int(V.shape[0]))
+
+    def rank(self):
+        return int(self.sigma.shape[0])
+
+    def dense(self):
+        U, s, V = _np64(self.U), _np64(self.sigma), _np64(self.V)
+        return (U * s) @ V.T
+
+
+class BarycentricMatrix2D:
+    """The barycentric block of the kernel f on boxes [a, b] x [c, d] for the
+    points x[ir], y[jr] (src/BarycentricMatrix.jl:236-297): U F V^T with U, V
+    the Lagrange bases at first-kind Chebyshev nodes and F the kernel at the
+    nodes.  Factors are computed on the GPU in FP64 and stored as ``dtype``
+    device tensors."""
+
+    def __init__(self, f, a, b, c, d, x, y, ir, jr, *, rank=20, dtype=np.float64, device="cuda"):
+        import torch
+        from .kernelmatrix import _kernel_id
+        xs = np.ascontiguousarray(_np64(x)[ir.start:ir.stop])
+        ys = np.ascontiguousarray(_np64(y)[jr.start:jr.stop])
+        tdt = torch.float64 if np.dtype(dtype) == np.float64 else torch.float32
+        self.U = torch.empty((rank, len(xs)), dtype=tdt, device=device).t()    # column-major m x r
+        self.V = torch.empty((rank, len(ys)), dtype=tdt, device=device).t()
+        self.F = torch.empty((rank, rank), dtype=tdt, device=device).t()
+        check(lib.hm_bary_factors(_kernel_id(f), rank, float(a), float(b), float(c), float(d), _lib.f64_ptr(xs),
+                                  len(xs), _lib.f64_ptr(ys), len(ys),
+                                  _lib.HM_F64 if tdt == torch.float64 else _lib.HM_F32,
+                                  self.U.data_ptr(), self.F.data_ptr(), self.V.data_ptr(), None))
+        self.ir, self.jr = ir, jr
+        self.shape = (len(xs), len(ys))
+
+    def rank(self):
+        return int(self.F.shape[0])
+
+    def dense(self):
+        U, F, V = _np64(self.U), _np64(self.F), _np64(self.V)
+        return U @ F @ V.T
+
+
+class Transpose:
+    """transpose(A) for a dense block (src/algebra.jl:50-65)."""
+
+    def __init__(self, A):
+        self.parent = A
+        self.shape = (A.shape[1], A.shape[0])
+
+
+class Adjoint:
+    """adjoint(L) for a LowRankMatrix or a real dense block (src/algebra.jl:67-82, 133-159)."""
+
+    def __init__(self, A):
+        self.parent = A
+        self.shape = (A.shape[1], A.shape[0])
+
+
+def transpose(A):
+    return Transpose(A)
+
+
+def adjoint(A):
+    return Adjoint(A)
+
+
+# --------------------------------------------------------------------- @hierarchical
+
+class AbstractHierarchical:
+    """Base of the classes made by ``hierarchical``: an M x N grid of blocks,
+    each of one of the declared types or of the class itself, with the
+    ``assigned`` tags of src/hierarchical.jl:49-52 (1 = the class itself,
+    l = the (l-1)-th declared type, 0 = empty)."""
+
+    _types = ()
+    _store_names = ()
+
+    def __init__(self, M, N, dtype=np.float64):
+        self.M, self.N = int(M), int(N)
+        self.dtype = np.dtype(dtype)
+        self.assigned = np.zeros((self.M, self.N), dtype=np.int64)
+        for name in self._store_names:
+            setattr(self, name, [[None] * self.N for _ in range(self.M)])
+        self._handle = None
+        self._handle_dtype = None
+
+    def _tag_of(self, A):
+        if isinstance(A, type(self)):
+            return 1
+        for l, T in enumerate(self._types):
+            if _isa(A, T):
+                return l + 2
+        return 0
+
+    def __setitem__(self, key, A):
+        bm, bn = key
+        if not (isinstance(bm, Block) and isinstance(bn, Block)):
+            raise TypeError("index blocks with H[Block(m), Block(n)] (1-based)")
+        m, n = bm.K - 1, bn.K - 1
+        tag = self._tag_of(A)
+        if tag == 0:
+            return        # the reference ignores blocks of other types (src/hierarchical.jl:149-172)
+        getattr(self, self._store_names[tag - 1])[m][n] = A
+        self.assigned[m, n] = tag
+        self._invalidate()
+
+    def __getitem__(self, key):
+        bm, bn = key
+        if isinstance(bm, Block) and isinstance(bn, Block):
+            m, n = bm.K - 1, bn.K - 1
+            tag = self.assigned[m, n]
+            return None if tag == 0 else getattr(self, self._store_names[tag - 1])[m][n]
+        return self.getindex(int(bm), int(bn))
+
+    def _invalidate(self):
+        if self._handle is not None:
+            lib.hm_free(self._handle)
+        self._handle = None
+
+    def block(self, m, n):
+        tag = self.assigned[m, n]
+        return None if tag == 0 else getattr(self, self._store_names[tag - 1])[m][n]
+
+    def blocksize(self, m=None, n=None, k=None):
+        """blocksize(H) = (M, N); blocksize(H, m, n, k) (1-based) = size of block (m, n) along k."""
+        if m is None:
+            return (self.M, self.N)
+        b = self.block(m - 1, n - 1)
+        return 0 if b is None else int(_shape(b)[k - 1])
+
+    @property
+    def shape(self):
+        # rows from block column N, columns from block row 1 (src/hierarchical.jl:33-47)
+        return (sum(self.blocksize(m, self.N, 1) for m in range(1, self.M + 1)),
+                sum(self.blocksize(1, n, 2) for n in range(1, self.N + 1)))
+
+    def size(self, dim=None):
+        return self.shape if dim is None else self.shape[dim - 1]
+
+    def getindex(self, i, j):
+        """Element (i, j), 1-based (src/hierarchical.jl:120-147); CPU."""
+        m = 1
+        while m <= self.M:
+            r = self.blocksize(m, self.N, 1)
+            if i > r:
+                i -= r
+                m += 1
+            else:
+                break
+        n = 1
+        while n <= self.N:
+            s = self.blocksize(1, n, 2)
+            if j > s:
+                j -= s
+                n += 1
+            else:
+                break
+        b = self.block(m - 1, n - 1)
+        if b is None:
+            return 0.0
+        if isinstance(b, AbstractHierarchical):
+            return b.getindex(i, j)
+        return float(_dense(b)[i - 1, j - 1])
+
+    # -- flattening and the GPU product ---------------------------------------
+    def leaves(self, row0=0, col0=0):
+        """Leaf blocks with the offsets of the reference's block walk
+        (src/HierarchicalMatrix.jl:24-52): (block, row0, col0)."""
+        out = []
+        p = 0
+        for m in range(self.M):
+            q = 0
+            for n in range(self.N):
+                b = self.block(m, n)
+                if isinstance(b, AbstractHierarchical):
+                    out.extend(b.leaves(row0 + p, col0 + q))
+                elif b is not None:
+                    out.append((b, row0 + p, col0 + q))
+                q += self.blocksize(1, n + 1, 2)
+            p += self.blocksize(m + 1, self.N, 1)
+        return out
+
+    def handle(self, dtype=None):
+        dtype = np.dtype(dtype or self.dtype)
+        if self._handle is not None and self._handle_dtype == dtype:
+            return self._handle
+        self._invalidate()
+        kinds, r0, rr, c0, cc, rk, offs, vals = [], [], [], [], [], [], [], []
+        off = 0
+        for b, p, q in self.leaves():
+            if isinstance(b, LowRankMatrix):
+                U, s, V = _np64(b.U), _np64(b.sigma), _np64(b.V)
+                data = np.concatenate([U.ravel(order="F"), s.ravel(), V.ravel(order="F")])
+                kind, rank = 1, len(s)
+            elif isinstance(b, BarycentricMatrix2D):
+                U, F, V = _np64(b.U), _np64(b.F), _np64(b.V)
+                data = np.concatenate([U.ravel(order="F"), F.ravel(order="F"), V.ravel(order="F")])
+                kind, rank = 2, F.shape[0]
+            else:
+                data = _dense(b).ravel(order="F")
+                kind, rank = 0, 0
+            sh = _shape(b)
+            kinds.append(kind); r0.append(p); rr.append(sh[0]); c0.append(q); cc.append(sh[1]); rk.append(rank)
+            offs.append(off); vals.append(data); off += len(data)
+        values = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1))
+        arr = lambda v, t=np.int64: np.ascontiguousarray(np.array(v, dtype=t))   # noqa: E731
+        kinds_a, r0a, rra, c0a, cca, rka, offa = arr(kinds, np.int32), arr(r0), arr(rr), arr(c0), arr(cc), arr(rk), arr(offs)
+        m, n = self.shape
+        h = _vp()
+        check(lib.hm_hier_build(_lib.HM_F64 if dtype == np.float64 else _lib.HM_F32, m, n, len(kinds),
+                                kinds_a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), r0a.ctypes.data_as(_pi64),
+                                rra.ctypes.data_as(_pi64), c0a.ctypes.data_as(_pi64), cca.ctypes.data_as(_pi64),
+                                rka.ctypes.data_as(_pi64), _lib.f64_ptr(values), offa.ctypes.data_as(_pi64), None,
+                                ctypes.byref(h)))
+        self._handle, self._handle_dtype = h, dtype
+        return h
+
+    def mul(self, y, x, istart=1, jstart=1, incx=1, incy=1, *, stream=None):
+        """mul!(y, H, x, istart, jstart, INCX, INCY) on device vectors (accumulates)."""
+        from .kernelmatrix import _stream_ptr
+        h = self.handle(_np_dtype(y))
+        check(lib.hm_mul_strided(h, x.data_ptr(), x.numel(), jstart, incx, y.data_ptr(), y.numel(), istart, incy,
+                                 _stream_ptr(stream)))
+        return y
+
+    def __matmul__(self, x):
+        import torch
+        from .kernelmatrix import _stream_ptr
+        h = self.handle(_np_dtype(x))
+        if x.dim() == 1:
+            y = torch.zeros(self.shape[0], dtype=x.dtype, device=x.device)
+            return self.mul(y, x.contiguous())
+        X = x if x.stride(0) == 1 else x.t().contiguous().t()
+        Y = torch.zeros((x.shape[1], self.shape[0]), dtype=x.dtype, device=x.device).t()
+        check(lib.hm_mul(h, X.data_ptr(), max(X.stride(1), self.shape[1]), Y.data_ptr(), max(Y.stride(1), self.shape[0]),
+                         x.shape[1], 1, _stream_ptr(None)))
+        return Y
+
+    def __del__(self):
+        try:
+            self._invalidate()
+        except Exception:
+            pass
+
+
+def _np_dtype(t):
+    import torch
+    return np.float64 if t.dtype == torch.float64 else np.float32
+
+
+def _shape(b):
+    if isinstance(b, AbstractHierarchical):
+        return b.shape
+    return tuple(int(v) for v in b.shape)
+
+
+def _dense(b):
+    if isinstance(b, (LowRankMatrix, BarycentricMatrix2D)):
+        return b.dense()
+    return _np64(b)
+
+
+_TYPE_NAMES = {"LowRankMatrix": LowRankMatrix, "BarycentricMatrix2D": BarycentricMatrix2D, "Matrix": None}
+
+
+def _isa(A, T):
+    if isinstance(T, tuple):              # parametric member, e.g. ("UpperTriangular", "LowRankMatrix")
+        return isinstance(A, tuple) and len(A) == 2 and A[0] == T[0] and _isa(A[1], T[1])
+    if T is None or T == "Matrix":
+        return _is_dense(A)
+    if isinstance(T, str):
+        T = _TYPE_NAMES.get(T, T)
+        if isinstance(T, str):
+            return type(A).__name__ == T
+    return isinstance(A, T)
+
+
+def _is_dense(A):
+    if isinstance(A, np.ndarray):
+        return A.ndim == 2
+    try:
+        import torch
+        return isinstance(A, torch.Tensor) and A.dim() == 2
+    except ImportError:
+        return False
+
+
+def hierarchical(name, *types):
+    """The @hierarchical macro (src/hierarchical.jl:4-232): a class named
+    ``name`` whose blocks are itself or one of ``types`` (a class, a type name
+    such as "Matrix" or "LowRankMatrix", or a parametric pair such as
+    ("UpperTriangular", "LowRankMatrix")).  Block stores are named
+    ``<Type>blocks`` like the generated Julia fields."""
+
+    def store(T):
+        if isinstance(T, tuple):
+            return f"{T[0]}blocks"
+        return f"{T if isinstance(T, str) else T.__name__}blocks"
+
+    stores = (f"{name}blocks",) + tuple(store(T) for T in types)
+    cls = type(name, (AbstractHierarchical,), {"_types": tuple(types), "_store_names": stores,
+                                                "block_types": tuple(types)})
+    return cls
+
+
+HierarchicalMatrix = hierarchical("HierarchicalMatrix", LowRankMatrix, "Matrix")
+
+
+# --------------------------------------------------------------------- mul!
+
+def _strided_args(t):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dim() != 1 or not t.is_contiguous():
+        raise TypeError("vectors must be contiguous 1-D CUDA tensors")
+    return t.data_ptr(), t.numel()
+
+
+def mul_(y, A, x, istart=1, jstart=1, incx=1, incy=1, *, stream=None):
+    """mul!(y, A, x, istart, jstart[, INCX, INCY]): y[istart + (i-1) INCY] += (A x)[i]
+    with x read at x[jstart + (j-1) INCX] (1-based, as in src/algebra.jl:26-30).
+    Accumulates into y.  A: dense CUDA matrix, Transpose/Adjoint of one,
+    LowRankMatrix (or its Adjoint), BarycentricMatrix2D, a hierarchical matrix
+    or a KernelMatrix."""
+    import torch
+    from .kernelmatrix import KernelMatrix, _stream_ptr
+    sp = _stream_ptr(stream)
+    if isinstance(A, AbstractHierarchical):
+        return A.mul(y, x, istart, jstart, incx, incy, stream=stream)
+    if isinstance(A, KernelMatrix):
+        if istart == jstart == incx == incy == 1 and y.numel() == A.shape[0] and x.numel() == A.shape[1]:
+            return A.mul(y, x, accumulate=True, stream=stream)
+        return A.mul_strided(y, x, istart, jstart, incx, incy, stream=stream)
+    yp, ly = _strided_args(y)
+    xp, lx = _strided_args(x)
+    dt = _lib.HM_F64 if y.dtype == torch.float64 else _lib.HM_F32
+    trans = isinstance(A, (Transpose, Adjoint))
+    B = A.parent if trans else A
+    if isinstance(B, LowRankMatrix):
+        U, s, V = B.U, B.sigma, B.V
+        m, n, r = U.shape[0], V.shape[0], s.shape[0]
+        check(lib.hm_lowrank_mul(1 if trans else 0, dt, _colmajor(U).data_ptr(), s.contiguous().data_ptr(), 1,
+                                 _colmajor(V).data_ptr(), m, n, r, xp, lx, jstart, incx, yp, ly, istart, incy, sp))
+        return y
+    if isinstance(B, BarycentricMatrix2D):
+        m, n = B.shape
+        check(lib.hm_lowrank_mul(1 if trans else 0, dt, _colmajor(B.U).data_ptr(), _colmajor(B.F).data_ptr(), 0,
+                                 _colmajor(B.V).data_ptr(), m, n, B.rank(), xp, lx, jstart, incx, yp, ly, istart,
+                                 incy, sp))
+        return y
+    M = _colmajor(B)
+    check(lib.hm_dense_mul(1 if trans else 0, dt, M.data_ptr(), M.shape[0], M.shape[1], max(M.stride(1), M.shape[0]),
+                           xp, lx, jstart, incx, yp, ly, istart, incy, sp))
+    return y
+
+
+def _colmajor(t):
+    """A column-major (stride(0) == 1) view or copy of a 2-D CUDA tensor."""
+    if t.dim() == 1:
+        return t.contiguous()
+    if t.stride(0) == 1 and t.stride(1) >= t.shape[0]:
+        return t
+    return t.t().contiguous().t()

@@ -356,12 +356,3 @@ class _Transposed:
         if v.dim() == 2:
             u = u.t()
         return self.H.mul_t(u, v, accumulate=False)
-
-
-def mul_(u, H, v, istart=1, jstart=1, incx=None, incy=None, **kw):
-    """mul!(u, H, v[, istart, jstart[, INCX, INCY]]): accumulates H v into u."""
-    if incx is None and incy is None and istart == 1 and jstart == 1:
-        if isinstance(u, np.ndarray):
-            return H.mul_host(u, v, accumulate=True)
-        return H.mul(u, v, accumulate=True, **kw)
-    return H.mul_strided(u, v, istart, jstart, incx or 1, incy or 1, **kw)

@@ -83,6 +83,51 @@ int hm_kernelmatrix_batch_build(int kernel, int ninst, const int64_t *nx, const 
                                 const double *x, const double *y, const double *boxes, int rank,
                                 int64_t blocksize, int storage, void *stream, hm_handle **out);
 
+/* A user-assembled HierarchicalMatrix (src/HierarchicalMatrix.jl:1, built with
+   H[Block(m), Block(n)] = ..., src/hierarchical.jl:149-172), flattened to its
+   nblocks leaf blocks.  Block i occupies rows [row0, row0+rows) and columns
+   [col0, col0+cols) -- the offsets of the reference's block walk
+   (src/HierarchicalMatrix.jl:24-52) -- and its FP64 data starts at
+   values + offsets[i] (HOST memory):
+     kind 0 Matrix:              A, rows x cols, column-major
+     kind 1 LowRankMatrix:       U (rows x r), sigma (r), V (cols x r)   (src/LowRankMatrix.jl:28-33)
+     kind 2 BarycentricMatrix2D: U (rows x r), F (r x r), V (cols x r)   (src/BarycentricMatrix.jl:208-218)
+   ranks[i] = r (ignored for kind 0).  Blocks may overlap; their products add
+   up like the reference's walk.  hm_mul / hm_mul_strided then run the
+   product y += H x; transposed and derivative products are not available. */
+int hm_hier_build(int storage, int64_t m, int64_t n, int nblocks, const int32_t *kinds,
+                  const int64_t *row0, const int64_t *rows, const int64_t *col0, const int64_t *cols,
+                  const int64_t *ranks, const double *values, const int64_t *offsets, void *stream,
+                  hm_handle **out);
+
+/* Block-level products on DEVICE arrays of type dtype (HM_F64 / HM_F32),
+   1-based starts and positive increments like the reference; x and y
+   lengths are checked (HM_ERR_BOUNDS).  All accumulate into y.
+   hm_dense_mul: trans = 0: mul!(y, A, x, istart, jstart, INCX, INCY)
+   (src/algebra.jl:37-48); trans = 1: mul!(y, transpose(A), ...)
+   (src/algebra.jl:52-65; the adjoint of real data, :69-82, is the same).
+   A is m x n column-major with leading dimension lda. */
+int hm_dense_mul(int trans, int dtype, const void *A, int64_t m, int64_t n, int64_t lda,
+                 const void *x, int64_t lenx, int64_t jstart, int64_t incx, void *y, int64_t leny,
+                 int64_t istart, int64_t incy, void *stream);
+
+/* y += U C V^T x (adjoint = 0) or y += V C^T U^T x (adjoint = 1) with U m x r
+   and V n x r column-major; C = diag(core) when core_diag (LowRankMatrix
+   mul! and its adjoint, src/algebra.jl:110-131, 137-159) or the r x r
+   column-major core (BarycentricMatrix2D mul!, src/algebra.jl:243-277). */
+int hm_lowrank_mul(int adjoint, int dtype, const void *U, const void *core, int core_diag,
+                   const void *V, int64_t m, int64_t n, int64_t r, const void *x, int64_t lenx,
+                   int64_t jstart, int64_t incx, void *y, int64_t leny, int64_t istart, int64_t incy,
+                   void *stream);
+
+/* BarycentricMatrix2D(T, f, a, b, c, d, x, y, ir, jr) factors
+   (src/BarycentricMatrix.jl:147-178, 236-297) for the HOST points x (nx) and
+   y (ny) of the block: U (nx x rank), F (rank x rank), V (ny x rank), all
+   column-major DEVICE arrays of type dtype, computed in FP64.  Synchronous. */
+int hm_bary_factors(int kernel, int rank, double a, double b, double c, double d, const double *x,
+                    int64_t nx, const double *y, int64_t ny, int dtype, void *U, void *F, void *V,
+                    void *stream);
+
 /* size(H) (src/hierarchical.jl:33-47). */
 int hm_size(const hm_handle *h, int64_t *m, int64_t *n);
 /* Storage type of h (HM_F64 / HM_F32). */
