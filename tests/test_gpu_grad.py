@@ -98,6 +98,6 @@ def test_autograd_function(grad_case):
     loss = 0.5 * ((kernel_matvec(H64, wt, xt, yt) - tt) ** 2).sum()
     loss.backward()
     l2, gw, gx, gy = H64.loss_and_grad(wt.detach(), tt)
-    assert abs(float(loss) - l2) <= 1e-12 * abs(l2)
+    assert abs(loss.detach().item() - l2) <= 1e-12 * abs(l2)
     for a, b in ((wt.grad, gw), (xt.grad, gx), (yt.grad, gy)):
         assert float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) <= 1e-14
