@@ -148,9 +148,9 @@ template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, co
 // per (panel, chunk of QC right-hand sides); lane m owns column m of the
 // row-major panel (width <= 32, row stride ld).  Panels of up to 64 rows are
 // staged in shared memory (16-byte loads by all lanes) together with the
-// chunk's x values; longer panels are read directly.  QC = 1 accumulates with
-// compensated sums in FP32, QC > 1 with plain FMA.  Coefficients of a slot
-// are r apart per right-hand side.
+// chunk's x values; longer panels are read directly.  Plain FMA accumulation
+// (the coefficients feed only the far field).  Coefficients of a slot are r
+// apart per right-hand side.
 template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r)
 {
@@ -164,8 +164,7 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
     const int q0 = (int)(w % nq) * QC, qc = min(QC, ma.k - q0);
     const int pw = P.width;
     const S *Vp = V + P.off;
-    using AccT = typename std::conditional<QC == 1, Acc<A>, PlainAcc<A>>::type;
-    AccT acc[QC];
+    PlainAcc<A> acc[QC];
 #pragma unroll
     for (int qq = 0; qq < QC; ++qq) acc[qq].zero();
     if (P.nrows <= 64 && P.ld == pw) {
@@ -204,6 +203,52 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
 #pragma unroll
         for (int qq = 0; qq < QC; ++qq)
             if (qq < qc) t[((int64_t)P.slot * ma.k + q0 + qq) * r + P.col0 + lane] = acc[qq].value();
+    }
+}
+
+// One gather band: for each node, dst[node] = sum over its contributors of
+// M_path (applied in the layout of M) to the contributor's coefficients
+// (src_a, or src_b for contributors flagged final; mat < 0 is the identity).
+// One warp per (node, chunk of QC right-hand sides); lane = output index; the
+// contributor's coefficients are loaded one per lane and broadcast with
+// shuffles, M is read row by row (consecutive lanes, consecutive entries).
+// Nodes of a band read only coefficients produced before the launch.
+template <typename A, int QC>
+__global__ void gather_band(const hm_gnode *nodes, int nnodes, const hm_gsrc *srcs, const A *M, const A *src_a,
+                            const A *src_b, A *dst, int r, int k)
+{
+    const int lane = threadIdx.x & 31;
+    const int nq = (k + QC - 1) / QC;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= (int64_t)nnodes * nq) return;
+    const hm_gnode G = nodes[w / nq];
+    const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+    A acc[QC];
+#pragma unroll
+    for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
+    for (int e = G.begin; e < G.end; ++e) {
+        const hm_gsrc S = srcs[e];
+        const A *src = S.from_final ? src_b : src_a;
+        A v[QC];
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq)
+            v[qq] = (lane < r && qq < qc) ? src[((int64_t)S.slot * k + q0 + qq) * r + lane] : (A)0;
+        if (S.mat < 0) {
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq) acc[qq] += v[qq];
+        } else {
+            const A *Mp = M + (int64_t)S.mat * r * r;
+            for (int j = 0; j < r; ++j) {
+                const A mj = lane < r ? __ldg(Mp + j * r + lane) : (A)0;
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) acc[qq] += mj * __shfl_sync(0xffffffffu, v[qq], j);
+            }
+        }
+    }
+    if (lane < r) {
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq)
+            if (qq < qc) dst[((int64_t)G.slot * k + q0 + qq) * r + lane] = acc[qq];
     }
 }
 
@@ -258,40 +303,47 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
 
 // Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
 // (the F stage of src/algebra.jl:258-265, grouped by row cluster).  One warp
-// per (row slot, chunk of up to 8 right-hand sides); each r x r block is
-// staged in shared memory with 16-byte loads by all lanes and used for every
-// right-hand side of the chunk; column coefficients are loaded one per lane
-// and broadcast with shuffles.
+// per (row slot, chunk of up to QC right-hand sides).  Up to HM_M2L_BLOCKS
+// r x r blocks of the row are staged in shared memory at once with 16-byte
+// loads issued together (one round trip for the whole row); the column
+// coefficients are loaded one per lane and broadcast with shuffles.
 template <typename S, typename A, int QC>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
                     const A *t, A *s, int r, int k)
 {
     extern __shared__ unsigned char smem_raw[];
     constexpr int VE = 16 / sizeof(S);
-    S *Fb = reinterpret_cast<S *>(smem_raw) + (threadIdx.x >> 5) * fstride;
+    S *Fb = reinterpret_cast<S *>(smem_raw) + (int64_t)(threadIdx.x >> 5) * HM_M2L_BLOCKS * fstride;
     const int lane = threadIdx.x & 31;
     const int nq = (k + QC - 1) / QC;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (w >= (int64_t)nrows * nq) return;
     const hm_m2l_row R = rows[w / nq];
     const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+    const int n16 = fstride / VE;
     A acc[QC];
 #pragma unroll
     for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
-    for (int e = R.begin; e < R.end; ++e) {
-        const hm_m2l_ent E = ents[e];
-        const float4 *src = reinterpret_cast<const float4 *>(F + E.foff);
-        float4 *dst = reinterpret_cast<float4 *>(Fb);
-        for (int i = lane; i < fstride / VE; i += 32) dst[i] = __ldg(src + i);
-        A tv[QC];
-#pragma unroll
-        for (int qq = 0; qq < QC; ++qq)
-            tv[qq] = (lane < r && qq < qc) ? t[((int64_t)E.yslot * k + q0 + qq) * r + lane] : (A)0;
+    for (int e0 = R.begin; e0 < R.end; e0 += HM_M2L_BLOCKS) {
+        const int nb = min(HM_M2L_BLOCKS, R.end - e0);
+        for (int i = lane; i < nb * n16; i += 32) {
+            const int b = i / n16, j = i % n16;
+            reinterpret_cast<float4 *>(Fb + b * fstride)[j] =
+                __ldg(reinterpret_cast<const float4 *>(F + ents[e0 + b].foff) + j);
+        }
         __syncwarp();
-        for (int n = 0; n < r; ++n) {
-            const A f = lane < r ? (A)Fb[lane + r * n] : (A)0;
+        for (int b = 0; b < nb; ++b) {
+            const int ys = ents[e0 + b].yslot;
+            A tv[QC];
 #pragma unroll
-            for (int qq = 0; qq < QC; ++qq) acc[qq] += f * __shfl_sync(0xffffffffu, tv[qq], n);
+            for (int qq = 0; qq < QC; ++qq)
+                tv[qq] = (lane < r && qq < qc) ? t[((int64_t)ys * k + q0 + qq) * r + lane] : (A)0;
+            const S *Fe = Fb + b * fstride;
+            for (int n = 0; n < r; ++n) {
+                const A f = lane < r ? (A)Fe[lane + r * n] : (A)0;
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) acc[qq] += f * __shfl_sync(0xffffffffu, tv[qq], n);
+            }
         }
         __syncwarp();
     }
@@ -688,6 +740,10 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     HM_INST_PART(S, A, 1) HM_INST_PART(S, A, 2) HM_INST_PART(S, A, 4) HM_INST_PART(S, A, 8)               \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
                                             const A *, const A *, int, int);                            \
+    template __global__ void gather_band<A, 1>(const hm_gnode *, int, const hm_gsrc *, const A *, const A *,  \
+                                               const A *, A *, int, int);                               \
+    template __global__ void gather_band<A, 8>(const hm_gnode *, int, const hm_gsrc *, const A *, const A *,  \
+                                               const A *, A *, int, int);                               \
     template __global__ void xfer_up_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
                                                 A *, int, int);                                         \
     template __global__ void xfer_up_band<A, 8>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
