@@ -484,6 +484,8 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
 {
     const int r = h->r, k = ma.k;
     const int64_t nq = (k + QC - 1) / QC;
+    const size_t msm = (size_t)kNumPathMats * r * r * sizeof(A);     // composed matrices in shared memory
+    if (h->gup_band_ptr.size() > 1 || h->gdown_band_ptr.size() > 1) HM_TRY(ensure_smem(gather_band<A, QC>, msm));
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
@@ -496,8 +498,8 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         for (size_t bd = 0; bd + 1 < h->gup_band_ptr.size(); ++bd) {
             const int b = h->gup_band_ptr[bd], n = h->gup_band_ptr[bd + 1] - b;
             if (!n) continue;
-            gather_band<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, 0, st>>>(
-                h->d_gup_nodes + b, n, h->d_gup_srcs, static_cast<const A *>(h->d_Mup), t, t, t, r, k);
+            gather_band<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, msm, st>>>(
+                h->d_gup_nodes + b, n, h->d_gup_srcs, static_cast<const A *>(h->d_Mup), kNumPathMats, t, t, t, r, k);
             HM_CK_LAUNCH("gather_up");
         }
     }
@@ -513,8 +515,9 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         for (size_t bd = 0; bd + 1 < h->gdown_band_ptr.size(); ++bd) {
             const int b = h->gdown_band_ptr[bd], n = h->gdown_band_ptr[bd + 1] - b;
             if (!n) continue;
-            gather_band<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, 0, st>>>(
-                h->d_gdown_nodes + b, n, h->d_gdown_srcs, static_cast<const A *>(h->d_Mdown), loc, s, s, r, k);
+            gather_band<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, msm, st>>>(
+                h->d_gdown_nodes + b, n, h->d_gdown_srcs, static_cast<const A *>(h->d_Mdown), kNumPathMats, loc, s, s,
+                r, k);
             HM_CK_LAUNCH("gather_down");
         }
     }

@@ -147,8 +147,8 @@ template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
 
 template <typename A, int QC>
-__global__ void gather_band(const hm_gnode *nodes, int nnodes, const hm_gsrc *srcs, const A *M, const A *src_a,
-                            const A *src_b, A *dst, int r, int k);
+__global__ void gather_band(const hm_gnode *nodes, int nnodes, const hm_gsrc *srcs, const A *M, int nmats,
+                            const A *src_a, const A *src_b, A *dst, int r, int k);
 
 template <typename A, int QC>
 __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
