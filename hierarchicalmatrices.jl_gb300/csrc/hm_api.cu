@@ -112,56 +112,6 @@ void transfer_matrices(int r, const std::vector<double> &x, const std::vector<do
     }
 }
 
-// Composed transfer matrices M_path = T_{b_len} ... T_{b_1} for every path of
-// length 1..kGatherLevels (b_1 = first step from the ancestor, the top bit of
-// `bits`), in two layouts: up[idx][m'][m] = M[m'][m] (upward gathers read
-// M^T) and down[idx][m][m'] = M[m'][m] (downward gathers read M), so a lane
-// always reads consecutive entries.
-void path_matrices(int r, const std::vector<double> &x, const std::vector<double> &w, std::vector<double> &up,
-                   std::vector<double> &down)
-{
-    std::vector<long double> T(2 * r * r);
-    for (int c = 0; c < 2; ++c)
-        for (int mp = 0; mp < r; ++mp) {
-            const long double u = (c == 0 ? -0.5L : 0.5L) + 0.5L * (long double)x[mp];
-            int hit = -1;
-            for (int m = 0; m < r; ++m)
-                if (u == (long double)x[m]) hit = m;
-            long double sum = 0.0L;
-            for (int m = 0; m < r; ++m) {
-                const long double v = hit >= 0 ? (m == hit ? 1.0L : 0.0L) : (long double)w[m] / (u - (long double)x[m]);
-                T[c * r * r + mp * r + m] = v;
-                sum += v;
-            }
-            for (int m = 0; m < r; ++m) T[c * r * r + mp * r + m] /= sum;
-        }
-    up.assign((size_t)kNumPathMats * r * r, 0.0);
-    down.assign((size_t)kNumPathMats * r * r, 0.0);
-    std::vector<long double> M(r * r), N(r * r);
-    for (int len = 1; len <= kGatherLevels; ++len)
-        for (int bits = 0; bits < (1 << len); ++bits) {
-            for (int i = 0; i < r * r; ++i) M[i] = 0.0L;
-            for (int i = 0; i < r; ++i) M[i * r + i] = 1.0L;
-            for (int st = 0; st < len; ++st) {
-                const int b = (bits >> (len - 1 - st)) & 1;
-                const long double *Tb = T.data() + b * r * r;
-                for (int i = 0; i < r; ++i)
-                    for (int j = 0; j < r; ++j) {
-                        long double acc = 0.0L;
-                        for (int l = 0; l < r; ++l) acc += Tb[i * r + l] * M[l * r + j];
-                        N[i * r + j] = acc;
-                    }
-                M.swap(N);
-            }
-            const size_t idx = (size_t)((1 << len) - 2 + bits) * r * r;
-            for (int i = 0; i < r; ++i)
-                for (int j = 0; j < r; ++j) {
-                    up[idx + i * r + j] = (double)M[i * r + j];
-                    down[idx + j * r + i] = (double)M[i * r + j];
-                }
-        }
-}
-
 }  // namespace
 
 struct hm_handle {
@@ -196,11 +146,6 @@ struct hm_handle {
     hm_m2l_ent *d_m2l_ents = nullptr;
     hm_xfer *d_down = nullptr;
     std::vector<int> down_ptr;
-    // gather bands and composed transfer matrices (storage type)
-    hm_gnode *d_gup_nodes = nullptr, *d_gdown_nodes = nullptr;
-    hm_gsrc *d_gup_srcs = nullptr, *d_gdown_srcs = nullptr;
-    std::vector<int> gup_band_ptr, gdown_band_ptr;
-    void *d_Mup = nullptr, *d_Mdown = nullptr;
     // banded transfers
     hm_xfer *d_up_ents = nullptr, *d_down_ents = nullptr;
     hm_step *d_up_steps = nullptr, *d_down_steps = nullptr;
@@ -309,21 +254,6 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     h->up_band_ptr = P.up_band_ptr;
     h->down_band_ptr = P.down_band_ptr;
     h->fstride = P.fstride;
-    HM_TRY(h->upload(&h->d_gup_nodes, P.gup_nodes, st));
-    HM_TRY(h->upload(&h->d_gup_srcs, P.gup_srcs, st));
-    HM_TRY(h->upload(&h->d_gdown_nodes, P.gdown_nodes, st));
-    HM_TRY(h->upload(&h->d_gdown_srcs, P.gdown_srcs, st));
-    h->gup_band_ptr = P.gup_band_ptr;
-    h->gdown_band_ptr = P.gdown_band_ptr;
-    {
-        std::vector<double> mu, md;
-        path_matrices(h->r, cheb, lam, mu, md);
-        std::vector<S> su(mu.begin(), mu.end()), sd(md.begin(), md.end());
-        S *pu = nullptr, *pd = nullptr;
-        HM_TRY(h->upload(&pu, su, st));
-        HM_TRY(h->upload(&pd, sd, st));
-        h->d_Mup = pu; h->d_Mdown = pd;
-    }
     HM_TRY(h->upload(&h->d_segs, P.segs, st));
     h->n_segs = (int)P.segs.size();
     HM_TRY(h->upload(&h->d_pieces, P.pieces, st));
@@ -396,8 +326,6 @@ int build_hier_device(hm_handle *h, const Plan &P, const std::vector<double> &vs
     h->up_band_ptr = P.up_band_ptr;
     h->down_band_ptr = P.down_band_ptr;
     h->fstride = P.fstride;
-    h->gup_band_ptr.assign(1, 0);      // no tree: no gather bands
-    h->gdown_band_ptr.assign(1, 0);
     h->pstore_elems = P.pstore_elems;
     std::vector<S> v(vs.begin(), vs.end()), f(fs.begin(), fs.end()), p(ps.begin(), ps.end());
     S *dv = nullptr, *df = nullptr, *dp = nullptr;
@@ -432,7 +360,7 @@ int ensure_smem(K kernel, size_t bytes)
 
 // Per-call scratch: coefficients t (column slots) then s (row slots).
 struct ScratchLayout {
-    size_t t_off, s_off, loc_off, bytes;
+    size_t t_off, s_off, bytes;
 };
 
 inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
@@ -443,10 +371,7 @@ ScratchLayout scratch_layout(const hm_handle *h, int k)
     ScratchLayout L;
     L.t_off = 0;
     L.s_off = align256((size_t)h->n_yslots * k * h->r * sizeof(A));
-    L.loc_off = L.s_off + align256((size_t)h->n_xslots * k * h->r * sizeof(A));
-    // far-field results before the downward pass (only with downward gathers)
-    const size_t nloc = h->gdown_band_ptr.size() > 1 ? (size_t)h->n_xslots * k * h->r : 0;
-    L.bytes = L.loc_off + align256(nloc * sizeof(A));
+    L.bytes = L.s_off + align256((size_t)h->n_xslots * k * h->r * sizeof(A));
     return L;
 }
 
@@ -477,15 +402,14 @@ constexpr int kPartMaxK = 8;    // right-hand sides handled by the streaming pan
 
 inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
 
-// Tree passes on stream st: leaf bases, upward gather bands, far field,
-// downward gather bands.  QC right-hand sides per warp.
+// Tree passes on stream st: leaf bases, upward transfers level by level, far
+// field, downward transfers level by level.  QC right-hand sides per warp.
 template <typename S, typename A, int QC>
-int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, A *loc, bool timing)
+int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
 {
     const int r = h->r, k = ma.k;
     const int64_t nq = (k + QC - 1) / QC;
-    const size_t msm = (size_t)kNumPathMats * r * r * sizeof(A);     // composed matrices in shared memory
-    if (h->gup_band_ptr.size() > 1 || h->gdown_band_ptr.size() > 1) HM_TRY(ensure_smem(gather_band<A, QC>, msm));
+    const A *T = static_cast<const A *>(h->d_T);
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
@@ -495,40 +419,42 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
         }
-        for (size_t bd = 0; bd + 1 < h->gup_band_ptr.size(); ++bd) {
-            const int b = h->gup_band_ptr[bd], n = h->gup_band_ptr[bd + 1] - b;
+        const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * 2 * QC * HM_RMAX) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_up_band<A, QC>, xsm));
+        for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
+            const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
             if (!n) continue;
-            gather_band<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, msm, st>>>(
-                h->d_gup_nodes + b, n, h->d_gup_srcs, static_cast<const A *>(h->d_Mup), kNumPathMats, t, t, t, r, k);
-            HM_CK_LAUNCH("gather_up");
+            xfer_up_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, r, k);
+            HM_CK_LAUNCH("xfer_up_band");
         }
     }
     {
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
-            const size_t smem = (size_t)kWarpsPerCta * HM_M2L_BLOCKS * h->fstride * sizeof(S);
+            const size_t smem = (size_t)kWarpsPerCta * h->fstride * sizeof(S);
             HM_TRY(ensure_smem(m2l<S, A, QC>, smem));
             m2l<S, A, QC><<<warp_ctas((int64_t)h->n_m2l_rows * nq), 32 * kWarpsPerCta, smem, st>>>(
-                h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, loc, r, k);
+                h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
             HM_CK_LAUNCH("m2l");
         }
-        for (size_t bd = 0; bd + 1 < h->gdown_band_ptr.size(); ++bd) {
-            const int b = h->gdown_band_ptr[bd], n = h->gdown_band_ptr[bd + 1] - b;
+        const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * QC * HM_RMAX) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_down_band<A, QC>, xsm));
+        for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
+            const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
             if (!n) continue;
-            gather_band<A, QC><<<warp_grid((int64_t)n * nq), kWarpCta, msm, st>>>(
-                h->d_gdown_nodes + b, n, h->d_gdown_srcs, static_cast<const A *>(h->d_Mdown), kNumPathMats, loc, s, s,
-                r, k);
-            HM_CK_LAUNCH("gather_down");
+            xfer_down_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T,
+                                                            s, r, k);
+            HM_CK_LAUNCH("xfer_down_band");
         }
     }
     return HM_OK;
 }
 
 template <typename S, typename A>
-int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, A *loc, bool timing)
+int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
 {
-    if (ma.k == 1) return launch_tree_qc<S, A, 1>(h, ma, st, t, s, loc, timing);
-    return launch_tree_qc<S, A, 8>(h, ma, st, t, s, loc, timing);
+    if (ma.k == 1) return launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing);
+    return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing);
 }
 
 template <typename S, typename A, bool FAR, int KB>
@@ -578,8 +504,6 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
     const ScratchLayout L = scratch_layout<A>(h, k);
     A *t = reinterpret_cast<A *>(static_cast<char *>(scratch) + L.t_off);
     A *s = reinterpret_cast<A *>(static_cast<char *>(scratch) + L.s_off);
-    // without downward gathers (user-assembled matrices) the far-field stage writes s directly
-    A *loc = h->gdown_band_ptr.size() > 1 ? reinterpret_cast<A *>(static_cast<char *>(scratch) + L.loc_off) : s;
     const bool split = side != st;
     const bool tree = h->n_vp || h->n_m2l_rows;
     if (tree) {
@@ -587,7 +511,7 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
             HM_CK(cudaEventRecord(fork, st));
             HM_CK(cudaStreamWaitEvent(side, fork, 0));
         }
-        HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, loc, timing)));
+        HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing)));
         if (split) HM_CK(cudaEventRecord(join, side));
     }
     if (!h->n_segs) {
@@ -693,7 +617,7 @@ int noalloc_scratch(void **out)
 
 struct hm_plan {
     Plan P;
-    std::vector<double> cheb, lam, T, Mup;
+    std::vector<double> cheb, lam, T;
 };
 
 extern "C" {
@@ -717,10 +641,6 @@ int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, dou
     hm_plan *pl = new hm_plan();
     chebyshev_first_kind(rank, pl->cheb, pl->lam);
     transfer_matrices(rank, pl->cheb, pl->lam, pl->T);
-    {
-        std::vector<double> md;
-        path_matrices(rank, pl->cheb, pl->lam, pl->Mup, md);
-    }
     st = build_plan(x, nx, y, ny, a, b, c, d, rank, blocksize, kSegRows, pl->P);
     if (st == PLAN_ERR_BOUNDS) {
         set_error("indsplit would read past the end of the point list");
@@ -772,7 +692,7 @@ int hm_batch_plan_create(int ninst, const int64_t *nx, const int64_t *ny, const 
         ps.reserve(ninst);
         for (int i = 0; i < ninst; ++i) ps.push_back(std::move(parts[i]->P));
         merge_plans(ps, pl->P);
-        pl->cheb = parts[0]->cheb; pl->lam = parts[0]->lam; pl->T = parts[0]->T; pl->Mup = parts[0]->Mup;
+        pl->cheb = parts[0]->cheb; pl->lam = parts[0]->lam; pl->T = parts[0]->T;
     }
     for (hm_plan *p : parts) delete p;
     if (st) return st;
@@ -809,13 +729,6 @@ int hm_plan_table(const hm_plan *pl, int which, const void **data, int64_t *coun
     case 20: HM_TAB(P.down_steps)
     case 21: HM_TAB(P.down_tasks)
     case 22: HM_TAB(P.down_band_ptr)
-    case 23: HM_TAB(P.gup_nodes)
-    case 24: HM_TAB(P.gup_srcs)
-    case 25: HM_TAB(P.gup_band_ptr)
-    case 26: HM_TAB(P.gdown_nodes)
-    case 27: HM_TAB(P.gdown_srcs)
-    case 28: HM_TAB(P.gdown_band_ptr)
-    case 29: HM_TAB(pl->Mup)
     default: return HM_ERR_INVALID_ARG;
     }
 #undef HM_TAB
@@ -938,7 +851,7 @@ int build_from_plan(int kernel, int swap, hm_plan *pl, const double *x, const do
         for (size_t i = 0; i + 1 < ptr.size(); ++i) c += ptr[i + 1] > ptr[i];
         return c;
     };
-    h->launches_per_mul = (h->n_vp > 0) + nonempty(h->gup_band_ptr) + (h->n_m2l_rows > 0) + nonempty(h->gdown_band_ptr) +
+    h->launches_per_mul = (h->n_vp > 0) + nonempty(h->up_band_ptr) + (h->n_m2l_rows > 0) + nonempty(h->down_band_ptr) +
                           (h->n_segs > 0) * (1 + ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
     if (st) { hm_free(h); return st; }
     *out = h;
@@ -1017,8 +930,6 @@ int hm_hier_build(int storage, int64_t m, int64_t n, int nblocks, const int32_t 
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
     const int st = storage == HM_F64 ? build_hier_device<double>(h, P, vs, fs, ps, cs)
                                      : build_hier_device<float>(h, P, vs, fs, ps, cs);
-    h->gup_band_ptr.assign(1, 0);
-    h->gdown_band_ptr.assign(1, 0);
     h->launches_per_mul = (h->n_vp > 0) + (h->n_m2l_rows > 0) + (h->n_segs > 0) * (1 + (h->n_vp > 0));
     if (st) { hm_free(h); return st; }
     *out = h;

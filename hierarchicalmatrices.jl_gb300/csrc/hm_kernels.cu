@@ -206,71 +206,6 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
     }
 }
 
-// One gather band: for each node, dst[node] = sum over its contributors of
-// M_path (applied in the layout of M) to the contributor's coefficients
-// (src_a, or src_b for contributors flagged final; mat < 0 is the identity).
-// The composed matrices are staged once per CTA in shared memory.  One warp
-// per (node, chunk of QC right-hand sides); lane = output index.  The
-// contributors' records and coefficient vectors are loaded up front, up to
-// GB at a time (one round trip), then broadcast with shuffles.  Nodes of a
-// band read only coefficients produced before the launch.
-template <typename A, int QC>
-__global__ void gather_band(const hm_gnode *nodes, int nnodes, const hm_gsrc *srcs, const A *M, int nmats,
-                            const A *src_a, const A *src_b, A *dst, int r, int k)
-{
-    extern __shared__ unsigned char smem_raw[];
-    A *Ms = reinterpret_cast<A *>(smem_raw);
-    for (int i = threadIdx.x; i < nmats * r * r; i += blockDim.x) Ms[i] = M[i];
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int nq = (k + QC - 1) / QC;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= (int64_t)nnodes * nq) return;
-    const hm_gnode G = nodes[w / nq];
-    const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
-    constexpr int GB = QC == 1 ? 16 : 4;     // contributors loaded per round trip
-    A acc[QC];
-#pragma unroll
-    for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
-    for (int e0 = G.begin; e0 < G.end; e0 += GB) {
-        const int ne = min(GB, G.end - e0);
-        // lane e holds contributor e's record
-        hm_gsrc my = {0, -1, 0, 0};
-        if (lane < ne) my = srcs[e0 + lane];
-        A v[GB][QC];
-#pragma unroll
-        for (int e = 0; e < GB; ++e) {
-            const int slot = __shfl_sync(0xffffffffu, my.slot, e);
-            const int fin = __shfl_sync(0xffffffffu, my.from_final, e);
-            const A *src = fin ? src_b : src_a;
-#pragma unroll
-            for (int qq = 0; qq < QC; ++qq)
-                v[e][qq] = (e < ne && lane < r && qq < qc) ? src[((int64_t)slot * k + q0 + qq) * r + lane] : (A)0;
-        }
-#pragma unroll
-        for (int e = 0; e < GB; ++e) {
-            if (e >= ne) break;
-            const int mat = __shfl_sync(0xffffffffu, my.mat, e);
-            if (mat < 0) {
-#pragma unroll
-                for (int qq = 0; qq < QC; ++qq) acc[qq] += v[e][qq];
-            } else {
-                const A *Mp = Ms + mat * r * r;
-                for (int j = 0; j < r; ++j) {
-                    const A mj = lane < r ? Mp[j * r + lane] : (A)0;
-#pragma unroll
-                    for (int qq = 0; qq < QC; ++qq) acc[qq] += mj * __shfl_sync(0xffffffffu, v[e][qq], j);
-                }
-            }
-        }
-    }
-    if (lane < r) {
-#pragma unroll
-        for (int qq = 0; qq < QC; ++qq)
-            if (qq < qc) dst[((int64_t)G.slot * k + q0 + qq) * r + lane] = acc[qq];
-    }
-}
-
 // Upward transfers of one band: t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m'].
 // One CTA per task (a subtree cut to the band's levels); the task's steps
 // (levels, deepest first) run in order with a CTA barrier between them, warps
@@ -322,60 +257,40 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
 
 // Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
 // (the F stage of src/algebra.jl:258-265, grouped by row cluster).  One warp
-// per (row slot, chunk of up to QC right-hand sides).  Up to HM_M2L_BLOCKS
-// blocks of the row at a time: their records are read one per lane, then
-// every r x r block is staged in shared memory with 16-byte loads and the
-// column coefficients loaded, all issued together (one round trip); the
-// coefficients are broadcast with shuffles.
+// per (row slot, chunk of up to 8 right-hand sides); each r x r block is
+// staged in shared memory with 16-byte loads by all lanes and used for every
+// right-hand side of the chunk; column coefficients are loaded one per lane
+// and broadcast with shuffles.
 template <typename S, typename A, int QC>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
                     const A *t, A *s, int r, int k)
 {
     extern __shared__ unsigned char smem_raw[];
     constexpr int VE = 16 / sizeof(S);
-    S *Fb = reinterpret_cast<S *>(smem_raw) + (int64_t)(threadIdx.x >> 5) * HM_M2L_BLOCKS * fstride;
+    S *Fb = reinterpret_cast<S *>(smem_raw) + (threadIdx.x >> 5) * fstride;
     const int lane = threadIdx.x & 31;
     const int nq = (k + QC - 1) / QC;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (w >= (int64_t)nrows * nq) return;
     const hm_m2l_row R = rows[w / nq];
     const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
-    const int n16 = fstride / VE;
     A acc[QC];
 #pragma unroll
     for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
-    for (int e0 = R.begin; e0 < R.end; e0 += HM_M2L_BLOCKS) {
-        const int nb = min(HM_M2L_BLOCKS, R.end - e0);
-        int64_t my_off = 0;
-        int my_ys = 0;
-        if (lane < nb) { my_off = ents[e0 + lane].foff; my_ys = ents[e0 + lane].yslot; }
-        A tv[HM_M2L_BLOCKS][QC];
+    for (int e = R.begin; e < R.end; ++e) {
+        const hm_m2l_ent E = ents[e];
+        const float4 *src = reinterpret_cast<const float4 *>(F + E.foff);
+        float4 *dst = reinterpret_cast<float4 *>(Fb);
+        for (int i = lane; i < fstride / VE; i += 32) dst[i] = __ldg(src + i);
+        A tv[QC];
 #pragma unroll
-        for (int b = 0; b < HM_M2L_BLOCKS; ++b) {
-            const int ys = __shfl_sync(0xffffffffu, my_ys, b);
-#pragma unroll
-            for (int qq = 0; qq < QC; ++qq)
-                tv[b][qq] = (b < nb && lane < r && qq < qc) ? t[((int64_t)ys * k + q0 + qq) * r + lane] : (A)0;
-        }
-#pragma unroll
-        for (int b = 0; b < HM_M2L_BLOCKS; ++b) {
-            const int64_t off = __shfl_sync(0xffffffffu, my_off, b);
-            if (b < nb) {
-                const float4 *src = reinterpret_cast<const float4 *>(F + off);
-                float4 *dst = reinterpret_cast<float4 *>(Fb + b * fstride);
-                for (int j = lane; j < n16; j += 32) dst[j] = __ldg(src + j);
-            }
-        }
+        for (int qq = 0; qq < QC; ++qq)
+            tv[qq] = (lane < r && qq < qc) ? t[((int64_t)E.yslot * k + q0 + qq) * r + lane] : (A)0;
         __syncwarp();
+        for (int n = 0; n < r; ++n) {
+            const A f = lane < r ? (A)Fb[lane + r * n] : (A)0;
 #pragma unroll
-        for (int b = 0; b < HM_M2L_BLOCKS; ++b) {
-            if (b >= nb) break;
-            const S *Fe = Fb + b * fstride;
-            for (int n = 0; n < r; ++n) {
-                const A f = lane < r ? (A)Fe[lane + r * n] : (A)0;
-#pragma unroll
-                for (int qq = 0; qq < QC; ++qq) acc[qq] += f * __shfl_sync(0xffffffffu, tv[b][qq], n);
-            }
+            for (int qq = 0; qq < QC; ++qq) acc[qq] += f * __shfl_sync(0xffffffffu, tv[qq], n);
         }
         __syncwarp();
     }
@@ -772,10 +687,6 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     HM_INST_PART(S, A, 1) HM_INST_PART(S, A, 2) HM_INST_PART(S, A, 4) HM_INST_PART(S, A, 8)               \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
                                             const A *, const A *, int, int);                            \
-    template __global__ void gather_band<A, 1>(const hm_gnode *, int, const hm_gsrc *, const A *, int,       \
-                                               const A *, const A *, A *, int, int);                    \
-    template __global__ void gather_band<A, 8>(const hm_gnode *, int, const hm_gsrc *, const A *, int,       \
-                                               const A *, const A *, A *, int, int);                    \
     template __global__ void xfer_up_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
                                                 A *, int, int);                                         \
     template __global__ void xfer_up_band<A, 8>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \

@@ -7,7 +7,6 @@
 #include "hm_types.h"
 
 #define HM_RMAX 32
-#define HM_M2L_BLOCKS 6   // F blocks staged at once per warp by the far-field kernel
 
 namespace hm {
 
@@ -145,10 +144,6 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
 
 template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
-
-template <typename A, int QC>
-__global__ void gather_band(const hm_gnode *nodes, int nnodes, const hm_gsrc *srcs, const A *M, int nmats,
-                            const A *src_a, const A *src_b, A *dst, int r, int k);
 
 template <typename A, int QC>
 __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,

@@ -18,7 +18,6 @@
 #include "hm_plan.h"
 
 #include <algorithm>
-#include <array>
 
 namespace hm {
 
@@ -171,91 +170,6 @@ void transfer_steps(const Tree &T, bool deepest_first, std::vector<hm_xfer> &out
 
 inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
-inline int path_mat(int len, int bits) { return (1 << len) - 2 + bits; }
-
-// Upward gather bands: internal basis nodes in bands of kGatherLevels levels
-// counted from the deepest internal level.  A node's contributors are found by
-// descending: children inside the band are expanded, anything else (a basis
-// leaf, or an internal node of a deeper band) contributes through the
-// composed matrix of its path.
-void gather_up(const Tree &T, std::vector<hm_gnode> &nodes, std::vector<hm_gsrc> &srcs, std::vector<int> &band_ptr)
-{
-    nodes.clear(); srcs.clear(); band_ptr.assign(1, 0);
-    int maxlev = -1;
-    for (const Node &n : T.nodes) if (n.kind == 1) maxlev = std::max(maxlev, n.level);
-    if (maxlev < 0) return;
-    const int nb = maxlev / kGatherLevels + 1;
-    auto band_of = [&](int lev) { return (maxlev - lev) / kGatherLevels; };
-    std::vector<std::vector<int>> by(nb);
-    for (size_t i = 0; i < T.nodes.size(); ++i)
-        if (T.nodes[i].kind == 1) by[band_of(T.nodes[i].level)].push_back((int)i);
-    for (int b = 0; b < nb; ++b) {
-        std::sort(by[b].begin(), by[b].end(), [&](int u, int v) { return T.nodes[u].slot < T.nodes[v].slot; });
-        for (int id : by[b]) {
-            hm_gnode g;
-            g.slot = T.nodes[id].slot; g.begin = (int32_t)srcs.size(); g.pad = 0;
-            // (node, path length, path bits)
-            std::vector<std::array<int, 3>> stack = {{id, 0, 0}};
-            while (!stack.empty()) {
-                auto [cur, len, bits] = stack.back();
-                stack.pop_back();
-                for (int c = 1; c >= 0; --c) {
-                    const int ch = T.nodes[cur].child[c];
-                    const int nl = len + 1, nbits = (bits << 1) | c;
-                    if (T.nodes[ch].kind == 1 && band_of(T.nodes[ch].level) == b)
-                        stack.push_back({ch, nl, nbits});
-                    else
-                        srcs.push_back({T.nodes[ch].slot, path_mat(nl, nbits), 0, 0});
-                }
-            }
-            g.end = (int32_t)srcs.size();
-            nodes.push_back(g);
-        }
-        band_ptr.push_back((int)nodes.size());
-    }
-}
-
-// Downward gather bands: all basis nodes in bands of kGatherLevels levels
-// counted from the topmost basis level.  A node gathers its own far-field
-// result and those of its in-band ancestors, and the final coefficients of
-// the first ancestor above the band.
-void gather_down(const Tree &T, std::vector<hm_gnode> &nodes, std::vector<hm_gsrc> &srcs, std::vector<int> &band_ptr)
-{
-    nodes.clear(); srcs.clear(); band_ptr.assign(1, 0);
-    int minlev = 1 << 30, maxlev = -1;
-    for (const Node &n : T.nodes)
-        if (n.kind) { minlev = std::min(minlev, n.level); maxlev = std::max(maxlev, n.level); }
-    if (maxlev < 0) return;
-    const int nb = (maxlev - minlev) / kGatherLevels + 1;
-    auto band_of = [&](int lev) { return (lev - minlev) / kGatherLevels; };
-    std::vector<std::vector<int>> by(nb);
-    for (size_t i = 0; i < T.nodes.size(); ++i)
-        if (T.nodes[i].kind) by[band_of(T.nodes[i].level)].push_back((int)i);
-    for (int b = 0; b < nb; ++b) {
-        std::sort(by[b].begin(), by[b].end(), [&](int u, int v) { return T.nodes[u].slot < T.nodes[v].slot; });
-        for (int id : by[b]) {
-            hm_gnode g;
-            g.slot = T.nodes[id].slot; g.begin = (int32_t)srcs.size(); g.pad = 0;
-            srcs.push_back({T.nodes[id].slot, -1, 0, 0});
-            int cur = id, len = 0, bits = 0;
-            while (true) {
-                const int par = T.nodes[cur].parent;
-                if (par < 0 || T.nodes[par].kind == 0) break;
-                const int c = T.nodes[par].child[1] == cur ? 1 : 0;
-                bits |= c << len;          // bits read from the ancestor down: first step is the top bit
-                len += 1;
-                const bool in_band = band_of(T.nodes[par].level) == b;
-                srcs.push_back({T.nodes[par].slot, path_mat(len, bits), in_band ? 0 : 1, 0});
-                if (!in_band) break;
-                cur = par;
-            }
-            g.end = (int32_t)srcs.size();
-            nodes.push_back(g);
-        }
-        band_ptr.push_back((int)nodes.size());
-    }
-}
-
 // Groups the internal basis nodes into bands of kBandLevels levels (counted
 // from the deepest internal level).  Within a band, a task is the set of
 // nodes sharing the same topmost in-band ancestor; its steps are its levels,
@@ -357,8 +271,6 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
 
     band_transfers(P.Y, true, P.up_ents, P.up_steps, P.up_tasks, P.up_band_ptr);
     band_transfers(P.X, false, P.down_ents, P.down_steps, P.down_tasks, P.down_band_ptr);
-    gather_up(P.Y, P.gup_nodes, P.gup_srcs, P.gup_band_ptr);
-    gather_down(P.X, P.gdown_nodes, P.gdown_srcs, P.gdown_band_ptr);
 
     // M2L rows: barycentric blocks grouped by row cluster.
     P.fstride = (int)round_up((int64_t)r * r, 4);
@@ -528,39 +440,6 @@ void merge_bands(const std::vector<Plan> &parts, bool upward, Plan &out)
     }
 }
 
-void merge_gathers(const std::vector<Plan> &parts, bool upward, Plan &out)
-{
-    std::vector<hm_gnode> &nodes = upward ? out.gup_nodes : out.gdown_nodes;
-    std::vector<hm_gsrc> &srcs = upward ? out.gup_srcs : out.gdown_srcs;
-    std::vector<int> &bptr = upward ? out.gup_band_ptr : out.gdown_band_ptr;
-    size_t nb = 0;
-    for (const Plan &p : parts) {
-        const std::vector<int> &pb = upward ? p.gup_band_ptr : p.gdown_band_ptr;
-        nb = std::max(nb, pb.size() ? pb.size() - 1 : 0);
-    }
-    bptr.assign(1, 0);
-    std::vector<int32_t> off(parts.size());
-    int32_t o = 0;
-    for (size_t i = 0; i < parts.size(); ++i) { off[i] = o; o += upward ? parts[i].n_yslots : parts[i].n_xslots; }
-    for (size_t b = 0; b < nb; ++b) {
-        for (size_t i = 0; i < parts.size(); ++i) {
-            const Plan &p = parts[i];
-            const std::vector<int> &pb = upward ? p.gup_band_ptr : p.gdown_band_ptr;
-            if (b + 1 >= pb.size()) continue;
-            const std::vector<hm_gnode> &pn = upward ? p.gup_nodes : p.gdown_nodes;
-            const std::vector<hm_gsrc> &ps = upward ? p.gup_srcs : p.gdown_srcs;
-            for (int nd = pb[b]; nd < pb[b + 1]; ++nd) {
-                hm_gnode g{pn[nd].slot + off[i], (int32_t)srcs.size(), 0, 0};
-                for (int e = pn[nd].begin; e < pn[nd].end; ++e)
-                    srcs.push_back({ps[e].slot + off[i], ps[e].mat, ps[e].from_final, 0});
-                g.end = (int32_t)srcs.size();
-                nodes.push_back(g);
-            }
-        }
-        bptr.push_back((int)nodes.size());
-    }
-}
-
 }  // namespace
 
 void merge_plans(const std::vector<Plan> &parts, Plan &P)
@@ -602,8 +481,6 @@ void merge_plans(const std::vector<Plan> &parts, Plan &P)
     P.stats.n_xslots = xs; P.stats.n_yslots = ys;
     merge_bands(parts, true, P);
     merge_bands(parts, false, P);
-    merge_gathers(parts, true, P);
-    merge_gathers(parts, false, P);
     // level tables are per instance only; the merged plan keeps them empty
     P.up_level_ptr.assign(1, 0);
     P.down_level_ptr.assign(1, 0);

@@ -71,10 +71,6 @@ struct Plan {
     std::vector<hm_step> up_steps, down_steps;
     std::vector<hm_task> up_tasks, down_tasks;
     std::vector<int> up_band_ptr, down_band_ptr;   // task ranges per band, in launch order
-    // gather bands (one parallel step per band)
-    std::vector<hm_gnode> gup_nodes, gdown_nodes;
-    std::vector<hm_gsrc> gup_srcs, gdown_srcs;
-    std::vector<int> gup_band_ptr, gdown_band_ptr;  // node ranges per band, in launch order
     std::vector<hm_xfer> down;                // x tree, top level first
     std::vector<int> down_level_ptr;
     std::vector<hm_seg> segs;
@@ -92,8 +88,6 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
                double c, double d, int r, int64_t leaf, int seg_rows, Plan &out);
 
 constexpr int kBandLevels = 4;   // tree levels per transfer band
-constexpr int kGatherLevels = 4; // tree levels per gather band (composed paths up to this length)
-constexpr int kNumPathMats = (2 << kGatherLevels) - 2;   // composed matrices for lengths 1..kGatherLevels
 
 // A user-assembled HierarchicalMatrix flattened to leaf blocks (the block
 // walk of src/HierarchicalMatrix.jl:24-52 gives each leaf its row and column

@@ -33,17 +33,6 @@ struct hm_xfer {        // coefficient transfer between a node and its two child
     int32_t slot, c0, c1, pad;
 };
 
-// Gather bands: every basis node of a band of tree levels computes its
-// coefficients in one parallel step from its contributors through composed
-// transfer matrices M_path (products of the two child transfers along the
-// path; index (1 << len) - 2 + path bits, -1 for the identity).
-// Upward: t[node] = sum M_path^T t[descendant] over the descendants at the
-// band's lower boundary and the basis leaves inside the band.  Downward:
-// s[node] = sum M_path loc[ancestor] over the node and its in-band
-// ancestors, plus M_path s[first ancestor above the band].
-struct hm_gnode { int32_t slot, begin, end, pad; };   // contributor range
-struct hm_gsrc { int32_t slot, mat, from_final, pad; };
-
 // Transfer bands: the upward (downward) transfers are grouped into bands of a
 // few tree levels; a band is one launch, each of its tasks (a subtree cut to
 // the band's levels) one CTA, which walks the task's steps (one level each)

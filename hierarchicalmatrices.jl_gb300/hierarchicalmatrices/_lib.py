@@ -32,8 +32,6 @@ VPANEL = np.dtype([("row0", "<i8"), ("off", "<i8"), ("nrows", "<i4"), ("ld", "<i
                    ("width", "<i4"), ("slot", "<i4"), ("col0", "<i4"), ("pad", "<i4")])
 XFER = np.dtype([("slot", "<i4"), ("c0", "<i4"), ("c1", "<i4"), ("pad", "<i4")])
 STEP = np.dtype([("e0", "<i4"), ("e1", "<i4")])
-GNODE = np.dtype([("slot", "<i4"), ("begin", "<i4"), ("end", "<i4"), ("pad", "<i4")])
-GSRC = np.dtype([("slot", "<i4"), ("mat", "<i4"), ("from_final", "<i4"), ("pad", "<i4")])
 TASK = np.dtype([("step0", "<i4"), ("step1", "<i4")])
 M2L_ROW = np.dtype([("slot", "<i4"), ("begin", "<i4"), ("end", "<i4"), ("pad", "<i4")])
 M2L_ENT = np.dtype([("foff", "<i8"), ("yslot", "<i4"), ("pad", "<i4")])
@@ -52,9 +50,6 @@ PLAN_TABLES = {
     "up_ents": (15, XFER), "up_steps": (16, STEP), "up_tasks": (17, TASK),
     "up_band_ptr": (18, np.dtype("<i4")), "down_ents": (19, XFER), "down_steps": (20, STEP),
     "down_tasks": (21, TASK), "down_band_ptr": (22, np.dtype("<i4")),
-    "gup_nodes": (23, GNODE), "gup_srcs": (24, GSRC), "gup_band_ptr": (25, np.dtype("<i4")),
-    "gdown_nodes": (26, GNODE), "gdown_srcs": (27, GSRC), "gdown_band_ptr": (28, np.dtype("<i4")),
-    "path_mats": (29, np.dtype("<f8")),
 }
 PLAN_SIZES = ("r", "nx", "ny", "n_xslots", "n_yslots", "vstore", "fstore", "pstore", "max_width",
               "n_bary", "n_dense", "depth", "canonical_values", "reference_values", "stored_values",

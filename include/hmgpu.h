@@ -240,8 +240,7 @@ int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, dou
    8 downward level offsets, 9 row segments, 10 pieces, 11 segment fill info,
    12 transfer matrices, 13 Chebyshev nodes, 14 barycentric weights,
    15-18 upward band records / steps / tasks / band offsets, 19-22 the same
-   for the downward bands, 23-25 upward gather nodes / contributors / band
-   offsets, 26-28 the same downward, 29 composed transfer matrices):
+   for the downward bands):
    pointer, element count and element size (records of hm_types.h). */
 /* The merged plan of hm_kernelmatrix_batch_build (same arguments). */
 int hm_batch_plan_create(int ninst, const int64_t *nx, const int64_t *ny, const double *x,

@@ -49,13 +49,6 @@ def basis(pts, a, b, cheb, lam):
     return w / w.sum(axis=1, keepdims=True)
 
 
-def _gather_bands(plan, which):
-    """Gather bands in launch order: lists of (node slot, contributor records)."""
-    nodes, srcs, bptr = plan.table(f"{which}_nodes"), plan.table(f"{which}_srcs"), plan.table(f"{which}_band_ptr")
-    for bd in range(len(bptr) - 1):
-        yield [(int(g["slot"]), srcs[g["begin"]:g["end"]]) for g in nodes[bptr[bd]:bptr[bd + 1]]]
-
-
 def _banded(plan, which):
     """Transfer records in launch order: band by band, task by task, step by step."""
     ents = plan.table(f"{which}_ents")
@@ -92,23 +85,14 @@ def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
         rows = slice(vp["row0"], vp["row0"] + vp["nrows"])
         V = basis(y[rows], vf["a"], vf["b"], cheb, lam)
         t[vp["slot"]] = V.T @ B[rows]
-    # upward gather bands (as the GPU runs them): every node of a band reads
-    # only coefficients final before the band (`done`)
-    M = plan.table("path_mats").reshape(-1, r, r) if r else None     # M[idx][m', m]
+    # upward transfers in band / task / step order (as the GPU runs them);
+    # `done` checks that every child is final before its parent reads it
     done = np.zeros(S["n_yslots"], dtype=bool)
     done[[vp["slot"] for vp in plan.table("vpanels")]] = True
-    for band in _gather_bands(plan, "gup"):
-        new = {}
-        for node, srcs in band:
-            acc = np.zeros((r, k))
-            for src in srcs:
-                assert done[src["slot"]] and src["mat"] >= 0
-                acc += M[src["mat"]].T @ t[src["slot"]]
-            new[node] = acc
-        for node, acc in new.items():
-            assert not done[node]
-            t[node] = acc
-            done[node] = True
+    for e in _banded(plan, "up"):
+        assert done[e["c0"]] and done[e["c1"]] and not done[e["slot"]]
+        t[e["slot"]] = T[0].T @ t[e["c0"]] + T[1].T @ t[e["c1"]]
+        done[e["slot"]] = True
     # far field
     ents, ff = plan.table("m2l_ents"), plan.table("f_fill")
     for row in plan.table("m2l_rows"):
@@ -120,26 +104,17 @@ def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
             F = kernel_np(kernel, yn, xn) if swap else kernel_np(kernel, xn, yn)
             acc += F @ t[ents[e]["yslot"]]
         s[row["slot"]] = acc
-    # downward gather bands: a node sums its own and its in-band ancestors'
-    # far-field results and the final coefficients of the first ancestor above
-    loc = s.copy()
-    final = np.zeros(S["n_xslots"], dtype=bool)
-    for band in _gather_bands(plan, "gdown"):
-        new = {}
-        for node, srcs in band:
-            acc = np.zeros((r, k))
-            for src in srcs:
-                if src["from_final"]:
-                    assert final[src["slot"]]
-                    v = s[src["slot"]]
-                else:
-                    v = loc[src["slot"]]
-                acc += v if src["mat"] < 0 else M[src["mat"]] @ v
-            new[node] = acc
-        for node, acc in new.items():
-            s[node] = acc
-            final[node] = True
-    assert final.all() or S["n_xslots"] == 0
+    # downward transfers in band / task / step order; a parent is final once
+    # its own parent has pushed into it
+    pushed = np.zeros(S["n_xslots"], dtype=bool)
+    has_parent = np.zeros(S["n_xslots"], dtype=bool)
+    for e in plan.table("down"):
+        has_parent[e["c0"]] = has_parent[e["c1"]] = True
+    for e in _banded(plan, "down"):
+        assert pushed[e["slot"]] or not has_parent[e["slot"]]
+        s[e["c0"]] += T[0] @ s[e["slot"]]
+        s[e["c1"]] += T[1] @ s[e["slot"]]
+        pushed[e["c0"]] = pushed[e["c1"]] = True
     # row segments
     out = np.zeros((S["nx"], k))
     covered = np.zeros(S["nx"], dtype=np.int64)
