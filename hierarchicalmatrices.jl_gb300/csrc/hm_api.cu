@@ -360,7 +360,7 @@ int ensure_smem(K kernel, size_t bytes)
 
 // Per-call scratch: coefficients t (column slots) then s (row slots).
 struct ScratchLayout {
-    size_t t_off, s_off, bytes;
+    size_t t_off, s_off, yfar_off, bytes;
 };
 
 inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
@@ -371,8 +371,18 @@ ScratchLayout scratch_layout(const hm_handle *h, int k)
     ScratchLayout L;
     L.t_off = 0;
     L.s_off = align256((size_t)h->n_yslots * k * h->r * sizeof(A));
-    L.bytes = L.s_off + align256((size_t)h->n_xslots * k * h->r * sizeof(A));
+    L.yfar_off = L.s_off + align256((size_t)h->n_xslots * k * h->r * sizeof(A));
+    L.bytes = L.yfar_off;
     return L;
+}
+
+// Per-call scratch of hm_mul: the coefficients plus, for up to kPartMaxK
+// right-hand sides with the side stream, the far-field rows (nx x k, type A).
+template <typename A>
+size_t stream_scratch_bytes(const hm_handle *h, int k)
+{
+    const ScratchLayout L = scratch_layout<A>(h, k);
+    return L.yfar_off + (k <= 8 ? align256((size_t)h->nx * k * sizeof(A)) : 0);
 }
 
 // Scratch, side stream and fork/join events for products issued on stream st.
@@ -458,25 +468,28 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
 }
 
 template <typename S, typename A, bool FAR, int KB>
-int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
+int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, S *yfar,
+                   cudaStream_t st)
 {
     const int maxw = std::max(h->max_width, 1);
     const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(A);
     HM_TRY(ensure_smem(expand_part<S, A, FAR, KB>, smem));
     expand_part<S, A, FAR, KB><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
-        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(panels), s, t, h->r, maxw);
+        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(panels), s, t, h->r, maxw, yfar);
     HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
     return HM_OK;
 }
 
-// Near-field (FAR = false) or far-field (FAR = true) panel columns for k <= 8.
+// Near-field (FAR = false) or far-field (FAR = true) panel columns for k <= 8;
+// with yfar the far-field rows go to yfar (leading dimension ldy of ma).
 template <typename S, typename A, bool FAR>
-int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
+int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st,
+                S *yfar = nullptr)
 {
-    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, st);
-    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, st);
-    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, st);
-    return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, st);
+    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st);
+    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st);
+    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, yfar, st);
+    return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, yfar, st);
 }
 
 template <typename S, typename A>
@@ -492,9 +505,10 @@ int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, 
     return HM_OK;
 }
 
-// One product.  With a side stream the tree passes run there, concurrently
-// with the near-field panels on the caller's stream; the far field U s is
-// added after the join.  side == st runs everything in order on st.
+// One product.  With a side stream the tree passes and the far-field rows
+// (U s, into the scratch vector yfar) run there, concurrently with the
+// near-field panels on the caller's stream; yfar is added to y after the join.
+// side == st runs everything in order on st.
 template <typename S, typename A>
 int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStream_t side, cudaEvent_t fork,
                     cudaEvent_t join, void *scratch, bool timing, const void *panels = nullptr)
@@ -512,18 +526,37 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
             HM_CK(cudaStreamWaitEvent(side, fork, 0));
         }
         HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing)));
-        if (split) HM_CK(cudaEventRecord(join, side));
+        if (split && (k > kPartMaxK || !h->n_segs)) HM_CK(cudaEventRecord(join, side));
     }
     if (!h->n_segs) {
         if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
         return HM_OK;
     }
     if (k <= kPartMaxK) {
+        if (tree && split) {
+            // far-field rows on the side stream, into yfar (nx x k, leading dimension nx)
+            S *yfar = reinterpret_cast<S *>(static_cast<char *>(scratch) + L.yfar_off);
+            MulArgs<S> mf = ma;
+            mf.ldy = h->nx;
+            {
+                StageTimer tm(h, timing ? 3 : -1, side);
+                HM_TRY((launch_part<S, A, true>(h, mf, s, t, panels, side, yfar)));
+            }
+            HM_CK(cudaEventRecord(join, side));
+            {
+                StageTimer tm(h, timing ? 2 : -1, st);
+                HM_TRY((launch_part<S, A, false>(h, ma, s, t, panels, st)));
+            }
+            HM_CK(cudaStreamWaitEvent(st, join, 0));
+            const int64_t nk = h->nx * (int64_t)k;
+            add_far<S><<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(ma, h->nx, yfar, h->nx);
+            HM_CK_LAUNCH("add_far");
+            return HM_OK;
+        }
         {
             StageTimer tm(h, timing ? 2 : -1, st);
             HM_TRY((launch_part<S, A, false>(h, ma, s, t, panels, st)));
         }
-        if (tree && split) HM_CK(cudaStreamWaitEvent(st, join, 0));
         if (tree) {
             StageTimer tm(h, timing ? 3 : -1, st);
             HM_TRY((launch_part<S, A, true>(h, ma, s, t, panels, st)));
@@ -540,7 +573,7 @@ int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st, const void *panels = n
 {
     if (ma.k <= 0) return HM_OK;
     hm_handle::StreamCtx *sc = nullptr;
-    HM_TRY(stream_ctx(h, st, scratch_layout<A>(h, ma.k).bytes, &sc));
+    HM_TRY(stream_ctx(h, st, stream_scratch_bytes<A>(h, ma.k), &sc));
     return launch_pipeline<S, A>(h, ma, st, h->overlap ? sc->side : st, sc->fork, sc->join, sc->p, true, panels);
 }
 

@@ -410,7 +410,7 @@ struct SegAcc {
 
 template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                            const A *s, const A *t, int r, int maxw)
+                            const A *s, const A *t, int r, int maxw, S *yfar)
 {
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -420,14 +420,14 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
     A *g = reinterpret_cast<A *>(smem_raw) + (int64_t)wib * maxw * KB;
     const hm_seg G = segs[seg];
     const int k = ma.k;
-    // gather the right-hand sides of the columns this part uses
-    int pcs[2] = {0, 0};          // piece range [pc0, pc1) of the part
+    // gather the right-hand sides of the columns this part uses; the part's
+    // pieces are one contiguous column run [c0, c1) of the panel
     int c0 = -1, c1 = 0, col = 0;
     for (int pc = 0; pc < G.npieces; ++pc) {
         const hm_piece Q = pieces[G.piece0 + pc];
         const bool take = FAR ? (Q.kind != HM_PIECE_X) : (Q.kind == HM_PIECE_X);
         if (take) {
-            if (c0 < 0) { c0 = col; pcs[0] = pc; }
+            if (c0 < 0) c0 = col;
             const A *coef = Q.kind == HM_PIECE_TCOEF ? t : s;
             for (int i = lane; i < Q.width * KB; i += 32) {
                 const int c = i / KB, q = i % KB;
@@ -438,17 +438,19 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
                 g[(col + c) * KB + q] = v;
             }
             c1 = col + Q.width;
-            pcs[1] = pc + 1;
         }
         col += Q.width;
     }
     if (c0 < 0) {
-        if (FAR) return;          // no far field on these rows
+        if (FAR && !yfar) return;          // no far field on these rows
         c0 = c1 = 0;
     }
     __syncwarp();
     const S *Pg = P + G.poff;
-    const bool acc_y = FAR || ma.accumulate;
+    // FAR with yfar: write the far-field rows to yfar (added to y later);
+    // FAR without: add into y; near field: y (+)= per the caller's flag
+    const bool acc_y = FAR ? (yfar == nullptr) : (ma.accumulate != 0);
+    constexpr int FOLD = 64;              // columns between compensated folds (KB > 1)
     if (sizeof(S) == 4) {
         const int rg = lane & 15, h = lane >> 4;
         SegAcc<A, KB> acc[4];
@@ -457,18 +459,18 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
         if (4 * rg < G.ld) {
             const float4 *base = reinterpret_cast<const float4 *>(Pg + 4 * rg);
             const int64_t ld4 = G.ld / 4;
-            int cp = c0;
-            for (int pc = pcs[0]; pc < pcs[1]; ++pc) {
-                const int ce = cp + pieces[G.piece0 + pc].width;
-                int c = cp + ((h - cp) & 1);             // this half's first column (parity h)
-                for (; c + 6 < ce; c += 8) {
-                    const float4 p0 = __ldcs(base + ld4 * c), p1 = __ldcs(base + ld4 * (c + 2));
-                    const float4 p2 = __ldcs(base + ld4 * (c + 4)), p3 = __ldcs(base + ld4 * (c + 6));
-                    const A *g0 = g + c * KB, *g1 = g + (c + 2) * KB, *g2 = g + (c + 4) * KB, *g3 = g + (c + 6) * KB;
-                    acc[0].add(p0.x, g0); acc[1].add(p0.y, g0); acc[2].add(p0.z, g0); acc[3].add(p0.w, g0);
-                    acc[0].add(p1.x, g1); acc[1].add(p1.y, g1); acc[2].add(p1.z, g1); acc[3].add(p1.w, g1);
-                    acc[0].add(p2.x, g2); acc[1].add(p2.y, g2); acc[2].add(p2.z, g2); acc[3].add(p2.w, g2);
-                    acc[0].add(p3.x, g3); acc[1].add(p3.y, g3); acc[2].add(p3.z, g3); acc[3].add(p3.w, g3);
+            for (int cb = c0; cb < c1; cb += FOLD) {
+                const int ce = min(c1, cb + FOLD);
+                int c = cb + ((h - cb) & 1);             // this half's columns have parity h
+                for (; c + 14 < ce; c += 16) {
+                    float4 p[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) p[u] = __ldcs(base + ld4 * (c + 2 * u));
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const A *gu = g + (c + 2 * u) * KB;
+                        acc[0].add(p[u].x, gu); acc[1].add(p[u].y, gu); acc[2].add(p[u].z, gu); acc[3].add(p[u].w, gu);
+                    }
                 }
                 for (; c < ce; c += 2) {
                     const float4 p0 = __ldcs(base + ld4 * c);
@@ -477,7 +479,6 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
                 }
 #pragma unroll
                 for (int j = 0; j < 4; ++j) acc[j].fold();
-                cp = ce;
             }
         }
 #pragma unroll
@@ -495,10 +496,14 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
                 for (int j = 0; j < 4; ++j) {
                     const int row = 4 * rg + j;
                     if (row < G.nrows) {
-                        S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
-                        A v = val[j];
-                        if (acc_y) v += (A)(*yp);
-                        *yp = (S)v;
+                        if (FAR && yfar) {
+                            yfar[(G.row0 + row) + (int64_t)q * ma.ldy] = (S)val[j];
+                        } else {
+                            S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
+                            A v = val[j];
+                            if (acc_y) v += (A)(*yp);
+                            *yp = (S)v;
+                        }
                     }
                 }
             }
@@ -509,24 +514,21 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
         if (2 * lane < G.ld) {
             const double2 *base = reinterpret_cast<const double2 *>(Pg + 2 * lane);
             const int64_t ld2 = G.ld / 2;
-            int cp = c0;
-            for (int pc = pcs[0]; pc < pcs[1]; ++pc) {
-                const int ce = cp + pieces[G.piece0 + pc].width;
-                int c = cp;
-                for (; c + 4 <= ce; c += 4) {
-                    const double2 p0 = __ldcs(base + ld2 * c), p1 = __ldcs(base + ld2 * (c + 1));
-                    const double2 p2 = __ldcs(base + ld2 * (c + 2)), p3 = __ldcs(base + ld2 * (c + 3));
-                    a0.add(p0.x, g + c * KB); a1.add(p0.y, g + c * KB);
-                    a0.add(p1.x, g + (c + 1) * KB); a1.add(p1.y, g + (c + 1) * KB);
-                    a0.add(p2.x, g + (c + 2) * KB); a1.add(p2.y, g + (c + 2) * KB);
-                    a0.add(p3.x, g + (c + 3) * KB); a1.add(p3.y, g + (c + 3) * KB);
+            for (int cb = c0; cb < c1; cb += FOLD) {
+                const int ce = min(c1, cb + FOLD);
+                int c = cb;
+                for (; c + 8 <= ce; c += 8) {
+                    double2 p[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) p[u] = __ldcs(base + ld2 * (c + u));
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) { a0.add(p[u].x, g + (c + u) * KB); a1.add(p[u].y, g + (c + u) * KB); }
                 }
                 for (; c < ce; ++c) {
                     const double2 p0 = __ldcs(base + ld2 * c);
                     a0.add(p0.x, g + c * KB); a1.add(p0.y, g + c * KB);
                 }
                 a0.fold(); a1.fold();
-                cp = ce;
             }
         }
 #pragma unroll
@@ -537,14 +539,30 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
             for (int j = 0; j < 2; ++j) {
                 const int row = 2 * lane + j;
                 if (row < G.nrows) {
-                    S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
-                    A v = v2[j];
-                    if (acc_y) v += (A)(*yp);
-                    *yp = (S)v;
+                    if (FAR && yfar) {
+                        yfar[(G.row0 + row) + (int64_t)q * ma.ldy] = (S)v2[j];
+                    } else {
+                        S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
+                        A v = v2[j];
+                        if (acc_y) v += (A)(*yp);
+                        *yp = (S)v;
+                    }
                 }
             }
         }
     }
+}
+
+// y[i*incy + q*ldy] += yfar[i + q*ldf]: adds the far-field rows computed on the
+// side stream (after the join).
+template <typename S>
+__global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * ma.k) return;
+    const int64_t row = i % n, q = i / n;
+    S *yp = ma.y + row * ma.incy + q * ma.ldy;
+    *yp = *yp + yfar[row + q * ldf];
 }
 
 // Row segments, several right-hand sides.  One CTA (128 threads) per
@@ -674,9 +692,9 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
 
 #define HM_INST_PART(S, A, KB)                                                                       \
     template __global__ void expand_part<S, A, false, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *, \
-                                                          const S *, const A *, const A *, int, int);   \
+                                                          const S *, const A *, const A *, int, int, S *); \
     template __global__ void expand_part<S, A, true, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
-                                                         const S *, const A *, const A *, int, int);
+                                                         const S *, const A *, const A *, int, int, S *);
 #define HM_INST_MV(S, A)                                                                             \
     template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
     template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
@@ -697,6 +715,8 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                                   const A *, A *, int, int);
 HM_INST_MV(double, double)
 HM_INST_MV(float, float)
+template __global__ void add_far<double>(MulArgs<double>, int64_t, const double *, int64_t);
+template __global__ void add_far<float>(MulArgs<float>, int64_t, const float *, int64_t);
 
 // ============================================================== direct sums
 

@@ -159,7 +159,10 @@ __global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const
 
 template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                            const A *s, const A *t, int r, int maxw);
+                            const A *s, const A *t, int r, int maxw, S *yfar);
+
+template <typename S>
+__global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf);
 
 template <typename S, typename A>
 __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s,
