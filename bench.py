@@ -36,6 +36,22 @@ def grid_points(n):
     return x, y
 
 
+def profiled_traffic(n):
+    """DRAM bytes (read + write) per launch of the near-field kernel from the
+    committed ncu summary of the n = 2^20 workload, or None."""
+    if n != N_DEFAULT:
+        return None
+    p = os.path.join(REPO, "profiles", "expand_near_kernelmatrix_cauchy_n2p20_fp32.md")
+    try:
+        with open(p) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch"):
+                    return float(ln.split("=")[1]) / 1e9
+    except OSError:
+        pass
+    return None
+
+
 def peaks():
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -459,7 +475,7 @@ def main():
             "roofline": {
                 "bound": "hbm", "kernel": "expand_part<float,float,false> (near-field row-segment panels)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None,
+                "frac": achieved / hbm_peak, "traffic": profiled_traffic(n), "traffic_unit": "GB per launch",
                 "peak_source": peak_kind, "kernel_ms": exp_ms, "kernel_bytes": exp_bytes,
                 "stage_ms_serial": stages,
             },

@@ -885,7 +885,7 @@ int build_from_plan(int kernel, int swap, hm_plan *pl, const double *x, const do
         return c;
     };
     h->launches_per_mul = (h->n_vp > 0) + nonempty(h->up_band_ptr) + (h->n_m2l_rows > 0) + nonempty(h->down_band_ptr) +
-                          (h->n_segs > 0) * (1 + ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
+                          (h->n_segs > 0) * (1 + 2 * ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
     if (st) { hm_free(h); return st; }
     *out = h;
     return HM_OK;
@@ -963,7 +963,8 @@ int hm_hier_build(int storage, int64_t m, int64_t n, int nblocks, const int32_t 
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
     const int st = storage == HM_F64 ? build_hier_device<double>(h, P, vs, fs, ps, cs)
                                      : build_hier_device<float>(h, P, vs, fs, ps, cs);
-    h->launches_per_mul = (h->n_vp > 0) + (h->n_m2l_rows > 0) + (h->n_segs > 0) * (1 + (h->n_vp > 0));
+    h->launches_per_mul = (h->n_vp > 0) + (h->n_m2l_rows > 0) +
+                          (h->n_segs > 0) * (1 + 2 * ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
     if (st) { hm_free(h); return st; }
     *out = h;
     return HM_OK;

@@ -136,7 +136,7 @@ int hm_storage(const hm_handle *h);
 /* Statistics: out[0..] = barycentric blocks, dense blocks, tree depth, row slots,
    column slots, canonical stored values, reference-layout values, values this
    build stores, dense values, row segments, max panel width, device bytes,
-   kernel launches per single-RHS hm_mul.
+   kernel launches per single-RHS hm_mul with the side stream on (the default).
    Returns the number of values written (<= nout). */
 int hm_stats(const hm_handle *h, int64_t *out, int nout);
 
