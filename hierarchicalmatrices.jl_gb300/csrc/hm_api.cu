@@ -61,9 +61,7 @@ int cuda_status(cudaError_t e, const char *what)
 
 constexpr int kSegRows = 64;
 #define HM_NSTAGES 4   // upward pass, far field + downward pass, near-field panels, far-field panels
-constexpr int kWarpCta = 256;
-
-inline unsigned warp_grid(int64_t warps) { return (unsigned)((warps * 32 + kWarpCta - 1) / kWarpCta); }
+constexpr int kWarpCta = 256;   // threads of the band-transfer CTAs
 
 // sin(pi t) in extended precision, rounded once; t is formed in double like
 // the reference's (n-2k+1)/2n.
@@ -155,6 +153,14 @@ struct hm_handle {
     hm_seg *d_segs = nullptr;
     int n_segs = 0;
     hm_piece *d_pieces = nullptr;
+    // persistent panel streaming: CTA b of part p (0 near, 1 far) owns the
+    // segments [d_cta_seg[p*(stream_ctas+1) + b], ... + b + 1)
+    int *d_cta_seg = nullptr;
+    int stream_ctas = 0;
+    int part_width[2] = {0, 0};     // widest near / far column run of a segment
+    int part_segs[2] = {0, 0};      // most segments of one CTA (near / far)
+    int part_pieces[2] = {0, 0};    // most piece records of one CTA
+    int *d_status = nullptr;        // device-side status word (HM_DEV_*), 0 when clean
 
     std::mutex mu;
     // Per caller stream: coefficient scratch (grown stream-ordered), the side
@@ -217,6 +223,66 @@ int check_points(const double *x, int64_t n, const char *name)
     return HM_OK;
 }
 
+// Per-segment part widths and the CTA ranges of the streaming kernels: two
+// CTAs per SM, each owning a run of consecutive segments with about the same
+// number of panel bytes (plus a fixed cost per segment).  Streaming needs
+// the far-field pieces of every segment before its X pieces.
+int prepare_streaming(hm_handle *h, const std::vector<hm_seg> &segs, const std::vector<hm_piece> &pieces,
+                      cudaStream_t st)
+{
+    HM_TRY(h->alloc(&h->d_status, 1));
+    HM_CK(cudaMemsetAsync(h->d_status, 0, sizeof(int), st));
+    h->stream_ctas = 0;
+    if (segs.empty()) return HM_OK;
+    for (const hm_seg &g : segs) {
+        int nfar = 0;
+        bool seen_x = false;
+        for (int i = 0; i < g.npieces; ++i) {
+            const hm_piece &q = pieces[g.piece0 + i];
+            if (q.kind == HM_PIECE_X) { seen_x = true; continue; }
+            if (seen_x) return HM_OK;                 // not far-first: keep the per-warp kernels
+            nfar += q.width;
+        }
+        if (nfar != g.nfar || g.ld % 4 || g.poff % 32 || g.nrows > 64) return HM_OK;
+        if (&g != &segs[0] && g.piece0 != (&g)[-1].piece0 + (&g)[-1].npieces) return HM_OK;
+        h->part_width[0] = std::max(h->part_width[0], g.width - g.nfar);
+        h->part_width[1] = std::max(h->part_width[1], g.nfar);
+    }
+    int dev = 0, sms = 0;
+    HM_CK(cudaGetDevice(&dev));
+    HM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(2 * (int64_t)sms, (int64_t)segs.size()));
+    std::vector<int> split(2 * (size_t)(G + 1));
+    std::vector<double> pre(segs.size() + 1);
+    for (int part = 0; part < 2; ++part) {
+        pre[0] = 0;
+        for (size_t j = 0; j < segs.size(); ++j) {
+            const hm_seg &g = segs[j];
+            const int cols = part == 0 ? g.width - g.nfar : g.nfar;
+            pre[j + 1] = pre[j] + (double)cols * g.ld + 512.0;
+        }
+        int *sp = split.data() + (size_t)part * (G + 1);
+        for (int b = 0; b <= G; ++b) {
+            const double target = pre.back() * b / G;
+            sp[b] = (int)(std::lower_bound(pre.begin(), pre.end(), target) - pre.begin());
+            if (b == G) sp[b] = (int)segs.size();
+            sp[b] = std::min<int>(sp[b], (int)segs.size());
+            if (b > 0) sp[b] = std::max(sp[b], sp[b - 1]);
+        }
+        sp[0] = 0;
+        h->part_segs[part] = h->part_pieces[part] = 0;
+        for (int b = 0; b < G; ++b) {
+            if (sp[b + 1] <= sp[b]) continue;
+            const hm_seg &f = segs[sp[b]], &l = segs[sp[b + 1] - 1];
+            h->part_segs[part] = std::max(h->part_segs[part], sp[b + 1] - sp[b]);
+            h->part_pieces[part] = std::max(h->part_pieces[part], l.piece0 + l.npieces - f.piece0);
+        }
+    }
+    HM_TRY(h->upload(&h->d_cta_seg, split, st));
+    h->stream_ctas = G;
+    return HM_OK;
+}
+
 template <typename S>
 int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, const std::vector<double> &lam,
                  const std::vector<double> &T, const double *x, const double *y, cudaStream_t st)
@@ -257,6 +323,7 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     HM_TRY(h->upload(&h->d_segs, P.segs, st));
     h->n_segs = (int)P.segs.size();
     HM_TRY(h->upload(&h->d_pieces, P.pieces, st));
+    HM_TRY(prepare_streaming(h, P.segs, P.pieces, st));
     hm_fill_seg *sf = nullptr;
     HM_TRY(h->upload(&sf, P.seg_fill, st));
     h->d_seg_fill = sf;
@@ -323,6 +390,7 @@ int build_hier_device(hm_handle *h, const Plan &P, const std::vector<double> &vs
     HM_TRY(h->upload(&h->d_segs, P.segs, st));
     h->n_segs = (int)P.segs.size();
     HM_TRY(h->upload(&h->d_pieces, P.pieces, st));
+    HM_TRY(prepare_streaming(h, P.segs, P.pieces, st));
     h->up_band_ptr = P.up_band_ptr;
     h->down_band_ptr = P.down_band_ptr;
     h->fstride = P.fstride;
@@ -441,7 +509,8 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     {
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
-            const size_t smem = (size_t)kWarpsPerCta * h->fstride * sizeof(S);
+            const size_t smem =
+                (size_t)kWarpsPerCta * (2 * (size_t)h->fstride * sizeof(S) + 2 * (size_t)QC * HM_RMAX * sizeof(A));
             HM_TRY(ensure_smem(m2l<S, A, QC>, smem));
             m2l<S, A, QC><<<warp_ctas((int64_t)h->n_m2l_rows * nq), 32 * kWarpsPerCta, smem, st>>>(
                 h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
@@ -467,10 +536,35 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
     return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing);
 }
 
+constexpr int kNearStages = 8;       // ring stages (8 KB each) of the streaming kernels
+constexpr int kFarStages = 4;
+constexpr size_t kStreamSmemMax = 110 * 1024;   // two CTAs per SM
+
 template <typename S, typename A, bool FAR, int KB>
 int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, S *yfar,
                    cudaStream_t st)
 {
+    if (!FAR && h->stream_ctas > 0) {      // far-field runs are short: one warp per segment serves them better
+        const int nst = FAR ? kFarStages : kNearStages;
+        const int part = FAR ? 1 : 0;
+        const int gcap = std::max(h->part_width[part], 1);
+        // right-hand sides gathered three segments ahead when that fits, else one
+        int ngb = 4;
+        size_t smem = 0;
+        for (; ngb >= 2; ngb -= 2) {
+            smem = stream_smem_bytes(nst, gcap, ngb, KB, (int)sizeof(A), h->part_segs[part], h->part_pieces[part]);
+            if (smem <= kStreamSmemMax) break;
+        }
+        if (smem <= kStreamSmemMax) {
+            HM_TRY(ensure_smem(stream_part<S, A, FAR, KB>, smem));
+            stream_part<S, A, FAR, KB><<<h->stream_ctas, kStreamThreads, smem, st>>>(
+                ma, h->d_segs, h->d_cta_seg + (FAR ? h->stream_ctas + 1 : 0), h->d_pieces,
+                static_cast<const S *>(panels), s, t, h->r, nst, gcap, ngb, h->part_segs[part], yfar,
+                h->d_status);
+            HM_CK_LAUNCH(FAR ? "stream_far" : "stream_near");
+            return HM_OK;
+        }
+    }
     const int maxw = std::max(h->max_width, 1);
     const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(A);
     HM_TRY(ensure_smem(expand_part<S, A, FAR, KB>, smem));
@@ -1130,6 +1224,18 @@ int hm_stats(const hm_handle *h, int64_t *out, int nout)
     const int w = std::min(nv, nout);
     for (int i = 0; i < w; ++i) out[i] = v[i];
     return w;
+}
+
+int hm_device_status(hm_handle *h, int *code, int reset)
+{
+    if (!h || !code) return HM_ERR_INVALID_ARG;
+    *code = 0;
+    if (!h->d_status) return HM_OK;
+    HM_CK(cudaDeviceSynchronize());
+    HM_CK(cudaMemcpy(code, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (reset) HM_CK(cudaMemset(h->d_status, 0, sizeof(int)));
+    if (h->trans && *code == 0) return hm_device_status(h->trans, code, reset);
+    return HM_OK;
 }
 
 int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs, int accumulate,

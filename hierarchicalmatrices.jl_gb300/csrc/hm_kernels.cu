@@ -144,6 +144,95 @@ template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, co
 // near-field dense panels on the caller's stream; after the join
 // expand_part<.., true> adds the far field U s.
 
+// Asynchronous copies, mbarriers and compensated folds shared by the kernels below.
+namespace {
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+constexpr unsigned long long kDrainLimitNs = 200000000ull;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the completion of the phase of `bar` with the given parity;
+// false once limit_ns has passed.
+__device__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned long long limit_ns)
+{
+    if (mbar_test(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_test(bar, parity))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+// bytes (a multiple of 16) from 16-byte aligned global src to 16-byte
+// aligned shared dst, completing on bar.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+template <int B>
+__device__ __forceinline__ void async_copy(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(B) : "memory");
+}
+// 16 bytes, global -> shared, bypassing L1 (both addresses 16-byte aligned)
+__device__ __forceinline__ void async_copy16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void async_wait_all()
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+__device__ __forceinline__ void async_commit()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+// waits until at most `pending` (0..2) of this thread's latest cp.async groups are in flight
+__device__ __forceinline__ void async_wait_pending(int pending)
+{
+    if (pending <= 0) asm volatile("cp.async.wait_group 0;" ::: "memory");
+    else if (pending == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else asm volatile("cp.async.wait_group 2;" ::: "memory");
+}
+// hi + lo += p: compensated (TwoSum) for FP32; FP64 adds plainly (its
+// products are exact enough, and FP64 adds are scarce on this part).
+__device__ __forceinline__ void fold(float &hi, float &lo, float p)
+{
+    const float sm = hi + p;
+    const float bp = sm - hi;
+    lo += (hi - (sm - bp)) + (p - bp);
+    hi = sm;
+}
+__device__ __forceinline__ void fold(double &hi, double &, double p) { hi += p; }
+}  // namespace
+
 // t[slot][col0 + m] = (V^T x)[m] for each explicit basis panel.  One warp
 // per (panel, chunk of QC right-hand sides); lane m owns column m of the
 // row-major panel (width <= 32, row stride ld).  Panels of up to 64 rows are
@@ -171,17 +260,19 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
         S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * (64 * HM_RMAX + 64 * QC);
         A *xs = reinterpret_cast<A *>(Vs + 64 * HM_RMAX);    // xs[j * QC + qq]
         const int nel = P.nrows * pw;
+        // all of the panel's loads in flight at once (cp.async), then one wait
         if (sizeof(S) * nel % 16 == 0 && (P.off * sizeof(S)) % 16 == 0) {
-            const float4 *src = reinterpret_cast<const float4 *>(Vp);
-            float4 *dst = reinterpret_cast<float4 *>(Vs);
-            for (int i = lane; i < (int)(nel * sizeof(S) / 16); i += 32) dst[i] = __ldcs(src + i);
+            const char *src = reinterpret_cast<const char *>(Vp);
+            char *dst = reinterpret_cast<char *>(Vs);
+            for (int i = lane; i < (int)(nel * sizeof(S) / 16); i += 32) async_copy16(dst + 16 * i, src + 16 * i);
         } else {
-            for (int i = lane; i < nel; i += 32) Vs[i] = Vp[i];
+            for (int i = lane; i < nel; i += 32) async_copy<sizeof(S)>(Vs + i, Vp + i);
         }
         for (int i = lane; i < P.nrows * QC; i += 32) {
             const int j = i / QC, qq = i % QC;
             xs[i] = qq < qc ? (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx] : (A)0;
         }
+        async_wait_all();
         __syncwarp();
         if (lane < pw) {
             for (int j = 0; j < P.nrows; ++j) {
@@ -257,42 +348,62 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
 
 // Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
 // (the F stage of src/algebra.jl:258-265, grouped by row cluster).  One warp
-// per (row slot, chunk of up to 8 right-hand sides); each r x r block is
-// staged in shared memory with 16-byte loads by all lanes and used for every
-// right-hand side of the chunk; column coefficients are loaded one per lane
-// and broadcast with shuffles.
+// per (row slot, chunk of up to QC right-hand sides).  The r x r blocks of the
+// row and the column coefficients they multiply are double-buffered in
+// shared memory with cp.async: block e + 1 is in flight while block e is
+// used for every right-hand side of the chunk.  Lane m accumulates row m.
 template <typename S, typename A, int QC>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
                     const A *t, A *s, int r, int k)
 {
     extern __shared__ unsigned char smem_raw[];
-    constexpr int VE = 16 / sizeof(S);
-    S *Fb = reinterpret_cast<S *>(smem_raw) + (threadIdx.x >> 5) * fstride;
+    // per warp: two F blocks (fstride values of S) and two column-coefficient chunks (QC * HM_RMAX of A)
+    const int wib = threadIdx.x >> 5;
+    const size_t wbytes = 2 * (size_t)fstride * sizeof(S) + 2 * (size_t)QC * HM_RMAX * sizeof(A);
+    S *Fb = reinterpret_cast<S *>(smem_raw + wib * wbytes);
+    A *Tb = reinterpret_cast<A *>(Fb + 2 * fstride);
     const int lane = threadIdx.x & 31;
     const int nq = (k + QC - 1) / QC;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (w >= (int64_t)nrows * nq) return;
     const hm_m2l_row R = rows[w / nq];
     const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
+    auto fetch = [&](int e, int buf) {
+        const hm_m2l_ent E = ents[e];
+        const char *src = reinterpret_cast<const char *>(F + E.foff);
+        char *dst = reinterpret_cast<char *>(Fb + buf * fstride);
+        for (int i = lane; i < (int)(fstride * sizeof(S) / 16); i += 32) async_copy16(dst + 16 * i, src + 16 * i);
+        A *tb = Tb + buf * QC * HM_RMAX;
+        for (int i = lane; i < QC * r; i += 32) {
+            const int qq = i / r, m = i % r;
+            if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + m, t + ((int64_t)E.yslot * k + q0 + qq) * r + m);
+            else tb[qq * HM_RMAX + m] = A(0);
+        }
+        async_commit();
+    };
     A acc[QC];
 #pragma unroll
     for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
+    if (R.begin < R.end) fetch(R.begin, 0);
     for (int e = R.begin; e < R.end; ++e) {
-        const hm_m2l_ent E = ents[e];
-        const float4 *src = reinterpret_cast<const float4 *>(F + E.foff);
-        float4 *dst = reinterpret_cast<float4 *>(Fb);
-        for (int i = lane; i < fstride / VE; i += 32) dst[i] = __ldg(src + i);
-        A tv[QC];
-#pragma unroll
-        for (int qq = 0; qq < QC; ++qq)
-            tv[qq] = (lane < r && qq < qc) ? t[((int64_t)E.yslot * k + q0 + qq) * r + lane] : (A)0;
-        __syncwarp();
-        for (int n = 0; n < r; ++n) {
-            const A f = lane < r ? (A)Fb[lane + r * n] : (A)0;
-#pragma unroll
-            for (int qq = 0; qq < QC; ++qq) acc[qq] += f * __shfl_sync(0xffffffffu, tv[qq], n);
+        const int buf = (e - R.begin) & 1;
+        if (e + 1 < R.end) {
+            fetch(e + 1, buf ^ 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            async_wait_all();
         }
         __syncwarp();
+        const S *fb = Fb + buf * fstride;
+        const A *tb = Tb + buf * QC * HM_RMAX;
+        if (lane < r) {
+            for (int n = 0; n < r; ++n) {
+                const A f = (A)fb[lane + r * n];
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tb[qq * HM_RMAX + n];
+            }
+        }
+        __syncwarp();                         // buffer buf is refilled by the next fetch
     }
     if (lane < r) {
 #pragma unroll
@@ -565,6 +676,228 @@ __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf)
     *yp = *yp + yfar[row + q * ldf];
 }
 
+// ------------------------------------------------------- streamed panels
+//
+// One persistent CTA of 256 threads per slot (two per SM).  CTA b owns the
+// segments [cta_seg[b], cta_seg[b+1]), balanced by panel bytes on the host.
+// Thread 0 streams the part's columns of those panels chunk by chunk (ld rows
+// x cc columns, one contiguous run of the column-major panel) into a ring of
+// nst shared-memory stages with cp.async.bulk; each stage's mbarrier
+// completes when its bytes have landed.  All threads consume: thread
+// (row = tid % 64, group = tid / 64) multiplies its row by a quarter of the
+// chunk's columns with plain FMA and folds the chunk's partial into a
+// compensated (TwoSum) pair.  The gathered right-hand sides of the next
+// segment are fetched with cp.async while the current one streams.  Every
+// wait is bounded: after kWaitLimitNs the CTA records HM_DEV_WAIT_TIMEOUT in
+// *status, waits (bounded) for its copies in flight and returns.
+
+
+template <typename S, typename A, bool FAR, int KB>
+__global__ void __launch_bounds__(kStreamThreads, 2)
+    stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_seg, const hm_piece *pieces, const S *P,
+                const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs, S *yfar, int *status)
+{
+    static_assert(sizeof(S) == sizeof(A), "right-hand sides are copied into shared memory as they are");
+    constexpr int CC = kChunkBytes / (64 * (int)sizeof(S));   // columns per chunk
+    constexpr int CPT = CC / 4;                                // columns per thread per chunk
+    extern __shared__ unsigned char stream_smem[];
+    const int seg_lo = cta_seg[blockIdx.x], seg_hi = cta_seg[blockIdx.x + 1];
+    if (seg_lo >= seg_hi) return;
+    const int tid = threadIdx.x, row = tid & 63, grp = tid >> 6;
+    const int k = ma.k;
+    unsigned char *ring = stream_smem;
+    uint64_t *full = reinterpret_cast<uint64_t *>(stream_smem + (size_t)nst * kChunkBytes);
+    A *gbuf = reinterpret_cast<A *>(full + nst);
+    A *red = gbuf + ngb * gcap * KB;
+    // the CTA's segment and piece records, staged once (records of one CTA
+    // are consecutive in both arrays)
+    hm_seg *sseg = reinterpret_cast<hm_seg *>(red + 3 * 64 * KB * 2);
+    hm_piece *spc = reinterpret_cast<hm_piece *>(sseg + dsegs);
+    {
+        const int ns = seg_hi - seg_lo;
+        const int p_lo = segs[seg_lo].piece0;
+        const int np = segs[seg_hi - 1].piece0 + segs[seg_hi - 1].npieces - p_lo;
+        const int64_t *gs = reinterpret_cast<const int64_t *>(segs + seg_lo);
+        int64_t *ds = reinterpret_cast<int64_t *>(sseg);
+        for (int i = tid; i < ns * (int)(sizeof(hm_seg) / 8); i += kStreamThreads) ds[i] = gs[i];
+        const int64_t *gp = reinterpret_cast<const int64_t *>(pieces + p_lo);
+        int64_t *dp = reinterpret_cast<int64_t *>(spc);
+        for (int i = tid; i < np * (int)(sizeof(hm_piece) / 8); i += kStreamThreads) dp[i] = gp[i];
+        __syncthreads();
+        for (int i = tid; i < ns; i += kStreamThreads) sseg[i].piece0 -= p_lo;
+        __syncthreads();
+    }
+
+    auto part_range = [&](const hm_seg &G, int &cb, int &ce) {
+        cb = FAR ? 0 : G.nfar;
+        ce = FAR ? G.nfar : G.width;
+    };
+    // right-hand side entries of segment j's part columns into dst (cp.async)
+    auto gather = [&](int j, A *dst) {
+        const hm_seg G = sseg[j - seg_lo];
+        int col = 0;
+        for (int pc = 0; pc < G.npieces; ++pc) {
+            const hm_piece Q = spc[G.piece0 + pc];
+            const bool take = FAR ? (Q.kind != HM_PIECE_X) : (Q.kind == HM_PIECE_X);
+            if (!take) continue;
+            for (int i = tid; i < Q.width * KB; i += kStreamThreads) {
+                const int c = i / KB, q = i % KB;
+                A *d = dst + (col + c) * KB + q;
+                if (q < k) {
+                    const void *src;
+                    if (FAR)
+                        src = (Q.kind == HM_PIECE_TCOEF ? t : s) + ((int64_t)Q.src * k + q) * r + c;
+                    else
+                        src = ma.x + (Q.src + c) * ma.incx + (int64_t)q * ma.ldx;
+                    async_copy<sizeof(A)>(d, src);
+                } else {
+                    *d = A(0);
+                }
+            }
+            col += Q.width;
+        }
+    };
+
+    // producer state (thread 0): next chunk to issue
+    int pj = seg_lo, pc = 0, pce = 0, pld = 0, issued = 0;
+    int64_t pbase = 0;
+    auto seek = [&](int j) {
+        for (; j < seg_hi; ++j) {
+            const hm_seg G = sseg[j - seg_lo];
+            int cb, ce;
+            part_range(G, cb, ce);
+            if (ce > cb) {
+                pc = cb; pce = ce; pld = G.ld; pbase = G.poff;
+                break;
+            }
+        }
+        pj = j;
+    };
+    auto issue = [&](int stage) {
+        const int cols = min(CC, pce - pc);
+        const uint32_t bytes = (uint32_t)(cols * pld) * (uint32_t)sizeof(S);
+        bulk_load(ring + (size_t)stage * kChunkBytes, P + pbase + (int64_t)pc * pld, bytes, &full[stage]);
+        ++issued;
+        pc += CC;
+        if (pc >= pce) seek(pj + 1);
+    };
+
+    if (tid == 0) {
+        for (int i = 0; i < nst; ++i) mbar_init(&full[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // right-hand sides run ngb - 1 segments ahead (one cp.async group per segment)
+    for (int j = seg_lo; j < seg_lo + ngb - 1; ++j) {
+        if (j < seg_hi) gather(j, gbuf + ((j - seg_lo) % ngb) * gcap * KB);
+        async_commit();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        seek(seg_lo);
+        for (int i = 0; i < nst && pj < seg_hi; ++i) issue(i);
+    }
+
+    int stage = 0, consumed = 0;
+    uint32_t phase = 0;
+    bool abort = false;
+    for (int j = seg_lo; j < seg_hi && !abort; ++j) {
+        async_wait_pending(ngb - 2);
+        __syncthreads();                      // g of segment j visible; g and partials of j - 1 read
+        {
+            const int ja = j + ngb - 1;       // into the buffer segment j - 1 used
+            if (ja < seg_hi) gather(ja, gbuf + ((ja - seg_lo) % ngb) * gcap * KB);
+            async_commit();
+        }
+        const hm_seg G = sseg[j - seg_lo];
+        int cb, ce;
+        part_range(G, cb, ce);
+        const A *g = gbuf + ((j - seg_lo) % ngb) * gcap * KB;
+        A hi[KB], lo[KB];
+#pragma unroll
+        for (int q = 0; q < KB; ++q) hi[q] = lo[q] = A(0);
+        const bool live = row < G.nrows;
+        // y values this segment adds to, loaded now and used at its end
+        const bool acc_y = FAR ? (yfar == nullptr && ce > cb) : (ma.accumulate != 0);
+        S yold[KB];
+#pragma unroll
+        for (int q = 0; q < KB; ++q) yold[q] = S(0);
+        if (acc_y && grp == 0 && live) {
+#pragma unroll
+            for (int q = 0; q < KB; ++q)
+                if (q < k) yold[q] = ma.y[(G.row0 + row) * ma.incy + (int64_t)q * ma.ldy];
+        }
+        for (int c0 = cb; c0 < ce; c0 += CC) {
+            const int cols = min(CC, ce - c0);
+            const bool ok = mbar_wait(&full[stage], phase, kWaitLimitNs);
+            if (ok && live) {
+                const S *st = reinterpret_cast<const S *>(ring + (size_t)stage * kChunkBytes);
+                constexpr bool kFold = sizeof(A) == 4;     // FP64 sums straight into hi
+                A part[KB];
+#pragma unroll
+                for (int q = 0; q < KB; ++q) part[q] = kFold ? A(0) : hi[q];
+#pragma unroll
+                for (int u = 0; u < CPT; ++u) {
+                    const int c = grp * CPT + u;
+                    if (c < cols) {
+                        const A pv = (A)st[c * G.ld + row];
+                        const A *gc = g + (c0 - cb + c) * KB;
+#pragma unroll
+                        for (int q = 0; q < KB; ++q) part[q] = fma(pv, gc[q], part[q]);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < KB; ++q) {
+                    if (kFold) fold(hi[q], lo[q], part[q]);
+                    else hi[q] = part[q];
+                }
+            }
+            if (__syncthreads_or(!ok)) {      // every thread leaves together
+                abort = true;
+                break;
+            }
+            ++consumed;
+            if (tid == 0 && pj < seg_hi) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(stage);
+            }
+            if (++stage == nst) { stage = 0; phase ^= 1; }
+        }
+        if (abort) break;
+        // combine the four column groups (fixed order)
+        if (grp > 0 && live) {
+            A *rd = red + ((grp - 1) * 64 + row) * KB * 2;
+#pragma unroll
+            for (int q = 0; q < KB; ++q) { rd[2 * q] = hi[q]; rd[2 * q + 1] = lo[q]; }
+        }
+        __syncthreads();
+        if (grp == 0 && live && !(FAR && !yfar && ce == cb)) {
+#pragma unroll
+            for (int q = 0; q < KB; ++q) {
+                if (q >= k) break;
+                A h0 = hi[q], l0 = lo[q];
+#pragma unroll
+                for (int gg = 0; gg < 3; ++gg) {
+                    const A *rd = red + (gg * 64 + row) * KB * 2;
+                    fold(h0, l0, rd[2 * q]);
+                    l0 += rd[2 * q + 1];
+                }
+                const A v = h0 + l0;
+                if (FAR && yfar)
+                    yfar[(G.row0 + row) + (int64_t)q * ma.ldy] = (S)v;
+                else
+                    ma.y[(G.row0 + row) * ma.incy + (int64_t)q * ma.ldy] = acc_y ? (S)((A)yold[q] + v) : (S)v;
+            }
+        }
+    }
+    if (abort) {
+        async_wait_all();
+        if (tid == 0) {
+            atomicExch(status, HM_DEV_WAIT_TIMEOUT);
+            for (int m = consumed; m < issued; ++m) mbar_wait(&full[m % nst], (m / nst) & 1, kDrainLimitNs);
+        }
+    }
+}
+
 // Row segments, several right-hand sides.  One CTA (128 threads) per
 // segment: the whole column-major panel is staged once in shared memory
 // (16-byte streaming loads), then right-hand sides are processed in chunks
@@ -695,6 +1028,13 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                                           const S *, const A *, const A *, int, int, S *); \
     template __global__ void expand_part<S, A, true, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
                                                          const S *, const A *, const A *, int, int, S *);
+#define HM_INST_STREAM(S, A, KB)                                                                      \
+    template __global__ void stream_part<S, A, false, KB>(MulArgs<S>, const hm_seg *, const int *,       \
+                                                          const hm_piece *, const S *, const A *, const A *, \
+                                                          int, int, int, int, int, S *, int *);         \
+    template __global__ void stream_part<S, A, true, KB>(MulArgs<S>, const hm_seg *, const int *,        \
+                                                         const hm_piece *, const S *, const A *, const A *,  \
+                                                         int, int, int, int, int, S *, int *);
 #define HM_INST_MV(S, A)                                                                             \
     template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
     template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
@@ -703,6 +1043,7 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     template __global__ void m2l<S, A, 8>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,    \
                                           const A *, A *, int, int);                                    \
     HM_INST_PART(S, A, 1) HM_INST_PART(S, A, 2) HM_INST_PART(S, A, 4) HM_INST_PART(S, A, 8)               \
+    HM_INST_STREAM(S, A, 1) HM_INST_STREAM(S, A, 2) HM_INST_STREAM(S, A, 4) HM_INST_STREAM(S, A, 8)       \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \
                                             const A *, const A *, int, int);                            \
     template __global__ void xfer_up_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \

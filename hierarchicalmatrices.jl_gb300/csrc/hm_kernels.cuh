@@ -164,6 +164,27 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
 template <typename S>
 __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf);
 
+// Persistent panel streaming (cp.async.bulk into a ring of shared-memory
+// stages).  CTA b owns segments [cta_seg[b], cta_seg[b+1]); FAR selects the
+// columns [0, nfar) of each panel, otherwise [nfar, width).  Shared memory:
+// stream_smem_bytes(nst, gcap, KB, sizeof(A)).
+constexpr int kStreamThreads = 256;
+constexpr int kChunkBytes = 8192;
+constexpr int HM_DEV_WAIT_TIMEOUT = 1;    // *status: a stage copy did not complete in time
+// Shared memory of stream_part: the stage ring, its mbarriers, ngb (2..4)
+// gathered right-hand-side buffers, the column-group partials and the CTA's segment
+// and piece records (at most dsegs and dpieces of them).
+__host__ __device__ constexpr size_t stream_smem_bytes(int nst, int gcap, int ngb, int kb, int asize, int dsegs,
+                                                       int dpieces)
+{
+    return (size_t)nst * kChunkBytes + (size_t)nst * 8 + (size_t)ngb * gcap * kb * asize +
+           (size_t)3 * 64 * kb * 2 * asize + (size_t)dsegs * sizeof(hm_seg) + (size_t)dpieces * sizeof(hm_piece);
+}
+template <typename S, typename A, bool FAR, int KB>
+__global__ void stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_seg, const hm_piece *pieces,
+                            const S *P, const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs,
+                            S *yfar, int *status);
+
 template <typename S, typename A>
 __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s,
                          const A *t, int r, int maxw);

@@ -363,7 +363,7 @@ int build_plan(const double *x, int64_t nx, const double *y, int64_t ny, double 
                 }
                 s.npieces = (int32_t)P.pieces.size() - s.piece0;
                 s.poff = poff;
-                s.pad = 0;
+                s.nfar = leafid >= 0 ? r : 0;
                 poff += round_up((int64_t)s.ld * std::max(s.width, 1), 32);
                 P.max_width = std::max(P.max_width, s.width);
                 P.segs.push_back(s);
@@ -573,7 +573,7 @@ int build_hier_plan(int64_t m, int64_t n, const std::vector<HierBlock> &blocks, 
             g.ld = (int32_t)round_up(g.nrows, 4);
             g.piece0 = (int32_t)P.pieces.size();
             g.width = 0;
-            g.pad = 0;
+            g.nfar = 0;
             for (int i : order) {
                 const HierBlock &b = blocks[i];
                 hm_piece pc;
@@ -581,6 +581,7 @@ int build_hier_plan(int64_t m, int64_t n, const std::vector<HierBlock> &blocks, 
                 else { pc.kind = b.kind == 1 ? HM_PIECE_TCOEF : HM_PIECE_COEF; pc.src = slot[i]; pc.width = (int32_t)b.rank; }
                 P.pieces.push_back(pc);
                 g.width += pc.width;
+                if (b.kind != 0) g.nfar += pc.width;
             }
             g.npieces = (int32_t)P.pieces.size() - g.piece0;
             g.poff = (int64_t)pstore.size();

@@ -57,7 +57,7 @@ struct hm_seg {         // y[row0 : row0+nrows) (+)= panel * gathered rhs
     int32_t width;      // total panel columns
     int32_t piece0;     // first piece record
     int32_t npieces;
-    int32_t pad;
+    int32_t nfar;       // far-field columns: the pieces other than X come first
 };
 
 enum {
@@ -71,6 +71,7 @@ struct hm_piece {       // one block column run of a segment panel
     int32_t kind;
     int32_t width;
 };
+static_assert(sizeof(hm_seg) == 40 && sizeof(hm_piece) == 16, "records are copied as 8-byte words");
 
 // Build-time only: geometry needed to fill factors on the device.
 struct hm_fill_vpanel { double a, b; };          // box of an explicit basis panel

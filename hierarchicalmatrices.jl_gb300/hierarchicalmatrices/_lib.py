@@ -26,6 +26,7 @@ HM_ERR_DEGENERATE = 9
 HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
 HM_F64, HM_F32 = 0, 1
 HM_OPT_OVERLAP = 1
+HM_PIECE_COEF, HM_PIECE_X, HM_PIECE_TCOEF = 0, 1, 2
 
 # Records of csrc/hm_types.h.
 VPANEL = np.dtype([("row0", "<i8"), ("off", "<i8"), ("nrows", "<i4"), ("ld", "<i4"),
@@ -36,7 +37,7 @@ TASK = np.dtype([("step0", "<i4"), ("step1", "<i4")])
 M2L_ROW = np.dtype([("slot", "<i4"), ("begin", "<i4"), ("end", "<i4"), ("pad", "<i4")])
 M2L_ENT = np.dtype([("foff", "<i8"), ("yslot", "<i4"), ("pad", "<i4")])
 SEG = np.dtype([("row0", "<i8"), ("poff", "<i8"), ("nrows", "<i4"), ("ld", "<i4"), ("width", "<i4"),
-                ("piece0", "<i4"), ("npieces", "<i4"), ("pad", "<i4")])
+                ("piece0", "<i4"), ("npieces", "<i4"), ("nfar", "<i4")])
 PIECE = np.dtype([("src", "<i8"), ("kind", "<i4"), ("width", "<i4")])
 FILL_VPANEL = np.dtype([("a", "<f8"), ("b", "<f8")])
 FILL_F = np.dtype([("xa", "<f8"), ("xb", "<f8"), ("ya", "<f8"), ("yb", "<f8")])
@@ -61,7 +62,7 @@ STAGES = ("up", "down", "expand", "far")
 
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
-    "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_mul", "hm_mul_strided",
+    "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_device_status", "hm_mul", "hm_mul_strided",
     "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
     "hm_bary_factors",
@@ -123,6 +124,8 @@ def _load():
     L.hm_storage.argtypes = [_vp]
     L.hm_stats.restype = ctypes.c_int
     L.hm_stats.argtypes = [_vp, _pi64, ctypes.c_int]
+    L.hm_device_status.restype = ctypes.c_int
+    L.hm_device_status.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), ctypes.c_int]
     L.hm_mul.restype = ctypes.c_int
     L.hm_mul.argtypes = [_vp, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
     L.hm_mul_t.restype = ctypes.c_int

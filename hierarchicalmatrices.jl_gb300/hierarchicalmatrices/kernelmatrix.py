@@ -143,6 +143,13 @@ class KernelMatrix:
         n = lib.hm_stats(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(out))
         return dict(zip(_lib.STATS[:n], (int(v) for v in out[:n])))
 
+    def device_status(self, reset=False):
+        """Device-side status word of the streaming kernels: 0 when clean, 1
+        when a kernel gave up waiting for a stage copy (synchronises)."""
+        code = ctypes.c_int(0)
+        check(lib.hm_device_status(self._h, ctypes.byref(code), 1 if reset else 0))
+        return code.value
+
     @property
     def handle(self):
         return self._h

@@ -140,6 +140,13 @@ int hm_storage(const hm_handle *h);
    Returns the number of values written (<= nout). */
 int hm_stats(const hm_handle *h, int64_t *out, int nout);
 
+/* Device-side status of h's kernels (and of its transpose, once built):
+   0 when clean, 1 (HM_DEV_WAIT_TIMEOUT) when a streaming kernel gave up
+   waiting for a shared-memory stage copy (its products are then invalid).
+   Synchronises the device; reset != 0 clears the word.  No reference
+   counterpart (Julia raises inside mul!). */
+int hm_device_status(hm_handle *h, int *code, int reset);
+
 /* mul!(u, H, v, istart, jstart) (src/KernelMatrix.jl:14-45), generalised to
    nrhs right-hand sides: for q < nrhs,
      u[:, q] += H * v[:, q]   (accumulate = 1, the reference's semantics)

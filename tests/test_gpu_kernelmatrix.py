@@ -245,6 +245,7 @@ def test_2pow20_fp32_error(big):
     assert err <= TOL32
     u64 = H64 @ b.double()
     assert float(torch.linalg.norm(u32.double() - u64) / torch.linalg.norm(u64)) <= TOL32
+    assert H32.device_status() == 0 and H64.device_status() == 0
 
 
 def test_repeated_calls_and_streams():
@@ -263,6 +264,7 @@ def test_repeated_calls_and_streams():
         u3 = H @ b
     s.synchronize()
     assert torch.equal(u1, u3)
+    assert H.device_status() == 0
 
 
 @pytest.mark.parametrize("kernel,sign", [(O.CAUCHY, -1.0), (O.COULOMB, 1.0), (O.COULOMB_PRIME, -1.0), (O.LOG, 1.0)])

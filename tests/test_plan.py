@@ -85,7 +85,12 @@ def test_segments_cover_rows_once():
     for s in segs:
         ps = pieces[s["piece0"]:s["piece0"] + s["npieces"]]
         assert ps["width"].sum() == s["width"]
-        assert s["ld"] >= s["nrows"] and s["poff"] % 4 == 0
+        assert s["ld"] >= s["nrows"] and s["ld"] % 4 == 0 and s["poff"] % 32 == 0
+        # far-field pieces first; nfar counts their columns (the streaming
+        # kernels copy [0, nfar) and [nfar, width) as 16-byte aligned runs)
+        far = ps["kind"] != _lib.HM_PIECE_X
+        assert not np.any(far[1:] & ~far[:-1])
+        assert ps["width"][far].sum() == s["nfar"]
 
 
 def test_validation_errors():
