@@ -149,6 +149,7 @@ struct hm_handle {
     hm_step *d_up_steps = nullptr, *d_down_steps = nullptr;
     hm_task *d_up_tasks = nullptr, *d_down_tasks = nullptr;
     std::vector<int> up_band_ptr, down_band_ptr;
+    int band_locals[2] = {0, 0};    // most task-local coefficient vectors of an upward / downward task
     int fstride = 0;
     hm_seg *d_segs = nullptr;
     int n_segs = 0;
@@ -185,6 +186,7 @@ struct hm_handle {
     int64_t stage_launches[HM_NSTAGES] = {0};
     int launches_per_mul = 0;
     bool overlap = true;            // tree passes on a side stream
+    int near_stages = 4;            // ring stages of the near-field streaming kernel
 
     template <typename T>
     int alloc(T **p, size_t count)
@@ -210,6 +212,14 @@ struct hm_handle {
 
 namespace {
 
+// Streaming kernel geometry: one CTA's chunk loop (wait, use, barrier,
+// refill) paces its stream, so three CTAs share an SM, each with a short ring.
+// CTAs own about kStreamCtaBytes of panels each rather than persisting for
+// the whole product: CTAs that retire hand their SM slots to the tree passes
+// running beside them (on the higher-priority side stream).
+constexpr int kStreamCtasPerSm = 3;
+constexpr double kStreamCtaBytes = 400.0 * 1024;
+
 int check_points(const double *x, int64_t n, const char *name)
 {
     for (int64_t i = 0; i < n; ++i) {
@@ -223,8 +233,8 @@ int check_points(const double *x, int64_t n, const char *name)
     return HM_OK;
 }
 
-// Per-segment part widths and the CTA ranges of the streaming kernels: two
-// CTAs per SM, each owning a run of consecutive segments with about the same
+// Per-segment part widths and the CTA ranges of the streaming kernels:
+// kStreamCtasPerSm CTAs per SM, each owning a run of consecutive segments with about the same
 // number of panel bytes (plus a fixed cost per segment).  Streaming needs
 // the far-field pieces of every segment before its X pieces.
 int prepare_streaming(hm_handle *h, const std::vector<hm_seg> &segs, const std::vector<hm_piece> &pieces,
@@ -251,7 +261,10 @@ int prepare_streaming(hm_handle *h, const std::vector<hm_seg> &segs, const std::
     int dev = 0, sms = 0;
     HM_CK(cudaGetDevice(&dev));
     HM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(2 * (int64_t)sms, (int64_t)segs.size()));
+    double near_bytes = 0;
+    for (const hm_seg &g : segs) near_bytes += (double)(g.width - g.nfar) * g.ld * 4.0;
+    const int64_t want = std::max<int64_t>((int64_t)kStreamCtasPerSm * sms, (int64_t)(near_bytes / kStreamCtaBytes));
+    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)segs.size()));
     std::vector<int> split(2 * (size_t)(G + 1));
     std::vector<double> pre(segs.size() + 1);
     for (int part = 0; part < 2; ++part) {
@@ -281,6 +294,25 @@ int prepare_streaming(hm_handle *h, const std::vector<hm_seg> &segs, const std::
     HM_TRY(h->upload(&h->d_cta_seg, split, st));
     h->stream_ctas = G;
     return HM_OK;
+}
+
+// Most task-local coefficient vectors over the tasks of a band table (the
+// numbering the planner stores in the records' pad).
+int band_locals(const std::vector<hm_task> &tasks, const std::vector<hm_step> &steps,
+                const std::vector<hm_xfer> &ents, bool upward)
+{
+    int most = 0;
+    for (const hm_task &tk : tasks) {
+        if (tk.step1 <= tk.step0) continue;
+        const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
+        int n = upward ? nrec : 2 * nrec;
+        for (int e = e0; e < e1; ++e) {
+            if (upward) n = std::max(n, std::max(ents[e].pad & 0xffff, ents[e].pad >> 16) + 1);
+            else n = std::max(n, ents[e].pad + 1);
+        }
+        most = std::max(most, n);
+    }
+    return most;
 }
 
 template <typename S>
@@ -319,6 +351,8 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     HM_TRY(h->upload(&h->d_down_tasks, P.down_tasks, st));
     h->up_band_ptr = P.up_band_ptr;
     h->down_band_ptr = P.down_band_ptr;
+    h->band_locals[0] = band_locals(P.up_tasks, P.up_steps, P.up_ents, true);
+    h->band_locals[1] = band_locals(P.down_tasks, P.down_steps, P.down_ents, false);
     h->fstride = P.fstride;
     HM_TRY(h->upload(&h->d_segs, P.segs, st));
     h->n_segs = (int)P.segs.size();
@@ -480,6 +514,8 @@ constexpr int kPartMaxK = 8;    // right-hand sides handled by the streaming pan
 
 inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
 
+constexpr size_t kTaskSmemMax = 200 * 1024;     // shared memory of a band task kernel
+
 // Tree passes on stream st: leaf bases, upward transfers level by level, far
 // field, downward transfers level by level.  QC right-hand sides per warp.
 template <typename S, typename A, int QC>
@@ -497,13 +533,28 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
         }
-        const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * 2 * QC * HM_RMAX) * sizeof(A);
-        HM_TRY(ensure_smem(xfer_up_band<A, QC>, xsm));
-        for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
-            const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
-            if (!n) continue;
-            xfer_up_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, r, k);
-            HM_CK_LAUNCH("xfer_up_band");
+        const size_t usm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[0] * QC * r) * sizeof(A);
+        if (nq == 1 && usm <= kTaskSmemMax) {
+            const size_t xsm = usm;
+            HM_TRY(ensure_smem(xfer_up_task<A, QC>, xsm));
+            for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
+                const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
+                if (!n) continue;
+                xfer_up_task<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t,
+                                                              r, k);
+                HM_CK_LAUNCH("xfer_up_task");
+            }
+        } else {
+            const size_t xsm =
+                (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * 2 * QC * HM_RMAX) * sizeof(A);
+            HM_TRY(ensure_smem(xfer_up_band<A, QC>, xsm));
+            for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
+                const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
+                if (!n) continue;
+                xfer_up_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t,
+                                                              r, k);
+                HM_CK_LAUNCH("xfer_up_band");
+            }
         }
     }
     {
@@ -516,14 +567,27 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
             HM_CK_LAUNCH("m2l");
         }
-        const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * QC * HM_RMAX) * sizeof(A);
-        HM_TRY(ensure_smem(xfer_down_band<A, QC>, xsm));
-        for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
-            const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
-            if (!n) continue;
-            xfer_down_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T,
-                                                            s, r, k);
-            HM_CK_LAUNCH("xfer_down_band");
+        const size_t dsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[1] * QC * r) * sizeof(A);
+        if (nq == 1 && dsm <= kTaskSmemMax) {
+            const size_t xsm = dsm;
+            HM_TRY(ensure_smem(xfer_down_task<A, QC>, xsm));
+            for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
+                const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
+                if (!n) continue;
+                xfer_down_task<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_down_tasks + b, h->d_down_steps,
+                                                                h->d_down_ents, T, s, r, k);
+                HM_CK_LAUNCH("xfer_down_task");
+            }
+        } else {
+            const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * QC * HM_RMAX) * sizeof(A);
+            HM_TRY(ensure_smem(xfer_down_band<A, QC>, xsm));
+            for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
+                const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
+                if (!n) continue;
+                xfer_down_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_down_tasks + b, h->d_down_steps,
+                                                                h->d_down_ents, T, s, r, k);
+                HM_CK_LAUNCH("xfer_down_band");
+            }
         }
     }
     return HM_OK;
@@ -536,26 +600,30 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
     return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing);
 }
 
-constexpr int kNearStages = 8;       // ring stages (8 KB each) of the streaming kernels
-constexpr int kFarStages = 4;
-constexpr size_t kStreamSmemMax = 110 * 1024;   // two CTAs per SM
+// shared memory per streaming CTA: three per SM up to two right-hand sides
+// (whose registers allow three), more for four or more (one per SM)
+constexpr size_t kStreamSmemMax3 = 74 * 1024, kStreamSmemMax1 = 200 * 1024;
 
 template <typename S, typename A, bool FAR, int KB>
 int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, S *yfar,
                    cudaStream_t st)
 {
     if (!FAR && h->stream_ctas > 0) {      // far-field runs are short: one warp per segment serves them better
-        const int nst = FAR ? kFarStages : kNearStages;
         const int part = FAR ? 1 : 0;
         const int gcap = std::max(h->part_width[part], 1);
-        // right-hand sides gathered three segments ahead when that fits, else one
-        int ngb = 4;
+        // the configured stages, right-hand sides gathered three segments
+        // ahead; fewer of either until two CTAs fit on an SM
+        const size_t smax = KB >= 4 ? kStreamSmemMax1 : kStreamSmemMax3;
+        int nst = h->near_stages, ngb = 4;
         size_t smem = 0;
-        for (; ngb >= 2; ngb -= 2) {
+        for (;;) {
             smem = stream_smem_bytes(nst, gcap, ngb, KB, (int)sizeof(A), h->part_segs[part], h->part_pieces[part]);
-            if (smem <= kStreamSmemMax) break;
+            if (smem <= smax) break;
+            if (ngb > 2) ngb = 2;
+            else if (nst > 2) --nst;
+            else break;
         }
-        if (smem <= kStreamSmemMax) {
+        if (smem <= smax) {
             HM_TRY(ensure_smem(stream_part<S, A, FAR, KB>, smem));
             stream_part<S, A, FAR, KB><<<h->stream_ctas, kStreamThreads, smem, st>>>(
                 ma, h->d_segs, h->d_cta_seg + (FAR ? h->stream_ctas + 1 : 0), h->d_pieces,
@@ -1361,6 +1429,10 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     if (!h) return HM_ERR_INVALID_ARG;
     switch (option) {
     case HM_OPT_OVERLAP: h->overlap = value != 0; return HM_OK;
+    case HM_OPT_NEAR_STAGES:
+        if (value < 2 || value > 16) { set_error("HM_OPT_NEAR_STAGES must be in [2, 16]"); return HM_ERR_INVALID_ARG; }
+        h->near_stages = (int)value;
+        return HM_OK;
     default: set_error("unknown option %d", option); return HM_ERR_INVALID_ARG;
     }
 }

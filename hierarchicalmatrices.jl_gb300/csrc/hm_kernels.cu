@@ -346,6 +346,133 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
     }
 }
 
+// Band tasks with shared-memory-resident coefficients (k <= QC): the task's
+// external inputs (and T) are fetched once with cp.async, every level then
+// reads and writes shared memory only, with a CTA barrier between levels;
+// each coefficient the task produces is also written to global memory.
+// Task-local numbering (records' pad, set by the planner): upward, record i
+// produces local i and reads locals pad & 0xffff, pad >> 16; downward,
+// record i's children are locals 2i, 2i + 1 and its parent is local pad.
+// L holds QC x r values per local.
+template <typename A, int QC>
+__global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
+                             int r, int k)
+{
+    extern __shared__ unsigned char smem_raw[];
+    A *Ts = reinterpret_cast<A *>(smem_raw);
+    A *L = Ts + 2 * HM_RMAX * HM_RMAX;
+    const hm_task tk = tasks[blockIdx.x];
+    const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
+    for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
+    const int per = 2 * QC * r;
+    for (int i = threadIdx.x; i < nrec * per; i += blockDim.x) {
+        const int rec = i / per, rem = i % per, c = rem / (QC * r), qq = (rem % (QC * r)) / r, m = rem % r;
+        const hm_xfer X = ents[e0 + rec];
+        const int lc = c ? (X.pad >> 16) : (X.pad & 0xffff);
+        if (lc < nrec) continue;                          // produced by an earlier level of this task
+        A *d = L + ((int64_t)lc * QC + qq) * r + m;
+        if (qq < k) async_copy<sizeof(A)>(d, t + ((int64_t)(c ? X.c1 : X.c0) * k + qq) * r + m);
+        else *d = A(0);
+    }
+    async_wait_all();
+    __syncthreads();
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int st = tk.step0; st < tk.step1; ++st) {
+        const hm_step S = steps[st];
+        for (int w = threadIdx.x >> 5; w < S.e1 - S.e0; w += nw) {
+            const int e = S.e0 + w;
+            const hm_xfer X = ents[e];
+            const A *c0 = L + (int64_t)(X.pad & 0xffff) * QC * r;
+            const A *c1 = L + (int64_t)(X.pad >> 16) * QC * r;
+            A *out = L + (int64_t)(e - e0) * QC * r;
+            if (lane < r) {
+                A acc[QC];
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
+                for (int mp = 0; mp < r; ++mp) {
+                    const A a0 = Ts[mp * r + lane], a1 = Ts[r * r + mp * r + lane];
+#pragma unroll
+                    for (int qq = 0; qq < QC; ++qq) acc[qq] += a0 * c0[qq * r + mp] + a1 * c1[qq * r + mp];
+                }
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) {
+                    out[qq * r + lane] = acc[qq];
+                    if (qq < k) t[((int64_t)X.slot * k + qq) * r + lane] = acc[qq];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename A, int QC>
+__global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
+                               int r, int k)
+{
+    extern __shared__ unsigned char smem_raw[];
+    A *Ts = reinterpret_cast<A *>(smem_raw);
+    A *L = Ts + 2 * HM_RMAX * HM_RMAX;
+    const hm_task tk = tasks[blockIdx.x];
+    const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
+    for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
+    // children start from their far-field (m2l) coefficients; external parents as computed
+    const int per = 3 * QC * r;
+    for (int i = threadIdx.x; i < nrec * per; i += blockDim.x) {
+        const int rec = i / per, rem = i % per, c = rem / (QC * r), qq = (rem % (QC * r)) / r, m = rem % r;
+        const hm_xfer X = ents[e0 + rec];
+        int lc, slot;
+        if (c < 2) {
+            lc = 2 * rec + c;
+            slot = c ? X.c1 : X.c0;
+        } else {
+            lc = X.pad;
+            slot = X.slot;
+            if (lc < 2 * nrec) continue;                  // a child of an earlier level of this task
+        }
+        A *d = L + ((int64_t)lc * QC + qq) * r + m;
+        if (qq < k) async_copy<sizeof(A)>(d, s + ((int64_t)slot * k + qq) * r + m);
+        else *d = A(0);
+    }
+    async_wait_all();
+    __syncthreads();
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int st = tk.step0; st < tk.step1; ++st) {
+        const hm_step S = steps[st];
+        for (int w = threadIdx.x >> 5; w < S.e1 - S.e0; w += nw) {
+            const int e = S.e0 + w;
+            const hm_xfer X = ents[e];
+            const A *p = L + (int64_t)X.pad * QC * r;
+            A *o0 = L + (int64_t)(2 * (e - e0)) * QC * r;
+            A *o1 = o0 + QC * r;
+            if (lane < r) {
+                A a0[QC], a1[QC];
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) { a0[qq] = 0; a1[qq] = 0; }
+                for (int m = 0; m < r; ++m) {
+                    const A t0 = Ts[lane * r + m], t1 = Ts[r * r + lane * r + m];
+#pragma unroll
+                    for (int qq = 0; qq < QC; ++qq) {
+                        const A v = p[qq * r + m];
+                        a0[qq] += t0 * v;
+                        a1[qq] += t1 * v;
+                    }
+                }
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) {
+                    const A v0 = o0[qq * r + lane] + a0[qq], v1 = o1[qq * r + lane] + a1[qq];
+                    o0[qq * r + lane] = v0;
+                    o1[qq * r + lane] = v1;
+                    if (qq < k) {
+                        s[((int64_t)X.c0 * k + qq) * r + lane] = v0;
+                        s[((int64_t)X.c1 * k + qq) * r + lane] = v1;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Far field: s[slot][m] = sum_e sum_n F_e[m + r n] t[yslot_e][n]
 // (the F stage of src/algebra.jl:258-265, grouped by row cluster).  One warp
 // per (row slot, chunk of up to QC right-hand sides).  The r x r blocks of the
@@ -693,25 +820,33 @@ __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf)
 
 
 template <typename S, typename A, bool FAR, int KB>
-__global__ void __launch_bounds__(kStreamThreads, 2)
+__global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? 1 : 3)   // 4+ right-hand sides need the registers
     stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_seg, const hm_piece *pieces, const S *P,
                 const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs, S *yfar, int *status)
 {
     static_assert(sizeof(S) == sizeof(A), "right-hand sides are copied into shared memory as they are");
+    using V = typename std::conditional<sizeof(S) == 4, float4, double2>::type;
+    constexpr int VEC = 16 / (int)sizeof(S);                  // rows per thread (one 16-byte load)
+    constexpr int RQ = 64 / VEC;                               // row vectors of a 64-row segment
+    constexpr int NG = kStreamThreads / RQ;                    // column groups
     constexpr int CC = kChunkBytes / (64 * (int)sizeof(S));   // columns per chunk
-    constexpr int CPT = CC / 4;                                // columns per thread per chunk
+    constexpr int CPG = CC / NG;                               // columns per group per chunk
+    constexpr int FOLDC = 4;                                   // chunks between compensated folds
+    constexpr bool kFold = sizeof(A) == 4;                     // FP64 sums plainly
+    static_assert(CPG * NG == CC && NG * RQ == kStreamThreads, "chunk geometry");
     extern __shared__ unsigned char stream_smem[];
     const int seg_lo = cta_seg[blockIdx.x], seg_hi = cta_seg[blockIdx.x + 1];
     if (seg_lo >= seg_hi) return;
-    const int tid = threadIdx.x, row = tid & 63, grp = tid >> 6;
+    const int tid = threadIdx.x, rv = tid % RQ, grp = tid / RQ;
+    const int lane = tid & 31, warp = tid >> 5;
     const int k = ma.k;
     unsigned char *ring = stream_smem;
     uint64_t *full = reinterpret_cast<uint64_t *>(stream_smem + (size_t)nst * kChunkBytes);
     A *gbuf = reinterpret_cast<A *>(full + nst);
-    A *red = gbuf + ngb * gcap * KB;
+    A *red = gbuf + ngb * gcap * KB;                           // [warp][row][q][hi, lo]
     // the CTA's segment and piece records, staged once (records of one CTA
     // are consecutive in both arrays)
-    hm_seg *sseg = reinterpret_cast<hm_seg *>(red + 3 * 64 * KB * 2);
+    hm_seg *sseg = reinterpret_cast<hm_seg *>(red + 8 * 64 * KB * 2);
     hm_piece *spc = reinterpret_cast<hm_piece *>(sseg + dsegs);
     {
         const int ns = seg_hi - seg_lo;
@@ -812,43 +947,54 @@ __global__ void __launch_bounds__(kStreamThreads, 2)
         int cb, ce;
         part_range(G, cb, ce);
         const A *g = gbuf + ((j - seg_lo) % ngb) * gcap * KB;
-        A hi[KB], lo[KB];
-#pragma unroll
-        for (int q = 0; q < KB; ++q) hi[q] = lo[q] = A(0);
-        const bool live = row < G.nrows;
-        // y values this segment adds to, loaded now and used at its end
+        const int row0 = VEC * rv;
+        const bool live = row0 < G.nrows;
         const bool acc_y = FAR ? (yfar == nullptr && ce > cb) : (ma.accumulate != 0);
+        A part[VEC][KB], hi[VEC][KB], lo[VEC][KB];
+#pragma unroll
+        for (int v = 0; v < VEC; ++v)
+#pragma unroll
+            for (int q = 0; q < KB; ++q) part[v][q] = hi[v][q] = lo[v][q] = A(0);
+        // the final merge: thread t combines the partials of row t / 4 (the
+        // four threads of a row sit in one warp); t % 4 == 0 writes the row
+        const int mrow = tid >> 2, mpart = tid & 3;
+        const bool writer = mpart == 0 && mrow < G.nrows;
+        // y values the segment adds to, loaded now and used at its end
         S yold[KB];
 #pragma unroll
-        for (int q = 0; q < KB; ++q) yold[q] = S(0);
-        if (acc_y && grp == 0 && live) {
-#pragma unroll
-            for (int q = 0; q < KB; ++q)
-                if (q < k) yold[q] = ma.y[(G.row0 + row) * ma.incy + (int64_t)q * ma.ldy];
+        for (int q = 0; q < KB; ++q) {
+            yold[q] = S(0);
+            if (acc_y && writer && q < k) yold[q] = ma.y[(G.row0 + mrow) * ma.incy + (int64_t)q * ma.ldy];
         }
+        int nchunk = 0;
         for (int c0 = cb; c0 < ce; c0 += CC) {
             const int cols = min(CC, ce - c0);
             const bool ok = mbar_wait(&full[stage], phase, kWaitLimitNs);
             if (ok && live) {
                 const S *st = reinterpret_cast<const S *>(ring + (size_t)stage * kChunkBytes);
-                constexpr bool kFold = sizeof(A) == 4;     // FP64 sums straight into hi
-                A part[KB];
 #pragma unroll
-                for (int q = 0; q < KB; ++q) part[q] = kFold ? A(0) : hi[q];
-#pragma unroll
-                for (int u = 0; u < CPT; ++u) {
-                    const int c = grp * CPT + u;
+                for (int u = 0; u < CPG; ++u) {
+                    const int c = grp * CPG + u;
                     if (c < cols) {
-                        const A pv = (A)st[c * G.ld + row];
+                        const V pv = *reinterpret_cast<const V *>(st + c * G.ld + row0);
                         const A *gc = g + (c0 - cb + c) * KB;
+                        A pr[VEC];
+                        if constexpr (VEC == 4) { pr[0] = pv.x; pr[1] = pv.y; pr[2] = pv.z; pr[3] = pv.w; }
+                        else { pr[0] = pv.x; pr[1] = pv.y; }
 #pragma unroll
-                        for (int q = 0; q < KB; ++q) part[q] = fma(pv, gc[q], part[q]);
+                        for (int q = 0; q < KB; ++q) {
+                            const A gq = gc[q];
+#pragma unroll
+                            for (int v = 0; v < VEC; ++v) part[v][q] = fma(pr[v], gq, part[v][q]);
+                        }
                     }
                 }
+                if (kFold && ++nchunk == FOLDC) {
+                    nchunk = 0;
 #pragma unroll
-                for (int q = 0; q < KB; ++q) {
-                    if (kFold) fold(hi[q], lo[q], part[q]);
-                    else hi[q] = part[q];
+                    for (int v = 0; v < VEC; ++v)
+#pragma unroll
+                        for (int q = 0; q < KB; ++q) { fold(hi[v][q], lo[v][q], part[v][q]); part[v][q] = A(0); }
                 }
             }
             if (__syncthreads_or(!ok)) {      // every thread leaves together
@@ -863,29 +1009,62 @@ __global__ void __launch_bounds__(kStreamThreads, 2)
             if (++stage == nst) { stage = 0; phase ^= 1; }
         }
         if (abort) break;
-        // combine the four column groups (fixed order)
-        if (grp > 0 && live) {
-            A *rd = red + ((grp - 1) * 64 + row) * KB * 2;
 #pragma unroll
-            for (int q = 0; q < KB; ++q) { rd[2 * q] = hi[q]; rd[2 * q + 1] = lo[q]; }
+        for (int v = 0; v < VEC; ++v)
+#pragma unroll
+            for (int q = 0; q < KB; ++q) fold(hi[v][q], lo[v][q], part[v][q]);
+        // the column groups of a warp first (float: lanes l and l + 16 hold the same rows)
+        if constexpr (RQ == 16) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v)
+#pragma unroll
+                for (int q = 0; q < KB; ++q) {
+                    const A oh = __shfl_xor_sync(0xffffffffu, hi[v][q], 16);
+                    const A ol = __shfl_xor_sync(0xffffffffu, lo[v][q], 16);
+                    fold(hi[v][q], lo[v][q], oh);
+                    lo[v][q] += ol;
+                }
+        }
+        // every warp's partial to shared memory: red[warp][row][q][hi, lo]
+        const bool holder = RQ == 16 ? lane < 16 : true;
+        if (holder && live) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                A *rd = red + (warp * 64 + row0 + v) * KB * 2;
+#pragma unroll
+                for (int q = 0; q < KB; ++q) { rd[2 * q] = hi[v][q]; rd[2 * q + 1] = lo[v][q]; }
+            }
         }
         __syncthreads();
-        if (grp == 0 && live && !(FAR && !yfar && ce == cb)) {
+        // fixed-order tree: warps (2p, 2p + 1) per thread, then lanes ^1, ^2
+        if (mrow < 64) {
 #pragma unroll
             for (int q = 0; q < KB; ++q) {
-                if (q >= k) break;
-                A h0 = hi[q], l0 = lo[q];
-#pragma unroll
-                for (int gg = 0; gg < 3; ++gg) {
-                    const A *rd = red + (gg * 64 + row) * KB * 2;
-                    fold(h0, l0, rd[2 * q]);
-                    l0 += rd[2 * q + 1];
+                A h0 = A(0), l0 = A(0);
+                if (mrow < G.nrows) {
+                    const A *ra = red + ((2 * mpart) * 64 + mrow) * KB * 2;
+                    const A *rb = red + ((2 * mpart + 1) * 64 + mrow) * KB * 2;
+                    h0 = ra[2 * q];
+                    l0 = ra[2 * q + 1];
+                    fold(h0, l0, rb[2 * q]);
+                    l0 += rb[2 * q + 1];
                 }
-                const A v = h0 + l0;
-                if (FAR && yfar)
-                    yfar[(G.row0 + row) + (int64_t)q * ma.ldy] = (S)v;
-                else
-                    ma.y[(G.row0 + row) * ma.incy + (int64_t)q * ma.ldy] = acc_y ? (S)((A)yold[q] + v) : (S)v;
+#pragma unroll
+                for (int o = 1; o <= 2; o <<= 1) {
+                    const A oh = __shfl_xor_sync(0xffffffffu, h0, o);
+                    const A ol = __shfl_xor_sync(0xffffffffu, l0, o);
+                    fold(h0, l0, oh);
+                    l0 += ol;
+                }
+                if (writer && q < k && !(FAR && !yfar && ce == cb)) {
+                    const A val = h0 + l0;
+                    if (FAR && yfar)
+                        yfar[(G.row0 + mrow) + (int64_t)q * ma.ldy] = (S)val;
+                    else {
+                        S *yp = ma.y + (G.row0 + mrow) * ma.incy + (int64_t)q * ma.ldy;
+                        *yp = acc_y ? (S)((A)yold[q] + val) : (S)val;
+                    }
+                }
             }
         }
     }
@@ -1053,6 +1232,14 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     template __global__ void xfer_down_band<A, 1>(const hm_task *, const hm_step *, const hm_xfer *,        \
                                                   const A *, A *, int, int);                            \
     template __global__ void xfer_down_band<A, 8>(const hm_task *, const hm_step *, const hm_xfer *,        \
+                                                  const A *, A *, int, int);                            \
+    template __global__ void xfer_up_task<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
+                                                A *, int, int);                                         \
+    template __global__ void xfer_up_task<A, 8>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
+                                                A *, int, int);                                         \
+    template __global__ void xfer_down_task<A, 1>(const hm_task *, const hm_step *, const hm_xfer *,        \
+                                                  const A *, A *, int, int);                            \
+    template __global__ void xfer_down_task<A, 8>(const hm_task *, const hm_step *, const hm_xfer *,        \
                                                   const A *, A *, int, int);
 HM_INST_MV(double, double)
 HM_INST_MV(float, float)

@@ -146,6 +146,12 @@ template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
 
 template <typename A, int QC>
+__global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
+                             int r, int k);
+template <typename A, int QC>
+__global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
+                               int r, int k);
+template <typename A, int QC>
 __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
                              int r, int k);
 
@@ -178,7 +184,7 @@ __host__ __device__ constexpr size_t stream_smem_bytes(int nst, int gcap, int ng
                                                        int dpieces)
 {
     return (size_t)nst * kChunkBytes + (size_t)nst * 8 + (size_t)ngb * gcap * kb * asize +
-           (size_t)3 * 64 * kb * 2 * asize + (size_t)dsegs * sizeof(hm_seg) + (size_t)dpieces * sizeof(hm_piece);
+           (size_t)8 * 64 * kb * 2 * asize + (size_t)dsegs * sizeof(hm_seg) + (size_t)dpieces * sizeof(hm_piece);
 }
 template <typename S, typename A, bool FAR, int KB>
 __global__ void stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_seg, const hm_piece *pieces,

@@ -218,6 +218,38 @@ void band_transfers(const Tree &T, bool upward, std::vector<hm_xfer> &ents, std:
         }
         band_ptr.push_back((int)tasks.size());
     }
+    // Task-local numbering, so a task keeps its coefficients in shared memory:
+    // upward, record i of a task produces local i and its children are either
+    // produced earlier in the task or external (numbered after the records);
+    // pad = local(c0) | local(c1) << 16.  Downward, record i's children are
+    // locals 2i and 2i + 1 and its parent is an earlier child or external
+    // (numbered after the children); pad = local(parent).
+    for (const hm_task &tk : tasks) {
+        const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1;
+        const int nrec = e1 - e0;
+        std::vector<std::pair<int32_t, int32_t>> made;     // (slot, local), small per task
+        auto find = [&](int32_t slot) {
+            for (auto &m : made) if (m.first == slot) return m.second;
+            return -1;
+        };
+        int next = 0;
+        for (int e = e0; e < e1; ++e) {
+            hm_xfer &X = ents[e];
+            if (upward) {
+                int l0 = find(X.c0), l1 = find(X.c1);
+                if (l0 < 0) l0 = nrec + next++;
+                if (l1 < 0) l1 = nrec + next++;
+                X.pad = l0 | (l1 << 16);
+                made.push_back({X.slot, e - e0});
+            } else {
+                int lp = find(X.slot);
+                if (lp < 0) lp = 2 * nrec + next++;
+                X.pad = lp;
+                made.push_back({X.c0, 2 * (e - e0)});
+                made.push_back({X.c1, 2 * (e - e0) + 1});
+            }
+        }
+    }
 }
 
 }  // namespace
@@ -428,7 +460,7 @@ void merge_bands(const std::vector<Plan> &parts, bool upward, Plan &out)
                 for (int st = pt[t].step0; st < pt[t].step1; ++st) {
                     hm_step ns{(int32_t)ents.size(), (int32_t)ents.size()};
                     for (int e = ps[st].e0; e < ps[st].e1; ++e)
-                        ents.push_back({pe[e].slot + so, pe[e].c0 + so, pe[e].c1 + so, 0});
+                        ents.push_back({pe[e].slot + so, pe[e].c0 + so, pe[e].c1 + so, pe[e].pad});
                     ns.e1 = (int32_t)ents.size();
                     steps.push_back(ns);
                 }

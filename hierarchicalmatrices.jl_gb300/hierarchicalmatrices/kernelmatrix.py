@@ -283,6 +283,10 @@ class KernelMatrix:
         near-field panels (default), or every stage in order."""
         check(lib.hm_configure(self._h, _lib.HM_OPT_OVERLAP, 1 if enable else 0))
 
+    def set_near_stages(self, n):
+        """Shared-memory stages (8 KB each) of the near-field streaming kernel."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_NEAR_STAGES, int(n)))
+
     def profile(self, stages=_lib.STAGES):
         """Record CUDA events around the launches of the named matvec stages
         (see stage_times); an empty list turns timing off."""

@@ -199,7 +199,13 @@ int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t n
 /* Handle options.  HM_OPT_OVERLAP (default 1): run the tree passes of hm_mul
    on a side stream concurrently with the near-field panels; 0 runs every
    stage in order on the caller's stream. */
-enum { HM_OPT_OVERLAP = 1 };
+enum {
+    HM_OPT_OVERLAP = 1,
+    /* HM_OPT_NEAR_STAGES (default 4, 2..16): shared-memory stages (8 KB each)
+       of the near-field streaming kernel.  Values whose shared memory does
+       not fit the kernel's CTAs per SM fall back to the largest that does. */
+    HM_OPT_NEAR_STAGES = 2
+};
 int hm_configure(hm_handle *h, int option, int64_t value);
 
 /* Allocation-free single right-hand-side product (no counterpart in the

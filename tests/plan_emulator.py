@@ -49,8 +49,9 @@ def basis(pts, a, b, cheb, lam):
     return w / w.sum(axis=1, keepdims=True)
 
 
-def _banded(plan, which):
-    """Transfer records in launch order: band by band, task by task, step by step."""
+def _tasks(plan, which):
+    """Transfer tasks in launch order (band by band, task by task): for each,
+    its records and the step (level) index of each record within the task."""
     ents = plan.table(f"{which}_ents")
     steps = plan.table(f"{which}_steps")
     tasks = plan.table(f"{which}_tasks")
@@ -58,8 +59,11 @@ def _banded(plan, which):
     assert len(ents) == len(plan.table(which))
     for bd in range(len(bptr) - 1):
         for tk in tasks[bptr[bd]:bptr[bd + 1]]:
-            for st in steps[tk["step0"]:tk["step1"]]:
-                yield from ents[st["e0"]:st["e1"]]
+            recs, lev = [], []
+            for j, st in enumerate(steps[tk["step0"]:tk["step1"]]):
+                recs.extend(ents[st["e0"]:st["e1"]])
+                lev.extend([j] * (st["e1"] - st["e0"]))
+            yield recs, lev
 
 
 def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
@@ -85,14 +89,25 @@ def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
         rows = slice(vp["row0"], vp["row0"] + vp["nrows"])
         V = basis(y[rows], vf["a"], vf["b"], cheb, lam)
         t[vp["slot"]] = V.T @ B[rows]
-    # upward transfers in band / task / step order (as the GPU runs them);
-    # `done` checks that every child is final before its parent reads it
+    # upward transfers task by task with task-local vectors, as the GPU runs
+    # them: record i produces local i; its children (locals pad & 0xffff,
+    # pad >> 16) were produced at an earlier level of the task or are
+    # external (numbered after the records) and final before the launch
     done = np.zeros(S["n_yslots"], dtype=bool)
     done[[vp["slot"] for vp in plan.table("vpanels")]] = True
-    for e in _banded(plan, "up"):
-        assert done[e["c0"]] and done[e["c1"]] and not done[e["slot"]]
-        t[e["slot"]] = T[0].T @ t[e["c0"]] + T[1].T @ t[e["c1"]]
-        done[e["slot"]] = True
+    for recs, lev in _tasks(plan, "up"):
+        nrec, L, made = len(recs), {}, {}
+        for e in recs:
+            for lc, c in ((int(e["pad"]) & 0xffff, e["c0"]), (int(e["pad"]) >> 16, e["c1"])):
+                if lc >= nrec:
+                    assert lc not in L and done[c]
+                    L[lc], made[lc] = t[c].copy(), -1
+        for i, (e, lv) in enumerate(zip(recs, lev)):
+            l0, l1 = int(e["pad"]) & 0xffff, int(e["pad"]) >> 16
+            assert made[l0] < lv and made[l1] < lv and not done[e["slot"]]
+            L[i], made[i] = T[0].T @ L[l0] + T[1].T @ L[l1], lv
+            t[e["slot"]] = L[i]
+            done[e["slot"]] = True
     # far field
     ents, ff = plan.table("m2l_ents"), plan.table("f_fill")
     for row in plan.table("m2l_rows"):
@@ -104,17 +119,30 @@ def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
             F = kernel_np(kernel, yn, xn) if swap else kernel_np(kernel, xn, yn)
             acc += F @ t[ents[e]["yslot"]]
         s[row["slot"]] = acc
-    # downward transfers in band / task / step order; a parent is final once
-    # its own parent has pushed into it
+    # downward transfers task by task with task-local vectors: record i's
+    # children are locals 2i, 2i + 1 (starting from their far-field values);
+    # its parent (local pad) is a child of an earlier level of the task or
+    # external, and then final (pushed by its own parent) before the launch
     pushed = np.zeros(S["n_xslots"], dtype=bool)
     has_parent = np.zeros(S["n_xslots"], dtype=bool)
     for e in plan.table("down"):
         has_parent[e["c0"]] = has_parent[e["c1"]] = True
-    for e in _banded(plan, "down"):
-        assert pushed[e["slot"]] or not has_parent[e["slot"]]
-        s[e["c0"]] += T[0] @ s[e["slot"]]
-        s[e["c1"]] += T[1] @ s[e["slot"]]
-        pushed[e["c0"]] = pushed[e["c1"]] = True
+    for recs, lev in _tasks(plan, "down"):
+        nrec, L, made = len(recs), {}, {}
+        for i, e in enumerate(recs):
+            L[2 * i], L[2 * i + 1] = s[e["c0"]].copy(), s[e["c1"]].copy()
+            lp = int(e["pad"])
+            if lp >= 2 * nrec:
+                assert lp not in L and (pushed[e["slot"]] or not has_parent[e["slot"]])
+                L[lp], made[lp] = s[e["slot"]].copy(), -1
+        for i, (e, lv) in enumerate(zip(recs, lev)):
+            lp = int(e["pad"])
+            assert made[lp] < lv
+            L[2 * i] = L[2 * i] + T[0] @ L[lp]
+            L[2 * i + 1] = L[2 * i + 1] + T[1] @ L[lp]
+            made[2 * i] = made[2 * i + 1] = lv
+            s[e["c0"]], s[e["c1"]] = L[2 * i], L[2 * i + 1]
+            pushed[e["c0"]] = pushed[e["c1"]] = True
     # row segments
     out = np.zeros((S["nx"], k))
     covered = np.zeros(S["nx"], dtype=np.int64)
