@@ -162,6 +162,8 @@ struct hm_handle {
     int part_segs[2] = {0, 0};      // most segments of one CTA (near / far)
     int part_pieces[2] = {0, 0};    // most piece records of one CTA
     int *d_status = nullptr;        // device-side status word (HM_DEV_*), 0 when clean
+    bool tc_ok = false;             // segments fit the tensor-core panel kernel
+    bool tensor_cores = true;       // use it for FP32 products with many right-hand sides
 
     std::mutex mu;
     // Per caller stream: coefficient scratch (grown stream-ordered), the side
@@ -244,6 +246,9 @@ int prepare_streaming(hm_handle *h, const std::vector<hm_seg> &segs, const std::
     HM_CK(cudaMemsetAsync(h->d_status, 0, sizeof(int), st));
     h->stream_ctas = 0;
     if (segs.empty()) return HM_OK;
+    h->tc_ok = true;
+    for (const hm_seg &g : segs)
+        if (g.ld % 4 || g.poff % 32 || g.nrows > 64 || g.ld > 64) h->tc_ok = false;
     for (const hm_seg &g : segs) {
         int nfar = 0;
         bool seen_x = false;
@@ -534,14 +539,14 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
             HM_CK_LAUNCH("leaf_up");
         }
         const size_t usm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[0] * QC * r) * sizeof(A);
-        if (nq == 1 && usm <= kTaskSmemMax) {
+        if (usm <= kTaskSmemMax) {
             const size_t xsm = usm;
             HM_TRY(ensure_smem(xfer_up_task<A, QC>, xsm));
             for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
                 const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
                 if (!n) continue;
-                xfer_up_task<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t,
-                                                              r, k);
+                xfer_up_task<A, QC><<<dim3(n, (unsigned)nq), kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps,
+                                                                                 h->d_up_ents, T, t, r, k);
                 HM_CK_LAUNCH("xfer_up_task");
             }
         } else {
@@ -568,14 +573,14 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
             HM_CK_LAUNCH("m2l");
         }
         const size_t dsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[1] * QC * r) * sizeof(A);
-        if (nq == 1 && dsm <= kTaskSmemMax) {
+        if (dsm <= kTaskSmemMax) {
             const size_t xsm = dsm;
             HM_TRY(ensure_smem(xfer_down_task<A, QC>, xsm));
             for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
                 const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
                 if (!n) continue;
-                xfer_down_task<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_down_tasks + b, h->d_down_steps,
-                                                                h->d_down_ents, T, s, r, k);
+                xfer_down_task<A, QC><<<dim3(n, (unsigned)nq), kWarpCta, xsm, st>>>(
+                    h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T, s, r, k);
                 HM_CK_LAUNCH("xfer_down_task");
             }
         } else {
@@ -654,9 +659,23 @@ int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, cons
     return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, yfar, st);
 }
 
+constexpr int kTensorCoreMinK = 16;   // right-hand sides from which the tensor-core panels run
+
 template <typename S, typename A>
 int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
 {
+    if constexpr (sizeof(S) == 4 && sizeof(A) == 4) {
+        if (h->tensor_cores && h->tc_ok && ma.k >= kTensorCoreMinK) {
+            const size_t smem = expand_tc_smem_bytes();
+            HM_TRY(ensure_smem(expand_tc, smem));
+            // right-hand-side chunks of a segment run next to each other (its panel is re-read from L2)
+            const dim3 grid((unsigned)((ma.k + 127) / 128), (unsigned)h->n_segs);
+            expand_tc<<<grid, 256, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const float *>(panels), s, t,
+                                               h->r, h->d_status);
+            HM_CK_LAUNCH("expand_tc");
+            return HM_OK;
+        }
+    }
     const int maxw = std::max(h->max_width, 1);
     const int qc = sizeof(A) == 8 ? 16 : 32;
     const size_t smem = ((size_t)64 * maxw * sizeof(S) + 31) / 32 * 32 + (size_t)maxw * qc * sizeof(A);
@@ -1429,6 +1448,7 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     if (!h) return HM_ERR_INVALID_ARG;
     switch (option) {
     case HM_OPT_OVERLAP: h->overlap = value != 0; return HM_OK;
+    case HM_OPT_TENSOR_CORES: h->tensor_cores = value != 0; return HM_OK;
     case HM_OPT_NEAR_STAGES:
         if (value < 2 || value > 16) { set_error("HM_OPT_NEAR_STAGES must be in [2, 16]"); return HM_ERR_INVALID_ARG; }
         h->near_stages = (int)value;

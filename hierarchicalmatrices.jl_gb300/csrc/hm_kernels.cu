@@ -1,5 +1,6 @@
 // CUDA kernels: batched compression (fill) and the hierarchical matvec.
 #include "hm_kernels.cuh"
+#include "hm_async.cuh"
 
 #include <type_traits>
 
@@ -144,94 +145,6 @@ template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, co
 // near-field dense panels on the caller's stream; after the join
 // expand_part<.., true> adds the far field U s.
 
-// Asynchronous copies, mbarriers and compensated folds shared by the kernels below.
-namespace {
-constexpr unsigned long long kWaitLimitNs = 2000000000ull;
-constexpr unsigned long long kDrainLimitNs = 200000000ull;
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint64_t global_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Waits for the completion of the phase of `bar` with the given parity;
-// false once limit_ns has passed.
-__device__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned long long limit_ns)
-{
-    if (mbar_test(bar, parity)) return true;
-    const uint64_t t0 = global_ns();
-    while (!mbar_test(bar, parity))
-        if (global_ns() - t0 > limit_ns) return false;
-    return true;
-}
-// bytes (a multiple of 16) from 16-byte aligned global src to 16-byte
-// aligned shared dst, completing on bar.
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-template <int B>
-__device__ __forceinline__ void async_copy(void *dst, const void *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(B) : "memory");
-}
-// 16 bytes, global -> shared, bypassing L1 (both addresses 16-byte aligned)
-__device__ __forceinline__ void async_copy16(void *dst, const void *src)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void async_wait_all()
-{
-    asm volatile("cp.async.wait_all;" ::: "memory");
-}
-__device__ __forceinline__ void async_commit()
-{
-    asm volatile("cp.async.commit_group;" ::: "memory");
-}
-// waits until at most `pending` (0..2) of this thread's latest cp.async groups are in flight
-__device__ __forceinline__ void async_wait_pending(int pending)
-{
-    if (pending <= 0) asm volatile("cp.async.wait_group 0;" ::: "memory");
-    else if (pending == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
-    else asm volatile("cp.async.wait_group 2;" ::: "memory");
-}
-// hi + lo += p: compensated (TwoSum) for FP32; FP64 adds plainly (its
-// products are exact enough, and FP64 adds are scarce on this part).
-__device__ __forceinline__ void fold(float &hi, float &lo, float p)
-{
-    const float sm = hi + p;
-    const float bp = sm - hi;
-    lo += (hi - (sm - bp)) + (p - bp);
-    hi = sm;
-}
-__device__ __forceinline__ void fold(double &hi, double &, double p) { hi += p; }
-}  // namespace
 
 // t[slot][col0 + m] = (V^T x)[m] for each explicit basis panel.  One warp
 // per (panel, chunk of QC right-hand sides); lane m owns column m of the
@@ -268,17 +181,18 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
         } else {
             for (int i = lane; i < nel; i += 32) async_copy<sizeof(S)>(Vs + i, Vp + i);
         }
-        for (int i = lane; i < P.nrows * QC; i += 32) {
-            const int j = i / QC, qq = i % QC;
-            xs[i] = qq < qc ? (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx] : (A)0;
-        }
+        // x chunk, right-hand side major xs[qq * 64 + j] (lanes walk the rows of one right-hand side)
+#pragma unroll
+        for (int qq = 0; qq < QC; ++qq)
+            for (int j = lane; j < P.nrows; j += 32)
+                xs[qq * 64 + j] = qq < qc ? (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx] : (A)0;
         async_wait_all();
         __syncwarp();
         if (lane < pw) {
             for (int j = 0; j < P.nrows; ++j) {
                 const A v = (A)Vs[j * pw + lane];
 #pragma unroll
-                for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xs[j * QC + qq]);
+                for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xs[qq * 64 + j]);
             }
         }
     } else if (lane < pw) {
@@ -346,7 +260,8 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
     }
 }
 
-// Band tasks with shared-memory-resident coefficients (k <= QC): the task's
+// Band tasks with shared-memory-resident coefficients, one CTA per (task,
+// chunk of QC right-hand sides: blockIdx.y): the task's
 // external inputs (and T) are fetched once with cp.async, every level then
 // reads and writes shared memory only, with a CTA barrier between levels;
 // each coefficient the task produces is also written to global memory.
@@ -363,16 +278,24 @@ __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const h
     A *L = Ts + 2 * HM_RMAX * HM_RMAX;
     const hm_task tk = tasks[blockIdx.x];
     const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
+    const int q0 = blockIdx.y * QC, qc = min(QC, k - q0);      // this CTA's right-hand sides
     for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
-    const int per = 2 * QC * r;
-    for (int i = threadIdx.x; i < nrec * per; i += blockDim.x) {
-        const int rec = i / per, rem = i % per, c = rem / (QC * r), qq = (rem % (QC * r)) / r, m = rem % r;
+    // external children: warps take records, lanes coefficients
+    for (int rec = threadIdx.x >> 5; rec < nrec; rec += blockDim.x >> 5) {
         const hm_xfer X = ents[e0 + rec];
-        const int lc = c ? (X.pad >> 16) : (X.pad & 0xffff);
-        if (lc < nrec) continue;                          // produced by an earlier level of this task
-        A *d = L + ((int64_t)lc * QC + qq) * r + m;
-        if (qq < k) async_copy<sizeof(A)>(d, t + ((int64_t)(c ? X.c1 : X.c0) * k + qq) * r + m);
-        else *d = A(0);
+        const int ln = threadIdx.x & 31;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int lc = c ? (X.pad >> 16) : (X.pad & 0xffff);
+            if (lc < nrec || ln >= r) continue;           // produced by an earlier level of this task
+            const A *src = t + ((int64_t)(c ? X.c1 : X.c0) * k + q0) * r + ln;
+            A *d = L + (int64_t)lc * QC * r + ln;
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq) {
+                if (qq < qc) async_copy<sizeof(A)>(d + qq * r, src + (int64_t)qq * r);
+                else d[qq * r] = A(0);
+            }
+        }
     }
     async_wait_all();
     __syncthreads();
@@ -397,7 +320,7 @@ __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const h
 #pragma unroll
                 for (int qq = 0; qq < QC; ++qq) {
                     out[qq * r + lane] = acc[qq];
-                    if (qq < k) t[((int64_t)X.slot * k + qq) * r + lane] = acc[qq];
+                    if (qq < qc) t[((int64_t)X.slot * k + q0 + qq) * r + lane] = acc[qq];
                 }
             }
         }
@@ -414,24 +337,33 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
     A *L = Ts + 2 * HM_RMAX * HM_RMAX;
     const hm_task tk = tasks[blockIdx.x];
     const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
+    const int q0 = blockIdx.y * QC, qc = min(QC, k - q0);      // this CTA's right-hand sides
     for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
     // children start from their far-field (m2l) coefficients; external parents as computed
-    const int per = 3 * QC * r;
-    for (int i = threadIdx.x; i < nrec * per; i += blockDim.x) {
-        const int rec = i / per, rem = i % per, c = rem / (QC * r), qq = (rem % (QC * r)) / r, m = rem % r;
+    // warps take records, lanes coefficients
+    for (int rec = threadIdx.x >> 5; rec < nrec; rec += blockDim.x >> 5) {
         const hm_xfer X = ents[e0 + rec];
-        int lc, slot;
-        if (c < 2) {
-            lc = 2 * rec + c;
-            slot = c ? X.c1 : X.c0;
-        } else {
-            lc = X.pad;
-            slot = X.slot;
-            if (lc < 2 * nrec) continue;                  // a child of an earlier level of this task
+        const int ln = threadIdx.x & 31;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            int lc, slot;
+            if (c < 2) {
+                lc = 2 * rec + c;
+                slot = c ? X.c1 : X.c0;
+            } else {
+                lc = X.pad;
+                slot = X.slot;
+                if (lc < 2 * nrec) continue;              // a child of an earlier level of this task
+            }
+            if (ln >= r) continue;
+            const A *src = s + ((int64_t)slot * k + q0) * r + ln;
+            A *d = L + (int64_t)lc * QC * r + ln;
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq) {
+                if (qq < qc) async_copy<sizeof(A)>(d + qq * r, src + (int64_t)qq * r);
+                else d[qq * r] = A(0);
+            }
         }
-        A *d = L + ((int64_t)lc * QC + qq) * r + m;
-        if (qq < k) async_copy<sizeof(A)>(d, s + ((int64_t)slot * k + qq) * r + m);
-        else *d = A(0);
     }
     async_wait_all();
     __syncthreads();
@@ -462,9 +394,9 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
                     const A v0 = o0[qq * r + lane] + a0[qq], v1 = o1[qq * r + lane] + a1[qq];
                     o0[qq * r + lane] = v0;
                     o1[qq * r + lane] = v1;
-                    if (qq < k) {
-                        s[((int64_t)X.c0 * k + qq) * r + lane] = v0;
-                        s[((int64_t)X.c1 * k + qq) * r + lane] = v1;
+                    if (qq < qc) {
+                        s[((int64_t)X.c0 * k + q0 + qq) * r + lane] = v0;
+                        s[((int64_t)X.c1 * k + q0 + qq) * r + lane] = v1;
                     }
                 }
             }
@@ -501,10 +433,13 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
         char *dst = reinterpret_cast<char *>(Fb + buf * fstride);
         for (int i = lane; i < (int)(fstride * sizeof(S) / 16); i += 32) async_copy16(dst + 16 * i, src + 16 * i);
         A *tb = Tb + buf * QC * HM_RMAX;
-        for (int i = lane; i < QC * r; i += 32) {
-            const int qq = i / r, m = i % r;
-            if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + m, t + ((int64_t)E.yslot * k + q0 + qq) * r + m);
-            else tb[qq * HM_RMAX + m] = A(0);
+        if (lane < r) {
+            const A *src = t + ((int64_t)E.yslot * k + q0) * r + lane;
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq) {
+                if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + lane, src + (int64_t)qq * r);
+                else tb[qq * HM_RMAX + lane] = A(0);
+            }
         }
         async_commit();
     };
@@ -1128,33 +1063,40 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const hm_seg G = segs[blockIdx.x];
     S *Ps = reinterpret_cast<S *>(smem_raw);                              // ld x width
-    A *Gs = reinterpret_cast<A *>(smem_raw + (((size_t)64 * maxw * sizeof(S) + 31) / 32) * 32);  // width x QC
+    A *Gs = reinterpret_cast<A *>(smem_raw + (((size_t)64 * maxw * sizeof(S) + 31) / 32) * 32);  // QC x width
     {
-        const int64_t n16 = (int64_t)G.ld * G.width * sizeof(S) / 16;
-        const float4 *src = reinterpret_cast<const float4 *>(P + G.poff);
-        float4 *dst = reinterpret_cast<float4 *>(Ps);
-        for (int64_t i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = __ldcs(src + i);
+        // the whole panel in flight at once
+        const int n16 = (int)((int64_t)G.ld * G.width * sizeof(S) / 16);
+        const char *src = reinterpret_cast<const char *>(P + G.poff);
+        char *dst = reinterpret_cast<char *>(Ps);
+        for (int i = threadIdx.x; i < n16; i += blockDim.x) async_copy16(dst + 16 * i, src + 16 * i);
     }
+    const int W = G.width;
     const int rg = threadIdx.x % RG, qg = threadIdx.x / RG;
     for (int q0 = 0; q0 < ma.k; q0 += QC) {
         const int qc = min(QC, ma.k - q0);
-        __syncthreads();
+        __syncthreads();                      // the previous chunk's Gs is consumed
+        // gathered [s ; x pieces] chunk, right-hand side major: Gs[qq * W + c];
+        // consecutive threads take consecutive entries of one right-hand side
         int col = 0;
         for (int pc = 0; pc < G.npieces; ++pc) {
             const hm_piece Q = pieces[G.piece0 + pc];
             for (int idx = threadIdx.x; idx < Q.width * QC; idx += blockDim.x) {
-                const int c = idx / QC, qq = idx % QC;
-                A v = 0;
+                const int qq = idx / Q.width, c = idx - qq * Q.width;
+                A *d = Gs + qq * W + col + c;
                 if (qq < qc) {
                     if (Q.kind == HM_PIECE_X)
-                        v = (A)ma.x[(Q.src + c) * ma.incx + (int64_t)(q0 + qq) * ma.ldx];
+                        async_copy<sizeof(A)>(d, ma.x + (Q.src + c) * ma.incx + (int64_t)(q0 + qq) * ma.ldx);
                     else
-                        v = (Q.kind == HM_PIECE_TCOEF ? t : s)[((int64_t)Q.src * ma.k + q0 + qq) * r + c];
+                        async_copy<sizeof(A)>(d, (Q.kind == HM_PIECE_TCOEF ? t : s) +
+                                                     ((int64_t)Q.src * ma.k + q0 + qq) * r + c);
+                } else {
+                    *d = A(0);
                 }
-                Gs[(col + c) * QC + qq] = v;
             }
             col += Q.width;
         }
+        async_wait_all();
         __syncthreads();
         A hi[RB][QB], lo[RB][QB];
 #pragma unroll
@@ -1173,7 +1115,8 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                 for (; c < cend; ++c) {
                     A pv[RB], gv[QB];
                     load_vec<S, A, RB>(Ps + (int64_t)c * G.ld + rg * RB, pv);
-                    load_vec<A, A, QB>(Gs + c * QC + qg * QB, gv);
+#pragma unroll
+                    for (int j = 0; j < QB; ++j) gv[j] = Gs[(qg * QB + j) * W + c];
 #pragma unroll
                     for (int i = 0; i < RB; ++i)
 #pragma unroll

@@ -1,0 +1,315 @@
+// Tensor-core (tcgen05) row-segment panels for many right-hand sides, FP32
+// storage.  Written for sm_103a.
+//
+// For one row segment (nrows <= 64 rows, panel P of nrows x width, column-
+// major with leading dimension ld) and a chunk of up to 128 right-hand sides,
+// a CTA of 256 threads computes
+//     Y[row][q] (+)= sum_c P[row][c] G[q][c],
+// where G holds the gathered [s ; x pieces] entries of the chunk.  The MMA is
+// D = A B with A = G (M = 128 right-hand sides x K) and B = P^T (K x N = 64
+// rows), both stored K-major in shared memory, D (128 x 64, FP32) in tensor
+// memory.  FP32 accuracy comes from splitting every FP32 value exactly into
+// three BF16 pieces, v = v_h + v_m + v_l (round-to-nearest at each step;
+// 3 x 8 significant bits cover FP32's 24), and summing the six products
+//     G_h P_h + G_h P_m + G_m P_h + G_m P_m + G_h P_l + G_l P_h
+// with FP32 accumulation (the dropped terms are below 2^-24 relative).  The
+// G_h P_h products accumulate in one tensor-memory block and the five
+// correction products in a second, added at the end: the tensor core rounds
+// each accumulation relative to the running sum, so the corrections (2^-8 of
+// it) must not ride on the large sum.  K runs
+// in chunks of 32 columns: the raw panel columns (cp.async, 16 bytes) and
+// right-hand-side entries (cp.async, 4 bytes) of chunk c + 1 load while chunk
+// c is split into the operand layouts and multiplied.
+//
+// Operand layout (SWIZZLE_NONE, K-major, 16-bit): 8-row x 16-byte core
+// matrices; element (row, k) of a 32-column chunk sits at byte
+//     (row / 8) * 512 + (k / 8) * 128 + (row % 8) * 16 + (k % 8) * 2,
+// so core matrices adjacent in K are 128 bytes apart (leading byte offset)
+// and 8-row groups 512 bytes apart (stride byte offset).
+#include "hm_kernels.cuh"
+#include "hm_async.cuh"
+
+#include <cuda_bf16.h>
+
+namespace hm {
+
+namespace {
+
+constexpr int TC_M = 128;          // right-hand sides per CTA (MMA M)
+constexpr int TC_N = 64;           // rows per segment (MMA N)
+constexpr int TC_KC = 32;          // columns per K chunk
+constexpr int TC_GSTRIDE = 40;     // raw right-hand-side row stride (floats): conflict-free 8-byte split reads
+constexpr int TC_PSTRIDE = 68;     // raw panel column stride (floats): 16-byte multiple, conflict-free split reads
+constexpr int TC_THREADS = 256;
+
+struct TcSmem {
+    float rawG[2][TC_M * TC_GSTRIDE];      // [q][c], double-buffered
+    float rawP[2][TC_KC * TC_PSTRIDE];     // [c][row], double-buffered
+    uint32_t G3[3][TC_M * TC_KC / 2];      // BF16 pieces h, m, l of G, K-major core-matrix layout
+    uint32_t P3[3][TC_N * TC_KC / 2];      // BF16 pieces of P^T
+    const float *colbase[2][TC_KC];        // source of column c for the chunk's first right-hand side
+    int64_t colstride[2][TC_KC];           // element step between right-hand sides (0: no column)
+    uint64_t mma_bar;
+    uint32_t tmem_base;
+};
+
+// 32-bit word of the BF16 pair (row, k), (row, k + 1), k even
+__device__ __forceinline__ int kmajor_pair_word(int row, int k)
+{
+    return (row >> 3) * 128 + (k >> 3) * 32 + (row & 7) * 4 + ((k & 7) >> 1);
+}
+
+// (a, b) = h + m + l exactly, each a BF16 pair (round to nearest at every
+// step); the pairs are packed as stored: a in the low half.
+__device__ __forceinline__ void split3x2(float a, float b, uint32_t &h, uint32_t &m, uint32_t &l)
+{
+    const __nv_bfloat162 h2 = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h2);
+    const float ra = a - hf.x, rb = b - hf.y;
+    const __nv_bfloat162 m2 = __floats2bfloat162_rn(ra, rb);
+    const float2 mf = __bfloat1622float2(m2);
+    const __nv_bfloat162 l2 = __floats2bfloat162_rn(ra - mf.x, rb - mf.y);
+    h = *reinterpret_cast<const uint32_t *>(&h2);
+    m = *reinterpret_cast<const uint32_t *>(&m2);
+    l = *reinterpret_cast<const uint32_t *>(&l2);
+}
+
+// Shared-memory matrix descriptor, SWIZZLE_NONE, descriptor version 1.
+__device__ __forceinline__ uint64_t umma_desc(const void *p, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((smem_addr(p) & 0x3FFFF) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor (kind::f16): D FP32, A and B BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int m, int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace
+
+size_t expand_tc_smem_bytes() { return sizeof(TcSmem); }
+
+__global__ void __launch_bounds__(TC_THREADS, 2)
+    expand_tc(MulArgs<float> ma, const hm_seg *segs, const hm_piece *pieces, const float *P, const float *s,
+              const float *t, int r, int *status)
+{
+    extern __shared__ __align__(128) unsigned char tc_smem_raw[];
+    TcSmem &S = *reinterpret_cast<TcSmem *>(tc_smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const hm_seg G = segs[blockIdx.y];
+    const int q0 = blockIdx.x * TC_M;
+    const int qc = min(TC_M, ma.k - q0);
+    const int W = G.width;
+    const int nch = (W + TC_KC - 1) / TC_KC;
+
+    // tensor memory: two blocks of 64 FP32 columns x 128 lanes (h h products, corrections)
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem_base)),
+                     "r"(2 * TC_N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(&S.mma_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+
+    // raw loads of chunk ch into buffer b: panel columns (16-byte copies) and
+    // the chunk's right-hand-side entries (4-byte copies).  Column sources of
+    // the chunk are tabulated first (one thread per column).
+    auto load_raw = [&](int ch, int b) {
+        const int c0 = ch * TC_KC, cols = min(TC_KC, W - c0);
+        if (tid < TC_KC) {
+            const float *base = nullptr;
+            int64_t step = 0;
+            const int cc = c0 + tid;
+            if (tid < cols) {
+                int pc0 = 0;
+                for (int pi = 0; pi < G.npieces; ++pi) {
+                    const hm_piece Q = pieces[G.piece0 + pi];
+                    if (cc < pc0 + Q.width) {
+                        const int pcol = cc - pc0;
+                        if (Q.kind == HM_PIECE_X) {
+                            base = ma.x + (Q.src + pcol) * ma.incx + (int64_t)q0 * ma.ldx;
+                            step = ma.ldx;
+                        } else {
+                            base = (Q.kind == HM_PIECE_TCOEF ? t : s) + ((int64_t)Q.src * ma.k + q0) * r + pcol;
+                            step = r;
+                        }
+                        break;
+                    }
+                    pc0 += Q.width;
+                }
+            }
+            S.colbase[b][tid] = base;
+            S.colstride[b][tid] = step;
+        }
+        // panel: column c = i / 16, 16-byte piece j = i % 16 (pieces past ld skipped)
+        const float *src = P + G.poff + (int64_t)c0 * G.ld;
+        for (int i = tid; i < cols * 16; i += TC_THREADS) {
+            const int c = i >> 4, j = i & 15;
+            if (4 * j < G.ld) async_copy16(&S.rawP[b][c * TC_PSTRIDE + 4 * j], src + (int64_t)c * G.ld + 4 * j);
+        }
+        __syncthreads();                                        // column table visible
+        // right-hand sides: q = i / 32, column c = i % 32
+        for (int i = tid; i < qc * TC_KC; i += TC_THREADS) {
+            const int q = i >> 5, c = i & 31;
+            const int64_t step = S.colstride[b][c];
+            if (step) async_copy<4>(&S.rawG[b][q * TC_GSTRIDE + c], S.colbase[b][c] + q * step);
+        }
+        async_commit();
+    };
+
+    const uint32_t idesc = umma_idesc_bf16(TC_M, TC_N);
+    bool ok = true;
+    int committed = -1;                                         // last chunk whose MMAs were committed
+    if (nch > 0) load_raw(0, 0);
+    for (int ch = 0; ch < nch; ++ch) {
+        const int b = ch & 1;
+        if (ch + 1 < nch) {
+            load_raw(ch + 1, b ^ 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            async_wait_all();
+        }
+        // the previous chunk's MMAs read the operand buffers: wait for them
+        if (ch > 0 && !mbar_wait(&S.mma_bar, (ch - 1) & 1, kWaitLimitNs)) ok = false;
+        if (__syncthreads_or(!ok)) break;                       // raw chunk visible to all threads
+        tc_fence_after();
+        const int c0 = ch * TC_KC, cols = min(TC_KC, W - c0);
+        // split the right-hand sides: a warp covers 8 right-hand sides x 4 column pairs
+        for (int i = tid; i < TC_M * TC_KC / 2; i += TC_THREADS) {
+            const int blk = i >> 5, l = i & 31;
+            const int q = (blk >> 2) * 8 + (l >> 2), c = ((blk & 3) * 4 + (l & 3)) * 2;
+            float2 v = make_float2(0.f, 0.f);
+            if (q < qc) v = *reinterpret_cast<const float2 *>(&S.rawG[b][q * TC_GSTRIDE + c]);
+            if (c >= cols || q >= qc) v.x = 0.f;
+            if (c + 1 >= cols || q >= qc) v.y = 0.f;
+            const int w = kmajor_pair_word(q, c);
+            split3x2(v.x, v.y, S.G3[0][w], S.G3[1][w], S.G3[2][w]);
+        }
+        // split the panel: a warp covers 8 rows x 4 column pairs
+        for (int i = tid; i < TC_N * TC_KC / 2; i += TC_THREADS) {
+            const int blk = i >> 5, l = i & 31;
+            const int row = (blk >> 2) * 8 + (l & 7), c = ((blk & 3) * 4 + (l >> 3)) * 2;
+            float v0 = 0.f, v1 = 0.f;
+            if (row < G.ld) {
+                if (c < cols) v0 = S.rawP[b][c * TC_PSTRIDE + row];
+                if (c + 1 < cols) v1 = S.rawP[b][(c + 1) * TC_PSTRIDE + row];
+            }
+            const int w = kmajor_pair_word(row, c);
+            split3x2(v0, v1, S.P3[0][w], S.P3[1][w], S.P3[2][w]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // operands visible to the tensor core
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            // (G piece, P piece) of the six products, the largest first
+            constexpr int pa[6] = {0, 0, 1, 1, 0, 2}, pb[6] = {0, 1, 0, 1, 2, 0};
+#pragma unroll
+            for (int ks = 0; ks < TC_KC / 16; ++ks) {
+                const uint32_t off = ks * 256;                  // two core matrices of K per step
+#pragma unroll
+                for (int j = 0; j < 6; ++j) {
+                    const uint64_t ad = umma_desc(reinterpret_cast<const char *>(S.G3[pa[j]]) + off, 128, 512);
+                    const uint64_t bd = umma_desc(reinterpret_cast<const char *>(S.P3[pb[j]]) + off, 128, 512);
+                    const uint32_t dt = j == 0 ? tmem : tmem + TC_N;
+                    umma_bf16(dt, ad, bd, idesc, (ch > 0 || ks > 0 || j > 1) ? 1 : 0);
+                }
+            }
+            umma_commit(&S.mma_bar);
+        }
+        committed = ch;
+    }
+    // all MMAs done before reading D
+    if (ok && committed >= 0 && !mbar_wait(&S.mma_bar, committed & 1, kWaitLimitNs)) ok = false;
+    if (__syncthreads_or(!ok)) {
+        async_wait_all();
+        if (tid == 0) {
+            atomicExch(status, HM_DEV_WAIT_TIMEOUT);
+            if (committed >= 0) mbar_wait(&S.mma_bar, committed & 1, kDrainLimitNs);
+        }
+    } else if (nch == 0) {                                      // no columns: the rows are zero
+        for (int i = tid; i < qc * G.nrows; i += TC_THREADS) {
+            const int qq = i / G.nrows, row = i - qq * G.nrows;
+            float *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)(q0 + qq) * ma.ldy;
+            if (!ma.accumulate) *yp = 0.f;
+        }
+    } else {
+        tc_fence_after();
+        // D row q (lane) x column row: this warp's 32 right-hand sides, all 64 rows,
+        // staged through shared memory (rawG) for row-contiguous stores
+        float *Ys = &S.rawG[0][0];                              // [q][row], stride 65: spans both raw buffers
+        static_assert(sizeof(S.rawG) >= sizeof(float) * TC_M * 65, "epilogue stage");
+        // warp w reads tensor-memory lanes 32 (w % 4) .. + 31, columns 32 (w / 4) .. + 31
+        const int q = (warp & 3) * 32 + lane;
+        const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+#pragma unroll
+        for (int c0 = (warp >> 2) * 32; c0 < (warp >> 2) * 32 + 32; c0 += 16) {
+            float v[16], w[16];
+            tmem_ld16(tmem + lane_off + (uint32_t)c0, v);
+            tmem_ld16(tmem + lane_off + (uint32_t)(TC_N + c0), w);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) Ys[q * 65 + c0 + i] = v[i] + w[i];
+        }
+        __syncthreads();
+        for (int i = tid; i < qc * G.nrows; i += TC_THREADS) {
+            const int qq = i / G.nrows, row = i - qq * G.nrows;
+            float *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)(q0 + qq) * ma.ldy;
+            const float v = Ys[qq * 65 + row];
+            *yp = ma.accumulate ? *yp + v : v;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_N) : "memory");
+}
+
+}  // namespace hm

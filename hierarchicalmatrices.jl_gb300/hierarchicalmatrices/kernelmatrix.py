@@ -283,6 +283,11 @@ class KernelMatrix:
         near-field panels (default), or every stage in order."""
         check(lib.hm_configure(self._h, _lib.HM_OPT_OVERLAP, 1 if enable else 0))
 
+    def set_tensor_cores(self, enable=True):
+        """FP32 products with 16+ right-hand sides on the tensor cores (default)
+        or on the FP32 pipes."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_TENSOR_CORES, 1 if enable else 0))
+
     def set_near_stages(self, n):
         """Shared-memory stages (8 KB each) of the near-field streaming kernel."""
         check(lib.hm_configure(self._h, _lib.HM_OPT_NEAR_STAGES, int(n)))

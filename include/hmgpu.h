@@ -204,7 +204,12 @@ enum {
     /* HM_OPT_NEAR_STAGES (default 4, 2..16): shared-memory stages (8 KB each)
        of the near-field streaming kernel.  Values whose shared memory does
        not fit the kernel's CTAs per SM fall back to the largest that does. */
-    HM_OPT_NEAR_STAGES = 2
+    HM_OPT_NEAR_STAGES = 2,
+    /* HM_OPT_TENSOR_CORES (default 1): FP32 products with 16 or more
+       right-hand sides run their row-segment panels on the tensor cores
+       (three TF32 products per step, FP32 accumulation); 0 keeps them on the
+       FP32 pipes. */
+    HM_OPT_TENSOR_CORES = 3
 };
 int hm_configure(hm_handle *h, int option, int64_t value);
 
