@@ -173,6 +173,7 @@ struct hm_handle {
         size_t bytes = 0;
         cudaStream_t side = nullptr;
         cudaEvent_t fork = nullptr, join = nullptr;
+        cudaEvent_t mid = nullptr;  // a point inside the tree passes where the near field may start
     };
     std::map<void *, StreamCtx> streams;
     void *d_stage = nullptr;
@@ -187,8 +188,13 @@ struct hm_handle {
     double stage_ms[HM_NSTAGES] = {0};
     int64_t stage_launches[HM_NSTAGES] = {0};
     int launches_per_mul = 0;
-    bool overlap = true;            // tree passes on a side stream
+    // 0: every stage in order on the caller's stream; 1: tree passes on a side
+    // stream from the start of the product, the near field beside them; 2 (the
+    // default): the near field starts after the upward pass, whose streaming
+    // leaf stage it would otherwise slow; 3: after the far-field (M2L) stage
+    int overlap = 2;
     int near_stages = 4;            // ring stages of the near-field streaming kernel
+    int near_kernel = 0;            // 0 default (one warp per segment), 1 the same, 2 streamed CTAs
 
     template <typename T>
     int alloc(T **p, size_t count)
@@ -503,6 +509,7 @@ int stream_ctx(hm_handle *h, cudaStream_t st, size_t bytes, hm_handle::StreamCtx
         HM_CK(cudaStreamCreateWithPriority(&sc.side, cudaStreamNonBlocking, greatest));
         HM_CK(cudaEventCreateWithFlags(&sc.fork, cudaEventDisableTiming));
         HM_CK(cudaEventCreateWithFlags(&sc.join, cudaEventDisableTiming));
+        HM_CK(cudaEventCreateWithFlags(&sc.mid, cudaEventDisableTiming));
     }
     if (sc.bytes < bytes) {
         if (sc.p) HM_CK(cudaFreeAsync(sc.p, st));
@@ -524,7 +531,8 @@ constexpr size_t kTaskSmemMax = 200 * 1024;     // shared memory of a band task 
 // Tree passes on stream st: leaf bases, upward transfers level by level, far
 // field, downward transfers level by level.  QC right-hand sides per warp.
 template <typename S, typename A, int QC>
-int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
+int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing, cudaEvent_t mid,
+                   int mid_after)
 {
     const int r = h->r, k = ma.k;
     const int64_t nq = (k + QC - 1) / QC;
@@ -532,9 +540,9 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
-            const size_t smem = (size_t)kWarpsPerCta * 64 * (HM_RMAX + QC) * sizeof(S);
+            const size_t smem = (size_t)kWarpsPerCta * 64 * (HM_RMAX + 2 * QC) * sizeof(S);
             HM_TRY(ensure_smem(leaf_up<S, A, QC>, smem));
-            leaf_up<S, A, QC><<<warp_ctas(h->n_vp * nq), 32 * kWarpsPerCta, smem, st>>>(
+            leaf_up<S, A, QC><<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
         }
@@ -562,6 +570,7 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
             }
         }
     }
+    if (mid && mid_after == 0) HM_CK(cudaEventRecord(mid, st));     // upward pass done
     {
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
@@ -572,6 +581,7 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
             HM_CK_LAUNCH("m2l");
         }
+        if (mid && mid_after == 1) HM_CK(cudaEventRecord(mid, st));  // far-field stage done
         const size_t dsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[1] * QC * r) * sizeof(A);
         if (dsm <= kTaskSmemMax) {
             const size_t xsm = dsm;
@@ -599,26 +609,32 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
 }
 
 template <typename S, typename A>
-int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing)
+int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing,
+                cudaEvent_t mid = nullptr, int mid_after = 0)
 {
-    if (ma.k == 1) return launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing);
-    return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing);
+    if (ma.k == 1) return launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing, mid, mid_after);
+    return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing, mid, mid_after);
 }
 
 // shared memory per streaming CTA: three per SM up to two right-hand sides
-// (whose registers allow three), more for four or more (one per SM)
-constexpr size_t kStreamSmemMax3 = 74 * 1024, kStreamSmemMax1 = 200 * 1024;
+// (whose registers allow three), two for FP32 with four or more, one for FP64
+constexpr size_t kStreamSmemMax3 = 74 * 1024, kStreamSmemMax2 = 112 * 1024, kStreamSmemMax1 = 200 * 1024;
 
 template <typename S, typename A, bool FAR, int KB>
 int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, S *yfar,
                    cudaStream_t st)
 {
-    if (!FAR && h->stream_ctas > 0) {      // far-field runs are short: one warp per segment serves them better
+    // one warp per segment unless the streamed CTAs are asked for: measured on
+    // GB300, the warp kernel reads 64-row grid panels at 6.1 TB/s (90% of the
+    // copy peak) and keeps its lead on short segments and more right-hand
+    // sides; the streamed form reaches 5.7 TB/s alone and overlaps the tree
+    // passes no better
+    if (!FAR && h->stream_ctas > 0 && h->near_kernel == 2) {
         const int part = FAR ? 1 : 0;
         const int gcap = std::max(h->part_width[part], 1);
         // the configured stages, right-hand sides gathered three segments
         // ahead; fewer of either until two CTAs fit on an SM
-        const size_t smax = KB >= 4 ? kStreamSmemMax1 : kStreamSmemMax3;
+        const size_t smax = KB < 4 ? kStreamSmemMax3 : sizeof(S) == 4 ? kStreamSmemMax2 : kStreamSmemMax1;
         int nst = h->near_stages, ngb = 4;
         size_t smem = 0;
         for (;;) {
@@ -653,8 +669,13 @@ template <typename S, typename A, bool FAR>
 int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st,
                 S *yfar = nullptr)
 {
-    if (ma.k == 1) return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st);
-    if (ma.k == 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st);
+    // one right-hand side: FP32 runs the warp kernel's two-column form (FMA
+    // with a TwoSum fold every 64 columns issues less than per-element
+    // TwoProd/TwoSum); FP64 (plain FMA either way, on the scarce FP64 pipe) and
+    // the streamed kernel keep the one-column form
+    if (ma.k == 1 && (sizeof(A) == 8 || (!FAR && h->stream_ctas > 0 && h->near_kernel == 2)))
+        return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st);
+    if (ma.k <= 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st);
     if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, yfar, st);
     return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, yfar, st);
 }
@@ -692,7 +713,8 @@ int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, 
 // side == st runs everything in order on st.
 template <typename S, typename A>
 int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStream_t side, cudaEvent_t fork,
-                    cudaEvent_t join, void *scratch, bool timing, const void *panels = nullptr)
+                    cudaEvent_t join, void *scratch, bool timing, const void *panels = nullptr,
+                    cudaEvent_t mid = nullptr)
 {
     if (!panels) panels = h->d_P;
     const int k = ma.k;
@@ -706,7 +728,8 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
             HM_CK(cudaEventRecord(fork, st));
             HM_CK(cudaStreamWaitEvent(side, fork, 0));
         }
-        HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing)));
+        HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing, split ? mid : nullptr,
+                                  h->overlap == 3 ? 1 : 0)));
         if (split && (k > kPartMaxK || !h->n_segs)) HM_CK(cudaEventRecord(join, side));
     }
     if (!h->n_segs) {
@@ -724,6 +747,7 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
                 HM_TRY((launch_part<S, A, true>(h, mf, s, t, panels, side, yfar)));
             }
             HM_CK(cudaEventRecord(join, side));
+            if (mid) HM_CK(cudaStreamWaitEvent(st, mid, 0));
             {
                 StageTimer tm(h, timing ? 2 : -1, st);
                 HM_TRY((launch_part<S, A, false>(h, ma, s, t, panels, st)));
@@ -755,7 +779,8 @@ int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st, const void *panels = n
     if (ma.k <= 0) return HM_OK;
     hm_handle::StreamCtx *sc = nullptr;
     HM_TRY(stream_ctx(h, st, stream_scratch_bytes<A>(h, ma.k), &sc));
-    return launch_pipeline<S, A>(h, ma, st, h->overlap ? sc->side : st, sc->fork, sc->join, sc->p, true, panels);
+    return launch_pipeline<S, A>(h, ma, st, h->overlap ? sc->side : st, sc->fork, sc->join, sc->p, true, panels,
+                                 h->overlap >= 2 ? sc->mid : nullptr);
 }
 
 // Row-derivative panels (same layout as the panels), filled once.
@@ -1447,8 +1472,15 @@ int hm_configure(hm_handle *h, int option, int64_t value)
 {
     if (!h) return HM_ERR_INVALID_ARG;
     switch (option) {
-    case HM_OPT_OVERLAP: h->overlap = value != 0; return HM_OK;
+    case HM_OPT_OVERLAP:
+        if (value < 0 || value > 3) { set_error("HM_OPT_OVERLAP must be in [0, 3]"); return HM_ERR_INVALID_ARG; }
+        h->overlap = (int)value;
+        return HM_OK;
     case HM_OPT_TENSOR_CORES: h->tensor_cores = value != 0; return HM_OK;
+    case HM_OPT_NEAR_KERNEL:
+        if (value < 0 || value > 2) { set_error("HM_OPT_NEAR_KERNEL must be 0, 1 or 2"); return HM_ERR_INVALID_ARG; }
+        h->near_kernel = (int)value;
+        return HM_OK;
     case HM_OPT_NEAR_STAGES:
         if (value < 2 || value > 16) { set_error("HM_OPT_NEAR_STAGES must be in [2, 16]"); return HM_ERR_INVALID_ARG; }
         h->near_stages = (int)value;

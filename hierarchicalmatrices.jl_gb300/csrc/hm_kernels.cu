@@ -147,10 +147,10 @@ template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, co
 
 
 // t[slot][col0 + m] = (V^T x)[m] for each explicit basis panel.  One warp
-// per (panel, chunk of QC right-hand sides); lane m owns column m of the
-// row-major panel (width <= 32, row stride ld).  Panels of up to 64 rows are
-// staged in shared memory (16-byte loads by all lanes) together with the
-// chunk's x values; longer panels are read directly.  Plain FMA accumulation
+// per panel, looping over chunks of QC right-hand sides; lane m owns column m
+// of the row-major panel (width <= 32, row stride ld).  Panels of up to 64
+// rows are staged once in shared memory (cp.async) and the chunks' x values
+// double-buffered beside them; longer panels are read directly.  Plain FMA accumulation
 // (the coefficients feed only the far field).  Coefficients of a slot are r
 // apart per right-hand side.
 template <typename S, typename A, int QC>
@@ -159,21 +159,25 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int nq = (ma.k + QC - 1) / QC;
     const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
-    if (w >= (int64_t)npanels * nq) return;
-    const hm_vpanel P = vp[w / nq];
-    const int q0 = (int)(w % nq) * QC, qc = min(QC, ma.k - q0);
+    if (w >= (int64_t)npanels) return;
+    const hm_vpanel P = vp[w];
     const int pw = P.width;
     const S *Vp = V + P.off;
-    PlainAcc<A> acc[QC];
+    const int k = ma.k;
+    auto store = [&](int q0, int qc, PlainAcc<A> *acc) {
+        if (lane < pw) {
 #pragma unroll
-    for (int qq = 0; qq < QC; ++qq) acc[qq].zero();
+            for (int qq = 0; qq < QC; ++qq)
+                if (qq < qc) t[((int64_t)P.slot * k + q0 + qq) * r + P.col0 + lane] = acc[qq].value();
+        }
+    };
     if (P.nrows <= 64 && P.ld == pw) {
-        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * (64 * HM_RMAX + 64 * QC);
-        A *xs = reinterpret_cast<A *>(Vs + 64 * HM_RMAX);    // xs[j * QC + qq]
+        // the panel once; x chunks of QC right-hand sides double-buffered,
+        // right-hand side major xs[b][qq * 64 + j] (lanes walk rows)
+        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * (64 * HM_RMAX + 2 * 64 * QC);
+        A *xs = reinterpret_cast<A *>(Vs + 64 * HM_RMAX);
         const int nel = P.nrows * pw;
-        // all of the panel's loads in flight at once (cp.async), then one wait
         if (sizeof(S) * nel % 16 == 0 && (P.off * sizeof(S)) % 16 == 0) {
             const char *src = reinterpret_cast<const char *>(Vp);
             char *dst = reinterpret_cast<char *>(Vs);
@@ -181,33 +185,57 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
         } else {
             for (int i = lane; i < nel; i += 32) async_copy<sizeof(S)>(Vs + i, Vp + i);
         }
-        // x chunk, right-hand side major xs[qq * 64 + j] (lanes walk the rows of one right-hand side)
-#pragma unroll
-        for (int qq = 0; qq < QC; ++qq)
-            for (int j = lane; j < P.nrows; j += 32)
-                xs[qq * 64 + j] = qq < qc ? (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx] : (A)0;
-        async_wait_all();
-        __syncwarp();
-        if (lane < pw) {
-            for (int j = 0; j < P.nrows; ++j) {
-                const A v = (A)Vs[j * pw + lane];
-#pragma unroll
-                for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xs[qq * 64 + j]);
-            }
-        }
-    } else if (lane < pw) {
-        const S *col = Vp + lane;
-        for (int j = 0; j < P.nrows; ++j) {
-            const A v = (A)col[(int64_t)j * P.ld];
+        auto fetch = [&](int q0, int b) {
+            const int qc = min(QC, k - q0);
+            A *d = xs + b * 64 * QC;
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq)
-                if (qq < qc) acc[qq].add(v, (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx]);
-        }
-    }
-    if (lane < pw) {
+                for (int j = lane; j < P.nrows; j += 32) {
+                    if (qq < qc) async_copy<sizeof(A)>(d + qq * 64 + j, ma.x + (P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx);
+                    else d[qq * 64 + j] = A(0);
+                }
+            async_commit();
+        };
+        fetch(0, 0);
+        for (int q0 = 0, b = 0; q0 < k; q0 += QC, b ^= 1) {
+            if (q0 + QC < k) {
+                fetch(q0 + QC, b ^ 1);
+                asm volatile("cp.async.wait_group 1;" ::: "memory");
+            } else {
+                async_wait_all();
+            }
+            __syncwarp();
+            PlainAcc<A> acc[QC];
 #pragma unroll
-        for (int qq = 0; qq < QC; ++qq)
-            if (qq < qc) t[((int64_t)P.slot * ma.k + q0 + qq) * r + P.col0 + lane] = acc[qq].value();
+            for (int qq = 0; qq < QC; ++qq) acc[qq].zero();
+            const A *xb = xs + b * 64 * QC;
+            if (lane < pw) {
+                for (int j = 0; j < P.nrows; ++j) {
+                    const A v = (A)Vs[j * pw + lane];
+#pragma unroll
+                    for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xb[qq * 64 + j]);
+                }
+            }
+            store(q0, min(QC, k - q0), acc);
+            __syncwarp();                                 // buffer b is refilled next
+        }
+    } else {
+        for (int q0 = 0; q0 < k; q0 += QC) {
+            const int qc = min(QC, k - q0);
+            PlainAcc<A> acc[QC];
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq) acc[qq].zero();
+            if (lane < pw) {
+                const S *col = Vp + lane;
+                for (int j = 0; j < P.nrows; ++j) {
+                    const A v = (A)col[(int64_t)j * P.ld];
+#pragma unroll
+                    for (int qq = 0; qq < QC; ++qq)
+                        if (qq < qc) acc[qq].add(v, (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx]);
+                }
+            }
+            store(q0, qc, acc);
+        }
     }
 }
 
@@ -755,13 +783,17 @@ __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf)
 
 
 template <typename S, typename A, bool FAR, int KB>
-__global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? 1 : 3)   // 4+ right-hand sides need the registers
+__global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? (sizeof(S) == 4 ? 2 : 1) : 3)   // registers of 4+ right-hand sides
     stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_seg, const hm_piece *pieces, const S *P,
                 const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs, S *yfar, int *status)
 {
     static_assert(sizeof(S) == sizeof(A), "right-hand sides are copied into shared memory as they are");
-    using V = typename std::conditional<sizeof(S) == 4, float4, double2>::type;
-    constexpr int VEC = 16 / (int)sizeof(S);                  // rows per thread (one 16-byte load)
+    // rows per thread: one 16-byte load; FP32 with 4+ right-hand sides takes 2
+    // (8-byte loads) to keep its accumulators in registers
+    constexpr bool kNarrow = sizeof(S) == 4 && KB >= 4;
+    using V = typename std::conditional<sizeof(S) == 4, typename std::conditional<kNarrow, float2, float4>::type,
+                                        double2>::type;
+    constexpr int VEC = kNarrow ? 2 : 16 / (int)sizeof(S);
     constexpr int RQ = 64 / VEC;                               // row vectors of a 64-row segment
     constexpr int NG = kStreamThreads / RQ;                    // column groups
     constexpr int CC = kChunkBytes / (64 * (int)sizeof(S));   // columns per chunk
@@ -914,8 +946,11 @@ __global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? 1 : 3)   // 4+ right
                         const V pv = *reinterpret_cast<const V *>(st + c * G.ld + row0);
                         const A *gc = g + (c0 - cb + c) * KB;
                         A pr[VEC];
-                        if constexpr (VEC == 4) { pr[0] = pv.x; pr[1] = pv.y; pr[2] = pv.z; pr[3] = pv.w; }
-                        else { pr[0] = pv.x; pr[1] = pv.y; }
+                        if constexpr (VEC == 4) {
+                            pr[0] = pv.x; pr[1] = pv.y; pr[2] = pv.z; pr[3] = pv.w;
+                        } else {
+                            pr[0] = pv.x; pr[1] = pv.y;
+                        }
 #pragma unroll
                         for (int q = 0; q < KB; ++q) {
                             const A gq = gc[q];

@@ -28,6 +28,7 @@ HM_F64, HM_F32 = 0, 1
 HM_OPT_OVERLAP = 1
 HM_OPT_NEAR_STAGES = 2
 HM_OPT_TENSOR_CORES = 3
+HM_OPT_NEAR_KERNEL = 4
 HM_PIECE_COEF, HM_PIECE_X, HM_PIECE_TCOEF = 0, 1, 2
 
 # Records of csrc/hm_types.h.

@@ -279,14 +279,24 @@ class KernelMatrix:
         return out
 
     def set_overlap(self, enable=True):
-        """Run the tree passes on a side stream concurrently with the
-        near-field panels (default), or every stage in order."""
-        check(lib.hm_configure(self._h, _lib.HM_OPT_OVERLAP, 1 if enable else 0))
+        """Tree passes on a side stream beside the near-field panels: the near
+        field from the start (1), after the upward pass (2; True, the
+        default) or after the far-field stage (3); or every stage in order
+        (False or 0)."""
+        mode = int(enable) if not isinstance(enable, bool) else (2 if enable else 0)
+        check(lib.hm_configure(self._h, _lib.HM_OPT_OVERLAP, mode))
 
     def set_tensor_cores(self, enable=True):
         """FP32 products with 16+ right-hand sides on the tensor cores (default)
         or on the FP32 pipes."""
         check(lib.hm_configure(self._h, _lib.HM_OPT_TENSOR_CORES, 1 if enable else 0))
+
+    def set_near_kernel(self, which):
+        """Near-field panels with up to 8 right-hand sides: "warp" (one warp
+        per row segment; "auto", the default, chooses it) or "stream" (CTAs
+        streaming runs of segments through shared memory)."""
+        code = {"auto": 0, "warp": 1, "stream": 2}[which]
+        check(lib.hm_configure(self._h, _lib.HM_OPT_NEAR_KERNEL, code))
 
     def set_near_stages(self, n):
         """Shared-memory stages (8 KB each) of the near-field streaming kernel."""

@@ -196,9 +196,10 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate);
 int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t nrows, double *out,
                    void *stream);
 
-/* Handle options.  HM_OPT_OVERLAP (default 1): run the tree passes of hm_mul
-   on a side stream concurrently with the near-field panels; 0 runs every
-   stage in order on the caller's stream. */
+/* Handle options.  HM_OPT_OVERLAP (default 2): 1 runs the tree passes of
+   hm_mul on a side stream concurrently with the near-field panels from the
+   start, 2 starts the near field after the upward pass, 3 after the
+   far-field (M2L) stage; 0 runs every stage in order on the caller's stream. */
 enum {
     HM_OPT_OVERLAP = 1,
     /* HM_OPT_NEAR_STAGES (default 4, 2..16): shared-memory stages (8 KB each)
@@ -209,7 +210,11 @@ enum {
        right-hand sides run their row-segment panels on the tensor cores
        (three TF32 products per step, FP32 accumulation); 0 keeps them on the
        FP32 pipes. */
-    HM_OPT_TENSOR_CORES = 3
+    HM_OPT_TENSOR_CORES = 3,
+    /* HM_OPT_NEAR_KERNEL (default 0): near-field panels with up to 8
+       right-hand sides on 0 or 1 = one warp per row segment, 2 = CTAs
+       streaming runs of segments through shared memory (cp.async.bulk). */
+    HM_OPT_NEAR_KERNEL = 4
 };
 int hm_configure(hm_handle *h, int option, int64_t value);
 
