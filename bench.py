@@ -473,7 +473,7 @@ def main():
             "hbm_GBs_stored": stored_bytes / (ms * 1e-3) / 1e9,
             "hbm_GBs_effective_canonical": canonical_bytes / (ms * 1e-3) / 1e9,
             "roofline": {
-                "bound": "hbm", "kernel": "expand_part<float,float,false> (near-field row-segment panels)",
+                "bound": "hbm", "kernel": "expand_part<float,float,false,2> (near-field panels, one warp per row segment)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": profiled_traffic(n), "traffic_unit": "GB per launch",
                 "peak_source": peak_kind, "kernel_ms": exp_ms, "kernel_bytes": exp_bytes,
