@@ -335,6 +335,7 @@ def main():
 
     import torch
     import hierarchicalmatrices as hm
+    from hierarchicalmatrices import parallel
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -373,11 +374,7 @@ def main():
     exp_total, exp_launches = H32.stage_times(reset=True)["expand"]
     # per-stage breakdown: every stage timed in order on one stream (no overlap)
     stages = serial_stages(H32, lambda: H32.mul(u32, b32, accumulate=False), args.steps, torch)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = parallel.max_over_ranks(ms)             # the slowest rank's step time (N > 1)
     value = world * 1e3 / ms
     err32 = rel_err_sampled(H32, u32, b64, rows, torch)
 

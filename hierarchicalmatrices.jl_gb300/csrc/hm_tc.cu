@@ -157,6 +157,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = S.tmem_base;
+    // 8-row groups of A that hold live right-hand sides; the others stay zero
+    const int live_groups = (qc + 7) >> 3;
+    for (int p = 0; p < 3; ++p)
+        for (int w = live_groups * 128 + tid; w < TC_M * TC_KC / 2; w += TC_THREADS) S.G3[p][w] = 0u;
 
     // raw loads of chunk ch into buffer b: panel columns (16-byte copies) and
     // the chunk's right-hand-side entries (4-byte copies).  Column sources of
@@ -221,8 +225,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         if (__syncthreads_or(!ok)) break;                       // raw chunk visible to all threads
         tc_fence_after();
         const int c0 = ch * TC_KC, cols = min(TC_KC, W - c0);
-        // split the right-hand sides: a warp covers 8 right-hand sides x 4 column pairs
-        for (int i = tid; i < TC_M * TC_KC / 2; i += TC_THREADS) {
+        // split the right-hand sides: a warp covers 8 right-hand sides x 4 column
+        // pairs; only the 8-row groups holding live right-hand sides (the rest
+        // were zeroed once)
+        for (int i = tid; i < live_groups * 4 * 32; i += TC_THREADS) {
             const int blk = i >> 5, l = i & 31;
             const int q = (blk >> 2) * 8 + (l >> 2), c = ((blk & 3) * 4 + (l & 3)) * 2;
             float2 v = make_float2(0.f, 0.f);

@@ -66,12 +66,13 @@ def _tasks(plan, which):
             yield recs, lev
 
 
-def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
+def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None, segments=None):
     """Returns H @ b (b: (ny,) or (ny, k)) computed from the plan tables.
     drow=True: the row-derivative product D b (entries differentiated with
     respect to their row point); swap=True: entries f(col, row) (the
     transposed matrix); x / y replace the plan's points in the entries (the
-    tree stays the plan's)."""
+    tree stays the plan's); segments=(lo, hi) computes only the rows of those
+    row segments (the others are 0), as one rank of a row-sharded product."""
     S = plan.sizes
     r = S["r"]
     x = plan.x if x is None else np.asarray(x, dtype=np.float64)
@@ -147,9 +148,12 @@ def emulate(plan, kernel, b, drow=False, swap=False, x=None, y=None):
     out = np.zeros((S["nx"], k))
     covered = np.zeros(S["nx"], dtype=np.int64)
     pieces, sf = plan.table("pieces"), plan.table("seg_fill")
-    for sg, fi in zip(plan.table("segs"), sf):
+    seg_lo, seg_hi = segments if segments is not None else (0, len(sf))
+    for j, (sg, fi) in enumerate(zip(plan.table("segs"), sf)):
         rows = slice(sg["row0"], sg["row0"] + sg["nrows"])
         covered[rows] += 1
+        if not seg_lo <= j < seg_hi:
+            continue
         cols, g = [], []
         for p in pieces[sg["piece0"]:sg["piece0"] + sg["npieces"]]:
             if p["kind"] == 0:
