@@ -191,7 +191,8 @@ struct hm_handle {
     // 0: every stage in order on the caller's stream; 1: tree passes on a side
     // stream from the start of the product, the near field beside them; 2 (the
     // default): the near field starts after the upward pass, whose streaming
-    // leaf stage it would otherwise slow; 3: after the far-field (M2L) stage
+    // leaf stage it would otherwise slow; 3: after the far-field (M2L) stage;
+    // 4: after the leaf stage only
     int overlap = 2;
     int near_stages = 4;            // ring stages of the near-field streaming kernel
     int near_kernel = 0;            // 0 default (one warp per segment), 1 the same, 2 streamed CTAs
@@ -546,6 +547,7 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
         }
+        if (mid && mid_after == 2) HM_CK(cudaEventRecord(mid, st));  // leaf bases done
         const size_t usm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[0] * QC * r) * sizeof(A);
         if (usm <= kTaskSmemMax) {
             const size_t xsm = usm;
@@ -573,7 +575,21 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     if (mid && mid_after == 0) HM_CK(cudaEventRecord(mid, st));     // upward pass done
     {
         StageTimer tm(h, timing ? 1 : -1, st);
-        if (h->n_m2l_rows) {
+        bool done = false;
+        if constexpr (QC > 1) {
+            if (h->n_m2l_rows && nq > 1) {
+                // many right-hand sides: one CTA per row box, its blocks staged once
+                const size_t smem = 8 * (size_t)h->fstride * sizeof(S) +
+                                    (size_t)kWarpsPerCta * 2 * QC * HM_RMAX * sizeof(A);
+                HM_TRY(ensure_smem(m2l_k<S, A, QC>, smem));
+                m2l_k<S, A, QC><<<h->n_m2l_rows, 32 * kWarpsPerCta, smem, st>>>(
+                    h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s,
+                    r, k);
+                HM_CK_LAUNCH("m2l_k");
+                done = true;
+            }
+        }
+        if (!done && h->n_m2l_rows) {
             const size_t smem =
                 (size_t)kWarpsPerCta * (2 * (size_t)h->fstride * sizeof(S) + 2 * (size_t)QC * HM_RMAX * sizeof(A));
             HM_TRY(ensure_smem(m2l<S, A, QC>, smem));
@@ -729,7 +745,7 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
             HM_CK(cudaStreamWaitEvent(side, fork, 0));
         }
         HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing, split ? mid : nullptr,
-                                  h->overlap == 3 ? 1 : 0)));
+                                  h->overlap == 3 ? 1 : h->overlap == 4 ? 2 : 0)));
         if (split && (k > kPartMaxK || !h->n_segs)) HM_CK(cudaEventRecord(join, side));
     }
     if (!h->n_segs) {
@@ -1473,7 +1489,7 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     if (!h) return HM_ERR_INVALID_ARG;
     switch (option) {
     case HM_OPT_OVERLAP:
-        if (value < 0 || value > 3) { set_error("HM_OPT_OVERLAP must be in [0, 3]"); return HM_ERR_INVALID_ARG; }
+        if (value < 0 || value > 4) { set_error("HM_OPT_OVERLAP must be in [0, 4]"); return HM_ERR_INVALID_ARG; }
         h->overlap = (int)value;
         return HM_OK;
     case HM_OPT_TENSOR_CORES: h->tensor_cores = value != 0; return HM_OK;

@@ -502,6 +502,85 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
     }
 }
 
+// Far field for many right-hand sides (k > QC): one CTA (4 warps) per row
+// slot.  The row's r x r blocks are staged once in shared memory (up to
+// kM2lBlocks at a time, cp.async); the warps then take chunks of QC
+// right-hand sides in turn, double-buffering each block's column
+// coefficients, lane m accumulating row m of the chunk.
+constexpr int kM2lBlocks = 8;
+template <typename S, typename A, int QC>
+__global__ void m2l_k(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
+                      const A *t, A *s, int r, int k)
+{
+    extern __shared__ unsigned char smem_raw[];
+    S *Fb = reinterpret_cast<S *>(smem_raw);                                      // kM2lBlocks x fstride
+    A *Tb = reinterpret_cast<A *>(Fb + kM2lBlocks * fstride) + (threadIdx.x >> 5) * 2 * QC * HM_RMAX;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (blockIdx.x >= nrows) return;
+    const hm_m2l_row R = rows[blockIdx.x];
+    for (int e0 = R.begin; e0 < R.end || e0 == R.begin; e0 += kM2lBlocks) {
+        const int nb = min(kM2lBlocks, R.end - e0);
+        __syncthreads();                                                           // previous batch used
+        for (int b = 0; b < nb; ++b) {
+            const char *src = reinterpret_cast<const char *>(F + ents[e0 + b].foff);
+            char *dst = reinterpret_cast<char *>(Fb + b * fstride);
+            for (int i = threadIdx.x; i < (int)(fstride * sizeof(S) / 16); i += blockDim.x)
+                async_copy16(dst + 16 * i, src + 16 * i);
+        }
+        async_commit();
+        async_wait_all();
+        __syncthreads();
+        for (int q0 = warp * QC; q0 < k; q0 += nw * QC) {
+            const int qc = min(QC, k - q0);
+            auto fetch = [&](int b, int buf) {
+                A *tb = Tb + buf * QC * HM_RMAX;
+                if (lane < r) {
+                    const A *src = t + ((int64_t)ents[e0 + b].yslot * k + q0) * r + lane;
+#pragma unroll
+                    for (int qq = 0; qq < QC; ++qq) {
+                        if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + lane, src + (int64_t)qq * r);
+                        else tb[qq * HM_RMAX + lane] = A(0);
+                    }
+                }
+                async_commit();
+            };
+            A acc[QC];
+#pragma unroll
+            for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
+            if (nb > 0) fetch(0, 0);
+            for (int b = 0; b < nb; ++b) {
+                if (b + 1 < nb) {
+                    fetch(b + 1, (b + 1) & 1);
+                    asm volatile("cp.async.wait_group 1;" ::: "memory");
+                } else {
+                    async_wait_all();
+                }
+                __syncwarp();
+                const S *fb = Fb + b * fstride;
+                const A *tb = Tb + (b & 1) * QC * HM_RMAX;
+                if (lane < r) {
+                    for (int n = 0; n < r; ++n) {
+                        const A f = (A)fb[lane + r * n];
+#pragma unroll
+                        for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tb[qq * HM_RMAX + n];
+                    }
+                }
+                __syncwarp();
+            }
+            if (lane < r) {
+                A *sp = s + ((int64_t)R.slot * k + q0) * r + lane;
+#pragma unroll
+                for (int qq = 0; qq < QC; ++qq) {
+                    if (qq >= qc) break;
+                    if (e0 == R.begin) sp[(int64_t)qq * r] = acc[qq];
+                    else sp[(int64_t)qq * r] += acc[qq];
+                }
+            }
+        }
+        if (R.end <= R.begin) break;                                               // empty row: zeros written once
+    }
+}
+
 // Downward transfers of one band: s[child_c][m'] += sum_m T_c[m', m] s[parent][m].
 // Same task/step structure as xfer_up_band, topmost level first.
 template <typename A, int QC>
@@ -1199,6 +1278,8 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                           const A *, A *, int, int);                                    \
     template __global__ void m2l<S, A, 8>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,    \
                                           const A *, A *, int, int);                                    \
+    template __global__ void m2l_k<S, A, 8>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,  \
+                                            const A *, A *, int, int);                                  \
     HM_INST_PART(S, A, 1) HM_INST_PART(S, A, 2) HM_INST_PART(S, A, 4) HM_INST_PART(S, A, 8)               \
     HM_INST_STREAM(S, A, 1) HM_INST_STREAM(S, A, 2) HM_INST_STREAM(S, A, 4) HM_INST_STREAM(S, A, 8)       \
     template __global__ void expand_k<S, A>(MulArgs<S>, const hm_seg *, const hm_piece *, const S *,  \

@@ -159,6 +159,9 @@ template <typename S, typename A, int QC>
 __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
                     const A *t, A *s, int r, int k);
 
+template <typename S, typename A, int QC>
+__global__ void m2l_k(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const S *F, int fstride,
+                      const A *t, A *s, int r, int k);
 template <typename A, int QC>
 __global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
                                int r, int k);

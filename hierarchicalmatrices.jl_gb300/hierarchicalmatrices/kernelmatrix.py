@@ -281,8 +281,8 @@ class KernelMatrix:
     def set_overlap(self, enable=True):
         """Tree passes on a side stream beside the near-field panels: the near
         field from the start (1), after the upward pass (2; True, the
-        default) or after the far-field stage (3); or every stage in order
-        (False or 0)."""
+        default), after the far-field stage (3) or after the leaf-basis
+        stage (4); or every stage in order (False or 0)."""
         mode = int(enable) if not isinstance(enable, bool) else (2 if enable else 0)
         check(lib.hm_configure(self._h, _lib.HM_OPT_OVERLAP, mode))
 

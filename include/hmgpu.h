@@ -199,7 +199,8 @@ int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t n
 /* Handle options.  HM_OPT_OVERLAP (default 2): 1 runs the tree passes of
    hm_mul on a side stream concurrently with the near-field panels from the
    start, 2 starts the near field after the upward pass, 3 after the
-   far-field (M2L) stage; 0 runs every stage in order on the caller's stream. */
+   far-field (M2L) stage, 4 after the leaf-basis stage of the upward pass; 0
+   runs every stage in order on the caller's stream. */
 enum {
     HM_OPT_OVERLAP = 1,
     /* HM_OPT_NEAR_STAGES (default 4, 2..16): shared-memory stages (8 KB each)
