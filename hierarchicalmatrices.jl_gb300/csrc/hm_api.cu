@@ -703,12 +703,13 @@ int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, 
 {
     if constexpr (sizeof(S) == 4 && sizeof(A) == 4) {
         if (h->tensor_cores && h->tc_ok && ma.k >= kTensorCoreMinK) {
-            const size_t smem = expand_tc_smem_bytes();
+            const int maxw = std::max(h->max_width, 1);
+            const size_t smem = expand_tc_smem_bytes(maxw);
             HM_TRY(ensure_smem(expand_tc, smem));
             // right-hand-side chunks of a segment run next to each other (its panel is re-read from L2)
             const dim3 grid((unsigned)((ma.k + 127) / 128), (unsigned)h->n_segs);
             expand_tc<<<grid, 256, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const float *>(panels), s, t,
-                                               h->r, h->d_status);
+                                               h->r, maxw, h->d_status);
             HM_CK_LAUNCH("expand_tc");
             return HM_OK;
         }

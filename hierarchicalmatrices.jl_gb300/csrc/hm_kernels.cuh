@@ -195,11 +195,11 @@ __global__ void stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_se
                             S *yfar, int *status);
 
 // Tensor-core panels for many right-hand sides (FP32 storage): grid
-// (ceil(k / 128), segments), 256 threads, expand_tc_smem_bytes() of shared
+// (ceil(k / 128), segments), 256 threads, expand_tc_smem_bytes(maxw) of shared
 // memory; needs segments of <= 64 rows, ld % 4 == 0, poff % 32 == 0.
-size_t expand_tc_smem_bytes();
+size_t expand_tc_smem_bytes(int maxw);
 __global__ void expand_tc(MulArgs<float> ma, const hm_seg *segs, const hm_piece *pieces, const float *P,
-                          const float *s, const float *t, int r, int *status);
+                          const float *s, const float *t, int r, int maxw, int *status);
 
 template <typename S, typename A>
 __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s,

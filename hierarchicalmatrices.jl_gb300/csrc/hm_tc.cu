@@ -47,11 +47,12 @@ struct TcSmem {
     float rawP[2][TC_KC * TC_PSTRIDE];     // [c][row], double-buffered
     uint32_t G3[3][TC_M * TC_KC / 2];      // BF16 pieces h, m, l of G, K-major core-matrix layout
     uint32_t P3[3][TC_N * TC_KC / 2];      // BF16 pieces of P^T
-    const float *colbase[2][TC_KC];        // source of column c for the chunk's first right-hand side
-    int64_t colstride[2][TC_KC];           // element step between right-hand sides (0: no column)
     uint64_t mma_bar;
     uint32_t tmem_base;
 };
+// followed in shared memory by the segment's column table: for each panel
+// column, the source of its first right-hand side and the element step
+// between right-hand sides (maxw entries of each)
 
 // 32-bit word of the BF16 pair (row, k), (row, k + 1), k even
 __device__ __forceinline__ int kmajor_pair_word(int row, int k)
@@ -127,14 +128,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 
 }  // namespace
 
-size_t expand_tc_smem_bytes() { return sizeof(TcSmem); }
+size_t expand_tc_smem_bytes(int maxw)
+{
+    return (sizeof(TcSmem) + 15) / 16 * 16 + (size_t)maxw * (sizeof(const float *) + sizeof(int64_t));
+}
 
 __global__ void __launch_bounds__(TC_THREADS, 2)
     expand_tc(MulArgs<float> ma, const hm_seg *segs, const hm_piece *pieces, const float *P, const float *s,
-              const float *t, int r, int *status)
+              const float *t, int r, int maxw, int *status)
 {
     extern __shared__ __align__(128) unsigned char tc_smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(tc_smem_raw);
+    const float **colbase = reinterpret_cast<const float **>(tc_smem_raw + (sizeof(TcSmem) + 15) / 16 * 16);
+    int64_t *colstride = reinterpret_cast<int64_t *>(colbase + maxw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const hm_seg G = segs[blockIdx.y];
     const int q0 = blockIdx.x * TC_M;
@@ -157,6 +163,30 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = S.tmem_base;
+    // column table of the whole segment (pieces read once; W <= maxw)
+    for (int c = tid; c < W; c += TC_THREADS) {
+        const float *base = nullptr;
+        int64_t step = 0;
+        int pc0 = 0;
+        for (int pi = 0; pi < G.npieces; ++pi) {
+            const hm_piece Q = pieces[G.piece0 + pi];
+            if (c < pc0 + Q.width) {
+                const int pcol = c - pc0;
+                if (Q.kind == HM_PIECE_X) {
+                    base = ma.x + (Q.src + pcol) * ma.incx + (int64_t)q0 * ma.ldx;
+                    step = ma.ldx;
+                } else {
+                    base = (Q.kind == HM_PIECE_TCOEF ? t : s) + ((int64_t)Q.src * ma.k + q0) * r + pcol;
+                    step = r;
+                }
+                break;
+            }
+            pc0 += Q.width;
+        }
+        colbase[c] = base;
+        colstride[c] = step;
+    }
+    __syncthreads();
     // 8-row groups of A that hold live right-hand sides; the others stay zero
     const int live_groups = (qc + 7) >> 3;
     for (int p = 0; p < 3; ++p)
@@ -167,43 +197,16 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     // the chunk are tabulated first (one thread per column).
     auto load_raw = [&](int ch, int b) {
         const int c0 = ch * TC_KC, cols = min(TC_KC, W - c0);
-        if (tid < TC_KC) {
-            const float *base = nullptr;
-            int64_t step = 0;
-            const int cc = c0 + tid;
-            if (tid < cols) {
-                int pc0 = 0;
-                for (int pi = 0; pi < G.npieces; ++pi) {
-                    const hm_piece Q = pieces[G.piece0 + pi];
-                    if (cc < pc0 + Q.width) {
-                        const int pcol = cc - pc0;
-                        if (Q.kind == HM_PIECE_X) {
-                            base = ma.x + (Q.src + pcol) * ma.incx + (int64_t)q0 * ma.ldx;
-                            step = ma.ldx;
-                        } else {
-                            base = (Q.kind == HM_PIECE_TCOEF ? t : s) + ((int64_t)Q.src * ma.k + q0) * r + pcol;
-                            step = r;
-                        }
-                        break;
-                    }
-                    pc0 += Q.width;
-                }
-            }
-            S.colbase[b][tid] = base;
-            S.colstride[b][tid] = step;
-        }
         // panel: column c = i / 16, 16-byte piece j = i % 16 (pieces past ld skipped)
         const float *src = P + G.poff + (int64_t)c0 * G.ld;
         for (int i = tid; i < cols * 16; i += TC_THREADS) {
             const int c = i >> 4, j = i & 15;
             if (4 * j < G.ld) async_copy16(&S.rawP[b][c * TC_PSTRIDE + 4 * j], src + (int64_t)c * G.ld + 4 * j);
         }
-        __syncthreads();                                        // column table visible
         // right-hand sides: q = i / 32, column c = i % 32
         for (int i = tid; i < qc * TC_KC; i += TC_THREADS) {
             const int q = i >> 5, c = i & 31;
-            const int64_t step = S.colstride[b][c];
-            if (step) async_copy<4>(&S.rawG[b][q * TC_GSTRIDE + c], S.colbase[b][c] + q * step);
+            if (c < cols) async_copy<4>(&S.rawG[b][q * TC_GSTRIDE + c], colbase[c0 + c] + q * colstride[c0 + c]);
         }
         async_commit();
     };
