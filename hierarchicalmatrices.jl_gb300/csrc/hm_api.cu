@@ -179,6 +179,15 @@ struct hm_handle {
     void *d_stage = nullptr;
     size_t stage_bytes = 0;
     cudaStream_t host_stream = nullptr;
+    // hm_mul_host replays the product's launches as one CUDA graph: captured
+    // on the second call with the same right-hand-side count and accumulate
+    // flag (the first one runs plainly and sets up scratch and attributes)
+    struct HostGraph {
+        int nrhs = -1, acc = -1;
+        void *stage = nullptr;
+        bool warm = false;
+        cudaGraphExec_t exec = nullptr;
+    } host_graph;
 
     // Optional per-stage timing: CUDA events recorded on the launching stream
     // around each stage of hm_mul.
@@ -1444,8 +1453,31 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
     char *dv = static_cast<char *>(h->d_stage), *du = dv + bv;
     HM_CK(cudaMemcpyAsync(dv, v, bv, cudaMemcpyHostToDevice, st));
     if (accumulate) HM_CK(cudaMemcpyAsync(du, u, bu, cudaMemcpyHostToDevice, st));
-    int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, accumulate ? 1 : 0, st);
-    if (e) return e;
+    auto &hg = h->host_graph;
+    const int acc = accumulate ? 1 : 0;
+    if (hg.nrhs != nrhs || hg.acc != acc || hg.stage != h->d_stage) {
+        if (hg.exec) cudaGraphExecDestroy(hg.exec);
+        hg = hm_handle::HostGraph();
+        hg.nrhs = nrhs; hg.acc = acc; hg.stage = h->d_stage;
+    }
+    if (!hg.exec && hg.warm && h->profile_mask == 0) {
+        HM_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (e) { if (g) cudaGraphDestroy(g); return e; }
+        if (ce != cudaSuccess) { set_error("hm_mul_host capture: %s", cudaGetErrorString(ce)); return HM_ERR_CUDA; }
+        const cudaError_t ie = cudaGraphInstantiate(&hg.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) { hg.exec = nullptr; set_error("hm_mul_host graph: %s", cudaGetErrorString(ie)); return HM_ERR_CUDA; }
+    }
+    if (hg.exec && h->profile_mask == 0) {
+        HM_CK(cudaGraphLaunch(hg.exec, st));
+    } else {
+        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st);
+        if (e) return e;
+        hg.warm = true;
+    }
     HM_CK(cudaMemcpyAsync(u, du, bu, cudaMemcpyDeviceToHost, st));
     HM_CK(cudaStreamSynchronize(st));
     return HM_OK;
@@ -1488,6 +1520,12 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
 int hm_configure(hm_handle *h, int option, int64_t value)
 {
     if (!h) return HM_ERR_INVALID_ARG;
+    // the host-buffer product's captured graph follows the options: drop it
+    if (h->host_graph.exec) {
+        cudaStreamSynchronize(h->host_stream);
+        cudaGraphExecDestroy(h->host_graph.exec);
+    }
+    h->host_graph = hm_handle::HostGraph();
     switch (option) {
     case HM_OPT_OVERLAP:
         if (value < 0 || value > 4) { set_error("HM_OPT_OVERLAP must be in [0, 4]"); return HM_ERR_INVALID_ARG; }
@@ -1545,7 +1583,9 @@ void hm_free(hm_handle *h)
         if (kv.second.side) cudaStreamDestroy(kv.second.side);
         if (kv.second.fork) cudaEventDestroy(kv.second.fork);
         if (kv.second.join) cudaEventDestroy(kv.second.join);
+        if (kv.second.mid) cudaEventDestroy(kv.second.mid);
     }
+    if (h->host_graph.exec) cudaGraphExecDestroy(h->host_graph.exec);
     for (auto &e : h->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     if (h->d_stage) cudaFree(h->d_stage);
     if (h->host_stream) cudaStreamDestroy(h->host_stream);

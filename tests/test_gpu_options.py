@@ -59,3 +59,28 @@ def test_near_kernels_agree(mat, k):
         H.set_near_kernel("auto")
     assert colrel(Us, Uw) <= TOL[dt]
     assert H.device_status() == 0
+
+
+def test_host_buffer_product_replays(mat):
+    # hm_mul_host runs plainly once, then replays a captured graph; options
+    # changed in between are followed (the graph is dropped and captured again)
+    n, dt, H = mat
+    rng = np.random.default_rng(9)
+    v = rng.standard_normal(n).astype(dt)
+    ref = (H @ torch.tensor(v, device="cuda")).cpu().numpy()
+    outs = []
+    for i in range(4):
+        u = np.zeros(n, dtype=dt)
+        H.mul_host(u, v, accumulate=False)
+        outs.append(u)
+        if i == 1:
+            H.set_overlap(1)
+    H.set_overlap(True)
+    for u in outs:
+        assert np.array_equal(u, ref)
+    u0 = rng.standard_normal(n).astype(dt)
+    u = u0.copy()
+    for _ in range(3):
+        u = u0.copy()
+        H.mul_host(u, v, accumulate=True)
+    np.testing.assert_allclose(u, u0 + ref, rtol=TOL[dt], atol=TOL[dt] * np.abs(ref).max())
