@@ -86,7 +86,8 @@ def test_fp32_against_dense():
     assert rel(u[rows], ref) <= TOL32
 
 
-@pytest.mark.parametrize("dtype,k", [(np.float64, 3), (np.float64, 8), (np.float32, 5), (np.float32, 32)])
+@pytest.mark.parametrize("dtype,k", [(np.float64, 3), (np.float64, 8), (np.float64, 12), (np.float32, 5),
+                                     (np.float32, 12), (np.float32, 32)])
 def test_multi_rhs_matches_columns(dtype, k):
     n = 8192
     x, y = O.grid_points(n)
