@@ -892,7 +892,15 @@ int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, dou
 {
     if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
     *out = nullptr;
-    if (!x || !y || nx < 1 || ny < 1) { set_error("empty or NULL point list"); return HM_ERR_INVALID_ARG; }
+    if (nx < 0 || ny < 0 || (nx > 0 && !x) || (ny > 0 && !y)) {
+        set_error("negative length or NULL point list");
+        return HM_ERR_INVALID_ARG;
+    }
+    if (nx == 0 || ny == 0) {
+        // the reference's first indsplit reads x[1] (y[1]) of the empty list
+        set_error("index out of bounds: indsplit reads the first point of an empty point list");
+        return HM_ERR_BOUNDS;
+    }
     if (nx >= (int64_t)1 << 31 || ny >= (int64_t)1 << 31) { set_error("more than 2^31 points"); return HM_ERR_UNSUPPORTED; }
     if (rank == 0) rank = 20;
     if (rank < 1 || rank > HM_RMAX) { set_error("rank %d outside 1..%d", rank, HM_RMAX); return HM_ERR_UNSUPPORTED; }

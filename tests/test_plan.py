@@ -107,9 +107,8 @@ def test_validation_errors():
     with pytest.raises(hm.HMError) as e:
         _lib.Plan(x, x, 1.0, 0.0, 1.0, 0.0, rank=33)
     assert e.value.status == _lib.HM_ERR_UNSUPPORTED
-    with pytest.raises(hm.HMError) as e:
+    with pytest.raises(IndexError):                  # the reference's BoundsError (indsplit on [])
         _lib.Plan(np.zeros(0), x, 1.0, 0.0, 1.0, 0.0)
-    assert e.value.status == _lib.HM_ERR_INVALID_ARG
 
 
 def test_bounds_error_like_reference():
@@ -205,3 +204,18 @@ def test_transposed_row_derivative_is_column_derivative():
     d = emulate(PT, O.CAUCHY, r, drow=True, swap=True)
     ref = (O.kernel_dense(O.CAUCHY, x, y) ** 2).T @ r     # d/dy 1/(x - y) = 1/(x - y)^2
     assert np.linalg.norm(d - ref) / np.linalg.norm(ref) <= 1e-12
+
+
+def test_empty_and_tiny_inputs_like_reference():
+    # src/KernelMatrix.jl:49-50 runs indsplit first, which reads x[first(ir)]
+    # (src/BarycentricMatrix.jl:299-307): an empty point list is a BoundsError,
+    # as in the oracle; a single point on each side is one dense leaf
+    one = np.array([0.25])
+    for x, y in ((np.zeros(0), one), (one, np.zeros(0))):
+        with pytest.raises(IndexError):
+            _lib.Plan(x, y, 1.0, 0.0, 1.0, 0.0)
+        with pytest.raises(Exception):
+            O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0)
+    P = _lib.Plan(np.array([0.75]), np.array([0.25]), 1.0, 0.0, 1.0, 0.0)
+    assert P.sizes["nx"] == 1 and len(P.table("segs")) == 1
+    assert emulate(P, O.CAUCHY, np.array([2.0]))[0] == 2.0 / (0.75 - 0.25)
