@@ -887,6 +887,16 @@ struct hm_plan {
 
 extern "C" {
 
+int hm_chebyshev(int n, double *x, double *lambda)
+{
+    g_last_error.clear();
+    if (n < 1 || !x || !lambda) { set_error("hm_chebyshev: bad arguments"); return HM_ERR_INVALID_ARG; }
+    std::vector<double> xs, ws;
+    chebyshev_first_kind(n, xs, ws);
+    for (int k = 0; k < n; ++k) { x[k] = xs[k]; lambda[k] = ws[k]; }
+    return HM_OK;
+}
+
 int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b, double c,
                    double d, int rank, int64_t blocksize, hm_plan **out)
 {

@@ -8,13 +8,14 @@ and ``mul_`` (Julia's ``mul!``).  All products run CUDA kernels compiled for
 sm_103a in libhmgpu.so.
 """
 from ._lib import HMError, Plan
-from .hierarchical import (AbstractHierarchical, Adjoint, BarycentricMatrix2D, Block, HierarchicalMatrix,
-                           LowRankMatrix, Transpose, adjoint, hierarchical, mul_, transpose)
+from .hierarchical import (AbstractHierarchical, Adjoint, BarycentricMatrix2D, Block, EvenBarycentricMatrix,
+                           HierarchicalMatrix, LowRankMatrix, Transpose, adjoint, hierarchical, mul_, transpose)
 from .kernelmatrix import (BLOCKRANK, BLOCKSIZE, KERNELS, KernelMatrix, KernelMatrixBatch, cauchykernel,
                            coulombkernel, coulombprimekernel, indsplit, logkernel)
 
 __all__ = [
-    "AbstractHierarchical", "Adjoint", "BLOCKRANK", "BLOCKSIZE", "BarycentricMatrix2D", "Block", "HMError",
+    "AbstractHierarchical", "Adjoint", "BLOCKRANK", "BLOCKSIZE", "BarycentricMatrix2D", "Block",
+    "EvenBarycentricMatrix", "HMError",
     "HierarchicalMatrix", "KERNELS", "KernelMatrix", "KernelMatrixBatch", "LowRankMatrix", "Plan", "Transpose",
     "adjoint", "cauchykernel", "coulombkernel", "coulombprimekernel", "hierarchical", "indsplit", "logkernel",
     "mul_", "transpose",

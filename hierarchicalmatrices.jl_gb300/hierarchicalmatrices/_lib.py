@@ -65,7 +65,7 @@ STAGES = ("up", "down", "expand", "far")
 
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
-    "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_device_status", "hm_mul", "hm_mul_strided",
+    "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_device_status", "hm_chebyshev", "hm_mul", "hm_mul_strided",
     "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
     "hm_bary_factors",
@@ -129,6 +129,8 @@ def _load():
     L.hm_stats.argtypes = [_vp, _pi64, ctypes.c_int]
     L.hm_device_status.restype = ctypes.c_int
     L.hm_device_status.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), ctypes.c_int]
+    L.hm_chebyshev.restype = ctypes.c_int
+    L.hm_chebyshev.argtypes = [ctypes.c_int, _d, _d]
     L.hm_mul.restype = ctypes.c_int
     L.hm_mul.argtypes = [_vp, _vp, _i64, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp]
     L.hm_mul_t.restype = ctypes.c_int
@@ -228,3 +230,11 @@ def batch_plan(xs, ys, boxes, rank=20, blocksize=0):
     check(lib.hm_batch_plan_create(len(xs), nx.ctypes.data_as(_pi64), ny.ctypes.data_as(_pi64),
                                    f64_ptr(x), f64_ptr(y), f64_ptr(bx), rank, blocksize, ctypes.byref(h)))
     return Plan(x, y, 0, 0, 0, 0, _handle=h)
+
+
+def chebyshev(n):
+    """First-kind Chebyshev nodes and barycentric weights in FP64, as the
+    library builds them (src/BarycentricMatrix.jl:92-136)."""
+    x, lam = np.zeros(n), np.zeros(n)
+    check(lib.hm_chebyshev(int(n), f64_ptr(x), f64_ptr(lam)))
+    return x, lam

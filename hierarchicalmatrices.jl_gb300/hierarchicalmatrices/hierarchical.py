@@ -97,6 +97,66 @@ class BarycentricMatrix2D:
         return U @ F @ V.T
 
 
+class EvenBarycentricMatrix:
+    """EvenBarycentricMatrix(T, f, a, b, c, d) (src/BarycentricMatrix.jl:5-45):
+    the block of rows a:b and columns c:d (integers) of a kernel f(T, x, j)
+    that couples only rows and columns of matching parity, interpolated in
+    the row variable at BLOCKRANK(T) first-kind Chebyshev nodes of [a, b].
+    W (n x (b-a+1)) and F ((d-c+1) x n) are formed on the host in FP64 with
+    the reference's formulas (F calls the user's f) and stored on the device,
+    split by row and column parity, as ``dtype``; mul_ runs its products on
+    the GPU (two stride-2 low-rank products, src/algebra.jl:168-239)."""
+
+    @staticmethod
+    def factors(f, a, b, c, d, n, T=np.float64):
+        """(W, F) in FP64 by src/BarycentricMatrix.jl:17-45: w_i = sum_k
+        lambda_k / (2i - a - b - (b - a) x_k), W[k, i] = lambda_k / ((2i - a - b -
+        (b - a) x_k) w_i), F[j, k] = f(T, (a + b)/2 + (b - a) x_k / 2, j)."""
+        x, lam = _lib.chebyshev(n)
+        i = np.arange(a, b + 1, dtype=np.float64)
+        den = (2.0 * i[None, :] - a - b) - (b - a) * x[:, None]            # n x m
+        w = np.zeros(i.size)
+        for k in range(n):                                                  # the reference's order over k
+            w += lam[k] * (1.0 / den[k])
+        W = lam[:, None] * (1.0 / (den * w[None, :]))
+        F = np.empty((d - c + 1, n))
+        for k in range(n):
+            node = (a + b) / 2 + (b - a) * x[k] / 2
+            for jj in range(d - c + 1):
+                F[jj, k] = f(T, node, c + jj)
+        return W, F
+
+    def __init__(self, f, a, b, c, d, *, dtype=np.float64, rank=None, device="cuda"):
+        import torch
+        from .kernelmatrix import BLOCKRANK
+        T = np.dtype(dtype).type
+        n = int(rank) if rank else BLOCKRANK(T)
+        a, b, c, d = int(a), int(b), int(c), int(d)
+        W, F = self.factors(f, a, b, c, d, n, T)
+        self.W, self.F = W, F
+        self.a, self.b, self.c, self.d, self.n = a, b, c, d, n
+        self.shape = (b - a + 1, d - c + 1)
+        tdt = torch.float64 if np.dtype(dtype) == np.float64 else torch.float32
+
+        def dev(M):                                          # column-major device copy
+            return torch.tensor(np.ascontiguousarray(M.T), dtype=tdt, device=device).t()
+        # parity p (0-based row/column index parity) factors: U_p = W[:, p::2]^T, V_p = F[p::2, :]
+        self.U = [dev(W[:, p::2].T) for p in (0, 1)]
+        self.V = [dev(F[p::2, :]) for p in (0, 1)]
+        self.ones = torch.ones(n, dtype=tdt, device=device)
+
+    def rank(self):
+        return self.n
+
+    def dense(self, istart=1, jstart=1):
+        """The operator mul_ applies at these offsets (entries couple when
+        i + j + istart + jstart is even, 1-based i, j)."""
+        m, p = self.shape
+        M = (self.F @ self.W).T                                              # m x p, before the parity mask
+        ii, jj = np.meshgrid(np.arange(1, m + 1), np.arange(1, p + 1), indexing="ij")
+        return np.where((ii + jj + istart + jstart) % 2 == 0, M, 0.0)
+
+
 class Transpose:
     """transpose(A) for a dense block (src/algebra.jl:50-65)."""
 
@@ -397,6 +457,20 @@ def mul_(y, A, x, istart=1, jstart=1, incx=1, incy=1, *, stream=None):
         m, n, r = U.shape[0], V.shape[0], s.shape[0]
         check(lib.hm_lowrank_mul(1 if trans else 0, dt, _colmajor(U).data_ptr(), s.contiguous().data_ptr(), 1,
                                  _colmajor(V).data_ptr(), m, n, r, xp, lx, jstart, incx, yp, ly, istart, incy, sp))
+        return y
+    if isinstance(B, EvenBarycentricMatrix):
+        if trans:
+            raise TypeError("the reference defines no transposed EvenBarycentricMatrix product")
+        m, p = B.shape
+        ishift, jshift = istart - 1, jstart - 1
+        for pi in (0, 1):                              # 0-based row parity
+            pj = pi if (ishift + jshift) % 2 == 0 else 1 - pi
+            mu, nv = B.U[pi].shape[0], B.V[pj].shape[0]
+            if mu == 0 or nv == 0:
+                continue
+            check(lib.hm_lowrank_mul(0, dt, B.U[pi].data_ptr(), B.ones.data_ptr(), 1, B.V[pj].data_ptr(),
+                                     mu, nv, B.n, xp, lx, jstart + pj * incx, 2 * incx, yp, ly,
+                                     istart + pi * incy, 2 * incy, sp))
         return y
     if isinstance(B, BarycentricMatrix2D):
         m, n = B.shape

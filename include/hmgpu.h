@@ -111,6 +111,11 @@ int hm_dense_mul(int trans, int dtype, const void *A, int64_t m, int64_t n, int6
                  const void *x, int64_t lenx, int64_t jstart, int64_t incx, void *y, int64_t leny,
                  int64_t istart, int64_t incy, void *stream);
 
+/* chebyshevpoints(T, n) and chebyshevbarycentricweights(T, n), first kind,
+   in FP64 (src/BarycentricMatrix.jl:92-136): the nodes and weights of every
+   barycentric factor the library builds. */
+int hm_chebyshev(int n, double *x, double *lambda);
+
 /* y += U C V^T x (adjoint = 0) or y += V C^T U^T x (adjoint = 1) with U m x r
    and V n x r column-major; C = diag(core) when core_diag (LowRankMatrix
    mul! and its adjoint, src/algebra.jl:110-131, 137-159) or the r x r

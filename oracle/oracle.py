@@ -322,3 +322,53 @@ def beta_points(n, seed, min_gap=1e-9):
                 p[i] = p[i - 1] + min_gap
         out.append(p[::-1].copy())
     return out[0], out[1]
+
+
+# ------------------------------------------------------------ EvenBarycentricMatrix
+
+def even_bary_factors(f, a, b, c, d, n, T=np.float64):
+    """W (n x m) and F (p x n) of EvenBarycentricMatrix(T, f, a, b, c, d) in
+    FP64, in the loop order of src/BarycentricMatrix.jl:17-45 (f(T, x, j) is
+    the user's kernel on the integer grid)."""
+    x = chebyshevpoints(n)
+    lam = chebyshevbarycentricweights(n)
+    m, p = b - a + 1, d - c + 1
+    w = np.zeros(m)
+    for ii in range(m):
+        i = a + ii
+        for k in range(n):
+            w[ii] += lam[k] * (1.0 / ((2 * i - a - b) - (b - a) * x[k]))
+    W = np.zeros((n, m))
+    for ii in range(m):
+        i = a + ii
+        for k in range(n):
+            W[k, ii] = lam[k] * (1.0 / (((2 * i - a - b) - (b - a) * x[k]) * w[ii]))
+    F = np.zeros((p, n))
+    for k in range(n):
+        for jj in range(p):
+            F[jj, k] = f(T, (a + b) / 2 + (b - a) * x[k] / 2, c + jj)
+    return W, F
+
+
+def even_bary_mul(u, W, F, v, istart, jstart):
+    """mul!(u, B::EvenBarycentricMatrix, v, istart, jstart) in the loop order
+    of src/algebra.jl:168-239: rows and columns of matching parity (odd with
+    odd, even with even when istart + jstart is even; crossed otherwise)."""
+    n, m = W.shape
+    p = F.shape[0]
+    ishift, jshift = istart - 1, jstart - 1
+    # (first 1-based column of the inner sum, first 1-based row it feeds)
+    pairs = ((1, 1), (2, 2)) if (ishift + jshift) % 2 == 0 else ((2, 1), (1, 2))
+    for jfirst, ifirst in pairs:
+        beta = np.zeros(n)
+        for k in range(n):
+            bk = 0.0
+            for j in range(jfirst, p + 1, 2):
+                bk += v[jshift + j - 1] * F[j - 1, k]
+            beta[k] = bk
+        for i in range(ifirst, m + 1, 2):
+            ui = 0.0
+            for k in range(n):
+                ui += beta[k] * W[k, i - 1]
+            u[ishift + i - 1] += ui
+    return u
