@@ -231,18 +231,13 @@ int hm_configure(hm_handle *h, int option, int64_t value);
    start-up because those calls can synchronise the device.
      u (+)= H v   (accumulate = 1 adds, as the reference's mul!; 0 overwrites)
    u, v: DEVICE vectors of the handle's storage type (lengths nx, ny).
-   The coefficient scratch is a 16 MiB array compiled into the library
-   (every GPU that loads the library holds it until the process exits);
-   matrices needing more than (n_xslots + n_yslots) * rank * element size
-   bytes (each part rounded up to 256) are rejected with HM_ERR_UNSUPPORTED.  Besides coefficients (each call
-   writes them before reading them) the array holds synchronisation words
-   that must start at zero: they are zero when the library loads and every
-   complete call leaves them at zero again.  All calls
-   share the one array: calls that overlap on the GPU (different streams,
-   or different handles, at the same time) race and give wrong results.
-   The first call on each device looks up the array's device address
-   (cudaGetSymbolAddress) with that device current; make that first call
-   before any stream capture.  Calls no cudaMalloc/cudaFree. */
+   The coefficient scratch ((n_xslots + n_yslots) * rank elements of the
+   storage type) is reserved when the handle is built and freed by hm_free;
+   the call makes no cudaMalloc/cudaFree.  Calls on one handle from different
+   streams are ordered on the GPU (each waits for the previous call's end
+   through an event); inside stream capture that ordering is not recorded,
+   so replays of a captured call must not overlap other calls on the same
+   handle.  Different handles never share scratch. */
 int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *stream);
 
 /* Per-stage timing of hm_mul (the reference prints @time per call,

@@ -1,5 +1,6 @@
-"""FP32 products with many right-hand sides on the tensor cores (tcgen05,
-three TF32 products per step, FP32 accumulation) against the FP64-storage
+"""FP32 products with many right-hand sides on the tensor cores (tcgen05
+kind::f16: each FP32 operand split exactly into three BF16 pieces, six piece
+products, FP32 accumulation in tensor memory) against the FP64-storage
 product (<= 1e-12 of the dense FP64 one) and against the same FP32 factors on
 the FP32 pipes.  Tolerance: 1e-6 relative 2-norm error per column."""
 import numpy as np
