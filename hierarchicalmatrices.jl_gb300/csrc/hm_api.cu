@@ -34,6 +34,23 @@ void set_error(const char *fmt, ...)
     g_last_error = buf;
 }
 
+}  // namespace
+
+namespace hm {
+void set_last_error(const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+void clear_last_error() { g_last_error.clear(); }
+}  // namespace hm
+
+namespace {
+
 int cuda_status(cudaError_t e, const char *what)
 {
     if (e == cudaSuccess) return HM_OK;
@@ -1038,6 +1055,7 @@ const char *hm_status_string(int status)
     case HM_ERR_UNSUPPORTED: return "unsupported parameter";
     case HM_ERR_BOX: return "box ends must satisfy a > b and c > d";
     case HM_ERR_DEGENERATE: return "degenerate partition";
+    case HM_ERR_NOT_POSDEF: return "matrix is not positive definite";
     default: return "unknown status";
     }
 }

@@ -10,6 +10,10 @@
 
 namespace hm {
 
+// The calling thread's error message behind hm_last_error (hm_api.cu).
+void set_last_error(const char *fmt, ...);
+void clear_last_error();
+
 // ---------------------------------------------------------------- numerics
 
 // Kernels of examples/Kernel.jl:34-37, evaluated in FP64 with every operation

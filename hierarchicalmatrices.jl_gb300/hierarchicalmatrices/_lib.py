@@ -22,6 +22,9 @@ HM_ERR_ALLOC = 6
 HM_ERR_UNSUPPORTED = 7
 HM_ERR_BOX = 8
 HM_ERR_DEGENERATE = 9
+HM_ERR_NOT_POSDEF = 10
+HM_LR_KMAX = 96
+HM_SOLVE_TRSM, HM_SOLVE_LR, HM_SOLVE_DENSE = 0, 1, 2
 
 HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
 HM_F64, HM_F32 = 0, 1
@@ -68,13 +71,52 @@ EXPORTED = (
     "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_device_status", "hm_chebyshev", "hm_mul", "hm_mul_strided",
     "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
-    "hm_bary_factors",
+    "hm_bary_factors", "hm_lr_svd", "hm_gemm_batched", "hm_axpby_batched", "hm_potrf_batched",
+    "hm_solve_transposed",
 )
 
 _d = ctypes.POINTER(ctypes.c_double)
 _i64 = ctypes.c_int64
 _pi64 = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
+
+
+_c64 = ctypes.c_int64
+_c32 = ctypes.c_int32
+
+
+class LrProblem(ctypes.Structure):
+    """hm_lr_problem of include/hmgpu.h."""
+    _fields_ = [("m", _c64), ("n", _c64), ("t", _c64), ("a1", _c32), ("a2", _c32), ("b1", _c32), ("b2", _c32),
+                ("qr_left", _c32), ("qr_right", _c32), ("P1", _vp), ("P2", _vp), ("Q1", _vp), ("Q2", _vp),
+                ("ldp1", _c64), ("ldp2", _c64), ("ldq1", _c64), ("ldq2", _c64), ("s1", _vp), ("s2", _vp),
+                ("sign2", ctypes.c_double), ("Xm", _vp), ("Ym", _vp), ("ldx", _c64), ("ldy", _c64),
+                ("U", _vp), ("s", _vp), ("V", _vp)]
+
+
+class GemmProblem(ctypes.Structure):
+    """hm_gemm_problem of include/hmgpu.h."""
+    _fields_ = [("m", _c64), ("n", _c64), ("k", _c64), ("P", _vp), ("ldp", _c64), ("transp", _c32),
+                ("Q", _vp), ("ldq", _c64), ("transq", _c32), ("s", _vp), ("alpha", ctypes.c_double),
+                ("beta", ctypes.c_double), ("C", _vp), ("ldc", _c64), ("D", _vp), ("ldd", _c64)]
+
+
+class AxpbyProblem(ctypes.Structure):
+    """hm_axpby_problem of include/hmgpu.h."""
+    _fields_ = [("m", _c64), ("n", _c64), ("A", _vp), ("lda", _c64), ("B", _vp), ("ldb", _c64),
+                ("dr", _vp), ("dc", _vp), ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+                ("D", _vp), ("ldd", _c64)]
+
+
+class PotrfProblem(ctypes.Structure):
+    """hm_potrf_problem of include/hmgpu.h."""
+    _fields_ = [("n", _c64), ("A", _vp), ("lda", _c64), ("R", _vp), ("ldr", _c64)]
+
+
+class SolveOp(ctypes.Structure):
+    """hm_solve_op of include/hmgpu.h."""
+    _fields_ = [("kind", _c32), ("r", _c32), ("o1", _c64), ("n1", _c64), ("o2", _c64), ("n2", _c64),
+                ("ld", _c64), ("ld2", _c64), ("A", _vp), ("s", _vp), ("B", _vp)]
 
 
 class HMError(RuntimeError):
@@ -121,6 +163,17 @@ def _load():
     L.hm_bary_factors.restype = ctypes.c_int
     L.hm_bary_factors.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, _d, _i64, _d, _i64, ctypes.c_int, _vp, _vp, _vp, _vp]
+    L.hm_lr_svd.restype = ctypes.c_int
+    L.hm_lr_svd.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(LrProblem), ctypes.POINTER(ctypes.c_int32), _vp]
+    L.hm_gemm_batched.restype = ctypes.c_int
+    L.hm_gemm_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(GemmProblem), _vp]
+    L.hm_axpby_batched.restype = ctypes.c_int
+    L.hm_axpby_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(AxpbyProblem), _vp]
+    L.hm_potrf_batched.restype = ctypes.c_int
+    L.hm_potrf_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(PotrfProblem),
+                                   ctypes.POINTER(ctypes.c_int32), _vp]
+    L.hm_solve_transposed.restype = ctypes.c_int
+    L.hm_solve_transposed.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SolveOp), _vp, _i64, _i64, _vp]
     L.hm_size.restype = ctypes.c_int
     L.hm_size.argtypes = [_vp, _pi64, _pi64]
     L.hm_storage.restype = ctypes.c_int

@@ -65,6 +65,56 @@ class LowRankMatrix:
         U, s, V = _np64(self.U), _np64(self.sigma), _np64(self.V)
         return (U * s) @ V.T
 
+    def norm(self):
+        """norm(L) = first(sigma) (src/LowRankMatrix.jl:46)."""
+        return float(_np64(self.sigma[:1])[0])
+
+    def cond(self):
+        """cond(L) (src/LowRankMatrix.jl:47): Inf below full rank, else sigma_1 / sigma_r."""
+        s = _np64(self.sigma)
+        return float("inf") if len(s) < min(self.shape) else float(s[0] / s[-1])
+
+    def getindex(self, i, j):
+        """L[i, j], 1-based, summed over k = r:-1:1 (src/LowRankMatrix.jl:50-58)."""
+        U, s, V = _np64(self.U[i - 1]), _np64(self.sigma), _np64(self.V[j - 1])
+        ret = 0.0
+        for k in range(len(s) - 1, -1, -1):
+            ret += U[k] * s[k] * V[k]
+        return ret
+
+    def __getitem__(self, key):
+        """L[ir, jr] for 0-based slices: LowRankMatrix(U[ir, :], sigma, V[jr, :])
+        (src/LowRankMatrix.jl:60-62)."""
+        ir, jr = key
+        if isinstance(ir, slice) and isinstance(jr, slice):
+            return LowRankMatrix(self.U[ir], self.sigma, self.V[jr])
+        return self.getindex(int(ir) + 1, int(jr) + 1)
+
+    # the reference's arithmetic (src/LowRankMatrix.jl:95-171, src/algebra.jl:394-524)
+    def __add__(self, other):
+        from . import algebra
+        return algebra.add(self, other)
+
+    def __sub__(self, other):
+        from . import algebra
+        return algebra.sub(self, other)
+
+    def __mul__(self, other):
+        from . import algebra
+        return algebra.times(self, other)
+
+    def __rmul__(self, other):
+        from . import algebra
+        return algebra.times(other, self)
+
+    def __matmul__(self, other):
+        from . import algebra
+        return algebra.times(self, other)
+
+    def __truediv__(self, B):
+        from . import algebra
+        return algebra.lr_scale(self, 1.0 / float(B))
+
 
 class BarycentricMatrix2D:
     """The barycentric block of the kernel f on boxes [a, b] x [c, d] for the
@@ -172,6 +222,13 @@ class Adjoint:
         self.parent = A
         self.shape = (A.shape[1], A.shape[0])
 
+    def __mul__(self, other):
+        """L1' * L2 (src/LowRankMatrix.jl:120-126)."""
+        from . import algebra
+        return algebra.times(self, other)
+
+    __matmul__ = __mul__
+
 
 def transpose(A):
     return Transpose(A)
@@ -233,6 +290,15 @@ class AbstractHierarchical:
         if self._handle is not None:
             lib.hm_free(self._handle)
         self._handle = None
+
+    # blockwise sums (src/algebra.jl:394-524, src/hierarchical.jl:174-231)
+    def __add__(self, other):
+        from . import algebra
+        return algebra.add(self, other)
+
+    def __sub__(self, other):
+        from . import algebra
+        return algebra.sub(self, other)
 
     def block(self, m, n):
         tag = self.assigned[m, n]

@@ -35,7 +35,8 @@ enum {
     HM_ERR_ALLOC = 6,         /* device allocation failed */
     HM_ERR_UNSUPPORTED = 7,   /* rank above 32, unknown kernel or storage type */
     HM_ERR_BOX = 8,           /* box ends not strictly decreasing (a > b, c > d) */
-    HM_ERR_DEGENERATE = 9     /* a partition the reference itself builds inconsistently */
+    HM_ERR_DEGENERATE = 9,    /* a partition the reference itself builds inconsistently */
+    HM_ERR_NOT_POSDEF = 10    /* PosDefException: a Cholesky pivot is not positive */
 };
 
 /* Kernels of examples/Kernel.jl:34-37. */
@@ -276,6 +277,109 @@ int hm_plan_table(const hm_plan *p, int which, const void **data, int64_t *count
    reference-layout values, stored values, dense values, row segments. */
 int hm_plan_sizes(const hm_plan *p, int64_t *out, int nout);
 void hm_plan_free(hm_plan *p);
+
+/* ------------------------------------------------------------------------
+   Low-rank arithmetic and the blockwise Cholesky (src/LowRankMatrix.jl:70-171,
+   src/algebra.jl:394-524, src/hierarchical.jl:174-231, src/cholesky.jl).
+   The recursion over blocks runs on the host (hierarchicalmatrices/algebra.py);
+   these batched calls do the arithmetic on the GPU.  All matrices are
+   column-major DEVICE arrays of type dtype (HM_F64 or HM_F32), descriptors
+   and result arrays are HOST arrays.  Calls marked synchronous return after
+   the stream has finished the work.
+   ------------------------------------------------------------------------ */
+
+/* One truncated SVD of a product  X = P M Q^T  (the common core of every
+   LowRankMatrix operation of src/LowRankMatrix.jl:82-158):
+     P = [P1 P2]  m x (a1 + a2)       Q = [Q1 Q2]  n x (b1 + b2)
+     M = diag(s1 ; sign2 * s2)        when Xm == NULL (then a1 + a2 == b1 + b2)
+     M = diag(s1) Xm^T Ym diag(s2)    otherwise (Xm t x a1, Ym t x b1; a2 = b2 = 0)
+   qr_left / qr_right: orthonormalise P / Q by Householder QR first, as the
+   reference's qr! does (the sum, A*L and L*A forms); without QR the factor is
+   used as given (the L1*L2 and L1'*L2 forms).  Q1 == NULL stands for the
+   identity (n == b1, b2 == 0, qr_right == 0: svdtrunc of a dense P).
+   The core (R_P M R_Q^T, or M) is ka x kb with ka = qr_left ? min(m, a) : a
+   and kb likewise; its singular values are q = min(ka, kb), at most
+   HM_LR_KMAX of each of ka, kb.  Outputs: U (m x q, ld m), s (q) and V
+   (n x q, ld n) receive the first r columns / values in descending order,
+   r = getrank(sigma) = #{sigma_j > q * eps(sigma_1)} (src/LowRankMatrix.jl:70-80). */
+#define HM_LR_KMAX 96
+typedef struct {
+    int64_t m, n, t;
+    int32_t a1, a2, b1, b2;
+    int32_t qr_left, qr_right;
+    const void *P1, *P2, *Q1, *Q2;
+    int64_t ldp1, ldp2, ldq1, ldq2;
+    const void *s1, *s2;
+    double sign2;
+    const void *Xm, *Ym;
+    int64_t ldx, ldy;
+    void *U, *s, *V;
+} hm_lr_problem;
+
+/* Batched truncated SVDs (one CTA per problem).  ranks (host, nprob) receives
+   r per problem.  Synchronous. */
+int hm_lr_svd(int dtype, int nprob, const hm_lr_problem *probs, int32_t *ranks, void *stream);
+
+/* D = beta C + alpha P diag(s) Q^T with P m x k (or its transpose stored k x m
+   when transp), Q n x k (or k x n when transq), s = NULL for ones, C = NULL
+   for C = D (C may also equal D); beta = 0 never reads C.  Covers Matrix -/+
+   LowRankMatrix blocks of H -/+ L (src/algebra.jl:460-524), A22 - R12'R12
+   for a dense R12 (src/cholesky.jl:40-56) and the dense products A*L.U,
+   A'*L.V of src/LowRankMatrix.jl:128-142. */
+typedef struct {
+    int64_t m, n, k;
+    const void *P; int64_t ldp; int32_t transp;
+    const void *Q; int64_t ldq; int32_t transq;
+    const void *s;
+    double alpha, beta;
+    const void *C; int64_t ldc;
+    void *D; int64_t ldd;
+} hm_gemm_problem;
+int hm_gemm_batched(int dtype, int nprob, const hm_gemm_problem *probs, void *stream);
+
+/* D[i, j] = alpha dr[i] A[i, j] dc[j] + beta B[i, j] (m x n blocks; dr, dc =
+   NULL for ones; B = NULL when beta = 0): Matrix +/- Matrix of H +/- H
+   (src/hierarchical.jl:174-231), Diagonal * L.U and L.V * Diagonal
+   (src/LowRankMatrix.jl:144-158), scalar * L (:160-171) and block copies. */
+typedef struct {
+    int64_t m, n;
+    const void *A; int64_t lda;
+    const void *B; int64_t ldb;
+    const void *dr, *dc;
+    double alpha, beta;
+    void *D; int64_t ldd;
+} hm_axpby_problem;
+int hm_axpby_batched(int dtype, int nprob, const hm_axpby_problem *probs, void *stream);
+
+/* hierarchicalcholesky(A::Matrix) = Matrix(cholesky(Symmetric(A)).U)
+   (src/cholesky.jl:16-18): R (n x n, ld ldr) = the upper Cholesky factor of
+   the symmetric matrix whose upper triangle is A's (A n x n, ld lda), zeros
+   below the diagonal; R may equal A.  info (host, nprob): 0, or j >= 1 when
+   the j-th pivot is not positive (then the call returns HM_ERR_NOT_POSDEF).
+   Synchronous. */
+typedef struct {
+    int64_t n;
+    const void *A; int64_t lda;
+    void *R; int64_t ldr;
+} hm_potrf_problem;
+int hm_potrf_batched(int dtype, int nprob, const hm_potrf_problem *probs, int32_t *info, void *stream);
+
+/* solvetransposed(R, B) (src/cholesky.jl:97-228): B <- R^{-T} B in place for
+   the ncols columns of B (ld ldb), R an upper block-triangular hierarchical
+   matrix given as its forward-substitution schedule, ops in the order of the
+   reference's recursion:
+     HM_SOLVE_TRSM   x[o1 : o1+n1) <- R^{-T} x[..]          (A = R, n1 x n1 upper, ld)
+     HM_SOLVE_LR     x[o2 : o2+n2) -= V diag(s) U^T x[o1 : o1+n1)
+                                                              (A = U n1 x r ld, B = V n2 x r ld2)
+     HM_SOLVE_DENSE  x[o2 : o2+n2) -= M^T x[o1 : o1+n1)       (A = M n1 x n2, ld)  */
+enum { HM_SOLVE_TRSM = 0, HM_SOLVE_LR = 1, HM_SOLVE_DENSE = 2 };
+typedef struct {
+    int32_t kind, r;
+    int64_t o1, n1, o2, n2, ld, ld2;
+    const void *A, *s, *B;
+} hm_solve_op;
+int hm_solve_transposed(int dtype, int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t ncols,
+                        void *stream);
 
 #ifdef __cplusplus
 }

@@ -28,7 +28,7 @@ def test_header_symbols_exported():
 
 
 def test_status_strings():
-    for code in range(10):
+    for code in range(11):
         assert _lib.lib.hm_status_string(code).decode() != "unknown status"
     assert _lib.lib.hm_status_string(99).decode() == "unknown status"
     assert _lib.lib.hm_version() >= 100

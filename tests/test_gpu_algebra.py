@@ -1,0 +1,188 @@
+"""Low-rank algebra, H +/- L, H +/- H, hierarchicalcholesky and solvetransposed
+on the GPU (hm_lr_svd, hm_gemm_batched, hm_axpby_batched, hm_potrf_batched,
+hm_solve_transposed) against the CPU oracle (oracle/algebra.py, pinned by
+dense known answers).
+
+Truncated SVDs are unique only up to the singular vectors' signs, so results
+are compared as the matrices they represent (relative Frobenius error), with
+ranks compared where the spectrum is far from the getrank threshold.
+Tolerances: 1e-12 in FP64 and 2e-5 in FP32 for the block operations; the
+Cholesky factor's own bounds (CHOL) separate forward from backward error."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import hierarchicalmatrices as hm  # noqa: E402
+from hierarchicalmatrices import algebra as G  # noqa: E402
+from oracle import algebra as A  # noqa: E402
+
+TOL = {torch.float64: 1e-12, torch.float32: 2e-5}
+DT = [torch.float64, torch.float32]
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def dev(a, dt):
+    return torch.tensor(np.ascontiguousarray(np.asarray(a).T), dtype=dt, device="cuda").t() if np.ndim(a) == 2 \
+        else torch.tensor(np.asarray(a), dtype=dt, device="cuda")
+
+
+def host(t):
+    return t.detach().double().cpu().numpy()
+
+
+def lr_dev(L, dt):
+    return hm.LowRankMatrix(dev(L.U, dt), dev(L.s, dt), dev(L.V, dt))
+
+
+def lr_host(L):
+    return A.LR(host(L.U), host(L.sigma), host(L.V))
+
+
+def tree_dev(T, dt):
+    if isinstance(T, A.LR):
+        return lr_dev(T, dt)
+    if not isinstance(T, A.HB):
+        return dev(T, dt)
+    H = hm.HierarchicalMatrix(T.M, T.N, dtype=np.float64 if dt == torch.float64 else np.float32)
+    for m in range(T.M):
+        for n in range(T.N):
+            if T.blocks[m][n] is not None:
+                H[hm.Block(m + 1), hm.Block(n + 1)] = tree_dev(T.blocks[m][n], dt)
+    return H
+
+
+def tree_host(H):
+    if isinstance(H, hm.LowRankMatrix):
+        return lr_host(H)
+    if isinstance(H, torch.Tensor):
+        return host(H)
+    M, N = H.blocksize()
+    return A.HB([[None if H.block(m, n) is None else tree_host(H.block(m, n)) for n in range(N)] for m in range(M)])
+
+
+def rand_lr(rng, m, n, r, decay=0.5):
+    U, _ = np.linalg.qr(rng.standard_normal((m, r)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, r)))
+    return A.LR(U, decay ** np.arange(r), V)
+
+
+def check_svd_form(L, dt):
+    """Descending non-negative singular values and orthonormal factors."""
+    s = host(L.sigma)
+    assert np.all(np.diff(s) <= 0) and np.all(s >= 0)
+    tol = 1e-12 if dt == torch.float64 else 1e-5
+    for F in (host(L.U), host(L.V)):
+        assert np.abs(F.T @ F - np.eye(F.shape[1])).max() < tol
+
+
+@pytest.mark.parametrize("dt", DT)
+def test_lowrank_operations(dt):
+    rng = np.random.default_rng(11)
+    L1, L2 = rand_lr(rng, 300, 200, 6), rand_lr(rng, 300, 200, 9)
+    g1, g2 = lr_dev(L1, dt), lr_dev(L2, dt)
+    cases = [
+        (G.lr_add(g1, g2), A.lr_add(L1, L2)),
+        (G.lr_sub(g1, g2), A.lr_sub(L1, L2)),
+        (G.lr_add(g1, g1), A.lr_add(L1, L1)),
+    ]
+    L3 = rand_lr(rng, 200, 150, 5)
+    cases.append((G.lr_mul(g1, lr_dev(L3, dt)), A.lr_mul(L1, L3)))
+    L4 = rand_lr(rng, 300, 120, 4)
+    cases.append((G.times(hm.adjoint(g1), lr_dev(L4, dt)), A.lr_adjmul(L1, L4)))
+    M = rng.standard_normal((90, 300))
+    cases.append((G.times(dev(M, dt), g1), A.dense_lr_mul(M, L1)))
+    N = rng.standard_normal((200, 70))
+    cases.append((G.times(g1, dev(N, dt)), A.lr_dense_mul(L1, N)))
+    d1, d2 = rng.uniform(0.5, 2.0, 300), rng.uniform(0.5, 2.0, 200)
+    cases.append((G.times(G.Diagonal(dev(d1, dt)), g1), A.dense_lr_mul(np.diag(d1), L1)))
+    cases.append((G.times(g1, G.Diagonal(dev(d2, dt))), A.lr_dense_mul(L1, np.diag(d2))))
+    for got, ref in cases:
+        check_svd_form(got, dt)
+        assert got.rank() == len(ref.s)
+        assert rel(A.lr_dense(lr_host(got)), A.lr_dense(ref)) <= TOL[dt]
+    Z = G.lr_sub(g1, g1)                        # rank-deficient: ranks may differ, the matrix is ~0
+    assert np.linalg.norm(A.lr_dense(lr_host(Z))) <= TOL[dt] * np.linalg.norm(A.lr_dense(L1))
+    S = G.times(2.5, g1)
+    assert rel(host(S.sigma), 2.5 * L1.s) <= TOL[dt]
+
+
+@pytest.mark.parametrize("dt", DT)
+@pytest.mark.parametrize("m,n", [(400, 40), (40, 400), (96, 96), (7, 3)])
+def test_svdtrunc(dt, m, n):
+    rng = np.random.default_rng(m + n)
+    k = min(m, n, 12)
+    B = rng.standard_normal((m, k)) @ np.diag(0.7 ** np.arange(k)) @ rng.standard_normal((k, n))
+    got, ref = G.svdtrunc(dev(B, dt)), A.svdtrunc(B)
+    check_svd_form(got, dt)
+    if dt == torch.float64:
+        assert got.rank() == len(ref.s) == k
+    assert rel(A.lr_dense(lr_host(got)), B) <= TOL[dt] * 10
+
+
+@pytest.mark.parametrize("dt", DT)
+@pytest.mark.parametrize("dense_below", [0, 128])
+def test_tree_sums(dt, dense_below):
+    T, _ = A.spd_hodlr(512, 32, dense_below=dense_below, seed=12)
+    rng = np.random.default_rng(13)
+    L = rand_lr(rng, 512, 512, 5)
+    H, g = tree_dev(T, dt), lr_dev(L, dt)
+    for got, ref in ((G.add(H, g), A.h_lr(T, L, 1.0, 1.0, False)),
+                     (G.sub(H, g), A.h_lr(T, L, 1.0, -1.0, False)),
+                     (G.add(g, H), A.h_lr(T, L, 1.0, 1.0, True)),
+                     (G.sub(g, H), A.h_lr(T, L, -1.0, 1.0, True))):
+        assert (got.assigned == H.assigned).all()
+        assert rel(A.todense(tree_host(got)), A.todense(ref)) <= TOL[dt]
+    assert rel(A.todense(tree_host(G.add(H, H))), A.todense(A.h_h(T, T, 1.0))) <= TOL[dt]
+    D = A.todense(T)
+    assert np.linalg.norm(A.todense(tree_host(G.sub(H, H)))) <= TOL[dt] * np.linalg.norm(D)
+    assert rel(host(G.todense(H)), D) <= TOL[dt]
+
+
+# Cholesky tolerances: the factor's forward error grows with the condition
+# number (about 4e4 here), the backward errors (R'R - A, R'x - b) do not.
+CHOL = {torch.float64: dict(fwd=1e-10, bwd=1e-12, solve=1e-9),
+        torch.float32: dict(fwd=1e-2, bwd=1e-4, solve=5e-3)}
+
+
+@pytest.mark.parametrize("dt", DT)
+@pytest.mark.parametrize("kernel,dense_below", [("gauss", 0), ("gauss", 128), ("exp", 0)])
+def test_hierarchical_cholesky(dt, kernel, dense_below):
+    T, D = A.spd_hodlr(1024, 64, kernel=kernel, dense_below=dense_below, seed=14)
+    R = G.hierarchicalcholesky(tree_dev(T, dt))
+    Rd = A.todense(tree_host(R))
+    Ro = A.todense(A.cholesky(T))
+    tol = CHOL[dt]
+    assert np.allclose(np.tril(Rd, -1), 0)
+    assert rel(Rd, Ro) <= tol["fwd"]
+    assert rel(Rd.T @ Rd, D) <= tol["bwd"]
+    # solvetransposed on the factor: vector, matrix and low-rank right-hand sides
+    rng = np.random.default_rng(15)
+    b = rng.standard_normal(1024)
+    x = host(G.solvetransposed(R, dev(b, dt)))
+    assert rel(Rd.T @ x, b) <= tol["solve"]
+    if dt == torch.float64:
+        assert rel(x, A.solvetransposed(A.cholesky(T), b)) <= tol["fwd"]
+    B = rng.standard_normal((1024, 5))
+    X = host(G.solvetransposed(R, dev(B, dt)))
+    assert rel(Rd.T @ X, B) <= tol["solve"]
+    L = rand_lr(rng, 1024, 64, 3)
+    XL = G.solvetransposed(R, lr_dev(L, dt))
+    assert rel(Rd.T @ host(XL.U), L.U) <= tol["solve"]
+    assert np.array_equal(host(XL.V), host(lr_dev(L, dt).V))
+
+
+def test_cholesky_errors():
+    T, _ = A.spd_hodlr(256, 32, seed=16)
+    T.blocks[1][1].blocks[1][1][0, 0] = -1.0
+    with pytest.raises(np.linalg.LinAlgError):
+        G.hierarchicalcholesky(tree_dev(T, torch.float64))
+    H3 = hm.HierarchicalMatrix(3, 3)
+    with pytest.raises(AssertionError):
+        G.hierarchicalcholesky(H3)
+    with pytest.raises(np.linalg.LinAlgError):
+        G.hierarchicalcholesky(dev(-np.eye(4), torch.float64))
