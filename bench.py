@@ -293,6 +293,89 @@ def run_batch(hm, torch, dev, args, count=512, nrhs=8):
 
 # ----------------------------------------------------------------- gradients
 
+def spd_hodlr_gauss(hm, torch, dev, n, leaf, ell=0.15, shift=1e-2, tol=1e-12, seed=21):
+    """A synthetic symmetric positive definite HierarchicalMatrix of the shape
+    src/cholesky.jl factors: K(x_i, x_j) = exp(-(x_i - x_j)^2 / (2 ell^2)) +
+    shift I on n sorted uniform points of [0, 1], halved recursively down to
+    dense diagonal leaves of at most `leaf` rows, each upper off-diagonal
+    block a LowRankMatrix (its singular values above tol times the largest,
+    found on the device by a randomized range finder with two power steps),
+    the lower block unassigned.  FP64, built on the device (setup, untimed)."""
+    g = torch.Generator(device=dev).manual_seed(seed)
+    x = torch.sort(torch.rand(n, generator=g, device=dev, dtype=torch.float64)).values
+
+    def kblock(i0, i1, j0, j1):
+        d = x[i0:i1, None] - x[None, j0:j1]
+        return torch.exp(-d * d / (2 * ell * ell))
+
+    def colmajor(t):
+        return t.t().contiguous().t()
+
+    def build(i0, i1):
+        if i1 - i0 <= leaf:
+            return colmajor(kblock(i0, i1, i0, i1) + shift * torch.eye(i1 - i0, dtype=torch.float64, device=dev))
+        mid = (i0 + i1) // 2
+        B = kblock(i0, mid, mid, i1)
+        k = min(96, B.shape[0], B.shape[1])
+        Q = torch.linalg.qr(B @ torch.randn(B.shape[1], k, generator=g, device=dev, dtype=torch.float64))[0]
+        for _ in range(2):
+            Q = torch.linalg.qr(B @ (B.t() @ Q))[0]
+        Uc, S, Vt = torch.linalg.svd(Q.t() @ B, full_matrices=False)
+        r = int((S > tol * S[0]).sum())
+        H = hm.HierarchicalMatrix(2, 2)
+        H[hm.Block(1), hm.Block(1)] = build(i0, mid)
+        H[hm.Block(1), hm.Block(2)] = hm.LowRankMatrix(colmajor(Q @ Uc[:, :r]), S[:r].contiguous(), colmajor(Vt[:r].t()))
+        H[hm.Block(2), hm.Block(2)] = build(mid, i1)
+        return H
+
+    return build(0, n)
+
+
+def tree_ranks(H):
+    """Largest rank of the LowRankMatrix blocks of a tree."""
+    best = 0
+    for b, _, _ in H.leaves():
+        if hasattr(b, "sigma"):
+            best = max(best, int(b.sigma.shape[0]))
+    return best
+
+
+def run_cholesky(hm, torch, dev, args, n=16384, leaf=64):
+    """hierarchicalcholesky (src/cholesky.jl:12-92) of a Gaussian-kernel SPD
+    HierarchicalMatrix, FP64, and one solvetransposed with the factor:
+    wall time per factorisation (the host recursion and every batched block
+    call included)."""
+    from hierarchicalmatrices import algebra
+    A = spd_hodlr_gauss(hm, torch, dev, n, leaf)
+    R = algebra.hierarchicalcholesky(A)              # warm-up: kernels, attributes
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        R = algebra.hierarchicalcholesky(A)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    b = torch.randn(n, device=dev, dtype=torch.float64)
+    algebra.solvetransposed(R, b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        xs = algebra.solvetransposed(R, b)
+    torch.cuda.synchronize()
+    solve_ms = (time.perf_counter() - t0) / reps * 1e3
+    # residual of the solve through the factor's own product: R'x = b  <=>  x . (R e_j) = b_j;
+    # checked on the dense factor for the leading 2048 x 2048 block (R is upper triangular)
+    m = 2048
+    Rd = algebra.todense(R)[:m, :m]
+    resid = float(torch.linalg.norm(Rd.t() @ xs[:m] - b[:m]) / torch.linalg.norm(b[:m]))
+    return {"workload": f"hierarchicalcholesky of K + 1e-2 I, K Gaussian exp(-(x-y)^2/(2*0.15^2)) on n={n} sorted "
+                        f"uniform points, leaf {leaf}, off-diagonal LowRankMatrix blocks at 1e-12, FP64; "
+                        "then solvetransposed of one vector",
+            "n": n, "ms_per_factorization": ms, "factorizations_per_s": 1e3 / ms, "solve_ms": solve_ms,
+            "max_rank_A": tree_ranks(A), "max_rank_R": tree_ranks(R), "solve_rel_residual_leading_2048": resid,
+            "reps": reps}
+
+
 def run_grad(hm, torch, dev, args, n=65536):
     """L = 1/2 |H(x,y) w - t|^2 for a Cauchy KernelMatrix on n uniform sorted
     points, FP32: loss and dL/dw, dL/dx, dL/dy (forward product, transposed

@@ -128,12 +128,13 @@ __device__ void apply_q(const T *A, int64_t m, int kk, const T *tau, T *y)
     }
 }
 
-// Shared memory of lr_svd: D (p x q core, ld p; d_elems values), then J
-// (q x q right rotations, before that the staging area of the Xm^T Ym
-// product), sigma (q) and the sort order (q ints).
+// Core storage of lr_svd: D (p x q core, ld p), then J (q x q right
+// rotations, before that the staging area of the Xm^T Ym product), sigma (q)
+// and the sort order (q ints).  In shared memory (D takes d_elems values)
+// when core_off < 0, else at ws + core_off for cores too large for it.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *probs, const int64_t *ws_off, T *ws,
-                                                          int *ranks, int64_t d_elems)
+__global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *probs, const int64_t *ws_off,
+                                                          const int64_t *core_off, T *ws, int *ranks, int64_t d_elems)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const hm_lr_problem pr = probs[blockIdx.x];
@@ -153,8 +154,9 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *p
     T *WQ = WP + (pr.qr_left ? m * a : 0);
     T *tauP = WQ + (pr.qr_right ? n * b : 0);
     T *tauQ = tauP + a;
-    T *D = reinterpret_cast<T *>(smem_raw);
-    T *J = D + d_elems;
+    const int64_t co = core_off[blockIdx.x];
+    T *D = co < 0 ? reinterpret_cast<T *>(smem_raw) : ws + co;
+    T *J = D + (co < 0 ? d_elems : (int64_t)p * q);
 
     // 1. orthonormalise the factors that the operation orthonormalises
     if (pr.qr_left) {
@@ -630,10 +632,13 @@ int set_smem(K kernel, size_t bytes)
     return HM_OK;
 }
 
+// Cores whose storage exceeds this many bytes run from the global workspace.
+constexpr size_t kCoreSmemBytes = 200 * 1024;
+
 template <typename T>
 int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream_t st)
 {
-    std::vector<int64_t> off(nprob);
+    std::vector<int64_t> off(nprob), coff(nprob, -1);
     int64_t ws = 0, dmax = 1, jmax = 1;
     int qmax = 1;
     for (int i = 0; i < nprob; ++i) {
@@ -663,8 +668,8 @@ int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream
         }
         const int64_t ka = p.qr_left ? std::min<int64_t>(p.m, a) : a;
         const int64_t kb = p.qr_right ? std::min<int64_t>(p.n, b) : b;
-        if (ka > HM_LR_KMAX || kb > HM_LR_KMAX || (p.Xm && (a > HM_LR_KMAX || b > HM_LR_KMAX))) {
-            set_last_error("problem %d: core %lld x %lld exceeds %d", i, (long long)ka, (long long)kb, HM_LR_KMAX);
+        if (ka > 4096 || kb > 4096 || (p.Xm && (a > 4096 || b > 4096))) {
+            set_last_error("problem %d: core %lld x %lld exceeds 4096", i, (long long)ka, (long long)kb);
             return HM_ERR_UNSUPPORTED;
         }
         const int64_t q = std::min(ka, kb), pp = std::max(ka, kb);
@@ -672,9 +677,17 @@ int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream
         off[i] = ws;
         ws += (p.qr_left ? p.m * a : 0) + (p.qr_right ? p.n * b : 0) + a + b;
         ws = (ws + 31) / 32 * 32;
-        dmax = std::max(dmax, pp * q);
-        jmax = std::max(jmax, std::max(q * q, p.Xm ? (int64_t)32 * (a + b) : 0));
-        qmax = std::max<int>(qmax, (int)q);
+        const int64_t jn = std::max(q * q, p.Xm ? (int64_t)32 * (a + b) : 0);
+        const size_t need = (size_t)(pp * q + jn + q) * sizeof(T) + (size_t)q * sizeof(int) + 64;
+        if (need <= kCoreSmemBytes) {
+            dmax = std::max(dmax, pp * q);
+            jmax = std::max(jmax, jn);
+            qmax = std::max<int>(qmax, (int)q);
+        } else {
+            coff[i] = ws;
+            ws += pp * q + jn + 2 * q;          // sigma (q values) and the order (q ints) after J
+            ws = (ws + 31) / 32 * 32;
+        }
     }
     if (nprob == 0) return HM_OK;
     // J also holds sigma (q values) and the sort order (q ints) after it
@@ -682,14 +695,15 @@ int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream
     ALG_TRY(set_smem(lr_svd_kernel<T>, smem));
     Staged S(st);
     hm_lr_problem *d_probs = nullptr;
-    int64_t *d_off = nullptr;
+    int64_t *d_off = nullptr, *d_coff = nullptr;
     T *d_ws = nullptr;
     int *d_ranks = nullptr;
     ALG_TRY(S.put(probs, (size_t)nprob, &d_probs));
     ALG_TRY(S.put(off.data(), off.size(), &d_off));
+    ALG_TRY(S.put(coff.data(), coff.size(), &d_coff));
     ALG_TRY(S.zeros((size_t)std::max<int64_t>(ws, 1), &d_ws));
     ALG_TRY(S.zeros((size_t)nprob, &d_ranks));
-    lr_svd_kernel<T><<<nprob, kThreads, smem, st>>>(d_probs, d_off, d_ws, d_ranks, dmax);
+    lr_svd_kernel<T><<<nprob, kThreads, smem, st>>>(d_probs, d_off, d_coff, d_ws, d_ranks, dmax);
     ALG_CK(cudaGetLastError());
     std::vector<int> hr(nprob);
     ALG_CK(cudaMemcpyAsync(hr.data(), d_ranks, nprob * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -246,10 +246,10 @@ def lrzeros(dtype, m, n):
 
 def svdtrunc(A):
     """svdtrunc(A) (src/LowRankMatrix.jl:82-86): the SVD of a dense matrix
-    truncated by getrank (min(size(A)) <= HM_LR_KMAX)."""
+    truncated by getrank (min(size(A)) <= 4096)."""
     A = _dev(A)
     m, n = A.shape
-    if n > _lib.HM_LR_KMAX and m <= _lib.HM_LR_KMAX:
+    if n > m:
         L = svdtrunc(_dev(A.t().contiguous()))          # svd(A') = V S U'
         return LowRankMatrix(L.V, L.sigma, L.U)
     torch = _torch()

@@ -298,8 +298,9 @@ void hm_plan_free(hm_plan *p);
    used as given (the L1*L2 and L1'*L2 forms).  Q1 == NULL stands for the
    identity (n == b1, b2 == 0, qr_right == 0: svdtrunc of a dense P).
    The core (R_P M R_Q^T, or M) is ka x kb with ka = qr_left ? min(m, a) : a
-   and kb likewise; its singular values are q = min(ka, kb), at most
-   HM_LR_KMAX of each of ka, kb.  Outputs: U (m x q, ld m), s (q) and V
+   and kb likewise; its singular values are q = min(ka, kb).  Cores up to
+   about HM_LR_KMAX x HM_LR_KMAX are factored in shared memory, larger ones
+   (up to 4096 x 4096) from a global-memory workspace.  Outputs: U (m x q, ld m), s (q) and V
    (n x q, ld n) receive the first r columns / values in descending order,
    r = getrank(sigma) = #{sigma_j > q * eps(sigma_1)} (src/LowRankMatrix.jl:70-80). */
 #define HM_LR_KMAX 96

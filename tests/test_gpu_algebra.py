@@ -72,10 +72,11 @@ def rand_lr(rng, m, n, r, decay=0.5):
 
 
 def check_svd_form(L, dt):
-    """Descending non-negative singular values and orthonormal factors."""
+    """Descending non-negative singular values and orthonormal factors (to
+    about q eps: rotations accumulate rounding in proportion to the width)."""
     s = host(L.sigma)
     assert np.all(np.diff(s) <= 0) and np.all(s >= 0)
-    tol = 1e-12 if dt == torch.float64 else 1e-5
+    tol = 1e-12 if dt == torch.float64 else 4 * max(len(s), 20) * 1.19e-7
     for F in (host(L.U), host(L.V)):
         assert np.abs(F.T @ F - np.eye(F.shape[1])).max() < tol
 
@@ -105,6 +106,12 @@ def test_lowrank_operations(dt):
         check_svd_form(got, dt)
         assert got.rank() == len(ref.s)
         assert rel(A.lr_dense(lr_host(got)), A.lr_dense(ref)) <= TOL[dt]
+    # a 120 x 120 core: global-memory Jacobi in FP64 (shared memory in FP32)
+    L5, L6 = rand_lr(rng, 400, 300, 60, 0.9), rand_lr(rng, 400, 300, 60, 0.9)
+    got, ref = G.lr_add(lr_dev(L5, dt), lr_dev(L6, dt)), A.lr_add(L5, L6)
+    check_svd_form(got, dt)
+    assert got.rank() == len(ref.s) == 120
+    assert rel(A.lr_dense(lr_host(got)), A.lr_dense(ref)) <= TOL[dt]
     Z = G.lr_sub(g1, g1)                        # rank-deficient: ranks may differ, the matrix is ~0
     assert np.linalg.norm(A.lr_dense(lr_host(Z))) <= TOL[dt] * np.linalg.norm(A.lr_dense(L1))
     S = G.times(2.5, g1)
@@ -177,8 +184,8 @@ def test_hierarchical_cholesky(dt, kernel, dense_below):
 
 
 def test_cholesky_errors():
-    T, _ = A.spd_hodlr(256, 32, seed=16)
-    T.blocks[1][1].blocks[1][1][0, 0] = -1.0
+    T, _ = A.spd_hodlr(128, 32, seed=16)
+    T.blocks[1][1].blocks[1][1][0, 0] = -1.0          # the last 32 x 32 diagonal leaf
     with pytest.raises(np.linalg.LinAlgError):
         G.hierarchicalcholesky(tree_dev(T, torch.float64))
     H3 = hm.HierarchicalMatrix(3, 3)
