@@ -179,13 +179,6 @@ struct hm_handle {
     int part_segs[2] = {0, 0};      // most segments of one CTA (near / far)
     int part_pieces[2] = {0, 0};    // most piece records of one CTA
     int *d_status = nullptr;        // device-side status word (HM_DEV_*), 0 when clean
-    // hm_mul_noalloc: coefficient scratch reserved at build time; the event
-    // marks the end of the last call, which the next call on another stream
-    // waits for (outside stream capture)
-    void *d_noalloc = nullptr;
-    cudaEvent_t noalloc_done = nullptr;
-    bool noalloc_recorded = false;
-    std::mutex noalloc_mu;
     bool tc_ok = false;             // segments fit the tensor-core panel kernel
     bool tensor_cores = true;       // use it for FP32 products with many right-hand sides
 
@@ -872,19 +865,35 @@ int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y
 // another allocator (a framework memory pool that takes most of HBM at
 // start-up), and loops that must not call cudaMalloc/cudaFree after
 // initialisation because those calls can synchronise the device and take an
-// unbounded time.  hm_mul_noalloc serves them from coefficient scratch that
-// every handle reserves when it is built.
-template <typename A>
-int reserve_noalloc(hm_handle *h)
-{
-    HM_TRY(h->alloc(reinterpret_cast<unsigned char **>(&h->d_noalloc), scratch_layout<A>(h, 1).bytes + 256));
-    HM_CK(cudaEventCreateWithFlags(&h->noalloc_done, cudaEventDisableTiming));
-    return HM_OK;
-}
+// unbounded time.  hm_mul_noalloc serves them: its coefficient scratch is this
+// file-scope device array, sized at compile time and held by every GPU that
+// loads the library until the process exits.  All calls share it.
+#define HM_NOALLOC_SCRATCH_BYTES (16u << 20)
+static __device__ __align__(256) unsigned char hm_noalloc_scratch[HM_NOALLOC_SCRATCH_BYTES];
 
-int reserve_noalloc(hm_handle *h)
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[256];   // device address of hm_noalloc_scratch, per device ordinal
+
+// In host code `hm_noalloc_scratch` names a host-side stand-in, not device
+// memory: the device address is looked up once per device, with that device
+// current, and cached.
+int noalloc_scratch(void **out)
 {
-    return h->storage == HM_F64 ? reserve_noalloc<double>(h) : reserve_noalloc<float>(h);
+    int dev = -1;
+    HM_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) { set_error("device ordinal %d out of range", dev); return HM_ERR_UNSUPPORTED; }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, hm_noalloc_scratch);
+        if (e != cudaSuccess) {
+            set_error("cudaGetSymbolAddress(hm_noalloc_scratch): %s", cudaGetErrorString(e));
+            return HM_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return HM_OK;
 }
 
 }  // namespace
@@ -1146,7 +1155,6 @@ int build_from_plan(int kernel, int swap, hm_plan *pl, const double *x, const do
     };
     h->launches_per_mul = (h->n_vp > 0) + nonempty(h->up_band_ptr) + (h->n_m2l_rows > 0) + nonempty(h->down_band_ptr) +
                           (h->n_segs > 0) * (1 + 2 * ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
-    if (!st) st = reserve_noalloc(h);
     if (st) { hm_free(h); return st; }
     *out = h;
     return HM_OK;
@@ -1226,8 +1234,7 @@ int hm_hier_build(int storage, int64_t m, int64_t n, int nblocks, const int32_t 
                                      : build_hier_device<float>(h, P, vs, fs, ps, cs);
     h->launches_per_mul = (h->n_vp > 0) + (h->n_m2l_rows > 0) +
                           (h->n_segs > 0) * (1 + 2 * ((h->n_vp > 0) || (h->n_m2l_rows > 0)));
-    int rc = st ? st : reserve_noalloc(h);
-    if (rc) { hm_free(h); return rc; }
+    if (st) { hm_free(h); return st; }
     *out = h;
     return HM_OK;
 }
@@ -1528,29 +1535,24 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
 {
     g_last_error.clear();
     if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
-    if (!h->d_noalloc) { set_error("hm_mul_noalloc: handle has no reserved scratch"); return HM_ERR_INVALID_ARG; }
+    const size_t need = h->storage == HM_F64 ? scratch_layout<double>(h, 1).bytes : scratch_layout<float>(h, 1).bytes;
+    if (need > HM_NOALLOC_SCRATCH_BYTES) {
+        set_error("hm_mul_noalloc: this matrix needs %zu bytes of coefficient scratch; the library's fixed "
+                  "scratch holds %u bytes (use hm_mul)", need, (unsigned)HM_NOALLOC_SCRATCH_BYTES);
+        return HM_ERR_UNSUPPORTED;
+    }
+    void *scratch = nullptr;
+    HM_TRY(noalloc_scratch(&scratch));
+    // every stage runs in order on the caller's stream: no side stream, no event
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    HM_CK(cudaStreamIsCapturing(st, &cap));
-    // one scratch per handle: calls on different streams run one after another
-    std::lock_guard<std::mutex> lk(h->noalloc_mu);
-    if (cap == cudaStreamCaptureStatusNone && h->noalloc_recorded) HM_CK(cudaStreamWaitEvent(st, h->noalloc_done, 0));
-    int rc;
     if (h->storage == HM_F64) {
         MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, h->ny, 1, h->nx, 1,
                            accumulate ? 1 : 0};
-        rc = launch_pipeline<double, double>(h, ma, st, st, nullptr, nullptr, h->d_noalloc, false);
-    } else {
-        MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, h->ny, 1, h->nx, 1,
-                          accumulate ? 1 : 0};
-        rc = launch_pipeline<float, float>(h, ma, st, st, nullptr, nullptr, h->d_noalloc, false);
+        return launch_pipeline<double, double>(h, ma, st, st, nullptr, nullptr, scratch, false);
     }
-    if (rc) return rc;
-    if (cap == cudaStreamCaptureStatusNone) {
-        HM_CK(cudaEventRecord(h->noalloc_done, st));
-        h->noalloc_recorded = true;
-    }
-    return HM_OK;
+    MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, h->ny, 1, h->nx, 1,
+                      accumulate ? 1 : 0};
+    return launch_pipeline<float, float>(h, ma, st, st, nullptr, nullptr, scratch, false);
 }
 
 int hm_configure(hm_handle *h, int option, int64_t value)
@@ -1625,7 +1627,6 @@ void hm_free(hm_handle *h)
     for (auto &e : h->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     if (h->d_stage) cudaFree(h->d_stage);
     if (h->host_stream) cudaStreamDestroy(h->host_stream);
-    if (h->noalloc_done) cudaEventDestroy(h->noalloc_done);
     for (void *p : h->allocs) cudaFree(p);
     delete h;
 }

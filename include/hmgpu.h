@@ -225,20 +225,27 @@ enum {
 };
 int hm_configure(hm_handle *h, int option, int64_t value);
 
-/* Allocation-free single right-hand-side product (no counterpart in the
-   reference).  For callers that cannot let a library allocate device memory
-   during a product: processes whose GPU memory is reserved up front by
-   another allocator, and loops that must not call cudaMalloc/cudaFree after
-   start-up because those calls can synchronise the device.
+/* Allocation-free single right-hand-side product.  No counterpart in the
+   reference: it is an addition for callers that cannot let a library
+   allocate device memory while they run — processes whose GPU memory is
+   claimed up front by another allocator (a framework memory pool), and
+   loops that must not call cudaMalloc/cudaFree after start-up because those
+   calls can synchronise the whole device.
      u (+)= H v   (accumulate = 1 adds, as the reference's mul!; 0 overwrites)
-   u, v: DEVICE vectors of the handle's storage type (lengths nx, ny).
-   The coefficient scratch ((n_xslots + n_yslots) * rank elements of the
-   storage type) is reserved when the handle is built and freed by hm_free;
-   the call makes no cudaMalloc/cudaFree.  Calls on one handle from different
-   streams are ordered on the GPU (each waits for the previous call's end
-   through an event); inside stream capture that ordering is not recorded,
-   so replays of a captured call must not overlap other calls on the same
-   handle.  Different handles never share scratch. */
+   u, v: DEVICE vectors of the handle's storage type (lengths nx, ny); all
+   stages run in order on `stream`.
+   Scratch: a 16 MiB array compiled into the library (a file-scope __device__
+   array, held by every GPU that loads the library until the process exits).
+   A matrix whose coefficients need more, (n_yslots + n_xslots) * rank
+   elements with each part rounded up to 256 bytes, is rejected with
+   HM_ERR_UNSUPPORTED (hm_mul has no such limit).  Each call writes every
+   coefficient before reading it, so nothing has to start at zero, but all
+   calls share the one array: calls that overlap on the GPU (other streams,
+   or other handles, at the same time) race and give wrong results.
+   The first call on each device looks up the array's device address with
+   cudaGetSymbolAddress (that device current) and caches it; make that first
+   call before any stream capture.  The call makes no cudaMalloc, cudaFree or
+   other allocating call. */
 int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *stream);
 
 /* Per-stage timing of hm_mul (the reference prints @time per call,
