@@ -36,6 +36,20 @@ def grid_points(n):
     return x, y
 
 
+def beta_points(n, seed, min_gap=1e-9):
+    """x, y i.i.d. Beta(1/2, 1/2) on [0, 1] (clustered at both ends), sorted,
+    consecutive gaps raised to at least min_gap, returned descending."""
+    rng = np.random.default_rng(seed)
+    out = []
+    steps = np.arange(n, dtype=np.float64) * min_gap
+    for _ in range(2):
+        p = np.sort(rng.beta(0.5, 0.5, n))
+        # p'_i = max(p_i, p'_{i-1} + g)  <=>  p'_i - i g = running max of p_j - j g
+        p = np.maximum.accumulate(p - steps) + steps
+        out.append(p[::-1].copy())
+    return out[0], out[1]
+
+
 def profiled_traffic(n):
     """DRAM bytes (read + write) per launch of the near-field kernel from the
     committed ncu summary of the n = 2^20 workload, or None."""
@@ -506,6 +520,23 @@ def main():
             "build_s": build64_s, "stage_ms_serial": st64s}
         del H64, u64
         torch.cuda.empty_cache()
+        # clustered points: Beta(1/2, 1/2), FP64 (a deeper, uneven tree)
+        xb, yb = beta_points(n, 21)
+        hi = float(max(xb[0], yb[0], 1.0))
+        t0 = time.perf_counter()
+        Hb = hm.KernelMatrix(hm.cauchykernel, xb, yb, hi, 0.0, hi, 0.0, dtype=np.float64)
+        torch.cuda.synchronize()
+        buildb_s = time.perf_counter() - t0
+        ub = torch.empty(n, device=dev, dtype=torch.float64)
+        msb = time_device(lambda: Hb.mul(ub, b64, accumulate=False), k_steps, 3, torch)
+        stb = Hb.stats()
+        variants["fp64_k1_beta"] = {
+            "points": "x, y i.i.d. Beta(1/2,1/2) sorted, min gap 1e-9, seed 21",
+            "matvec_per_s": 1e3 / msb, "ms": msb, "rel_err_vs_dense_fp64": rel_err_sampled(Hb, ub, b64, rows, torch),
+            "stored_GBs": (stb["stored_values"] * 8 + 2 * n * 8) / (msb * 1e-3) / 1e9,
+            "build_s": buildb_s, "depth": stb["depth"], "n_bary": stb["n_bary"], "n_dense": stb["n_dense"]}
+        del Hb, ub
+        torch.cuda.empty_cache()
         for k in (32, 256):
             B = torch.randn(k, n, device=dev, dtype=torch.float32).t()    # column-major n x k
             U = torch.empty(k, n, device=dev, dtype=torch.float32).t()
@@ -524,8 +555,10 @@ def main():
     if not args.no_variants and not args.no_batch:
         batch = run_batch(hm, torch, dev, args)
     grad = None
+    chol = None
     if not args.no_variants:
         grad = run_grad(hm, torch, dev, args)
+        chol = run_cholesky(hm, torch, dev, args)
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -569,6 +602,7 @@ def main():
             "variants": variants,
             "batch": batch,
             "grad": grad,
+            "cholesky": chol,
             "cpu_baseline": cb,
         }
         print(json.dumps(line), flush=True)
