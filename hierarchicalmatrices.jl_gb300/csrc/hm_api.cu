@@ -127,6 +127,21 @@ void transfer_matrices(int r, const std::vector<double> &x, const std::vector<do
     }
 }
 
+// The options one product runs with (hm_configure's HM_OPT_* values).
+struct Sched {
+    int overlap, near_kernel, near_stages, tensor_cores;
+};
+
+// Right-hand-side buckets of the autotuned schedules: 1, 2, 3-4, 5-8, 9-16,
+// 17-32, 33-64, 65-128, 129 and more.
+constexpr int kSchedBuckets = 9;
+inline int sched_bucket(int k)
+{
+    int b = 0;
+    while (b + 1 < kSchedBuckets && (1 << b) < k) ++b;
+    return b;
+}
+
 }  // namespace
 
 struct hm_handle {
@@ -222,6 +237,10 @@ struct hm_handle {
     int overlap = 2;
     int near_stages = 4;            // ring stages of the near-field streaming kernel
     int near_kernel = 0;            // 0 default (one warp per segment), 1 the same, 2 streamed CTAs
+    // hm_autotune's choice per right-hand-side bucket; a product whose bucket
+    // has one runs with it instead of the options above
+    Sched tuned[kSchedBuckets] = {};
+    bool tuned_ok[kSchedBuckets] = {};
 
     template <typename T>
     int alloc(T **p, size_t count)
@@ -548,6 +567,28 @@ int stream_ctx(hm_handle *h, cudaStream_t st, size_t bytes, hm_handle::StreamCtx
     return HM_OK;
 }
 
+// The schedule of the product being issued by this host thread: set by
+// run_mul (and hm_autotune) for the duration of one product's launches;
+// launches issued outside them read the handle's configured options.
+thread_local const Sched *t_sched = nullptr;
+
+inline Sched configured_sched(const hm_handle *h)
+{
+    return Sched{h->overlap, h->near_kernel, h->near_stages, h->tensor_cores ? 1 : 0};
+}
+inline Sched cur_sched(const hm_handle *h) { return t_sched ? *t_sched : configured_sched(h); }
+inline Sched sched_for(const hm_handle *h, int k)
+{
+    if (t_sched) return *t_sched;
+    const int b = sched_bucket(k);
+    return h->tuned_ok[b] ? h->tuned[b] : configured_sched(h);
+}
+struct SchedScope {
+    const Sched *prev;
+    explicit SchedScope(const Sched *s) : prev(t_sched) { t_sched = s; }
+    ~SchedScope() { t_sched = prev; }
+};
+
 constexpr int kWarpsPerCta = 4;
 constexpr int kPartMaxK = 8;    // right-hand sides handled by the streaming panel kernels
 
@@ -671,13 +712,14 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
     // copy peak) and keeps its lead on short segments and more right-hand
     // sides; the streamed form reaches 5.7 TB/s alone and overlaps the tree
     // passes no better
-    if (!FAR && h->stream_ctas > 0 && h->near_kernel == 2) {
+    const Sched sc = cur_sched(h);
+    if (!FAR && h->stream_ctas > 0 && sc.near_kernel == 2) {
         const int part = FAR ? 1 : 0;
         const int gcap = std::max(h->part_width[part], 1);
         // the configured stages, right-hand sides gathered three segments
         // ahead; fewer of either until two CTAs fit on an SM
         const size_t smax = KB < 4 ? kStreamSmemMax3 : sizeof(S) == 4 ? kStreamSmemMax2 : kStreamSmemMax1;
-        int nst = h->near_stages, ngb = 4;
+        int nst = sc.near_stages, ngb = 4;
         size_t smem = 0;
         for (;;) {
             smem = stream_smem_bytes(nst, gcap, ngb, KB, (int)sizeof(A), h->part_segs[part], h->part_pieces[part]);
@@ -715,7 +757,7 @@ int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, cons
     // with a TwoSum fold every 64 columns issues less than per-element
     // TwoProd/TwoSum); FP64 (plain FMA either way, on the scarce FP64 pipe) and
     // the streamed kernel keep the one-column form
-    if (ma.k == 1 && (sizeof(A) == 8 || (!FAR && h->stream_ctas > 0 && h->near_kernel == 2)))
+    if (ma.k == 1 && (sizeof(A) == 8 || (!FAR && h->stream_ctas > 0 && cur_sched(h).near_kernel == 2)))
         return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st);
     if (ma.k <= 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st);
     if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, yfar, st);
@@ -728,7 +770,7 @@ template <typename S, typename A>
 int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
 {
     if constexpr (sizeof(S) == 4 && sizeof(A) == 4) {
-        if (h->tensor_cores && h->tc_ok && ma.k >= kTensorCoreMinK) {
+        if (cur_sched(h).tensor_cores && h->tc_ok && ma.k >= kTensorCoreMinK) {
             const int maxw = std::max(h->max_width, 1);
             const size_t smem = expand_tc_smem_bytes(maxw);
             HM_TRY(ensure_smem(expand_tc, smem));
@@ -772,7 +814,7 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
             HM_CK(cudaStreamWaitEvent(side, fork, 0));
         }
         HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing, split ? mid : nullptr,
-                                  h->overlap == 3 ? 1 : h->overlap == 4 ? 2 : 0)));
+                                  cur_sched(h).overlap == 3 ? 1 : cur_sched(h).overlap == 4 ? 2 : 0)));
         if (split && (k > kPartMaxK || !h->n_segs)) HM_CK(cudaEventRecord(join, side));
     }
     if (!h->n_segs) {
@@ -820,10 +862,12 @@ template <typename S, typename A>
 int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st, const void *panels = nullptr)
 {
     if (ma.k <= 0) return HM_OK;
+    const Sched sched = sched_for(h, ma.k);
+    SchedScope scope(&sched);
     hm_handle::StreamCtx *sc = nullptr;
     HM_TRY(stream_ctx(h, st, stream_scratch_bytes<A>(h, ma.k), &sc));
-    return launch_pipeline<S, A>(h, ma, st, h->overlap ? sc->side : st, sc->fork, sc->join, sc->p, true, panels,
-                                 h->overlap >= 2 ? sc->mid : nullptr);
+    return launch_pipeline<S, A>(h, ma, st, sched.overlap ? sc->side : st, sc->fork, sc->join, sc->p, true, panels,
+                                 sched.overlap >= 2 ? sc->mid : nullptr);
 }
 
 // Row-derivative panels (same layout as the panels), filled once.
@@ -856,6 +900,115 @@ int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y
     }
     MulArgs<float> ma{static_cast<const float *>(x), static_cast<float *>(y), incx, ldx, incy, ldy, k, accumulate};
     return run_mul<float, float>(h, ma, st);
+}
+
+// ---- autotuned schedules ----------------------------------------------------
+//
+// The fastest options for a product differ with the number of right-hand
+// sides and with the tree: when the near field should start beside the tree
+// passes (it shares HBM with the leaf stage and the far field), whether the
+// warp-per-segment or the streamed near-field kernel wins (segment lengths),
+// its ring depth, and whether FP32 panels with many right-hand sides run
+// faster on the tensor cores or on the FP32 pipes.  hm_autotune times every
+// candidate on the caller's stream and keeps the fastest for the call's
+// right-hand-side bucket.
+
+void drop_host_graph(hm_handle *h)
+{
+    if (h->host_graph.exec) {
+        cudaStreamSynchronize(h->host_stream);
+        cudaGraphExecDestroy(h->host_graph.exec);
+    }
+    h->host_graph = hm_handle::HostGraph();
+}
+
+std::vector<Sched> sched_candidates(const hm_handle *h, int k, bool fp32)
+{
+    const Sched base = configured_sched(h);
+    const bool tree = h->n_vp || h->n_m2l_rows;
+    std::vector<int> overlaps = !tree ? std::vector<int>{base.overlap}
+                                      : k <= kPartMaxK ? std::vector<int>{0, 1, 2, 3, 4} : std::vector<int>{0, 1};
+    std::vector<int> kernels = (k <= kPartMaxK && h->stream_ctas > 0 && h->n_segs) ? std::vector<int>{0, 2}
+                                                                                    : std::vector<int>{base.near_kernel};
+    std::vector<int> tcs = (fp32 && h->tc_ok && k >= kTensorCoreMinK) ? std::vector<int>{1, 0}
+                                                                       : std::vector<int>{base.tensor_cores};
+    std::vector<Sched> c{base};       // the configured schedule first, timed for comparison
+    auto add = [&c](Sched s) {
+        for (const Sched &o : c)
+            if (o.overlap == s.overlap && o.near_kernel == s.near_kernel && o.near_stages == s.near_stages &&
+                o.tensor_cores == s.tensor_cores)
+                return;
+        c.push_back(s);
+    };
+    for (int ov : overlaps)
+        for (int nk : kernels)
+            for (int tc : tcs) {
+                if (nk == 2)
+                    for (int ns : {3, 4, 6}) add(Sched{ov, nk, ns, tc});
+                else
+                    add(Sched{ov, nk, base.near_stages, tc});
+            }
+    return c;
+}
+
+template <typename S>
+int autotune(hm_handle *h, int k, int reps, cudaStream_t st, int32_t *choice, double *ms_out)
+{
+    const std::vector<Sched> cand = sched_candidates(h, k, sizeof(S) == 4);
+    const size_t nv = (size_t)h->ny * k, nu = (size_t)h->nx * k;
+    S *v = nullptr, *u = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = cuda_status(cudaMallocAsync(&v, std::max<size_t>(nv, 1) * sizeof(S), st), "cudaMallocAsync");
+    if (!rc) rc = cuda_status(cudaMallocAsync(&u, std::max<size_t>(nu, 1) * sizeof(S), st), "cudaMallocAsync");
+    // finite, normal inputs (0x3f bytes); the kernels' time does not depend on the values
+    if (!rc) rc = cuda_status(cudaMemsetAsync(v, 0x3f, nv * sizeof(S), st), "cudaMemsetAsync");
+    if (!rc) rc = cuda_status(cudaEventCreate(&e0), "cudaEventCreate");
+    if (!rc) rc = cuda_status(cudaEventCreate(&e1), "cudaEventCreate");
+    std::vector<double> best(cand.size(), 1e300);
+    const MulArgs<S> ma{v, u, 1, h->ny, 1, h->nx, k, 0};
+    // two rounds over the candidates, the better time of each kept, so that a
+    // clock ramp at the start favours none of them
+    for (int round = 0; round < 2 && !rc; ++round) {
+        for (size_t c = 0; c < cand.size() && !rc; ++c) {
+            SchedScope scope(&cand[c]);
+            for (int w = 0; w < 2 && !rc; ++w) rc = run_mul<S, S>(h, ma, st);
+            if (!rc) rc = cuda_status(cudaEventRecord(e0, st), "cudaEventRecord");
+            for (int i = 0; i < reps && !rc; ++i) rc = run_mul<S, S>(h, ma, st);
+            if (!rc) rc = cuda_status(cudaEventRecord(e1, st), "cudaEventRecord");
+            if (!rc) rc = cuda_status(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            float t = 0.f;
+            if (!rc) rc = cuda_status(cudaEventElapsedTime(&t, e0, e1), "cudaEventElapsedTime");
+            if (!rc) best[c] = std::min(best[c], (double)t / reps);
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (v) cudaFreeAsync(v, st);
+    if (u) cudaFreeAsync(u, st);
+    const int rs = cuda_status(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (rc) return rc;
+    if (rs) return rs;
+    size_t bi = 0;
+    for (size_t c = 1; c < cand.size(); ++c)
+        if (best[c] < best[bi]) bi = c;
+    const int b = sched_bucket(k);
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        h->tuned[b] = cand[bi];
+        h->tuned_ok[b] = true;
+    }
+    drop_host_graph(h);             // it was captured with the previous schedule
+    if (choice) {
+        choice[0] = cand[bi].overlap;
+        choice[1] = cand[bi].near_kernel;
+        choice[2] = cand[bi].near_stages;
+        choice[3] = cand[bi].tensor_cores;
+    }
+    if (ms_out) {
+        ms_out[0] = best[bi];
+        ms_out[1] = best[0];
+    }
+    return HM_OK;
 }
 
 // ---- allocation-free single right-hand-side product ------------------------
@@ -1555,31 +1708,55 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
     return launch_pipeline<float, float>(h, ma, st, st, nullptr, nullptr, scratch, false);
 }
 
+int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice, double *ms)
+{
+    g_last_error.clear();
+    if (!h || nrhs <= 0 || reps <= 0) { set_error("hm_autotune: bad argument"); return HM_ERR_INVALID_ARG; }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    HM_CK(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+        set_error("hm_autotune: not allowed while the stream is being captured");
+        return HM_ERR_INVALID_ARG;
+    }
+    return h->storage == HM_F64 ? autotune<double>(h, nrhs, reps, st, choice, ms)
+                                : autotune<float>(h, nrhs, reps, st, choice, ms);
+}
+
 int hm_configure(hm_handle *h, int option, int64_t value)
 {
     if (!h) return HM_ERR_INVALID_ARG;
-    // the host-buffer product's captured graph follows the options: drop it
-    if (h->host_graph.exec) {
-        cudaStreamSynchronize(h->host_stream);
-        cudaGraphExecDestroy(h->host_graph.exec);
-    }
-    h->host_graph = hm_handle::HostGraph();
     switch (option) {
     case HM_OPT_OVERLAP:
         if (value < 0 || value > 4) { set_error("HM_OPT_OVERLAP must be in [0, 4]"); return HM_ERR_INVALID_ARG; }
-        h->overlap = (int)value;
-        return HM_OK;
-    case HM_OPT_TENSOR_CORES: h->tensor_cores = value != 0; return HM_OK;
+        break;
+    case HM_OPT_TENSOR_CORES: break;
     case HM_OPT_NEAR_KERNEL:
         if (value < 0 || value > 2) { set_error("HM_OPT_NEAR_KERNEL must be 0, 1 or 2"); return HM_ERR_INVALID_ARG; }
-        h->near_kernel = (int)value;
-        return HM_OK;
+        break;
     case HM_OPT_NEAR_STAGES:
         if (value < 2 || value > 16) { set_error("HM_OPT_NEAR_STAGES must be in [2, 16]"); return HM_ERR_INVALID_ARG; }
-        h->near_stages = (int)value;
-        return HM_OK;
+        break;
+    case HM_OPT_AUTOTUNED:
+        if (value != 0) { set_error("HM_OPT_AUTOTUNED takes 0 (forget the tuned schedules)"); return HM_ERR_INVALID_ARG; }
+        break;
     default: set_error("unknown option %d", option); return HM_ERR_INVALID_ARG;
     }
+    // the host-buffer product's captured graph follows the options: drop it;
+    // an explicit option also replaces the autotuned schedules
+    drop_host_graph(h);
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        for (bool &ok : h->tuned_ok) ok = false;
+    }
+    switch (option) {
+    case HM_OPT_OVERLAP: h->overlap = (int)value; break;
+    case HM_OPT_TENSOR_CORES: h->tensor_cores = value != 0; break;
+    case HM_OPT_NEAR_KERNEL: h->near_kernel = (int)value; break;
+    case HM_OPT_NEAR_STAGES: h->near_stages = (int)value; break;
+    default: break;
+    }
+    return HM_OK;
 }
 
 int hm_profile(hm_handle *h, int stage_mask)

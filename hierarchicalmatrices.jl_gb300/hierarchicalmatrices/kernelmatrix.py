@@ -302,6 +302,22 @@ class KernelMatrix:
         """Shared-memory stages (8 KB each) of the near-field streaming kernel."""
         check(lib.hm_configure(self._h, _lib.HM_OPT_NEAR_STAGES, int(n)))
 
+    def autotune(self, nrhs=1, reps=20, *, stream=None):
+        """Time every candidate schedule of a product with ``nrhs`` right-hand
+        sides (stream placement of the near field, near-field kernel and ring
+        depth, tensor cores) and keep the fastest for that right-hand-side
+        bucket.  Returns the choice and the time per product of it and of the
+        configured options."""
+        choice = (ctypes.c_int32 * 4)()
+        ms = (ctypes.c_double * 2)()
+        check(lib.hm_autotune(self._h, int(nrhs), int(reps), _stream_ptr(stream), choice, ms))
+        return {"overlap": choice[0], "near_kernel": choice[1], "near_stages": choice[2],
+                "tensor_cores": bool(choice[3]), "ms": ms[0], "ms_configured": ms[1]}
+
+    def forget_autotune(self):
+        """Drop the autotuned schedules: products run with the configured options."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_AUTOTUNED, 0))
+
     def profile(self, stages=_lib.STAGES):
         """Record CUDA events around the launches of the named matvec stages
         (see stage_times); an empty list turns timing off."""

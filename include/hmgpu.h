@@ -221,9 +221,30 @@ enum {
     /* HM_OPT_NEAR_KERNEL (default 0): near-field panels with up to 8
        right-hand sides on 0 or 1 = one warp per row segment, 2 = CTAs
        streaming runs of segments through shared memory (cp.async.bulk). */
-    HM_OPT_NEAR_KERNEL = 4
+    HM_OPT_NEAR_KERNEL = 4,
+    /* HM_OPT_AUTOTUNED: value 0 forgets the schedules hm_autotune chose, so
+       every product runs with the options above again.  Setting any other
+       option forgets them too. */
+    HM_OPT_AUTOTUNED = 5
 };
 int hm_configure(hm_handle *h, int option, int64_t value);
+
+/* Autotuner (no counterpart in the reference, which has one serial loop).
+   Times every candidate schedule of a product with nrhs right-hand sides
+   on `stream` (reps products each, CUDA events, after two warm-up products,
+   two rounds with the better time kept) and keeps the fastest for nrhs's
+   bucket (1, 2, 3-4, 5-8, 9-16, 17-32, 33-64, 65-128, 129+): later hm_mul,
+   hm_mul_strided, hm_mul_host and hm_mul_drow calls of that bucket run with
+   it, including inside stream capture.  Candidates: HM_OPT_OVERLAP 0..4
+   (0..1 above 8 right-hand sides), HM_OPT_NEAR_KERNEL 0 or 2 with
+   HM_OPT_NEAR_STAGES 3, 4 or 6 (up to 8 right-hand sides), HM_OPT_TENSOR_CORES
+   on or off (FP32, 16 or more).  Inputs are scratch vectors allocated on
+   `stream` and freed before return; synchronous; not allowed while `stream`
+   is being captured.  choice (host, 4 values, may be NULL) receives the
+   chosen overlap, near kernel, near stages and tensor-core flag; ms (host, 2
+   values, may be NULL) the chosen schedule's time per product and that of
+   the configured options. */
+int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice, double *ms);
 
 /* Allocation-free single right-hand-side product.  No counterpart in the
    reference: it is an addition for callers that cannot let a library
