@@ -28,6 +28,7 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kJacobiSweeps = 40;
 constexpr int kTkChunk = 128;       // coefficients per warp of a low-rank solve update
+constexpr int kInvMax = 256;        // largest block of an HM_SOLVE_INV op
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v)
@@ -482,31 +483,36 @@ __global__ void __launch_bounds__(kThreads) potrf_batched(const hm_potrf_problem
 }
 
 // x <- R^{-T} x for an upper triangular n x n block R by one warp (forward
-// substitution with column dot products: x_i = (x_i - R[0:i, i] . x[0:i]) / R_ii).
-// Up to 256 unknowns stay in registers (lane l holds x[l + 32 t]).
+// substitution).  Up to 256 unknowns stay in registers (lane l holds
+// x[l + 32 t]) and the right-looking order is used: once x_i is final (its
+// owner multiplies by the pivot's reciprocal, computed for all rows up front)
+// it is broadcast by a shuffle and every lane subtracts R[i, l] x_i from the
+// rows l > i it holds; each step is one shuffle and independent loads, with
+// no reduction on the dependent path.  Larger blocks use column dot products.
 template <typename T>
 __device__ void trsm_t_warp(const T *R, int64_t ld, int64_t n, T *x)
 {
     const int lane = threadIdx.x & 31;
     if (n <= 256) {
-        T xr[8];
+        T xr[8], rinv[8];
 #pragma unroll
-        for (int t = 0; t < 8; ++t) { const int64_t i = lane + 32 * t; xr[t] = i < n ? x[i] : T(0); }
+        for (int t = 0; t < 8; ++t) {
+            const int64_t i = lane + 32 * t;
+            xr[t] = i < n ? x[i] : T(0);
+            rinv[t] = i < n ? T(1) / R[i + ld * i] : T(0);
+        }
         for (int64_t i = 0; i < n; ++i) {
-            const T *col = R + ld * i;
-            T part = 0;
+            const int owner = (int)(i & 31), ti = (int)(i >> 5);
+            T xi = 0;
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if (t == ti) xi = xr[t] * rinv[t];
+            xi = __shfl_sync(0xffffffffu, xi, owner);
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
                 const int64_t l = lane + 32 * t;
-                if (l < i) part = fma(col[l], xr[t], part);
-            }
-            part = warp_sum(part);
-            if (lane == (int)(i & 31)) {
-                const T d = col[i];
-                const int ti = (int)(i >> 5);
-#pragma unroll
-                for (int t = 0; t < 8; ++t)
-                    if (t == ti) xr[t] = (xr[t] - part) / d;
+                if (t == ti && lane == owner) xr[t] = xi;
+                else if (l > i && l < n) xr[t] = fma(-R[i + ld * l], xi, xr[t]);
             }
         }
 #pragma unroll
@@ -524,46 +530,105 @@ __device__ void trsm_t_warp(const T *R, int64_t ld, int64_t n, T *x)
     __syncwarp();
 }
 
-// One warp per column of B walks the whole schedule; columns are independent,
-// so no CTA barrier is needed.
+// W = R^{-1} for upper triangular n x n blocks, one CTA per block, R staged in
+// shared memory.  Column j of W is the back substitution R w = e_j, run by a
+// group of four lanes (partial sums over k = i+1+q, i+5+q, ... reduced by two
+// shuffles); warp w takes the columns w, w+8, w+16, ... so that the long
+// columns are spread over all warps.  GB300's FP64 rate is low (about two
+// FMAs per clock per SM), so the work is spread over every SM sub-partition.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *ops, int nops, T *B, int64_t ldb,
-                                                           int64_t ncols)
+__global__ void __launch_bounds__(kThreads) trtri_batched(const hm_trtri_problem *probs, int64_t nmax)
 {
-    __shared__ T tk[kWarps][kTkChunk];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t c = (int64_t)blockIdx.x * kWarps + warp;
-    if (c >= ncols) return;
-    T *x = B + ldb * c;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const hm_trtri_problem g = probs[blockIdx.x];
+    const int64_t n = g.n, ls = nmax + 1;
+    T *Rs = reinterpret_cast<T *>(smem_raw);            // ls x n, padded
+    T *Ws = Rs + ls * nmax;                              // ls x n, padded
+    T *rinv = Ws + ls * nmax;                            // n
+    const T *R = static_cast<const T *>(g.R);
+    T *W = static_cast<T *>(g.W);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, q = lane & 3;
+    for (int64_t k = warp; k < n; k += kWarps)
+        for (int64_t i = lane; i < n; i += 32) Rs[i + ls * k] = i <= k ? R[i + g.ldr * k] : T(0);
+    __syncthreads();
+    for (int64_t i = tid; i < n; i += kThreads) rinv[i] = T(1) / Rs[i + ls * i];
+    __syncthreads();
+    // columns j = warp + 8 (g8 + 8 c), g8 = lane / 4 the lane group; the loop
+    // bounds are the same for every lane of a warp, so the shuffles are uniform
+    for (int64_t c = 0; c * 64 < n; ++c) {
+        const int64_t j = warp + 8 * ((lane >> 2) + 8 * c);
+        for (int64_t i = n - 1; i >= 0; --i) {
+            T part = 0;
+            if (j < n && i < j)
+                for (int64_t k = i + 1 + q; k <= j; k += 4) part = fma(Rs[i + ls * k], Ws[k + ls * j], part);
+            part += __shfl_xor_sync(0xffffffffu, part, 1);
+            part += __shfl_xor_sync(0xffffffffu, part, 2);
+            if (j < n && q == 0) Ws[i + ls * j] = i == j ? rinv[i] : i < j ? -part * rinv[i] : T(0);
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int64_t j = warp; j < n; j += kWarps)
+        for (int64_t i = lane; i < n; i += 32) W[i + g.ldw * j] = Ws[i + ls * j];
+}
+
+// One CTA per column of B walks the whole schedule in order: a triangular
+// block on warp 0, low-rank and dense updates on all warps (coefficients of a
+// low-rank block one warp each, then the rows of x2 over all threads).
+// Global writes of x are made visible to the CTA by the barrier after each op.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *ops, int nops, T *B, int64_t ldb)
+{
+    __shared__ T tk[kTkChunk];
+    __shared__ T xs[kInvMax];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    T *x = B + ldb * (int64_t)blockIdx.x;
     for (int o = 0; o < nops; ++o) {
         const hm_solve_op op = ops[o];
         const T *A = static_cast<const T *>(op.A);
         if (op.kind == HM_SOLVE_TRSM) {
-            trsm_t_warp(A, op.ld, op.n1, x + op.o1);
+            if (warp == 0) trsm_t_warp(A, op.ld, op.n1, x + op.o1);
+        } else if (op.kind == HM_SOLVE_INV) {
+            // x1 <- W^T x1, W = R^{-1} upper: four lanes per output, all warps
+            T *x1 = x + op.o1;
+            for (int64_t i = tid; i < op.n1; i += kThreads) xs[i] = x1[i];
+            __syncthreads();
+            const int q = lane & 3;
+            for (int64_t jb = 0; jb < op.n1; jb += kThreads / 4) {
+                const int64_t j = jb + (tid >> 2);
+                T part = 0;
+                if (j < op.n1) {
+                    const T *col = A + op.ld * j;
+                    for (int64_t i = q; i <= j; i += 4) part = fma(col[i], xs[i], part);
+                }
+                part += __shfl_xor_sync(0xffffffffu, part, 1);
+                part += __shfl_xor_sync(0xffffffffu, part, 2);
+                if (j < op.n1 && q == 0) x1[j] = part;
+            }
         } else if (op.kind == HM_SOLVE_LR) {
             const T *s = static_cast<const T *>(op.s), *V = static_cast<const T *>(op.B);
             const T *x1 = x + op.o1;
             T *x2 = x + op.o2;
             for (int k0 = 0; k0 < op.r; k0 += kTkChunk) {
                 const int kn = op.r - k0 < kTkChunk ? op.r - k0 : kTkChunk;
-                for (int k = 0; k < kn; ++k) {
+                for (int k = warp; k < kn; k += kWarps) {
                     const T *u = A + op.ld * (k0 + k);
                     T part = 0;
                     for (int64_t i = lane; i < op.n1; i += 32) part = fma(u[i], x1[i], part);
                     part = warp_sum(part);
-                    if (lane == 0) tk[warp][k] = part * s[k0 + k];
+                    if (lane == 0) tk[k] = part * s[k0 + k];
                 }
-                __syncwarp();
-                for (int64_t j = lane; j < op.n2; j += 32) {
+                __syncthreads();
+                for (int64_t j = tid; j < op.n2; j += kThreads) {
                     T acc = 0;
-                    for (int k = 0; k < kn; ++k) acc = fma(V[j + op.ld2 * (k0 + k)], tk[warp][k], acc);
+                    for (int k = 0; k < kn; ++k) acc = fma(V[j + op.ld2 * (k0 + k)], tk[k], acc);
                     x2[j] -= acc;
                 }
-                __syncwarp();
+                __syncthreads();
             }
         } else {
             const T *x1 = x + op.o1;
-            for (int64_t j = 0; j < op.n2; ++j) {
+            for (int64_t j = warp; j < op.n2; j += kWarps) {
                 const T *col = A + op.ld * j;
                 T part = 0;
                 for (int64_t i = lane; i < op.n1; i += 32) part = fma(col[i], x1[i], part);
@@ -571,7 +636,7 @@ __global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *op
                 if (lane == 0) x[op.o2 + j] -= part;
             }
         }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -760,7 +825,7 @@ int axpby_run(int nprob, const hm_axpby_problem *probs, cudaStream_t st)
 }
 
 template <typename T>
-int potrf_run(int nprob, const hm_potrf_problem *probs, int32_t *info, cudaStream_t st)
+int potrf_run(int nprob, const hm_potrf_problem *probs, int32_t *info, cudaStream_t st, int32_t *d_info_out = nullptr)
 {
     int64_t nmax = 0;
     for (int i = 0; i < nprob; ++i) {
@@ -782,6 +847,12 @@ int potrf_run(int nprob, const hm_potrf_problem *probs, int32_t *info, cudaStrea
     hm_potrf_problem *d_probs = nullptr;
     int *d_info = nullptr;
     ALG_TRY(S.put(probs, (size_t)nprob, &d_probs));
+    if (d_info_out) {
+        // asynchronous form: the kernel writes every problem's info word
+        potrf_batched<T><<<nprob, kThreads, smem, st>>>(d_probs, d_info_out, nsmem);
+        ALG_CK(cudaGetLastError());
+        return HM_OK;
+    }
     ALG_TRY(S.zeros((size_t)nprob, &d_info));
     potrf_batched<T><<<nprob, kThreads, smem, st>>>(d_probs, d_info, nsmem);
     ALG_CK(cudaGetLastError());
@@ -799,19 +870,56 @@ int potrf_run(int nprob, const hm_potrf_problem *probs, int32_t *info, cudaStrea
     return bad ? HM_ERR_NOT_POSDEF : HM_OK;
 }
 
+// largest block trtri_batched keeps in shared memory (R, W and the pivots)
+template <typename T>
+int64_t trtri_max()
+{
+    int64_t n = 0;
+    while ((2 * (n + 1) * (n + 2) + (n + 1)) * (int64_t)sizeof(T) <= 200 * 1024) ++n;
+    return n;
+}
+
+template <typename T>
+int trtri_run(int nprob, const hm_trtri_problem *probs, cudaStream_t st)
+{
+    int64_t nmax = 0;
+    for (int i = 0; i < nprob; ++i) {
+        const hm_trtri_problem &g = probs[i];
+        if (g.n < 0 || (g.n && (!g.R || !g.W || g.ldr < g.n || g.ldw < g.n))) {
+            set_last_error("problem %d: bad block", i);
+            return HM_ERR_INVALID_ARG;
+        }
+        nmax = std::max(nmax, g.n);
+    }
+    if (nmax > trtri_max<T>()) {
+        set_last_error("hm_trtri_batched: blocks up to %lld rows, got %lld", (long long)trtri_max<T>(), (long long)nmax);
+        return HM_ERR_UNSUPPORTED;
+    }
+    if (nprob == 0 || nmax == 0) return HM_OK;
+    const size_t smem = (size_t)(2 * (nmax + 1) * nmax + nmax) * sizeof(T);
+    ALG_TRY(set_smem(trtri_batched<T>, smem));
+    Staged S(st);
+    hm_trtri_problem *d_probs = nullptr;
+    ALG_TRY(S.put(probs, (size_t)nprob, &d_probs));
+    trtri_batched<T><<<nprob, kThreads, smem, st>>>(d_probs, nmax);
+    ALG_CK(cudaGetLastError());
+    return HM_OK;
+}
+
 template <typename T>
 int solve_run(int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t ncols, cudaStream_t st)
 {
     int64_t extent = 0;
     for (int i = 0; i < nops; ++i) {
         const hm_solve_op &o = ops[i];
-        if (o.kind < HM_SOLVE_TRSM || o.kind > HM_SOLVE_DENSE || o.n1 < 0 || o.n2 < 0 || o.o1 < 0 || o.o2 < 0 ||
+        if (o.kind < HM_SOLVE_TRSM || o.kind > HM_SOLVE_INV || (o.kind == HM_SOLVE_INV && o.n1 > kInvMax) || o.n1 < 0 || o.n2 < 0 || o.o1 < 0 || o.o2 < 0 ||
             !o.A || (o.kind == HM_SOLVE_LR && (o.r < 0 || (o.r && (!o.s || !o.B || o.ld < o.n1 || o.ld2 < o.n2)))) ||
             (o.kind != HM_SOLVE_LR && o.ld < o.n1)) {
             set_last_error("solve op %d: bad operation", i);
             return HM_ERR_INVALID_ARG;
         }
-        extent = std::max(extent, std::max(o.o1 + o.n1, o.kind == HM_SOLVE_TRSM ? 0 : o.o2 + o.n2));
+        const bool diag = o.kind == HM_SOLVE_TRSM || o.kind == HM_SOLVE_INV;
+        extent = std::max(extent, std::max(o.o1 + o.n1, diag ? 0 : o.o2 + o.n2));
     }
     if (ncols < 0 || (ncols > 0 && (!B || ldb < extent))) {
         set_last_error("right-hand sides: %lld rows needed, leading dimension %lld", (long long)extent, (long long)ldb);
@@ -821,8 +929,8 @@ int solve_run(int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t nc
     Staged S(st);
     hm_solve_op *d_ops = nullptr;
     ALG_TRY(S.put(ops, (size_t)nops, &d_ops));
-    const int64_t blocks = (ncols + kWarps - 1) / kWarps;
-    solve_schedule<T><<<(unsigned)blocks, kThreads, 0, st>>>(d_ops, nops, static_cast<T *>(B), ldb, ncols);
+    if (ncols > 0x7fffffff) { set_last_error("too many right-hand sides"); return HM_ERR_INVALID_ARG; }
+    solve_schedule<T><<<(unsigned)ncols, kThreads, 0, st>>>(d_ops, nops, static_cast<T *>(B), ldb);
     ALG_CK(cudaGetLastError());
     return HM_OK;
 }
@@ -874,6 +982,28 @@ int hm_potrf_batched(int dtype, int nprob, const hm_potrf_problem *probs, int32_
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (dtype == HM_F64) return potrf_run<double>(nprob, probs, info, st);
     if (dtype == HM_F32) return potrf_run<float>(nprob, probs, info, st);
+    set_last_error("unknown dtype %d", dtype);
+    return HM_ERR_UNSUPPORTED;
+}
+
+int hm_potrf_batched_async(int dtype, int nprob, const hm_potrf_problem *probs, int32_t *d_info, void *stream)
+{
+    clear_last_error();
+    if (nprob < 0 || (nprob && (!probs || !d_info))) { set_last_error("bad problem list"); return HM_ERR_INVALID_ARG; }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dtype == HM_F64) return potrf_run<double>(nprob, probs, nullptr, st, d_info);
+    if (dtype == HM_F32) return potrf_run<float>(nprob, probs, nullptr, st, d_info);
+    set_last_error("unknown dtype %d", dtype);
+    return HM_ERR_UNSUPPORTED;
+}
+
+int hm_trtri_batched(int dtype, int nprob, const hm_trtri_problem *probs, void *stream)
+{
+    clear_last_error();
+    if (nprob < 0 || (nprob && !probs)) { set_last_error("bad problem list"); return HM_ERR_INVALID_ARG; }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dtype == HM_F64) return trtri_run<double>(nprob, probs, st);
+    if (dtype == HM_F32) return trtri_run<float>(nprob, probs, st);
     set_last_error("unknown dtype %d", dtype);
     return HM_ERR_UNSUPPORTED;
 }

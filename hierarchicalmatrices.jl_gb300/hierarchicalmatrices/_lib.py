@@ -24,7 +24,7 @@ HM_ERR_BOX = 8
 HM_ERR_DEGENERATE = 9
 HM_ERR_NOT_POSDEF = 10
 HM_LR_KMAX = 96
-HM_SOLVE_TRSM, HM_SOLVE_LR, HM_SOLVE_DENSE = 0, 1, 2
+HM_SOLVE_TRSM, HM_SOLVE_LR, HM_SOLVE_DENSE, HM_SOLVE_INV = 0, 1, 2, 3
 
 HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
 HM_F64, HM_F32 = 0, 1
@@ -73,7 +73,7 @@ EXPORTED = (
     "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_autotune", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
     "hm_bary_factors", "hm_lr_svd", "hm_gemm_batched", "hm_axpby_batched", "hm_potrf_batched",
-    "hm_solve_transposed",
+    "hm_solve_transposed", "hm_potrf_batched_async", "hm_trtri_batched",
 )
 
 _d = ctypes.POINTER(ctypes.c_double)
@@ -112,6 +112,11 @@ class AxpbyProblem(ctypes.Structure):
 class PotrfProblem(ctypes.Structure):
     """hm_potrf_problem of include/hmgpu.h."""
     _fields_ = [("n", _c64), ("A", _vp), ("lda", _c64), ("R", _vp), ("ldr", _c64)]
+
+
+class TrtriProblem(ctypes.Structure):
+    """hm_trtri_problem of include/hmgpu.h."""
+    _fields_ = [("n", _c64), ("R", _vp), ("ldr", _c64), ("W", _vp), ("ldw", _c64)]
 
 
 class SolveOp(ctypes.Structure):
@@ -173,6 +178,10 @@ def _load():
     L.hm_potrf_batched.restype = ctypes.c_int
     L.hm_potrf_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(PotrfProblem),
                                    ctypes.POINTER(ctypes.c_int32), _vp]
+    L.hm_potrf_batched_async.restype = ctypes.c_int
+    L.hm_potrf_batched_async.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(PotrfProblem), _vp, _vp]
+    L.hm_trtri_batched.restype = ctypes.c_int
+    L.hm_trtri_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(TrtriProblem), _vp]
     L.hm_solve_transposed.restype = ctypes.c_int
     L.hm_solve_transposed.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SolveOp), _vp, _i64, _i64, _vp]
     L.hm_size.restype = ctypes.c_int

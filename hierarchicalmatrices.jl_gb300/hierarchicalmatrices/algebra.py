@@ -28,7 +28,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import check, lib
-from .hierarchical import AbstractHierarchical, Adjoint, LowRankMatrix, _colmajor, _is_dense
+from .hierarchical import _EPOCH, AbstractHierarchical, Adjoint, LowRankMatrix, _colmajor, _is_dense
 
 
 class Diagonal:
@@ -569,8 +569,10 @@ def todense(H, dtype=None):
 
 # ------------------------------------------------------------------ Cholesky and the solve
 
-def _potrf(A):
-    """hierarchicalcholesky(A::Matrix) = Matrix(cholesky(Symmetric(A)).U)."""
+def _potrf(A, infos=None):
+    """hierarchicalcholesky(A::Matrix) = Matrix(cholesky(Symmetric(A)).U).
+    With ``infos`` (a list) the factorisation is queued without waiting and
+    its device info word appended; the caller checks the words later."""
     A = _dev(A)
     n = A.shape[0]
     if A.dim() != 2 or A.shape[1] != n:
@@ -578,6 +580,11 @@ def _potrf(A):
     R = _empty(n, n, A.dtype)
     arr = (_lib.PotrfProblem * 1)()
     arr[0].n, arr[0].A, arr[0].lda, arr[0].R, arr[0].ldr = n, _ptr(A), _ld(A), _ptr(R), _ld(R)
+    if infos is not None:
+        word = _torch().zeros(1, dtype=_torch().int32, device=A.device)
+        check(lib.hm_potrf_batched_async(_dt(A), 1, arr, ctypes.c_void_p(word.data_ptr()), _stream()))
+        infos.append(word)
+        return R
     info = (ctypes.c_int32 * 1)()
     st = lib.hm_potrf_batched(_dt(A), 1, arr, info, _stream())
     if st == _lib.HM_ERR_NOT_POSDEF:
@@ -605,15 +612,32 @@ def hierarchicalcholesky(A):
     """hierarchicalcholesky(A) (src/cholesky.jl:12-92): the upper factor R with
     R'R = A of a symmetric positive definite 2 x 2 hierarchical matrix (or a
     dense matrix), in the reference's block order:
-    R11 = chol(A11); R12 = R11^{-T} A12; R22 = chol(A22 - R12'R12)."""
+    R11 = chol(A11); R12 = R11^{-T} A12; R22 = chol(A22 - R12'R12).
+    The dense diagonal leaves are factored without waiting; their pivot checks
+    are read once at the end, and the first failing leaf (in the reference's
+    order) raises the PosDefException the reference would raise."""
+    if _is_dense(A) or not isinstance(A, AbstractHierarchical):
+        return _hchol(A, None)
+    infos = []
+    R = _hchol(A, infos)
+    if infos:
+        words = _torch().cat(infos).cpu().numpy()
+        bad = np.flatnonzero(words)
+        if bad.size:
+            raise np.linalg.LinAlgError(f"PosDefException: matrix is not positive definite; "
+                                        f"Cholesky factorization failed at pivot {int(words[bad[0]])}")
+    return R
+
+
+def _hchol(A, infos):
     if _is_dense(A):
-        return _potrf(A)
+        return _potrf(A, infos)
     if not isinstance(A, AbstractHierarchical):
         raise TypeError(f"no method hierarchicalcholesky for {type(A).__name__}")
     _check_2x2(A)
     R = type(A)(2, 2, dtype=A.dtype)
     A11, A12, A22 = A.block(0, 0), A.block(0, 1), A.block(1, 1)
-    R11 = hierarchicalcholesky(A11)
+    R11 = _hchol(A11, infos)
     R[_block(1), _block(1)] = R11
     R12 = solvetransposed(R11, A12)
     R[_block(1), _block(2)] = R12
@@ -633,13 +657,61 @@ def hierarchicalcholesky(A):
         A22m = _empty(D.shape[0], D.shape[1], D.dtype)
         _gemm(D.dtype, [dict(m=D.shape[0], n=D.shape[1], k=M.shape[0], P=M, transp=1, Q=M, transq=1,
                              alpha=-1.0, beta=1.0, C=D, D=A22m)])
-    R[_block(2), _block(2)] = hierarchicalcholesky(A22m)
+    R[_block(2), _block(2)] = _hchol(A22m, infos)
     return R
 
 
 def _schedule(R, off, ops, keep):
     """The forward-substitution schedule of R^{-T} in the order of the
-    reference's recursion (src/cholesky.jl:142-228)."""
+    reference's recursion (src/cholesky.jl:142-228).  A hierarchical R keeps
+    its own schedule (offsets from its first row) until the next block
+    assignment, so a factor's schedule is built from its halves' schedules."""
+    if isinstance(R, AbstractHierarchical):
+        c = getattr(R, "_solve_sched", None)
+        if c is None or c[0] != _EPOCH[0]:
+            own_ops, own_keep = [], []
+            _schedule_build(R, 0, own_ops, own_keep)
+            _invert_leaves(own_ops, own_keep)
+            c = (_EPOCH[0], own_ops, own_keep)
+            R._solve_sched = c
+        for o in c[1]:
+            if off:
+                o = dict(o)
+                o["o1"] += off
+                if "o2" in o:
+                    o["o2"] += off
+            ops.append(o)
+        keep.extend(c[2])
+        return R.shape[1]
+    return _schedule_build(R, off, ops, keep)
+
+
+_INV_MAX = 96      # diagonal leaves up to this size are applied through their inverse
+
+
+def _invert_leaves(ops, keep):
+    """Replace the triangular solves of small diagonal leaves by products with
+    their inverses (HM_SOLVE_INV), the inverses made by one batched call: a
+    leaf's serial forward substitution on one warp is slow at GB300's FP64
+    rate, its inverse's product runs on every warp of the CTA."""
+    todo = [o for o in ops if o["kind"] == _lib.HM_SOLVE_TRSM and 0 < o["n1"] <= _INV_MAX]
+    if not todo or any(o["A"].dtype != todo[0]["A"].dtype for o in todo):
+        return                                    # nothing to do, or mixed storage: keep the substitutions
+    dtype = todo[0]["A"].dtype
+    arr = (_lib.TrtriProblem * len(todo))()
+    inv = []
+    for i, o in enumerate(todo):
+        W = _empty(o["n1"], o["n1"], dtype)
+        inv.append(W)
+        pb = arr[i]
+        pb.n, pb.R, pb.ldr, pb.W, pb.ldw = o["n1"], _ptr(o["A"]), o["ld"], _ptr(W), _ld(W)
+    check(lib.hm_trtri_batched(_dt(todo[0]["A"]), len(todo), arr, _stream()))
+    keep.extend(inv)
+    for o, W in zip(todo, inv):
+        o["kind"], o["A"], o["ld"] = _lib.HM_SOLVE_INV, W, _ld(W)
+
+
+def _schedule_build(R, off, ops, keep):
     if _is_dense(R):
         Rd = _dev(R)
         n = Rd.shape[0]

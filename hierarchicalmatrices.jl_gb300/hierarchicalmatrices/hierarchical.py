@@ -240,6 +240,11 @@ def adjoint(A):
 
 # --------------------------------------------------------------------- @hierarchical
 
+# Incremented by every block assignment of every hierarchical matrix: a cached
+# shape or solve schedule is valid while the epoch it was made in is current.
+_EPOCH = [0]
+
+
 class AbstractHierarchical:
     """Base of the classes made by ``hierarchical``: an M x N grid of blocks,
     each of one of the declared types or of the class itself, with the
@@ -276,6 +281,7 @@ class AbstractHierarchical:
             return        # the reference ignores blocks of other types (src/hierarchical.jl:149-172)
         getattr(self, self._store_names[tag - 1])[m][n] = A
         self.assigned[m, n] = tag
+        _EPOCH[0] += 1
         self._invalidate()
 
     def __getitem__(self, key):
@@ -313,9 +319,15 @@ class AbstractHierarchical:
 
     @property
     def shape(self):
-        # rows from block column N, columns from block row 1 (src/hierarchical.jl:33-47)
-        return (sum(self.blocksize(m, self.N, 1) for m in range(1, self.M + 1)),
-                sum(self.blocksize(1, n, 2) for n in range(1, self.N + 1)))
+        # rows from block column N, columns from block row 1 (src/hierarchical.jl:33-47);
+        # cached until the next block assignment anywhere
+        c = getattr(self, "_shape_cache", None)
+        if c is not None and c[0] == _EPOCH[0]:
+            return c[1]
+        sh = (sum(self.blocksize(m, self.N, 1) for m in range(1, self.M + 1)),
+              sum(self.blocksize(1, n, 2) for n in range(1, self.N + 1)))
+        self._shape_cache = (_EPOCH[0], sh)
+        return sh
 
     def size(self, dim=None):
         return self.shape if dim is None else self.shape[dim - 1]

@@ -392,6 +392,12 @@ typedef struct {
     void *R; int64_t ldr;
 } hm_potrf_problem;
 int hm_potrf_batched(int dtype, int nprob, const hm_potrf_problem *probs, int32_t *info, void *stream);
+/* The same without waiting: d_info is a DEVICE array (nprob values) that the
+   kernel fills with 0 or the failing pivot j >= 1; the caller reads it later
+   (hierarchicalcholesky reads the words of all its leaves once, at the end,
+   and raises for the first failing leaf as src/cholesky.jl:16-18 would).
+   Returns after the launch is queued. */
+int hm_potrf_batched_async(int dtype, int nprob, const hm_potrf_problem *probs, int32_t *d_info, void *stream);
 
 /* solvetransposed(R, B) (src/cholesky.jl:97-228): B <- R^{-T} B in place for
    the ncols columns of B (ld ldb), R an upper block-triangular hierarchical
@@ -400,13 +406,30 @@ int hm_potrf_batched(int dtype, int nprob, const hm_potrf_problem *probs, int32_
      HM_SOLVE_TRSM   x[o1 : o1+n1) <- R^{-T} x[..]          (A = R, n1 x n1 upper, ld)
      HM_SOLVE_LR     x[o2 : o2+n2) -= V diag(s) U^T x[o1 : o1+n1)
                                                               (A = U n1 x r ld, B = V n2 x r ld2)
-     HM_SOLVE_DENSE  x[o2 : o2+n2) -= M^T x[o1 : o1+n1)       (A = M n1 x n2, ld)  */
-enum { HM_SOLVE_TRSM = 0, HM_SOLVE_LR = 1, HM_SOLVE_DENSE = 2 };
+     HM_SOLVE_DENSE  x[o2 : o2+n2) -= M^T x[o1 : o1+n1)       (A = M n1 x n2, ld)
+     HM_SOLVE_INV    x[o1 : o1+n1) <- W^T x[..], W = R^{-1}  (A = W, n1 x n1 upper, ld;
+                                                              n1 <= 256; from hm_trtri_batched)
+   One CTA per column of B runs the ops in order.  HM_SOLVE_INV turns the
+   serial forward substitution of a diagonal block into one parallel product
+   (GB300's FP64 rate makes a one-warp substitution slow). */
+enum { HM_SOLVE_TRSM = 0, HM_SOLVE_LR = 1, HM_SOLVE_DENSE = 2, HM_SOLVE_INV = 3 };
 typedef struct {
     int32_t kind, r;
     int64_t o1, n1, o2, n2, ld, ld2;
     const void *A, *s, *B;
 } hm_solve_op;
+/* W = R^{-1} for upper triangular blocks (W upper, zeros below the diagonal),
+   one CTA per block in shared memory: blocks up to 112 rows in FP64 and 159
+   in FP32 (larger ones: HM_ERR_UNSUPPORTED).  Used once per diagonal leaf of
+   a hierarchical Cholesky factor, so that solvetransposed applies each leaf
+   as a product (HM_SOLVE_INV).  Asynchronous. */
+typedef struct {
+    int64_t n;
+    const void *R; int64_t ldr;
+    void *W; int64_t ldw;
+} hm_trtri_problem;
+int hm_trtri_batched(int dtype, int nprob, const hm_trtri_problem *probs, void *stream);
+
 int hm_solve_transposed(int dtype, int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t ncols,
                         void *stream);
 

@@ -183,10 +183,48 @@ def test_hierarchical_cholesky(dt, kernel, dense_below):
     assert np.array_equal(host(XL.V), host(lr_dev(L, dt).V))
 
 
+@pytest.mark.parametrize("dt", DT)
+def test_trtri_batched(dt):
+    """hm_trtri_batched: W = R^{-1} of upper triangular blocks (the inverses
+    solvetransposed applies to small diagonal leaves) against numpy's inverse."""
+    import ctypes
+    from hierarchicalmatrices import _lib
+    rng = np.random.default_rng(17)
+    nmax = 112 if dt == torch.float64 else 159
+    sizes = [1, 17, 64, 96, nmax]
+    Rs = [np.triu(rng.standard_normal((n, n))) + 4 * np.eye(n) for n in sizes]
+    Rd = [dev(R, dt) for R in Rs]
+    Wd = [torch.full((n, n), float("nan"), dtype=dt, device="cuda").t() for n in sizes]
+    arr = (_lib.TrtriProblem * len(sizes))()
+    for i, n in enumerate(sizes):
+        arr[i].n, arr[i].R, arr[i].ldr = n, Rd[i].data_ptr(), Rd[i].stride(1)
+        arr[i].W, arr[i].ldw = Wd[i].data_ptr(), Wd[i].stride(1)
+    dti = _lib.HM_F64 if dt == torch.float64 else _lib.HM_F32
+    _lib.check(_lib.lib.hm_trtri_batched(dti, len(sizes), arr, None))
+    torch.cuda.synchronize()
+    tol = 1e-13 if dt == torch.float64 else 2e-6
+    for R, W in zip(Rs, Wd):
+        Wh = host(W)
+        assert np.all(np.tril(Wh, -1) == 0)
+        assert rel(Wh, np.linalg.inv(R)) <= tol * np.linalg.cond(R)
+    big = nmax + 1
+    Rb = dev(np.eye(big), dt)
+    Wb = torch.empty((big, big), dtype=dt, device="cuda")
+    pb = (_lib.TrtriProblem * 1)()
+    pb[0].n, pb[0].R, pb[0].ldr, pb[0].W, pb[0].ldw = big, Rb.data_ptr(), big, Wb.data_ptr(), big
+    assert _lib.lib.hm_trtri_batched(dti, 1, pb, None) == _lib.HM_ERR_UNSUPPORTED
+
+
 def test_cholesky_errors():
     T, _ = A.spd_hodlr(128, 32, seed=16)
     T.blocks[1][1].blocks[1][1][0, 0] = -1.0          # the last 32 x 32 diagonal leaf
     with pytest.raises(np.linalg.LinAlgError):
+        G.hierarchicalcholesky(tree_dev(T, torch.float64))
+    # the first leaf fails: the rest of the factorisation runs on its NaNs and
+    # the pivot check at the end still names the first failure
+    T, _ = A.spd_hodlr(128, 32, seed=16)
+    T.blocks[0][0].blocks[0][0][0, 0] = -1.0
+    with pytest.raises(np.linalg.LinAlgError, match="pivot 1"):
         G.hierarchicalcholesky(tree_dev(T, torch.float64))
     H3 = hm.HierarchicalMatrix(3, 3)
     with pytest.raises(AssertionError):
