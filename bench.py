@@ -383,12 +383,39 @@ def run_cholesky(hm, torch, dev, args, n=16384, leaf=64):
     m = 2048
     Rd = algebra.todense(R)[:m, :m]
     resid = float(torch.linalg.norm(Rd.t() @ xs[:m] - b[:m]) / torch.linalg.norm(b[:m]))
+    cpu = None if args.no_cpu_baseline else cholesky_cpu_baseline(hm, A, b.cpu().numpy())
     return {"workload": f"hierarchicalcholesky of K + 1e-2 I, K Gaussian exp(-(x-y)^2/(2*0.15^2)) on n={n} sorted "
                         f"uniform points, leaf {leaf}, off-diagonal LowRankMatrix blocks at 1e-12, FP64; "
                         "then solvetransposed of one vector",
             "n": n, "ms_per_factorization": ms, "factorizations_per_s": 1e3 / ms, "solve_ms": solve_ms,
             "max_rank_A": tree_ranks(A), "max_rank_R": tree_ranks(R), "solve_rel_residual_leading_2048": resid,
-            "reps": reps}
+            "reps": reps, "cpu_baseline": cpu}
+
+
+def cholesky_cpu_baseline(hm, A, b):
+    """The oracle's hierarchicalcholesky and solvetransposed (numpy/LAPACK on
+    the host cores, the reference's block order) on the same matrix: one run
+    each (the factorisation takes about a second at n = 16384)."""
+    from oracle import algebra as OA
+
+    def host_tree(H):
+        if isinstance(H, hm.LowRankMatrix):
+            return OA.LR(H.U.cpu().numpy(), H.sigma.cpu().numpy(), H.V.cpu().numpy())
+        if not hasattr(H, "blocksize"):
+            return H.cpu().numpy()
+        M, N = H.blocksize()
+        return OA.HB([[None if H.block(i, j) is None else host_tree(H.block(i, j)) for j in range(N)]
+                      for i in range(M)])
+
+    T = host_tree(A)
+    t0 = time.perf_counter()
+    R = OA.cholesky(T)
+    chol_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    OA.solvetransposed(R, b)
+    solve_ms = (time.perf_counter() - t0) * 1e3
+    return {"kind": "port", "cores": os.cpu_count(), "ms_per_factorization": chol_ms, "solve_ms": solve_ms,
+            "sample": "oracle/algebra.py cholesky + solvetransposed (numpy, LAPACK leaves) on the same matrix, one run"}
 
 
 def run_grad(hm, torch, dev, args, n=65536):

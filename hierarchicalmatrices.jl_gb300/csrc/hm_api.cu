@@ -77,7 +77,7 @@ int cuda_status(cudaError_t e, const char *what)
     } while (0)
 
 constexpr int kSegRows = 64;
-#define HM_NSTAGES 4   // upward pass, far field + downward pass, near-field panels, far-field panels
+#define HM_NSTAGES 5   // upward pass, far field + downward pass, near-field panels, far-field panels, whole product
 constexpr int kWarpCta = 256;   // threads of the band-transfer CTAs
 
 // sin(pi t) in extended precision, rounded once; t is formed in double like
@@ -129,7 +129,7 @@ void transfer_matrices(int r, const std::vector<double> &x, const std::vector<do
 
 // The options one product runs with (hm_configure's HM_OPT_* values).
 struct Sched {
-    int overlap, near_kernel, near_stages, tensor_cores;
+    int overlap, near_kernel, near_stages, tensor_cores, pdl;
 };
 
 // Right-hand-side buckets of the autotuned schedules: 1, 2, 3-4, 5-8, 9-16,
@@ -237,6 +237,12 @@ struct hm_handle {
     int overlap = 2;
     int near_stages = 4;            // ring stages of the near-field streaming kernel
     int near_kernel = 0;            // 0 default (one warp per segment), 1 the same, 2 streamed CTAs
+    // programmatic dependent launches along the tree passes: on for FP32
+    // storage (measured 0.219 vs 0.231 ms at n = 2^20 with the near field after
+    // the leaf stage), off for FP64, whose near field runs beside the tree
+    // passes at the FP64 pipe's limit and lost more to CTAs scheduled early
+    // (0.759 vs 0.702 ms); set at build from the storage type
+    int pdl = -1;
     // hm_autotune's choice per right-hand-side bucket; a product whose bucket
     // has one runs with it instead of the options above
     Sched tuned[kSchedBuckets] = {};
@@ -446,6 +452,27 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     return HM_OK;
 }
 
+// Launches kernel on st.  With pdl the launch is a programmatic dependent of
+// the kernel issued just before it on st: it may be scheduled while that
+// kernel finishes, and the kernel itself waits (pdl_wait) before it reads the
+// predecessor's results.  Only kernels that call pdl_wait get pdl = true.
+template <typename... KArgs, typename... Args>
+int launch_k(const char *what, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+             bool pdl, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cuda_status(cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...), what);
+}
+
 struct StageTimer {
     hm_handle *h;
     int stage;
@@ -574,7 +601,8 @@ thread_local const Sched *t_sched = nullptr;
 
 inline Sched configured_sched(const hm_handle *h)
 {
-    return Sched{h->overlap, h->near_kernel, h->near_stages, h->tensor_cores ? 1 : 0};
+    return Sched{h->overlap, h->near_kernel, h->near_stages, h->tensor_cores ? 1 : 0,
+                 h->pdl >= 0 ? h->pdl : (h->storage == HM_F32 ? 1 : 0)};
 }
 inline Sched cur_sched(const hm_handle *h) { return t_sched ? *t_sched : configured_sched(h); }
 inline Sched sched_for(const hm_handle *h, int k)
@@ -600,9 +628,15 @@ constexpr size_t kTaskSmemMax = 200 * 1024;     // shared memory of a band task 
 // field, downward transfers level by level.  QC right-hand sides per warp.
 template <typename S, typename A, int QC>
 int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing, cudaEvent_t mid,
-                   int mid_after)
+                   int mid_after, bool *ends_with_kernel)
 {
     const int r = h->r, k = ma.k;
+    // a launch may be a programmatic dependent while the previous operation on
+    // st is one of this product's kernels (no event recorded since)
+    // (timing events of the upward or downward stage would sit between the
+    // chained kernels; the near-field and whole-product events do not)
+    const bool pdl_on = cur_sched(h).pdl && !(h->profile_mask & 0x3u);
+    bool chain = false;
     const int64_t nq = (k + QC - 1) / QC;
     const A *T = static_cast<const A *>(h->d_T);
     {
@@ -613,8 +647,9 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
             leaf_up<S, A, QC><<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(
                 ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
             HM_CK_LAUNCH("leaf_up");
+            chain = true;
         }
-        if (mid && mid_after == 2) HM_CK(cudaEventRecord(mid, st));  // leaf bases done
+        if (mid && mid_after == 2) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // leaf bases done
         const size_t usm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[0] * QC * r) * sizeof(A);
         if (usm <= kTaskSmemMax) {
             const size_t xsm = usm;
@@ -622,9 +657,9 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
             for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
                 const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
                 if (!n) continue;
-                xfer_up_task<A, QC><<<dim3(n, (unsigned)nq), kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps,
-                                                                                 h->d_up_ents, T, t, r, k);
-                HM_CK_LAUNCH("xfer_up_task");
+                HM_TRY(launch_k("xfer_up_task", xfer_up_task<A, QC>, dim3(n, (unsigned)nq), dim3(kWarpCta), xsm, st,
+                                pdl_on && chain, h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, r, k));
+                chain = true;
             }
         } else {
             const size_t xsm =
@@ -636,10 +671,11 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 xfer_up_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t,
                                                               r, k);
                 HM_CK_LAUNCH("xfer_up_band");
+                chain = true;
             }
         }
     }
-    if (mid && mid_after == 0) HM_CK(cudaEventRecord(mid, st));     // upward pass done
+    if (mid && mid_after == 0) { HM_CK(cudaEventRecord(mid, st)); chain = false; }    // upward pass done
     {
         StageTimer tm(h, timing ? 1 : -1, st);
         bool done = false;
@@ -649,10 +685,10 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 const size_t smem = 8 * (size_t)h->fstride * sizeof(S) +
                                     (size_t)kWarpsPerCta * 2 * QC * HM_RMAX * sizeof(A);
                 HM_TRY(ensure_smem(m2l_k<S, A, QC>, smem));
-                m2l_k<S, A, QC><<<h->n_m2l_rows, 32 * kWarpsPerCta, smem, st>>>(
-                    h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s,
-                    r, k);
-                HM_CK_LAUNCH("m2l_k");
+                HM_TRY(launch_k("m2l_k", m2l_k<S, A, QC>, dim3(h->n_m2l_rows), dim3(32 * kWarpsPerCta), smem, st,
+                                pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents,
+                                static_cast<const S *>(h->d_F), h->fstride, t, s, r, k));
+                chain = true;
                 done = true;
             }
         }
@@ -660,11 +696,12 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
             const size_t smem =
                 (size_t)kWarpsPerCta * (2 * (size_t)h->fstride * sizeof(S) + 2 * (size_t)QC * HM_RMAX * sizeof(A));
             HM_TRY(ensure_smem(m2l<S, A, QC>, smem));
-            m2l<S, A, QC><<<warp_ctas((int64_t)h->n_m2l_rows * nq), 32 * kWarpsPerCta, smem, st>>>(
-                h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k);
-            HM_CK_LAUNCH("m2l");
+            HM_TRY(launch_k("m2l", m2l<S, A, QC>, dim3(warp_ctas((int64_t)h->n_m2l_rows * nq)),
+                            dim3(32 * kWarpsPerCta), smem, st, pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows,
+                            h->d_m2l_ents, static_cast<const S *>(h->d_F), h->fstride, t, s, r, k));
+            chain = true;
         }
-        if (mid && mid_after == 1) HM_CK(cudaEventRecord(mid, st));  // far-field stage done
+        if (mid && mid_after == 1) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // far-field stage done
         const size_t dsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[1] * QC * r) * sizeof(A);
         if (dsm <= kTaskSmemMax) {
             const size_t xsm = dsm;
@@ -672,9 +709,10 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
             for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
                 const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
                 if (!n) continue;
-                xfer_down_task<A, QC><<<dim3(n, (unsigned)nq), kWarpCta, xsm, st>>>(
-                    h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T, s, r, k);
-                HM_CK_LAUNCH("xfer_down_task");
+                HM_TRY(launch_k("xfer_down_task", xfer_down_task<A, QC>, dim3(n, (unsigned)nq), dim3(kWarpCta), xsm,
+                                st, pdl_on && chain, h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T, s,
+                                r, k));
+                chain = true;
             }
         } else {
             const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)(kWarpCta / 32) * QC * HM_RMAX) * sizeof(A);
@@ -685,18 +723,23 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
                 xfer_down_band<A, QC><<<n, kWarpCta, xsm, st>>>(h->d_down_tasks + b, h->d_down_steps,
                                                                 h->d_down_ents, T, s, r, k);
                 HM_CK_LAUNCH("xfer_down_band");
+                chain = true;
             }
         }
     }
+    *ends_with_kernel = chain && pdl_on;
     return HM_OK;
 }
 
 template <typename S, typename A>
 int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing,
-                cudaEvent_t mid = nullptr, int mid_after = 0)
+                cudaEvent_t mid = nullptr, int mid_after = 0, bool *ends_with_kernel = nullptr)
 {
-    if (ma.k == 1) return launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing, mid, mid_after);
-    return launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing, mid, mid_after);
+    bool ends = false;
+    const int rc = ma.k == 1 ? launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing, mid, mid_after, &ends)
+                             : launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing, mid, mid_after, &ends);
+    if (ends_with_kernel) *ends_with_kernel = ends;
+    return rc;
 }
 
 // shared memory per streaming CTA: three per SM up to two right-hand sides
@@ -705,7 +748,7 @@ constexpr size_t kStreamSmemMax3 = 74 * 1024, kStreamSmemMax2 = 112 * 1024, kStr
 
 template <typename S, typename A, bool FAR, int KB>
 int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, S *yfar,
-                   cudaStream_t st)
+                   cudaStream_t st, bool pdl = false)
 {
     // one warp per segment unless the streamed CTAs are asked for: measured on
     // GB300, the warp kernel reads 64-row grid panels at 6.1 TB/s (90% of the
@@ -741,9 +784,10 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
     const int maxw = std::max(h->max_width, 1);
     const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(A);
     HM_TRY(ensure_smem(expand_part<S, A, FAR, KB>, smem));
-    expand_part<S, A, FAR, KB><<<warp_ctas(h->n_segs), 32 * kWarpsPerCta, smem, st>>>(
-        ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(panels), s, t, h->r, maxw, yfar);
-    HM_CK_LAUNCH(FAR ? "expand_far" : "expand_near");
+    // only the far-field form waits for its predecessor (pdl_wait)
+    HM_TRY(launch_k(FAR ? "expand_far" : "expand_near", expand_part<S, A, FAR, KB>, dim3(warp_ctas(h->n_segs)),
+                    dim3(32 * kWarpsPerCta), smem, st, FAR && pdl, ma, h->d_segs, h->n_segs, h->d_pieces,
+                    static_cast<const S *>(panels), s, t, h->r, maxw, yfar));
     return HM_OK;
 }
 
@@ -751,17 +795,17 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
 // with yfar the far-field rows go to yfar (leading dimension ldy of ma).
 template <typename S, typename A, bool FAR>
 int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st,
-                S *yfar = nullptr)
+                S *yfar = nullptr, bool pdl = false)
 {
     // one right-hand side: FP32 runs the warp kernel's two-column form (FMA
     // with a TwoSum fold every 64 columns issues less than per-element
     // TwoProd/TwoSum); FP64 (plain FMA either way, on the scarce FP64 pipe) and
     // the streamed kernel keep the one-column form
     if (ma.k == 1 && (sizeof(A) == 8 || (!FAR && h->stream_ctas > 0 && cur_sched(h).near_kernel == 2)))
-        return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st);
-    if (ma.k <= 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st);
-    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, yfar, st);
-    return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, yfar, st);
+        return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st, pdl);
+    if (ma.k <= 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st, pdl);
+    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, yfar, st, pdl);
+    return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, yfar, st, pdl);
 }
 
 constexpr int kTensorCoreMinK = 16;   // right-hand sides from which the tensor-core panels run
@@ -808,13 +852,14 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
     A *s = reinterpret_cast<A *>(static_cast<char *>(scratch) + L.s_off);
     const bool split = side != st;
     const bool tree = h->n_vp || h->n_m2l_rows;
+    bool tree_chain = false;         // the tree passes ended with a kernel: the next launch may be dependent
     if (tree) {
         if (split) {
             HM_CK(cudaEventRecord(fork, st));
             HM_CK(cudaStreamWaitEvent(side, fork, 0));
         }
         HM_TRY((launch_tree<S, A>(h, ma, split ? side : st, t, s, timing, split ? mid : nullptr,
-                                  cur_sched(h).overlap == 3 ? 1 : cur_sched(h).overlap == 4 ? 2 : 0)));
+                                  cur_sched(h).overlap == 3 ? 1 : cur_sched(h).overlap == 4 ? 2 : 0, &tree_chain)));
         if (split && (k > kPartMaxK || !h->n_segs)) HM_CK(cudaEventRecord(join, side));
     }
     if (!h->n_segs) {
@@ -829,7 +874,8 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
             mf.ldy = h->nx;
             {
                 StageTimer tm(h, timing ? 3 : -1, side);
-                HM_TRY((launch_part<S, A, true>(h, mf, s, t, panels, side, yfar)));
+                HM_TRY((launch_part<S, A, true>(h, mf, s, t, panels, side, yfar,
+                                                tree_chain && !(h->profile_mask & 0x8u))));
             }
             HM_CK(cudaEventRecord(join, side));
             if (mid) HM_CK(cudaStreamWaitEvent(st, mid, 0));
@@ -848,8 +894,10 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
             HM_TRY((launch_part<S, A, false>(h, ma, s, t, panels, st)));
         }
         if (tree) {
+            // after the near field on the same stream
             StageTimer tm(h, timing ? 3 : -1, st);
-            HM_TRY((launch_part<S, A, true>(h, ma, s, t, panels, st)));
+            HM_TRY((launch_part<S, A, true>(h, ma, s, t, panels, st, nullptr,
+                                            cur_sched(h).pdl && !(h->profile_mask & 0xcu))));
         }
         return HM_OK;
     }
@@ -866,6 +914,7 @@ int run_mul(hm_handle *h, MulArgs<S> ma, cudaStream_t st, const void *panels = n
     SchedScope scope(&sched);
     hm_handle::StreamCtx *sc = nullptr;
     HM_TRY(stream_ctx(h, st, stream_scratch_bytes<A>(h, ma.k), &sc));
+    StageTimer whole(h, 4, st);
     return launch_pipeline<S, A>(h, ma, st, sched.overlap ? sc->side : st, sc->fork, sc->join, sc->p, true, panels,
                                  sched.overlap >= 2 ? sc->mid : nullptr);
 }
@@ -936,18 +985,20 @@ std::vector<Sched> sched_candidates(const hm_handle *h, int k, bool fp32)
     auto add = [&c](Sched s) {
         for (const Sched &o : c)
             if (o.overlap == s.overlap && o.near_kernel == s.near_kernel && o.near_stages == s.near_stages &&
-                o.tensor_cores == s.tensor_cores)
+                o.tensor_cores == s.tensor_cores && o.pdl == s.pdl)
                 return;
         c.push_back(s);
     };
+    const std::vector<int> pdls = tree ? std::vector<int>{1, 0} : std::vector<int>{base.pdl};
     for (int ov : overlaps)
         for (int nk : kernels)
-            for (int tc : tcs) {
-                if (nk == 2)
-                    for (int ns : {3, 4, 6}) add(Sched{ov, nk, ns, tc});
-                else
-                    add(Sched{ov, nk, base.near_stages, tc});
-            }
+            for (int tc : tcs)
+                for (int pd : pdls) {
+                    if (nk == 2)
+                        for (int ns : {3, 4, 6}) add(Sched{ov, nk, ns, tc, pd});
+                    else
+                        add(Sched{ov, nk, base.near_stages, tc, pd});
+                }
     return c;
 }
 
@@ -1003,6 +1054,7 @@ int autotune(hm_handle *h, int k, int reps, cudaStream_t st, int32_t *choice, do
         choice[1] = cand[bi].near_kernel;
         choice[2] = cand[bi].near_stages;
         choice[3] = cand[bi].tensor_cores;
+        choice[4] = cand[bi].pdl;
     }
     if (ms_out) {
         ms_out[0] = best[bi];
@@ -1740,6 +1792,7 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     case HM_OPT_AUTOTUNED:
         if (value != 0) { set_error("HM_OPT_AUTOTUNED takes 0 (forget the tuned schedules)"); return HM_ERR_INVALID_ARG; }
         break;
+    case HM_OPT_PDL: break;
     default: set_error("unknown option %d", option); return HM_ERR_INVALID_ARG;
     }
     // the host-buffer product's captured graph follows the options: drop it;
@@ -1754,6 +1807,7 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     case HM_OPT_TENSOR_CORES: h->tensor_cores = value != 0; break;
     case HM_OPT_NEAR_KERNEL: h->near_kernel = (int)value; break;
     case HM_OPT_NEAR_STAGES: h->near_stages = (int)value; break;
+    case HM_OPT_PDL: h->pdl = value != 0 ? 1 : 0; break;
     default: break;
     }
     return HM_OK;
@@ -1786,6 +1840,39 @@ int hm_profile_read(hm_handle *h, double *ms, int64_t *launches, int n, int rese
     if (reset)
         for (int i = 0; i < HM_NSTAGES; ++i) { h->stage_ms[i] = 0; h->stage_launches[i] = 0; }
     return HM_OK;
+}
+
+int hm_profile_timeline(hm_handle *h, double *out, int nmax)
+{
+    if (!h || (nmax > 0 && !out)) return HM_ERR_INVALID_ARG;
+    // the earliest start among the pending events is the origin
+    int first = -1;
+    float best = 0.f;
+    for (size_t i = 0; i < h->events.size(); ++i) {
+        HM_CK(cudaEventSynchronize(h->events[i].b));
+        if (first < 0) { first = (int)i; continue; }
+        float t = 0.f;
+        HM_CK(cudaEventElapsedTime(&t, h->events[first].a, h->events[i].a));
+        if (t < best) best = t;
+    }
+    int n = 0;
+    for (auto &e : h->events) {
+        float t0 = 0.f, t1 = 0.f, d = 0.f;
+        HM_CK(cudaEventElapsedTime(&t0, h->events[first].a, e.a));
+        HM_CK(cudaEventElapsedTime(&t1, h->events[first].a, e.b));
+        HM_CK(cudaEventElapsedTime(&d, e.a, e.b));
+        if (n < nmax) {
+            out[3 * n] = e.stage;
+            out[3 * n + 1] = t0 - best;
+            out[3 * n + 2] = t1 - best;
+        }
+        ++n;
+        h->stage_ms[e.stage] += d;
+        h->stage_launches[e.stage] += 1;
+    }
+    for (auto &e : h->events) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    h->events.clear();
+    return n;
 }
 
 void hm_free(hm_handle *h)

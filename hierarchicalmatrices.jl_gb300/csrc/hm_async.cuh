@@ -10,6 +10,14 @@ namespace {
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;
 constexpr unsigned long long kDrainLimitNs = 200000000ull;
 
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream serialisation attribute may start while its predecessor in the stream
+// is finishing; pdl_wait() returns once the predecessor has completed and its
+// writes are visible (immediately for a kernel launched without the
+// attribute).  pdl_trigger() lets the successor be scheduled early.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
     return (uint32_t)__cvta_generic_to_shared(p);

@@ -157,6 +157,7 @@ template <typename S, typename A, int QC>
 __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r)
 {
     extern __shared__ unsigned char smem_raw[];
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
@@ -307,7 +308,9 @@ __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const h
     const hm_task tk = tasks[blockIdx.x];
     const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
     const int q0 = blockIdx.y * QC, qc = min(QC, k - q0);      // this CTA's right-hand sides
+    pdl_trigger();
     for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
+    pdl_wait();                                                // the children's coefficients are ready
     // external children: warps take records, lanes coefficients
     for (int rec = threadIdx.x >> 5; rec < nrec; rec += blockDim.x >> 5) {
         const hm_xfer X = ents[e0 + rec];
@@ -366,7 +369,9 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
     const hm_task tk = tasks[blockIdx.x];
     const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
     const int q0 = blockIdx.y * QC, qc = min(QC, k - q0);      // this CTA's right-hand sides
+    pdl_trigger();
     for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
+    pdl_wait();                                                // far-field and parent coefficients are ready
     // children start from their far-field (m2l) coefficients; external parents as computed
     // warps take records, lanes coefficients
     for (int rec = threadIdx.x >> 5; rec < nrec; rec += blockDim.x >> 5) {
@@ -452,6 +457,8 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
     const int lane = threadIdx.x & 31;
     const int nq = (k + QC - 1) / QC;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    pdl_trigger();
+    pdl_wait();                                                // the upward pass's coefficients are ready
     if (w >= (int64_t)nrows * nq) return;
     const hm_m2l_row R = rows[w / nq];
     const int q0 = (int)(w % nq) * QC, qc = min(QC, k - q0);
@@ -516,6 +523,8 @@ __global__ void m2l_k(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents,
     S *Fb = reinterpret_cast<S *>(smem_raw);                                      // kM2lBlocks x fstride
     A *Tb = reinterpret_cast<A *>(Fb + kM2lBlocks * fstride) + (threadIdx.x >> 5) * 2 * QC * HM_RMAX;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    pdl_trigger();
+    pdl_wait();
     if (blockIdx.x >= nrows) return;
     const hm_m2l_row R = rows[blockIdx.x];
     for (int e0 = R.begin; e0 < R.end || e0 == R.begin; e0 += kM2lBlocks) {
@@ -696,6 +705,7 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int seg = blockIdx.x * (blockDim.x >> 5) + wib;
+    if constexpr (FAR) pdl_wait();                             // the downward pass's coefficients are ready
     if (seg >= nsegs) return;
     A *g = reinterpret_cast<A *>(smem_raw) + (int64_t)wib * maxw * KB;
     const hm_seg G = segs[seg];

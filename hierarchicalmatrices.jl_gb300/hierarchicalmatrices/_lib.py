@@ -33,6 +33,7 @@ HM_OPT_NEAR_STAGES = 2
 HM_OPT_TENSOR_CORES = 3
 HM_OPT_NEAR_KERNEL = 4
 HM_OPT_AUTOTUNED = 5
+HM_OPT_PDL = 6
 HM_PIECE_COEF, HM_PIECE_X, HM_PIECE_TCOEF = 0, 1, 2
 
 # Records of csrc/hm_types.h.
@@ -65,12 +66,12 @@ PLAN_SIZES = ("r", "nx", "ny", "n_xslots", "n_yslots", "vstore", "fstore", "psto
 STATS = ("n_bary", "n_dense", "depth", "n_xslots", "n_yslots", "canonical_values",
          "reference_values", "stored_values", "dense_values", "n_segments", "max_width",
          "device_bytes", "launches_per_mul")
-STAGES = ("up", "down", "expand", "far")
+STAGES = ("up", "down", "expand", "far", "product")
 
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
     "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_device_status", "hm_chebyshev", "hm_mul", "hm_mul_strided",
-    "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_autotune", "hm_profile", "hm_profile_read", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
+    "hm_mul_host", "hm_mul_noalloc", "hm_direct_rows", "hm_configure", "hm_autotune", "hm_profile", "hm_profile_read", "hm_profile_timeline", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
     "hm_bary_factors", "hm_lr_svd", "hm_gemm_batched", "hm_axpby_batched", "hm_potrf_batched",
     "hm_solve_transposed", "hm_potrf_batched_async", "hm_trtri_batched",
@@ -213,6 +214,8 @@ def _load():
     L.hm_autotune.restype = ctypes.c_int
     L.hm_autotune.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.POINTER(ctypes.c_int32),
                               ctypes.POINTER(ctypes.c_double)]
+    L.hm_profile_timeline.restype = ctypes.c_int
+    L.hm_profile_timeline.argtypes = [_vp, _vp, ctypes.c_int]
     L.hm_profile.restype = ctypes.c_int
     L.hm_profile.argtypes = [_vp, ctypes.c_int]
     L.hm_profile_read.restype = ctypes.c_int

@@ -286,6 +286,11 @@ class KernelMatrix:
         mode = int(enable) if not isinstance(enable, bool) else (2 if enable else 0)
         check(lib.hm_configure(self._h, _lib.HM_OPT_OVERLAP, mode))
 
+    def set_pdl(self, enable=True):
+        """Programmatic dependent launches along the tree passes (default) or
+        plain launches."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_PDL, 1 if enable else 0))
+
     def set_tensor_cores(self, enable=True):
         """FP32 products with 16+ right-hand sides on the tensor cores (default)
         or on the FP32 pipes."""
@@ -305,14 +310,14 @@ class KernelMatrix:
     def autotune(self, nrhs=1, reps=20, *, stream=None):
         """Time every candidate schedule of a product with ``nrhs`` right-hand
         sides (stream placement of the near field, near-field kernel and ring
-        depth, tensor cores) and keep the fastest for that right-hand-side
+        depth, tensor cores, programmatic dependent launches) and keep the fastest for that right-hand-side
         bucket.  Returns the choice and the time per product of it and of the
         configured options."""
-        choice = (ctypes.c_int32 * 4)()
+        choice = (ctypes.c_int32 * 5)()
         ms = (ctypes.c_double * 2)()
         check(lib.hm_autotune(self._h, int(nrhs), int(reps), _stream_ptr(stream), choice, ms))
         return {"overlap": choice[0], "near_kernel": choice[1], "near_stages": choice[2],
-                "tensor_cores": bool(choice[3]), "ms": ms[0], "ms_configured": ms[1]}
+                "tensor_cores": bool(choice[3]), "pdl": bool(choice[4]), "ms": ms[0], "ms_configured": ms[1]}
 
     def forget_autotune(self):
         """Drop the autotuned schedules: products run with the configured options."""

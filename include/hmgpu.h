@@ -225,7 +225,13 @@ enum {
     /* HM_OPT_AUTOTUNED: value 0 forgets the schedules hm_autotune chose, so
        every product runs with the options above again.  Setting any other
        option forgets them too. */
-    HM_OPT_AUTOTUNED = 5
+    HM_OPT_AUTOTUNED = 5,
+    /* HM_OPT_PDL (default 1 for FP32 storage, 0 for FP64): the kernels of the tree passes (and the
+       far-field rows after them) are launched as programmatic dependents of
+       the kernel before them on the stream, so that each is scheduled while
+       its predecessor finishes and stages its constant inputs before it waits
+       for the predecessor's results; 0 launches them plainly. */
+    HM_OPT_PDL = 6
 };
 int hm_configure(hm_handle *h, int option, int64_t value);
 
@@ -238,10 +244,10 @@ int hm_configure(hm_handle *h, int option, int64_t value);
    it, including inside stream capture.  Candidates: HM_OPT_OVERLAP 0..4
    (0..1 above 8 right-hand sides), HM_OPT_NEAR_KERNEL 0 or 2 with
    HM_OPT_NEAR_STAGES 3, 4 or 6 (up to 8 right-hand sides), HM_OPT_TENSOR_CORES
-   on or off (FP32, 16 or more).  Inputs are scratch vectors allocated on
+   on or off (FP32, 16 or more), HM_OPT_PDL on or off.  Inputs are scratch vectors allocated on
    `stream` and freed before return; synchronous; not allowed while `stream`
-   is being captured.  choice (host, 4 values, may be NULL) receives the
-   chosen overlap, near kernel, near stages and tensor-core flag; ms (host, 2
+   is being captured.  choice (host, 5 values, may be NULL) receives the
+   chosen overlap, near kernel, near stages, tensor-core flag and PDL flag; ms (host, 2
    values, may be NULL) the chosen schedule's time per product and that of
    the configured options. */
 int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice, double *ms);
@@ -272,12 +278,18 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
 /* Per-stage timing of hm_mul (the reference prints @time per call,
    examples/Kernel.jl:73-76): for each stage whose bit is set in stage_mask
    (0 upward pass: leaf bases and transfers, 1 far field and downward
-   transfers, 2 near-field panels, 3 far-field panel columns), CUDA events are recorded on the launching stream around
-   its launches.  hm_profile_read synchronises on them and returns accumulated
+   transfers, 2 near-field panels, 3 far-field panel columns, 4 the whole
+   product on the caller's stream), CUDA events are recorded on the stream
+   that launches the stage, around its launches.  hm_profile_read synchronises on them and returns accumulated
    milliseconds and launch counts per stage; reset = 1 clears the totals.
    stage_mask = 0 turns timing off. */
 int hm_profile(hm_handle *h, int stage_mask);
 int hm_profile_read(hm_handle *h, double *ms, int64_t *launches, int n, int reset);
+/* Timeline of the pending timed stages (consumed as by hm_profile_read):
+   for each, in the order recorded, out[3i] = stage, out[3i+1] = start and
+   out[3i+2] = end in ms from the earliest start.  Returns the number of
+   records (only the first nmax are written), or a negative status. */
+int hm_profile_timeline(hm_handle *h, double *out, int nmax);
 
 void hm_free(hm_handle *h);
 

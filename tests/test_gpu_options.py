@@ -84,3 +84,26 @@ def test_host_buffer_product_replays(mat):
         u = u0.copy()
         H.mul_host(u, v, accumulate=True)
     np.testing.assert_allclose(u, u0 + ref, rtol=TOL[dt], atol=TOL[dt] * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("k", [1, 4, 32])
+def test_programmatic_launches_change_nothing(mat, k):
+    """Launching the tree passes as programmatic dependents (HM_OPT_PDL) runs
+    the same kernels on the same data: results equal bit for bit, for every
+    stream schedule (one stream, side stream, near field after each stage)."""
+    n, dt, H = mat
+    B = torch.randn(k, n, device="cuda", dtype=TDT[dt]).t()
+    try:
+        for mode in (0, 1, 2, 3, 4):
+            H.set_overlap(mode)
+            H.set_pdl(False)
+            U0 = torch.empty(k, n, device="cuda", dtype=TDT[dt]).t()
+            H.mul(U0, B, accumulate=False)
+            H.set_pdl(True)
+            for _ in range(3):
+                U1 = torch.empty(k, n, device="cuda", dtype=TDT[dt]).t()
+                H.mul(U1, B, accumulate=False)
+                assert torch.equal(U1, U0), (mode, k)
+    finally:
+        H.set_overlap(True)
+        H.set_pdl(True)
