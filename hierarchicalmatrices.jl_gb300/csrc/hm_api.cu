@@ -624,6 +624,15 @@ inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerC
 
 constexpr size_t kTaskSmemMax = 200 * 1024;     // shared memory of a band task kernel
 
+// Index of the last non-empty band of a band pointer array, or -1.
+inline int last_band(const std::vector<int> &ptr)
+{
+    int last = -1;
+    for (size_t bd = 0; bd + 1 < ptr.size(); ++bd)
+        if (ptr[bd + 1] > ptr[bd]) last = (int)bd;
+    return last;
+}
+
 // Tree passes on stream st: leaf bases, upward transfers level by level, far
 // field, downward transfers level by level.  QC right-hand sides per warp.
 template <typename S, typename A, int QC>
@@ -654,11 +663,14 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         if (usm <= kTaskSmemMax) {
             const size_t xsm = usm;
             HM_TRY(ensure_smem(xfer_up_task<A, QC>, xsm));
+            const int last = last_band(h->up_band_ptr);
             for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
                 const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
                 if (!n) continue;
+                // the last band is followed by the M2L grid: no early trigger
                 HM_TRY(launch_k("xfer_up_task", xfer_up_task<A, QC>, dim3(n, (unsigned)nq), dim3(kWarpCta), xsm, st,
-                                pdl_on && chain, h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, r, k));
+                                pdl_on && chain, h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, r, k,
+                                (int)bd != last ? 1 : 0));
                 chain = true;
             }
         } else {
@@ -706,12 +718,14 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         if (dsm <= kTaskSmemMax) {
             const size_t xsm = dsm;
             HM_TRY(ensure_smem(xfer_down_task<A, QC>, xsm));
+            const int last = last_band(h->down_band_ptr);
             for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
                 const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
                 if (!n) continue;
+                // the last band is followed by the far-field rows' grid: no early trigger
                 HM_TRY(launch_k("xfer_down_task", xfer_down_task<A, QC>, dim3(n, (unsigned)nq), dim3(kWarpCta), xsm,
                                 st, pdl_on && chain, h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T, s,
-                                r, k));
+                                r, k, (int)bd != last ? 1 : 0));
                 chain = true;
             }
         } else {
@@ -748,7 +762,7 @@ constexpr size_t kStreamSmemMax3 = 74 * 1024, kStreamSmemMax2 = 112 * 1024, kStr
 
 template <typename S, typename A, bool FAR, int KB>
 int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, S *yfar,
-                   cudaStream_t st, bool pdl = false)
+                   cudaStream_t st, bool pdl = false, int64_t ldf = 0)
 {
     // one warp per segment unless the streamed CTAs are asked for: measured on
     // GB300, the warp kernel reads 64-row grid panels at 6.1 TB/s (90% of the
@@ -787,25 +801,25 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
     // only the far-field form waits for its predecessor (pdl_wait)
     HM_TRY(launch_k(FAR ? "expand_far" : "expand_near", expand_part<S, A, FAR, KB>, dim3(warp_ctas(h->n_segs)),
                     dim3(32 * kWarpsPerCta), smem, st, FAR && pdl, ma, h->d_segs, h->n_segs, h->d_pieces,
-                    static_cast<const S *>(panels), s, t, h->r, maxw, yfar));
+                    static_cast<const S *>(panels), s, t, h->r, maxw, yfar, ldf));
     return HM_OK;
 }
 
 // Near-field (FAR = false) or far-field (FAR = true) panel columns for k <= 8;
-// with yfar the far-field rows go to yfar (leading dimension ldy of ma).
+// with yfar the far-field rows go to yfar (leading dimension ldf).
 template <typename S, typename A, bool FAR>
 int launch_part(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st,
-                S *yfar = nullptr, bool pdl = false)
+                S *yfar = nullptr, bool pdl = false, int64_t ldf = 0)
 {
     // one right-hand side: FP32 runs the warp kernel's two-column form (FMA
     // with a TwoSum fold every 64 columns issues less than per-element
     // TwoProd/TwoSum); FP64 (plain FMA either way, on the scarce FP64 pipe) and
     // the streamed kernel keep the one-column form
     if (ma.k == 1 && (sizeof(A) == 8 || (!FAR && h->stream_ctas > 0 && cur_sched(h).near_kernel == 2)))
-        return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st, pdl);
-    if (ma.k <= 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st, pdl);
-    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, yfar, st, pdl);
-    return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, yfar, st, pdl);
+        return launch_part_kb<S, A, FAR, 1>(h, ma, s, t, panels, yfar, st, pdl, ldf);
+    if (ma.k <= 2) return launch_part_kb<S, A, FAR, 2>(h, ma, s, t, panels, yfar, st, pdl, ldf);
+    if (ma.k <= 4) return launch_part_kb<S, A, FAR, 4>(h, ma, s, t, panels, yfar, st, pdl, ldf);
+    return launch_part_kb<S, A, FAR, 8>(h, ma, s, t, panels, yfar, st, pdl, ldf);
 }
 
 constexpr int kTensorCoreMinK = 16;   // right-hand sides from which the tensor-core panels run
@@ -870,12 +884,10 @@ int launch_pipeline(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, cudaStr
         if (tree && split) {
             // far-field rows on the side stream, into yfar (nx x k, leading dimension nx)
             S *yfar = reinterpret_cast<S *>(static_cast<char *>(scratch) + L.yfar_off);
-            MulArgs<S> mf = ma;
-            mf.ldy = h->nx;
             {
                 StageTimer tm(h, timing ? 3 : -1, side);
-                HM_TRY((launch_part<S, A, true>(h, mf, s, t, panels, side, yfar,
-                                                tree_chain && !(h->profile_mask & 0x8u))));
+                HM_TRY((launch_part<S, A, true>(h, ma, s, t, panels, side, yfar,
+                                                tree_chain && !(h->profile_mask & 0x8u), h->nx)));
             }
             HM_CK(cudaEventRecord(join, side));
             if (mid) HM_CK(cudaStreamWaitEvent(st, mid, 0));

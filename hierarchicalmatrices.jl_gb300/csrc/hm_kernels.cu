@@ -300,7 +300,7 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
 // L holds QC x r values per local.
 template <typename A, int QC>
 __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
-                             int r, int k)
+                             int r, int k, int early)
 {
     extern __shared__ unsigned char smem_raw[];
     A *Ts = reinterpret_cast<A *>(smem_raw);
@@ -308,7 +308,7 @@ __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const h
     const hm_task tk = tasks[blockIdx.x];
     const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
     const int q0 = blockIdx.y * QC, qc = min(QC, k - q0);      // this CTA's right-hand sides
-    pdl_trigger();
+    if (early) pdl_trigger();     // the next band may be scheduled now (a small grid; not before a large one)
     for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
     pdl_wait();                                                // the children's coefficients are ready
     // external children: warps take records, lanes coefficients
@@ -361,7 +361,7 @@ __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const h
 
 template <typename A, int QC>
 __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
-                               int r, int k)
+                               int r, int k, int early)
 {
     extern __shared__ unsigned char smem_raw[];
     A *Ts = reinterpret_cast<A *>(smem_raw);
@@ -369,7 +369,7 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
     const hm_task tk = tasks[blockIdx.x];
     const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
     const int q0 = blockIdx.y * QC, qc = min(QC, k - q0);      // this CTA's right-hand sides
-    pdl_trigger();
+    if (early) pdl_trigger();
     for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
     pdl_wait();                                                // far-field and parent coefficients are ready
     // children start from their far-field (m2l) coefficients; external parents as computed
@@ -697,9 +697,12 @@ struct SegAcc {
     }
 };
 
+// Near field (FAR = false: y (+)= D x) or far field (FAR = true: U s) of one
+// row segment per warp.  The far field goes to yfar (leading dimension ldf)
+// when given, else it is added into y.
 template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                            const A *s, const A *t, int r, int maxw, S *yfar)
+                            const A *s, const A *t, int r, int maxw, S *yfar, int64_t ldf)
 {
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -787,7 +790,7 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
                     const int row = 4 * rg + j;
                     if (row < G.nrows) {
                         if (FAR && yfar) {
-                            yfar[(G.row0 + row) + (int64_t)q * ma.ldy] = (S)val[j];
+                            yfar[(G.row0 + row) + (int64_t)q * ldf] = (S)val[j];
                         } else {
                             S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
                             A v = val[j];
@@ -830,7 +833,7 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
                 const int row = 2 * lane + j;
                 if (row < G.nrows) {
                     if (FAR && yfar) {
-                        yfar[(G.row0 + row) + (int64_t)q * ma.ldy] = (S)v2[j];
+                        yfar[(G.row0 + row) + (int64_t)q * ldf] = (S)v2[j];
                     } else {
                         S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
                         A v = v2[j];
@@ -1271,9 +1274,11 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
 
 #define HM_INST_PART(S, A, KB)                                                                       \
     template __global__ void expand_part<S, A, false, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *, \
-                                                          const S *, const A *, const A *, int, int, S *); \
+                                                          const S *, const A *, const A *, int, int, S *, \
+                                                          int64_t);                                     \
     template __global__ void expand_part<S, A, true, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *,  \
-                                                         const S *, const A *, const A *, int, int, S *);
+                                                         const S *, const A *, const A *, int, int, S *,  \
+                                                         int64_t);
 #define HM_INST_STREAM(S, A, KB)                                                                      \
     template __global__ void stream_part<S, A, false, KB>(MulArgs<S>, const hm_seg *, const int *,       \
                                                           const hm_piece *, const S *, const A *, const A *, \
@@ -1303,13 +1308,13 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
     template __global__ void xfer_down_band<A, 8>(const hm_task *, const hm_step *, const hm_xfer *,        \
                                                   const A *, A *, int, int);                            \
     template __global__ void xfer_up_task<A, 1>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
-                                                A *, int, int);                                         \
+                                                A *, int, int, int);                                    \
     template __global__ void xfer_up_task<A, 8>(const hm_task *, const hm_step *, const hm_xfer *, const A *, \
-                                                A *, int, int);                                         \
+                                                A *, int, int, int);                                    \
     template __global__ void xfer_down_task<A, 1>(const hm_task *, const hm_step *, const hm_xfer *,        \
-                                                  const A *, A *, int, int);                            \
+                                                  const A *, A *, int, int, int);                       \
     template __global__ void xfer_down_task<A, 8>(const hm_task *, const hm_step *, const hm_xfer *,        \
-                                                  const A *, A *, int, int);
+                                                  const A *, A *, int, int, int);
 HM_INST_MV(double, double)
 HM_INST_MV(float, float)
 template __global__ void add_far<double>(MulArgs<double>, int64_t, const double *, int64_t);

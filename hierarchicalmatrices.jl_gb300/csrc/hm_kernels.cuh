@@ -151,10 +151,10 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
 
 template <typename A, int QC>
 __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
-                             int r, int k);
+                             int r, int k, int early);
 template <typename A, int QC>
 __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *s,
-                               int r, int k);
+                               int r, int k, int early);
 template <typename A, int QC>
 __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
                              int r, int k);
@@ -172,7 +172,7 @@ __global__ void xfer_down_band(const hm_task *tasks, const hm_step *steps, const
 
 template <typename S, typename A, bool FAR, int KB>
 __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
-                            const A *s, const A *t, int r, int maxw, S *yfar);
+                            const A *s, const A *t, int r, int maxw, S *yfar, int64_t ldf);
 
 template <typename S>
 __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf);

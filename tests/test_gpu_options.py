@@ -107,3 +107,26 @@ def test_programmatic_launches_change_nothing(mat, k):
     finally:
         H.set_overlap(True)
         H.set_pdl(True)
+
+
+@pytest.mark.parametrize("k", [1, 3, 8])
+def test_split_schedules_accumulate_like_serial(mat, k):
+    """u += H v with the tree passes on a side stream: the near and far parts
+    of each row segment are combined by whichever kernel finishes second, as
+    (u + near) + far, which is what the one-stream schedule computes; results
+    equal it bit for bit, call after call."""
+    n, dt, H = mat
+    B = torch.randn(k, n, device="cuda", dtype=TDT[dt]).t()
+    U0 = torch.randn(k, n, device="cuda", dtype=TDT[dt]).t()
+    try:
+        H.set_overlap(0)
+        ref = U0.clone()
+        H.mul(ref, B, accumulate=True)
+        for mode in (1, 2, 3, 4):
+            H.set_overlap(mode)
+            for _ in range(3):
+                got = U0.clone()
+                H.mul(got, B, accumulate=True)
+                assert torch.equal(got, ref), (mode, k)
+    finally:
+        H.set_overlap(True)
