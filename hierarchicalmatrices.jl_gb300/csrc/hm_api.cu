@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <atomic>
 #include <map>
+#include <set>
 #include <thread>
 #include <mutex>
 #include <string>
@@ -169,6 +170,7 @@ struct hm_handle {
     void *d_V = nullptr, *d_F = nullptr, *d_P = nullptr;
     hm_vpanel *d_vp = nullptr;
     int n_vp = 0;
+    int vp_cap = 64, vp_wcap = HM_RMAX;   // leaf_up's shared-memory panel: rows (multiple of 32) x columns
     hm_xfer *d_up = nullptr;
     std::vector<int> up_ptr;
     hm_m2l_row *d_m2l_rows = nullptr;
@@ -378,6 +380,20 @@ int band_locals(const std::vector<hm_task> &tasks, const std::vector<hm_step> &s
     return most;
 }
 
+// leaf_up stages panels of up to vp_cap rows (the largest panel's rows rounded
+// up to 32, at most 128: leaves of clustered or random points have up to
+// BLOCKSIZE - 1 rows) and vp_wcap columns in shared memory.
+void set_vp_caps(hm_handle *h, const std::vector<hm_vpanel> &vps)
+{
+    int rows = 1, width = 1;
+    for (const hm_vpanel &p : vps) {
+        rows = std::max(rows, (int)p.nrows);
+        width = std::max(width, (int)p.width);
+    }
+    h->vp_cap = rows <= 128 ? (rows + 31) / 32 * 32 : 64;
+    h->vp_wcap = std::min(width, HM_RMAX);
+}
+
 template <typename S>
 int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, const std::vector<double> &lam,
                  const std::vector<double> &T, const double *x, const double *y, cudaStream_t st)
@@ -397,6 +413,7 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     HM_TRY(h->upload(&vp, P.vpanels, st));
     HM_TRY(h->upload(&vpf, P.vpanel_fill, st));
     h->d_vp = vp; h->n_vp = (int)P.vpanels.size();
+    set_vp_caps(h, P.vpanels);
     HM_TRY(h->upload(&h->d_up, P.up, st));
     h->up_ptr = P.up_level_ptr;
     HM_TRY(h->upload(&h->d_m2l_rows, P.m2l_rows, st));
@@ -502,6 +519,7 @@ int build_hier_device(hm_handle *h, const Plan &P, const std::vector<double> &vs
     hm_vpanel *vp = nullptr;
     HM_TRY(h->upload(&vp, P.vpanels, st));
     h->d_vp = vp; h->n_vp = (int)P.vpanels.size();
+    set_vp_caps(h, P.vpanels);
     HM_TRY(h->upload(&h->d_m2l_rows, P.m2l_rows, st));
     h->n_m2l_rows = (int)P.m2l_rows.size();
     HM_TRY(h->upload(&h->d_m2l_ents, P.m2l_ents, st));
@@ -541,6 +559,22 @@ int ensure_smem(K kernel, size_t bytes)
     if (have >= bytes) return HM_OK;
     HM_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     have = bytes;
+    return HM_OK;
+}
+
+// The largest shared-memory carveout for a streaming panel kernel (set once
+// per device and kernel, like ensure_smem): its blocks then fit by their
+// registers, not by the default L1/shared split.
+std::set<std::pair<int, const void *>> g_carveout_set;
+template <typename K>
+int prefer_shared(K kernel)
+{
+    int dev = 0;
+    HM_CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    if (!g_carveout_set.insert({dev, reinterpret_cast<const void *>(kernel)}).second) return HM_OK;
+    HM_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared));
     return HM_OK;
 }
 
@@ -651,10 +685,10 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
-            const size_t smem = (size_t)kWarpsPerCta * 64 * (HM_RMAX + 2 * QC) * sizeof(S);
+            const size_t smem = (size_t)kWarpsPerCta * leaf_up_warp_bytes<S, A, QC>(h->vp_cap, h->vp_wcap);
             HM_TRY(ensure_smem(leaf_up<S, A, QC>, smem));
             leaf_up<S, A, QC><<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(
-                ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r);
+                ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, r, h->vp_cap, h->vp_wcap);
             HM_CK_LAUNCH("leaf_up");
             chain = true;
         }
@@ -798,6 +832,9 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
     const int maxw = std::max(h->max_width, 1);
     const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(A);
     HM_TRY(ensure_smem(expand_part<S, A, FAR, KB>, smem));
+    // four or more right-hand sides: blocks limited by registers, not by the
+    // default carveout (with one or two, L1 serves the x gathers: keep it)
+    if (KB >= 4) HM_TRY(prefer_shared(expand_part<S, A, FAR, KB>));
     // only the far-field form waits for its predecessor (pdl_wait)
     HM_TRY(launch_k(FAR ? "expand_far" : "expand_near", expand_part<S, A, FAR, KB>, dim3(warp_ctas(h->n_segs)),
                     dim3(32 * kWarpsPerCta), smem, st, FAR && pdl, ma, h->d_segs, h->n_segs, h->d_pieces,

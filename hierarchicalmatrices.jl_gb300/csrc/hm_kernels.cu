@@ -148,13 +148,14 @@ template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, co
 
 // t[slot][col0 + m] = (V^T x)[m] for each explicit basis panel.  One warp
 // per panel, looping over chunks of QC right-hand sides; lane m owns column m
-// of the row-major panel (width <= 32, row stride ld).  Panels of up to 64
-// rows are staged once in shared memory (cp.async) and the chunks' x values
-// double-buffered beside them; longer panels are read directly.  Plain FMA accumulation
+// of the row-major panel (width <= 32, row stride ld).  Panels of up to cap
+// rows and wcap columns (the handle's largest, up to 128 rows) are staged
+// once in shared memory (cp.async) and the chunks' x values double-buffered
+// beside them; longer panels are read directly.  Plain FMA accumulation
 // (the coefficients feed only the far field).  Coefficients of a slot are r
 // apart per right-hand side.
 template <typename S, typename A, int QC>
-__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r)
+__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r, int cap, int wcap)
 {
     extern __shared__ unsigned char smem_raw[];
     pdl_trigger();
@@ -173,11 +174,11 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
                 if (qq < qc) t[((int64_t)P.slot * k + q0 + qq) * r + P.col0 + lane] = acc[qq].value();
         }
     };
-    if (P.nrows <= 64 && P.ld == pw) {
+    if (P.nrows <= cap && P.ld == pw && pw <= wcap) {
         // the panel once; x chunks of QC right-hand sides double-buffered,
-        // right-hand side major xs[b][qq * 64 + j] (lanes walk rows)
-        S *Vs = reinterpret_cast<S *>(smem_raw) + (int64_t)wib * (64 * HM_RMAX + 2 * 64 * QC);
-        A *xs = reinterpret_cast<A *>(Vs + 64 * HM_RMAX);
+        // right-hand side major xs[b][qq * cap + j] (lanes walk rows)
+        S *Vs = reinterpret_cast<S *>(smem_raw + (size_t)wib * leaf_up_warp_bytes<S, A, QC>(cap, wcap));
+        A *xs = reinterpret_cast<A *>(Vs + cap * wcap);
         const int nel = P.nrows * pw;
         if (sizeof(S) * nel % 16 == 0 && (P.off * sizeof(S)) % 16 == 0) {
             const char *src = reinterpret_cast<const char *>(Vp);
@@ -188,12 +189,12 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
         }
         auto fetch = [&](int q0, int b) {
             const int qc = min(QC, k - q0);
-            A *d = xs + b * 64 * QC;
+            A *d = xs + b * cap * QC;
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq)
                 for (int j = lane; j < P.nrows; j += 32) {
-                    if (qq < qc) async_copy<sizeof(A)>(d + qq * 64 + j, ma.x + (P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx);
-                    else d[qq * 64 + j] = A(0);
+                    if (qq < qc) async_copy<sizeof(A)>(d + qq * cap + j, ma.x + (P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx);
+                    else d[qq * cap + j] = A(0);
                 }
             async_commit();
         };
@@ -209,12 +210,12 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
             PlainAcc<A> acc[QC];
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq) acc[qq].zero();
-            const A *xb = xs + b * 64 * QC;
+            const A *xb = xs + b * cap * QC;
             if (lane < pw) {
                 for (int j = 0; j < P.nrows; ++j) {
                     const A v = (A)Vs[j * pw + lane];
 #pragma unroll
-                    for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xb[qq * 64 + j]);
+                    for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xb[qq * cap + j]);
                 }
             }
             store(q0, min(QC, k - q0), acc);
@@ -722,13 +723,23 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
         if (take) {
             if (c0 < 0) c0 = col;
             const A *coef = Q.kind == HM_PIECE_TCOEF ? t : s;
-            for (int i = lane; i < Q.width * KB; i += 32) {
-                const int c = i / KB, q = i % KB;
-                A v = 0;
-                if (q < k)
-                    v = FAR ? coef[((int64_t)Q.src * k + q) * r + c]
-                            : (A)ma.x[(Q.src + c) * ma.incx + (int64_t)q * ma.ldx];
-                g[(col + c) * KB + q] = v;
+            // eight loads in flight per lane, then their stores
+            const int n = Q.width * KB;
+            for (int i0 = lane; i0 < n; i0 += 32 * 8) {
+                A v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int i = i0 + 32 * u, c = i / KB, q = i % KB;
+                    v[u] = 0;
+                    if (i < n && q < k)
+                        v[u] = FAR ? coef[((int64_t)Q.src * k + q) * r + c]
+                                   : (A)ma.x[(Q.src + c) * ma.incx + (int64_t)q * ma.ldx];
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int i = i0 + 32 * u;
+                    if (i < n) g[(col + i / KB) * KB + i % KB] = v[u];
+                }
             }
             c1 = col + Q.width;
         }
@@ -744,7 +755,60 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
     // FAR without: add into y; near field: y (+)= per the caller's flag
     const bool acc_y = FAR ? (yfar == nullptr) : (ma.accumulate != 0);
     constexpr int FOLD = 64;              // columns between compensated folds (KB > 1)
-    if (sizeof(S) == 4) {
+    if constexpr (sizeof(S) == 4 && KB >= 4) {
+        // four or more right-hand sides: each value loaded feeds KB FMAs, so
+        // two rows per lane (float2) and every column in turn, which halves
+        // the accumulators of the four-row form (3 KB values per row) and lets
+        // twice as many warps hide the loads' latency
+        SegAcc<A, KB> a0, a1;
+        a0.zero(); a1.zero();
+        if (2 * lane < G.ld) {
+            const float2 *base = reinterpret_cast<const float2 *>(Pg + 2 * lane);
+            const int64_t ld2 = G.ld / 2;
+            for (int cb = c0; cb < c1; cb += FOLD) {
+                const int ce = min(c1, cb + FOLD);
+                int c = cb;
+                for (; c + 16 <= ce; c += 16) {      // 16 loads in flight per lane
+                    float2 p[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) p[u] = __ldcs(base + ld2 * (c + u));
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) { a0.add(p[u].x, g + (c + u) * KB); a1.add(p[u].y, g + (c + u) * KB); }
+                }
+                for (; c + 8 <= ce; c += 8) {
+                    float2 p[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) p[u] = __ldcs(base + ld2 * (c + u));
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) { a0.add(p[u].x, g + (c + u) * KB); a1.add(p[u].y, g + (c + u) * KB); }
+                }
+                for (; c < ce; ++c) {
+                    const float2 p0 = __ldcs(base + ld2 * c);
+                    a0.add(p0.x, g + c * KB); a1.add(p0.y, g + c * KB);
+                }
+                a0.fold(); a1.fold();
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < KB; ++q) {
+            if (q >= k) break;
+            const A v2[2] = {a0.merged(q, 0, 0), a1.merged(q, 0, 0)};
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int row = 2 * lane + j;
+                if (row < G.nrows) {
+                    if (FAR && yfar) {
+                        yfar[(G.row0 + row) + (int64_t)q * ldf] = (S)v2[j];
+                    } else {
+                        S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
+                        A v = v2[j];
+                        if (acc_y) v += (A)(*yp);
+                        *yp = (S)v;
+                    }
+                }
+            }
+        }
+    } else if (sizeof(S) == 4) {
         const int rg = lane & 15, h = lane >> 4;
         SegAcc<A, KB> acc[4];
 #pragma unroll
@@ -1287,8 +1351,8 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                                          const hm_piece *, const S *, const A *, const A *,  \
                                                          int, int, int, int, int, S *, int *);
 #define HM_INST_MV(S, A)                                                                             \
-    template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
-    template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int);   \
+    template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int, int, int); \
+    template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int, int, int); \
     template __global__ void m2l<S, A, 1>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,    \
                                           const A *, A *, int, int);                                    \
     template __global__ void m2l<S, A, 8>(const hm_m2l_row *, int, const hm_m2l_ent *, const S *, int,    \

@@ -147,7 +147,15 @@ __global__ void fill_segments(FillArgs fa, const hm_seg *segs, const hm_piece *p
 // ---------------------------------------------------------------- matvec
 
 template <typename S, typename A, int QC>
-__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r);
+__global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S *V, A *t, int r, int cap, int wcap);
+
+// Shared memory of one leaf_up warp: a panel of cap x wcap values of S and two
+// x chunks of cap x QC values of A (16-byte multiples: cap is a multiple of 32).
+template <typename S, typename A, int QC>
+__host__ __device__ constexpr size_t leaf_up_warp_bytes(int cap, int wcap)
+{
+    return ((size_t)cap * wcap * sizeof(S) + 15) / 16 * 16 + 2 * (size_t)cap * QC * sizeof(A);
+}
 
 template <typename A, int QC>
 __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
