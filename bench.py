@@ -454,6 +454,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--autotune-reps", type=int, default=50,
+                    help="products timed per candidate schedule by the autotuner (fewer for profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -491,7 +493,7 @@ def main():
 
     # ---- headline: FP32 storage, 1 RHS, device-resident inputs
     # the product's schedule is picked by the library's autotuner (untimed setup)
-    sched = H32.autotune(1, reps=50)
+    sched = H32.autotune(1, reps=args.autotune_reps)
     # CUDA events around the dominant stage only, on the launching stream,
     # inside the timed region (two events per step).
     H32.profile(["expand"])
