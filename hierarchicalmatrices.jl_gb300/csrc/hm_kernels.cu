@@ -723,28 +723,27 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
         if (take) {
             if (c0 < 0) c0 = col;
             const A *coef = Q.kind == HM_PIECE_TCOEF ? t : s;
-            // eight loads in flight per lane, then their stores
+            // fire-and-forget copies into shared memory for every piece, one
+            // wait after the loop (no load-to-store round trip per piece)
             const int n = Q.width * KB;
-            for (int i0 = lane; i0 < n; i0 += 32 * 8) {
-                A v[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int i = i0 + 32 * u, c = i / KB, q = i % KB;
-                    v[u] = 0;
-                    if (i < n && q < k)
-                        v[u] = FAR ? coef[((int64_t)Q.src * k + q) * r + c]
-                                   : (A)ma.x[(Q.src + c) * ma.incx + (int64_t)q * ma.ldx];
-                }
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int i = i0 + 32 * u;
-                    if (i < n) g[(col + i / KB) * KB + i % KB] = v[u];
+            for (int i = lane; i < n; i += 32) {
+                const int c = i / KB, q = i % KB;
+                A *d = g + (col + c) * KB + q;
+                if (q >= k) {
+                    *d = A(0);
+                } else if constexpr (FAR) {
+                    async_copy<sizeof(A)>(d, coef + ((int64_t)Q.src * k + q) * r + c);
+                } else if constexpr (sizeof(S) == sizeof(A)) {
+                    async_copy<sizeof(A)>(d, ma.x + (Q.src + c) * ma.incx + (int64_t)q * ma.ldx);
+                } else {
+                    *d = (A)ma.x[(Q.src + c) * ma.incx + (int64_t)q * ma.ldx];
                 }
             }
             c1 = col + Q.width;
         }
         col += Q.width;
     }
+    async_wait_all();
     if (c0 < 0) {
         if (FAR && !yfar) return;          // no far field on these rows
         c0 = c1 = 0;
@@ -781,6 +780,13 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
                     for (int u = 0; u < 8; ++u) p[u] = __ldcs(base + ld2 * (c + u));
 #pragma unroll
                     for (int u = 0; u < 8; ++u) { a0.add(p[u].x, g + (c + u) * KB); a1.add(p[u].y, g + (c + u) * KB); }
+                }
+                for (; c + 4 <= ce; c += 4) {
+                    float2 p[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) p[u] = __ldcs(base + ld2 * (c + u));
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) { a0.add(p[u].x, g + (c + u) * KB); a1.add(p[u].y, g + (c + u) * KB); }
                 }
                 for (; c < ce; ++c) {
                     const float2 p0 = __ldcs(base + ld2 * c);

@@ -130,3 +130,29 @@ def test_split_schedules_accumulate_like_serial(mat, k):
                 assert torch.equal(got, ref), (mode, k)
     finally:
         H.set_overlap(True)
+
+
+def test_profile_timeline(mat):
+    """hm_profile_timeline: one record per timed stage of the last product,
+    each inside the whole-product record, consumed when read."""
+    import ctypes
+    from hierarchicalmatrices import _lib
+    n, dt, H = mat
+    b = torch.randn(n, device="cuda", dtype=TDT[dt])
+    u = torch.empty_like(b)
+    H.profile()
+    try:
+        H.mul(u, b, accumulate=False)
+        out = np.zeros(3 * 16)
+        k = _lib.lib.hm_profile_timeline(H.handle, out.ctypes.data_as(ctypes.c_void_p), 16)
+        recs = out[:3 * k].reshape(k, 3)
+        names = [_lib.STAGES[int(s)] for s in recs[:, 0]]
+        assert sorted(names) == sorted(_lib.STAGES)
+        whole = recs[names.index("product")]
+        assert whole[1] == 0.0 and whole[2] > 0.0
+        for st, t0, t1 in recs:
+            assert whole[1] <= t0 <= t1 <= whole[2] + 1e-3
+        assert _lib.lib.hm_profile_timeline(H.handle, out.ctypes.data_as(ctypes.c_void_p), 16) == 0
+    finally:
+        H.profile([])
+        H.stage_times(reset=True)
