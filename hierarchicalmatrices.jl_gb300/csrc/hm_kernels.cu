@@ -835,6 +835,22 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
                         acc[0].add(p[u].x, gu); acc[1].add(p[u].y, gu); acc[2].add(p[u].z, gu); acc[3].add(p[u].w, gu);
                     }
                 }
+                for (; c + 6 < ce; c += 8) {           // tails in batches: fewer dependent round trips
+                    float4 p[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) p[u] = __ldcs(base + ld4 * (c + 2 * u));
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const A *gu = g + (c + 2 * u) * KB;
+                        acc[0].add(p[u].x, gu); acc[1].add(p[u].y, gu); acc[2].add(p[u].z, gu); acc[3].add(p[u].w, gu);
+                    }
+                }
+                for (; c + 2 < ce; c += 4) {
+                    const float4 p0 = __ldcs(base + ld4 * c), p1 = __ldcs(base + ld4 * (c + 2));
+                    const A *g0 = g + c * KB, *g1 = g + (c + 2) * KB;
+                    acc[0].add(p0.x, g0); acc[1].add(p0.y, g0); acc[2].add(p0.z, g0); acc[3].add(p0.w, g0);
+                    acc[0].add(p1.x, g1); acc[1].add(p1.y, g1); acc[2].add(p1.z, g1); acc[3].add(p1.w, g1);
+                }
                 for (; c < ce; c += 2) {
                     const float4 p0 = __ldcs(base + ld4 * c);
                     const A *g0 = g + c * KB;
