@@ -320,3 +320,27 @@ def test_batch_matches_instances(dtype, k):
         for q in range(k):
             ref = Ho @ B[c0:c1, q].double().cpu().numpy().copy()
             assert rel(U[r0:r1, q].double().cpu().numpy(), ref) <= (TOL64 if dtype == np.float64 else TOL32)
+
+
+@pytest.mark.parametrize("nx,ny", [(1, 1), (1, 5000), (5000, 1), (79, 79), (80, 80), (81, 81),
+                                   (159, 161), (160, 160), (320, 321), (3, 4097)])
+def test_threshold_and_ragged_sizes(nx, ny):
+    """One point per side, sizes on either side of the leaf rule (BLOCKSIZE 80:
+    all four halves below it, src/KernelMatrix.jl:55) and very uneven
+    rectangles: the GPU product equals the oracle's, FP64 and FP32."""
+    rng = np.random.default_rng(nx * 7919 + ny)
+    x = np.sort(rng.random(nx))[::-1].copy()
+    y = np.sort(rng.random(ny))[::-1].copy()
+    b = rng.standard_normal(ny)
+    ref = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0) @ b
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+    assert rel((H @ dev(b)).cpu().numpy(), ref) <= TOL64
+    H32 = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    ref32 = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0) @ b.astype(np.float32).astype(np.float64)
+    got32 = (H32 @ torch.tensor(b, device="cuda", dtype=torch.float32)).cpu().numpy()
+    assert rel(got32, ref32) <= TOL32
+    # no right-hand sides: nothing is written
+    U = torch.full((nx, 0), 7.0, device="cuda", dtype=torch.float64)
+    H.mul(U, torch.zeros((ny, 0), device="cuda", dtype=torch.float64))
+    H.free()
+    H32.free()
