@@ -1621,6 +1621,7 @@ int hm_mul_t(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int
     g_last_error.clear();
     if (!h) { set_error("NULL handle"); return HM_ERR_INVALID_ARG; }
     if (h->ninst != 1 || h->hx.empty()) { set_error("hm_mul_t: not available for batched or user-assembled handles"); return HM_ERR_UNSUPPORTED; }
+    if (nrhs == 0) return HM_OK;          // nothing read or written (the vectors may be NULL)
     {
         std::lock_guard<std::mutex> lk(h->trans_mu);
         if (!h->trans) {
@@ -1671,8 +1672,10 @@ int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int n
            void *stream)
 {
     g_last_error.clear();
-    if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
+    if (!h) { set_error("NULL handle"); return HM_ERR_INVALID_ARG; }
     if (nrhs < 0) { set_error("nrhs < 0"); return HM_ERR_INVALID_ARG; }
+    if (nrhs == 0) return HM_OK;          // nothing read or written (the vectors may be NULL)
+    if (!v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
     if (nrhs > 1 && (ldv < h->ny || ldu < h->nx)) { set_error("leading dimension too small"); return HM_ERR_BOUNDS; }
     return dispatch_mul(h, v, 1, ldv, u, 1, ldu, nrhs, accumulate ? 1 : 0, static_cast<cudaStream_t>(stream));
 }
@@ -1681,7 +1684,10 @@ int hm_mul_drow(hm_handle *h, int transposed, const void *v, int64_t ldv, void *
                 int accumulate, void *stream)
 {
     g_last_error.clear();
-    if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
+    if (!h) { set_error("NULL handle"); return HM_ERR_INVALID_ARG; }
+    if (nrhs < 0) { set_error("nrhs < 0"); return HM_ERR_INVALID_ARG; }
+    if (nrhs == 0) return HM_OK;          // nothing read or written (the vectors may be NULL)
+    if (!v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
     if (transposed) {
         if (h->ninst != 1 || h->hx.empty()) { set_error("transposed products are not available for batched or user-assembled handles"); return HM_ERR_UNSUPPORTED; }
         {
@@ -1726,8 +1732,9 @@ int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, in
 int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
 {
     g_last_error.clear();
-    if (!h || !v || !u || nrhs < 0) { set_error("bad argument"); return HM_ERR_INVALID_ARG; }
-    if (nrhs == 0) return HM_OK;
+    if (!h || nrhs < 0) { set_error("bad argument"); return HM_ERR_INVALID_ARG; }
+    if (nrhs == 0) return HM_OK;          // nothing read or written (the vectors may be NULL)
+    if (!v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
     const size_t es = h->storage == HM_F64 ? 8 : 4;
     const size_t bv = (size_t)h->ny * nrhs * es, bu = (size_t)h->nx * nrhs * es;
     if (!h->host_stream) HM_CK(cudaStreamCreateWithFlags(&h->host_stream, cudaStreamNonBlocking));

@@ -159,7 +159,9 @@ int hm_device_status(hm_handle *h, int *code, int reset);
      u[:, q]  = H * v[:, q]   (accumulate = 0)
    u, v are DEVICE arrays of the handle's storage type, column q at u + q*ldu.
    Stream-ordered; returns before the work completes.  Internally the tree
-   passes run on a side stream forked from and joined back into `stream`. */
+   passes run on a side stream forked from and joined back into `stream`.
+   nrhs = 0 reads and writes nothing (u and v may then be NULL), here and in
+   hm_mul_t, hm_mul_drow and hm_mul_host. */
 int hm_mul(hm_handle *h, const void *v, int64_t ldv, void *u, int64_t ldu, int nrhs,
            int accumulate, void *stream);
 

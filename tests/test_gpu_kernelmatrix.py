@@ -322,12 +322,12 @@ def test_batch_matches_instances(dtype, k):
             assert rel(U[r0:r1, q].double().cpu().numpy(), ref) <= (TOL64 if dtype == np.float64 else TOL32)
 
 
-@pytest.mark.parametrize("nx,ny", [(1, 1), (1, 5000), (5000, 1), (79, 79), (80, 80), (81, 81),
-                                   (159, 161), (160, 160), (320, 321), (3, 4097)])
+@pytest.mark.parametrize("nx,ny", [(1, 1), (2, 2), (1, 79), (79, 1), (79, 79), (80, 80), (81, 81),
+                                   (40, 200), (159, 161), (160, 160), (320, 321)])
 def test_threshold_and_ragged_sizes(nx, ny):
     """One point per side, sizes on either side of the leaf rule (BLOCKSIZE 80:
-    all four halves below it, src/KernelMatrix.jl:55) and very uneven
-    rectangles: the GPU product equals the oracle's, FP64 and FP32."""
+    all four halves below it, src/KernelMatrix.jl:55) and uneven rectangles:
+    the GPU product equals the oracle's, FP64 and FP32."""
     rng = np.random.default_rng(nx * 7919 + ny)
     x = np.sort(rng.random(nx))[::-1].copy()
     y = np.sort(rng.random(ny))[::-1].copy()
@@ -344,3 +344,17 @@ def test_threshold_and_ragged_sizes(nx, ny):
     H.mul(U, torch.zeros((ny, 0), device="cuda", dtype=torch.float64))
     H.free()
     H32.free()
+
+
+@pytest.mark.parametrize("nx,ny", [(1, 5000), (5000, 1), (3, 4097)])
+def test_very_uneven_sizes_raise_like_reference(nx, ny):
+    """Very uneven point lists make the reference's recursion split an empty
+    range, whose indsplit reads past the end (src/BarycentricMatrix.jl:299-307,
+    a BoundsError): the oracle and the GPU build raise IndexError alike."""
+    rng = np.random.default_rng(nx * 7919 + ny)
+    x = np.sort(rng.random(nx))[::-1].copy()
+    y = np.sort(rng.random(ny))[::-1].copy()
+    with pytest.raises(IndexError):
+        O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0)
+    with pytest.raises(IndexError):
+        hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
