@@ -219,6 +219,7 @@ struct hm_handle {
     struct HostGraph {
         int nrhs = -1, acc = -1;
         void *stage = nullptr;
+        void *out = nullptr;          // page-locked destination written by the last kernel, or none
         bool warm = false;
         cudaGraphExec_t exec = nullptr;
     } host_graph;
@@ -990,14 +991,24 @@ int ensure_drow(hm_handle *h, cudaStream_t st)
 }
 
 int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
-                 int k, int accumulate, cudaStream_t st)
+                 int k, int accumulate, cudaStream_t st, void *yout = nullptr)
 {
     if (h->storage == HM_F64) {
         MulArgs<double> ma{static_cast<const double *>(x), static_cast<double *>(y), incx, ldx, incy, ldy, k, accumulate};
+        ma.yout = static_cast<double *>(yout);
         return run_mul<double, double>(h, ma, st);
     }
     MulArgs<float> ma{static_cast<const float *>(x), static_cast<float *>(y), incx, ldx, incy, ldy, k, accumulate};
+    ma.yout = static_cast<float *>(yout);
     return run_mul<float, float>(h, ma, st);
+}
+
+// True when a product with k right-hand sides ends with add_far (tree passes
+// on the side stream, k <= kPartMaxK, row segments present), which can then
+// write the result to MulArgs::yout.
+bool ends_with_add_far(const hm_handle *h, int k)
+{
+    return (h->n_vp || h->n_m2l_rows) && h->n_segs > 0 && k <= kPartMaxK && sched_for(h, k).overlap != 0;
 }
 
 // ---- autotuned schedules ----------------------------------------------------
@@ -1749,18 +1760,27 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
         }
     }
     char *dv = static_cast<char *>(h->d_stage), *du = dv + bv;
+    // a page-locked destination is written by the product's last kernel
+    // directly (no separate device-to-host copy after it)
+    void *uout = nullptr;
+    if (ends_with_add_far(h, nrhs)) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, u) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+            uout = pa.devicePointer;
+        cudaGetLastError();       // an unregistered pointer is not an error here
+    }
     HM_CK(cudaMemcpyAsync(dv, v, bv, cudaMemcpyHostToDevice, st));
     if (accumulate) HM_CK(cudaMemcpyAsync(du, u, bu, cudaMemcpyHostToDevice, st));
     auto &hg = h->host_graph;
     const int acc = accumulate ? 1 : 0;
-    if (hg.nrhs != nrhs || hg.acc != acc || hg.stage != h->d_stage) {
+    if (hg.nrhs != nrhs || hg.acc != acc || hg.stage != h->d_stage || hg.out != uout) {
         if (hg.exec) cudaGraphExecDestroy(hg.exec);
         hg = hm_handle::HostGraph();
-        hg.nrhs = nrhs; hg.acc = acc; hg.stage = h->d_stage;
+        hg.nrhs = nrhs; hg.acc = acc; hg.stage = h->d_stage; hg.out = uout;
     }
     if (!hg.exec && hg.warm && h->profile_mask == 0) {
         HM_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st);
+        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st, uout);
         cudaGraph_t g = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (e) { if (g) cudaGraphDestroy(g); return e; }
@@ -1772,11 +1792,11 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
     if (hg.exec && h->profile_mask == 0) {
         HM_CK(cudaGraphLaunch(hg.exec, st));
     } else {
-        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st);
+        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st, uout);
         if (e) return e;
         hg.warm = true;
     }
-    HM_CK(cudaMemcpyAsync(u, du, bu, cudaMemcpyDeviceToHost, st));
+    if (!uout) HM_CK(cudaMemcpyAsync(u, du, bu, cudaMemcpyDeviceToHost, st));
     HM_CK(cudaStreamSynchronize(st));
     return HM_OK;
 }

@@ -941,7 +941,8 @@ __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf)
     if (i >= n * ma.k) return;
     const int64_t row = i % n, q = i / n;
     S *yp = ma.y + row * ma.incy + q * ma.ldy;
-    *yp = *yp + yfar[row + q * ldf];
+    S *dst = ma.yout ? ma.yout + row + q * n : yp;
+    *dst = *yp + yfar[row + q * ldf];
 }
 
 // ------------------------------------------------------- streamed panels

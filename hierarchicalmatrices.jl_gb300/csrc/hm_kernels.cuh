@@ -130,6 +130,10 @@ struct MulArgs {
     int64_t incx, ldx, incy, ldy;
     int k;           // right-hand sides
     int accumulate;  // 1: y += H x (the reference's mul!), 0: y = H x
+    // when set, the final combination of near and far fields (add_far) writes
+    // the result here (ld = the row count, e.g. a caller's page-locked host
+    // buffer) instead of back into y
+    S *yout = nullptr;
 };
 
 // ---------------------------------------------------------------- fill (build)

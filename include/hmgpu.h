@@ -195,7 +195,12 @@ int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, in
                    void *y, int64_t leny, int64_t istart, int64_t incy, void *stream);
 
 /* H * v with HOST arrays (u = H v or u += H v): copies v to the device, runs
-   hm_mul and copies the result back; synchronous. */
+   hm_mul and brings the result back; synchronous.  When u is page-locked
+   (cudaHostAlloc / cudaHostRegister) and the product ends by combining its
+   near and far fields, that last kernel writes u directly; otherwise the
+   result is copied back.  The launches are replayed from a CUDA graph from
+   the second call with the same right-hand-side count, accumulate flag and
+   destination. */
 int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate);
 
 /* Exact dense rows: out[q] = sum_j f(x[rows[q]], y[j]) b[j] evaluated in FP64

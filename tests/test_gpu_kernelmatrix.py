@@ -358,3 +358,27 @@ def test_very_uneven_sizes_raise_like_reference(nx, ny):
         O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0)
     with pytest.raises(IndexError):
         hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
+
+
+@pytest.mark.parametrize("k", [1, 4])
+@pytest.mark.parametrize("accumulate", [False, True])
+def test_host_product_pinned_and_pageable(k, accumulate):
+    """hm_mul_host with host buffers: a page-locked destination is written by
+    the product's last kernel directly, a pageable one through a copy; both
+    equal the device product bit for bit, call after call."""
+    n = 65536
+    x, y = O.grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    g = torch.Generator().manual_seed(k)
+    B = torch.randn(k, n, generator=g, dtype=torch.float32)          # column-major n x k as k rows
+    U0 = torch.randn(k, n, generator=g, dtype=torch.float32)
+    ref = U0.clone().cuda().t()
+    H.mul(ref, B.cuda().t(), accumulate=accumulate)
+    ref = ref.t().cpu()
+    for pinned in (True, False):
+        for _ in range(3):                                           # plain call, then graph replays
+            hb = B.clone().pin_memory() if pinned else B.clone()
+            hu = U0.clone().pin_memory() if pinned else U0.clone()
+            H.mul_host(hu.numpy().T, hb.numpy().T, accumulate=accumulate)    # (n, k) Fortran-ordered views
+            assert torch.equal(hu, ref), (pinned, k, accumulate)
+    H.free()
