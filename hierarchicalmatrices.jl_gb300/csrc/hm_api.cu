@@ -171,6 +171,7 @@ struct hm_handle {
     hm_vpanel *d_vp = nullptr;
     int n_vp = 0;
     int vp_cap = 64, vp_wcap = HM_RMAX;   // leaf_up's shared-memory panel: rows (multiple of 32) x columns
+    bool vp_covers_x = false;             // the leaf panels' rows partition [0, ny): leaf_up reads every x once
     hm_xfer *d_up = nullptr;
     std::vector<int> up_ptr;
     hm_m2l_row *d_m2l_rows = nullptr;
@@ -220,6 +221,7 @@ struct hm_handle {
         int nrhs = -1, acc = -1;
         void *stage = nullptr;
         void *out = nullptr;          // page-locked destination written by the last kernel, or none
+        const void *in = nullptr;     // page-locked source read by the leaf stage, or none
         bool warm = false;
         cudaGraphExec_t exec = nullptr;
     } host_graph;
@@ -393,6 +395,16 @@ void set_vp_caps(hm_handle *h, const std::vector<hm_vpanel> &vps)
     }
     h->vp_cap = rows <= 128 ? (rows + 31) / 32 * 32 : 64;
     h->vp_wcap = std::min(width, HM_RMAX);
+    std::vector<std::pair<int64_t, int64_t>> runs;
+    for (const hm_vpanel &p : vps) runs.push_back({p.row0, (int64_t)p.nrows});
+    std::sort(runs.begin(), runs.end());
+    int64_t cur = 0;
+    bool ok = !runs.empty();
+    for (const auto &rn : runs) {
+        if (rn.first != cur) { ok = false; break; }
+        cur += rn.second;
+    }
+    h->vp_covers_x = ok && cur == h->ny;
 }
 
 template <typename S>
@@ -991,16 +1003,36 @@ int ensure_drow(hm_handle *h, cudaStream_t st)
 }
 
 int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
-                 int k, int accumulate, cudaStream_t st, void *yout = nullptr)
+                 int k, int accumulate, cudaStream_t st, void *yout = nullptr, const void *xin = nullptr)
 {
     if (h->storage == HM_F64) {
         MulArgs<double> ma{static_cast<const double *>(x), static_cast<double *>(y), incx, ldx, incy, ldy, k, accumulate};
         ma.yout = static_cast<double *>(yout);
+        ma.xin = static_cast<const double *>(xin);
         return run_mul<double, double>(h, ma, st);
     }
     MulArgs<float> ma{static_cast<const float *>(x), static_cast<float *>(y), incx, ldx, incy, ldy, k, accumulate};
     ma.yout = static_cast<float *>(yout);
+    ma.xin = static_cast<const float *>(xin);
     return run_mul<float, float>(h, ma, st);
+}
+
+// True when leaf_up can bring the right-hand sides in: its panels cover every
+// row of x once, and every later reader of x (the near field) starts after it.
+bool leaf_reads_input(const hm_handle *h, int k)
+{
+    return h->vp_covers_x && h->n_vp > 0 && sched_for(h, k).overlap != 1;
+}
+
+// Device-accessible address of a page-locked host buffer, or nullptr.
+void *pinned_device_ptr(const void *p)
+{
+    cudaPointerAttributes pa{};
+    void *d = nullptr;
+    if (cudaPointerGetAttributes(&pa, p) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+        d = pa.devicePointer;
+    cudaGetLastError();           // an unregistered pointer is not an error here
+    return d;
 }
 
 // True when a product with k right-hand sides ends with add_far (tree passes
@@ -1762,25 +1794,22 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
     char *dv = static_cast<char *>(h->d_stage), *du = dv + bv;
     // a page-locked destination is written by the product's last kernel
     // directly (no separate device-to-host copy after it)
-    void *uout = nullptr;
-    if (ends_with_add_far(h, nrhs)) {
-        cudaPointerAttributes pa{};
-        if (cudaPointerGetAttributes(&pa, u) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
-            uout = pa.devicePointer;
-        cudaGetLastError();       // an unregistered pointer is not an error here
-    }
-    HM_CK(cudaMemcpyAsync(dv, v, bv, cudaMemcpyHostToDevice, st));
+    void *uout = ends_with_add_far(h, nrhs) ? pinned_device_ptr(u) : nullptr;
+    // a page-locked source is read by the leaf stage, which stores it for the
+    // near field (no separate host-to-device copy before the product)
+    const void *vin = leaf_reads_input(h, nrhs) ? pinned_device_ptr(v) : nullptr;
+    if (!vin) HM_CK(cudaMemcpyAsync(dv, v, bv, cudaMemcpyHostToDevice, st));
     if (accumulate) HM_CK(cudaMemcpyAsync(du, u, bu, cudaMemcpyHostToDevice, st));
     auto &hg = h->host_graph;
     const int acc = accumulate ? 1 : 0;
-    if (hg.nrhs != nrhs || hg.acc != acc || hg.stage != h->d_stage || hg.out != uout) {
+    if (hg.nrhs != nrhs || hg.acc != acc || hg.stage != h->d_stage || hg.out != uout || hg.in != vin) {
         if (hg.exec) cudaGraphExecDestroy(hg.exec);
         hg = hm_handle::HostGraph();
-        hg.nrhs = nrhs; hg.acc = acc; hg.stage = h->d_stage; hg.out = uout;
+        hg.nrhs = nrhs; hg.acc = acc; hg.stage = h->d_stage; hg.out = uout; hg.in = vin;
     }
     if (!hg.exec && hg.warm && h->profile_mask == 0) {
         HM_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st, uout);
+        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st, uout, vin);
         cudaGraph_t g = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (e) { if (g) cudaGraphDestroy(g); return e; }
@@ -1792,7 +1821,7 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
     if (hg.exec && h->profile_mask == 0) {
         HM_CK(cudaGraphLaunch(hg.exec, st));
     } else {
-        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st, uout);
+        const int e = dispatch_mul(h, dv, 1, h->ny, du, 1, h->nx, nrhs, acc, st, uout, vin);
         if (e) return e;
         hg.warm = true;
     }

@@ -167,6 +167,9 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
     const int pw = P.width;
     const S *Vp = V + P.off;
     const int k = ma.k;
+    // right-hand sides read from xin (and copied into x as they pass) or from x
+    const S *xsrc = ma.xin ? ma.xin : ma.x;
+    S *xcopy = ma.xin ? const_cast<S *>(ma.x) : nullptr;
     auto store = [&](int q0, int qc, PlainAcc<A> *acc) {
         if (lane < pw) {
 #pragma unroll
@@ -193,8 +196,17 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq)
                 for (int j = lane; j < P.nrows; j += 32) {
-                    if (qq < qc) async_copy<sizeof(A)>(d + qq * cap + j, ma.x + (P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx);
-                    else d[qq * cap + j] = A(0);
+                    const int64_t e = (P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx;
+                    if (qq >= qc) {
+                        d[qq * cap + j] = A(0);
+                    } else if (xcopy) {
+                        // host-mapped source: plain loads, stored here and into x
+                        const S v = xsrc[e];
+                        d[qq * cap + j] = (A)v;
+                        xcopy[e] = v;
+                    } else {
+                        async_copy<sizeof(A)>(d + qq * cap + j, ma.x + e);
+                    }
                 }
             async_commit();
         };
@@ -233,9 +245,15 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
                     const A v = (A)col[(int64_t)j * P.ld];
 #pragma unroll
                     for (int qq = 0; qq < QC; ++qq)
-                        if (qq < qc) acc[qq].add(v, (A)ma.x[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx]);
+                        if (qq < qc) acc[qq].add(v, (A)xsrc[(P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx]);
                 }
             }
+            if (xcopy)
+                for (int qq = 0; qq < qc; ++qq)
+                    for (int j = lane; j < P.nrows; j += 32) {
+                        const int64_t e = (P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx;
+                        xcopy[e] = xsrc[e];
+                    }
             store(q0, qc, acc);
         }
     }

@@ -134,6 +134,10 @@ struct MulArgs {
     // the result here (ld = the row count, e.g. a caller's page-locked host
     // buffer) instead of back into y
     S *yout = nullptr;
+    // when set, leaf_up reads the right-hand sides here (e.g. a caller's
+    // page-locked host buffer, same layout as x) and stores them into x for
+    // the kernels after it; only when the leaf panels cover every row of x once
+    const S *xin = nullptr;
 };
 
 // ---------------------------------------------------------------- fill (build)

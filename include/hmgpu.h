@@ -198,7 +198,10 @@ int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, in
    hm_mul and brings the result back; synchronous.  When u is page-locked
    (cudaHostAlloc / cudaHostRegister) and the product ends by combining its
    near and far fields, that last kernel writes u directly; otherwise the
-   result is copied back.  The launches are replayed from a CUDA graph from
+   result is copied back.  When v is page-locked, the leaf panels cover every
+   row of v once and the near field starts after the leaf stage, the leaf
+   stage reads v from the host and stores it on the device as it goes,
+   instead of a copy before the product.  The launches are replayed from a CUDA graph from
    the second call with the same right-hand-side count, accumulate flag and
    destination. */
 int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate);
