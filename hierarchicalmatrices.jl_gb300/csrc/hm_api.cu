@@ -998,6 +998,8 @@ int ensure_drow(hm_handle *h, cudaStream_t st)
         fill_segments<S, true><<<h->n_segs, 128, 0, st>>>(fa, h->d_segs, h->d_pieces, h->d_seg_fill, h->n_segs, dP);
         HM_CK_LAUNCH("fill_segments<drow>");
     }
+    // complete before the panels are published: a later product may run on another stream
+    HM_CK(cudaStreamSynchronize(st));
     h->d_dP = dP;
     return HM_OK;
 }

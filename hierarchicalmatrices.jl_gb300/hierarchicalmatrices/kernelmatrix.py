@@ -212,17 +212,30 @@ class KernelMatrix:
 
     def loss_and_grad(self, w, t):
         """L = 1/2 |H w - t|^2 and its gradients (dL/dw, dL/dx, dL/dy) with the
-        block tree held fixed; w, t device tensors of the handle's dtype."""
+        block tree held fixed; w, t device tensors of the handle's dtype.
+        The products that do not depend on each other run on two streams
+        (H w beside D_x w, then H^T r beside D_y^T r) and the host waits once,
+        for the loss, at the end."""
         import torch
-        r = self @ w
-        r -= t
-        loss = 0.5 * float(torch.dot(r.double(), r.double()))
-        gw = self.T @ r
+        cur = torch.cuda.current_stream(w.device)
+        aux = getattr(self, "_aux_stream", None)
+        if aux is None or aux.device != w.device:
+            aux = self._aux_stream = torch.cuda.Stream(device=w.device)
         dxw = torch.empty(self.shape[0], dtype=w.dtype, device=w.device)
-        self.mul_drow(dxw, w, accumulate=False)
         dyr = torch.empty(self.shape[1], dtype=w.dtype, device=w.device)
-        self.mul_drow(dyr, r, transposed=True, accumulate=False)
-        return loss, gw, r * dxw, w * dyr
+        r = torch.empty(self.shape[0], dtype=w.dtype, device=w.device)
+        aux.wait_stream(cur)                                   # w ready
+        self.mul_drow(dxw, w, accumulate=False, stream=aux)
+        self.mul(r, w, accumulate=False, stream=cur)
+        r -= t
+        aux.wait_stream(cur)                                   # r ready
+        self.mul_drow(dyr, r, transposed=True, accumulate=False, stream=aux)
+        gw = torch.empty(self.shape[1], dtype=w.dtype, device=w.device)
+        self.mul_t(gw, r, accumulate=False, stream=cur)
+        loss = 0.5 * torch.dot(r.double(), r.double())
+        cur.wait_stream(aux)                                   # the derivative products are done
+        gx, gy = r * dxw, w * dyr
+        return float(loss), gw, gx, gy
 
     @property
     def T(self):
@@ -399,7 +412,7 @@ class _Transposed:
     def __matmul__(self, v):
         import torch
         shape = (self.shape[0],) if v.dim() == 1 else (v.shape[1], self.shape[0])
-        u = torch.zeros(shape, dtype=v.dtype, device=v.device)
+        u = torch.empty(shape, dtype=v.dtype, device=v.device)        # overwritten (accumulate=False)
         if v.dim() == 2:
             u = u.t()
         return self.H.mul_t(u, v, accumulate=False)
