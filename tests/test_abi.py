@@ -46,3 +46,18 @@ def test_kernels_callable():
     np.testing.assert_allclose(hm.cauchykernel(x, y), 1 / (x - y))
     np.testing.assert_allclose(hm.logkernel(x, y), np.log(np.abs(x - y)))
     assert sorted(hm.KERNELS) == ["cauchykernel", "coulombkernel", "coulombprimekernel", "logkernel"]
+
+
+def test_null_arguments_rejected_without_a_gpu():
+    """Argument checks that happen before any CUDA call: NULL handles and
+    invalid counts return status codes (no GPU needed)."""
+    L = _lib.lib
+    assert L.hm_autotune(None, 1, 1, None, None, None) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_configure(None, _lib.HM_OPT_PDL, 1) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_mul(None, None, 0, None, 0, 1, 1, None) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_mul_noalloc(None, None, None, 1, None) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_mul_host(None, None, None, 1, 1) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_profile_timeline(None, None, 0) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_trtri_batched(_lib.HM_F64, -1, None, None) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_potrf_batched_async(_lib.HM_F64, 1, None, None, None) == _lib.HM_ERR_INVALID_ARG
+    assert L.hm_solve_transposed(_lib.HM_F64, -1, None, None, 0, 0, None) == _lib.HM_ERR_INVALID_ARG
