@@ -360,18 +360,21 @@ def test_very_uneven_sizes_raise_like_reference(nx, ny):
         hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("k", [1, 4])
 @pytest.mark.parametrize("accumulate", [False, True])
-def test_host_product_pinned_and_pageable(k, accumulate):
-    """hm_mul_host with host buffers: a page-locked destination is written by
-    the product's last kernel directly, a pageable one through a copy; both
-    equal the device product bit for bit, call after call."""
+def test_host_product_pinned_and_pageable(dtype, k, accumulate):
+    """hm_mul_host with host buffers: a page-locked source is read by the leaf
+    stage and a page-locked destination written by the product's last kernel
+    directly, pageable ones go through copies; all equal the device product
+    bit for bit, call after call."""
     n = 65536
     x, y = O.grid_points(n)
-    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=dtype)
+    tdt = torch.float32 if dtype == np.float32 else torch.float64
     g = torch.Generator().manual_seed(k)
-    B = torch.randn(k, n, generator=g, dtype=torch.float32)          # column-major n x k as k rows
-    U0 = torch.randn(k, n, generator=g, dtype=torch.float32)
+    B = torch.randn(k, n, generator=g, dtype=tdt)                    # column-major n x k as k rows
+    U0 = torch.randn(k, n, generator=g, dtype=tdt)
     ref = U0.clone().cuda().t()
     H.mul(ref, B.cuda().t(), accumulate=accumulate)
     ref = ref.t().cpu()
