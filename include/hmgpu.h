@@ -259,7 +259,9 @@ int hm_configure(hm_handle *h, int option, int64_t value);
    is being captured.  choice (host, 5 values, may be NULL) receives the
    chosen overlap, near kernel, near stages, tensor-core flag and PDL flag; ms (host, 2
    values, may be NULL) the chosen schedule's time per product and that of
-   the configured options. */
+   the configured options.  Like hm_configure, it changes the handle: do not
+   call it while products on the same handle are being issued from other
+   host threads. */
 int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice, double *ms);
 
 /* Allocation-free single right-hand-side product.  No counterpart in the
