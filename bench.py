@@ -469,6 +469,10 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=512,
+                    help="instances of the batch workload (512 in the configuration it reports)")
+    ap.add_argument("--only-batch", action="store_true",
+                    help="run only the batch workload and print its result (for profiling)")
     ap.add_argument("--autotune-reps", type=int, default=50,
                     help="products timed per candidate schedule by the autotuner (fewer for profiling runs)")
     args = ap.parse_args()
@@ -488,6 +492,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
         barrier = lambda: dist.barrier()  # noqa: E731
+
+    if args.only_batch:
+        print(json.dumps({"batch": run_batch(hm, torch, torch.device("cuda", local), args,
+                                             count=args.batch_instances)}), flush=True)
+        return 0
 
     n = args.n
     x, y = grid_points(n)
@@ -605,7 +614,7 @@ def main():
 
     batch = None
     if not args.no_variants and not args.no_batch:
-        batch = run_batch(hm, torch, dev, args)
+        batch = run_batch(hm, torch, dev, args, count=args.batch_instances)
     grad = None
     chol = None
     if not args.no_variants:
