@@ -433,6 +433,40 @@ def cholesky_cpu_baseline(hm, A, b):
             "sample": "oracle/algebra.py cholesky + solvetransposed (numpy, LAPACK leaves) on the same matrix, one run"}
 
 
+def stage_timeline(hm, torch, n, reps=50):
+    """Start and end of every stage of the FP32 headline product (CUDA events on
+    the stream that launches each stage, hm_profile_timeline), in microseconds
+    from the product's start, averaged over reps products, for each stream
+    schedule HM_OPT_OVERLAP 0-4.  Timing the tree stages records events between
+    their kernels, so these products run with plain launches."""
+    import ctypes
+    from hierarchicalmatrices import _lib
+    x, y = grid_points(n)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float32)
+    b = torch.randn(n, device="cuda", dtype=torch.float32)
+    u = torch.empty_like(b)
+    out = {}
+    for mode in (0, 1, 2, 3, 4):
+        H.set_overlap(mode)
+        for _ in range(20):
+            H.mul(u, b, accumulate=False)
+        torch.cuda.synchronize()
+        H.profile()
+        acc = {}
+        buf = np.zeros(3 * 16)
+        for _ in range(reps):
+            H.mul(u, b, accumulate=False)
+            cnt = _lib.lib.hm_profile_timeline(H.handle, buf.ctypes.data_as(ctypes.c_void_p), 16)
+            for i in range(min(cnt, 16)):
+                a = acc.setdefault(_lib.STAGES[int(buf[3 * i])], [0.0, 0.0])
+                a[0] += buf[3 * i + 1] * 1e3 / reps
+                a[1] += buf[3 * i + 2] * 1e3 / reps
+        H.profile([])
+        out[f"overlap{mode}"] = {k: [round(v[0], 1), round(v[1], 1)] for k, v in sorted(acc.items(), key=lambda kv: kv[1][0])}
+    H.free()
+    return out
+
+
 def run_grad(hm, torch, dev, args, n=65536):
     """L = 1/2 |H(x,y) w - t|^2 for a Cauchy KernelMatrix on n uniform sorted
     points, FP32: loss and dL/dw, dL/dx, dL/dy (forward product, transposed
@@ -473,6 +507,8 @@ def main():
                     help="instances of the batch workload (512 in the configuration it reports)")
     ap.add_argument("--only-batch", action="store_true",
                     help="run only the batch workload and print its result (for profiling)")
+    ap.add_argument("--timeline", action="store_true",
+                    help="print the headline product's stage timeline for each stream schedule (for profiling)")
     ap.add_argument("--autotune-reps", type=int, default=50,
                     help="products timed per candidate schedule by the autotuner (fewer for profiling runs)")
     args = ap.parse_args()
@@ -492,6 +528,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
         barrier = lambda: dist.barrier()  # noqa: E731
+
+    if args.timeline:
+        print(json.dumps({"timeline_us": stage_timeline(hm, torch, args.n)}), flush=True)
+        return 0
 
     if args.only_batch:
         print(json.dumps({"batch": run_batch(hm, torch, torch.device("cuda", local), args,
