@@ -78,3 +78,26 @@ def test_unassigned_and_foreign_blocks():
     H = hm.HierarchicalMatrix(2, 2)
     H[hm.Block(1), hm.Block(1)] = "not a block"              # ignored, as the generated setindex! does
     assert H.assigned[0, 0] == 0 and H.blocksize(1, 1, 1) == 0
+
+
+def test_cached_shape_follows_block_assignments():
+    """size(H) is cached between block assignments (it is read many times by
+    the algebra's walks); assigning a block anywhere, also inside a child,
+    makes the parent report the new size (src/hierarchical.jl:33-47)."""
+    rng = np.random.default_rng(3)
+    inner = hm.HierarchicalMatrix(2, 2)
+    for i, j in ((1, 1), (1, 2), (2, 1), (2, 2)):
+        inner[hm.Block(i), hm.Block(j)] = rng.standard_normal((2, 3))
+    H = hm.HierarchicalMatrix(2, 2)
+    H[hm.Block(1), hm.Block(1)] = inner
+    H[hm.Block(1), hm.Block(2)] = rng.standard_normal((4, 5))
+    H[hm.Block(2), hm.Block(1)] = rng.standard_normal((1, 6))
+    H[hm.Block(2), hm.Block(2)] = rng.standard_normal((1, 5))
+    assert H.shape == (5, 11)
+    assert H.shape == (5, 11)                       # served from the cache
+    inner[hm.Block(2), hm.Block(1)] = rng.standard_normal((7, 3))     # a child's block changes
+    H[hm.Block(1), hm.Block(2)] = rng.standard_normal((9, 5))         # rows come from block column 2
+    assert inner.shape == (4, 6)
+    assert H.shape == (10, 11)
+    inner[hm.Block(1), hm.Block(1)] = rng.standard_normal((2, 10))    # widens block row 1 of the child
+    assert H.shape == (10, 18)                      # the parent sees the child's change
