@@ -171,9 +171,11 @@ def rel_err_sampled(H, u, b64, rows, torch):
 
 # ----------------------------------------------------------------- CPU baseline
 
-def cpu_baseline(n, budget_s=25.0, threads=None):
+def cpu_baseline(n, budget_s=25.0, threads=None, single_core=True):
     """The oracle (CPU restatement of the reference, reference layout and loop
-    order) timed on this host: build once, then full matvecs until ~budget_s."""
+    order) timed on this host: build once, then full matvecs on all host
+    threads until ~budget_s, and (single_core) a few on one thread -- the
+    reference itself is single-threaded Julia."""
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
     avail = None
@@ -194,44 +196,51 @@ def cpu_baseline(n, budget_s=25.0, threads=None):
     build_s = time.perf_counter() - t0
     b = np.random.default_rng(7).standard_normal(n_run)
     u = np.zeros(n_run)
-    H.mul(u, b, nthreads=threads)          # warm-up
-    times = []
-    t_end = time.perf_counter() + budget_s
-    while len(times) < 2 or (time.perf_counter() < t_end and len(times) < 20):
-        u[:] = 0
-        t0 = time.perf_counter()
-        H.mul(u, b, nthreads=threads)
-        times.append(time.perf_counter() - t0)
-    med = statistics.median(times)
+
+    def timed(nthr, budget, least, most):
+        H.mul(u, b, nthreads=nthr)          # warm-up
+        times = []
+        t_end = time.perf_counter() + budget
+        while len(times) < least or (time.perf_counter() < t_end and len(times) < most):
+            u[:] = 0
+            t0 = time.perf_counter()
+            H.mul(u, b, nthreads=nthr)
+            times.append(time.perf_counter() - t0)
+        return statistics.median(times), len(times)
+
+    med, cnt = timed(threads, budget_s, 2, 20)
     st = H.stats()
-    value = 1.0 / med
-    scaled = n_run != n
-    if scaled:
+    scale = 1.0
+    if n_run != n:
         # scale by the reference-layout values streamed per matvec at full size
         from hierarchicalmatrices import Plan
         xf, yf = grid_points(n)
-        full = Plan(xf, yf, 1.0, 0.0, 1.0, 0.0).sizes["reference_values"]
-        value = value * st["stored_values"] / full
+        scale = st["stored_values"] / Plan(xf, yf, 1.0, 0.0, 1.0, 0.0).sizes["reference_values"]
     sample = (f"oracle KernelMatrix n={n_run} grid, reference per-block layout "
-              f"({st['stored_values']} values), {len(times)} full matvecs after 1 warm-up, "
+              f"({st['stored_values']} values), {cnt} full matvecs on {threads} threads after 1 warm-up, "
               f"median {med * 1e3:.1f} ms; build {build_s:.1f} s")
-    if scaled:
+    if n_run != n:
         sample += f"; scaled to n={n} by reference-layout values (host memory)"
-    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    out = {"value": scale / med, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    if single_core:
+        med1, cnt1 = timed(1, 0.0, 3, 3)
+        out["single_core"] = {
+            "value": scale / med1, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"the same matrix and vector, {cnt1} full matvecs on 1 thread after 1 warm-up, "
+                      f"median {med1 * 1e3:.1f} ms (the reference is single-threaded)"}
+    return out
 
 
-def workload_config(n, world, stored_bytes=None):
-    """The headline workload as both arms report it."""
-    cfg = {
+def workload_config(n, world):
+    """The headline workload as both arms report it (the same keys and values)."""
+    return {
         "workload": "KernelMatrix Cauchy 1/(x-y), n=2^20 interleaved grid (descending, "
                     "a=c=1, b=d=0), rank 20, leaf 80, FP64 compression, FP32 factors/leaves, "
                     "1 RHS per step",
         "n": n, "rank": 20, "blocksize": 80, "nrhs": 1, "parallelism": f"replicas{world}",
+        "l2": "inputs larger than L2 every step: the factors streamed per product (1.14 GB in FP32, "
+              "14 GB in the reference's FP64 per-block layout at n=2^20) exceed the 129 MB L2; no flush",
     }
-    if stored_bytes is not None:
-        cfg["l2"] = (f"inputs larger than L2: {stored_bytes / 1e9:.2f} GB of factors per step "
-                     f"vs {L2_BYTES / 1e6:.0f} MB L2")
-    return cfg
 
 
 def run_reference(args):
@@ -247,6 +256,8 @@ def run_reference(args):
         "ms_per_step": 1e3 / cb["value"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args.n, args.gpus),
+        "precision_note": "the reference computes in FP64 (its only CPU path); the GPU arm's headline is FP32 "
+                          "storage from FP64 compression, and its FP64 product is under variants.fp64_k1",
         "reference_path": "the oracle's restatement of the reference's KernelMatrix product (reference "
                           "per-block layout and loop order, FP64) on the host cores; Julia is not installed",
         "cpu_baseline": cb,
@@ -290,7 +301,7 @@ def run_batch(hm, torch, dev, args, count=512, nrhs=8):
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g, stream=cs):
         Hb.mul(U, B, accumulate=False, stream=cs)
-    reps = max(10, min(200, args.steps // 5))
+    reps = max(10, args.steps)
     for _ in range(3):
         g.replay()
     torch.cuda.synchronize()
@@ -603,7 +614,7 @@ def main():
 
     variants = {}
     if not args.no_variants:
-        k_steps = max(3, args.steps // 5)
+        k_steps = max(3, args.steps)
         # plain FP64 product
         t0 = time.perf_counter()
         H64 = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=np.float64)
@@ -615,11 +626,24 @@ def main():
         st64s = serial_stages(H64, lambda: H64.mul(u64, b64, accumulate=False), 10, torch)
         err64 = rel_err_sampled(H64, u64, b64, rows, torch)
         st64 = H64.stats()
+        # end to end through hm_mul_host with page-locked host buffers, as the headline's e2e
+        hb64 = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        hb64.copy_(b64.cpu())
+        hu64 = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        hb64_np, hu64_np = hb64.numpy(), hu64.numpy()
+        for _ in range(max(3, args.warmup)):
+            H64.mul_host(hu64_np, hb64_np, accumulate=False)
+        t0 = time.perf_counter()
+        for _ in range(k_steps):
+            H64.mul_host(hu64_np, hb64_np, accumulate=False)
+        e2e64 = k_steps / (time.perf_counter() - t0)
         variants["fp64_k1"] = {
             "matvec_per_s": 1e3 / ms64, "ms": ms64, "rel_err_vs_dense_fp64": err64,
             "stored_GBs": (st64["stored_values"] * 8 + 2 * n * 8) / (ms64 * 1e-3) / 1e9,
             "effective_canonical_GBs": (st64["canonical_values"] * 8 + 2 * n * 8) / (ms64 * 1e-3) / 1e9,
-            "build_s": build64_s, "stage_ms_serial": st64s, "schedule": sched64}
+            "build_s": build64_s, "stage_ms_serial": st64s, "schedule": sched64, "steps": k_steps,
+            "e2e": {"value": e2e64, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
+                    "api": "hm_mul_host, page-locked host buffers"}}
         del H64, u64
         torch.cuda.empty_cache()
         # clustered points: Beta(1/2, 1/2), FP64 (a deeper, uneven tree)
@@ -644,7 +668,7 @@ def main():
             B = torch.randn(k, n, device=dev, dtype=torch.float32).t()    # column-major n x k
             U = torch.empty(k, n, device=dev, dtype=torch.float32).t()
             schedk = H32.autotune(k, reps=10 if k <= 32 else 4)
-            msk = time_device(lambda: H32.mul(U, B, accumulate=False), max(3, k_steps // 2), 2, torch)
+            msk = time_device(lambda: H32.mul(U, B, accumulate=False), k_steps, 3, torch)
             stk = serial_stages(H32, lambda: H32.mul(U, B, accumulate=False), 3, torch)
             errk = rel_err_sampled(H32, U[:, k - 1].contiguous(), B[:, k - 1].to(torch.float64).contiguous(),
                                    rows, torch)
@@ -678,7 +702,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(n, world, stored_bytes),
+            "config": workload_config(n, world),
             "rel_err_vs_dense_fp64": err32,
             "hbm_GBs_stored": stored_bytes / (ms * 1e-3) / 1e9,
             "hbm_GBs_effective_canonical": canonical_bytes / (ms * 1e-3) / 1e9,
@@ -689,6 +713,9 @@ def main():
                            "expand_part<float,float,false,2> (near-field panels, one warp per row segment)"),
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": profiled_traffic(n), "traffic_unit": "GB per launch",
+                "traffic_source": "not measured in this run: ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                  "one launch of this kernel on this workload, from the committed profile "
+                                  "profiles/expand_near_kernelmatrix_cauchy_n2p20_fp32.md",
                 "peak_source": peak_kind, "kernel_ms": exp_ms, "kernel_bytes": exp_bytes,
                 "stage_ms_serial": stages,
             },

@@ -671,7 +671,7 @@ struct Staged {
     int put(const T *host, size_t count, T **dev)
     {
         void *p = nullptr;
-        ALG_CK(cudaMallocAsync(&p, std::max<size_t>(count, 1) * sizeof(T), st));
+        ALG_CK(device_malloc_async(&p, std::max<size_t>(count, 1) * sizeof(T), st));
         ptrs.push_back(p);
         if (count) ALG_CK(cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, st));
         *dev = static_cast<T *>(p);
@@ -681,7 +681,7 @@ struct Staged {
     int zeros(size_t count, T **dev)
     {
         void *p = nullptr;
-        ALG_CK(cudaMallocAsync(&p, std::max<size_t>(count, 1) * sizeof(T), st));
+        ALG_CK(device_malloc_async(&p, std::max<size_t>(count, 1) * sizeof(T), st));
         ptrs.push_back(p);
         *dev = static_cast<T *>(p);
         return HM_OK;

@@ -48,6 +48,30 @@ void set_last_error(const char *fmt, ...)
     g_last_error = buf;
 }
 void clear_last_error() { g_last_error.clear(); }
+
+namespace {
+// hm_debug_fail_alloc: allocations left to succeed before one fails, or -1
+std::atomic<int64_t> g_fail_alloc{-1};
+bool hook_fails()
+{
+    int64_t v = g_fail_alloc.load();
+    while (v >= 0) {
+        if (g_fail_alloc.compare_exchange_weak(v, v - 1)) return v == 0;   // 0 -> -1: this one fails
+    }
+    return false;
+}
+}  // namespace
+
+cudaError_t device_malloc(void **p, size_t bytes)
+{
+    if (hook_fails()) { *p = nullptr; return cudaErrorMemoryAllocation; }
+    return cudaMalloc(p, bytes);
+}
+cudaError_t device_malloc_async(void **p, size_t bytes, cudaStream_t stream)
+{
+    if (hook_fails()) { *p = nullptr; return cudaErrorMemoryAllocation; }
+    return cudaMallocAsync(p, bytes, stream);
+}
 }  // namespace hm
 
 namespace {
@@ -147,6 +171,7 @@ inline int sched_bucket(int k)
 
 struct hm_handle {
     int kernel = 0, storage = HM_F64, r = 0;
+    int device = -1;               // the device current when the handle was built
     int swap = 0;                  // 1: this handle holds the transpose of the kernel matrix
     int ninst = 1;                 // instances of a batched (block-diagonal) handle
     hm_fill_seg *d_seg_fill = nullptr;
@@ -197,6 +222,11 @@ struct hm_handle {
     int part_segs[2] = {0, 0};      // most segments of one CTA (near / far)
     int part_pieces[2] = {0, 0};    // most piece records of one CTA
     int *d_status = nullptr;        // device-side status word (HM_DEV_*), 0 when clean
+    // bounded waits of the streamed and tensor-core panel kernels give up after
+    // this long (HM_OPT_WAIT_LIMIT_NS); test_stall (HM_OPT_TEST_STALL) makes the
+    // first wait of every CTA run out, to exercise the give-up path
+    unsigned long long wait_ns = 2000000000ull;
+    int test_stall = 0;
     bool tc_ok = false;             // segments fit the tensor-core panel kernel
     bool tensor_cores = true;       // use it for FP32 products with many right-hand sides
 
@@ -259,7 +289,7 @@ struct hm_handle {
         *p = nullptr;
         if (count == 0) return HM_OK;
         void *q = nullptr;
-        HM_CK(cudaMalloc(&q, count * sizeof(T)));
+        HM_CK(device_malloc(&q, count * sizeof(T)));
         allocs.push_back(q);
         device_bytes += (int64_t)(count * sizeof(T));
         *p = static_cast<T *>(q);
@@ -634,7 +664,7 @@ int stream_ctx(hm_handle *h, cudaStream_t st, size_t bytes, hm_handle::StreamCtx
     if (sc.bytes < bytes) {
         if (sc.p) HM_CK(cudaFreeAsync(sc.p, st));
         sc.p = nullptr; sc.bytes = 0;
-        HM_CK(cudaMallocAsync(&sc.p, bytes, st));
+        HM_CK(device_malloc_async(&sc.p, bytes, st));
         sc.bytes = bytes;
     }
     *out = &sc;
@@ -837,7 +867,7 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
             stream_part<S, A, FAR, KB><<<h->stream_ctas, kStreamThreads, smem, st>>>(
                 ma, h->d_segs, h->d_cta_seg + (FAR ? h->stream_ctas + 1 : 0), h->d_pieces,
                 static_cast<const S *>(panels), s, t, h->r, nst, gcap, ngb, h->part_segs[part], yfar,
-                h->d_status);
+                h->d_status, h->wait_ns, h->test_stall);
             HM_CK_LAUNCH(FAR ? "stream_far" : "stream_near");
             return HM_OK;
         }
@@ -885,7 +915,7 @@ int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, 
             // right-hand-side chunks of a segment run next to each other (its panel is re-read from L2)
             const dim3 grid((unsigned)((ma.k + 127) / 128), (unsigned)h->n_segs);
             expand_tc<<<grid, 256, smem, st>>>(ma, h->d_segs, h->d_pieces, static_cast<const float *>(panels), s, t,
-                                               h->r, maxw, h->d_status);
+                                               h->r, maxw, h->d_status, h->wait_ns, h->test_stall);
             HM_CK_LAUNCH("expand_tc");
             return HM_OK;
         }
@@ -1103,8 +1133,8 @@ int autotune(hm_handle *h, int k, int reps, cudaStream_t st, int32_t *choice, do
     const size_t nv = (size_t)h->ny * k, nu = (size_t)h->nx * k;
     S *v = nullptr, *u = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    int rc = cuda_status(cudaMallocAsync(&v, std::max<size_t>(nv, 1) * sizeof(S), st), "cudaMallocAsync");
-    if (!rc) rc = cuda_status(cudaMallocAsync(&u, std::max<size_t>(nu, 1) * sizeof(S), st), "cudaMallocAsync");
+    int rc = cuda_status(device_malloc_async((void **)&v, std::max<size_t>(nv, 1) * sizeof(S), st), "cudaMallocAsync");
+    if (!rc) rc = cuda_status(device_malloc_async((void **)&u, std::max<size_t>(nu, 1) * sizeof(S), st), "cudaMallocAsync");
     // finite, normal inputs (0x3f bytes); the kernels' time does not depend on the values
     if (!rc) rc = cuda_status(cudaMemsetAsync(v, 0x3f, nv * sizeof(S), st), "cudaMemsetAsync");
     if (!rc) rc = cuda_status(cudaEventCreate(&e0), "cudaEventCreate");
@@ -1440,6 +1470,7 @@ int build_from_plan(int kernel, int swap, hm_plan *pl, const double *x, const do
     const std::vector<double> &cheb = pl->cheb, &lam = pl->lam, &T = pl->T;
 
     hm_handle *h = new hm_handle();
+    cudaGetDevice(&h->device);
     h->kernel = kernel; h->storage = storage; h->r = rank; h->nx = nx; h->ny = ny; h->swap = swap;
     h->stats = P.stats;
     h->n_xslots = P.n_xslots; h->n_yslots = P.n_yslots; h->max_width = P.max_width;
@@ -1524,6 +1555,7 @@ int hm_hier_build(int storage, int64_t m, int64_t n, int nblocks, const int32_t 
         return HM_ERR_UNSUPPORTED;
     }
     hm_handle *h = new hm_handle();
+    cudaGetDevice(&h->device);
     h->kernel = -1; h->storage = storage; h->r = P.r; h->nx = m; h->ny = n;
     h->stats = P.stats;
     h->n_xslots = P.n_xslots; h->n_yslots = P.n_yslots; h->max_width = P.max_width;
@@ -1588,7 +1620,7 @@ static int lowrank_mul_t(int adjoint, const T *U, const T *core, int core_diag, 
     const int64_t rin = adjoint ? m : n, rout = adjoint ? n : m;
     if (r == 0 || rout == 0) return HM_OK;
     T *t = nullptr;
-    HM_CK(cudaMallocAsync((void **)&t, sizeof(T) * r, st));
+    HM_CK(device_malloc_async((void **)&t, sizeof(T) * r, st));
     lr_project<T><<<(unsigned)((r * 32 + 255) / 256), 256, 0, st>>>(Win, rin, rin, r, x, incx, t);
     int e = cuda_status(cudaGetLastError(), "lr_project");
     if (!e) {
@@ -1638,7 +1670,7 @@ int hm_bary_factors(int kernel, int rank, double a, double b, double c, double d
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double *dbuf = nullptr;
     const size_t nbuf = 2 * (size_t)rank + nx + ny;
-    HM_CK(cudaMallocAsync((void **)&dbuf, sizeof(double) * std::max<size_t>(nbuf, 1), st));
+    HM_CK(device_malloc_async((void **)&dbuf, sizeof(double) * std::max<size_t>(nbuf, 1), st));
     int e = cuda_status(cudaMemcpyAsync(dbuf, cheb.data(), sizeof(double) * rank, cudaMemcpyHostToDevice, st), "copy");
     if (!e) e = cuda_status(cudaMemcpyAsync(dbuf + rank, lam.data(), sizeof(double) * rank, cudaMemcpyHostToDevice, st), "copy");
     if (!e && nx) e = cuda_status(cudaMemcpyAsync(dbuf + 2 * rank, x, sizeof(double) * nx, cudaMemcpyHostToDevice, st), "copy");
@@ -1789,7 +1821,7 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
         if (h->stage_bytes < bv + bu) {
             if (h->d_stage) HM_CK(cudaFree(h->d_stage));
             h->d_stage = nullptr; h->stage_bytes = 0;
-            HM_CK(cudaMalloc(&h->d_stage, bv + bu));
+            HM_CK(device_malloc(&h->d_stage, bv + bu));
             h->stage_bytes = bv + bu;
         }
     }
@@ -1853,9 +1885,20 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
                   "scratch holds %u bytes (use hm_mul)", need, (unsigned)HM_NOALLOC_SCRATCH_BYTES);
         return HM_ERR_UNSUPPORTED;
     }
+    int dev = -1;
+    HM_CK(cudaGetDevice(&dev));
+    if (dev != h->device) {
+        set_error("hm_mul_noalloc: the handle was built on device %d, device %d is current", h->device, dev);
+        return HM_ERR_INVALID_ARG;
+    }
     void *scratch = nullptr;
     HM_TRY(noalloc_scratch(&scratch));
-    // every stage runs in order on the caller's stream: no side stream, no event
+    // the schedule hm_mul would use for one right-hand side (the autotuned one
+    // when there is one), with every stage in order on the caller's stream:
+    // no side stream, no event
+    Sched sched = sched_for(h, 1);
+    sched.overlap = 0;
+    SchedScope scope(&sched);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (h->storage == HM_F64) {
         MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, h->ny, 1, h->nx, 1,
@@ -1865,6 +1908,13 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
     MulArgs<float> ma{static_cast<const float *>(v), static_cast<float *>(u), 1, h->ny, 1, h->nx, 1,
                       accumulate ? 1 : 0};
     return launch_pipeline<float, float>(h, ma, st, st, nullptr, nullptr, scratch, false);
+}
+
+int hm_debug_fail_alloc(int64_t after)
+{
+    if (after < -1) { set_error("hm_debug_fail_alloc: after must be >= -1"); return HM_ERR_INVALID_ARG; }
+    hm::g_fail_alloc.store(after);
+    return HM_OK;
 }
 
 int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice, double *ms)
@@ -1885,6 +1935,19 @@ int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice,
 int hm_configure(hm_handle *h, int option, int64_t value)
 {
     if (!h) return HM_ERR_INVALID_ARG;
+    // options of the bounded waits: no schedule changes, tuned schedules kept
+    // (the host-buffer graph holds the old kernel arguments: dropped)
+    if (option == HM_OPT_WAIT_LIMIT_NS || option == HM_OPT_TEST_STALL) {
+        if (option == HM_OPT_WAIT_LIMIT_NS && (value < 1 || value > 2000000000)) {
+            set_error("HM_OPT_WAIT_LIMIT_NS must be in [1, 2e9]");
+            return HM_ERR_INVALID_ARG;
+        }
+        drop_host_graph(h);
+        if (option == HM_OPT_WAIT_LIMIT_NS) h->wait_ns = (unsigned long long)value;
+        else h->test_stall = value != 0 ? 1 : 0;
+        if (h->trans) return hm_configure(h->trans, option, value);
+        return HM_OK;
+    }
     switch (option) {
     case HM_OPT_OVERLAP:
         if (value < 0 || value > 4) { set_error("HM_OPT_OVERLAP must be in [0, 4]"); return HM_ERR_INVALID_ARG; }

@@ -55,6 +55,19 @@ __device__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned long long lim
         if ((it & 1023) == 0 && global_ns() - t0 > limit_ns) return false;   // the clock, now and then
     }
 }
+// The first wait of a CTA in the kernels with bounded waits: on `bar`, or,
+// when `stall` is set (the handle's test hook for the timeout path), on
+// `never`, a barrier that nothing arrives on, so that the wait runs out after
+// limit_ns and the kernel takes its give-up path.  Later waits use `bar`.
+__device__ __forceinline__ bool mbar_wait_first(uint64_t *bar, uint32_t parity, unsigned long long limit_ns,
+                                                bool &stall, uint64_t *never)
+{
+    if (stall) {
+        stall = false;
+        return mbar_wait(never, 0, limit_ns);
+    }
+    return mbar_wait(bar, parity, limit_ns);
+}
 // bytes (a multiple of 16) from 16-byte aligned global src to 16-byte
 // aligned shared dst, completing on bar.
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)

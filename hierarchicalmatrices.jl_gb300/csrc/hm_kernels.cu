@@ -975,14 +975,17 @@ __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf)
 // chunk's columns with plain FMA and folds the chunk's partial into a
 // compensated (TwoSum) pair.  The gathered right-hand sides of the next
 // segment are fetched with cp.async while the current one streams.  Every
-// wait is bounded: after kWaitLimitNs the CTA records HM_DEV_WAIT_TIMEOUT in
-// *status, waits (bounded) for its copies in flight and returns.
+// wait is bounded: after wait_ns (the handle's HM_OPT_WAIT_LIMIT_NS) the CTA
+// records HM_DEV_WAIT_TIMEOUT in *status, waits (bounded by kDrainLimitNs) for
+// its copies in flight and returns.  stall != 0 (a test hook) makes the first
+// wait of every CTA run out.
 
 
 template <typename S, typename A, bool FAR, int KB>
 __global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? (sizeof(S) == 4 ? 2 : 1) : 3)   // registers of 4+ right-hand sides
     stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_seg, const hm_piece *pieces, const S *P,
-                const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs, S *yfar, int *status)
+                const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs, S *yfar, int *status,
+                unsigned long long wait_ns, int stall)
 {
     static_assert(sizeof(S) == sizeof(A), "right-hand sides are copied into shared memory as they are");
     // rows per thread: one 16-byte load; FP32 with 4+ right-hand sides takes 2
@@ -1006,7 +1009,8 @@ __global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? (sizeof(S) == 4 ? 2 
     const int k = ma.k;
     unsigned char *ring = stream_smem;
     uint64_t *full = reinterpret_cast<uint64_t *>(stream_smem + (size_t)nst * kChunkBytes);
-    A *gbuf = reinterpret_cast<A *>(full + nst);
+    uint64_t *never = full + nst;                              // nothing arrives on it (stall hook)
+    A *gbuf = reinterpret_cast<A *>(full + nst + 1);
     A *red = gbuf + ngb * gcap * KB;                           // [warp][row][q][hi, lo]
     // the CTA's segment and piece records, staged once (records of one CTA
     // are consecutive in both arrays)
@@ -1082,7 +1086,7 @@ __global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? (sizeof(S) == 4 ? 2 
     };
 
     if (tid == 0) {
-        for (int i = 0; i < nst; ++i) mbar_init(&full[i], 1);
+        for (int i = 0; i <= nst; ++i) mbar_init(&full[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     // right-hand sides run ngb - 1 segments ahead (one cp.async group per segment)
@@ -1099,6 +1103,7 @@ __global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? (sizeof(S) == 4 ? 2 
     int stage = 0, consumed = 0;
     uint32_t phase = 0;
     bool abort = false;
+    bool stall_first = stall != 0;
     for (int j = seg_lo; j < seg_hi && !abort; ++j) {
         async_wait_pending(ngb - 2);
         __syncthreads();                      // g of segment j visible; g and partials of j - 1 read
@@ -1133,7 +1138,7 @@ __global__ void __launch_bounds__(kStreamThreads, KB >= 4 ? (sizeof(S) == 4 ? 2 
         int nchunk = 0;
         for (int c0 = cb; c0 < ce; c0 += CC) {
             const int cols = min(CC, ce - c0);
-            const bool ok = mbar_wait(&full[stage], phase, kWaitLimitNs);
+            const bool ok = mbar_wait_first(&full[stage], phase, wait_ns, stall_first, never);
             if (ok && live) {
                 const S *st = reinterpret_cast<const S *>(ring + (size_t)stage * kChunkBytes);
 #pragma unroll
@@ -1387,10 +1392,12 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
 #define HM_INST_STREAM(S, A, KB)                                                                      \
     template __global__ void stream_part<S, A, false, KB>(MulArgs<S>, const hm_seg *, const int *,       \
                                                           const hm_piece *, const S *, const A *, const A *, \
-                                                          int, int, int, int, int, S *, int *);         \
+                                                          int, int, int, int, int, S *, int *,          \
+                                                          unsigned long long, int);                     \
     template __global__ void stream_part<S, A, true, KB>(MulArgs<S>, const hm_seg *, const int *,        \
                                                          const hm_piece *, const S *, const A *, const A *,  \
-                                                         int, int, int, int, int, S *, int *);
+                                                         int, int, int, int, int, S *, int *,           \
+                                                         unsigned long long, int);
 #define HM_INST_MV(S, A)                                                                             \
     template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int, int, int); \
     template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int, int, int); \

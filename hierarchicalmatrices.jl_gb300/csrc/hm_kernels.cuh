@@ -14,6 +14,13 @@ namespace hm {
 void set_last_error(const char *fmt, ...);
 void clear_last_error();
 
+// Every device allocation of the library goes through these (hm_api.cu), so
+// that the test hook hm_debug_fail_alloc can make one of them fail with
+// cudaErrorMemoryAllocation without calling CUDA.  stream == nullptr in
+// device_malloc_async means the legacy default stream, as in CUDA.
+cudaError_t device_malloc(void **p, size_t bytes);
+cudaError_t device_malloc_async(void **p, size_t bytes, cudaStream_t stream);
+
 // ---------------------------------------------------------------- numerics
 
 // Kernels of examples/Kernel.jl:34-37, evaluated in FP64 with every operation
@@ -200,26 +207,30 @@ __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf);
 constexpr int kStreamThreads = 256;
 constexpr int kChunkBytes = 8192;
 constexpr int HM_DEV_WAIT_TIMEOUT = 1;    // *status: a stage copy did not complete in time
-// Shared memory of stream_part: the stage ring, its mbarriers, ngb (2..4)
+// Shared memory of stream_part: the stage ring, its mbarriers (and one that
+// nothing arrives on, for the stall hook), ngb (2..4)
 // gathered right-hand-side buffers, the column-group partials and the CTA's segment
 // and piece records (at most dsegs and dpieces of them).
 __host__ __device__ constexpr size_t stream_smem_bytes(int nst, int gcap, int ngb, int kb, int asize, int dsegs,
                                                        int dpieces)
 {
-    return (size_t)nst * kChunkBytes + (size_t)nst * 8 + (size_t)ngb * gcap * kb * asize +
+    return (size_t)nst * kChunkBytes + (size_t)(nst + 1) * 8 + (size_t)ngb * gcap * kb * asize +
            (size_t)8 * 64 * kb * 2 * asize + (size_t)dsegs * sizeof(hm_seg) + (size_t)dpieces * sizeof(hm_piece);
 }
 template <typename S, typename A, bool FAR, int KB>
 __global__ void stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_seg, const hm_piece *pieces,
                             const S *P, const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs,
-                            S *yfar, int *status);
+                            S *yfar, int *status, unsigned long long wait_ns, int stall);
 
 // Tensor-core panels for many right-hand sides (FP32 storage): grid
 // (ceil(k / 128), segments), 256 threads, expand_tc_smem_bytes(maxw) of shared
 // memory; needs segments of <= 64 rows, ld % 4 == 0, poff % 32 == 0.
+// Waits on the tensor core give up after wait_ns (HM_DEV_WAIT_TIMEOUT in
+// *status); stall != 0 makes each CTA's first wait run out (test hook).
 size_t expand_tc_smem_bytes(int maxw);
 __global__ void expand_tc(MulArgs<float> ma, const hm_seg *segs, const hm_piece *pieces, const float *P,
-                          const float *s, const float *t, int r, int maxw, int *status);
+                          const float *s, const float *t, int r, int maxw, int *status, unsigned long long wait_ns,
+                          int stall);
 
 template <typename S, typename A>
 __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *pieces, const S *P, const A *s,

@@ -48,6 +48,7 @@ struct TcSmem {
     uint32_t G3[3][TC_M * TC_KC / 2];      // BF16 pieces h, m, l of G, K-major core-matrix layout
     uint32_t P3[3][TC_N * TC_KC / 2];      // BF16 pieces of P^T
     uint64_t mma_bar;
+    uint64_t never_bar;                    // nothing arrives on it (stall hook)
     uint32_t tmem_base;
 };
 // followed in shared memory by the segment's column table: for each panel
@@ -135,7 +136,7 @@ size_t expand_tc_smem_bytes(int maxw)
 
 __global__ void __launch_bounds__(TC_THREADS, 2)
     expand_tc(MulArgs<float> ma, const hm_seg *segs, const hm_piece *pieces, const float *P, const float *s,
-              const float *t, int r, int maxw, int *status)
+              const float *t, int r, int maxw, int *status, unsigned long long wait_ns, int stall)
 {
     extern __shared__ __align__(128) unsigned char tc_smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(tc_smem_raw);
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     }
     if (tid == 0) {
         mbar_init(&S.mma_bar, 1);
+        mbar_init(&S.never_bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     tc_fence_before();
@@ -213,6 +215,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 
     const uint32_t idesc = umma_idesc_bf16(TC_M, TC_N);
     bool ok = true;
+    bool stall_first = stall != 0;
     int committed = -1;                                         // last chunk whose MMAs were committed
     if (nch > 0) load_raw(0, 0);
     for (int ch = 0; ch < nch; ++ch) {
@@ -224,7 +227,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             async_wait_all();
         }
         // the previous chunk's MMAs read the operand buffers: wait for them
-        if (ch > 0 && !mbar_wait(&S.mma_bar, (ch - 1) & 1, kWaitLimitNs)) ok = false;
+        if (ch > 0 && !mbar_wait_first(&S.mma_bar, (ch - 1) & 1, wait_ns, stall_first, &S.never_bar)) ok = false;
         if (__syncthreads_or(!ok)) break;                       // raw chunk visible to all threads
         tc_fence_after();
         const int c0 = ch * TC_KC, cols = min(TC_KC, W - c0);
@@ -276,7 +279,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         committed = ch;
     }
     // all MMAs done before reading D
-    if (ok && committed >= 0 && !mbar_wait(&S.mma_bar, committed & 1, kWaitLimitNs)) ok = false;
+    if (ok && committed >= 0 && !mbar_wait_first(&S.mma_bar, committed & 1, wait_ns, stall_first, &S.never_bar))
+        ok = false;
     if (__syncthreads_or(!ok)) {
         async_wait_all();
         if (tid == 0) {

@@ -9,7 +9,7 @@ and ``mul_`` (Julia's ``mul!``), the low-rank and blockwise arithmetic and
 src/algebra.jl, src/cholesky.jl).  All products and block arithmetic run CUDA
 kernels compiled for sm_103a in libhmgpu.so.
 """
-from ._lib import HMError, Plan
+from ._lib import DeviceWaitTimeout, HMError, Plan
 from .hierarchical import (AbstractHierarchical, Adjoint, BarycentricMatrix2D, Block, EvenBarycentricMatrix,
                            HierarchicalMatrix, LowRankMatrix, Transpose, adjoint, hierarchical, mul_, transpose)
 from .algebra import (Diagonal, getrank, hierarchicalcholesky, lrzeros, solvetransposed, svdtrunc, times,
@@ -18,7 +18,8 @@ from .kernelmatrix import (BLOCKRANK, BLOCKSIZE, KERNELS, KernelMatrix, KernelMa
                            coulombkernel, coulombprimekernel, indsplit, logkernel)
 
 __all__ = [
-    "AbstractHierarchical", "Adjoint", "BLOCKRANK", "BLOCKSIZE", "BarycentricMatrix2D", "Block", "Diagonal",
+    "AbstractHierarchical", "Adjoint", "BLOCKRANK", "BLOCKSIZE", "BarycentricMatrix2D", "Block", "DeviceWaitTimeout",
+    "Diagonal",
     "EvenBarycentricMatrix", "HMError", "getrank", "hierarchicalcholesky", "lrzeros", "solvetransposed", "svdtrunc",
     "times", "todense",
     "HierarchicalMatrix", "KERNELS", "KernelMatrix", "KernelMatrixBatch", "LowRankMatrix", "Plan", "Transpose",

@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import check, lib
+from ._lib import DeviceWaitTimeout, check, lib
 
 _vp = ctypes.c_void_p
 
@@ -149,6 +149,25 @@ class KernelMatrix:
         code = ctypes.c_int(0)
         check(lib.hm_device_status(self._h, ctypes.byref(code), 1 if reset else 0))
         return code.value
+
+    def check_device(self):
+        """Raises DeviceWaitTimeout (and clears the word) when a kernel of
+        this handle gave up a bounded wait since the last check: the products
+        issued since then are invalid.  Synchronises the device."""
+        code = self.device_status(reset=True)
+        if code:
+            raise DeviceWaitTimeout(
+                f"a kernel of this KernelMatrix gave up waiting (device status {code}): its products are invalid")
+
+    def set_wait_limit(self, ns):
+        """Nanoseconds (1 .. 2e9, default 2e9) after which a wait of the
+        streamed near-field or tensor-core panel kernel gives up."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_WAIT_LIMIT_NS, int(ns)))
+
+    def _set_test_stall(self, enable):
+        """Test hook: the first wait of every CTA of those kernels waits on a
+        barrier nothing arrives on, so it runs out after the wait limit."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_TEST_STALL, 1 if enable else 0))
 
     @property
     def handle(self):

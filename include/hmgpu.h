@@ -225,8 +225,8 @@ enum {
     HM_OPT_NEAR_STAGES = 2,
     /* HM_OPT_TENSOR_CORES (default 1): FP32 products with 16 or more
        right-hand sides run their row-segment panels on the tensor cores
-       (three TF32 products per step, FP32 accumulation); 0 keeps them on the
-       FP32 pipes. */
+       (every FP32 value split exactly into three BF16 pieces, six products
+       per step, FP32 accumulation); 0 keeps them on the FP32 pipes. */
     HM_OPT_TENSOR_CORES = 3,
     /* HM_OPT_NEAR_KERNEL (default 0): near-field panels with up to 8
        right-hand sides on 0 or 1 = one warp per row segment, 2 = CTAs
@@ -241,7 +241,20 @@ enum {
        the kernel before them on the stream, so that each is scheduled while
        its predecessor finishes and stages its constant inputs before it waits
        for the predecessor's results; 0 launches them plainly. */
-    HM_OPT_PDL = 6
+    HM_OPT_PDL = 6,
+    /* HM_OPT_WAIT_LIMIT_NS (default 2e9, 1..2e9): nanoseconds after which a
+       wait of the streamed near-field kernel (HM_OPT_NEAR_KERNEL 2) or of the
+       tensor-core panel kernel on its copies or MMAs gives up: the CTA
+       records HM_DEV_WAIT_TIMEOUT (hm_device_status), lets what it has in
+       flight land (bounded by 0.2 s), releases its tensor memory and returns;
+       the product's output is then invalid.  Keeps autotuned schedules.
+       No reference counterpart. */
+    HM_OPT_WAIT_LIMIT_NS = 7,
+    /* HM_OPT_TEST_STALL (default 0): test hook for that give-up path.  With 1,
+       the first wait of every CTA of those two kernels waits on a barrier
+       nothing arrives on, so it runs out after HM_OPT_WAIT_LIMIT_NS.  Keeps
+       autotuned schedules.  No reference counterpart. */
+    HM_OPT_TEST_STALL = 8
 };
 int hm_configure(hm_handle *h, int option, int64_t value);
 
@@ -264,6 +277,16 @@ int hm_configure(hm_handle *h, int option, int64_t value);
    host threads. */
 int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice, double *ms);
 
+/* Test hook for the allocation-failure paths (no reference counterpart: the
+   reference allocates through Julia's GC).  after >= 0: the next `after`
+   device allocations of the library (cudaMalloc / cudaMallocAsync, builds,
+   per-stream scratch, staging, the autotuner's vectors, the algebra's
+   workspaces) succeed and the one after them fails with HM_ERR_ALLOC without
+   calling CUDA; the hook then disarms itself.  after = -1 disarms it.
+   Process-wide.  Every entry point that allocates returns HM_ERR_ALLOC from
+   such a failure and frees what it had allocated. */
+int hm_debug_fail_alloc(int64_t after);
+
 /* Allocation-free single right-hand-side product.  No counterpart in the
    reference: it is an addition for callers that cannot let a library
    allocate device memory while they run — processes whose GPU memory is
@@ -282,8 +305,13 @@ int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice,
    calls share the one array: calls that overlap on the GPU (other streams,
    or other handles, at the same time) race and give wrong results.
    The first call on each device looks up the array's device address with
-   cudaGetSymbolAddress (that device current) and caches it; make that first
-   call before any stream capture.  The call makes no cudaMalloc, cudaFree or
+   cudaGetSymbolAddress (that device current) and caches it for the life of
+   the process; make that first call before any stream capture.  A device
+   reset (cudaDeviceReset) can move the array: after one, load the library
+   afresh before calling again.  The device current at the call must be the
+   one the handle was built on (HM_ERR_INVALID_ARG otherwise).  The call runs
+   the schedule hm_mul would pick for one right-hand side (hm_autotune's, when
+   it ran) with every stage on `stream`.  It makes no cudaMalloc, cudaFree or
    other allocating call. */
 int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *stream);
 

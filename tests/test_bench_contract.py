@@ -23,3 +23,10 @@ def test_reference_arm_json_line():
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert d["config"]["workload"] and d["config"]["n"] == 4096
+    # the same config as the GPU arm's line (same keys and values), and the
+    # single-threaded figure of the (single-threaded) reference beside it
+    sys.path.insert(0, REPO)
+    import bench
+    assert d["config"] == bench.workload_config(4096, 1)
+    one = d["cpu_baseline"]["single_core"]
+    assert one["cores"] == 1 and one["value"] > 0

@@ -72,21 +72,51 @@ def test_grad_fp32_against_dense_fp64(grad_case):
     assert rel(gy.double().cpu().numpy()[cols], gy_ref) <= 1e-5
 
 
-def test_grad_fp64_against_central_differences(grad_case):
-    # dL/dx_i = r_i d(row_i . w)/dx_i; rows depend only on their own point, so
-    # one shifted product per step gives every row's difference quotient
+@pytest.fixture(scope="module")
+def central_differences(grad_case):
+    """FP64 central differences (h = 1e-6, Richardson-extrapolated) of L with
+    the block tree held fixed, on 1024 rows and 1024 columns whose nearest
+    point of the other side is at least 20 h away.  dL/dx_i = r_i d(row_i . w)/dx_i
+    and dL/dy_j = w_j d(col_j . r)/dy_j: a row of H (a row of H^T, the
+    KernelMatrix of (y, x) with swapped arguments) depends only on its own
+    point, so one shifted product per step gives every row's quotient."""
     n, x, y, w, t, H32, H64 = grad_case
-    loss, gw, gx, gy = H64.loss_and_grad(torch.tensor(w, device="cuda"), torch.tensor(t, device="cuda"))
     P = _lib.Plan(x, y, 1.0, 0.0, 1.0, 0.0)
+    PT = _lib.Plan(y, x, 1.0, 0.0, 1.0, 0.0)
     r = emulate(P, O.CAUCHY, w) - t
     h = 1e-6
 
-    def cd(hh):
+    def cdx(hh):
         return (emulate(P, O.CAUCHY, w, x=x + hh) - emulate(P, O.CAUCHY, w, x=x - hh)) / (2 * hh)
-    fd = r * (4 * cd(h / 2) - cd(h)) / 3
-    ok = np.nonzero(nearest_gap(x, y) >= 20 * h)[0]
-    sub = np.random.default_rng(8).choice(ok, 1024, replace=False)
-    assert rel(gx.cpu().numpy()[sub], fd[sub]) <= 1e-5
+
+    def cdy(hh):
+        return (emulate(PT, O.CAUCHY, r, swap=True, x=y + hh)
+                - emulate(PT, O.CAUCHY, r, swap=True, x=y - hh)) / (2 * hh)
+    fdx = r * (4 * cdx(h / 2) - cdx(h)) / 3
+    fdy = w * (4 * cdy(h / 2) - cdy(h)) / 3
+    rng = np.random.default_rng(8)
+    subx = rng.choice(np.nonzero(nearest_gap(x, y) >= 20 * h)[0], 1024, replace=False)
+    suby = rng.choice(np.nonzero(nearest_gap(y, x) >= 20 * h)[0], 1024, replace=False)
+    return fdx, fdy, subx, suby
+
+
+def test_grad_fp64_against_central_differences(grad_case, central_differences):
+    n, x, y, w, t, H32, H64 = grad_case
+    fdx, fdy, subx, suby = central_differences
+    loss, gw, gx, gy = H64.loss_and_grad(torch.tensor(w, device="cuda"), torch.tensor(t, device="cuda"))
+    assert rel(gx.cpu().numpy()[subx], fdx[subx]) <= 1e-5
+    assert rel(gy.cpu().numpy()[suby], fdy[suby]) <= 1e-5
+
+
+def test_grad_fp32_forward_against_central_differences(grad_case, central_differences):
+    """The FP32 forward (FP32 factors from FP64 compression, FP32 w and t):
+    dL/dx and dL/dy against the same FP64 central differences, <= 1e-5."""
+    n, x, y, w, t, H32, H64 = grad_case
+    fdx, fdy, subx, suby = central_differences
+    loss, gw, gx, gy = H32.loss_and_grad(torch.tensor(w, device="cuda", dtype=torch.float32),
+                                         torch.tensor(t, device="cuda", dtype=torch.float32))
+    assert rel(gx.double().cpu().numpy()[subx], fdx[subx]) <= 1e-5
+    assert rel(gy.double().cpu().numpy()[suby], fdy[suby]) <= 1e-5
 
 
 def test_autograd_function(grad_case):

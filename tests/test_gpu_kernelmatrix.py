@@ -249,6 +249,84 @@ def test_2pow20_fp32_error(big):
     assert H32.device_status() == 0 and H64.device_status() == 0
 
 
+def test_2pow20_fp64_full_vector_matches_oracle(big):
+    """Plain FP64 product at n = 2^20 (interleaved grid): every entry of the
+    GPU vector against the oracle's reference-order product (reference
+    per-block layout and loop order, src/KernelMatrix.jl:17-45,
+    src/algebra.jl:243-277), relative 2-norm <= 1e-12."""
+    n, x, y, H64, H32 = big
+    b = np.random.default_rng(1234).standard_normal(n)
+    Ho = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0, nthreads=os.cpu_count())
+    ref = np.zeros(n)
+    Ho.mul(ref, b, nthreads=os.cpu_count())
+    del Ho
+    u = (H64 @ dev(b)).cpu().numpy()
+    assert rel(u, ref) <= TOL64
+
+
+def test_2pow20_beta_fp64_full_vector_matches_oracle():
+    """The clustered variant of the same workload: x, y i.i.d. Beta(1/2, 1/2)
+    at n = 2^20, sorted, minimum gap 1e-9, seed 21 (the benchmark's points),
+    FP64; the whole vector against the oracle at <= 1e-12."""
+    n = 1 << 20
+    x, y = O.beta_points(n, 21)
+    hi = float(max(x[0], y[0], 1.0))
+    b = np.random.default_rng(21).standard_normal(n)
+    Ho = O.OracleKernelMatrix(O.CAUCHY, x, y, hi, 0.0, hi, 0.0, nthreads=os.cpu_count())
+    ref = np.zeros(n)
+    Ho.mul(ref, b, nthreads=os.cpu_count())
+    st_o = Ho.stats()
+    del Ho
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, hi, 0.0, hi, 0.0)
+    st = H.stats()
+    assert (st["n_bary"], st["n_dense"]) == (st_o["bary"], st_o["dense"])
+    assert rel((H @ dev(b)).cpu().numpy(), ref) <= TOL64
+    assert H.device_status() == 0
+    H.free()
+
+
+def _dense_rows_fp64(x, y, B64, rows, chunk=512):
+    """FP64 dense rows sum_j 1/(x_i - y_j) B[j, q] for every column q of B:
+    the Cauchy kernel block of the sampled rows formed in FP64 on the device
+    (one rounding for the difference, one for the reciprocal, as the
+    reference evaluates it) and multiplied in FP64, a chunk of rows at a time."""
+    xd = torch.tensor(x, device="cuda", dtype=torch.float64)
+    yd = torch.tensor(y, device="cuda", dtype=torch.float64)
+    out = torch.empty(len(rows), B64.shape[1], device="cuda", dtype=torch.float64)
+    for i0 in range(0, len(rows), chunk):
+        r = torch.tensor(rows[i0:i0 + chunk], device="cuda")
+        K = torch.reciprocal(xd[r][:, None] - yd[None, :])
+        out[i0:i0 + chunk] = K @ B64
+        del K
+    return out
+
+
+@pytest.mark.parametrize("k", [32, 256])
+def test_2pow20_fp32_multi_rhs_every_column(big, k):
+    """FP32 storage with a block of k right-hand sides at n = 2^20: every
+    column on 4096 sampled rows against the FP64 dense product, <= 1e-6
+    relative, with the tensor-core panels on (the default for 16 or more
+    right-hand sides) and off (FP32 pipes).  The FP64 dense rows are pinned to
+    the oracle's compensated dense rows on one column."""
+    n, x, y, H64, H32 = big
+    g = torch.Generator(device="cuda").manual_seed(k)
+    B = torch.randn(k, n, device="cuda", dtype=torch.float32, generator=g).t()     # column-major n x k
+    rows = np.sort(np.random.default_rng(k).choice(n, 4096, replace=False))
+    ref = _dense_rows_fp64(x, y, B.double(), rows)
+    pin = O.dense_rows(O.CAUCHY, x, y, B[:, 0].double().cpu().numpy(), rows[:64], nthreads=os.cpu_count())
+    assert rel(ref[:64, 0].cpu().numpy(), pin) <= 1e-12
+    rt = torch.tensor(rows, device="cuda")
+    for tc in (True, False):
+        H32.set_tensor_cores(tc)
+        U = torch.empty(k, n, device="cuda", dtype=torch.float32).t()
+        H32.mul(U, B, accumulate=False)
+        got = U.index_select(0, rt).double()
+        err = torch.linalg.norm(got - ref, dim=0) / torch.linalg.norm(ref, dim=0)
+        assert float(err.max()) <= TOL32, (tc, int(err.argmax()), float(err.max()))
+        assert H32.device_status() == 0
+    H32.set_tensor_cores(True)
+
+
 def test_repeated_calls_and_streams():
     # the single-launch passes reset their synchronisation words: repeated
     # products, and products on a second stream, give identical results

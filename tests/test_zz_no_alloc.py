@@ -38,6 +38,16 @@ def test_noalloc_matches_mul_twice(dtype):
     H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=dtype)
     g = torch.Generator(device="cuda").manual_seed(3)
     stream = torch.cuda.current_stream().cuda_stream
+    # the device's free memory does not move across a call (after the first
+    # call on this handle set up its kernels' attributes)
+    v = torch.randn(n, device="cuda", dtype=TDT[dtype], generator=g)
+    u = torch.zeros(n, device="cuda", dtype=TDT[dtype])
+    _lib.check(_lib.lib.hm_mul_noalloc(H.handle, v.data_ptr(), u.data_ptr(), 0, stream))
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    _lib.check(_lib.lib.hm_mul_noalloc(H.handle, v.data_ptr(), u.data_ptr(), 0, stream))
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
     for call in range(2):
         v = torch.randn(n, device="cuda", dtype=TDT[dtype], generator=g)
         u0 = torch.randn(n, device="cuda", dtype=TDT[dtype], generator=g)
