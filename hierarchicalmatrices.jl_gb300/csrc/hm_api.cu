@@ -13,6 +13,7 @@
 #include <thread>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "hm_kernels.cuh"
@@ -167,6 +168,9 @@ inline int sched_bucket(int k)
     return b;
 }
 
+// Storage types whose vectors (right-hand sides, results, coefficients) are FP64.
+inline bool f64_vectors(int storage) { return storage != HM_F32; }
+
 }  // namespace
 
 struct hm_handle {
@@ -217,7 +221,8 @@ struct hm_handle {
     // persistent panel streaming: CTA b of part p (0 near, 1 far) owns the
     // segments [d_cta_seg[p*(stream_ctas+1) + b], ... + b + 1)
     int *d_cta_seg = nullptr;
-    int stream_ctas = 0;
+    int stream_ctas = 0;            // > 0: every segment's far and near parts are contiguous column runs
+    int sms = 1;                    // multiprocessors of the device
     int part_width[2] = {0, 0};     // widest near / far column run of a segment
     int part_segs[2] = {0, 0};      // most segments of one CTA (near / far)
     int part_pieces[2] = {0, 0};    // most piece records of one CTA
@@ -359,6 +364,7 @@ int prepare_streaming(hm_handle *h, const std::vector<hm_seg> &segs, const std::
     int dev = 0, sms = 0;
     HM_CK(cudaGetDevice(&dev));
     HM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    h->sms = sms;
     double near_bytes = 0;
     for (const hm_seg &g : segs) near_bytes += (double)(g.width - g.nfar) * g.ld * 4.0;
     const int64_t want = std::max<int64_t>((int64_t)kStreamCtasPerSm * sms, (int64_t)(near_bytes / kStreamCtaBytes));
@@ -437,6 +443,29 @@ void set_vp_caps(hm_handle *h, const std::vector<hm_vpanel> &vps)
     h->vp_covers_x = ok && cur == h->ny;
 }
 
+// HM_DF64 storage: the FP64 panel values become (h, l) FP32 pairs in place;
+// a value too large for the pair is an error (HM_ERR_UNSUPPORTED).
+int to_double_float(hm_handle *h, double *P, cudaStream_t st)
+{
+    if (!P || h->pstore_elems == 0) return HM_OK;
+    int *bad = nullptr;
+    HM_TRY(h->alloc(&bad, 1));
+    HM_CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    const int64_t n = h->pstore_elems;
+    const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
+    panels_to_df<<<grid, 256, 0, st>>>(P, n, bad);
+    HM_CK_LAUNCH("panels_to_df");
+    int hb = 0;
+    HM_CK(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HM_CK(cudaStreamSynchronize(st));
+    if (hb) {
+        set_error("a panel value's magnitude reaches 2^127: too large for double-float (HM_DF64) storage; "
+                  "use HM_F64");
+        return HM_ERR_UNSUPPORTED;
+    }
+    return HM_OK;
+}
+
 template <typename S>
 int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, const std::vector<double> &lam,
                  const std::vector<double> &T, const double *x, const double *y, cudaStream_t st)
@@ -507,6 +536,9 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
     if (h->n_segs) {
         fill_segments<S, false><<<h->n_segs, 128, 0, st>>>(fa, h->d_segs, h->d_pieces, sf, h->n_segs, Pn);
         HM_CK_LAUNCH("fill_segments");
+    }
+    if constexpr (sizeof(S) == 8) {
+        if (h->storage == HM_DF64) HM_TRY(to_double_float(h, reinterpret_cast<double *>(Pn), st));
     }
     HM_CK(cudaStreamSynchronize(st));
     return HM_OK;
@@ -679,7 +711,7 @@ thread_local const Sched *t_sched = nullptr;
 inline Sched configured_sched(const hm_handle *h)
 {
     return Sched{h->overlap, h->near_kernel, h->near_stages, h->tensor_cores ? 1 : 0,
-                 h->pdl >= 0 ? h->pdl : (h->storage == HM_F32 ? 1 : 0)};
+                 h->pdl >= 0 ? h->pdl : (h->storage != HM_F64 ? 1 : 0)};
 }
 inline Sched cur_sched(const hm_handle *h) { return t_sched ? *t_sched : configured_sched(h); }
 inline Sched sched_for(const hm_handle *h, int k)
@@ -837,10 +869,27 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
 // (whose registers allow three), two for FP32 with four or more, one for FP64
 constexpr size_t kStreamSmemMax3 = 74 * 1024, kStreamSmemMax2 = 112 * 1024, kStreamSmemMax1 = 200 * 1024;
 
+// Double-float panels (HM_DF64): PART 0 near-field columns, 1 far-field
+// columns, 2 every column; right-hand sides q0 .. q0 + KB - 1.
+template <int PART, int KB>
+int launch_df(hm_handle *h, const MulArgs<double> &ma, const double *s, const double *t, const void *panels,
+              double *yfar, cudaStream_t st, bool pdl, int64_t ldf, int q0)
+{
+    const int maxw = std::max(h->max_width, 1);
+    const size_t smem = (size_t)kWarpsPerCta * maxw * KB * sizeof(float2);
+    HM_TRY(ensure_smem(expand_df<PART, KB>, smem));
+    return launch_k(PART == 1 ? "expand_df_far" : "expand_df", expand_df<PART, KB>, dim3(warp_ctas(h->n_segs)),
+                    dim3(32 * kWarpsPerCta), smem, st, PART == 1 && pdl, ma, h->d_segs, h->n_segs, h->d_pieces,
+                    static_cast<const float2 *>(panels), s, t, h->r, maxw, yfar, ldf, q0);
+}
+
 template <typename S, typename A, bool FAR, int KB>
 int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, S *yfar,
                    cudaStream_t st, bool pdl = false, int64_t ldf = 0)
 {
+    if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
+        if (h->storage == HM_DF64) return launch_df<FAR ? 1 : 0, KB>(h, ma, s, t, panels, yfar, st, pdl, ldf, 0);
+    }
     // one warp per segment unless the streamed CTAs are asked for: measured on
     // GB300, the warp kernel reads 64-row grid panels at 6.1 TB/s (90% of the
     // copy peak) and keeps its lead on short segments and more right-hand
@@ -869,6 +918,24 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
                 static_cast<const S *>(panels), s, t, h->r, nst, gcap, ngb, h->part_segs[part], yfar,
                 h->d_status, h->wait_ns, h->test_stall);
             HM_CK_LAUNCH(FAR ? "stream_far" : "stream_near");
+            return HM_OK;
+        }
+    }
+    if constexpr (sizeof(S) == 4 && sizeof(A) == 4 && KB >= 4) {
+        // per-warp rings (the default for 3-8 FP32 right-hand sides): each warp
+        // keeps several chunks of its run of segments in flight
+        if (h->stream_ctas > 0 && (sc.near_kernel == 0 || sc.near_kernel == 3)) {
+            auto kern = ring_part<KB, FAR>;
+            const size_t smem = ring_smem_bytes(KB);
+            HM_TRY(ensure_smem(kern, smem));
+            HM_TRY(prefer_shared(kern));
+            // about kRingSegsPerWarp segments per warp: CTAs retire through the
+            // product and hand their slots to the tree passes on the side stream
+            const int64_t warps = (h->n_segs + kRingSegsPerWarp - 1) / kRingSegsPerWarp;
+            const unsigned grid = (unsigned)((warps + kRingWarps - 1) / kRingWarps);
+            HM_TRY(launch_k(FAR ? "ring_far" : "ring_near", kern, dim3(grid), dim3(32 * kRingWarps), smem, st,
+                            FAR && pdl, ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const float *>(panels),
+                            s, t, h->r, yfar, ldf));
             return HM_OK;
         }
     }
@@ -907,6 +974,13 @@ constexpr int kTensorCoreMinK = 16;   // right-hand sides from which the tensor-
 template <typename S, typename A>
 int launch_expand_k(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, const void *panels, cudaStream_t st)
 {
+    if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
+        if (h->storage == HM_DF64) {
+            for (int q0 = 0; q0 < ma.k; q0 += 8)
+                HM_TRY((launch_df<2, 8>(h, ma, s, t, panels, nullptr, st, false, 0, q0)));
+            return HM_OK;
+        }
+    }
     if constexpr (sizeof(S) == 4 && sizeof(A) == 4) {
         if (cur_sched(h).tensor_cores && h->tc_ok && ma.k >= kTensorCoreMinK) {
             const int maxw = std::max(h->max_width, 1);
@@ -1028,6 +1102,9 @@ int ensure_drow(hm_handle *h, cudaStream_t st)
         fill_segments<S, true><<<h->n_segs, 128, 0, st>>>(fa, h->d_segs, h->d_pieces, h->d_seg_fill, h->n_segs, dP);
         HM_CK_LAUNCH("fill_segments<drow>");
     }
+    if constexpr (sizeof(S) == 8) {
+        if (h->storage == HM_DF64) HM_TRY(to_double_float(h, reinterpret_cast<double *>(dP), st));
+    }
     // complete before the panels are published: a later product may run on another stream
     HM_CK(cudaStreamSynchronize(st));
     h->d_dP = dP;
@@ -1037,7 +1114,7 @@ int ensure_drow(hm_handle *h, cudaStream_t st)
 int dispatch_mul(hm_handle *h, const void *x, int64_t incx, int64_t ldx, void *y, int64_t incy, int64_t ldy,
                  int k, int accumulate, cudaStream_t st, void *yout = nullptr, const void *xin = nullptr)
 {
-    if (h->storage == HM_F64) {
+    if (f64_vectors(h->storage)) {
         MulArgs<double> ma{static_cast<const double *>(x), static_cast<double *>(y), incx, ldx, incy, ldy, k, accumulate};
         ma.yout = static_cast<double *>(yout);
         ma.xin = static_cast<const double *>(xin);
@@ -1101,8 +1178,14 @@ std::vector<Sched> sched_candidates(const hm_handle *h, int k, bool fp32)
     const bool tree = h->n_vp || h->n_m2l_rows;
     std::vector<int> overlaps = !tree ? std::vector<int>{base.overlap}
                                       : k <= kPartMaxK ? std::vector<int>{0, 1, 2, 3, 4} : std::vector<int>{0, 1};
-    std::vector<int> kernels = (k <= kPartMaxK && h->stream_ctas > 0 && h->n_segs) ? std::vector<int>{0, 2}
-                                                                                    : std::vector<int>{base.near_kernel};
+    // near-field kernels: the default (per-warp rings for 3-8 FP32 right-hand
+    // sides, else one warp per segment), the warp kernel where that differs,
+    // and the streamed CTAs
+    std::vector<int> kernels{base.near_kernel};
+    if (k <= kPartMaxK && h->stream_ctas > 0 && h->n_segs && h->storage != HM_DF64) {
+        kernels = {0, 2};
+        if (fp32 && k >= 3) kernels = {0, 1, 2};
+    }
     std::vector<int> tcs = (fp32 && h->tc_ok && k >= kTensorCoreMinK) ? std::vector<int>{1, 0}
                                                                        : std::vector<int>{base.tensor_cores};
     std::vector<Sched> c{base};       // the configured schedule first, timed for comparison
@@ -1443,7 +1526,7 @@ int build_kernelmatrix(int kernel, int swap, const double *x, int64_t nx, const 
     if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
     *out = nullptr;
     if (kernel < HM_KERNEL_CAUCHY || kernel > HM_KERNEL_LOG) { set_error("unknown kernel %d", kernel); return HM_ERR_UNSUPPORTED; }
-    if (storage != HM_F64 && storage != HM_F32) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
+    if (storage != HM_F64 && storage != HM_F32 && storage != HM_DF64) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
     hm_plan *pl = nullptr;
     int st = hm_plan_create(x, nx, y, ny, a, b, c, d, rank, blocksize, &pl);
     if (st) return st;
@@ -1475,7 +1558,7 @@ int build_from_plan(int kernel, int swap, hm_plan *pl, const double *x, const do
     h->stats = P.stats;
     h->n_xslots = P.n_xslots; h->n_yslots = P.n_yslots; h->max_width = P.max_width;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
-    st = (storage == HM_F64) ? build_device<double>(h, P, cheb, lam, T, x, y, cs)
+    st = f64_vectors(storage) ? build_device<double>(h, P, cheb, lam, T, x, y, cs)
                              : build_device<float>(h, P, cheb, lam, T, x, y, cs);
     hm_plan_free(pl);
     auto nonempty = [](const std::vector<int> &ptr) {
@@ -1510,7 +1593,7 @@ int hm_kernelmatrix_batch_build(int kernel, int ninst, const int64_t *nx, const 
     if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
     *out = nullptr;
     if (kernel < HM_KERNEL_CAUCHY || kernel > HM_KERNEL_LOG) { set_error("unknown kernel %d", kernel); return HM_ERR_UNSUPPORTED; }
-    if (storage != HM_F64 && storage != HM_F32) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
+    if (storage != HM_F64 && storage != HM_F32 && storage != HM_DF64) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
     hm_plan *pl = nullptr;
     HM_TRY(hm_batch_plan_create(ninst, nx, ny, x, y, boxes, rank, blocksize, &pl));
     const int st = build_from_plan(kernel, 0, pl, x, y, storage, stream, out);
@@ -1525,7 +1608,7 @@ int hm_hier_build(int storage, int64_t m, int64_t n, int nblocks, const int32_t 
     g_last_error.clear();
     if (!out) { set_error("out is NULL"); return HM_ERR_INVALID_ARG; }
     *out = nullptr;
-    if (storage != HM_F64 && storage != HM_F32) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
+    if (storage != HM_F64 && storage != HM_F32 && storage != HM_DF64) { set_error("unknown storage %d", storage); return HM_ERR_UNSUPPORTED; }
     if (m < 0 || n < 0 || nblocks < 0 || (nblocks && (!kinds || !row0 || !rows || !col0 || !cols || !ranks || !values || !offsets))) {
         set_error("hm_hier_build: bad arguments");
         return HM_ERR_INVALID_ARG;
@@ -1780,7 +1863,7 @@ int hm_mul_drow(hm_handle *h, int transposed, const void *v, int64_t ldv, void *
     if (nrhs < 0) { set_error("nrhs < 0"); return HM_ERR_INVALID_ARG; }
     if (nrhs > 1 && (ldv < h->ny || ldu < h->nx)) { set_error("leading dimension too small"); return HM_ERR_BOUNDS; }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (h->storage == HM_F64) {
+    if (f64_vectors(h->storage)) {
         HM_TRY(ensure_drow<double>(h, st));
         MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, ldv, 1, ldu, nrhs, accumulate ? 1 : 0};
         return run_mul<double, double>(h, ma, st, h->d_dP);
@@ -1800,7 +1883,7 @@ int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, in
         set_error("strided access past the end of x or y");
         return HM_ERR_BOUNDS;
     }
-    const size_t es = h->storage == HM_F64 ? 8 : 4;
+    const size_t es = f64_vectors(h->storage) ? 8 : 4;
     const char *xb = static_cast<const char *>(x) + (size_t)(jstart - 1) * es;
     char *yb = static_cast<char *>(y) + (size_t)(istart - 1) * es;
     return dispatch_mul(h, xb, incx, 0, yb, incy, 0, 1, 1, static_cast<cudaStream_t>(stream));
@@ -1812,7 +1895,7 @@ int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate)
     if (!h || nrhs < 0) { set_error("bad argument"); return HM_ERR_INVALID_ARG; }
     if (nrhs == 0) return HM_OK;          // nothing read or written (the vectors may be NULL)
     if (!v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
-    const size_t es = h->storage == HM_F64 ? 8 : 4;
+    const size_t es = f64_vectors(h->storage) ? 8 : 4;
     const size_t bv = (size_t)h->ny * nrhs * es, bu = (size_t)h->nx * nrhs * es;
     if (!h->host_stream) HM_CK(cudaStreamCreateWithFlags(&h->host_stream, cudaStreamNonBlocking));
     cudaStream_t st = h->host_stream;
@@ -1879,7 +1962,7 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
 {
     g_last_error.clear();
     if (!h || !v || !u) { set_error("NULL argument"); return HM_ERR_INVALID_ARG; }
-    const size_t need = h->storage == HM_F64 ? scratch_layout<double>(h, 1).bytes : scratch_layout<float>(h, 1).bytes;
+    const size_t need = f64_vectors(h->storage) ? scratch_layout<double>(h, 1).bytes : scratch_layout<float>(h, 1).bytes;
     if (need > HM_NOALLOC_SCRATCH_BYTES) {
         set_error("hm_mul_noalloc: this matrix needs %zu bytes of coefficient scratch; the library's fixed "
                   "scratch holds %u bytes (use hm_mul)", need, (unsigned)HM_NOALLOC_SCRATCH_BYTES);
@@ -1900,7 +1983,7 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
     sched.overlap = 0;
     SchedScope scope(&sched);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (h->storage == HM_F64) {
+    if (f64_vectors(h->storage)) {
         MulArgs<double> ma{static_cast<const double *>(v), static_cast<double *>(u), 1, h->ny, 1, h->nx, 1,
                            accumulate ? 1 : 0};
         return launch_pipeline<double, double>(h, ma, st, st, nullptr, nullptr, scratch, false);
@@ -1928,7 +2011,7 @@ int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice,
         set_error("hm_autotune: not allowed while the stream is being captured");
         return HM_ERR_INVALID_ARG;
     }
-    return h->storage == HM_F64 ? autotune<double>(h, nrhs, reps, st, choice, ms)
+    return f64_vectors(h->storage) ? autotune<double>(h, nrhs, reps, st, choice, ms)
                                 : autotune<float>(h, nrhs, reps, st, choice, ms);
 }
 
@@ -1954,7 +2037,7 @@ int hm_configure(hm_handle *h, int option, int64_t value)
         break;
     case HM_OPT_TENSOR_CORES: break;
     case HM_OPT_NEAR_KERNEL:
-        if (value < 0 || value > 2) { set_error("HM_OPT_NEAR_KERNEL must be 0, 1 or 2"); return HM_ERR_INVALID_ARG; }
+        if (value < 0 || value > 3) { set_error("HM_OPT_NEAR_KERNEL must be 0, 1, 2 or 3"); return HM_ERR_INVALID_ARG; }
         break;
     case HM_OPT_NEAR_STAGES:
         if (value < 2 || value > 16) { set_error("HM_OPT_NEAR_STAGES must be in [2, 16]"); return HM_ERR_INVALID_ARG; }

@@ -222,6 +222,37 @@ __global__ void stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_se
                             const S *P, const A *s, const A *t, int r, int nst, int gcap, int ngb, int dsegs,
                             S *yfar, int *status, unsigned long long wait_ns, int stall);
 
+// Per-warp rings (hm_ring.cu), FP32 storage, KB = 4 or 8 right-hand sides:
+// warp w of the grid owns segments [w * nsegs / W, (w + 1) * nsegs / W) and
+// streams their part's columns (FAR: the far-field pieces, else the X
+// pieces; each part one contiguous column run) through kRingStages stages of
+// ring_stage_floats(KB) floats; segments of at most 64 rows, ld % 4 == 0,
+// poff % 4 == 0.  Grid: a whole number of CTAs of kRingWarps warps, shared
+// memory ring_smem_bytes(KB).
+constexpr int kRingWarps = 2;
+constexpr int kRingSegsPerWarp = 24;      // segments per warp (the launch's grid follows from it)
+constexpr int kRingStages = 3;
+constexpr int kRingCols = 32;              // columns per chunk at most (lane c gathers column c)
+constexpr int kRingPanelFloats = 768;      // panel values per chunk at most (3 KB)
+__host__ __device__ constexpr int ring_stage_floats(int kb) { return kRingPanelFloats + kRingCols * kb; }
+__host__ __device__ constexpr size_t ring_smem_bytes(int kb)
+{
+    return (size_t)kRingWarps * kRingStages * ring_stage_floats(kb) * sizeof(float);
+}
+template <int KB, bool FAR>
+__global__ void ring_part(MulArgs<float> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const float *P,
+                          const float *s, const float *t, int r, float *yfar, int64_t ldf);
+
+// Double-float panels (hm_df.cu, HM_DF64 storage): panels_to_df turns FP64
+// panel values into (h, l) FP32 pairs in place; expand_df multiplies them on
+// the FP32 pipes, one warp per row segment (PART 0 near-field columns, 1
+// far-field columns, 2 all), right-hand sides q0 .. q0 + KB - 1 of k;
+// shared memory kWarpsPerCta * maxw * KB * 8 bytes per CTA.
+__global__ void panels_to_df(double *P, int64_t n, int *bad);
+template <int PART, int KB>
+__global__ void expand_df(MulArgs<double> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const float2 *P,
+                          const double *s, const double *t, int r, int maxw, double *yfar, int64_t ldf, int q0);
+
 // Tensor-core panels for many right-hand sides (FP32 storage): grid
 // (ceil(k / 128), segments), 256 threads, expand_tc_smem_bytes(maxw) of shared
 // memory; needs segments of <= 64 rows, ld % 4 == 0, poff % 32 == 0.

@@ -27,7 +27,7 @@ HM_LR_KMAX = 96
 HM_SOLVE_TRSM, HM_SOLVE_LR, HM_SOLVE_DENSE, HM_SOLVE_INV = 0, 1, 2, 3
 
 HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
-HM_F64, HM_F32 = 0, 1
+HM_F64, HM_F32, HM_DF64 = 0, 1, 2
 HM_OPT_OVERLAP = 1
 HM_OPT_NEAR_STAGES = 2
 HM_OPT_TENSOR_CORES = 3

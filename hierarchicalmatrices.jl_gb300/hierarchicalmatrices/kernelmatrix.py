@@ -54,12 +54,20 @@ def _kernel_id(f):
                      "a fixed kernel set")
 
 
+DF64 = "df64"   # storage: FP64 vectors and tree passes, row-segment panels as double-float pairs
+
+
 def _storage_of(dtype):
+    """(storage code, numpy dtype of the vectors) for a dtype argument:
+    np.float64, np.float32 or "df64" (HM_DF64: the FP64 product with its
+    panels stored as double-float pairs and multiplied on the FP32 pipes)."""
+    if isinstance(dtype, str) and dtype == DF64:
+        return _lib.HM_DF64, np.dtype(np.float64)
     dt = np.dtype(dtype)
     if dt == np.float64:
-        return _lib.HM_F64
+        return _lib.HM_F64, dt
     if dt == np.float32:
-        return _lib.HM_F32
+        return _lib.HM_F32, dt
     raise ValueError(f"unsupported storage dtype {dt}")
 
 
@@ -123,13 +131,13 @@ class KernelMatrix:
         self.x = _host_f64(x)
         self.y = _host_f64(y)
         self.box = (float(a), float(b), float(c), float(d))
-        self.dtype = np.dtype(dtype)
+        self.storage, self.dtype = _storage_of(dtype)
         self.rank = int(rank) if rank else BLOCKRANK(np.float64)
         self.blocksize = int(blocksize) if blocksize else 4 * self.rank
         h = _vp()
         check(lib.hm_kernelmatrix_build(self.kernel, _lib.f64_ptr(self.x), len(self.x),
                                         _lib.f64_ptr(self.y), len(self.y), *self.box, self.rank,
-                                        self.blocksize, _storage_of(self.dtype),
+                                        self.blocksize, self.storage,
                                         _stream_ptr(stream), ctypes.byref(h)))
         self._h = h
         self.shape = (len(self.x), len(self.y))
@@ -329,10 +337,13 @@ class KernelMatrix:
         check(lib.hm_configure(self._h, _lib.HM_OPT_TENSOR_CORES, 1 if enable else 0))
 
     def set_near_kernel(self, which):
-        """Near-field panels with up to 8 right-hand sides: "warp" (one warp
-        per row segment; "auto", the default, chooses it) or "stream" (CTAs
-        streaming runs of segments through shared memory)."""
-        code = {"auto": 0, "warp": 1, "stream": 2}[which]
+        """Near-field panels with up to 8 right-hand sides: "auto" (the
+        default: per-warp rings for 3-8 FP32 right-hand sides, else one warp
+        per row segment), "warp" (one warp per row segment), "stream" (CTAs
+        streaming runs of segments through shared memory with cp.async.bulk)
+        or "ring" (warps streaming runs of segments through per-warp rings
+        with cp.async; FP32 with 3-8 right-hand sides, else as "auto")."""
+        code = {"auto": 0, "warp": 1, "stream": 2, "ring": 3}[which]
         check(lib.hm_configure(self._h, _lib.HM_OPT_NEAR_KERNEL, code))
 
     def set_near_stages(self, n):
@@ -397,7 +408,7 @@ class KernelMatrixBatch(KernelMatrix):
     def __init__(self, f, xs, ys, boxes, *, dtype=np.float64, rank=None, blocksize=None, stream=None):
         self.kernel = _kernel_id(f)
         self.f = f
-        self.dtype = np.dtype(dtype)
+        self.storage, self.dtype = _storage_of(dtype)
         self.rank = int(rank) if rank else BLOCKRANK(np.float64)
         self.blocksize = int(blocksize) if blocksize else 4 * self.rank
         nx = np.array([len(v) for v in xs], dtype=np.int64)
@@ -411,7 +422,7 @@ class KernelMatrixBatch(KernelMatrix):
         check(lib.hm_kernelmatrix_batch_build(
             self.kernel, len(xs), nx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
             ny.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _lib.f64_ptr(self.x), _lib.f64_ptr(self.y),
-            _lib.f64_ptr(bx), self.rank, self.blocksize, _storage_of(self.dtype), _stream_ptr(stream),
+            _lib.f64_ptr(bx), self.rank, self.blocksize, self.storage, _stream_ptr(stream),
             ctypes.byref(h)))
         self._h = h
         self.ninst = len(xs)

@@ -48,7 +48,17 @@ enum {
 };
 
 /* Storage / arithmetic type of factors, leaves and vectors. */
-enum { HM_F64 = 0, HM_F32 = 1 };
+/* Storage types.  HM_F64 and HM_F32: factors and leaves in FP64 / FP32.
+   HM_DF64 (no reference counterpart): the FP64 product with its row-segment
+   panels (near-field leaves and row bases, the bulk of the stored values) kept
+   as pairs of FP32 values (h, l), h + l within 2^-48 relative of the FP64
+   value, and multiplied in double-float arithmetic on the FP32 pipes (GB300's
+   FP64 pipe is about 1/56 of its FP32 rate); vectors, the column bases, the
+   far-field blocks and the tree passes stay FP64.  Same bytes as HM_F64;
+   products agree with HM_F64 to about 1e-14 relative.  Building fails with
+   HM_ERR_UNSUPPORTED when a panel value's magnitude reaches 2^127.
+   KernelMatrix builds only (not hm_hier_build). */
+enum { HM_F64 = 0, HM_F32 = 1, HM_DF64 = 2 };
 
 const char *hm_status_string(int status);
 /* Message of the last failing call on this thread ("" if none). */
@@ -68,7 +78,7 @@ int hm_indsplit(const double *x, int64_t n, int64_t start, int64_t len, double a
    x (nx) and y (ny) are HOST arrays in non-increasing order with a > b, c > d,
    as the reference requires.  rank = BLOCKRANK (0 selects 20), blocksize =
    BLOCKSIZE leaf threshold (0 selects 4*rank).  Compression runs on the GPU in
-   FP64; factors and leaves are stored as `storage` (HM_F64 or HM_F32). */
+   FP64; factors and leaves are stored as `storage` (HM_F64, HM_F32 or HM_DF64). */
 int hm_kernelmatrix_build(int kernel, const double *x, int64_t nx, const double *y, int64_t ny,
                           double a, double b, double c, double d, int rank, int64_t blocksize,
                           int storage, void *stream, hm_handle **out);
@@ -136,7 +146,7 @@ int hm_bary_factors(int kernel, int rank, double a, double b, double c, double d
 
 /* size(H) (src/hierarchical.jl:33-47). */
 int hm_size(const hm_handle *h, int64_t *m, int64_t *n);
-/* Storage type of h (HM_F64 / HM_F32). */
+/* Storage type of h (HM_F64 / HM_F32 / HM_DF64). */
 int hm_storage(const hm_handle *h);
 
 /* Statistics: out[0..] = barycentric blocks, dense blocks, tree depth, row slots,
@@ -228,9 +238,13 @@ enum {
        (every FP32 value split exactly into three BF16 pieces, six products
        per step, FP32 accumulation); 0 keeps them on the FP32 pipes. */
     HM_OPT_TENSOR_CORES = 3,
-    /* HM_OPT_NEAR_KERNEL (default 0): near-field panels with up to 8
-       right-hand sides on 0 or 1 = one warp per row segment, 2 = CTAs
-       streaming runs of segments through shared memory (cp.async.bulk). */
+    /* HM_OPT_NEAR_KERNEL (default 0): near-field and far-field panels with up
+       to 8 right-hand sides on 0 = per-warp rings for 3-8 FP32 right-hand
+       sides and one warp per row segment otherwise, 1 = one warp per row
+       segment, 2 = CTAs streaming runs of segments through shared memory
+       (cp.async.bulk), 3 = per-warp rings (warps streaming runs of segments
+       through shared-memory stages with cp.async; FP32 with 3-8 right-hand
+       sides, otherwise as 0). */
     HM_OPT_NEAR_KERNEL = 4,
     /* HM_OPT_AUTOTUNED: value 0 forgets the schedules hm_autotune chose, so
        every product runs with the options above again.  Setting any other
@@ -265,8 +279,9 @@ int hm_configure(hm_handle *h, int option, int64_t value);
    bucket (1, 2, 3-4, 5-8, 9-16, 17-32, 33-64, 65-128, 129+): later hm_mul,
    hm_mul_strided, hm_mul_host and hm_mul_drow calls of that bucket run with
    it, including inside stream capture.  Candidates: HM_OPT_OVERLAP 0..4
-   (0..1 above 8 right-hand sides), HM_OPT_NEAR_KERNEL 0 or 2 with
-   HM_OPT_NEAR_STAGES 3, 4 or 6 (up to 8 right-hand sides), HM_OPT_TENSOR_CORES
+   (0..1 above 8 right-hand sides), HM_OPT_NEAR_KERNEL 0, 1 (FP32 with 3-8
+   right-hand sides) or 2 with HM_OPT_NEAR_STAGES 3, 4 or 6 (up to 8
+   right-hand sides), HM_OPT_TENSOR_CORES
    on or off (FP32, 16 or more), HM_OPT_PDL on or off.  Inputs are scratch vectors allocated on
    `stream` and freed before return; synchronous; not allowed while `stream`
    is being captured.  choice (host, 5 values, may be NULL) receives the

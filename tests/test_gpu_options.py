@@ -61,6 +61,38 @@ def test_near_kernels_agree(mat, k):
     assert H.device_status() == 0
 
 
+@pytest.mark.parametrize("k", [3, 4, 5, 8])
+def test_ring_kernel_agrees(mat, k):
+    """Per-warp rings (the default for 3-8 FP32 right-hand sides) against the
+    one-warp-per-segment kernel, near and far parts, accumulate on and off;
+    FP64 falls back to the warp kernel (bitwise equal)."""
+    n, dt, H = mat
+    B = torch.randn(k, n, device="cuda", dtype=TDT[dt]).t()
+    U0 = torch.randn(k, n, device="cuda", dtype=TDT[dt]).t()
+    try:
+        for acc in (False, True):
+            H.set_near_kernel("warp")
+            Uw = U0.clone()
+            H.mul(Uw, B, accumulate=acc)
+            H.set_near_kernel("ring")
+            Ur = U0.clone()
+            H.mul(Ur, B, accumulate=acc)
+            if dt == np.float64:
+                assert torch.equal(Ur, Uw)
+            else:
+                assert colrel(Ur, Uw) <= 5e-7, acc
+            for mode in (0, 1, 4):
+                H.set_overlap(mode)
+                again = U0.clone()
+                H.mul(again, B, accumulate=acc)
+                assert colrel(again, Ur) <= (1e-15 if mode else 5e-7)
+            H.set_overlap(True)
+    finally:
+        H.set_near_kernel("auto")
+        H.set_overlap(True)
+    assert H.device_status() == 0
+
+
 def test_host_buffer_product_replays(mat):
     # hm_mul_host runs plainly once, then replays a captured graph; options
     # changed in between are followed (the graph is dropped and captured again)
