@@ -646,6 +646,34 @@ def main():
                     "api": "hm_mul_host, page-locked host buffers"}}
         del H64, u64
         torch.cuda.empty_cache()
+        # the same FP64 product with HM_DF64 storage: row-segment panels as
+        # double-float pairs multiplied on the FP32 pipes (tree passes FP64)
+        t0 = time.perf_counter()
+        Hd = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype="df64")
+        torch.cuda.synchronize()
+        buildd_s = time.perf_counter() - t0
+        ud = torch.empty(n, device=dev, dtype=torch.float64)
+        schedd = Hd.autotune(1, reps=20)
+        msd = time_device(lambda: Hd.mul(ud, b64, accumulate=False), k_steps, 3, torch)
+        stds = serial_stages(Hd, lambda: Hd.mul(ud, b64, accumulate=False), 10, torch)
+        errd = rel_err_sampled(Hd, ud, b64, rows, torch)
+        stdd = Hd.stats()
+        for _ in range(max(3, args.warmup)):
+            Hd.mul_host(hu64_np, hb64_np, accumulate=False)
+        t0 = time.perf_counter()
+        for _ in range(k_steps):
+            Hd.mul_host(hu64_np, hb64_np, accumulate=False)
+        e2ed = k_steps / (time.perf_counter() - t0)
+        variants["fp64_df_k1"] = {
+            "storage": "HM_DF64: FP64 vectors, bases, far-field blocks and tree passes; row-segment panels as "
+                       "double-float (h, l) FP32 pairs multiplied on the FP32 pipes",
+            "matvec_per_s": 1e3 / msd, "ms": msd, "rel_err_vs_dense_fp64": errd,
+            "stored_GBs": (stdd["stored_values"] * 8 + 2 * n * 8) / (msd * 1e-3) / 1e9,
+            "build_s": buildd_s, "stage_ms_serial": stds, "schedule": schedd, "steps": k_steps,
+            "e2e": {"value": e2ed, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
+                    "api": "hm_mul_host, page-locked host buffers"}}
+        del Hd, ud
+        torch.cuda.empty_cache()
         # clustered points: Beta(1/2, 1/2), FP64 (a deeper, uneven tree)
         xb, yb = beta_points(n, 21)
         hi = float(max(xb[0], yb[0], 1.0))

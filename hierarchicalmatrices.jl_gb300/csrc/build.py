@@ -20,7 +20,7 @@ LIB = os.path.join(LIB_DIR, "libhmgpu.so")
 INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["hm_kernels.cu", "hm_ring.cu", "hm_df.cu", "hm_blocks.cu", "hm_tc.cu", "hm_algebra.cu", "hm_api.cu"]
+CU_SOURCES = ["hm_kernels.cu", "hm_ring.cu", "hm_df.cu", "hm_wide.cu", "hm_blocks.cu", "hm_tc.cu", "hm_algebra.cu", "hm_api.cu"]
 CPP_SOURCES = ["hm_plan.cpp"]
 HEADERS = ["hm_types.h", "hm_plan.h", "hm_kernels.cuh", "hm_async.cuh"]
 

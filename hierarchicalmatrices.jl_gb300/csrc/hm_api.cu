@@ -156,6 +156,8 @@ void transfer_matrices(int r, const std::vector<double> &x, const std::vector<do
 // The options one product runs with (hm_configure's HM_OPT_* values).
 struct Sched {
     int overlap, near_kernel, near_stages, tensor_cores, pdl;
+    int tile = 0;      // per-warp ring tile (kRingTile index) for 3-8 FP32 right-hand sides
+    int wide = 1;      // tree passes on the lane-per-right-hand-side kernels (32+ right-hand sides)
 };
 
 // Right-hand-side buckets of the autotuned schedules: 1, 2, 3-4, 5-8, 9-16,
@@ -201,6 +203,9 @@ struct hm_handle {
     int n_vp = 0;
     int vp_cap = 64, vp_wcap = HM_RMAX;   // leaf_up's shared-memory panel: rows (multiple of 32) x columns
     bool vp_covers_x = false;             // the leaf panels' rows partition [0, ny): leaf_up reads every x once
+    bool vp_wide = false;                 // every leaf panel row-major with ld == width == 20 (leaf_up_w)
+    bool wide_tree = true;                // tree passes for 32+ right-hand sides on the lane-per-RHS kernels
+    int ring_tile = 0;                    // per-warp ring tile (HM_OPT_RING_TILE)
     hm_xfer *d_up = nullptr;
     std::vector<int> up_ptr;
     hm_m2l_row *d_m2l_rows = nullptr;
@@ -431,6 +436,9 @@ void set_vp_caps(hm_handle *h, const std::vector<hm_vpanel> &vps)
     }
     h->vp_cap = rows <= 128 ? (rows + 31) / 32 * 32 : 64;
     h->vp_wcap = std::min(width, HM_RMAX);
+    h->vp_wide = !vps.empty() && rows <= 128;
+    for (const hm_vpanel &p : vps)
+        if (p.ld != 20 || p.width != 20 || p.off % 4) h->vp_wide = false;
     std::vector<std::pair<int64_t, int64_t>> runs;
     for (const hm_vpanel &p : vps) runs.push_back({p.row0, (int64_t)p.nrows});
     std::sort(runs.begin(), runs.end());
@@ -711,7 +719,7 @@ thread_local const Sched *t_sched = nullptr;
 inline Sched configured_sched(const hm_handle *h)
 {
     return Sched{h->overlap, h->near_kernel, h->near_stages, h->tensor_cores ? 1 : 0,
-                 h->pdl >= 0 ? h->pdl : (h->storage != HM_F64 ? 1 : 0)};
+                 h->pdl >= 0 ? h->pdl : (h->storage != HM_F64 ? 1 : 0), h->ring_tile, h->wide_tree ? 1 : 0};
 }
 inline Sched cur_sched(const hm_handle *h) { return t_sched ? *t_sched : configured_sched(h); }
 inline Sched sched_for(const hm_handle *h, int k)
@@ -732,6 +740,7 @@ constexpr int kPartMaxK = 8;    // right-hand sides handled by the streaming pan
 inline unsigned warp_ctas(int64_t warps) { return (unsigned)((warps + kWarpsPerCta - 1) / kWarpsPerCta); }
 
 constexpr size_t kTaskSmemMax = 200 * 1024;     // shared memory of a band task kernel
+constexpr int kWideMinK = 32;                    // right-hand sides from which the lane-per-RHS tree kernels run
 
 // Index of the last non-empty band of a band pointer array, or -1.
 inline int last_band(const std::vector<int> &ptr)
@@ -854,13 +863,102 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     return HM_OK;
 }
 
+// Whether the tree passes of a product with k right-hand sides can run the
+// kernels for 32 and more (lane = right-hand side): rank 20, panels of the
+// stored layout, band tasks within shared memory.
+template <typename S, typename A>
+bool wide_tree_ok(const hm_handle *h, const MulArgs<S> &ma)
+{
+    if (!(std::is_same<S, A>::value && ma.k >= kWideMinK && h->r == 20 && h->vp_wide && !ma.xin &&
+          h->fstride % 4 == 0))
+        return false;
+    const size_t lv = (size_t)32 * 20 * sizeof(A);
+    return (2 * 400 * sizeof(A) + (size_t)h->band_locals[0] * lv) <= kTaskSmemMax &&
+           (2 * 400 * sizeof(A) + (size_t)h->band_locals[1] * lv) <= kTaskSmemMax &&
+           (size_t)kWideWarps * ((size_t)h->vp_cap * 20 + 32 * ((size_t)h->vp_cap + 4)) * sizeof(A) <= 200 * 1024;
+}
+
+// The tree passes for 32 and more right-hand sides: leaf_up_w, xfer_task_w
+// bands, m2l_w, the same stage and event structure as launch_tree_qc.
+template <typename S, typename A>
+int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing, cudaEvent_t mid,
+                     int mid_after, bool *ends_with_kernel)
+{
+    constexpr int R = 20;
+    const int k = ma.k;
+    const bool pdl_on = cur_sched(h).pdl && !(h->profile_mask & 0x3u);
+    bool chain = false;
+    const int64_t nq = (k + 31) / 32;
+    const A *T = static_cast<const A *>(h->d_T);
+    const MulArgs<A> &mw = reinterpret_cast<const MulArgs<A> &>(ma);
+    {
+        StageTimer tm(h, timing ? 0 : -1, st);
+        if (h->n_vp) {
+            const size_t smem = (size_t)kWideWarps * ((size_t)h->vp_cap * R + 32 * ((size_t)h->vp_cap + 4)) * sizeof(A);
+            HM_TRY(ensure_smem(leaf_up_w<A, R>, smem));
+            const int64_t warps = (int64_t)h->n_vp * nq;
+            HM_TRY(launch_k("leaf_up_w", leaf_up_w<A, R>, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
+                            dim3(32 * kWideWarps), smem, st, false, mw, h->d_vp, h->n_vp,
+                            static_cast<const A *>(h->d_V), t, h->vp_cap));
+            chain = true;
+        }
+        if (mid && mid_after == 2) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // leaf bases done
+        const size_t xsm = (2 * (size_t)R * R + (size_t)h->band_locals[0] * 32 * R) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_task_w<A, R, true>, xsm));
+        const int last = last_band(h->up_band_ptr);
+        for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
+            const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
+            if (!n) continue;
+            HM_TRY(launch_k("xfer_up_w", xfer_task_w<A, R, true>, dim3(n, (unsigned)nq), dim3(kWideTaskThreads), xsm,
+                            st, pdl_on && chain, h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, k,
+                            (int)bd != last ? 1 : 0));
+            chain = true;
+        }
+    }
+    if (mid && mid_after == 0) { HM_CK(cudaEventRecord(mid, st)); chain = false; }    // upward pass done
+    {
+        StageTimer tm(h, timing ? 1 : -1, st);
+        if (h->n_m2l_rows) {
+            const size_t smem = (size_t)kWideWarps * 2 * ((size_t)h->fstride + 32 * R) * sizeof(A);
+            HM_TRY(ensure_smem(m2l_w<A, R>, smem));
+            const int64_t warps = (int64_t)h->n_m2l_rows * nq;
+            HM_TRY(launch_k("m2l_w", m2l_w<A, R>, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
+                            dim3(32 * kWideWarps), smem, st, pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows,
+                            h->d_m2l_ents, static_cast<const A *>(h->d_F), h->fstride, t, s, k));
+            chain = true;
+        }
+        if (mid && mid_after == 1) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // far-field stage done
+        const size_t xsm = (2 * (size_t)R * R + (size_t)h->band_locals[1] * 32 * R) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_task_w<A, R, false>, xsm));
+        const int last = last_band(h->down_band_ptr);
+        for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
+            const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
+            if (!n) continue;
+            HM_TRY(launch_k("xfer_down_w", xfer_task_w<A, R, false>, dim3(n, (unsigned)nq), dim3(kWideTaskThreads),
+                            xsm, st, pdl_on && chain, h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T, s, k,
+                            (int)bd != last ? 1 : 0));
+            chain = true;
+        }
+    }
+    *ends_with_kernel = chain && pdl_on;
+    return HM_OK;
+}
+
 template <typename S, typename A>
 int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing,
                 cudaEvent_t mid = nullptr, int mid_after = 0, bool *ends_with_kernel = nullptr)
 {
     bool ends = false;
-    const int rc = ma.k == 1 ? launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing, mid, mid_after, &ends)
-                             : launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing, mid, mid_after, &ends);
+    int rc;
+    if constexpr (std::is_same<S, A>::value) {
+        if (cur_sched(h).wide && wide_tree_ok<S, A>(h, ma)) {
+            rc = launch_tree_wide<S, A>(h, ma, st, t, s, timing, mid, mid_after, &ends);
+            if (ends_with_kernel) *ends_with_kernel = ends;
+            return rc;
+        }
+    }
+    rc = ma.k == 1 ? launch_tree_qc<S, A, 1>(h, ma, st, t, s, timing, mid, mid_after, &ends)
+                   : launch_tree_qc<S, A, 8>(h, ma, st, t, s, timing, mid, mid_after, &ends);
     if (ends_with_kernel) *ends_with_kernel = ends;
     return rc;
 }
@@ -925,8 +1023,11 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
         // per-warp rings (the default for 3-8 FP32 right-hand sides): each warp
         // keeps several chunks of its run of segments in flight
         if (h->stream_ctas > 0 && (sc.near_kernel == 0 || sc.near_kernel == 3)) {
-            auto kern = ring_part<KB, FAR>;
-            const size_t smem = ring_smem_bytes(KB);
+            auto kern = sc.tile == 1   ? ring_part<KB, FAR, kRingTile[1].pf, kRingTile[1].ns>
+                        : sc.tile == 2 ? ring_part<KB, FAR, kRingTile[2].pf, kRingTile[2].ns>
+                                       : ring_part<KB, FAR, kRingTile[0].pf, kRingTile[0].ns>;
+            const RingTile tl = kRingTile[sc.tile >= 0 && sc.tile < kRingTiles ? sc.tile : 0];
+            const size_t smem = ring_smem_bytes(KB, tl.pf, tl.ns);
             HM_TRY(ensure_smem(kern, smem));
             HM_TRY(prefer_shared(kern));
             // about kRingSegsPerWarp segments per warp: CTAs retire through the
@@ -1188,11 +1289,17 @@ std::vector<Sched> sched_candidates(const hm_handle *h, int k, bool fp32)
     }
     std::vector<int> tcs = (fp32 && h->tc_ok && k >= kTensorCoreMinK) ? std::vector<int>{1, 0}
                                                                        : std::vector<int>{base.tensor_cores};
+    // ring tiles where the per-warp rings run (3-8 FP32 right-hand sides), and
+    // the lane-per-right-hand-side tree kernels on and off (32+, unless the
+    // option turned them off)
+    const bool ring = fp32 && k >= 3 && k <= kPartMaxK && h->stream_ctas > 0 && h->n_segs;
+    const std::vector<int> wides =
+        (tree && k >= kWideMinK && h->wide_tree) ? std::vector<int>{1, 0} : std::vector<int>{base.wide};
     std::vector<Sched> c{base};       // the configured schedule first, timed for comparison
     auto add = [&c](Sched s) {
         for (const Sched &o : c)
             if (o.overlap == s.overlap && o.near_kernel == s.near_kernel && o.near_stages == s.near_stages &&
-                o.tensor_cores == s.tensor_cores && o.pdl == s.pdl)
+                o.tensor_cores == s.tensor_cores && o.pdl == s.pdl && o.tile == s.tile && o.wide == s.wide)
                 return;
         c.push_back(s);
     };
@@ -1200,12 +1307,16 @@ std::vector<Sched> sched_candidates(const hm_handle *h, int k, bool fp32)
     for (int ov : overlaps)
         for (int nk : kernels)
             for (int tc : tcs)
-                for (int pd : pdls) {
-                    if (nk == 2)
-                        for (int ns : {3, 4, 6}) add(Sched{ov, nk, ns, tc, pd});
-                    else
-                        add(Sched{ov, nk, base.near_stages, tc, pd});
-                }
+                for (int pd : pdls)
+                    for (int wd : wides) {
+                        if (nk == 2) {
+                            for (int ns : {3, 4, 6}) add(Sched{ov, nk, ns, tc, pd, 0, wd});
+                        } else if (ring && (nk == 0 || nk == 3)) {
+                            for (int tl = 0; tl < kRingTiles; ++tl) add(Sched{ov, nk, base.near_stages, tc, pd, tl, wd});
+                        } else {
+                            add(Sched{ov, nk, base.near_stages, tc, pd, 0, wd});
+                        }
+                    }
     return c;
 }
 
@@ -1993,6 +2104,21 @@ int hm_mul_noalloc(hm_handle *h, const void *v, void *u, int accumulate, void *s
     return launch_pipeline<float, float>(h, ma, st, st, nullptr, nullptr, scratch, false);
 }
 
+int hm_autotune_choice(const hm_handle *h, int nrhs, int32_t *out, int nout)
+{
+    if (!h || nrhs <= 0 || !out || nout < 0) { set_error("hm_autotune_choice: bad argument"); return -HM_ERR_INVALID_ARG; }
+    const int b = sched_bucket(nrhs);
+    Sched sc;
+    {
+        std::lock_guard<std::mutex> lk(const_cast<hm_handle *>(h)->mu);
+        sc = h->tuned_ok[b] ? h->tuned[b] : configured_sched(h);
+    }
+    const int32_t v[7] = {sc.overlap, sc.near_kernel, sc.near_stages, sc.tensor_cores, sc.pdl, sc.tile, sc.wide};
+    const int n = std::min(nout, 7);
+    for (int i = 0; i < n; ++i) out[i] = v[i];
+    return n;
+}
+
 int hm_debug_fail_alloc(int64_t after)
 {
     if (after < -1) { set_error("hm_debug_fail_alloc: after must be >= -1"); return HM_ERR_INVALID_ARG; }
@@ -2020,6 +2146,16 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     if (!h) return HM_ERR_INVALID_ARG;
     // options of the bounded waits: no schedule changes, tuned schedules kept
     // (the host-buffer graph holds the old kernel arguments: dropped)
+    if (option == HM_OPT_WIDE_TREE) {
+        drop_host_graph(h);
+        {
+            std::lock_guard<std::mutex> lk(h->mu);
+            h->wide_tree = value != 0;
+            for (Sched &t : h->tuned) t.wide = value != 0 ? 1 : 0;
+        }
+        if (h->trans) return hm_configure(h->trans, option, value);
+        return HM_OK;
+    }
     if (option == HM_OPT_WAIT_LIMIT_NS || option == HM_OPT_TEST_STALL) {
         if (option == HM_OPT_WAIT_LIMIT_NS && (value < 1 || value > 2000000000)) {
             set_error("HM_OPT_WAIT_LIMIT_NS must be in [1, 2e9]");
@@ -2046,6 +2182,9 @@ int hm_configure(hm_handle *h, int option, int64_t value)
         if (value != 0) { set_error("HM_OPT_AUTOTUNED takes 0 (forget the tuned schedules)"); return HM_ERR_INVALID_ARG; }
         break;
     case HM_OPT_PDL: break;
+    case HM_OPT_RING_TILE:
+        if (value < 0 || value >= kRingTiles) { set_error("HM_OPT_RING_TILE must be 0, 1 or 2"); return HM_ERR_INVALID_ARG; }
+        break;
     default: set_error("unknown option %d", option); return HM_ERR_INVALID_ARG;
     }
     // the host-buffer product's captured graph follows the options: drop it;
@@ -2061,6 +2200,7 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     case HM_OPT_NEAR_KERNEL: h->near_kernel = (int)value; break;
     case HM_OPT_NEAR_STAGES: h->near_stages = (int)value; break;
     case HM_OPT_PDL: h->pdl = value != 0 ? 1 : 0; break;
+    case HM_OPT_RING_TILE: h->ring_tile = (int)value; break;
     default: break;
     }
     return HM_OK;

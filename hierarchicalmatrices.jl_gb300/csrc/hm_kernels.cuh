@@ -225,23 +225,44 @@ __global__ void stream_part(MulArgs<S> ma, const hm_seg *segs, const int *cta_se
 // Per-warp rings (hm_ring.cu), FP32 storage, KB = 4 or 8 right-hand sides:
 // warp w of the grid owns segments [w * nsegs / W, (w + 1) * nsegs / W) and
 // streams their part's columns (FAR: the far-field pieces, else the X
-// pieces; each part one contiguous column run) through kRingStages stages of
-// ring_stage_floats(KB) floats; segments of at most 64 rows, ld % 4 == 0,
+// pieces; each part one contiguous column run) through NS stages of
+// ring_stage_floats(KB, PF) floats; segments of at most 64 rows, ld % 4 == 0,
 // poff % 4 == 0.  Grid: a whole number of CTAs of kRingWarps warps, shared
-// memory ring_smem_bytes(KB).
+// memory ring_smem_bytes(KB, PF, NS).
 constexpr int kRingWarps = 2;
 constexpr int kRingSegsPerWarp = 24;      // segments per warp (the launch's grid follows from it)
-constexpr int kRingStages = 3;
 constexpr int kRingCols = 32;              // columns per chunk at most (lane c gathers column c)
-constexpr int kRingPanelFloats = 768;      // panel values per chunk at most (3 KB)
-__host__ __device__ constexpr int ring_stage_floats(int kb) { return kRingPanelFloats + kRingCols * kb; }
-__host__ __device__ constexpr size_t ring_smem_bytes(int kb)
+// The compiled tiles: panel values per stage (at most) and stages.
+struct RingTile { int pf, ns; };
+constexpr int kRingTiles = 3;
+constexpr RingTile kRingTile[kRingTiles] = {{768, 3}, {512, 4}, {1024, 3}};
+__host__ __device__ constexpr int ring_stage_floats(int kb, int pf) { return pf + kRingCols * kb; }
+__host__ __device__ constexpr size_t ring_smem_bytes(int kb, int pf, int ns)
 {
-    return (size_t)kRingWarps * kRingStages * ring_stage_floats(kb) * sizeof(float);
+    return (size_t)kRingWarps * ns * ring_stage_floats(kb, pf) * sizeof(float);
 }
-template <int KB, bool FAR>
+template <int KB, bool FAR, int PF, int NS>
 __global__ void ring_part(MulArgs<float> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const float *P,
                           const float *s, const float *t, int r, float *yfar, int64_t ldf);
+
+// Tree passes for 32 and more right-hand sides (hm_wide.cu): lane q of a
+// warp owns right-hand side q of a chunk of 32; R (the rank) a multiple of 4.
+// m2l_w: one warp per (row slot, chunk), shared memory
+// kWideWarps * 2 * (fstride + 32 R) values; leaf_up_w: one warp per (panel,
+// chunk), panels row-major with ld == width == R and at most cap rows (a
+// multiple of 8), shared memory kWideWarps * (cap R + 32 (cap + 4)) values;
+// xfer_task_w: one CTA of kWideTaskThreads per (task, chunk), shared memory
+// (2 R^2 + locals * 32 R) values.
+constexpr int kWideWarps = 4;
+constexpr int kWideTaskThreads = 256;
+template <typename A, int R>
+__global__ void m2l_w(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const A *F, int fstride, const A *t,
+                      A *s, int k);
+template <typename A, int R>
+__global__ void leaf_up_w(MulArgs<A> ma, const hm_vpanel *vp, int npanels, const A *V, A *t, int cap);
+template <typename A, int R, bool UP>
+__global__ void xfer_task_w(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *coef, int k,
+                            int early);
 
 // Double-float panels (hm_df.cu, HM_DF64 storage): panels_to_df turns FP64
 // panel values into (h, l) FP32 pairs in place; expand_df multiplies them on

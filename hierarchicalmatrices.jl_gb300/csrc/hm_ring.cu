@@ -8,11 +8,13 @@
 // contiguous run in HBM) together with the chunk's right-hand-side entries
 // g[c][q].  Chunks go through a ring of kRingStages shared-memory stages with
 // cp.async: while chunk j is multiplied, chunks j+1 .. j+kRingStages-1 are in
-// flight, across segment boundaries, so a warp keeps about 13 KB of HBM reads
-// outstanding without holding them in registers.  Lane l owns rows 2l and
+// flight, across segment boundaries, so a warp keeps several KB of HBM reads
+// outstanding without holding them in registers.  The stage size and count
+// (the tile: PF panel values x NS stages) are template parameters; the
+// autotuner picks among the compiled tiles (kRingTile).  Lane l owns rows 2l and
 // 2l+1 of the current segment (8-byte reads of the staged columns) and
 // accumulates KB right-hand sides with FMA, folding the partial sums into
-// compensated (TwoSum) pairs every 32-63 columns, as the per-segment warp
+// compensated (TwoSum) pairs at most every 64 columns, as the per-segment warp
 // kernel does.  Only cp.async groups of the warp's own lanes are waited on
 // (cp.async.wait_group, then __syncwarp): no barrier spans warps or kernels.
 #include "hm_kernels.cuh"
@@ -50,13 +52,14 @@ __device__ __forceinline__ void copy4(float *dst, const float *src) { async_copy
 
 }  // namespace
 
-template <int KB, bool FAR>
+template <int KB, bool FAR, int PF, int NS>
 __global__ void __launch_bounds__(kRingWarps * 32)
     ring_part(MulArgs<float> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const float *P,
               const float *s, const float *t, int r, float *yfar, int64_t ldf)
 {
     extern __shared__ __align__(16) unsigned char ring_smem[];
-    constexpr int SF = ring_stage_floats(KB);
+    constexpr int kRingStages = NS, kRingPanelFloats = PF;
+    constexpr int SF = ring_stage_floats(KB, PF);
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     if constexpr (FAR) pdl_wait();                             // the downward pass's coefficients are ready
     const int64_t gw = (int64_t)blockIdx.x * kRingWarps + wib;
@@ -240,13 +243,14 @@ __global__ void __launch_bounds__(kRingWarps * 32)
     async_wait_all();                                           // empty groups: nothing lands after exit
 }
 
-template __global__ void ring_part<4, false>(MulArgs<float>, const hm_seg *, int, const hm_piece *, const float *,
-                                             const float *, const float *, int, float *, int64_t);
-template __global__ void ring_part<4, true>(MulArgs<float>, const hm_seg *, int, const hm_piece *, const float *,
-                                            const float *, const float *, int, float *, int64_t);
-template __global__ void ring_part<8, false>(MulArgs<float>, const hm_seg *, int, const hm_piece *, const float *,
-                                             const float *, const float *, int, float *, int64_t);
-template __global__ void ring_part<8, true>(MulArgs<float>, const hm_seg *, int, const hm_piece *, const float *,
-                                            const float *, const float *, int, float *, int64_t);
+#define HM_INST_RING(KB, PF, NS)                                                                             \
+    template __global__ void ring_part<KB, false, PF, NS>(MulArgs<float>, const hm_seg *, int, const hm_piece *, \
+                                                          const float *, const float *, const float *, int,     \
+                                                          float *, int64_t);                                    \
+    template __global__ void ring_part<KB, true, PF, NS>(MulArgs<float>, const hm_seg *, int, const hm_piece *,  \
+                                                         const float *, const float *, const float *, int,      \
+                                                         float *, int64_t);
+HM_INST_RING(4, 768, 3) HM_INST_RING(4, 512, 4) HM_INST_RING(4, 1024, 3)
+HM_INST_RING(8, 768, 3) HM_INST_RING(8, 512, 4) HM_INST_RING(8, 1024, 3)
 
 }  // namespace hm

@@ -1,0 +1,344 @@
+// Tree passes for 32 and more right-hand sides: lane q of a warp owns
+// right-hand side q of a chunk of 32 and accumulates all R coefficients of it
+// in registers.  Written for sm_103a.
+//
+// With the basis width R (= rank, 20) on the lanes, as the kernels for up to 8
+// right-hand sides have it, 12 of 32 lanes idle and every FMA needs its own
+// shared-memory read of the right-hand side.  Here the small dense operand of
+// a step (an R x R far-field block F, a transfer matrix, or R-value rows of a
+// basis panel) is read from shared memory as 16-byte broadcasts and the
+// right-hand side's own values as one 16-byte read per four, so about four of
+// five instructions are FMAs.  All are small GEMMs:
+//   m2l_w:       s[slot][q][:] = sum_e F_e t[yslot_e][q][:]         (R x R times R)
+//   leaf_up_w:   t[slot][q][:] = V^T x[rows][q]                      (R x nrows times nrows)
+//   xfer_task_w: t[parent] = sum_c T_c^T t[child_c], s[child_c] += T_c s[parent]
+// Shared memory: m2l_w two stages per warp of (one F block, the column slot's
+// 32 x R coefficients), cp.async with 16-byte copies; leaf_up_w per warp the
+// panel (nrows x R) and the 32 right-hand sides' rows, [q][j] with a row
+// stride of 4 mod 8 words (conflict-free 16-byte reads by eight lanes);
+// xfer_task_w per CTA the two transfer matrices and the task's local vectors.
+#include "hm_kernels.cuh"
+#include "hm_async.cuh"
+
+namespace hm {
+
+namespace {
+
+// four consecutive values from 16-byte aligned shared memory
+__device__ __forceinline__ void ld4(const float *p, float *v)
+{
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ld4(const double *p, double *v)
+{
+    const double2 a = *reinterpret_cast<const double2 *>(p);
+    const double2 b = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+template <typename A>
+__device__ __forceinline__ void st4(A *p, const A *v);
+template <>
+__device__ __forceinline__ void st4<float>(float *p, const float *v)
+{
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void st4<double>(double *p, const double *v)
+{
+    reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+}
+
+// 16-byte copies of `bytes` (a multiple of 16) from global to shared memory by the warp
+__device__ __forceinline__ void warp_copy16(void *dst, const void *src, int bytes, int lane)
+{
+    const char *s = static_cast<const char *>(src);
+    char *d = static_cast<char *>(dst);
+    for (int i = lane * 16; i < bytes; i += 32 * 16) async_copy16(d + i, s + i);
+}
+
+}  // namespace
+
+// One warp per (row slot, chunk of 32 right-hand sides).  F blocks are R x R
+// column-major (F[m + R n]) with fstride values between blocks; coefficients
+// coef[(slot * k + q) * R + m].  Needs R % 4 == 0 and fstride % 4 == 0.
+template <typename A, int R>
+__global__ void __launch_bounds__(kWideWarps * 32)
+    m2l_w(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const A *F, int fstride, const A *t, A *s,
+          int k)
+{
+    extern __shared__ __align__(16) unsigned char wide_smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nq = (k + 31) >> 5;
+    const int64_t w = (int64_t)blockIdx.x * kWideWarps + wib;
+    pdl_trigger();
+    pdl_wait();                                                // the upward pass's coefficients are ready
+    if (w >= (int64_t)nrows * nq) return;
+    const hm_m2l_row Rw = rows[w / nq];
+    const int q0 = (int)(w % nq) * 32, qc = min(32, k - q0);
+    const int stage_vals = fstride + 32 * R;
+    A *buf = reinterpret_cast<A *>(wide_smem) + (size_t)wib * 2 * stage_vals;
+    auto fetch = [&](int e, int b) {
+        const hm_m2l_ent E = ents[e];
+        A *fb = buf + b * stage_vals;
+        warp_copy16(fb, F + E.foff, R * R * (int)sizeof(A), lane);
+        warp_copy16(fb + fstride, t + ((int64_t)E.yslot * k + q0) * R, qc * R * (int)sizeof(A), lane);
+        async_commit();
+    };
+    A acc[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) acc[m] = A(0);
+    if (Rw.begin < Rw.end) fetch(Rw.begin, 0);
+    for (int e = Rw.begin; e < Rw.end; ++e) {
+        const int b = (e - Rw.begin) & 1;
+        if (e + 1 < Rw.end) {
+            fetch(e + 1, b ^ 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            async_wait_all();
+        }
+        __syncwarp();
+        const A *fb = buf + b * stage_vals;
+        const A *tq = fb + fstride + lane * R;                 // this lane's right-hand side (rows past qc unused)
+#pragma unroll
+        for (int n = 0; n < R; n += 4) {
+            A tv[4];
+            ld4(tq + n, tv);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const A *col = fb + (n + u) * R;
+#pragma unroll
+                for (int m = 0; m < R; m += 4) {
+                    A f[4];
+                    ld4(col + m, f);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[m + i] = fma(f[i], tv[u], acc[m + i]);
+                }
+            }
+        }
+        __syncwarp();                                          // stage b is refilled by the next fetch
+    }
+    if (lane < qc) {
+        A *sp = s + ((int64_t)Rw.slot * k + q0 + lane) * R;
+#pragma unroll
+        for (int m = 0; m < R; m += 4) st4<A>(sp + m, acc + m);
+    }
+}
+
+// One warp per (explicit basis panel, chunk of 32 right-hand sides):
+// t[slot][q][col0 + m] = sum_j V[j][m] x[row0 + j][q], the panel row-major
+// (V[j * R + m], ld == width == R), at most cap rows (a multiple of 8).
+template <typename A, int R>
+__global__ void __launch_bounds__(kWideWarps * 32)
+    leaf_up_w(MulArgs<A> ma, const hm_vpanel *vp, int npanels, const A *V, A *t, int cap)
+{
+    extern __shared__ __align__(16) unsigned char wide_smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int k = ma.k, nq = (k + 31) >> 5;
+    const int64_t w = (int64_t)blockIdx.x * kWideWarps + wib;
+    pdl_trigger();
+    if (w >= (int64_t)npanels * nq) return;
+    const hm_vpanel Pn = vp[w / nq];
+    const int q0 = (int)(w % nq) * 32, qc = min(32, k - q0);
+    const int xs_stride = cap + 4;                             // 4 mod 8 words
+    A *Vs = reinterpret_cast<A *>(wide_smem) + (size_t)wib * (cap * R + 32 * xs_stride);
+    A *Xs = Vs + cap * R;
+    const int nr = Pn.nrows;
+    // the panel: one contiguous run of nr * R values
+    warp_copy16(Vs, V + Pn.off, nr * R * (int)sizeof(A), lane);
+    async_commit();
+    // the right-hand sides: lanes walk rows (coalesced), right-hand side by
+    // right-hand side; rows up to a multiple of 4 are zero-filled
+    const int nr4 = (nr + 3) & ~3;
+    for (int q = 0; q < 32; ++q) {
+        const A *xq = ma.x + Pn.row0 * ma.incx + (int64_t)(q0 + q) * ma.ldx;
+        for (int j = lane; j < nr4; j += 32)
+            Xs[q * xs_stride + j] = (q < qc && j < nr) ? xq[(int64_t)j * ma.incx] : A(0);
+    }
+    async_wait_all();
+    __syncwarp();
+    A acc[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) acc[m] = A(0);
+    const A *xr = Xs + lane * xs_stride;
+    for (int j = 0; j < nr4; j += 4) {
+        A xv[4];
+        ld4(xr + j, xv);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (j + u >= nr) break;
+            const A *row = Vs + (j + u) * R;
+#pragma unroll
+            for (int m = 0; m < R; m += 4) {
+                A v[4];
+                ld4(row + m, v);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[m + i] = fma(v[i], xv[u], acc[m + i]);
+            }
+        }
+    }
+    if (lane < qc) {
+        A *tp = t + ((int64_t)Pn.slot * k + q0 + lane) * R + Pn.col0;
+#pragma unroll
+        for (int m = 0; m < R; m += 4) st4<A>(tp + m, acc + m);
+    }
+}
+
+// Transfer band tasks (the task-local numbering of xfer_up_task /
+// xfer_down_task), one CTA per (task, chunk of 32 right-hand sides), warps
+// taking the records of a level, lane q the chunk's right-hand side q.  Local
+// coefficient vectors L[local][q][0 .. R) in shared memory, after the two
+// transfer matrices (upward: as stored, T_c[m' R + m]; downward: transposed,
+// so that both read R contiguous values per step).  Needs R % 4 == 0.
+//   upward:   t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m']
+//   downward: s[child_c][m'] += sum_m T_c[m', m] s[parent][m]
+template <typename A, int R, bool UP>
+__global__ void __launch_bounds__(kWideTaskThreads)
+    xfer_task_w(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *coef, int k,
+                int early)
+{
+    extern __shared__ __align__(16) unsigned char wide_smem[];
+    A *Ts = reinterpret_cast<A *>(wide_smem);
+    A *L = Ts + 2 * R * R;
+    constexpr int LV = 32 * R;                                 // values of one local vector
+    const hm_task tk = tasks[blockIdx.x];
+    const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
+    const int q0 = blockIdx.y * 32, qc = min(32, k - q0);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (early) pdl_trigger();
+    if (UP) {
+        for (int i = threadIdx.x; i < 2 * R * R; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
+    } else {
+        // T_c transposed: Ts[c][m][m'] = T_c[m', m]
+        for (int i = threadIdx.x; i < 2 * R * R; i += blockDim.x) {
+            const int c = i / (R * R), mm = i % (R * R), m = mm / R, mp = mm % R;
+            async_copy<sizeof(A)>(Ts + i, T + c * R * R + mp * R + m);
+        }
+    }
+    pdl_wait();                                                // inputs of the band are ready
+    // external inputs: warps take records, the warp copies a 32 x R block
+    for (int rec = warp; rec < nrec; rec += nw) {
+        const hm_xfer X = ents[e0 + rec];
+#pragma unroll
+        for (int c = 0; c < (UP ? 2 : 3); ++c) {
+            int lc, slot;
+            if (UP) {
+                lc = c ? (X.pad >> 16) : (X.pad & 0xffff);
+                slot = c ? X.c1 : X.c0;
+                if (lc < nrec) continue;                       // produced by an earlier level of this task
+            } else if (c < 2) {
+                lc = 2 * rec + c;                              // children start from their far-field values
+                slot = c ? X.c1 : X.c0;
+            } else {
+                lc = X.pad;
+                slot = X.slot;
+                if (lc < 2 * nrec) continue;                   // a child of an earlier level of this task
+            }
+            warp_copy16(L + (int64_t)lc * LV, coef + ((int64_t)slot * k + q0) * R, qc * R * (int)sizeof(A), lane);
+        }
+    }
+    async_wait_all();
+    __syncthreads();
+    for (int st = tk.step0; st < tk.step1; ++st) {
+        const hm_step S = steps[st];
+        for (int w = warp; w < S.e1 - S.e0; w += nw) {
+            const int e = S.e0 + w;
+            const hm_xfer X = ents[e];
+            if (UP) {
+                const A *c0 = L + (int64_t)(X.pad & 0xffff) * LV + lane * R;
+                const A *c1 = L + (int64_t)(X.pad >> 16) * LV + lane * R;
+                A acc[R];
+#pragma unroll
+                for (int m = 0; m < R; ++m) acc[m] = A(0);
+#pragma unroll
+                for (int mp = 0; mp < R; mp += 4) {
+                    A a[4], b[4];
+                    ld4(c0 + mp, a);
+                    ld4(c1 + mp, b);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+                        for (int m = 0; m < R; m += 4) {
+                            A t0[4], t1[4];
+                            ld4(Ts + (mp + u) * R + m, t0);
+                            ld4(Ts + R * R + (mp + u) * R + m, t1);
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) acc[m + i] = fma(t1[i], b[u], fma(t0[i], a[u], acc[m + i]));
+                        }
+                    }
+                }
+                A *out = L + (int64_t)(e - e0) * LV + lane * R;
+#pragma unroll
+                for (int m = 0; m < R; m += 4) st4<A>(out + m, acc + m);
+                if (lane < qc) {
+                    A *g = coef + ((int64_t)X.slot * k + q0 + lane) * R;
+#pragma unroll
+                    for (int m = 0; m < R; m += 4) st4<A>(g + m, acc + m);
+                }
+            } else {
+                const A *p = L + (int64_t)X.pad * LV + lane * R;
+                A *o0 = L + (int64_t)(2 * (e - e0)) * LV + lane * R;
+                A *o1 = o0 + LV;
+                A a0[R], a1[R];
+#pragma unroll
+                for (int m = 0; m < R; m += 4) {
+                    ld4(o0 + m, a0 + m);
+                    ld4(o1 + m, a1 + m);
+                }
+#pragma unroll
+                for (int m = 0; m < R; m += 4) {
+                    A pv[4];
+                    ld4(p + m, pv);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+                        for (int mq = 0; mq < R; mq += 4) {
+                            A t0[4], t1[4];
+                            ld4(Ts + (m + u) * R + mq, t0);
+                            ld4(Ts + R * R + (m + u) * R + mq, t1);
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                a0[mq + i] = fma(t0[i], pv[u], a0[mq + i]);
+                                a1[mq + i] = fma(t1[i], pv[u], a1[mq + i]);
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int m = 0; m < R; m += 4) {
+                    st4<A>(o0 + m, a0 + m);
+                    st4<A>(o1 + m, a1 + m);
+                }
+                if (lane < qc) {
+                    A *g0 = coef + ((int64_t)X.c0 * k + q0 + lane) * R;
+                    A *g1 = coef + ((int64_t)X.c1 * k + q0 + lane) * R;
+#pragma unroll
+                    for (int m = 0; m < R; m += 4) {
+                        st4<A>(g0 + m, a0 + m);
+                        st4<A>(g1 + m, a1 + m);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template __global__ void m2l_w<float, 20>(const hm_m2l_row *, int, const hm_m2l_ent *, const float *, int,
+                                          const float *, float *, int);
+template __global__ void m2l_w<double, 20>(const hm_m2l_row *, int, const hm_m2l_ent *, const double *, int,
+                                           const double *, double *, int);
+template __global__ void leaf_up_w<float, 20>(MulArgs<float>, const hm_vpanel *, int, const float *, float *, int);
+template __global__ void leaf_up_w<double, 20>(MulArgs<double>, const hm_vpanel *, int, const double *, double *,
+                                               int);
+template __global__ void xfer_task_w<float, 20, true>(const hm_task *, const hm_step *, const hm_xfer *, const float *,
+                                                      float *, int, int);
+template __global__ void xfer_task_w<float, 20, false>(const hm_task *, const hm_step *, const hm_xfer *,
+                                                       const float *, float *, int, int);
+template __global__ void xfer_task_w<double, 20, true>(const hm_task *, const hm_step *, const hm_xfer *,
+                                                       const double *, double *, int, int);
+template __global__ void xfer_task_w<double, 20, false>(const hm_task *, const hm_step *, const hm_xfer *,
+                                                        const double *, double *, int, int);
+
+}  // namespace hm

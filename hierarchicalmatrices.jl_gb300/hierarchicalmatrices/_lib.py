@@ -36,6 +36,8 @@ HM_OPT_AUTOTUNED = 5
 HM_OPT_PDL = 6
 HM_OPT_WAIT_LIMIT_NS = 7
 HM_OPT_TEST_STALL = 8
+HM_OPT_WIDE_TREE = 9
+HM_OPT_RING_TILE = 10
 HM_DEV_WAIT_TIMEOUT = 1
 HM_PIECE_COEF, HM_PIECE_X, HM_PIECE_TCOEF = 0, 1, 2
 
@@ -74,7 +76,7 @@ STAGES = ("up", "down", "expand", "far", "product")
 EXPORTED = (
     "hm_status_string", "hm_last_error", "hm_version", "hm_blockrank", "hm_indsplit",
     "hm_kernelmatrix_build", "hm_kernelmatrix_batch_build", "hm_mul_t", "hm_mul_drow", "hm_size", "hm_storage", "hm_stats", "hm_device_status", "hm_chebyshev", "hm_mul", "hm_mul_strided",
-    "hm_mul_host", "hm_mul_noalloc", "hm_debug_fail_alloc", "hm_direct_rows", "hm_configure", "hm_autotune", "hm_profile", "hm_profile_read", "hm_profile_timeline", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
+    "hm_mul_host", "hm_mul_noalloc", "hm_debug_fail_alloc", "hm_direct_rows", "hm_configure", "hm_autotune", "hm_autotune_choice", "hm_profile", "hm_profile_read", "hm_profile_timeline", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
     "hm_bary_factors", "hm_lr_svd", "hm_gemm_batched", "hm_axpby_batched", "hm_potrf_batched",
     "hm_solve_transposed", "hm_potrf_batched_async", "hm_trtri_batched",
@@ -214,6 +216,8 @@ def _load():
     L.hm_mul_host.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
     L.hm_mul_noalloc.restype = ctypes.c_int
     L.hm_mul_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_int, _vp]
+    L.hm_autotune_choice.restype = ctypes.c_int
+    L.hm_autotune_choice.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.c_int]
     L.hm_debug_fail_alloc.restype = ctypes.c_int
     L.hm_debug_fail_alloc.argtypes = [_i64]
     L.hm_direct_rows.restype = ctypes.c_int

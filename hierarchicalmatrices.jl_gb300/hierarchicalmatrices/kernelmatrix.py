@@ -167,6 +167,18 @@ class KernelMatrix:
             raise DeviceWaitTimeout(
                 f"a kernel of this KernelMatrix gave up waiting (device status {code}): its products are invalid")
 
+    def set_wide_tree(self, enable=True):
+        """Tree passes of products with 32 or more right-hand sides on the
+        lane-per-right-hand-side kernels (True, the default) or on the
+        kernels for chunks of 8."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_WIDE_TREE, 1 if enable else 0))
+
+    def set_ring_tile(self, tile):
+        """Tile of the per-warp rings (3-8 FP32 right-hand sides): 0 = up to
+        768 panel values x 3 stages per warp (default), 1 = 512 x 4,
+        2 = 1024 x 3."""
+        check(lib.hm_configure(self._h, _lib.HM_OPT_RING_TILE, int(tile)))
+
     def set_wait_limit(self, ns):
         """Nanoseconds (1 .. 2e9, default 2e9) after which a wait of the
         streamed near-field or tensor-core panel kernel gives up."""
@@ -359,8 +371,23 @@ class KernelMatrix:
         choice = (ctypes.c_int32 * 5)()
         ms = (ctypes.c_double * 2)()
         check(lib.hm_autotune(self._h, int(nrhs), int(reps), _stream_ptr(stream), choice, ms))
-        return {"overlap": choice[0], "near_kernel": choice[1], "near_stages": choice[2],
-                "tensor_cores": bool(choice[3]), "pdl": bool(choice[4]), "ms": ms[0], "ms_configured": ms[1]}
+        out = self.schedule(nrhs)
+        out.update(ms=ms[0], ms_configured=ms[1])
+        return out
+
+    def schedule(self, nrhs=1):
+        """The schedule products with ``nrhs`` right-hand sides run with (the
+        autotuner's choice for its bucket, else the configured options),
+        including the ring tile (panel values x stages per warp) and whether the
+        tree passes run on the lane-per-right-hand-side kernels."""
+        v = (ctypes.c_int32 * 7)()
+        n = lib.hm_autotune_choice(self._h, int(nrhs), v, 7)
+        if n < 0:
+            check(-n)
+        tiles = ((768, 3), (512, 4), (1024, 3))
+        return {"overlap": v[0], "near_kernel": v[1], "near_stages": v[2], "tensor_cores": bool(v[3]),
+                "pdl": bool(v[4]), "ring_tile": {"panel_values": tiles[v[5]][0], "stages": tiles[v[5]][1]},
+                "wide_tree": bool(v[6])}
 
     def forget_autotune(self):
         """Drop the autotuned schedules: products run with the configured options."""

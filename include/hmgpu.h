@@ -268,7 +268,18 @@ enum {
        the first wait of every CTA of those two kernels waits on a barrier
        nothing arrives on, so it runs out after HM_OPT_WAIT_LIMIT_NS.  Keeps
        autotuned schedules.  No reference counterpart. */
-    HM_OPT_TEST_STALL = 8
+    HM_OPT_TEST_STALL = 8,
+    /* HM_OPT_WIDE_TREE (default 1): products with 32 or more right-hand sides
+       (rank 20) run the tree passes (leaf bases, transfers, far-field blocks)
+       on kernels that give each lane one right-hand side of a chunk of 32 and
+       all 20 coefficients of it; 0 keeps the kernels with the coefficients on
+       the lanes and chunks of 8 right-hand sides.  Applies to the autotuned
+       schedules too (it overrides their choice).  No reference counterpart. */
+    HM_OPT_WIDE_TREE = 9,
+    /* HM_OPT_RING_TILE (default 0): the per-warp rings' tile for 3-8 FP32
+       right-hand sides: 0 = up to 768 panel values x 3 stages per warp,
+       1 = 512 x 4, 2 = 1024 x 3.  No reference counterpart. */
+    HM_OPT_RING_TILE = 10
 };
 int hm_configure(hm_handle *h, int option, int64_t value);
 
@@ -279,9 +290,11 @@ int hm_configure(hm_handle *h, int option, int64_t value);
    bucket (1, 2, 3-4, 5-8, 9-16, 17-32, 33-64, 65-128, 129+): later hm_mul,
    hm_mul_strided, hm_mul_host and hm_mul_drow calls of that bucket run with
    it, including inside stream capture.  Candidates: HM_OPT_OVERLAP 0..4
-   (0..1 above 8 right-hand sides), HM_OPT_NEAR_KERNEL 0, 1 (FP32 with 3-8
+   (0..1 above 8 right-hand sides), HM_OPT_NEAR_KERNEL 0 (with each of the
+   three ring tiles for 3-8 FP32 right-hand sides), 1 (FP32 with 3-8
    right-hand sides) or 2 with HM_OPT_NEAR_STAGES 3, 4 or 6 (up to 8
-   right-hand sides), HM_OPT_TENSOR_CORES
+   right-hand sides), HM_OPT_WIDE_TREE on or off (32 or more),
+   HM_OPT_TENSOR_CORES
    on or off (FP32, 16 or more), HM_OPT_PDL on or off.  Inputs are scratch vectors allocated on
    `stream` and freed before return; synchronous; not allowed while `stream`
    is being captured.  choice (host, 5 values, may be NULL) receives the
@@ -291,6 +304,15 @@ int hm_configure(hm_handle *h, int option, int64_t value);
    call it while products on the same handle are being issued from other
    host threads. */
 int hm_autotune(hm_handle *h, int nrhs, int reps, void *stream, int32_t *choice, double *ms);
+
+/* The schedule products with nrhs right-hand sides run with (hm_autotune's
+   choice for nrhs's bucket, else the configured options): out[0..6] =
+   overlap, near kernel, near stages, tensor-core flag, PDL flag, ring tile
+   (0: 768 panel values x 3 stages per warp, 1: 512 x 4, 2: 1024 x 3; for 3-8
+   FP32 right-hand sides) and the lane-per-right-hand-side tree flag (32+).
+   Returns the number of values written (<= nout), or minus a status.  No
+   reference counterpart. */
+int hm_autotune_choice(const hm_handle *h, int nrhs, int32_t *out, int nout);
 
 /* Test hook for the allocation-failure paths (no reference counterpart: the
    reference allocates through Julia's GC).  after >= 0: the next `after`
