@@ -146,6 +146,30 @@ template __global__ void fill_segments<float, true>(FillArgs, const hm_seg *, co
 // expand_part<.., true> adds the far field U s.
 
 
+// N consecutive values from 16-byte aligned shared memory, as 16-byte loads
+// where N values fill them (the chunks of right-hand sides below are stored
+// right-hand side fastest, so that one step's N values are adjacent).
+template <int N, typename A>
+__device__ __forceinline__ void ld_vec(const A *p, A *v)
+{
+    if constexpr (sizeof(A) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < N / 4; ++i) {
+            const float4 w = reinterpret_cast<const float4 *>(p)[i];
+            v[4 * i] = w.x; v[4 * i + 1] = w.y; v[4 * i + 2] = w.z; v[4 * i + 3] = w.w;
+        }
+    } else if constexpr (sizeof(A) == 8 && N % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < N / 2; ++i) {
+            const double2 w = reinterpret_cast<const double2 *>(p)[i];
+            v[2 * i] = w.x; v[2 * i + 1] = w.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = p[i];
+    }
+}
+
 // t[slot][col0 + m] = (V^T x)[m] for each explicit basis panel.  One warp
 // per panel, looping over chunks of QC right-hand sides; lane m owns column m
 // of the row-major panel (width <= 32, row stride ld).  Panels of up to cap
@@ -179,7 +203,7 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
     };
     if (P.nrows <= cap && P.ld == pw && pw <= wcap) {
         // the panel once; x chunks of QC right-hand sides double-buffered,
-        // right-hand side major xs[b][qq * cap + j] (lanes walk rows)
+        // row major xs[b][j * QC + qq] (lanes walk rows)
         S *Vs = reinterpret_cast<S *>(smem_raw + (size_t)wib * leaf_up_warp_bytes<S, A, QC>(cap, wcap));
         A *xs = reinterpret_cast<A *>(Vs + cap * wcap);
         const int nel = P.nrows * pw;
@@ -198,14 +222,14 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
                 for (int j = lane; j < P.nrows; j += 32) {
                     const int64_t e = (P.row0 + j) * ma.incx + (int64_t)(q0 + qq) * ma.ldx;
                     if (qq >= qc) {
-                        d[qq * cap + j] = A(0);
+                        d[j * QC + qq] = A(0);
                     } else if (xcopy) {
                         // host-mapped source: plain loads, stored here and into x
                         const S v = xsrc[e];
-                        d[qq * cap + j] = (A)v;
+                        d[j * QC + qq] = (A)v;
                         xcopy[e] = v;
                     } else {
-                        async_copy<sizeof(A)>(d + qq * cap + j, ma.x + e);
+                        async_copy<sizeof(A)>(d + j * QC + qq, ma.x + e);
                     }
                 }
             async_commit();
@@ -226,8 +250,10 @@ __global__ void leaf_up(MulArgs<S> ma, const hm_vpanel *vp, int npanels, const S
             if (lane < pw) {
                 for (int j = 0; j < P.nrows; ++j) {
                     const A v = (A)Vs[j * pw + lane];
+                    A xv[QC];
+                    ld_vec<QC>(xb + j * QC, xv);
 #pragma unroll
-                    for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xb[qq * cap + j]);
+                    for (int qq = 0; qq < QC; ++qq) acc[qq].add(v, xv[qq]);
                 }
             }
             store(q0, min(QC, k - q0), acc);
@@ -316,7 +342,7 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
 // Task-local numbering (records' pad, set by the planner): upward, record i
 // produces local i and reads locals pad & 0xffff, pad >> 16; downward,
 // record i's children are locals 2i, 2i + 1 and its parent is local pad.
-// L holds QC x r values per local.
+// L holds r x QC values per local, right-hand side fastest (L[local][m][qq]).
 template <typename A, int QC>
 __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
                              int r, int k, int early)
@@ -339,11 +365,11 @@ __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const h
             const int lc = c ? (X.pad >> 16) : (X.pad & 0xffff);
             if (lc < nrec || ln >= r) continue;           // produced by an earlier level of this task
             const A *src = t + ((int64_t)(c ? X.c1 : X.c0) * k + q0) * r + ln;
-            A *d = L + (int64_t)lc * QC * r + ln;
+            A *d = L + (int64_t)lc * QC * r + ln * QC;
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq) {
-                if (qq < qc) async_copy<sizeof(A)>(d + qq * r, src + (int64_t)qq * r);
-                else d[qq * r] = A(0);
+                if (qq < qc) async_copy<sizeof(A)>(d + qq, src + (int64_t)qq * r);
+                else d[qq] = A(0);
             }
         }
     }
@@ -364,12 +390,15 @@ __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const h
                 for (int qq = 0; qq < QC; ++qq) acc[qq] = 0;
                 for (int mp = 0; mp < r; ++mp) {
                     const A a0 = Ts[mp * r + lane], a1 = Ts[r * r + mp * r + lane];
+                    A v0[QC], v1[QC];
+                    ld_vec<QC>(c0 + mp * QC, v0);
+                    ld_vec<QC>(c1 + mp * QC, v1);
 #pragma unroll
-                    for (int qq = 0; qq < QC; ++qq) acc[qq] += a0 * c0[qq * r + mp] + a1 * c1[qq * r + mp];
+                    for (int qq = 0; qq < QC; ++qq) acc[qq] += a0 * v0[qq] + a1 * v1[qq];
                 }
 #pragma unroll
                 for (int qq = 0; qq < QC; ++qq) {
-                    out[qq * r + lane] = acc[qq];
+                    out[lane * QC + qq] = acc[qq];
                     if (qq < qc) t[((int64_t)X.slot * k + q0 + qq) * r + lane] = acc[qq];
                 }
             }
@@ -409,11 +438,11 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
             }
             if (ln >= r) continue;
             const A *src = s + ((int64_t)slot * k + q0) * r + ln;
-            A *d = L + (int64_t)lc * QC * r + ln;
+            A *d = L + (int64_t)lc * QC * r + ln * QC;
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq) {
-                if (qq < qc) async_copy<sizeof(A)>(d + qq * r, src + (int64_t)qq * r);
-                else d[qq * r] = A(0);
+                if (qq < qc) async_copy<sizeof(A)>(d + qq, src + (int64_t)qq * r);
+                else d[qq] = A(0);
             }
         }
     }
@@ -434,18 +463,19 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
                 for (int qq = 0; qq < QC; ++qq) { a0[qq] = 0; a1[qq] = 0; }
                 for (int m = 0; m < r; ++m) {
                     const A t0 = Ts[lane * r + m], t1 = Ts[r * r + lane * r + m];
+                    A pv[QC];
+                    ld_vec<QC>(p + m * QC, pv);
 #pragma unroll
                     for (int qq = 0; qq < QC; ++qq) {
-                        const A v = p[qq * r + m];
-                        a0[qq] += t0 * v;
-                        a1[qq] += t1 * v;
+                        a0[qq] += t0 * pv[qq];
+                        a1[qq] += t1 * pv[qq];
                     }
                 }
 #pragma unroll
                 for (int qq = 0; qq < QC; ++qq) {
-                    const A v0 = o0[qq * r + lane] + a0[qq], v1 = o1[qq * r + lane] + a1[qq];
-                    o0[qq * r + lane] = v0;
-                    o1[qq * r + lane] = v1;
+                    const A v0 = o0[lane * QC + qq] + a0[qq], v1 = o1[lane * QC + qq] + a1[qq];
+                    o0[lane * QC + qq] = v0;
+                    o1[lane * QC + qq] = v1;
                     if (qq < qc) {
                         s[((int64_t)X.c0 * k + q0 + qq) * r + lane] = v0;
                         s[((int64_t)X.c1 * k + q0 + qq) * r + lane] = v1;
@@ -491,8 +521,8 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
             const A *src = t + ((int64_t)E.yslot * k + q0) * r + lane;
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq) {
-                if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + lane, src + (int64_t)qq * r);
-                else tb[qq * HM_RMAX + lane] = A(0);
+                if (qq < qc) async_copy<sizeof(A)>(tb + lane * QC + qq, src + (int64_t)qq * r);
+                else tb[lane * QC + qq] = A(0);
             }
         }
         async_commit();
@@ -515,8 +545,10 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
         if (lane < r) {
             for (int n = 0; n < r; ++n) {
                 const A f = (A)fb[lane + r * n];
+                A tv[QC];
+                ld_vec<QC>(tb + n * QC, tv);
 #pragma unroll
-                for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tb[qq * HM_RMAX + n];
+                for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tv[qq];
             }
         }
         __syncwarp();                         // buffer buf is refilled by the next fetch
@@ -566,8 +598,8 @@ __global__ void m2l_k(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents,
                     const A *src = t + ((int64_t)ents[e0 + b].yslot * k + q0) * r + lane;
 #pragma unroll
                     for (int qq = 0; qq < QC; ++qq) {
-                        if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + lane, src + (int64_t)qq * r);
-                        else tb[qq * HM_RMAX + lane] = A(0);
+                        if (qq < qc) async_copy<sizeof(A)>(tb + lane * QC + qq, src + (int64_t)qq * r);
+                        else tb[lane * QC + qq] = A(0);
                     }
                 }
                 async_commit();
@@ -589,8 +621,10 @@ __global__ void m2l_k(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents,
                 if (lane < r) {
                     for (int n = 0; n < r; ++n) {
                         const A f = (A)fb[lane + r * n];
+                        A tv[QC];
+                        ld_vec<QC>(tb + n * QC, tv);
 #pragma unroll
-                        for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tb[qq * HM_RMAX + n];
+                        for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tv[qq];
                     }
                 }
                 __syncwarp();

@@ -149,13 +149,18 @@ __global__ void __launch_bounds__(kWideWarps * 32)
     warp_copy16(Vs, V + Pn.off, nr * R * (int)sizeof(A), lane);
     async_commit();
     // the right-hand sides: lanes walk rows (coalesced), right-hand side by
-    // right-hand side; rows up to a multiple of 4 are zero-filled
+    // right-hand side, every copy in flight at once (cp.async); rows up to a
+    // multiple of 4 and right-hand sides past the chunk are zero-filled
     const int nr4 = (nr + 3) & ~3;
     for (int q = 0; q < 32; ++q) {
         const A *xq = ma.x + Pn.row0 * ma.incx + (int64_t)(q0 + q) * ma.ldx;
-        for (int j = lane; j < nr4; j += 32)
-            Xs[q * xs_stride + j] = (q < qc && j < nr) ? xq[(int64_t)j * ma.incx] : A(0);
+        for (int j = lane; j < nr4; j += 32) {
+            A *d = Xs + q * xs_stride + j;
+            if (q < qc && j < nr) async_copy<sizeof(A)>(d, xq + (int64_t)j * ma.incx);
+            else *d = A(0);
+        }
     }
+    async_commit();
     async_wait_all();
     __syncwarp();
     A acc[R];
