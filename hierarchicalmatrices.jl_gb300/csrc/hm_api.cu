@@ -875,7 +875,7 @@ bool wide_tree_ok(const hm_handle *h, const MulArgs<S> &ma)
     const size_t lv = (size_t)32 * 20 * sizeof(A);
     return (2 * 400 * sizeof(A) + (size_t)h->band_locals[0] * lv) <= kTaskSmemMax &&
            (2 * 400 * sizeof(A) + (size_t)h->band_locals[1] * lv) <= kTaskSmemMax &&
-           (size_t)kWideWarps * ((size_t)h->vp_cap * 20 + 32 * ((size_t)h->vp_cap + 4)) * sizeof(A) <= 200 * 1024;
+           (size_t)kWideWarps * ((size_t)h->vp_cap * 20 + 64 * ((size_t)h->vp_cap + 4)) * sizeof(A) <= 200 * 1024;
 }
 
 // The tree passes for 32 and more right-hand sides: leaf_up_w, xfer_task_w
@@ -894,10 +894,14 @@ int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, 
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
-            const size_t smem = (size_t)kWideWarps * ((size_t)h->vp_cap * R + 32 * ((size_t)h->vp_cap + 4)) * sizeof(A);
-            HM_TRY(ensure_smem(leaf_up_w<A, R>, smem));
-            const int64_t warps = (int64_t)h->n_vp * nq;
-            HM_TRY(launch_k("leaf_up_w", leaf_up_w<A, R>, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
+            // two right-hand sides per lane from 64 on (half the shared-memory reads per FMA)
+            const int qpl = k >= 64 ? 2 : 1;
+            auto kern = qpl == 2 ? leaf_up_w<A, R, 2> : leaf_up_w<A, R, 1>;
+            const size_t smem =
+                (size_t)kWideWarps * ((size_t)h->vp_cap * R + 32 * qpl * ((size_t)h->vp_cap + 4)) * sizeof(A);
+            HM_TRY(ensure_smem(kern, smem));
+            const int64_t warps = (int64_t)h->n_vp * ((k + 32 * qpl - 1) / (32 * qpl));
+            HM_TRY(launch_k("leaf_up_w", kern, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
                             dim3(32 * kWideWarps), smem, st, false, mw, h->d_vp, h->n_vp,
                             static_cast<const A *>(h->d_V), t, h->vp_cap));
             chain = true;
@@ -919,10 +923,12 @@ int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, 
     {
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
-            const size_t smem = (size_t)kWideWarps * 2 * ((size_t)h->fstride + 32 * R) * sizeof(A);
-            HM_TRY(ensure_smem(m2l_w<A, R>, smem));
-            const int64_t warps = (int64_t)h->n_m2l_rows * nq;
-            HM_TRY(launch_k("m2l_w", m2l_w<A, R>, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
+            const int qpl = k >= 64 ? 2 : 1;
+            auto kern = qpl == 2 ? m2l_w<A, R, 2> : m2l_w<A, R, 1>;
+            const size_t smem = (size_t)kWideWarps * 2 * ((size_t)h->fstride + 32 * qpl * R) * sizeof(A);
+            HM_TRY(ensure_smem(kern, smem));
+            const int64_t warps = (int64_t)h->n_m2l_rows * ((k + 32 * qpl - 1) / (32 * qpl));
+            HM_TRY(launch_k("m2l_w", kern, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
                             dim3(32 * kWideWarps), smem, st, pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows,
                             h->d_m2l_ents, static_cast<const A *>(h->d_F), h->fstride, t, s, k));
             chain = true;

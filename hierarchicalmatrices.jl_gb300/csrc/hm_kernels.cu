@@ -342,7 +342,8 @@ __global__ void xfer_up_band(const hm_task *tasks, const hm_step *steps, const h
 // Task-local numbering (records' pad, set by the planner): upward, record i
 // produces local i and reads locals pad & 0xffff, pad >> 16; downward,
 // record i's children are locals 2i, 2i + 1 and its parent is local pad.
-// L holds r x QC values per local, right-hand side fastest (L[local][m][qq]).
+// Upward, L holds r x QC values per local, right-hand side fastest
+// (L[local][m][qq]); downward QC x r (L[local][qq][m]).
 template <typename A, int QC>
 __global__ void xfer_up_task(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *t,
                              int r, int k, int early)
@@ -438,11 +439,11 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
             }
             if (ln >= r) continue;
             const A *src = s + ((int64_t)slot * k + q0) * r + ln;
-            A *d = L + (int64_t)lc * QC * r + ln * QC;
+            A *d = L + (int64_t)lc * QC * r + ln;
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq) {
-                if (qq < qc) async_copy<sizeof(A)>(d + qq, src + (int64_t)qq * r);
-                else d[qq] = A(0);
+                if (qq < qc) async_copy<sizeof(A)>(d + qq * r, src + (int64_t)qq * r);
+                else d[qq * r] = A(0);
             }
         }
     }
@@ -463,19 +464,18 @@ __global__ void xfer_down_task(const hm_task *tasks, const hm_step *steps, const
                 for (int qq = 0; qq < QC; ++qq) { a0[qq] = 0; a1[qq] = 0; }
                 for (int m = 0; m < r; ++m) {
                     const A t0 = Ts[lane * r + m], t1 = Ts[r * r + lane * r + m];
-                    A pv[QC];
-                    ld_vec<QC>(p + m * QC, pv);
 #pragma unroll
                     for (int qq = 0; qq < QC; ++qq) {
-                        a0[qq] += t0 * pv[qq];
-                        a1[qq] += t1 * pv[qq];
+                        const A v = p[qq * r + m];
+                        a0[qq] += t0 * v;
+                        a1[qq] += t1 * v;
                     }
                 }
 #pragma unroll
                 for (int qq = 0; qq < QC; ++qq) {
-                    const A v0 = o0[lane * QC + qq] + a0[qq], v1 = o1[lane * QC + qq] + a1[qq];
-                    o0[lane * QC + qq] = v0;
-                    o1[lane * QC + qq] = v1;
+                    const A v0 = o0[qq * r + lane] + a0[qq], v1 = o1[qq * r + lane] + a1[qq];
+                    o0[qq * r + lane] = v0;
+                    o1[qq * r + lane] = v1;
                     if (qq < qc) {
                         s[((int64_t)X.c0 * k + q0 + qq) * r + lane] = v0;
                         s[((int64_t)X.c1 * k + q0 + qq) * r + lane] = v1;
@@ -521,8 +521,8 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
             const A *src = t + ((int64_t)E.yslot * k + q0) * r + lane;
 #pragma unroll
             for (int qq = 0; qq < QC; ++qq) {
-                if (qq < qc) async_copy<sizeof(A)>(tb + lane * QC + qq, src + (int64_t)qq * r);
-                else tb[lane * QC + qq] = A(0);
+                if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + lane, src + (int64_t)qq * r);
+                else tb[qq * HM_RMAX + lane] = A(0);
             }
         }
         async_commit();
@@ -545,10 +545,8 @@ __global__ void m2l(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, c
         if (lane < r) {
             for (int n = 0; n < r; ++n) {
                 const A f = (A)fb[lane + r * n];
-                A tv[QC];
-                ld_vec<QC>(tb + n * QC, tv);
 #pragma unroll
-                for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tv[qq];
+                for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tb[qq * HM_RMAX + n];
             }
         }
         __syncwarp();                         // buffer buf is refilled by the next fetch
@@ -598,8 +596,8 @@ __global__ void m2l_k(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents,
                     const A *src = t + ((int64_t)ents[e0 + b].yslot * k + q0) * r + lane;
 #pragma unroll
                     for (int qq = 0; qq < QC; ++qq) {
-                        if (qq < qc) async_copy<sizeof(A)>(tb + lane * QC + qq, src + (int64_t)qq * r);
-                        else tb[lane * QC + qq] = A(0);
+                        if (qq < qc) async_copy<sizeof(A)>(tb + qq * HM_RMAX + lane, src + (int64_t)qq * r);
+                        else tb[qq * HM_RMAX + lane] = A(0);
                     }
                 }
                 async_commit();
@@ -621,10 +619,8 @@ __global__ void m2l_k(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents,
                 if (lane < r) {
                     for (int n = 0; n < r; ++n) {
                         const A f = (A)fb[lane + r * n];
-                        A tv[QC];
-                        ld_vec<QC>(tb + n * QC, tv);
 #pragma unroll
-                        for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tv[qq];
+                        for (int qq = 0; qq < QC; ++qq) acc[qq] += f * tb[qq * HM_RMAX + n];
                     }
                 }
                 __syncwarp();

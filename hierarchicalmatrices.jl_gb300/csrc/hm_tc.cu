@@ -18,13 +18,13 @@
 // each accumulation relative to the running sum, so the corrections (2^-8 of
 // it) must not ride on the large sum.
 //
-// K runs in chunks of 32 columns through a three-stage pipeline: the
-// right-hand-side entries of chunk c + 2 are gathered into a ring of raw
-// shared-memory stages with cp.async and its panel values loaded into
-// registers while chunk c is split into the operand buffer and multiplied,
-// so two chunks' loads are always in flight.  The operand buffer is
-// refilled once the MMAs of the previous chunk have completed (tcgen05.commit
-// to an mbarrier); they are short beside the split.
+// K runs in chunks of 32 columns through a two-stage pipeline: every thread
+// loads its share of chunk c + 1 (right-hand-side pairs and panel pairs) from
+// global memory into registers while it splits chunk c into one of two
+// operand buffers, and thread 0 issues chunk c's MMAs as soon as the buffer
+// is written; a buffer is refilled only after the MMAs that read it (chunk
+// c - 2) have completed (tcgen05.commit to that buffer's mbarrier), so the
+// split of chunk c overlaps the MMAs of chunk c - 1.
 //
 // Operand layout (SWIZZLE_NONE, K-major, 16-bit): 8-row x 16-byte core
 // matrices; element (row, k) of a 32-column chunk sits at byte
@@ -44,20 +44,17 @@ constexpr int TC_M = 128;          // right-hand sides per CTA (MMA M)
 constexpr int TC_N = 64;           // rows per segment (MMA N)
 constexpr int TC_KC = 32;          // columns per K chunk
 constexpr int TC_THREADS = 256;
-constexpr int TC_STAGES = 3;       // raw right-hand-side stages (two chunks ahead)
-constexpr int TC_GSTRIDE = 40;     // raw right-hand-side row stride (floats): conflict-free 8-byte split reads
 constexpr int TC_GI = TC_M * TC_KC / 2 / TC_THREADS;   // right-hand-side pairs per thread and chunk (8)
 constexpr int TC_PI = TC_N * TC_KC / 2 / TC_THREADS;   // panel pairs per thread and chunk (4)
 
 struct TcSmem {
-    float rawG[TC_STAGES][TC_M * TC_GSTRIDE];   // [q][c] per stage
-    uint32_t G3[3][TC_M * TC_KC / 2];           // BF16 pieces h, m, l of G, K-major core-matrix layout
-    uint32_t P3[3][TC_N * TC_KC / 2];           // BF16 pieces of P^T
-    uint64_t mma_bar;                           // completion of a chunk's MMAs
-    uint64_t never_bar;                         // nothing arrives on it (stall hook)
+    uint32_t G3[2][3][TC_M * TC_KC / 2];   // two buffers of the BF16 pieces h, m, l of G (K-major core matrices)
+    uint32_t P3[2][3][TC_N * TC_KC / 2];   // two buffers of the BF16 pieces of P^T
+    uint64_t mma_bar[2];                   // completion of the MMAs that read buffer 0 / 1
+    uint64_t never_bar;                    // nothing arrives on it (stall hook)
     uint32_t tmem_base;
 };
-static_assert(sizeof(TcSmem::rawG) >= sizeof(float) * TC_M * 65, "epilogue stage fits the raw ring");
+static_assert(sizeof(TcSmem::G3) >= sizeof(float) * TC_M * 65, "epilogue stage fits the operand buffers");
 // followed in shared memory by the segment's column table: for each panel
 // column, the source of its first right-hand side and the element step
 // between right-hand sides (maxw entries of each)
@@ -164,7 +161,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        mbar_init(&S.mma_bar, 1);
+        mbar_init(&S.mma_bar[0], 1);
+        mbar_init(&S.mma_bar[1], 1);
         mbar_init(&S.never_bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -195,65 +193,64 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         colbase[c] = base;
         colstride[c] = step;
     }
-    // 8-row groups of A that hold live right-hand sides; the others stay zero
+    // 8-row groups of A that hold live right-hand sides; the others stay zero in both buffers
     const int live_groups = (qc + 7) >> 3;
-    for (int p = 0; p < 3; ++p)
-        for (int w = live_groups * 128 + tid; w < TC_M * TC_KC / 2; w += TC_THREADS) S.G3[p][w] = 0u;
+    for (int b = 0; b < 2; ++b)
+        for (int p = 0; p < 3; ++p)
+            for (int w = live_groups * 128 + tid; w < TC_M * TC_KC / 2; w += TC_THREADS) S.G3[b][p][w] = 0u;
     __syncthreads();
 
-    // right-hand-side entries of chunk ch into raw stage b (4-byte cp.async,
-    // q = i / 32, column c = i % 32; columns past the chunk are never read)
-    auto load_g = [&](int ch, int b) {
+    // This thread's pairs of a chunk.  Pair j of the right-hand sides is
+    // (q, columns c, c + 1) with q = qb + 16 j, and pair j of the panel is
+    // (row, columns c, c + 1) with row = rb + 16 j: a warp covers 8 right-hand
+    // sides (rows) x 4 column pairs, the thread's columns are the same for all
+    // j, so that only the q / row offsets change from pair to pair.
+    const int gq0 = (warp >> 2) * 8 + (lane >> 2), gc = ((warp & 3) * 4 + (lane & 3)) * 2;
+    const int pr0 = (warp >> 2) * 8 + (lane & 7), pcol = ((warp & 3) * 4 + (lane >> 3)) * 2;
+    // output words: kmajor_pair_word(q, c) advances by 256 words per 16 rows
+    const int gw0 = kmajor_pair_word(gq0, gc), pw0 = kmajor_pair_word(pr0, pcol);
+    // global loads of chunk ch into registers (zeros outside the live block)
+    auto load = [&](int ch, float2 *gv, float2 *pv) {
         const int c0 = ch * TC_KC, cols = min(TC_KC, W - c0);
-        float *dst = S.rawG[b];
-        for (int i = tid; i < qc * TC_KC; i += TC_THREADS) {
-            const int q = i >> 5, c = i & 31;
-            if (c < cols) async_copy<4>(dst + q * TC_GSTRIDE + c, colbase[c0 + c] + q * colstride[c0 + c]);
+        const bool l0 = gc < cols, l1 = gc + 1 < cols;
+        const float *b0 = l0 ? colbase[c0 + gc] : nullptr, *b1 = l1 ? colbase[c0 + gc + 1] : nullptr;
+        const int64_t s0 = l0 ? colstride[c0 + gc] : 0, s1 = l1 ? colstride[c0 + gc + 1] : 0;
+#pragma unroll
+        for (int j = 0; j < TC_GI; ++j) {
+            const int q = gq0 + 16 * j;
+            float2 v = make_float2(0.f, 0.f);
+            if (q < qc) {
+                if (l0) v.x = b0[q * s0];
+                if (l1) v.y = b1[q * s1];
+            }
+            gv[j] = v;
         }
-    };
-    // this thread's panel pairs of chunk ch into registers: pair j (row, columns c, c + 1)
-    // for i = tid + j * 256 (a warp covers 8 rows x 4 column pairs)
-    auto p_item = [&](int j, int &row, int &c) {
-        const int i = tid + j * TC_THREADS, blk = i >> 5, l = i & 31;
-        row = (blk >> 2) * 8 + (l & 7);
-        c = ((blk & 3) * 4 + (l >> 3)) * 2;
-    };
-    auto load_p = [&](int ch, float2 *pv) {
-        const int c0 = ch * TC_KC, cols = min(TC_KC, W - c0);
-        const float *pb = P + G.poff + (int64_t)c0 * G.ld;
+        const bool m0 = pcol < cols, m1 = pcol + 1 < cols;
+        const float *pb = P + G.poff + (int64_t)(c0 + pcol) * G.ld;
 #pragma unroll
         for (int j = 0; j < TC_PI; ++j) {
-            int row, c;
-            p_item(j, row, c);
+            const int row = pr0 + 16 * j;
             float2 v = make_float2(0.f, 0.f);
             if (row < G.ld) {
-                if (c < cols) v.x = __ldcs(pb + (int64_t)c * G.ld + row);
-                if (c + 1 < cols) v.y = __ldcs(pb + (int64_t)(c + 1) * G.ld + row);
+                if (m0) v.x = __ldcs(pb + row);
+                if (m1) v.y = __ldcs(pb + G.ld + row);
             }
             pv[j] = v;
         }
     };
-    // split raw stage b and the panel registers of chunk ch into the operand buffer
-    auto split = [&](int ch, int b, const float2 *pv) {
-        const int cols = min(TC_KC, W - ch * TC_KC);
-        // right-hand sides: a warp covers 8 right-hand sides x 4 column pairs; only
-        // the 8-row groups holding live right-hand sides (the rest were zeroed once)
-        for (int i = tid; i < live_groups * 4 * 32; i += TC_THREADS) {
-            const int blk = i >> 5, l = i & 31;
-            const int q = (blk >> 2) * 8 + (l >> 2), c = ((blk & 3) * 4 + (l & 3)) * 2;
-            float2 v = make_float2(0.f, 0.f);
-            if (q < qc) v = *reinterpret_cast<const float2 *>(&S.rawG[b][q * TC_GSTRIDE + c]);
-            if (c >= cols || q >= qc) v.x = 0.f;
-            if (c + 1 >= cols || q >= qc) v.y = 0.f;
-            const int w = kmajor_pair_word(q, c);
-            split3x2(v.x, v.y, S.G3[0][w], S.G3[1][w], S.G3[2][w]);
+    // split the registers into operand buffer b
+    auto split = [&](int b, const float2 *gv, const float2 *pv) {
+#pragma unroll
+        for (int j = 0; j < TC_GI; ++j) {
+            if (gq0 + 16 * j < live_groups * 8) {
+                const int w = gw0 + 256 * j;
+                split3x2(gv[j].x, gv[j].y, S.G3[b][0][w], S.G3[b][1][w], S.G3[b][2][w]);
+            }
         }
 #pragma unroll
         for (int j = 0; j < TC_PI; ++j) {
-            int row, c;
-            p_item(j, row, c);
-            const int w = kmajor_pair_word(row, c);
-            split3x2(pv[j].x, pv[j].y, S.P3[0][w], S.P3[1][w], S.P3[2][w]);
+            const int w = pw0 + 256 * j;
+            split3x2(pv[j].x, pv[j].y, S.P3[b][0][w], S.P3[b][1][w], S.P3[b][2][w]);
         }
     };
 
@@ -261,37 +258,24 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     bool ok = true;
     bool stall_first = stall != 0;
     int committed = -1;                                         // last chunk whose MMAs were committed
-    float2 pv[TC_STAGES][TC_PI];
-    // prologue: chunks 0 and 1 in flight (one cp.async group each)
+    float2 gv[2][TC_GI], pv[2][TC_PI];
+    if (nch > 0) load(0, gv[0], pv[0]);
+    // two chunks per trip, so that the register sets are indexed statically
+    for (int ch = 0; ch < nch && ok; ch += 2) {
 #pragma unroll
-    for (int i = 0; i < TC_STAGES - 1; ++i) {
-        if (i < nch) {
-            load_g(i, i);
-            load_p(i, pv[i]);
-        }
-        async_commit();
-    }
-    // three chunks per trip, so that the panel registers are indexed statically
-    for (int ch = 0; ch < nch && ok; ch += TC_STAGES) {
-#pragma unroll
-        for (int u = 0; u < TC_STAGES; ++u) {
-            const int cc = ch + u;
+        for (int h = 0; h < 2; ++h) {
+            const int cc = ch + h;
             if (cc >= nch) break;
-            asm volatile("cp.async.wait_group %0;" ::"n"(TC_STAGES - 2) : "memory");   // chunk cc landed
-            __syncthreads();                                    // ... for every thread; stage (cc - 1) % 3 is free
-            if (cc + TC_STAGES - 1 < nch) {
-                load_g(cc + TC_STAGES - 1, (u + TC_STAGES - 1) % TC_STAGES);
-                load_p(cc + TC_STAGES - 1, pv[(u + TC_STAGES - 1) % TC_STAGES]);
-            }
-            async_commit();
-            // the operand buffer was read by the MMAs of chunk cc - 1
-            if (cc >= 1 && !mbar_wait_first(&S.mma_bar, (cc - 1) & 1, wait_ns, stall_first, &S.never_bar)) ok = false;
+            if (cc + 1 < nch) load(cc + 1, gv[h ^ 1], pv[h ^ 1]);
+            // buffer h was read by the MMAs of chunk cc - 2
+            if (cc >= 2 && !mbar_wait_first(&S.mma_bar[h], ((cc - 2) >> 1) & 1, wait_ns, stall_first, &S.never_bar))
+                ok = false;
             if (__syncthreads_or(!ok)) {
                 ok = false;
                 break;
             }
             tc_fence_after();
-            split(cc, u, pv[u]);
+            split(h, gv[h], pv[h]);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // operands visible to the tensor core
             tc_fence_before();
             __syncthreads();
@@ -304,26 +288,25 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
                     const uint32_t off = ks * 256;              // two core matrices of K per step
 #pragma unroll
                     for (int j = 0; j < 6; ++j) {
-                        const uint64_t ad = umma_desc(reinterpret_cast<const char *>(S.G3[pa[j]]) + off, 128, 512);
-                        const uint64_t bd = umma_desc(reinterpret_cast<const char *>(S.P3[pb[j]]) + off, 128, 512);
+                        const uint64_t ad = umma_desc(reinterpret_cast<const char *>(S.G3[h][pa[j]]) + off, 128, 512);
+                        const uint64_t bd = umma_desc(reinterpret_cast<const char *>(S.P3[h][pb[j]]) + off, 128, 512);
                         const uint32_t dt = j == 0 ? tmem : tmem + TC_N;
                         umma_bf16(dt, ad, bd, idesc, (cc > 0 || ks > 0 || j > 1) ? 1 : 0);
                     }
                 }
-                umma_commit(&S.mma_bar);
+                umma_commit(&S.mma_bar[h]);
             }
             committed = cc;
         }
     }
-    // all MMAs done before reading D
+    // all MMAs done before reading D (a commit tracks every earlier MMA of the thread)
     if (ok && committed >= 0 &&
-        !mbar_wait_first(&S.mma_bar, committed & 1, wait_ns, stall_first, &S.never_bar))
+        !mbar_wait_first(&S.mma_bar[committed & 1], (committed >> 1) & 1, wait_ns, stall_first, &S.never_bar))
         ok = false;
     if (__syncthreads_or(!ok)) {
-        async_wait_all();
         if (tid == 0) {
             atomicExch(status, HM_DEV_WAIT_TIMEOUT);
-            if (committed >= 0) mbar_wait(&S.mma_bar, committed & 1, kDrainLimitNs);
+            if (committed >= 0) mbar_wait(&S.mma_bar[committed & 1], (committed >> 1) & 1, kDrainLimitNs);
         }
     } else if (nch == 0) {                                      // no columns: the rows are zero
         for (int i = tid; i < qc * G.nrows; i += TC_THREADS) {
@@ -332,12 +315,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             if (!ma.accumulate) *yp = 0.f;
         }
     } else {
-        async_wait_all();                                       // (only empty groups remain)
         tc_fence_after();
         // D row q (lane) x column row: this warp's 32 right-hand sides, all 64 rows,
-        // staged through shared memory (the raw ring, no longer read) for
+        // staged through shared memory (the operand buffers, no longer read) for
         // row-contiguous stores
-        float *Ys = &S.rawG[0][0];                              // [q][row], stride 65
+        float *Ys = reinterpret_cast<float *>(&S.G3[0][0][0]);  // [q][row], stride 65
         // warp w reads tensor-memory lanes 32 (w % 4) .. + 31, columns 32 (w / 4) .. + 31
         const int q = (warp & 3) * 32 + lane;
         const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;

@@ -60,24 +60,27 @@ __device__ __forceinline__ void warp_copy16(void *dst, const void *src, int byte
 
 }  // namespace
 
-// One warp per (row slot, chunk of 32 right-hand sides).  F blocks are R x R
-// column-major (F[m + R n]) with fstride values between blocks; coefficients
-// coef[(slot * k + q) * R + m].  Needs R % 4 == 0 and fstride % 4 == 0.
-template <typename A, int R>
+// One warp per (row slot, chunk of 32 QPL right-hand sides); lane l owns
+// right-hand sides l + 32 p, p < QPL (two per lane halve the shared-memory
+// reads per FMA).  F blocks are R x R column-major (F[m + R n]) with fstride
+// values between blocks; coefficients coef[(slot * k + q) * R + m].  Needs
+// R % 4 == 0 and fstride % 4 == 0.
+template <typename A, int R, int QPL>
 __global__ void __launch_bounds__(kWideWarps * 32)
     m2l_w(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const A *F, int fstride, const A *t, A *s,
           int k)
 {
     extern __shared__ __align__(16) unsigned char wide_smem[];
+    constexpr int QW = 32 * QPL;                               // right-hand sides of a warp
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int nq = (k + 31) >> 5;
+    const int nq = (k + QW - 1) / QW;
     const int64_t w = (int64_t)blockIdx.x * kWideWarps + wib;
     pdl_trigger();
     pdl_wait();                                                // the upward pass's coefficients are ready
     if (w >= (int64_t)nrows * nq) return;
     const hm_m2l_row Rw = rows[w / nq];
-    const int q0 = (int)(w % nq) * 32, qc = min(32, k - q0);
-    const int stage_vals = fstride + 32 * R;
+    const int q0 = (int)(w % nq) * QW, qc = min(QW, k - q0);
+    const int stage_vals = fstride + QW * R;
     A *buf = reinterpret_cast<A *>(wide_smem) + (size_t)wib * 2 * stage_vals;
     auto fetch = [&](int e, int b) {
         const hm_m2l_ent E = ents[e];
@@ -86,9 +89,11 @@ __global__ void __launch_bounds__(kWideWarps * 32)
         warp_copy16(fb + fstride, t + ((int64_t)E.yslot * k + q0) * R, qc * R * (int)sizeof(A), lane);
         async_commit();
     };
-    A acc[R];
+    A acc[QPL][R];
 #pragma unroll
-    for (int m = 0; m < R; ++m) acc[m] = A(0);
+    for (int p = 0; p < QPL; ++p)
+#pragma unroll
+        for (int m = 0; m < R; ++m) acc[p][m] = A(0);
     if (Rw.begin < Rw.end) fetch(Rw.begin, 0);
     for (int e = Rw.begin; e < Rw.end; ++e) {
         const int b = (e - Rw.begin) & 1;
@@ -100,11 +105,12 @@ __global__ void __launch_bounds__(kWideWarps * 32)
         }
         __syncwarp();
         const A *fb = buf + b * stage_vals;
-        const A *tq = fb + fstride + lane * R;                 // this lane's right-hand side (rows past qc unused)
+        const A *tq = fb + fstride + lane * R;                 // this lane's right-hand sides (rows past qc unused)
 #pragma unroll
         for (int n = 0; n < R; n += 4) {
-            A tv[4];
-            ld4(tq + n, tv);
+            A tv[QPL][4];
+#pragma unroll
+            for (int p = 0; p < QPL; ++p) ld4(tq + p * 32 * R + n, tv[p]);
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const A *col = fb + (n + u) * R;
@@ -113,46 +119,52 @@ __global__ void __launch_bounds__(kWideWarps * 32)
                     A f[4];
                     ld4(col + m, f);
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) acc[m + i] = fma(f[i], tv[u], acc[m + i]);
+                    for (int p = 0; p < QPL; ++p)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) acc[p][m + i] = fma(f[i], tv[p][u], acc[p][m + i]);
                 }
             }
         }
         __syncwarp();                                          // stage b is refilled by the next fetch
     }
-    if (lane < qc) {
-        A *sp = s + ((int64_t)Rw.slot * k + q0 + lane) * R;
 #pragma unroll
-        for (int m = 0; m < R; m += 4) st4<A>(sp + m, acc + m);
+    for (int p = 0; p < QPL; ++p) {
+        if (lane + 32 * p < qc) {
+            A *sp = s + ((int64_t)Rw.slot * k + q0 + lane + 32 * p) * R;
+#pragma unroll
+            for (int m = 0; m < R; m += 4) st4<A>(sp + m, acc[p] + m);
+        }
     }
 }
 
-// One warp per (explicit basis panel, chunk of 32 right-hand sides):
-// t[slot][q][col0 + m] = sum_j V[j][m] x[row0 + j][q], the panel row-major
-// (V[j * R + m], ld == width == R), at most cap rows (a multiple of 8).
-template <typename A, int R>
+// One warp per (explicit basis panel, chunk of 32 QPL right-hand sides), lane
+// l right-hand sides l + 32 p: t[slot][q][col0 + m] = sum_j V[j][m] x[row0 + j][q],
+// the panel row-major (V[j * R + m], ld == width == R), at most cap rows (a
+// multiple of 8).
+template <typename A, int R, int QPL>
 __global__ void __launch_bounds__(kWideWarps * 32)
     leaf_up_w(MulArgs<A> ma, const hm_vpanel *vp, int npanels, const A *V, A *t, int cap)
 {
     extern __shared__ __align__(16) unsigned char wide_smem[];
+    constexpr int QW = 32 * QPL;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int k = ma.k, nq = (k + 31) >> 5;
+    const int k = ma.k, nq = (k + QW - 1) / QW;
     const int64_t w = (int64_t)blockIdx.x * kWideWarps + wib;
     pdl_trigger();
     if (w >= (int64_t)npanels * nq) return;
     const hm_vpanel Pn = vp[w / nq];
-    const int q0 = (int)(w % nq) * 32, qc = min(32, k - q0);
+    const int q0 = (int)(w % nq) * QW, qc = min(QW, k - q0);
     const int xs_stride = cap + 4;                             // 4 mod 8 words
-    A *Vs = reinterpret_cast<A *>(wide_smem) + (size_t)wib * (cap * R + 32 * xs_stride);
+    A *Vs = reinterpret_cast<A *>(wide_smem) + (size_t)wib * (cap * R + QW * xs_stride);
     A *Xs = Vs + cap * R;
     const int nr = Pn.nrows;
     // the panel: one contiguous run of nr * R values
     warp_copy16(Vs, V + Pn.off, nr * R * (int)sizeof(A), lane);
-    async_commit();
     // the right-hand sides: lanes walk rows (coalesced), right-hand side by
     // right-hand side, every copy in flight at once (cp.async); rows up to a
     // multiple of 4 and right-hand sides past the chunk are zero-filled
     const int nr4 = (nr + 3) & ~3;
-    for (int q = 0; q < 32; ++q) {
+    for (int q = 0; q < QW; ++q) {
         const A *xq = ma.x + Pn.row0 * ma.incx + (int64_t)(q0 + q) * ma.ldx;
         for (int j = lane; j < nr4; j += 32) {
             A *d = Xs + q * xs_stride + j;
@@ -163,13 +175,16 @@ __global__ void __launch_bounds__(kWideWarps * 32)
     async_commit();
     async_wait_all();
     __syncwarp();
-    A acc[R];
+    A acc[QPL][R];
 #pragma unroll
-    for (int m = 0; m < R; ++m) acc[m] = A(0);
+    for (int p = 0; p < QPL; ++p)
+#pragma unroll
+        for (int m = 0; m < R; ++m) acc[p][m] = A(0);
     const A *xr = Xs + lane * xs_stride;
     for (int j = 0; j < nr4; j += 4) {
-        A xv[4];
-        ld4(xr + j, xv);
+        A xv[QPL][4];
+#pragma unroll
+        for (int p = 0; p < QPL; ++p) ld4(xr + p * 32 * xs_stride + j, xv[p]);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (j + u >= nr) break;
@@ -179,14 +194,19 @@ __global__ void __launch_bounds__(kWideWarps * 32)
                 A v[4];
                 ld4(row + m, v);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) acc[m + i] = fma(v[i], xv[u], acc[m + i]);
+                for (int p = 0; p < QPL; ++p)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[p][m + i] = fma(v[i], xv[p][u], acc[p][m + i]);
             }
         }
     }
-    if (lane < qc) {
-        A *tp = t + ((int64_t)Pn.slot * k + q0 + lane) * R + Pn.col0;
 #pragma unroll
-        for (int m = 0; m < R; m += 4) st4<A>(tp + m, acc + m);
+    for (int p = 0; p < QPL; ++p) {
+        if (lane + 32 * p < qc) {
+            A *tp = t + ((int64_t)Pn.slot * k + q0 + lane + 32 * p) * R + Pn.col0;
+#pragma unroll
+            for (int m = 0; m < R; m += 4) st4<A>(tp + m, acc[p] + m);
+        }
     }
 }
 
@@ -330,13 +350,11 @@ __global__ void __launch_bounds__(kWideTaskThreads)
     }
 }
 
-template __global__ void m2l_w<float, 20>(const hm_m2l_row *, int, const hm_m2l_ent *, const float *, int,
-                                          const float *, float *, int);
-template __global__ void m2l_w<double, 20>(const hm_m2l_row *, int, const hm_m2l_ent *, const double *, int,
-                                           const double *, double *, int);
-template __global__ void leaf_up_w<float, 20>(MulArgs<float>, const hm_vpanel *, int, const float *, float *, int);
-template __global__ void leaf_up_w<double, 20>(MulArgs<double>, const hm_vpanel *, int, const double *, double *,
-                                               int);
+#define HM_INST_WIDE(A, QPL)                                                                                \
+    template __global__ void m2l_w<A, 20, QPL>(const hm_m2l_row *, int, const hm_m2l_ent *, const A *, int,     \
+                                               const A *, A *, int);                                            \
+    template __global__ void leaf_up_w<A, 20, QPL>(MulArgs<A>, const hm_vpanel *, int, const A *, A *, int);
+HM_INST_WIDE(float, 1) HM_INST_WIDE(float, 2) HM_INST_WIDE(double, 1) HM_INST_WIDE(double, 2)
 template __global__ void xfer_task_w<float, 20, true>(const hm_task *, const hm_step *, const hm_xfer *, const float *,
                                                       float *, int, int);
 template __global__ void xfer_task_w<float, 20, false>(const hm_task *, const hm_step *, const hm_xfer *,
