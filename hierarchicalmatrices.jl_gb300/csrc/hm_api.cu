@@ -894,9 +894,10 @@ int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, 
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
-            // two right-hand sides per lane from 64 on (half the shared-memory reads per FMA)
-            const int qpl = k >= 64 ? 2 : 1;
-            auto kern = qpl == 2 ? leaf_up_w<A, R, 2> : leaf_up_w<A, R, 1>;
+            // one right-hand side per lane (measured at 256: 0.69 ms against 0.94 ms
+            // with two, whose larger staging halves the warps per SM)
+            const int qpl = 1;
+            auto kern = leaf_up_w<A, R, 1>;
             const size_t smem =
                 (size_t)kWideWarps * ((size_t)h->vp_cap * R + 32 * qpl * ((size_t)h->vp_cap + 4)) * sizeof(A);
             HM_TRY(ensure_smem(kern, smem));

@@ -164,12 +164,26 @@ __global__ void __launch_bounds__(kWideWarps * 32)
     // right-hand side, every copy in flight at once (cp.async); rows up to a
     // multiple of 4 and right-hand sides past the chunk are zero-filled
     const int nr4 = (nr + 3) & ~3;
-    for (int q = 0; q < QW; ++q) {
-        const A *xq = ma.x + Pn.row0 * ma.incx + (int64_t)(q0 + q) * ma.ldx;
-        for (int j = lane; j < nr4; j += 32) {
-            A *d = Xs + q * xs_stride + j;
-            if (q < qc && j < nr) async_copy<sizeof(A)>(d, xq + (int64_t)j * ma.incx);
-            else *d = A(0);
+    constexpr int VW = 16 / sizeof(A);                         // values per 16-byte copy
+    if (ma.incx == 1 && Pn.row0 % VW == 0 && ma.ldx % VW == 0 && nr % VW == 0) {
+        // rows of every right-hand side start on a 16-byte boundary: 16-byte copies,
+        // lane (q, piece) over the QW x nr / VW pieces
+        const int per_q = nr / VW;
+        for (int i = lane; i < QW * per_q; i += 32) {
+            const int q = i / per_q, v = i - q * per_q;
+            A *d = Xs + q * xs_stride + v * VW;
+            if (q < qc) async_copy16(d, ma.x + Pn.row0 + (int64_t)(q0 + q) * ma.ldx + v * VW);
+            else for (int u = 0; u < VW; ++u) d[u] = A(0);
+        }
+        for (int i = lane; i < QW * (nr4 - nr); i += 32) Xs[(i / (nr4 - nr)) * xs_stride + nr + i % (nr4 - nr)] = A(0);
+    } else {
+        for (int q = 0; q < QW; ++q) {
+            const A *xq = ma.x + Pn.row0 * ma.incx + (int64_t)(q0 + q) * ma.ldx;
+            for (int j = lane; j < nr4; j += 32) {
+                A *d = Xs + q * xs_stride + j;
+                if (q < qc && j < nr) async_copy<sizeof(A)>(d, xq + (int64_t)j * ma.incx);
+                else *d = A(0);
+            }
         }
     }
     async_commit();
