@@ -157,7 +157,7 @@ void transfer_matrices(int r, const std::vector<double> &x, const std::vector<do
 struct Sched {
     int overlap, near_kernel, near_stages, tensor_cores, pdl;
     int tile = 0;      // per-warp ring tile (kRingTile index) for 3-8 FP32 right-hand sides
-    int wide = 1;      // tree passes on the lane-per-right-hand-side kernels (32+ right-hand sides)
+    int wide = 1;      // tree passes on the lane-per-right-hand-side kernels: 0 never, 1 from 32, 2 from 2 RHS
 };
 
 // Right-hand-side buckets of the autotuned schedules: 1, 2, 3-4, 5-8, 9-16,
@@ -204,7 +204,7 @@ struct hm_handle {
     int vp_cap = 64, vp_wcap = HM_RMAX;   // leaf_up's shared-memory panel: rows (multiple of 32) x columns
     bool vp_covers_x = false;             // the leaf panels' rows partition [0, ny): leaf_up reads every x once
     bool vp_wide = false;                 // every leaf panel row-major with ld == width == 20 (leaf_up_w)
-    bool wide_tree = true;                // tree passes for 32+ right-hand sides on the lane-per-RHS kernels
+    int wide_tree = 1;                    // lane-per-RHS tree kernels: 0 never, 1 from 32 RHS, 2 from 2 (HM_OPT_WIDE_TREE)
     int ring_tile = 0;                    // per-warp ring tile (HM_OPT_RING_TILE)
     hm_xfer *d_up = nullptr;
     std::vector<int> up_ptr;
@@ -719,7 +719,7 @@ thread_local const Sched *t_sched = nullptr;
 inline Sched configured_sched(const hm_handle *h)
 {
     return Sched{h->overlap, h->near_kernel, h->near_stages, h->tensor_cores ? 1 : 0,
-                 h->pdl >= 0 ? h->pdl : (h->storage != HM_F64 ? 1 : 0), h->ring_tile, h->wide_tree ? 1 : 0};
+                 h->pdl >= 0 ? h->pdl : (h->storage != HM_F64 ? 1 : 0), h->ring_tile, h->wide_tree};
 }
 inline Sched cur_sched(const hm_handle *h) { return t_sched ? *t_sched : configured_sched(h); }
 inline Sched sched_for(const hm_handle *h, int k)
@@ -866,56 +866,62 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
 // Whether the tree passes of a product with k right-hand sides can run the
 // kernels for 32 and more (lane = right-hand side): rank 20, panels of the
 // stored layout, band tasks within shared memory.
+// Lane groups per warp of the lane-per-right-hand-side kernels for k right-hand
+// sides: four groups of 8 up to 8, two of 16 up to 16, one warp of 32 beyond.
+inline int wide_groups(int k) { return k <= 8 ? 4 : k <= 16 ? 2 : 1; }
+
+// Whether the tree passes of a product with k right-hand sides run on those
+// kernels under the schedule's `wide` (0 never, 1 from kWideMinK, 2 from 2 on):
+// rank 20, panels of the stored layout, band tasks within shared memory.
 template <typename S, typename A>
-bool wide_tree_ok(const hm_handle *h, const MulArgs<S> &ma)
+bool wide_tree_ok(const hm_handle *h, const MulArgs<S> &ma, int wide)
 {
-    if (!(std::is_same<S, A>::value && ma.k >= kWideMinK && h->r == 20 && h->vp_wide && !ma.xin &&
-          h->fstride % 4 == 0))
+    const int kmin = wide >= 2 ? 2 : wide == 1 ? kWideMinK : INT32_MAX;
+    if (!(std::is_same<S, A>::value && ma.k >= kmin && h->r == 20 && h->vp_wide && !ma.xin && h->fstride % 4 == 0))
         return false;
-    const size_t lv = (size_t)32 * 20 * sizeof(A);
+    const int G = wide_groups(ma.k);
+    const size_t lv = (size_t)(32 / G) * 20 * sizeof(A);
     return (2 * 400 * sizeof(A) + (size_t)h->band_locals[0] * lv) <= kTaskSmemMax &&
            (2 * 400 * sizeof(A) + (size_t)h->band_locals[1] * lv) <= kTaskSmemMax &&
-           (size_t)kWideWarps * ((size_t)h->vp_cap * 20 + 64 * ((size_t)h->vp_cap + 4)) * sizeof(A) <= 200 * 1024;
+           (size_t)kWideWarps * ((size_t)h->vp_cap * 20 + 32 * ((size_t)h->vp_cap + 4)) * sizeof(A) <= 200 * 1024;
 }
 
 // The tree passes for 32 and more right-hand sides: leaf_up_w, xfer_task_w
 // bands, m2l_w, the same stage and event structure as launch_tree_qc.
-template <typename S, typename A>
+template <typename S, typename A, int G>
 int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s, bool timing, cudaEvent_t mid,
                      int mid_after, bool *ends_with_kernel)
 {
-    constexpr int R = 20;
+    constexpr int R = 20, QL = 32 / G;
     const int k = ma.k;
     const bool pdl_on = cur_sched(h).pdl && !(h->profile_mask & 0x3u);
     bool chain = false;
-    const int64_t nq = (k + 31) / 32;
+    const int64_t nq = (k + QL - 1) / QL;
     const A *T = static_cast<const A *>(h->d_T);
     const MulArgs<A> &mw = reinterpret_cast<const MulArgs<A> &>(ma);
+    auto ctas = [](int64_t groups) { return (unsigned)((groups + kWideWarps * G - 1) / (kWideWarps * G)); };
     {
         StageTimer tm(h, timing ? 0 : -1, st);
         if (h->n_vp) {
             // one right-hand side per lane (measured at 256: 0.69 ms against 0.94 ms
             // with two, whose larger staging halves the warps per SM)
-            const int qpl = 1;
-            auto kern = leaf_up_w<A, R, 1>;
-            const size_t smem =
-                (size_t)kWideWarps * ((size_t)h->vp_cap * R + 32 * qpl * ((size_t)h->vp_cap + 4)) * sizeof(A);
+            auto kern = leaf_up_w<A, R, 1, G>;
+            const size_t smem = (size_t)kWideWarps * G *
+                                ((G == 1 ? (size_t)h->vp_cap * R : 0) + QL * ((size_t)h->vp_cap + 4)) * sizeof(A);
             HM_TRY(ensure_smem(kern, smem));
-            const int64_t warps = (int64_t)h->n_vp * ((k + 32 * qpl - 1) / (32 * qpl));
-            HM_TRY(launch_k("leaf_up_w", kern, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
-                            dim3(32 * kWideWarps), smem, st, false, mw, h->d_vp, h->n_vp,
-                            static_cast<const A *>(h->d_V), t, h->vp_cap));
+            HM_TRY(launch_k("leaf_up_w", kern, dim3(ctas((int64_t)h->n_vp * nq)), dim3(32 * kWideWarps), smem, st,
+                            false, mw, h->d_vp, h->n_vp, static_cast<const A *>(h->d_V), t, h->vp_cap));
             chain = true;
         }
         if (mid && mid_after == 2) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // leaf bases done
-        const size_t xsm = (2 * (size_t)R * R + (size_t)h->band_locals[0] * 32 * R) * sizeof(A);
-        HM_TRY(ensure_smem(xfer_task_w<A, R, true>, xsm));
+        const size_t xsm = (2 * (size_t)R * R + (size_t)h->band_locals[0] * QL * R) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_task_w<A, R, true, G>, xsm));
         const int last = last_band(h->up_band_ptr);
         for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
             const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
             if (!n) continue;
-            HM_TRY(launch_k("xfer_up_w", xfer_task_w<A, R, true>, dim3(n, (unsigned)nq), dim3(kWideTaskThreads), xsm,
-                            st, pdl_on && chain, h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, k,
+            HM_TRY(launch_k("xfer_up_w", xfer_task_w<A, R, true, G>, dim3(n, (unsigned)nq), dim3(kWideTaskThreads),
+                            xsm, st, pdl_on && chain, h->d_up_tasks + b, h->d_up_steps, h->d_up_ents, T, t, k,
                             (int)bd != last ? 1 : 0));
             chain = true;
         }
@@ -924,26 +930,27 @@ int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, 
     {
         StageTimer tm(h, timing ? 1 : -1, st);
         if (h->n_m2l_rows) {
-            const int qpl = k >= 64 ? 2 : 1;
-            auto kern = qpl == 2 ? m2l_w<A, R, 2> : m2l_w<A, R, 1>;
-            const size_t smem = (size_t)kWideWarps * 2 * ((size_t)h->fstride + 32 * qpl * R) * sizeof(A);
+            // two right-hand sides per lane from 64 on (half the shared-memory reads per FMA)
+            const int qpl = (G == 1 && k >= 64) ? 2 : 1;
+            auto kern = qpl == 2 ? m2l_w<A, R, 2, G> : m2l_w<A, R, 1, G>;
+            const size_t smem = (size_t)kWideWarps * G * 2 * ((size_t)h->fstride + QL * qpl * R) * sizeof(A);
             HM_TRY(ensure_smem(kern, smem));
-            const int64_t warps = (int64_t)h->n_m2l_rows * ((k + 32 * qpl - 1) / (32 * qpl));
-            HM_TRY(launch_k("m2l_w", kern, dim3((unsigned)((warps + kWideWarps - 1) / kWideWarps)),
-                            dim3(32 * kWideWarps), smem, st, pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows,
-                            h->d_m2l_ents, static_cast<const A *>(h->d_F), h->fstride, t, s, k));
+            const int64_t groups = (int64_t)h->n_m2l_rows * ((k + QL * qpl - 1) / (QL * qpl));
+            HM_TRY(launch_k("m2l_w", kern, dim3(ctas(groups)), dim3(32 * kWideWarps), smem, st, pdl_on && chain,
+                            h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents, static_cast<const A *>(h->d_F), h->fstride,
+                            t, s, k));
             chain = true;
         }
         if (mid && mid_after == 1) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // far-field stage done
-        const size_t xsm = (2 * (size_t)R * R + (size_t)h->band_locals[1] * 32 * R) * sizeof(A);
-        HM_TRY(ensure_smem(xfer_task_w<A, R, false>, xsm));
+        const size_t xsm = (2 * (size_t)R * R + (size_t)h->band_locals[1] * QL * R) * sizeof(A);
+        HM_TRY(ensure_smem(xfer_task_w<A, R, false, G>, xsm));
         const int last = last_band(h->down_band_ptr);
         for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
             const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
             if (!n) continue;
-            HM_TRY(launch_k("xfer_down_w", xfer_task_w<A, R, false>, dim3(n, (unsigned)nq), dim3(kWideTaskThreads),
-                            xsm, st, pdl_on && chain, h->d_down_tasks + b, h->d_down_steps, h->d_down_ents, T, s, k,
-                            (int)bd != last ? 1 : 0));
+            HM_TRY(launch_k("xfer_down_w", xfer_task_w<A, R, false, G>, dim3(n, (unsigned)nq),
+                            dim3(kWideTaskThreads), xsm, st, pdl_on && chain, h->d_down_tasks + b, h->d_down_steps,
+                            h->d_down_ents, T, s, k, (int)bd != last ? 1 : 0));
             chain = true;
         }
     }
@@ -958,8 +965,11 @@ int launch_tree(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A *s,
     bool ends = false;
     int rc;
     if constexpr (std::is_same<S, A>::value) {
-        if (cur_sched(h).wide && wide_tree_ok<S, A>(h, ma)) {
-            rc = launch_tree_wide<S, A>(h, ma, st, t, s, timing, mid, mid_after, &ends);
+        if (wide_tree_ok<S, A>(h, ma, cur_sched(h).wide)) {
+            const int G = wide_groups(ma.k);
+            rc = G == 4 ? launch_tree_wide<S, A, 4>(h, ma, st, t, s, timing, mid, mid_after, &ends)
+                 : G == 2 ? launch_tree_wide<S, A, 2>(h, ma, st, t, s, timing, mid, mid_after, &ends)
+                          : launch_tree_wide<S, A, 1>(h, ma, st, t, s, timing, mid, mid_after, &ends);
             if (ends_with_kernel) *ends_with_kernel = ends;
             return rc;
         }
@@ -1300,8 +1310,10 @@ std::vector<Sched> sched_candidates(const hm_handle *h, int k, bool fp32)
     // the lane-per-right-hand-side tree kernels on and off (32+, unless the
     // option turned them off)
     const bool ring = fp32 && k >= 3 && k <= kPartMaxK && h->stream_ctas > 0 && h->n_segs;
-    const std::vector<int> wides =
-        (tree && k >= kWideMinK && h->wide_tree) ? std::vector<int>{1, 0} : std::vector<int>{base.wide};
+    // (from 32 right-hand sides: on or off; from 2 to 31: the chunk-of-8 kernels or the grouped ones)
+    std::vector<int> wides{base.wide};
+    if (tree && h->wide_tree && k >= kWideMinK) wides = {1, 0};
+    else if (tree && h->wide_tree && k >= 2) wides = {1, 2};
     std::vector<Sched> c{base};       // the configured schedule first, timed for comparison
     auto add = [&c](Sched s) {
         for (const Sched &o : c)
@@ -2154,11 +2166,12 @@ int hm_configure(hm_handle *h, int option, int64_t value)
     // options of the bounded waits: no schedule changes, tuned schedules kept
     // (the host-buffer graph holds the old kernel arguments: dropped)
     if (option == HM_OPT_WIDE_TREE) {
+        if (value < 0 || value > 2) { set_error("HM_OPT_WIDE_TREE must be 0, 1 or 2"); return HM_ERR_INVALID_ARG; }
         drop_host_graph(h);
         {
             std::lock_guard<std::mutex> lk(h->mu);
-            h->wide_tree = value != 0;
-            for (Sched &t : h->tuned) t.wide = value != 0 ? 1 : 0;
+            h->wide_tree = (int)value;
+            for (Sched &t : h->tuned) t.wide = (int)value;
         }
         if (h->trans) return hm_configure(h->trans, option, value);
         return HM_OK;

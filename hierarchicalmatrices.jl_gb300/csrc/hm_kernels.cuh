@@ -246,22 +246,23 @@ __global__ void ring_part(MulArgs<float> ma, const hm_seg *segs, int nsegs, cons
                           const float *s, const float *t, int r, float *yfar, int64_t ldf);
 
 // Tree passes for 32 and more right-hand sides (hm_wide.cu): lane q of a
-// warp owns right-hand sides q + 32 p (p < QPL) of a chunk of 32 QPL; R (the
-// rank) a multiple of 4.  m2l_w: one warp per (row slot, chunk), shared
-// memory kWideWarps * 2 * (fstride + 32 QPL R) values; leaf_up_w: one warp
-// per (panel, chunk), panels row-major with ld == width == R and at most cap
-// rows (a multiple of 8), shared memory kWideWarps * (cap R + 32 QPL (cap + 4))
-// values; xfer_task_w: one chunk of 32 per CTA;
+// warp's group of QL = 32 / G lanes owns right-hand sides q + QL p (p < QPL)
+// of a chunk of QL QPL; R (the rank) a multiple of 4.  m2l_w: a group per
+// (row slot, chunk), shared memory kWideWarps * G * 2 * (fstride + QL QPL R)
+// values; leaf_up_w: a group per (panel, chunk), panels row-major with ld ==
+// width == R and at most cap rows (a multiple of 8), shared memory
+// kWideWarps * G * ((G == 1 ? cap R : 0) + QL QPL (cap + 4)) values;
+// xfer_task_w: one chunk of QL per CTA, groups taking records;
 // xfer_task_w: one CTA of kWideTaskThreads per (task, chunk), shared memory
-// (2 R^2 + locals * 32 R) values.
+// (2 R^2 + locals * QL R) values.
 constexpr int kWideWarps = 4;
 constexpr int kWideTaskThreads = 256;
-template <typename A, int R, int QPL>
+template <typename A, int R, int QPL, int G>
 __global__ void m2l_w(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const A *F, int fstride, const A *t,
                       A *s, int k);
-template <typename A, int R, int QPL>
+template <typename A, int R, int QPL, int G>
 __global__ void leaf_up_w(MulArgs<A> ma, const hm_vpanel *vp, int npanels, const A *V, A *t, int cap);
-template <typename A, int R, bool UP>
+template <typename A, int R, bool UP, int G>
 __global__ void xfer_task_w(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *coef, int k,
                             int early);
 

@@ -58,35 +58,53 @@ __device__ __forceinline__ void warp_copy16(void *dst, const void *src, int byte
     for (int i = lane * 16; i < bytes; i += 32 * 16) async_copy16(d + i, s + i);
 }
 
+// the same by the QL lanes of a group (ql its lane within the group)
+__device__ __forceinline__ void group_copy16(void *dst, const void *src, int bytes, int ql, int QL)
+{
+    const char *s = static_cast<const char *>(src);
+    char *d = static_cast<char *>(dst);
+    for (int i = ql * 16; i < bytes; i += QL * 16) async_copy16(d + i, s + i);
+}
+
+// lanes of group g of QL lanes
+__device__ __forceinline__ unsigned group_mask(int g, int QL)
+{
+    return QL == 32 ? 0xffffffffu : (((1u << QL) - 1u) << (g * QL));
+}
+
 }  // namespace
 
-// One warp per (row slot, chunk of 32 QPL right-hand sides); lane l owns
-// right-hand sides l + 32 p, p < QPL (two per lane halve the shared-memory
-// reads per FMA).  F blocks are R x R column-major (F[m + R n]) with fstride
-// values between blocks; coefficients coef[(slot * k + q) * R + m].  Needs
-// R % 4 == 0 and fstride % 4 == 0.
-template <typename A, int R, int QPL>
+// A warp holds G groups of QL = 32 / G lanes; each group takes one (row
+// slot, chunk of QL QPL right-hand sides), lane l of a group right-hand sides
+// l + QL p, p < QPL (two per lane halve the shared-memory reads per FMA; four
+// groups of 8 serve up to 8 right-hand sides with every lane busy).  F blocks
+// are R x R column-major (F[m + R n]) with fstride values between blocks;
+// coefficients coef[(slot * k + q) * R + m].  Needs R % 4 == 0 and
+// fstride % 4 == 0.  Groups synchronise only among their own lanes.
+template <typename A, int R, int QPL, int G>
 __global__ void __launch_bounds__(kWideWarps * 32)
     m2l_w(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const A *F, int fstride, const A *t, A *s,
           int k)
 {
     extern __shared__ __align__(16) unsigned char wide_smem[];
-    constexpr int QW = 32 * QPL;                               // right-hand sides of a warp
+    constexpr int QL = 32 / G, QW = QL * QPL;                  // lanes and right-hand sides of a group
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int g = lane / QL, ql = lane % QL;
+    const unsigned gmask = group_mask(g, QL);
     const int nq = (k + QW - 1) / QW;
-    const int64_t w = (int64_t)blockIdx.x * kWideWarps + wib;
+    const int64_t w = ((int64_t)blockIdx.x * kWideWarps + wib) * G + g;
     pdl_trigger();
     pdl_wait();                                                // the upward pass's coefficients are ready
     if (w >= (int64_t)nrows * nq) return;
     const hm_m2l_row Rw = rows[w / nq];
     const int q0 = (int)(w % nq) * QW, qc = min(QW, k - q0);
     const int stage_vals = fstride + QW * R;
-    A *buf = reinterpret_cast<A *>(wide_smem) + (size_t)wib * 2 * stage_vals;
+    A *buf = reinterpret_cast<A *>(wide_smem) + ((size_t)wib * G + g) * 2 * stage_vals;
     auto fetch = [&](int e, int b) {
         const hm_m2l_ent E = ents[e];
         A *fb = buf + b * stage_vals;
-        warp_copy16(fb, F + E.foff, R * R * (int)sizeof(A), lane);
-        warp_copy16(fb + fstride, t + ((int64_t)E.yslot * k + q0) * R, qc * R * (int)sizeof(A), lane);
+        group_copy16(fb, F + E.foff, R * R * (int)sizeof(A), ql, QL);
+        group_copy16(fb + fstride, t + ((int64_t)E.yslot * k + q0) * R, qc * R * (int)sizeof(A), ql, QL);
         async_commit();
     };
     A acc[QPL][R];
@@ -103,14 +121,14 @@ __global__ void __launch_bounds__(kWideWarps * 32)
         } else {
             async_wait_all();
         }
-        __syncwarp();
+        __syncwarp(gmask);
         const A *fb = buf + b * stage_vals;
-        const A *tq = fb + fstride + lane * R;                 // this lane's right-hand sides (rows past qc unused)
+        const A *tq = fb + fstride + ql * R;                   // this lane's right-hand sides (rows past qc unused)
 #pragma unroll
         for (int n = 0; n < R; n += 4) {
             A tv[QPL][4];
 #pragma unroll
-            for (int p = 0; p < QPL; ++p) ld4(tq + p * 32 * R + n, tv[p]);
+            for (int p = 0; p < QPL; ++p) ld4(tq + p * QL * R + n, tv[p]);
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const A *col = fb + (n + u) * R;
@@ -125,41 +143,52 @@ __global__ void __launch_bounds__(kWideWarps * 32)
                 }
             }
         }
-        __syncwarp();                                          // stage b is refilled by the next fetch
+        __syncwarp(gmask);                                     // stage b is refilled by the next fetch
     }
 #pragma unroll
     for (int p = 0; p < QPL; ++p) {
-        if (lane + 32 * p < qc) {
-            A *sp = s + ((int64_t)Rw.slot * k + q0 + lane + 32 * p) * R;
+        if (ql + QL * p < qc) {
+            A *sp = s + ((int64_t)Rw.slot * k + q0 + ql + QL * p) * R;
 #pragma unroll
             for (int m = 0; m < R; m += 4) st4<A>(sp + m, acc[p] + m);
         }
     }
 }
 
-// One warp per (explicit basis panel, chunk of 32 QPL right-hand sides), lane
-// l right-hand sides l + 32 p: t[slot][q][col0 + m] = sum_j V[j][m] x[row0 + j][q],
-// the panel row-major (V[j * R + m], ld == width == R), at most cap rows (a
-// multiple of 8).
-template <typename A, int R, int QPL>
+// Groups as in m2l_w: each group takes one (explicit basis panel, chunk of
+// QL QPL right-hand sides), lane l of a group right-hand sides l + QL p:
+// t[slot][q][col0 + m] = sum_j V[j][m] x[row0 + j][q], the panel row-major
+// (V[j * R + m], ld == width == R), at most cap rows (a multiple of 8).  With
+// one group the panel is staged in shared memory; with several, each group
+// reads its panel's rows straight from global memory (16-byte loads all lanes
+// of the group share).
+template <typename A, int R, int QPL, int G>
 __global__ void __launch_bounds__(kWideWarps * 32)
     leaf_up_w(MulArgs<A> ma, const hm_vpanel *vp, int npanels, const A *V, A *t, int cap)
 {
     extern __shared__ __align__(16) unsigned char wide_smem[];
-    constexpr int QW = 32 * QPL;
+    constexpr int QL = 32 / G, QW = QL * QPL;
+    constexpr bool kStageV = G == 1;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int g = lane / QL, ql = lane % QL;
+    const unsigned gmask = group_mask(g, QL);
     const int k = ma.k, nq = (k + QW - 1) / QW;
-    const int64_t w = (int64_t)blockIdx.x * kWideWarps + wib;
+    const int64_t w = ((int64_t)blockIdx.x * kWideWarps + wib) * G + g;
     pdl_trigger();
     if (w >= (int64_t)npanels * nq) return;
     const hm_vpanel Pn = vp[w / nq];
     const int q0 = (int)(w % nq) * QW, qc = min(QW, k - q0);
     const int xs_stride = cap + 4;                             // 4 mod 8 words
-    A *Vs = reinterpret_cast<A *>(wide_smem) + (size_t)wib * (cap * R + QW * xs_stride);
-    A *Xs = Vs + cap * R;
+    A *Xs = reinterpret_cast<A *>(wide_smem) +
+            ((size_t)wib * G + g) * ((kStageV ? cap * R : 0) + QW * xs_stride);
+    const A *Vr = V + Pn.off;                                  // the panel's rows (global, or staged below)
     const int nr = Pn.nrows;
-    // the panel: one contiguous run of nr * R values
-    warp_copy16(Vs, V + Pn.off, nr * R * (int)sizeof(A), lane);
+    if constexpr (kStageV) {
+        A *Vs = Xs;
+        Xs += cap * R;
+        group_copy16(Vs, V + Pn.off, nr * R * (int)sizeof(A), ql, QL);
+        Vr = Vs;
+    }
     // the right-hand sides: lanes walk rows (coalesced), right-hand side by
     // right-hand side, every copy in flight at once (cp.async); rows up to a
     // multiple of 4 and right-hand sides past the chunk are zero-filled
@@ -169,17 +198,17 @@ __global__ void __launch_bounds__(kWideWarps * 32)
         // rows of every right-hand side start on a 16-byte boundary: 16-byte copies,
         // lane (q, piece) over the QW x nr / VW pieces
         const int per_q = nr / VW;
-        for (int i = lane; i < QW * per_q; i += 32) {
+        for (int i = ql; i < QW * per_q; i += QL) {
             const int q = i / per_q, v = i - q * per_q;
             A *d = Xs + q * xs_stride + v * VW;
             if (q < qc) async_copy16(d, ma.x + Pn.row0 + (int64_t)(q0 + q) * ma.ldx + v * VW);
             else for (int u = 0; u < VW; ++u) d[u] = A(0);
         }
-        for (int i = lane; i < QW * (nr4 - nr); i += 32) Xs[(i / (nr4 - nr)) * xs_stride + nr + i % (nr4 - nr)] = A(0);
+        for (int i = ql; i < QW * (nr4 - nr); i += QL) Xs[(i / (nr4 - nr)) * xs_stride + nr + i % (nr4 - nr)] = A(0);
     } else {
         for (int q = 0; q < QW; ++q) {
             const A *xq = ma.x + Pn.row0 * ma.incx + (int64_t)(q0 + q) * ma.ldx;
-            for (int j = lane; j < nr4; j += 32) {
+            for (int j = ql; j < nr4; j += QL) {
                 A *d = Xs + q * xs_stride + j;
                 if (q < qc && j < nr) async_copy<sizeof(A)>(d, xq + (int64_t)j * ma.incx);
                 else *d = A(0);
@@ -188,21 +217,21 @@ __global__ void __launch_bounds__(kWideWarps * 32)
     }
     async_commit();
     async_wait_all();
-    __syncwarp();
+    __syncwarp(gmask);
     A acc[QPL][R];
 #pragma unroll
     for (int p = 0; p < QPL; ++p)
 #pragma unroll
         for (int m = 0; m < R; ++m) acc[p][m] = A(0);
-    const A *xr = Xs + lane * xs_stride;
+    const A *xr = Xs + ql * xs_stride;
     for (int j = 0; j < nr4; j += 4) {
         A xv[QPL][4];
 #pragma unroll
-        for (int p = 0; p < QPL; ++p) ld4(xr + p * 32 * xs_stride + j, xv[p]);
+        for (int p = 0; p < QPL; ++p) ld4(xr + p * QL * xs_stride + j, xv[p]);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (j + u >= nr) break;
-            const A *row = Vs + (j + u) * R;
+            const A *row = Vr + (j + u) * R;
 #pragma unroll
             for (int m = 0; m < R; m += 4) {
                 A v[4];
@@ -216,8 +245,8 @@ __global__ void __launch_bounds__(kWideWarps * 32)
     }
 #pragma unroll
     for (int p = 0; p < QPL; ++p) {
-        if (lane + 32 * p < qc) {
-            A *tp = t + ((int64_t)Pn.slot * k + q0 + lane + 32 * p) * R + Pn.col0;
+        if (ql + QL * p < qc) {
+            A *tp = t + ((int64_t)Pn.slot * k + q0 + ql + QL * p) * R + Pn.col0;
 #pragma unroll
             for (int m = 0; m < R; m += 4) st4<A>(tp + m, acc[p] + m);
         }
@@ -232,19 +261,22 @@ __global__ void __launch_bounds__(kWideWarps * 32)
 // so that both read R contiguous values per step).  Needs R % 4 == 0.
 //   upward:   t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m']
 //   downward: s[child_c][m'] += sum_m T_c[m', m] s[parent][m]
-template <typename A, int R, bool UP>
+template <typename A, int R, bool UP, int G>
 __global__ void __launch_bounds__(kWideTaskThreads)
     xfer_task_w(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const A *T, A *coef, int k,
                 int early)
 {
     extern __shared__ __align__(16) unsigned char wide_smem[];
+    constexpr int QL = 32 / G;                                 // lanes of a group = right-hand sides of the CTA
     A *Ts = reinterpret_cast<A *>(wide_smem);
     A *L = Ts + 2 * R * R;
-    constexpr int LV = 32 * R;                                 // values of one local vector
+    constexpr int LV = QL * R;                                 // values of one local vector
     const hm_task tk = tasks[blockIdx.x];
     const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
-    const int q0 = blockIdx.y * 32, qc = min(32, k - q0);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int q0 = blockIdx.y * QL, qc = min(QL, k - q0);
+    const int lane0 = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // group (warp, g) of QL lanes takes records warp * G + g, + nw * G, ...
+    const int g = lane0 / QL, lane = lane0 % QL, gw = warp * G + g, nw = (blockDim.x >> 5) * G;
     if (early) pdl_trigger();
     if (UP) {
         for (int i = threadIdx.x; i < 2 * R * R; i += blockDim.x) async_copy<sizeof(A)>(Ts + i, T + i);
@@ -256,8 +288,8 @@ __global__ void __launch_bounds__(kWideTaskThreads)
         }
     }
     pdl_wait();                                                // inputs of the band are ready
-    // external inputs: warps take records, the warp copies a 32 x R block
-    for (int rec = warp; rec < nrec; rec += nw) {
+    // external inputs: groups take records, a group copies a QL x R block
+    for (int rec = gw; rec < nrec; rec += nw) {
         const hm_xfer X = ents[e0 + rec];
 #pragma unroll
         for (int c = 0; c < (UP ? 2 : 3); ++c) {
@@ -274,14 +306,15 @@ __global__ void __launch_bounds__(kWideTaskThreads)
                 slot = X.slot;
                 if (lc < 2 * nrec) continue;                   // a child of an earlier level of this task
             }
-            warp_copy16(L + (int64_t)lc * LV, coef + ((int64_t)slot * k + q0) * R, qc * R * (int)sizeof(A), lane);
+            group_copy16(L + (int64_t)lc * LV, coef + ((int64_t)slot * k + q0) * R, qc * R * (int)sizeof(A), lane,
+                         QL);
         }
     }
     async_wait_all();
     __syncthreads();
     for (int st = tk.step0; st < tk.step1; ++st) {
         const hm_step S = steps[st];
-        for (int w = warp; w < S.e1 - S.e0; w += nw) {
+        for (int w = gw; w < S.e1 - S.e0; w += nw) {
             const int e = S.e0 + w;
             const hm_xfer X = ents[e];
             if (UP) {
@@ -364,18 +397,18 @@ __global__ void __launch_bounds__(kWideTaskThreads)
     }
 }
 
-#define HM_INST_WIDE(A, QPL)                                                                                \
-    template __global__ void m2l_w<A, 20, QPL>(const hm_m2l_row *, int, const hm_m2l_ent *, const A *, int,     \
-                                               const A *, A *, int);                                            \
-    template __global__ void leaf_up_w<A, 20, QPL>(MulArgs<A>, const hm_vpanel *, int, const A *, A *, int);
-HM_INST_WIDE(float, 1) HM_INST_WIDE(float, 2) HM_INST_WIDE(double, 1) HM_INST_WIDE(double, 2)
-template __global__ void xfer_task_w<float, 20, true>(const hm_task *, const hm_step *, const hm_xfer *, const float *,
-                                                      float *, int, int);
-template __global__ void xfer_task_w<float, 20, false>(const hm_task *, const hm_step *, const hm_xfer *,
-                                                       const float *, float *, int, int);
-template __global__ void xfer_task_w<double, 20, true>(const hm_task *, const hm_step *, const hm_xfer *,
-                                                       const double *, double *, int, int);
-template __global__ void xfer_task_w<double, 20, false>(const hm_task *, const hm_step *, const hm_xfer *,
-                                                        const double *, double *, int, int);
+#define HM_INST_WIDE(A, QPL, G)                                                                             \
+    template __global__ void m2l_w<A, 20, QPL, G>(const hm_m2l_row *, int, const hm_m2l_ent *, const A *, int,  \
+                                                  const A *, A *, int);                                         \
+    template __global__ void leaf_up_w<A, 20, QPL, G>(MulArgs<A>, const hm_vpanel *, int, const A *, A *, int);
+#define HM_INST_XFER(A, G)                                                                                     \
+    template __global__ void xfer_task_w<A, 20, true, G>(const hm_task *, const hm_step *, const hm_xfer *,     \
+                                                         const A *, A *, int, int);                             \
+    template __global__ void xfer_task_w<A, 20, false, G>(const hm_task *, const hm_step *, const hm_xfer *,    \
+                                                          const A *, A *, int, int);
+HM_INST_WIDE(float, 1, 1) HM_INST_WIDE(float, 2, 1) HM_INST_WIDE(float, 1, 2) HM_INST_WIDE(float, 1, 4)
+HM_INST_WIDE(double, 1, 1) HM_INST_WIDE(double, 2, 1) HM_INST_WIDE(double, 1, 2) HM_INST_WIDE(double, 1, 4)
+HM_INST_XFER(float, 1) HM_INST_XFER(float, 2) HM_INST_XFER(float, 4)
+HM_INST_XFER(double, 1) HM_INST_XFER(double, 2) HM_INST_XFER(double, 4)
 
 }  // namespace hm

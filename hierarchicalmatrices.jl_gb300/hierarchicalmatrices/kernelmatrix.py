@@ -168,10 +168,11 @@ class KernelMatrix:
                 f"a kernel of this KernelMatrix gave up waiting (device status {code}): its products are invalid")
 
     def set_wide_tree(self, enable=True):
-        """Tree passes of products with 32 or more right-hand sides on the
-        lane-per-right-hand-side kernels (True, the default) or on the
-        kernels for chunks of 8."""
-        check(lib.hm_configure(self._h, _lib.HM_OPT_WIDE_TREE, 1 if enable else 0))
+        """Tree passes on the lane-per-right-hand-side kernels: True (the
+        default) from 32 right-hand sides, "all" from 2, False never (the
+        kernels for chunks of 8)."""
+        code = 2 if enable == "all" else (1 if enable else 0)
+        check(lib.hm_configure(self._h, _lib.HM_OPT_WIDE_TREE, code))
 
     def set_ring_tile(self, tile):
         """Tile of the per-warp rings (3-8 FP32 right-hand sides): 0 = up to
@@ -387,7 +388,7 @@ class KernelMatrix:
         tiles = ((768, 3), (512, 4), (1024, 3))
         return {"overlap": v[0], "near_kernel": v[1], "near_stages": v[2], "tensor_cores": bool(v[3]),
                 "pdl": bool(v[4]), "ring_tile": {"panel_values": tiles[v[5]][0], "stages": tiles[v[5]][1]},
-                "wide_tree": bool(v[6])}
+                "wide_tree": {0: False, 1: True, 2: "all"}.get(v[6], v[6])}
 
     def forget_autotune(self):
         """Drop the autotuned schedules: products run with the configured options."""

@@ -271,10 +271,13 @@ enum {
     HM_OPT_TEST_STALL = 8,
     /* HM_OPT_WIDE_TREE (default 1): products with 32 or more right-hand sides
        (rank 20) run the tree passes (leaf bases, transfers, far-field blocks)
-       on kernels that give each lane one right-hand side of a chunk of 32 and
-       all 20 coefficients of it; 0 keeps the kernels with the coefficients on
-       the lanes and chunks of 8 right-hand sides.  Applies to the autotuned
-       schedules too (it overrides their choice).  No reference counterpart. */
+       on kernels that give each lane one right-hand side and all 20
+       coefficients of it (a warp of 32, or 2 or 4 groups of 16 or 8 lanes);
+       2 uses them from 2 right-hand sides on; 0 keeps the kernels with the
+       coefficients on the lanes and chunks of 8 right-hand sides.  Applies to
+       the autotuned schedules too (it overrides their choice; the autotuner
+       tries 1 and 2 for 2-31 right-hand sides, 1 and 0 from 32).  No reference
+       counterpart. */
     HM_OPT_WIDE_TREE = 9,
     /* HM_OPT_RING_TILE (default 0): the per-warp rings' tile for 3-8 FP32
        right-hand sides: 0 = up to 768 panel values x 3 stages per warp,

@@ -58,6 +58,32 @@ def test_wide_tree_matches_narrow(points, dtype, k):
     H.free()
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("k", [2, 3, 8, 12, 20])
+def test_grouped_wide_tree_matches_narrow(points, dtype, k):
+    """Fewer than 32 right-hand sides on the grouped lane-per-RHS kernels
+    (HM_OPT_WIDE_TREE 2: four groups of 8 lanes up to 8, two of 16 up to 16,
+    a warp beyond) against the chunk-of-8 kernels."""
+    n, x, y = points
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=dtype)
+    g = torch.Generator(device="cuda").manual_seed(100 + k)
+    B = torch.randn(k, n, device="cuda", dtype=TDT[dtype], generator=g).t()
+    H.set_near_kernel("warp")                # the same panel kernel on both sides
+    H.set_wide_tree("all")
+    assert H.schedule(k)["wide_tree"] == "all"
+    Uw = H @ B
+    H.set_wide_tree(False)
+    Un = H @ B
+    assert colrel(Uw, Un) <= (1e-13 if dtype == np.float64 else 5e-7)
+    if dtype == np.float64:
+        Ho = O.OracleKernelMatrix(O.CAUCHY, x, y, 1.0, 0.0, 1.0, 0.0)
+        ref = Ho @ B[:, k - 1].cpu().numpy().copy()
+        got = Uw[:, k - 1].cpu().numpy()
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-12
+    assert H.device_status() == 0
+    H.free()
+
+
 def test_wide_tree_batch_and_transpose():
     # a batched (block-diagonal) plan, and the transposed product's own plan
     rng = np.random.default_rng(40)
@@ -73,6 +99,11 @@ def test_wide_tree_batch_and_transpose():
     Hb.set_wide_tree(False)
     Un = Hb @ B
     assert colrel(Uw, Un) <= 1e-13
+    B8 = B[:, :8].contiguous().t().contiguous().t()            # 8 right-hand sides, column-major
+    Hb.set_wide_tree("all")
+    W8 = Hb @ B8
+    Hb.set_wide_tree(False)
+    assert colrel(W8, Hb @ B8) <= 1e-13
     x = np.sort(rng.random(12000))[::-1].copy()
     y = np.sort(rng.random(9000))[::-1].copy()
     H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0)
