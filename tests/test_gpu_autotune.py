@@ -25,7 +25,9 @@ def colrel(a, b):
 
 def valid(choice, k, dtype):
     assert 0 <= choice["overlap"] <= 4
-    assert choice["near_kernel"] in (0, 2)
+    assert choice["near_kernel"] in (0, 1, 2)       # 1 (warp per segment) is a candidate for 3-8 FP32 RHS
+    assert (choice["ring_tile"]["panel_values"], choice["ring_tile"]["stages"]) in ((768, 3), (512, 4), (1024, 3))
+    assert choice["wide_tree"] in (True, False, "all")
     assert 2 <= choice["near_stages"] <= 16
     if dtype == np.float64 or k < 16:
         assert choice["tensor_cores"]          # the configured value, untouched
