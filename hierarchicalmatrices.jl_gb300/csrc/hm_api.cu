@@ -902,7 +902,17 @@ int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, 
     auto ctas = [](int64_t groups) { return (unsigned)((groups + kWideWarps * G - 1) / (kWideWarps * G)); };
     {
         StageTimer tm(h, timing ? 0 : -1, st);
-        if (h->n_vp) {
+        if (h->n_vp && G > 1) {
+            // up to 16 right-hand sides the leaf stage keeps the chunk-of-8 kernel
+            // (measured on the 512-instance batch at 8: faster than four groups of 8
+            // reading their panels from global memory)
+            const size_t smem = (size_t)kWarpsPerCta * leaf_up_warp_bytes<S, A, 8>(h->vp_cap, h->vp_wcap);
+            HM_TRY(ensure_smem(leaf_up<S, A, 8>, smem));
+            leaf_up<S, A, 8><<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(
+                ma, h->d_vp, h->n_vp, static_cast<const S *>(h->d_V), t, h->r, h->vp_cap, h->vp_wcap);
+            HM_CK_LAUNCH("leaf_up");
+            chain = true;
+        } else if (h->n_vp) {
             // one right-hand side per lane (measured at 256: 0.69 ms against 0.94 ms
             // with two, whose larger staging halves the warps per SM)
             auto kern = leaf_up_w<A, R, 1, G>;
@@ -1040,10 +1050,11 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
         // per-warp rings (the default for 3-8 FP32 right-hand sides): each warp
         // keeps several chunks of its run of segments in flight
         if (h->stream_ctas > 0 && (sc.near_kernel == 0 || sc.near_kernel == 3)) {
-            auto kern = sc.tile == 1   ? ring_part<KB, FAR, kRingTile[1].pf, kRingTile[1].ns>
+            auto kern = FAR            ? ring_part<KB, FAR, kRingFarTile.pf, kRingFarTile.ns>
+                        : sc.tile == 1 ? ring_part<KB, FAR, kRingTile[1].pf, kRingTile[1].ns>
                         : sc.tile == 2 ? ring_part<KB, FAR, kRingTile[2].pf, kRingTile[2].ns>
                                        : ring_part<KB, FAR, kRingTile[0].pf, kRingTile[0].ns>;
-            const RingTile tl = kRingTile[sc.tile >= 0 && sc.tile < kRingTiles ? sc.tile : 0];
+            const RingTile tl = FAR ? kRingFarTile : kRingTile[sc.tile >= 0 && sc.tile < kRingTiles ? sc.tile : 0];
             const size_t smem = ring_smem_bytes(KB, tl.pf, tl.ns);
             HM_TRY(ensure_smem(kern, smem));
             HM_TRY(prefer_shared(kern));

@@ -236,6 +236,9 @@ constexpr int kRingCols = 32;              // columns per chunk at most (lane c 
 struct RingTile { int pf, ns; };
 constexpr int kRingTiles = 3;
 constexpr RingTile kRingTile[kRingTiles] = {{768, 3}, {512, 4}, {1024, 3}};
+// the far-field part (the row basis, r = 20 columns) takes a whole 64-row
+// segment's basis columns in one chunk
+constexpr RingTile kRingFarTile = {1280, 3};
 __host__ __device__ constexpr int ring_stage_floats(int kb, int pf) { return pf + kRingCols * kb; }
 __host__ __device__ constexpr size_t ring_smem_bytes(int kb, int pf, int ns)
 {
