@@ -1015,6 +1015,17 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
     if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
         if (h->storage == HM_DF64) return launch_df<FAR ? 1 : 0, KB>(h, ma, s, t, panels, yfar, st, pdl, ldf, 0);
     }
+    if constexpr (FAR && std::is_same<S, A>::value) {
+        // far-field rows one thread per row (the default and ring schedules;
+        // the warp and streamed kernels keep their own far-field form)
+        const Sched fs = cur_sched(h);
+        if (h->stream_ctas > 0 && h->part_width[1] <= 64 && (fs.near_kernel == 0 || fs.near_kernel == 3)) {
+            HM_TRY(launch_k("far_rows", far_rows<S, A, KB>, dim3((unsigned)((h->n_segs + 3) / 4)), dim3(256), 0, st,
+                            pdl, ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const S *>(panels), s, t, h->r,
+                            yfar, ldf));
+            return HM_OK;
+        }
+    }
     // one warp per segment unless the streamed CTAs are asked for: measured on
     // GB300, the warp kernel reads 64-row grid panels at 6.1 TB/s (90% of the
     // copy peak) and keeps its lead on short segments and more right-hand
@@ -1050,11 +1061,10 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
         // per-warp rings (the default for 3-8 FP32 right-hand sides): each warp
         // keeps several chunks of its run of segments in flight
         if (h->stream_ctas > 0 && (sc.near_kernel == 0 || sc.near_kernel == 3)) {
-            auto kern = FAR            ? ring_part<KB, FAR, kRingFarTile.pf, kRingFarTile.ns>
-                        : sc.tile == 1 ? ring_part<KB, FAR, kRingTile[1].pf, kRingTile[1].ns>
+            auto kern = sc.tile == 1   ? ring_part<KB, FAR, kRingTile[1].pf, kRingTile[1].ns>
                         : sc.tile == 2 ? ring_part<KB, FAR, kRingTile[2].pf, kRingTile[2].ns>
                                        : ring_part<KB, FAR, kRingTile[0].pf, kRingTile[0].ns>;
-            const RingTile tl = FAR ? kRingFarTile : kRingTile[sc.tile >= 0 && sc.tile < kRingTiles ? sc.tile : 0];
+            const RingTile tl = kRingTile[sc.tile >= 0 && sc.tile < kRingTiles ? sc.tile : 0];
             const size_t smem = ring_smem_bytes(KB, tl.pf, tl.ns);
             HM_TRY(ensure_smem(kern, smem));
             HM_TRY(prefer_shared(kern));

@@ -980,6 +980,66 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
     }
 }
 
+// Far-field rows U s with one thread per row: four segments per CTA of 256
+// threads, 64 threads per segment.  The segment's far-field coefficients (its
+// non-X pieces, at most 64 columns, KB right-hand sides) are gathered once into
+// shared memory; thread `row` then reads its row of the column-major basis
+// columns (consecutive threads, consecutive rows: coalesced) and accumulates
+// KB sums with FMA (at most 64 terms, as the warp kernels' folds do).  The
+// rows go to yfar (leading dimension ldf) or, without it, are added into y.
+template <typename S, typename A, int KB>
+__global__ void __launch_bounds__(256)
+    far_rows(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P, const A *s,
+             const A *t, int r, S *yfar, int64_t ldf)
+{
+    __shared__ A cs[4][64 * KB];                               // [segment][column][q]
+    pdl_wait();                                                // the downward pass's coefficients are ready
+    const int ls = threadIdx.x >> 6, row = threadIdx.x & 63;
+    const int j = blockIdx.x * 4 + ls;
+    const int k = ma.k;
+    hm_seg G{};
+    int nfar = 0;
+    if (j < nsegs) {
+        G = segs[j];
+        nfar = G.nfar;
+        // coefficients of the far columns: element e = (column c, q) with c = e / KB
+        for (int e = row; e < nfar * KB; e += 64) {
+            const int c = e / KB, q = e % KB;
+            int pc = 0, pi = 0;
+            hm_piece Q = pieces[G.piece0];
+            while (c >= pc + Q.width) {
+                pc += Q.width;
+                Q = pieces[G.piece0 + ++pi];
+            }
+            A v = A(0);
+            if (q < k) v = (Q.kind == HM_PIECE_TCOEF ? t : s)[((int64_t)Q.src * k + q) * r + (c - pc)];
+            cs[ls][e] = v;
+        }
+    }
+    __syncthreads();
+    if (j >= nsegs || row >= G.nrows) return;
+    if (nfar == 0 && !yfar) return;                            // y += 0
+    A acc[KB];
+#pragma unroll
+    for (int q = 0; q < KB; ++q) acc[q] = A(0);
+    const S *pr = P + G.poff + row;
+    for (int c = 0; c < nfar; ++c) {
+        const A u = (A)__ldcs(pr + (int64_t)c * G.ld);
+#pragma unroll
+        for (int q = 0; q < KB; ++q) acc[q] = fma(u, cs[ls][c * KB + q], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < KB; ++q) {
+        if (q >= k) break;
+        if (yfar) {
+            yfar[(G.row0 + row) + (int64_t)q * ldf] = (S)acc[q];
+        } else {
+            S *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q * ma.ldy;
+            *yp = (S)((A)(*yp) + acc[q]);
+        }
+    }
+}
+
 // y[i*incy + q*ldy] += yfar[i + q*ldf]: adds the far-field rows computed on the
 // side stream (after the join).
 template <typename S>
@@ -1428,6 +1488,12 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
                                                          const hm_piece *, const S *, const A *, const A *,  \
                                                          int, int, int, int, int, S *, int *,           \
                                                          unsigned long long, int);
+#define HM_INST_FAR(S, A, KB)                                                                        \
+    template __global__ void far_rows<S, A, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *, const S *, \
+                                                const A *, const A *, int, S *, int64_t);
+HM_INST_FAR(float, float, 1) HM_INST_FAR(float, float, 2) HM_INST_FAR(float, float, 4) HM_INST_FAR(float, float, 8)
+HM_INST_FAR(double, double, 1) HM_INST_FAR(double, double, 2) HM_INST_FAR(double, double, 4)
+HM_INST_FAR(double, double, 8)
 #define HM_INST_MV(S, A)                                                                             \
     template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int, int, int); \
     template __global__ void leaf_up<S, A, 8>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int, int, int); \

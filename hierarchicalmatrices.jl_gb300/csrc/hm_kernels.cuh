@@ -200,6 +200,12 @@ __global__ void expand_part(MulArgs<S> ma, const hm_seg *segs, int nsegs, const 
 template <typename S>
 __global__ void add_far(MulArgs<S> ma, int64_t n, const S *yfar, int64_t ldf);
 
+// Far-field rows U s, one thread per row (four segments of at most 64 rows per
+// CTA of 256 threads); segments' far columns first and at most 64 of them.
+template <typename S, typename A, int KB>
+__global__ void far_rows(MulArgs<S> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const S *P,
+                         const A *s, const A *t, int r, S *yfar, int64_t ldf);
+
 // Persistent panel streaming (cp.async.bulk into a ring of shared-memory
 // stages).  CTA b owns segments [cta_seg[b], cta_seg[b+1]); FAR selects the
 // columns [0, nfar) of each panel, otherwise [nfar, width).  Shared memory:
@@ -236,9 +242,6 @@ constexpr int kRingCols = 32;              // columns per chunk at most (lane c 
 struct RingTile { int pf, ns; };
 constexpr int kRingTiles = 3;
 constexpr RingTile kRingTile[kRingTiles] = {{768, 3}, {512, 4}, {1024, 3}};
-// the far-field part (the row basis, r = 20 columns) takes a whole 64-row
-// segment's basis columns in one chunk
-constexpr RingTile kRingFarTile = {1280, 3};
 __host__ __device__ constexpr int ring_stage_floats(int kb, int pf) { return pf + kRingCols * kb; }
 __host__ __device__ constexpr size_t ring_smem_bytes(int kb, int pf, int ns)
 {

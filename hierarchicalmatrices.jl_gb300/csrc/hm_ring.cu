@@ -252,11 +252,5 @@ __global__ void __launch_bounds__(kRingWarps * 32)
                                                          float *, int64_t);
 HM_INST_RING(4, 768, 3) HM_INST_RING(4, 512, 4) HM_INST_RING(4, 1024, 3)
 HM_INST_RING(8, 768, 3) HM_INST_RING(8, 512, 4) HM_INST_RING(8, 1024, 3)
-template __global__ void ring_part<4, true, 1280, 3>(MulArgs<float>, const hm_seg *, int, const hm_piece *,
-                                                     const float *, const float *, const float *, int, float *,
-                                                     int64_t);
-template __global__ void ring_part<8, true, 1280, 3>(MulArgs<float>, const hm_seg *, int, const hm_piece *,
-                                                     const float *, const float *, const float *, int, float *,
-                                                     int64_t);
 
 }  // namespace hm
