@@ -1015,9 +1015,12 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
     if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
         if (h->storage == HM_DF64) return launch_df<FAR ? 1 : 0, KB>(h, ma, s, t, panels, yfar, st, pdl, ldf, 0);
     }
-    if constexpr (FAR && std::is_same<S, A>::value) {
-        // far-field rows one thread per row (the default and ring schedules;
-        // the warp and streamed kernels keep their own far-field form)
+    if constexpr (FAR && KB >= 4 && std::is_same<S, A>::value) {
+        // far-field rows one thread per row for 3-8 right-hand sides (the default
+        // and ring schedules; the warp and streamed kernels keep their own
+        // far-field form).  Measured: 512-instance batch at 8, 0.55 against
+        // 0.76 ms; with 1 right-hand side at n = 2^20 the warp kernel's
+        // four-rows-per-lane form stays faster (25 against 41 us)
         const Sched fs = cur_sched(h);
         if (h->stream_ctas > 0 && h->part_width[1] <= 64 && (fs.near_kernel == 0 || fs.near_kernel == 3)) {
             HM_TRY(launch_k("far_rows", far_rows<S, A, KB>, dim3((unsigned)((h->n_segs + 3) / 4)), dim3(256), 0, st,

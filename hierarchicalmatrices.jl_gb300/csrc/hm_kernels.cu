@@ -1491,8 +1491,7 @@ __global__ void expand_k(MulArgs<S> ma, const hm_seg *segs, const hm_piece *piec
 #define HM_INST_FAR(S, A, KB)                                                                        \
     template __global__ void far_rows<S, A, KB>(MulArgs<S>, const hm_seg *, int, const hm_piece *, const S *, \
                                                 const A *, const A *, int, S *, int64_t);
-HM_INST_FAR(float, float, 1) HM_INST_FAR(float, float, 2) HM_INST_FAR(float, float, 4) HM_INST_FAR(float, float, 8)
-HM_INST_FAR(double, double, 1) HM_INST_FAR(double, double, 2) HM_INST_FAR(double, double, 4)
+HM_INST_FAR(float, float, 4) HM_INST_FAR(float, float, 8) HM_INST_FAR(double, double, 4)
 HM_INST_FAR(double, double, 8)
 #define HM_INST_MV(S, A)                                                                             \
     template __global__ void leaf_up<S, A, 1>(MulArgs<S>, const hm_vpanel *, int, const S *, A *, int, int, int); \
