@@ -286,6 +286,8 @@ def run_batch(hm, torch, dev, args, count=512, nrhs=8):
     xs, ys, boxes = batch_instances(count)
     t0 = time.perf_counter()
     Hb = hm.KernelMatrixBatch(hm.cauchykernel, xs, ys, boxes, dtype=np.float32)
+    if getattr(args, "wide_tree", None):
+        Hb.set_wide_tree({"off": False, "on": True, "all": "all"}[args.wide_tree])
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     st = Hb.stats()
@@ -502,6 +504,33 @@ def run_grad(hm, torch, dev, args, n=65536):
             "ms_per_grad": ms, "grads_per_s": 1e3 / ms, "reps": reps}
 
 
+def profile_case(hm, torch, args):
+    """Three products of one workload, for ncu captures (no timing)."""
+    n = args.n
+    x, y = grid_points(n)
+    case = args.profile_case
+    dtype = {"fp64": np.float64, "df64": "df64"}.get(case, np.float32)
+    k = {"k8": 8, "k32": 32, "k256": 256}.get(case, 1)
+    H = hm.KernelMatrix(hm.cauchykernel, x, y, 1.0, 0.0, 1.0, 0.0, dtype=dtype)
+    if args.wide_tree:
+        H.set_wide_tree({"off": False, "on": True, "all": "all"}[args.wide_tree])
+    if case == "headline":
+        H.set_overlap(4)                        # the autotuner's choice for one FP32 right-hand side
+        H.set_pdl(True)
+    else:
+        H.set_overlap(0)
+    tdt = torch.float64 if case in ("fp64", "df64") else torch.float32
+    B = torch.randn(k, n, device="cuda", dtype=tdt).t()
+    U = torch.empty(k, n, device="cuda", dtype=tdt).t()
+    if k == 1:
+        B, U = B[:, 0].contiguous(), U[:, 0].contiguous()
+    for _ in range(3):
+        H.mul(U, B, accumulate=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": case, "n": n, "nrhs": k, "ok": True}), flush=True)
+    return 0
+
+
 # ----------------------------------------------------------------- GPU arm
 
 def main():
@@ -525,6 +554,14 @@ def main():
                     help="print the headline product's stage timeline for each stream schedule (for profiling)")
     ap.add_argument("--autotune-reps", type=int, default=50,
                     help="products timed per candidate schedule by the autotuner (fewer for profiling runs)")
+    ap.add_argument("--profile-case", default=None,
+                    choices=["headline", "fp64", "df64", "k8", "k32", "k256"],
+                    help="run three products of one workload at --n points and exit (for ncu captures): the "
+                         "headline FP32 product with the autotuner's choice for it (near field after the leaf "
+                         "stage, programmatic launches), the FP64 / FP64-double-float product, or FP32 with 8, 32 "
+                         "or 256 right-hand sides with every stage on one stream")
+    ap.add_argument("--wide-tree", default=None, choices=["off", "on", "all"],
+                    help="HM_OPT_WIDE_TREE for --profile-case and --only-batch runs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -546,6 +583,9 @@ def main():
     if args.timeline:
         print(json.dumps({"timeline_us": stage_timeline(hm, torch, args.n)}), flush=True)
         return 0
+
+    if args.profile_case:
+        return profile_case(hm, torch, args)
 
     if args.only_batch:
         print(json.dumps({"batch": run_batch(hm, torch, torch.device("cuda", local), args,
