@@ -453,13 +453,12 @@ void set_vp_caps(hm_handle *h, const std::vector<hm_vpanel> &vps)
 
 // HM_DF64 storage: the FP64 panel values become (h, l) FP32 pairs in place;
 // a value too large for the pair is an error (HM_ERR_UNSUPPORTED).
-int to_double_float(hm_handle *h, double *P, cudaStream_t st)
+int to_double_float(hm_handle *h, double *P, int64_t n, cudaStream_t st)
 {
-    if (!P || h->pstore_elems == 0) return HM_OK;
+    if (!P || n == 0) return HM_OK;
     int *bad = nullptr;
     HM_TRY(h->alloc(&bad, 1));
     HM_CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
-    const int64_t n = h->pstore_elems;
     const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
     panels_to_df<<<grid, 256, 0, st>>>(P, n, bad);
     HM_CK_LAUNCH("panels_to_df");
@@ -467,7 +466,7 @@ int to_double_float(hm_handle *h, double *P, cudaStream_t st)
     HM_CK(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     HM_CK(cudaStreamSynchronize(st));
     if (hb) {
-        set_error("a panel value's magnitude reaches 2^127: too large for double-float (HM_DF64) storage; "
+        set_error("a stored value's magnitude reaches 2^127: too large for double-float (HM_DF64) storage; "
                   "use HM_F64");
         return HM_ERR_UNSUPPORTED;
     }
@@ -546,7 +545,12 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
         HM_CK_LAUNCH("fill_segments");
     }
     if constexpr (sizeof(S) == 8) {
-        if (h->storage == HM_DF64) HM_TRY(to_double_float(h, reinterpret_cast<double *>(Pn), st));
+        if (h->storage == HM_DF64) {
+            // panels, column bases and far-field blocks as double-float pairs
+            HM_TRY(to_double_float(h, reinterpret_cast<double *>(Pn), P.pstore_elems, st));
+            HM_TRY(to_double_float(h, reinterpret_cast<double *>(V), P.vstore_elems, st));
+            HM_TRY(to_double_float(h, reinterpret_cast<double *>(F), P.fstore_elems, st));
+        }
     }
     HM_CK(cudaStreamSynchronize(st));
     return HM_OK;
@@ -768,7 +772,20 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     const A *T = static_cast<const A *>(h->d_T);
     {
         StageTimer tm(h, timing ? 0 : -1, st);
-        if (h->n_vp) {
+        bool leaf_done = false;
+        if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
+            if (h->n_vp && h->storage == HM_DF64) {
+                // column bases as double-float pairs: every right-hand side in one launch
+                const size_t smem = (size_t)kWarpsPerCta * h->vp_cap * sizeof(float2);
+                HM_TRY(ensure_smem(leaf_up_df, smem));
+                leaf_up_df<<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(
+                    ma, h->d_vp, h->n_vp, static_cast<const float2 *>(h->d_V), t, r, h->vp_cap);
+                HM_CK_LAUNCH("leaf_up_df");
+                chain = true;
+                leaf_done = true;
+            }
+        }
+        if (h->n_vp && !leaf_done) {
             const size_t smem = (size_t)kWarpsPerCta * leaf_up_warp_bytes<S, A, QC>(h->vp_cap, h->vp_wcap);
             HM_TRY(ensure_smem(leaf_up<S, A, QC>, smem));
             leaf_up<S, A, QC><<<warp_ctas(h->n_vp), 32 * kWarpsPerCta, smem, st>>>(
@@ -809,8 +826,18 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
     {
         StageTimer tm(h, timing ? 1 : -1, st);
         bool done = false;
+        if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
+            if (h->n_m2l_rows && h->storage == HM_DF64) {
+                // far-field blocks as double-float pairs: every right-hand side in one launch
+                HM_TRY(launch_k("m2l_df", m2l_df, dim3((unsigned)((h->n_m2l_rows + 7) / 8)), dim3(256), 0, st,
+                                pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents,
+                                static_cast<const float2 *>(h->d_F), h->fstride, t, s, r, k));
+                chain = true;
+                done = true;
+            }
+        }
         if constexpr (QC > 1) {
-            if (h->n_m2l_rows && nq > 1) {
+            if (!done && h->n_m2l_rows && nq > 1) {
                 // many right-hand sides: one CTA per row box, its blocks staged once
                 const size_t smem = 8 * (size_t)h->fstride * sizeof(S) +
                                     (size_t)kWarpsPerCta * 2 * QC * HM_RMAX * sizeof(A);
@@ -877,7 +904,8 @@ template <typename S, typename A>
 bool wide_tree_ok(const hm_handle *h, const MulArgs<S> &ma, int wide)
 {
     const int kmin = wide >= 2 ? 2 : wide == 1 ? kWideMinK : INT32_MAX;
-    if (!(std::is_same<S, A>::value && ma.k >= kmin && h->r == 20 && h->vp_wide && !ma.xin && h->fstride % 4 == 0))
+    if (!(std::is_same<S, A>::value && ma.k >= kmin && h->r == 20 && h->vp_wide && !ma.xin && h->fstride % 4 == 0 &&
+          h->storage != HM_DF64))
         return false;
     const int G = wide_groups(ma.k);
     const size_t lv = (size_t)(32 / G) * 20 * sizeof(A);
@@ -1245,7 +1273,7 @@ int ensure_drow(hm_handle *h, cudaStream_t st)
         HM_CK_LAUNCH("fill_segments<drow>");
     }
     if constexpr (sizeof(S) == 8) {
-        if (h->storage == HM_DF64) HM_TRY(to_double_float(h, reinterpret_cast<double *>(dP), st));
+        if (h->storage == HM_DF64) HM_TRY(to_double_float(h, reinterpret_cast<double *>(dP), h->pstore_elems, st));
     }
     // complete before the panels are published: a later product may run on another stream
     HM_CK(cudaStreamSynchronize(st));

@@ -15,8 +15,10 @@
 // (the "sloppy" double-word addition analysed by Joldes, Muller and Popescu,
 // ACM TOMS 44(2), 2017): 15 FP32 operations per term, all rounded to nearest
 // (no contraction: the error-free transformations need exact roundings).
-// Row results are formed in FP64 as sh + sl.  The tree passes (bases,
-// transfers, far-field blocks) stay in FP64.
+// Row results are formed in FP64 as sh + sl.  The column bases V and the
+// far-field blocks F are stored the same way and their products (leaf_up_df,
+// m2l_df) run in the same arithmetic; coefficients stay FP64 in memory and the
+// transfer passes between tree levels stay FP64.
 #include "hm_kernels.cuh"
 #include "hm_async.cuh"
 
@@ -147,6 +149,104 @@ __global__ void expand_df(MulArgs<double> ma, const hm_seg *segs, int nsegs, con
                 }
             }
         }
+    }
+}
+
+// Explicit column bases with HM_DF64 storage (V as (h, l) pairs, row-major,
+// ld == width <= 32): t[slot][q][col0 + m] = sum_j V[j][m] x[row0 + j][q] in
+// double-float arithmetic on the FP32 pipes, one warp per panel, lane m one
+// basis column; the panel's right-hand-side rows are split into pairs once
+// per right-hand side in shared memory (cap pairs per warp).  With ma.xin
+// (a page-locked host source) the rows are read there and stored into x for
+// the kernels after this one, as leaf_up does.
+__global__ void leaf_up_df(MulArgs<double> ma, const hm_vpanel *vp, int npanels, const float2 *V, double *t, int r,
+                           int cap)
+{
+    extern __shared__ float2 leaf_df_smem[];
+    pdl_trigger();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    if (w >= (int64_t)npanels) return;
+    const hm_vpanel P = vp[w];
+    float2 *xs = leaf_df_smem + (size_t)wib * cap;
+    const float2 *Vp = V + P.off;
+    const double *xsrc = ma.xin ? ma.xin : ma.x;
+    double *xcopy = ma.xin ? const_cast<double *>(ma.x) : nullptr;
+    const int nr = min((int)P.nrows, cap);
+    for (int q = 0; q < ma.k; ++q) {
+        for (int j = lane; j < P.nrows; j += 32) {
+            const int64_t e = (P.row0 + j) * ma.incx + (int64_t)q * ma.ldx;
+            const double v = xsrc[e];
+            if (xcopy) xcopy[e] = v;
+            if (j < nr) xs[j] = df_split(v);
+        }
+        __syncwarp();
+        if (lane < P.width) {
+            float sh = 0.f, sl = 0.f;
+            int j = 0;
+            for (; j + 8 <= nr; j += 8) {
+                float2 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = Vp[(int64_t)(j + u) * P.ld + lane];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) df_fma(sh, sl, v[u].x, v[u].y, xs[j + u].x, xs[j + u].y);
+            }
+            for (; j < nr; ++j) {
+                const float2 v = Vp[(int64_t)j * P.ld + lane];
+                df_fma(sh, sl, v.x, v.y, xs[j].x, xs[j].y);
+            }
+            // rows past the staged ones (panels longer than cap) straight from x
+            for (j = nr; j < P.nrows; ++j) {
+                const float2 v = Vp[(int64_t)j * P.ld + lane];
+                const float2 xv = df_split(xsrc[(P.row0 + j) * ma.incx + (int64_t)q * ma.ldx]);
+                df_fma(sh, sl, v.x, v.y, xv.x, xv.y);
+            }
+            t[((int64_t)P.slot * ma.k + q) * r + P.col0 + lane] = __dadd_rn((double)sh, (double)sl);
+        }
+        __syncwarp();
+    }
+}
+
+// Far-field blocks with HM_DF64 storage (F as (h, l) pairs, r x r column-major
+// with fstride pairs between blocks): s[slot][q][m] = sum_e sum_n F_e[m + r n]
+// t[yslot_e][q][n], one warp per row slot, lane m one coefficient; each
+// block's column coefficients are split into pairs in shared memory (lane n
+// splits coefficient n) and the next block's pairs of F are loaded while the
+// current block is multiplied.
+__global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, int fstride,
+                       const double *t, double *s, int r, int k)
+{
+    __shared__ float2 ts[8][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    pdl_trigger();
+    pdl_wait();                                                // the upward pass's coefficients are ready
+    if (w >= (int64_t)nrows) return;
+    const hm_m2l_row R = rows[w];
+    for (int q = 0; q < k; ++q) {
+        float sh = 0.f, sl = 0.f;
+        for (int e = R.begin; e < R.end; ++e) {
+            const hm_m2l_ent E = ents[e];
+            if (lane < r) ts[wib][lane] = df_split(t[((int64_t)E.yslot * k + q) * r + lane]);
+            __syncwarp();
+            if (lane < r) {
+                const float2 *Fe = F + E.foff + lane;
+                int n = 0;
+                for (; n + 4 <= r; n += 4) {
+                    float2 f[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) f[u] = Fe[(int64_t)r * (n + u)];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) df_fma(sh, sl, f[u].x, f[u].y, ts[wib][n + u].x, ts[wib][n + u].y);
+                }
+                for (; n < r; ++n) {
+                    const float2 f = Fe[(int64_t)r * n];
+                    df_fma(sh, sl, f.x, f.y, ts[wib][n].x, ts[wib][n].y);
+                }
+            }
+            __syncwarp();
+        }
+        if (lane < r) s[((int64_t)R.slot * k + q) * r + lane] = __dadd_rn((double)sh, (double)sl);
     }
 }
 

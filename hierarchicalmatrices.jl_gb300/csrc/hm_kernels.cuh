@@ -278,6 +278,12 @@ __global__ void xfer_task_w(const hm_task *tasks, const hm_step *steps, const hm
 // far-field columns, 2 all), right-hand sides q0 .. q0 + KB - 1 of k;
 // shared memory kWarpsPerCta * maxw * KB * 8 bytes per CTA.
 __global__ void panels_to_df(double *P, int64_t n, int *bad);
+// leaf_up_df: one warp per basis panel, shared memory cap pairs per warp;
+// m2l_df: one warp per row slot, 256 threads per CTA (8 warps).
+__global__ void leaf_up_df(MulArgs<double> ma, const hm_vpanel *vp, int npanels, const float2 *V, double *t, int r,
+                           int cap);
+__global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, int fstride,
+                       const double *t, double *s, int r, int k);
 template <int PART, int KB>
 __global__ void expand_df(MulArgs<double> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const float2 *P,
                           const double *s, const double *t, int r, int maxw, double *yfar, int64_t ldf, int q0);
