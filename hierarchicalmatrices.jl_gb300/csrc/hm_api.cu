@@ -550,6 +550,7 @@ int build_device(hm_handle *h, const Plan &P, const std::vector<double> &cheb, c
             HM_TRY(to_double_float(h, reinterpret_cast<double *>(Pn), P.pstore_elems, st));
             HM_TRY(to_double_float(h, reinterpret_cast<double *>(V), P.vstore_elems, st));
             HM_TRY(to_double_float(h, reinterpret_cast<double *>(F), P.fstore_elems, st));
+            HM_TRY(to_double_float(h, reinterpret_cast<double *>(h->d_T), (int64_t)T.size(), st));
         }
     }
     HM_CK(cudaStreamSynchronize(st));
@@ -795,7 +796,26 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         }
         if (mid && mid_after == 2) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // leaf bases done
         const size_t usm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[0] * QC * r) * sizeof(A);
-        if (usm <= kTaskSmemMax) {
+        bool up_done = false;
+        if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
+            if (h->storage == HM_DF64) {
+                // transfers in double-float arithmetic, one right-hand side per CTA
+                const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[0] * r) * sizeof(float2);
+                HM_TRY(ensure_smem(xfer_df<true>, xsm));
+                const int last = last_band(h->up_band_ptr);
+                for (size_t bd = 0; bd + 1 < h->up_band_ptr.size(); ++bd) {
+                    const int b = h->up_band_ptr[bd], n = h->up_band_ptr[bd + 1] - b;
+                    if (!n) continue;
+                    HM_TRY(launch_k("xfer_up_df", xfer_df<true>, dim3(n, (unsigned)k), dim3(kWarpCta), xsm, st,
+                                    pdl_on && chain, h->d_up_tasks + b, h->d_up_steps, h->d_up_ents,
+                                    static_cast<const float2 *>(h->d_T), t, r, k, (int)bd != last ? 1 : 0));
+                    chain = true;
+                }
+                up_done = true;
+            }
+        }
+        if (up_done) {
+        } else if (usm <= kTaskSmemMax) {
             const size_t xsm = usm;
             HM_TRY(ensure_smem(xfer_up_task<A, QC>, xsm));
             const int last = last_band(h->up_band_ptr);
@@ -860,7 +880,25 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         }
         if (mid && mid_after == 1) { HM_CK(cudaEventRecord(mid, st)); chain = false; }  // far-field stage done
         const size_t dsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[1] * QC * r) * sizeof(A);
-        if (dsm <= kTaskSmemMax) {
+        bool down_done = false;
+        if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
+            if (h->storage == HM_DF64) {
+                const size_t xsm = (2 * (size_t)HM_RMAX * HM_RMAX + (size_t)h->band_locals[1] * r) * sizeof(float2);
+                HM_TRY(ensure_smem(xfer_df<false>, xsm));
+                const int last = last_band(h->down_band_ptr);
+                for (size_t bd = 0; bd + 1 < h->down_band_ptr.size(); ++bd) {
+                    const int b = h->down_band_ptr[bd], n = h->down_band_ptr[bd + 1] - b;
+                    if (!n) continue;
+                    HM_TRY(launch_k("xfer_down_df", xfer_df<false>, dim3(n, (unsigned)k), dim3(kWarpCta), xsm, st,
+                                    pdl_on && chain, h->d_down_tasks + b, h->d_down_steps, h->d_down_ents,
+                                    static_cast<const float2 *>(h->d_T), s, r, k, (int)bd != last ? 1 : 0));
+                    chain = true;
+                }
+                down_done = true;
+            }
+        }
+        if (down_done) {
+        } else if (dsm <= kTaskSmemMax) {
             const size_t xsm = dsm;
             HM_TRY(ensure_smem(xfer_down_task<A, QC>, xsm));
             const int last = last_band(h->down_band_ptr);

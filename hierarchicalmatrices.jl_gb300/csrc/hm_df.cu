@@ -17,8 +17,9 @@
 // (no contraction: the error-free transformations need exact roundings).
 // Row results are formed in FP64 as sh + sl.  The column bases V and the
 // far-field blocks F are stored the same way and their products (leaf_up_df,
-// m2l_df) run in the same arithmetic; coefficients stay FP64 in memory and the
-// transfer passes between tree levels stay FP64.
+// m2l_df) and the transfers between tree levels (xfer_df, with the transfer
+// matrices as pairs) run in the same arithmetic; coefficients stay FP64 in
+// memory.
 #include "hm_kernels.cuh"
 #include "hm_async.cuh"
 
@@ -249,6 +250,89 @@ __global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents
         if (lane < r) s[((int64_t)R.slot * k + q) * r + lane] = __dadd_rn((double)sh, (double)sl);
     }
 }
+
+// Transfer bands with HM_DF64 storage (the transfer matrices T_0, T_1 as
+// (h, l) pairs, T_c[m' r + m]): the task structure of xfer_up_task /
+// xfer_down_task with one right-hand side per CTA (grid: tasks x k), local
+// coefficient vectors as pairs in shared memory, products in double-float
+// arithmetic; the coefficients in global memory stay FP64 (split when read,
+// h + l when written).
+//   upward:   t[parent][m] = sum_c sum_m' T_c[m', m] t[child_c][m']
+//   downward: s[child_c][m'] += sum_m T_c[m', m] s[parent][m]
+template <bool UP>
+__global__ void xfer_df(const hm_task *tasks, const hm_step *steps, const hm_xfer *ents, const float2 *T,
+                        double *coef, int r, int k, int early)
+{
+    extern __shared__ float2 xfer_df_smem[];
+    float2 *Ts = xfer_df_smem;                                 // 2 r r pairs
+    float2 *L = Ts + 2 * HM_RMAX * HM_RMAX;                    // r pairs per local
+    const hm_task tk = tasks[blockIdx.x];
+    const int e0 = steps[tk.step0].e0, e1 = steps[tk.step1 - 1].e1, nrec = e1 - e0;
+    const int q = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (early) pdl_trigger();
+    for (int i = threadIdx.x; i < 2 * r * r; i += blockDim.x) Ts[i] = T[i];
+    pdl_wait();                                                // inputs of the band are ready
+    for (int rec = warp; rec < nrec; rec += nw) {
+        const hm_xfer X = ents[e0 + rec];
+        if (lane >= r) continue;
+#pragma unroll
+        for (int c = 0; c < (UP ? 2 : 3); ++c) {
+            int lc, slot;
+            if (UP) {
+                lc = c ? (X.pad >> 16) : (X.pad & 0xffff);
+                slot = c ? X.c1 : X.c0;
+                if (lc < nrec) continue;                       // produced by an earlier level of this task
+            } else if (c < 2) {
+                lc = 2 * rec + c;                              // children start from their far-field values
+                slot = c ? X.c1 : X.c0;
+            } else {
+                lc = X.pad;
+                slot = X.slot;
+                if (lc < 2 * nrec) continue;                   // a child of an earlier level of this task
+            }
+            L[lc * r + lane] = df_split(coef[((int64_t)slot * k + q) * r + lane]);
+        }
+    }
+    __syncthreads();
+    for (int st = tk.step0; st < tk.step1; ++st) {
+        const hm_step S = steps[st];
+        for (int w = warp; w < S.e1 - S.e0; w += nw) {
+            const int e = S.e0 + w;
+            const hm_xfer X = ents[e];
+            if (lane >= r) continue;
+            if (UP) {
+                const float2 *c0 = L + (X.pad & 0xffff) * r, *c1 = L + (X.pad >> 16) * r;
+                float sh = 0.f, sl = 0.f;
+                for (int mp = 0; mp < r; ++mp) {
+                    const float2 a0 = Ts[mp * r + lane], a1 = Ts[r * r + mp * r + lane];
+                    df_fma(sh, sl, a0.x, a0.y, c0[mp].x, c0[mp].y);
+                    df_fma(sh, sl, a1.x, a1.y, c1[mp].x, c1[mp].y);
+                }
+                L[(e - e0) * r + lane] = make_float2(sh, sl);
+                coef[((int64_t)X.slot * k + q) * r + lane] = __dadd_rn((double)sh, (double)sl);
+            } else {
+                const float2 *p = L + X.pad * r;
+                float2 *o0 = L + (2 * (e - e0)) * r, *o1 = o0 + r;
+                float h0 = o0[lane].x, l0 = o0[lane].y, h1 = o1[lane].x, l1 = o1[lane].y;
+                for (int m = 0; m < r; ++m) {
+                    const float2 t0 = Ts[lane * r + m], t1 = Ts[r * r + lane * r + m];
+                    df_fma(h0, l0, t0.x, t0.y, p[m].x, p[m].y);
+                    df_fma(h1, l1, t1.x, t1.y, p[m].x, p[m].y);
+                }
+                o0[lane] = make_float2(h0, l0);
+                o1[lane] = make_float2(h1, l1);
+                coef[((int64_t)X.c0 * k + q) * r + lane] = __dadd_rn((double)h0, (double)l0);
+                coef[((int64_t)X.c1 * k + q) * r + lane] = __dadd_rn((double)h1, (double)l1);
+            }
+        }
+        __syncthreads();
+    }
+}
+template __global__ void xfer_df<true>(const hm_task *, const hm_step *, const hm_xfer *, const float2 *, double *,
+                                       int, int, int);
+template __global__ void xfer_df<false>(const hm_task *, const hm_step *, const hm_xfer *, const float2 *, double *,
+                                        int, int, int);
 
 #define HM_INST_DF(PART)                                                                                        \
     template __global__ void expand_df<PART, 1>(MulArgs<double>, const hm_seg *, int, const hm_piece *,          \
