@@ -1079,7 +1079,17 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
                    cudaStream_t st, bool pdl = false, int64_t ldf = 0)
 {
     if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
-        if (h->storage == HM_DF64) return launch_df<FAR ? 1 : 0, KB>(h, ma, s, t, panels, yfar, st, pdl, ldf, 0);
+        if (h->storage == HM_DF64) {
+            if (FAR && h->stream_ctas > 0 && h->part_width[1] <= 64) {
+                // far-field rows one thread per row, right-hand side by right-hand side
+                for (int q0 = 0; q0 < ma.k; ++q0)
+                    HM_TRY(launch_k("far_rows_df", far_rows_df, dim3((unsigned)((h->n_segs + 3) / 4)), dim3(256), 0,
+                                    st, pdl && q0 == 0, ma, h->d_segs, h->n_segs, h->d_pieces,
+                                    static_cast<const float2 *>(panels), s, t, h->r, yfar, ldf, q0));
+                return HM_OK;
+            }
+            return launch_df<FAR ? 1 : 0, KB>(h, ma, s, t, panels, yfar, st, pdl, ldf, 0);
+        }
     }
     if constexpr (FAR && KB >= 4 && std::is_same<S, A>::value) {
         // far-field rows one thread per row for 3-8 right-hand sides (the default
@@ -1138,8 +1148,11 @@ int launch_part_kb(hm_handle *h, const MulArgs<S> &ma, const A *s, const A *t, c
             HM_TRY(ensure_smem(kern, smem));
             HM_TRY(prefer_shared(kern));
             // about kRingSegsPerWarp segments per warp: CTAs retire through the
-            // product and hand their slots to the tree passes on the side stream
-            const int64_t warps = (h->n_segs + kRingSegsPerWarp - 1) / kRingSegsPerWarp;
+            // product and hand their slots to the tree passes on the side stream;
+            // fewer per warp where that would leave SMs short of 16 warps each
+            const int64_t spw = std::max<int64_t>(
+                1, std::min<int64_t>(kRingSegsPerWarp, h->n_segs / ((int64_t)16 * std::max(h->sms, 1))));
+            const int64_t warps = (h->n_segs + spw - 1) / spw;
             const unsigned grid = (unsigned)((warps + kRingWarps - 1) / kRingWarps);
             HM_TRY(launch_k(FAR ? "ring_far" : "ring_near", kern, dim3(grid), dim3(32 * kRingWarps), smem, st,
                             FAR && pdl, ma, h->d_segs, h->n_segs, h->d_pieces, static_cast<const float *>(panels),

@@ -214,6 +214,46 @@ __global__ void leaf_up_df(MulArgs<double> ma, const hm_vpanel *vp, int npanels,
 // block's column coefficients are split into pairs in shared memory (lane n
 // splits coefficient n) and the next block's pairs of F are loaded while the
 // current block is multiplied.
+namespace {
+// rank 20: the next block's pairs of F (and its column coefficients) are
+// loaded into registers while the current block is multiplied
+__device__ __forceinline__ void m2l_df_r20(const hm_m2l_row &R, const hm_m2l_ent *ents, const float2 *F,
+                                           const double *t, double *s, int k, int lane, float2 *ts)
+{
+    constexpr int R20 = 20;
+    for (int q = 0; q < k; ++q) {
+        float sh = 0.f, sl = 0.f;
+        float2 fc[R20];
+        double tc = 0.0;
+        if (R.begin < R.end && lane < R20) {
+            const hm_m2l_ent E = ents[R.begin];
+#pragma unroll
+            for (int n = 0; n < R20; ++n) fc[n] = F[E.foff + lane + (int64_t)R20 * n];
+            tc = t[((int64_t)E.yslot * k + q) * R20 + lane];
+        }
+        for (int e = R.begin; e < R.end; ++e) {
+            if (lane < R20) ts[lane] = df_split(tc);
+            __syncwarp();
+            float2 fn[R20];
+            if (e + 1 < R.end && lane < R20) {
+                const hm_m2l_ent E = ents[e + 1];
+#pragma unroll
+                for (int n = 0; n < R20; ++n) fn[n] = F[E.foff + lane + (int64_t)R20 * n];
+                tc = t[((int64_t)E.yslot * k + q) * R20 + lane];
+            }
+            if (lane < R20) {
+#pragma unroll
+                for (int n = 0; n < R20; ++n) df_fma(sh, sl, fc[n].x, fc[n].y, ts[n].x, ts[n].y);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int n = 0; n < R20; ++n) fc[n] = fn[n];
+        }
+        if (lane < R20) s[((int64_t)R.slot * k + q) * R20 + lane] = __dadd_rn((double)sh, (double)sl);
+    }
+}
+}  // namespace
+
 __global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, int fstride,
                        const double *t, double *s, int r, int k)
 {
@@ -224,6 +264,10 @@ __global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents
     pdl_wait();                                                // the upward pass's coefficients are ready
     if (w >= (int64_t)nrows) return;
     const hm_m2l_row R = rows[w];
+    if (r == 20) {
+        m2l_df_r20(R, ents, F, t, s, k, lane, ts[wib]);
+        return;
+    }
     for (int q = 0; q < k; ++q) {
         float sh = 0.f, sl = 0.f;
         for (int e = R.begin; e < R.end; ++e) {
@@ -333,6 +377,62 @@ template __global__ void xfer_df<true>(const hm_task *, const hm_step *, const h
                                        int, int, int);
 template __global__ void xfer_df<false>(const hm_task *, const hm_step *, const hm_xfer *, const float2 *, double *,
                                         int, int, int);
+
+// Far-field rows with HM_DF64 storage, one thread per row (four segments of at
+// most 64 rows per CTA of 256 threads): y_far[row] = sum_c U[row][c] s[c] over
+// the segment's far columns (at most 64), the coefficients split into pairs
+// once per segment in shared memory, the row's pairs read column by column
+// (consecutive threads, consecutive rows), double-float accumulation; one
+// right-hand side q0.  Rows go to yfar or, without it, are added into y.
+__global__ void __launch_bounds__(256)
+    far_rows_df(MulArgs<double> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces, const float2 *P,
+                const double *s, const double *t, int r, double *yfar, int64_t ldf, int q0)
+{
+    __shared__ float2 cs[4][64];
+    pdl_wait();                                                // the downward pass's coefficients are ready
+    const int ls = threadIdx.x >> 6, row = threadIdx.x & 63;
+    const int j = blockIdx.x * 4 + ls;
+    const int k = ma.k;
+    hm_seg G{};
+    int nfar = 0;
+    if (j < nsegs) {
+        G = segs[j];
+        nfar = G.nfar;
+        if (row < nfar) {
+            int pc = 0, pi = 0;
+            hm_piece Q = pieces[G.piece0];
+            while (row >= pc + Q.width) {
+                pc += Q.width;
+                Q = pieces[G.piece0 + ++pi];
+            }
+            cs[ls][row] = df_split((Q.kind == HM_PIECE_TCOEF ? t : s)[((int64_t)Q.src * k + q0) * r + (row - pc)]);
+        }
+    }
+    __syncthreads();
+    if (j >= nsegs || row >= G.nrows) return;
+    if (nfar == 0 && !yfar) return;                            // y += 0
+    float sh = 0.f, sl = 0.f;
+    const float2 *pr = P + G.poff + row;
+    int c = 0;
+    for (; c + 4 <= nfar; c += 4) {
+        float2 u[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) u[i] = pr[(int64_t)(c + i) * G.ld];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) df_fma(sh, sl, u[i].x, u[i].y, cs[ls][c + i].x, cs[ls][c + i].y);
+    }
+    for (; c < nfar; ++c) {
+        const float2 u = pr[(int64_t)c * G.ld];
+        df_fma(sh, sl, u.x, u.y, cs[ls][c].x, cs[ls][c].y);
+    }
+    const double v = __dadd_rn((double)sh, (double)sl);
+    if (yfar) {
+        yfar[(G.row0 + row) + (int64_t)q0 * ldf] = v;
+    } else {
+        double *yp = ma.y + (G.row0 + row) * ma.incy + (int64_t)q0 * ma.ldy;
+        *yp = *yp + v;
+    }
+}
 
 #define HM_INST_DF(PART)                                                                                        \
     template __global__ void expand_df<PART, 1>(MulArgs<double>, const hm_seg *, int, const hm_piece *,          \

@@ -284,6 +284,11 @@ __global__ void leaf_up_df(MulArgs<double> ma, const hm_vpanel *vp, int npanels,
                            int cap);
 __global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, int fstride,
                        const double *t, double *s, int r, int k);
+// far_rows_df: far-field rows of right-hand side q0, one thread per row, four
+// segments of at most 64 rows per CTA of 256 threads (at most 64 far columns).
+__global__ void far_rows_df(MulArgs<double> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces,
+                            const float2 *P, const double *s, const double *t, int r, double *yfar, int64_t ldf,
+                            int q0);
 // xfer_df: one CTA per (band task, right-hand side), shared memory
 // (2 HM_RMAX^2 + locals r) pairs.
 template <bool UP>
