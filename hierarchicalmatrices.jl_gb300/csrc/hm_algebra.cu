@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
@@ -129,16 +130,113 @@ __device__ void apply_q(const T *A, int64_t m, int kk, const T *tau, T *y)
     }
 }
 
+// The Jacobi rotation of lr_svd: t = tan(theta) is the smaller root of
+// t^2 + 2 zeta t - 1 = 0, zeta = (be - al) / (2 ga), i.e.
+// |t| = |g| / (|a| + sqrt(a^2 + g^2)) with a = be - al, g = 2 ga and the sign
+// of a g.  t is formed in FP32 (FP64 issue time is scarce on GB300): from a
+// and g scaled by a common power of two when |g| >= 2^-30 |a|, else as
+// t = g / (2a) from the two mantissas with the exponents applied apart
+// (strongly graded columns give angles far below FP32's range).  Its
+// relative error, about 1e-7, only leaves an inner product of that relative
+// size for the next sweep.  c = (1 + t^2)^(-1/2) is then refined in T by two
+// Newton steps from the FP32 estimate, so c^2 + s^2 = 1 to T's rounding and
+// every rotation is orthogonal in T.  Returns false when t underflows.
+__device__ __forceinline__ int exponent_of(double x) { return ((__double2hiint(x) >> 20) & 0x7ff) - 1023; }
+__device__ __forceinline__ int exponent_of(float x) { return ((__float_as_int(x) >> 23) & 0xff) - 127; }
+template <typename T> __device__ __forceinline__ T pow2(int e);
+template <> __device__ __forceinline__ double pow2<double>(int e)
+{
+    e = e < -1022 ? -1022 : (e > 1023 ? 1023 : e);
+    return __hiloint2double((1023 + e) << 20, 0);
+}
+template <> __device__ __forceinline__ float pow2<float>(int e)
+{
+    e = e < -126 ? -126 : (e > 127 ? 127 : e);
+    return __int_as_float((127 + e) << 23);
+}
+
+template <typename T>
+__device__ __forceinline__ bool jacobi_tangent(T al, T be, T ga, T &t)
+{
+    const T a = be - al, g = ga + ga;
+    const int ea = a == T(0) ? -100000 : exponent_of(a), eg = exponent_of(g);
+    if (eg < ea - 30) {
+        const float am = (float)(a * pow2<T>(-ea)), gm = (float)(g * pow2<T>(-eg));
+        if (eg - ea < (sizeof(T) == 8 ? -1000 : -120)) return false;     // t below T's normal range
+        t = (T)(gm / (am + am)) * pow2<T>(eg - ea);
+    } else {
+        const int e = ea > eg ? ea : eg;
+        const T sc = pow2<T>(-e);
+        const float af = (float)(a * sc), gf = (float)(g * sc);
+        float t32 = fabsf(gf) / (fabsf(af) + sqrtf(fmaf(af, af, gf * gf)));
+        if ((af < 0.f) != (gf < 0.f)) t32 = -t32;
+        t = (T)t32;
+    }
+    return t != T(0);
+}
+
+template <typename T>
+__device__ __forceinline__ bool jacobi_rotation(T al, T be, T ga, T &c, T &s)
+{
+    T t;
+    if (!jacobi_tangent(al, be, ga, t)) return false;
+    const float tf = (float)t;
+    const T h = T(-0.5) * fma(t, t, T(1));
+    T cc = (T)rsqrtf(fmaf(tf, tf, 1.f));
+    cc = cc * fma(h, cc * cc, T(1.5));
+    cc = cc * fma(h, cc * cc, T(1.5));
+    c = cc;
+    s = cc * t;
+    return true;
+}
+
+// d^(-1/2) for d > 0 by Newton's iteration y <- y (3 - d y^2) / 2 from the
+// FP32 estimate: d = m 2^e with e even and m in [1, 4), two steps take the
+// estimate's 2^-23 to T's precision.  (Subnormal d: the library square root.)
+__device__ __forceinline__ double rsqrt_pos(double d)
+{
+    if (d < 1e-300) return 1.0 / sqrt(d);
+    int e = exponent_of(d);
+    e -= e & 1;
+    const double m = d * pow2<double>(-e);
+    double y = (double)rsqrtf((float)m);
+    const double h = -0.5 * m;
+    y = y * fma(h, y * y, 1.5);
+    y = y * fma(h, y * y, 1.5);
+    return y * pow2<double>(-e / 2);
+}
+__device__ __forceinline__ float rsqrt_pos(float d)
+{
+    if (d < 1e-36f) return 1.f / sqrtf(d);
+    const float y = rsqrtf(d);
+    return y * fmaf(-0.5f * d, y * y, 1.5f);
+}
+
+// One problem of lr_svd as the kernel reads it: the public descriptor and,
+// for the hierarchical Cholesky's A22 - R12'R12 updates, an optional full
+// middle block for part 2: M = diag(s1 ; sign2 * M2) with M2 a2 x a2 (ld
+// ldm2) in place of diag(s2) (then a1 == b1, a2 == b2 and both factors are
+// orthonormalised).  M2 = R12'R12 lets that update skip the separate
+// truncated SVD of R12'R12: its truncation would drop only singular values
+// below q eps(sigma_1), and the update's own SVD truncates the sum.
+struct LrJob {
+    hm_lr_problem p;
+    const void *M2;
+    int64_t ldm2;
+};
+
 // Core storage of lr_svd: D (p x q core, ld p), then J (q x q right
 // rotations, before that the staging area of the Xm^T Ym product), sigma (q)
 // and the sort order (q ints).  In shared memory (D takes d_elems values)
 // when core_off < 0, else at ws + core_off for cores too large for it.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *probs, const int64_t *ws_off,
+__global__ void __launch_bounds__(kThreads) lr_svd_kernel(const LrJob *jobs, const int64_t *ws_off,
                                                           const int64_t *core_off, T *ws, int *ranks, int64_t d_elems)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const hm_lr_problem pr = probs[blockIdx.x];
+    const hm_lr_problem pr = jobs[blockIdx.x].p;
+    const T *M2 = static_cast<const T *>(jobs[blockIdx.x].M2);
+    const int64_t ldm2 = jobs[blockIdx.x].ldm2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int a = pr.a1 + pr.a2, b = pr.b1 + pr.b2;
     const int64_t m = pr.m, n = pr.n;
@@ -147,6 +245,7 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *p
     const bool tr = kb > ka;
     const int p = tr ? kb : ka, q = tr ? ka : kb;
     __shared__ int s_flag, s_rank;
+    __shared__ T s_scale, s_unscale;
     if (q == 0) {
         if (tid == 0) ranks[blockIdx.x] = 0;
         return;
@@ -209,6 +308,31 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *p
             const int i = e % a, j = e / a;
             D[didx(i, j)] *= s1[i] * s2[j];
         }
+    } else if (M2) {
+        // C = R_P diag(s1 ; sign2 M2) R_Q^T: first Tm = R_P M (ka x b) in J's area
+        const T *s1 = static_cast<const T *>(pr.s1);
+        const T sign2 = (T)pr.sign2;
+        T *Tm = J;
+        for (int e = tid; e < ka * b; e += kThreads) {
+            const int i = e % ka, l2 = e / ka;
+            T acc = 0;
+            if (l2 < pr.a1) {
+                if (l2 >= i) acc = WP[i + m * l2] * s1[l2];
+            } else {
+                for (int l = i > pr.a1 ? i : pr.a1; l < a; ++l)
+                    acc = fma(WP[i + m * l], M2[(l - pr.a1) + ldm2 * (l2 - pr.a1)], acc);
+                acc *= sign2;
+            }
+            Tm[e] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < ka * kb; e += kThreads) {
+            const int i = e % ka, j = e / ka;
+            T acc = 0;
+            for (int l2 = j; l2 < b; ++l2) acc = fma(Tm[i + ka * l2], WQ[j + n * l2], acc);
+            D[didx(i, j)] = acc;
+        }
+        __syncthreads();                                   // Tm is read before J is written
     } else {
         // C = L diag(sd) R^T with L = R_P (ka x a) or I, R = R_Q (kb x b) or I
         const T *s1 = static_cast<const T *>(pr.s1), *s2 = static_cast<const T *>(pr.s2);
@@ -234,42 +358,79 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *p
     for (int e = tid; e < q * q; e += kThreads) J[e] = (e % q == e / q) ? T(1) : T(0);
     __syncthreads();
 
-    // 3. one-sided Jacobi on the columns of D (p x q, q <= p)
-    const int qq = (q + 1) & ~1;
+    // 3. one-sided Jacobi on the columns of D (p x q, q <= p).  D is first
+    //    scaled by a power of two to max |D| in [0.5, 1) (exact; the singular
+    //    values are scaled back in step 4), so that the squared column norms
+    //    of the convergence test neither overflow nor underflow early.  A
+    //    group of G lanes takes one column pair (rows strided by G), so that
+    //    small cores keep every lane of a warp busy: on GB300 an FP64 warp
+    //    instruction costs the same issue time with 1 or 32 lanes active.
+    {
+        T mx = 0;
+        for (int64_t e = tid; e < (int64_t)p * q; e += kThreads) mx = fmax(mx, fabs(D[e]));
+#pragma unroll
+        for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __shared__ T s_red[kWarps];
+        if (lane == 0) s_red[warp] = mx;
+        __syncthreads();
+        if (tid == 0) {
+            T m = 0;
+            for (int w = 0; w < kWarps; ++w) m = fmax(m, s_red[w]);
+            int ex = 0;
+            if (m > T(0) && isfinite(m)) frexp(m, &ex);
+            s_scale = ldexp(T(1), -ex);
+            s_unscale = ldexp(T(1), ex);
+        }
+        __syncthreads();
+        const T sc = s_scale;
+        if (sc != T(1))
+            for (int64_t e = tid; e < (int64_t)p * q; e += kThreads) D[e] *= sc;
+        __syncthreads();
+    }
+    const int qq = (q + 1) & ~1, npairs = qq / 2;
+    const int G = p <= 32 ? 8 : (p <= 64 ? 16 : 32);
+    const int gpw = 32 / G, lg = lane & (G - 1), grp = lane / G;
+    const T eps2 = Lim<T>::eps * Lim<T>::eps;
     for (int sweep = 0; sweep < kJacobiSweeps; ++sweep) {
         if (tid == 0) s_flag = 0;
         __syncthreads();
         for (int round = 0; round < qq - 1; ++round) {
-            for (int pi = warp; pi < qq / 2; pi += kWarps) {
-                int i, j;
-                if (pi == 0) { i = round; j = qq - 1; }
-                else { i = (round + pi) % (qq - 1); j = (round - pi + qq - 1) % (qq - 1); }
-                if (i > j) { const int tmp = i; i = j; j = tmp; }
-                if (j >= q) continue;
-                T *di = D + (int64_t)p * i, *dj = D + (int64_t)p * j;
-                T al = 0, be = 0, ga = 0;
-                for (int r = lane; r < p; r += 32) {
-                    const T u = di[r], v = dj[r];
-                    al = fma(u, u, al); be = fma(v, v, be); ga = fma(u, v, ga);
+            for (int pb = warp * gpw; pb < npairs; pb += kWarps * gpw) {     // warp-uniform
+                const int pi = pb + grp;
+                int i = 0, j = q;
+                if (pi < npairs) {
+                    if (pi == 0) { i = round; j = qq - 1; }
+                    else { i = (round + pi) % (qq - 1); j = (round - pi + qq - 1) % (qq - 1); }
+                    if (i > j) { const int tmp = i; i = j; j = tmp; }
                 }
-                al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
-                if (al == T(0) || be == T(0) || !(fabs(ga) > Lim<T>::eps * sqrt(al) * sqrt(be))) continue;
-                const T zeta = (be - al) / (2 * ga);
-                const T az = fabs(zeta);
-                const T t = az > Lim<T>::big ? T(0.5) / zeta : copysign(T(1) / (az + sqrt(fma(zeta, zeta, T(1)))), zeta);
-                const T c = T(1) / sqrt(fma(t, t, T(1))), s = c * t;
-                for (int r = lane; r < p; r += 32) {
+                const bool live = j < q;
+                T *di = D + (int64_t)p * i, *dj = D + (int64_t)p * (live ? j : i);
+                T al = 0, be = 0, ga = 0;
+                if (live)
+                    for (int r = lg; r < p; r += G) {
+                        const T u = di[r], v = dj[r];
+                        al = fma(u, u, al); be = fma(v, v, be); ga = fma(u, v, ga);
+                    }
+                for (int o = G >> 1; o; o >>= 1) {              // within the aligned group of G lanes
+                    al += __shfl_xor_sync(0xffffffffu, al, o);
+                    be += __shfl_xor_sync(0xffffffffu, be, o);
+                    ga += __shfl_xor_sync(0xffffffffu, ga, o);
+                }
+                if (!live || al == T(0) || be == T(0) || !(ga * ga > eps2 * al * be)) continue;
+                T c, sn;
+                if (!jacobi_rotation(al, be, ga, c, sn)) continue;
+                for (int r = lg; r < p; r += G) {
                     const T u = di[r], v = dj[r];
-                    di[r] = c * u - s * v;
-                    dj[r] = s * u + c * v;
+                    di[r] = c * u - sn * v;
+                    dj[r] = sn * u + c * v;
                 }
                 T *ji = J + (int64_t)q * i, *jj = J + (int64_t)q * j;
-                for (int r = lane; r < q; r += 32) {
+                for (int r = lg; r < q; r += G) {
                     const T u = ji[r], v = jj[r];
-                    ji[r] = c * u - s * v;
-                    jj[r] = s * u + c * v;
+                    ji[r] = c * u - sn * v;
+                    jj[r] = sn * u + c * v;
                 }
-                if (lane == 0) s_flag = 1;
+                if (lg == 0) s_flag = 1;
             }
             __syncthreads();
         }
@@ -282,15 +443,18 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const hm_lr_problem *p
     T *sig = J + (int64_t)q * q;
     int *perm = reinterpret_cast<int *>(sig + q);
     for (int j = warp; j < q; j += kWarps) {
-        T *dj = D + (int64_t)p * j;
-        T ss = 0;
+        T *dj = D + (int64_t)p * j, *jj = J + (int64_t)q * j;
+        T ss = 0, sj = 0;
         for (int r = lane; r < p; r += 32) ss = fma(dj[r], dj[r], ss);
-        const T sv = sqrt(warp_sum(ss));
+        for (int r = lane; r < q; r += 32) sj = fma(jj[r], jj[r], sj);
+        const T sv = sqrt(warp_sum(ss)), nj = sqrt(warp_sum(sj));
         if (sv > T(0)) {
             const T inv = T(1) / sv;
             for (int r = lane; r < p; r += 32) dj[r] *= inv;
         }
-        if (lane == 0) sig[j] = sv;
+        const T invj = T(1) / nj;
+        for (int r = lane; r < q; r += 32) jj[r] *= invj;
+        if (lane == 0) sig[j] = sv * invj * s_unscale;
     }
     __syncthreads();
     for (int j = tid; j < q; j += kThreads) {
@@ -460,16 +624,18 @@ __global__ void __launch_bounds__(kThreads) potrf_batched(const hm_potrf_problem
     if (threadIdx.x == 0) s_fail = 0;
     __syncthreads();
     for (int64_t j = 0; j < n; ++j) {
-        if (threadIdx.x == 0) {
+        if (warp == 0) {                    // the pivot row, by one warp (FP64 issue time is scarce)
             const T d = S[j + ld * j];
-            if (!(d > T(0))) s_fail = (int)(j + 1);
-            else S[j + ld * j] = sqrt(d);
+            if (!(d > T(0))) {
+                if (lane == 0) s_fail = (int)(j + 1);
+            } else {
+                const T y = rsqrt_pos(d);
+                for (int64_t i = j + 1 + lane; i < n; i += 32) S[j + ld * i] *= y;
+                if (lane == 0) S[j + ld * j] = d * y;
+            }
         }
         __syncthreads();
         if (s_fail) break;
-        const T inv = T(1) / S[j + ld * j];
-        for (int64_t i = j + 1 + threadIdx.x; i < n; i += kThreads) S[j + ld * i] *= inv;
-        __syncthreads();
         for (int64_t l = j + 1 + warp; l < n; l += kWarps) {
             const T rl = S[j + ld * l];
             for (int64_t i = j + 1 + lane; i <= l; i += 32) S[i + ld * l] = fma(-S[j + ld * i], rl, S[i + ld * l]);
@@ -530,6 +696,199 @@ __device__ void trsm_t_warp(const T *R, int64_t ld, int64_t n, T *x)
     __syncwarp();
 }
 
+// (i, j), i <= j, of the p-th entry of an upper triangle in column order
+__device__ __forceinline__ void upper_pair(int p, int &i, int &j)
+{
+    int l = (int)((sqrtf(8.f * (float)p + 1.f) - 1.f) * 0.5f);
+    while (l * (l + 1) / 2 > p) --l;
+    while ((l + 1) * (l + 2) / 2 <= p) ++l;
+    j = l;
+    i = p - l * (l + 1) / 2;
+}
+
+// A dense diagonal leaf of the hierarchical Cholesky: R = chol(A) (the upper
+// triangle of A read) and W = R^{-1}, one CTA, both in shared memory.  The
+// factorisation is right-looking: one warp forms each pivot (Newton's
+// reciprocal square root) and scales its row, then the trailing triangle is
+// updated with its entries spread evenly over all threads (an FP64 warp
+// instruction costs the same with idle lanes).  W comes from Gauss-Jordan
+// elimination on [R | I] from the last row up: step k scales row k of W by
+// 1/R_kk and subtracts R_ik times it from the rows i < k, k (n - k)
+// independent FMAs per step and no dot-product chain.
+struct LeafChol {
+    int64_t n;
+    const void *A; int64_t lda;
+    void *R; int64_t ldr;
+    void *W; int64_t ldw;
+};
+template <typename T>
+__global__ void __launch_bounds__(kThreads) leaf_chol(const LeafChol *probs, int *info)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const LeafChol g = probs[blockIdx.x];
+    const int n = (int)g.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    T *S = reinterpret_cast<T *>(smem_raw);            // n x n, ld n
+    T *Wm = S + (int64_t)n * n;                        // n x n, ld n
+    T *rinv = Wm + (int64_t)n * n;                     // n
+    __shared__ int s_fail;
+    const T *A = static_cast<const T *>(g.A);
+    for (int e = tid; e < n * n; e += kThreads) {
+        const int i = e % n, j = e / n;
+        S[e] = i <= j ? A[i + g.lda * j] : T(0);
+        Wm[e] = i == j ? T(1) : T(0);
+    }
+    if (tid == 0) s_fail = 0;
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        if (warp == 0) {
+            const T d = S[j + n * j];
+            if (!(d > T(0))) {
+                if (lane == 0) s_fail = j + 1;
+            } else {
+                const T y = rsqrt_pos(d);
+                for (int l = j + 1 + lane; l < n; l += 32) S[j + n * l] *= y;
+                if (lane == 0) { S[j + n * j] = d * y; rinv[j] = y; }
+            }
+        }
+        __syncthreads();
+        if (s_fail) break;
+        const int m = n - j - 1, tj = m * (m + 1) / 2;
+        for (int p = tid; p < tj; p += kThreads) {
+            int i, l;
+            upper_pair(p, i, l);
+            i += j + 1;
+            l += j + 1;
+            S[i + n * l] = fma(-S[j + n * i], S[j + n * l], S[i + n * l]);
+        }
+        __syncthreads();
+    }
+    if (s_fail) {
+        if (tid == 0) info[blockIdx.x] = s_fail;
+        return;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        const T y = rinv[k];
+        for (int jj = k + tid; jj < n; jj += kThreads) Wm[k + n * jj] *= y;
+        __syncthreads();
+        const int cnt = k * (n - k);
+        for (int p = tid; p < cnt; p += kThreads) {
+            const int i = p % k, jj = k + p / k;
+            Wm[i + n * jj] = fma(-S[i + n * k], Wm[k + n * jj], Wm[i + n * jj]);
+        }
+        __syncthreads();
+    }
+    T *R = static_cast<T *>(g.R), *W = static_cast<T *>(g.W);
+    for (int e = tid; e < n * n; e += kThreads) {
+        const int i = e % n, j = e / n;
+        R[i + g.ldr * j] = S[e];
+        W[i + g.ldw * j] = Wm[e];
+    }
+    if (tid == 0) info[blockIdx.x] = 0;
+}
+
+// H = diag(s) X^T X diag(s) for a tall X (rows x r, r <= kGramMax) by
+// several CTAs: CTA c sums rows [c chunk, (c + 1) chunk) into its partial
+// Gram matrix (ws + c r^2; thread e owns entries e, e + 256, ...; 32 rows of X
+// staged in shared memory at a time); the last CTA to finish (a counter,
+// reset by it for the next launch) adds the partials in CTA order, so the
+// result does not depend on which CTA finishes last.
+constexpr int kGramMax = 64;
+template <typename T>
+__global__ void __launch_bounds__(kThreads) hchol_gram(const T *X, int64_t ldx, int64_t rows, int r, const T *s,
+                                                        T *ws, unsigned *counter, T *H, int64_t chunk)
+{
+    __shared__ T xs[kGramMax * 33];
+    __shared__ bool last;
+    const int tid = threadIdx.x, no = r * r;
+    constexpr int kPer = kGramMax * kGramMax / kThreads;
+    T acc[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) acc[u] = T(0);
+    const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = min(rows, r0 + chunk);
+    for (int64_t b = r0; b < r1; b += 32) {
+        const int nb = (int)(r1 - b < 32 ? r1 - b : 32);
+        __syncthreads();
+        for (int e = tid; e < 32 * r; e += kThreads) {
+            const int c = e >> 5, i = e & 31;
+            xs[c * 33 + i] = i < nb ? X[(b + i) + ldx * c] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int e = tid + kThreads * u;
+            if (e < no) {
+                const T *xi = xs + (e % r) * 33, *xj = xs + (e / r) * 33;
+                T a = acc[u];
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) a = fma(xi[k], xj[k], a);
+                acc[u] = a;
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+        const int e = tid + kThreads * u;
+        if (e < no) ws[(int64_t)blockIdx.x * no + e] = acc[u];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int e = tid; e < no; e += kThreads) {
+        T v = 0;
+        for (unsigned c = 0; c < gridDim.x; ++c) v += __ldcg(ws + (int64_t)c * no + e);
+        H[e] = s[e % r] * v * s[e / r];
+    }
+    if (tid == 0) *counter = 0u;
+}
+
+// Dense leaves of A22 - R12'R12: D_out = D_in - Vp H Vp^T on the upper
+// triangle (the part the leaf's Cholesky reads), one CTA per leaf, Vp (n x r)
+// and T = Vp H in shared memory.
+struct LeafUpd {
+    int64_t n;
+    const void *Vp; int64_t ldv;
+    const void *Din; int64_t ldi;
+    void *Dout; int64_t ldo;
+};
+constexpr int kLeafUpdMax = 256;
+template <typename T>
+__global__ void __launch_bounds__(kThreads) hchol_leaf_update(const LeafUpd *ups, const T *H, int r)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const LeafUpd u = ups[blockIdx.x];
+    const int n = (int)u.n, tid = threadIdx.x;
+    T *Vs = reinterpret_cast<T *>(smem_raw);       // n x r
+    T *Ts = Vs + (int64_t)n * r;                    // n x r
+    T *Hs = Ts + (int64_t)n * r;                    // r x r
+    const T *Vp = static_cast<const T *>(u.Vp);
+    for (int e = tid; e < n * r; e += kThreads) Vs[e] = Vp[(e % n) + u.ldv * (e / n)];
+    for (int e = tid; e < r * r; e += kThreads) Hs[e] = H[e];
+    __syncthreads();
+    for (int e = tid; e < n * r; e += kThreads) {
+        const int i = e % n, k = e / n;
+        T a = 0;
+        for (int m = 0; m < r; ++m) a = fma(Vs[i + n * m], Hs[m + r * k], a);
+        Ts[e] = a;
+    }
+    __syncthreads();
+    const T *Din = static_cast<const T *>(u.Din);
+    T *Dout = static_cast<T *>(u.Dout);
+    const int npair = n * (n + 1) / 2;
+    for (int e = tid; e < npair; e += kThreads) {
+        // (i, l), i <= l, of the e-th upper entry in column order
+        int l = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
+        while (l * (l + 1) / 2 > e) --l;
+        while ((l + 1) * (l + 2) / 2 <= e) ++l;
+        const int i = e - l * (l + 1) / 2;
+        T a = Din[i + u.ldi * l];
+        for (int k = 0; k < r; ++k) a = fma(-Ts[i + n * k], Vs[l + n * k], a);
+        Dout[i + u.ldo * l] = a;
+    }
+}
+
 // W = R^{-1} for upper triangular n x n blocks, one CTA per block, R staged in
 // shared memory.  Column j of W is the back substitution R w = e_j, run by a
 // group of four lanes (partial sums over k = i+1+q, i+5+q, ... reduced by two
@@ -577,20 +936,22 @@ __global__ void __launch_bounds__(kThreads) trtri_batched(const hm_trtri_problem
 // low-rank block one warp each, then the rows of x2 over all threads).
 // Global writes of x are made visible to the CTA by the barrier after each op.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *ops, int nops, T *B, int64_t ldb)
+__global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *ops, int nops, T *B, int64_t ldb,
+                                                           int64_t base)
 {
     __shared__ T tk[kTkChunk];
     __shared__ T xs[kInvMax];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    T *x = B + ldb * (int64_t)blockIdx.x;
+    T *const xb = B + ldb * (int64_t)blockIdx.x;
+    auto xat = [&](int64_t o) { return xb + (o - base); };    // row o of the schedule is row o - base of B
     for (int o = 0; o < nops; ++o) {
         const hm_solve_op op = ops[o];
         const T *A = static_cast<const T *>(op.A);
         if (op.kind == HM_SOLVE_TRSM) {
-            if (warp == 0) trsm_t_warp(A, op.ld, op.n1, x + op.o1);
+            if (warp == 0) trsm_t_warp(A, op.ld, op.n1, xat(op.o1));
         } else if (op.kind == HM_SOLVE_INV) {
             // x1 <- W^T x1, W = R^{-1} upper: four lanes per output, all warps
-            T *x1 = x + op.o1;
+            T *x1 = xat(op.o1);
             for (int64_t i = tid; i < op.n1; i += kThreads) xs[i] = x1[i];
             __syncthreads();
             const int q = lane & 3;
@@ -607,8 +968,8 @@ __global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *op
             }
         } else if (op.kind == HM_SOLVE_LR) {
             const T *s = static_cast<const T *>(op.s), *V = static_cast<const T *>(op.B);
-            const T *x1 = x + op.o1;
-            T *x2 = x + op.o2;
+            const T *x1 = xat(op.o1);
+            T *x2 = xat(op.o2);
             for (int k0 = 0; k0 < op.r; k0 += kTkChunk) {
                 const int kn = op.r - k0 < kTkChunk ? op.r - k0 : kTkChunk;
                 for (int k = warp; k < kn; k += kWarps) {
@@ -627,13 +988,13 @@ __global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *op
                 __syncthreads();
             }
         } else {
-            const T *x1 = x + op.o1;
+            const T *x1 = xat(op.o1);
             for (int64_t j = warp; j < op.n2; j += kWarps) {
                 const T *col = A + op.ld * j;
                 T part = 0;
                 for (int64_t i = lane; i < op.n1; i += 32) part = fma(col[i], x1[i], part);
                 part = warp_sum(part);
-                if (lane == 0) x[op.o2 + j] -= part;
+                if (lane == 0) xat(op.o2)[j] -= part;
             }
         }
         __syncthreads();
@@ -671,7 +1032,7 @@ struct Staged {
     int put(const T *host, size_t count, T **dev)
     {
         void *p = nullptr;
-        ALG_CK(device_malloc_async(&p, std::max<size_t>(count, 1) * sizeof(T), st));
+        ALG_CK(device_malloc_pooled(&p, std::max<size_t>(count, 1) * sizeof(T), st));
         ptrs.push_back(p);
         if (count) ALG_CK(cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, st));
         *dev = static_cast<T *>(p);
@@ -681,7 +1042,7 @@ struct Staged {
     int zeros(size_t count, T **dev)
     {
         void *p = nullptr;
-        ALG_CK(device_malloc_async(&p, std::max<size_t>(count, 1) * sizeof(T), st));
+        ALG_CK(device_malloc_pooled(&p, std::max<size_t>(count, 1) * sizeof(T), st));
         ptrs.push_back(p);
         *dev = static_cast<T *>(p);
         return HM_OK;
@@ -700,27 +1061,40 @@ int set_smem(K kernel, size_t bytes)
 // Cores whose storage exceeds this many bytes run from the global workspace.
 constexpr size_t kCoreSmemBytes = 200 * 1024;
 
+// Workspace layout and shared memory of one lr_svd launch.
+struct LrPlan {
+    std::vector<int64_t> off, coff;
+    int64_t ws = 0, dmax = 1;
+    size_t smem = 0;
+};
+
 template <typename T>
-int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream_t st)
+int lr_svd_plan(int nprob, const LrJob *jobs, LrPlan &pl)
 {
-    std::vector<int64_t> off(nprob), coff(nprob, -1);
+    pl.off.assign(nprob, 0);
+    pl.coff.assign(nprob, -1);
     int64_t ws = 0, dmax = 1, jmax = 1;
     int qmax = 1;
     for (int i = 0; i < nprob; ++i) {
-        const hm_lr_problem &p = probs[i];
+        const hm_lr_problem &p = jobs[i].p;
+        const bool full2 = jobs[i].M2 != nullptr;
         const int a = p.a1 + p.a2, b = p.b1 + p.b2;
         if (p.m < 0 || p.n < 0 || p.a1 < 0 || p.a2 < 0 || p.b1 < 0 || p.b2 < 0) {
             set_last_error("problem %d: negative size", i);
             return HM_ERR_INVALID_ARG;
         }
         if (p.Xm) {
-            if (p.a2 || p.b2 || p.qr_left || p.qr_right || p.t < 0 || (p.t > 0 && !p.Ym) || (p.a1 && !p.s1) ||
+            if (full2 || p.a2 || p.b2 || p.qr_left || p.qr_right || p.t < 0 || (p.t > 0 && !p.Ym) || (p.a1 && !p.s1) ||
                 (p.b1 && !p.s2)) {
                 set_last_error("problem %d: the Xm^T Ym core takes one part per side, no QR", i);
                 return HM_ERR_INVALID_ARG;
             }
-        } else if (a != b || (p.a1 && !p.s1) || (p.a2 && !p.s2)) {
+        } else if (a != b || (p.a1 && !p.s1) || (p.a2 && !p.s2 && !full2)) {
             set_last_error("problem %d: a diagonal middle needs a1 + a2 == b1 + b2 and its values", i);
+            return HM_ERR_INVALID_ARG;
+        }
+        if (full2 && (p.a1 != p.b1 || !p.qr_left || !p.qr_right || jobs[i].ldm2 < p.a2)) {
+            set_last_error("problem %d: a full middle block needs a1 == b1, both QRs and ldm2 >= a2", i);
             return HM_ERR_INVALID_ARG;
         }
         if (!p.Q1 && p.b1 && (p.n != p.b1 || p.b2 || p.qr_right)) {
@@ -739,36 +1113,47 @@ int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream
         }
         const int64_t q = std::min(ka, kb), pp = std::max(ka, kb);
         if (q > 0 && (!p.U || !p.s || !p.V)) { set_last_error("problem %d: NULL output", i); return HM_ERR_INVALID_ARG; }
-        off[i] = ws;
+        pl.off[i] = ws;
         ws += (p.qr_left ? p.m * a : 0) + (p.qr_right ? p.n * b : 0) + a + b;
         ws = (ws + 31) / 32 * 32;
-        const int64_t jn = std::max(q * q, p.Xm ? (int64_t)32 * (a + b) : 0);
+        const int64_t jn = std::max({q * q, p.Xm ? (int64_t)32 * (a + b) : 0, full2 ? ka * b : 0});
         const size_t need = (size_t)(pp * q + jn + q) * sizeof(T) + (size_t)q * sizeof(int) + 64;
         if (need <= kCoreSmemBytes) {
             dmax = std::max(dmax, pp * q);
             jmax = std::max(jmax, jn);
             qmax = std::max<int>(qmax, (int)q);
         } else {
-            coff[i] = ws;
+            pl.coff[i] = ws;
             ws += pp * q + jn + 2 * q;          // sigma (q values) and the order (q ints) after J
             ws = (ws + 31) / 32 * 32;
         }
     }
-    if (nprob == 0) return HM_OK;
+    pl.ws = std::max<int64_t>(ws, 1);
+    pl.dmax = dmax;
     // J also holds sigma (q values) and the sort order (q ints) after it
-    const size_t smem = (size_t)(dmax + jmax + qmax) * sizeof(T) + (size_t)qmax * sizeof(int) + 64;
-    ALG_TRY(set_smem(lr_svd_kernel<T>, smem));
+    pl.smem = (size_t)(dmax + jmax + qmax) * sizeof(T) + (size_t)qmax * sizeof(int) + 64;
+    return set_smem(lr_svd_kernel<T>, pl.smem);
+}
+
+template <typename T>
+int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream_t st)
+{
+    std::vector<LrJob> jobs(nprob);
+    for (int i = 0; i < nprob; ++i) jobs[i] = LrJob{probs[i], nullptr, 0};
+    LrPlan pl;
+    ALG_TRY(lr_svd_plan<T>(nprob, jobs.data(), pl));
+    if (nprob == 0) return HM_OK;
     Staged S(st);
-    hm_lr_problem *d_probs = nullptr;
+    LrJob *d_jobs = nullptr;
     int64_t *d_off = nullptr, *d_coff = nullptr;
     T *d_ws = nullptr;
     int *d_ranks = nullptr;
-    ALG_TRY(S.put(probs, (size_t)nprob, &d_probs));
-    ALG_TRY(S.put(off.data(), off.size(), &d_off));
-    ALG_TRY(S.put(coff.data(), coff.size(), &d_coff));
-    ALG_TRY(S.zeros((size_t)std::max<int64_t>(ws, 1), &d_ws));
+    ALG_TRY(S.put(jobs.data(), (size_t)nprob, &d_jobs));
+    ALG_TRY(S.put(pl.off.data(), pl.off.size(), &d_off));
+    ALG_TRY(S.put(pl.coff.data(), pl.coff.size(), &d_coff));
+    ALG_TRY(S.zeros((size_t)pl.ws, &d_ws));
     ALG_TRY(S.zeros((size_t)nprob, &d_ranks));
-    lr_svd_kernel<T><<<nprob, kThreads, smem, st>>>(d_probs, d_off, d_coff, d_ws, d_ranks, dmax);
+    lr_svd_kernel<T><<<nprob, kThreads, pl.smem, st>>>(d_jobs, d_off, d_coff, d_ws, d_ranks, pl.dmax);
     ALG_CK(cudaGetLastError());
     std::vector<int> hr(nprob);
     ALG_CK(cudaMemcpyAsync(hr.data(), d_ranks, nprob * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -777,8 +1162,8 @@ int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream
     return HM_OK;
 }
 
-template <typename T>
-int gemm_run(int nprob, const hm_gemm_problem *probs, cudaStream_t st)
+template <typename T, typename Stage>
+int gemm_launch(int nprob, const hm_gemm_problem *probs, cudaStream_t st, Stage &S)
 {
     std::vector<int64_t> tile0(nprob + 1, 0);
     for (int i = 0; i < nprob; ++i) {
@@ -790,7 +1175,6 @@ int gemm_run(int nprob, const hm_gemm_problem *probs, cudaStream_t st)
     const int64_t tiles = tile0[nprob];
     if (tiles == 0) return HM_OK;
     if (tiles > INT32_MAX) { set_last_error("too many output tiles"); return HM_ERR_UNSUPPORTED; }
-    Staged S(st);
     hm_gemm_problem *d_probs = nullptr;
     int64_t *d_tile0 = nullptr;
     ALG_TRY(S.put(probs, (size_t)nprob, &d_probs));
@@ -801,7 +1185,14 @@ int gemm_run(int nprob, const hm_gemm_problem *probs, cudaStream_t st)
 }
 
 template <typename T>
-int axpby_run(int nprob, const hm_axpby_problem *probs, cudaStream_t st)
+int gemm_run(int nprob, const hm_gemm_problem *probs, cudaStream_t st)
+{
+    Staged S(st);
+    return gemm_launch<T>(nprob, probs, st, S);
+}
+
+template <typename T, typename Stage>
+int axpby_launch(int nprob, const hm_axpby_problem *probs, cudaStream_t st, Stage &S)
 {
     int64_t most = 0;
     for (int i = 0; i < nprob; ++i) {
@@ -815,13 +1206,28 @@ int axpby_run(int nprob, const hm_axpby_problem *probs, cudaStream_t st)
     }
     if (nprob == 0 || most == 0) return HM_OK;
     if (nprob > 65535) { set_last_error("more than 65535 problems"); return HM_ERR_UNSUPPORTED; }
-    Staged S(st);
     hm_axpby_problem *d_probs = nullptr;
     ALG_TRY(S.put(probs, (size_t)nprob, &d_probs));
     const unsigned bx = (unsigned)std::min<int64_t>((most + 255) / 256, 1024);
     axpby_batched<T><<<dim3(bx, nprob), 256, 0, st>>>(d_probs);
     ALG_CK(cudaGetLastError());
     return HM_OK;
+}
+
+template <typename T>
+int axpby_run(int nprob, const hm_axpby_problem *probs, cudaStream_t st)
+{
+    Staged S(st);
+    return axpby_launch<T>(nprob, probs, st, S);
+}
+
+template <typename T>
+int64_t potrf_nsmem(int64_t nmax)
+{
+    // blocks up to nsmem rows are factored in shared memory (<= 200 KB)
+    int64_t nsmem = 0;
+    while ((nsmem + 1) * (nsmem + 1) * (int64_t)sizeof(T) <= 200 * 1024) ++nsmem;
+    return std::min(nsmem, nmax);
 }
 
 template <typename T>
@@ -879,8 +1285,8 @@ int64_t trtri_max()
     return n;
 }
 
-template <typename T>
-int trtri_run(int nprob, const hm_trtri_problem *probs, cudaStream_t st)
+template <typename T, typename Stage>
+int trtri_launch(int nprob, const hm_trtri_problem *probs, cudaStream_t st, Stage &S)
 {
     int64_t nmax = 0;
     for (int i = 0; i < nprob; ++i) {
@@ -898,12 +1304,18 @@ int trtri_run(int nprob, const hm_trtri_problem *probs, cudaStream_t st)
     if (nprob == 0 || nmax == 0) return HM_OK;
     const size_t smem = (size_t)(2 * (nmax + 1) * nmax + nmax) * sizeof(T);
     ALG_TRY(set_smem(trtri_batched<T>, smem));
-    Staged S(st);
     hm_trtri_problem *d_probs = nullptr;
     ALG_TRY(S.put(probs, (size_t)nprob, &d_probs));
     trtri_batched<T><<<nprob, kThreads, smem, st>>>(d_probs, nmax);
     ALG_CK(cudaGetLastError());
     return HM_OK;
+}
+
+template <typename T>
+int trtri_run(int nprob, const hm_trtri_problem *probs, cudaStream_t st)
+{
+    Staged S(st);
+    return trtri_launch<T>(nprob, probs, st, S);
 }
 
 template <typename T>
@@ -930,8 +1342,528 @@ int solve_run(int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t nc
     hm_solve_op *d_ops = nullptr;
     ALG_TRY(S.put(ops, (size_t)nops, &d_ops));
     if (ncols > 0x7fffffff) { set_last_error("too many right-hand sides"); return HM_ERR_INVALID_ARG; }
-    solve_schedule<T><<<(unsigned)ncols, kThreads, 0, st>>>(d_ops, nops, static_cast<T *>(B), ldb);
+    solve_schedule<T><<<(unsigned)ncols, kThreads, 0, st>>>(d_ops, nops, static_cast<T *>(B), ldb, 0);
     ALG_CK(cudaGetLastError());
+    return HM_OK;
+}
+
+
+// ---- hierarchical Cholesky driver (hm_hchol_factor) --------------------------
+//
+// src/cholesky.jl:12-92 on a HODLR tree (2 x 2 blocks; upper off-diagonal
+// blocks LowRankMatrix, diagonal blocks hierarchical or dense), the
+// reference's recursion and block order run on the host in C++:
+//   R11 = chol(A11);  R12 = R11^{-T} A12 (the U factor solved);
+//   A22 <- A22 - R12'R12;  R22 = chol(A22).
+// Every block of A22 is updated when its ancestor is reached, as the
+// reference does: a dense leaf D <- D - V_p H V_p^T (two batched GEMMs) and a
+// LowRankMatrix block by one truncated SVD of [U_b | V_p] diag(s_b ; -H)
+// [V_b | V_q]^T (all blocks of A22 in one launch), where R12 = X diag(s) V^T
+// and H = diag(s) X^T X diag(s), so R12'R12 = V H V^T.  The reference forms
+// R12'R12 as a truncated SVD first; passing H whole skips that SVD (it would
+// drop only singular values below q eps(sigma_1)) and the update's SVD
+// truncates the sum.  R12 = R11^{-T} U runs through the left subtree's
+// forward-substitution schedule (its leaves as products with their inverses).
+// The host waits once per node whose A22 holds LowRankMatrix blocks (their
+// new ranks size the next problems); everything else is queued on the stream.
+// Problem descriptors go to the device from pinned host memory.
+
+// Device memory handed out in 256-byte aligned pieces from chunks of at
+// least 32 MB, all released together.
+struct Arena {
+    std::vector<void *> chunks;
+    char *cur = nullptr;
+    size_t left = 0;
+    Arena() = default;
+    Arena(const Arena &) = delete;
+    Arena &operator=(const Arena &) = delete;
+    ~Arena() { release(); }
+    void release()
+    {
+        for (void *c : chunks) cudaFree(c);
+        chunks.clear();
+        cur = nullptr;
+        left = 0;
+    }
+    template <typename T>
+    int get(size_t count, T **p)
+    {
+        const size_t bytes = (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~size_t(255);
+        if (bytes > left) {
+            const size_t sz = std::max<size_t>(bytes, size_t(32) << 20);
+            void *c = nullptr;
+            ALG_CK(device_malloc(&c, sz));
+            chunks.push_back(c);
+            cur = static_cast<char *>(c);
+            left = sz;
+        }
+        *p = reinterpret_cast<T *>(cur);
+        cur += bytes;
+        left -= bytes;
+        return HM_OK;
+    }
+};
+
+// Descriptor staging through pinned host memory (asynchronous copies) and a
+// device scratch area, both reused from the start once the caller has
+// synchronised the stream (drained()); a full buffer is replaced by a larger
+// one and kept until the end, so pointers handed out stay valid.
+struct PinnedStager {
+    cudaStream_t st;
+    std::vector<char *> old_host, old_dev;
+    char *host = nullptr, *dev = nullptr, *scratch = nullptr;
+    size_t cap = 0, used = 0, scap = 0, sused = 0;
+    explicit PinnedStager(cudaStream_t s) : st(s) {}
+    PinnedStager(const PinnedStager &) = delete;
+    PinnedStager &operator=(const PinnedStager &) = delete;
+    ~PinnedStager()
+    {
+        for (char *h : old_host) cudaFreeHost(h);
+        for (char *d : old_dev) cudaFree(d);
+        if (host) cudaFreeHost(host);
+        if (dev) cudaFree(dev);
+        if (scratch) cudaFree(scratch);
+    }
+    void drained() { used = sused = 0; }
+    template <typename T>
+    int put(const T *src, size_t count, T **d)
+    {
+        const size_t bytes = count * sizeof(T), al = (std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+        if (used + al > cap) {
+            const size_t nc = std::max(al, std::max<size_t>(2 * cap, size_t(1) << 20));
+            char *h = nullptr, *dv = nullptr;
+            ALG_CK(cudaMallocHost((void **)&h, nc));
+            const int st_ = cuda_fail(device_malloc((void **)&dv, nc), "device_malloc");
+            if (st_) { cudaFreeHost(h); return st_; }
+            if (host) { old_host.push_back(host); old_dev.push_back(dev); }
+            host = h; dev = dv; cap = nc; used = 0;
+        }
+        if (bytes) {
+            std::memcpy(host + used, src, bytes);
+            ALG_CK(cudaMemcpyAsync(dev + used, host + used, bytes, cudaMemcpyHostToDevice, st));
+        }
+        *d = reinterpret_cast<T *>(dev + used);
+        used += al;
+        return HM_OK;
+    }
+    template <typename T>
+    int zeros(size_t count, T **d)
+    {
+        const size_t al = (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~size_t(255);
+        if (sused + al > scap) {
+            const size_t nc = std::max(al, std::max<size_t>(2 * scap, size_t(32) << 20));
+            char *dv = nullptr;
+            ALG_CK(device_malloc((void **)&dv, nc));
+            if (scratch) old_dev.push_back(scratch);
+            scratch = dv; scap = nc; sused = 0;
+        }
+        *d = reinterpret_cast<T *>(scratch + sused);
+        sused += al;
+        return HM_OK;
+    }
+};
+
+// What hm_hchol_factor hands back: R's pieces, in memory owned here.
+struct HCholResult {
+    Arena keep;
+    std::vector<hm_hchol_out> out;
+};
+
+template <typename T>
+struct HChol {
+    struct Node {
+        int64_t off = 0;
+        int inord = -1, leaf = -1, ob = 0, oe = 0;      // in-order position, leaf number, subtree's op range
+        const T *U = nullptr, *s = nullptr, *V = nullptr;   // the current A12 (internal nodes)
+        int64_t ldu = 1, ldv = 1;
+        int r = 0;
+        const T *D = nullptr;                            // the current block (leaves)
+        int64_t ldd = 1;
+    };
+    const hm_hchol_node *in;
+    int nn;
+    cudaStream_t st;
+    HCholResult *res;
+    std::vector<Node> nd;
+    std::vector<int> inorder;
+    Arena temp;
+    PinnedStager S;
+    hm_solve_op *h_ops = nullptr, *d_ops = nullptr;
+    int32_t *h_small = nullptr, *d_info = nullptr;       // h_small: pinned, ranks and pivot words read back
+    unsigned *counter = nullptr;                         // hchol_gram's last-CTA counter
+    int64_t h_small_n = 0;
+    int nleaves = 0;
+
+    HChol(const hm_hchol_node *nodes, int n, cudaStream_t s, HCholResult *r) : in(nodes), nn(n), st(s), res(r), S(s) {}
+    ~HChol()
+    {
+        if (h_ops) cudaFreeHost(h_ops);
+        if (h_small) cudaFreeHost(h_small);
+    }
+
+    static bool is_leaf(const hm_hchol_node &g) { return g.left < 0 && g.right < 0; }
+
+    // offsets, in-order numbering and the checks of the tree (iterative: trees may be deep)
+    int layout(int root)
+    {
+        if (root < 0 || root >= nn) { set_last_error("root %d out of range", root); return HM_ERR_INVALID_ARG; }
+        nd.assign(nn, Node());
+        std::vector<char> seen(nn, 0);
+        struct Frame { int i, stage; };
+        std::vector<Frame> stack{{root, 0}};
+        seen[root] = 1;
+        nd[root].off = 0;
+        while (!stack.empty()) {
+            Frame &f = stack.back();
+            const hm_hchol_node &g = in[f.i];
+            Node &N = nd[f.i];
+            if (f.stage == 0) {
+                N.ob = (int)inorder.size();
+                if (g.n < 1) { set_last_error("node %d: %lld rows", f.i, (long long)g.n); return HM_ERR_INVALID_ARG; }
+                if (is_leaf(g)) {
+                    if (!g.D || g.ldd < g.n) { set_last_error("leaf %d: no block or ld < n", f.i); return HM_ERR_INVALID_ARG; }
+                    N.D = static_cast<const T *>(g.D);
+                    N.ldd = g.ldd;
+                    N.inord = (int)inorder.size();
+                    N.leaf = nleaves++;
+                    inorder.push_back(f.i);
+                    N.oe = (int)inorder.size();
+                    stack.pop_back();
+                    continue;
+                }
+                const int64_t n1 = g.n1, n2 = g.n - g.n1;
+                if (g.left < 0 || g.right < 0 || g.left >= nn || g.right >= nn || g.left == g.right || seen[g.left] ||
+                    seen[g.right] || n1 < 1 || n2 < 1 || in[g.left].n != n1 || in[g.right].n != n2) {
+                    set_last_error("node %d: children or sizes inconsistent", f.i);
+                    return HM_ERR_INVALID_ARG;
+                }
+                if (g.r < 0 || (g.r > 0 && (!g.U || !g.s || !g.V || g.ldu < n1 || g.ldv < n2))) {
+                    set_last_error("node %d: bad LowRankMatrix block", f.i);
+                    return HM_ERR_INVALID_ARG;
+                }
+                N.U = static_cast<const T *>(g.U);
+                N.s = static_cast<const T *>(g.s);
+                N.V = static_cast<const T *>(g.V);
+                N.ldu = std::max<int64_t>(g.ldu, 1);
+                N.ldv = std::max<int64_t>(g.ldv, 1);
+                N.r = g.r;
+                seen[g.left] = seen[g.right] = 1;
+                nd[g.left].off = N.off;
+                nd[g.right].off = N.off + n1;
+                f.stage = 1;
+                stack.push_back({g.left, 0});
+            } else if (f.stage == 1) {
+                N.inord = (int)inorder.size();
+                inorder.push_back(f.i);
+                f.stage = 2;
+                stack.push_back({g.right, 0});
+            } else {
+                N.oe = (int)inorder.size();
+                stack.pop_back();
+            }
+        }
+        return HM_OK;
+    }
+
+    int small_host(int64_t n)
+    {
+        if (n <= h_small_n) return HM_OK;
+        if (h_small) cudaFreeHost(h_small);
+        h_small = nullptr;
+        h_small_n = 0;
+        ALG_CK(cudaMallocHost((void **)&h_small, sizeof(int32_t) * n));
+        h_small_n = n;
+        return HM_OK;
+    }
+
+    int setup(int root)
+    {
+        ALG_TRY(layout(root));
+        res->out.assign(nn, hm_hchol_out{});
+        const int64_t tmax = trtri_max<T>();
+        ALG_CK(cudaMallocHost((void **)&h_ops, sizeof(hm_solve_op) * inorder.size()));
+        ALG_TRY(temp.get(inorder.size(), &d_ops));
+        ALG_TRY(temp.get((size_t)nleaves, &d_info));
+        ALG_TRY(temp.get(1, &counter));
+        ALG_CK(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+        ALG_TRY(small_host(std::max(nleaves, 64)));
+        const void *any = nullptr;
+        for (int i : inorder) {
+            const hm_hchol_node &g = in[i];
+            hm_solve_op &op = h_ops[nd[i].inord];
+            op = hm_solve_op{};
+            op.o1 = nd[i].off;
+            op.n1 = is_leaf(g) ? g.n : g.n1;
+            if (is_leaf(g)) {
+                T *R = nullptr, *W = nullptr;
+                ALG_TRY(res->keep.get((size_t)(g.n * g.n), &R));
+                hm_hchol_out &o = res->out[i];
+                o.R = R;
+                o.ldr = g.n;
+                op.A = R;
+                op.ld = g.n;
+                op.kind = HM_SOLVE_TRSM;
+                if (g.n <= tmax && g.n <= kInvMax) {  // factored with its inverse by leaf_chol
+                    ALG_TRY(res->keep.get((size_t)(g.n * g.n), &W));
+                    o.W = W;
+                    o.ldw = g.n;
+                    op.A = W;
+                    op.kind = HM_SOLVE_INV;
+                }
+                any = R;
+            } else {
+                op.kind = HM_SOLVE_LR;                 // rank 0 until the node is reached
+                op.o2 = nd[i].off + g.n1;
+                op.n2 = g.n - g.n1;
+                op.ld = std::max<int64_t>(g.n1, 1);
+                op.ld2 = std::max<int64_t>(op.n2, 1);
+            }
+        }
+        for (int i : inorder)
+            if (!h_ops[nd[i].inord].A) h_ops[nd[i].inord].A = any;
+        ALG_CK(cudaMemcpyAsync(d_ops, h_ops, sizeof(hm_solve_op) * inorder.size(), cudaMemcpyHostToDevice, st));
+        return HM_OK;
+    }
+
+    int leaf(int i)
+    {
+        const hm_hchol_node &g = in[i];
+        Node &N = nd[i];
+        hm_hchol_out &o = res->out[i];
+        if (o.W) {
+            const LeafChol lc{g.n, N.D, N.ldd, o.R, o.ldr, o.W, o.ldw};
+            const size_t smem = (size_t)(2 * g.n * g.n + g.n) * sizeof(T);
+            ALG_TRY(set_smem(leaf_chol<T>, smem));
+            LeafChol *dl = nullptr;
+            ALG_TRY(S.put(&lc, 1, &dl));
+            leaf_chol<T><<<1, kThreads, smem, st>>>(dl, d_info + N.leaf);
+            ALG_CK(cudaGetLastError());
+            return HM_OK;
+        }
+        const hm_potrf_problem pp{g.n, N.D, N.ldd, o.R, o.ldr};
+        const int64_t nsmem = potrf_nsmem<T>(g.n);
+        const size_t smem = (size_t)nsmem * nsmem * sizeof(T);
+        ALG_TRY(set_smem(potrf_batched<T>, smem));
+        hm_potrf_problem *dp = nullptr;
+        ALG_TRY(S.put(&pp, 1, &dp));
+        potrf_batched<T><<<1, kThreads, smem, st>>>(dp, d_info + N.leaf, nsmem);
+        ALG_CK(cudaGetLastError());
+        return HM_OK;
+    }
+
+    // every node and leaf below node j (j itself included)
+    void subtree(int j, std::vector<int> &leaves, std::vector<int> &inner)
+    {
+        for (int k = nd[j].ob; k < nd[j].oe; ++k) {
+            const int i = inorder[k];
+            (is_leaf(in[i]) ? leaves : inner).push_back(i);
+        }
+    }
+
+    // A22 <- A22 - V H V^T over the right subtree of node i (X n1 x r, V n2 x r)
+    int update(int i, const T *X, const T *sk, const T *Vk, int r)
+    {
+        const hm_hchol_node &g = in[i];
+        const int64_t n1 = g.n1, n2 = g.n - g.n1, b0 = nd[g.right].off;
+        T *H = nullptr;
+        ALG_TRY(temp.get((size_t)r * r, &H));
+        if (r <= kGramMax) {
+            const int64_t nch = std::max<int64_t>(1, std::min<int64_t>((n1 + 255) / 256, 128));
+            const int64_t chunk = ((n1 + nch - 1) / nch + 31) / 32 * 32;
+            const int64_t nblk = (n1 + chunk - 1) / chunk;
+            T *ws = nullptr;
+            ALG_TRY(S.zeros((size_t)(nblk * r * r), &ws));
+            hchol_gram<T><<<(unsigned)nblk, kThreads, 0, st>>>(X, n1, n1, r, sk, ws, counter, H, chunk);
+            ALG_CK(cudaGetLastError());
+        } else {
+            T *G = nullptr;
+            ALG_TRY(temp.get((size_t)r * r, &G));
+            hm_gemm_problem gp{};
+            gp.m = r; gp.n = r; gp.k = n1;
+            gp.P = X; gp.ldp = n1; gp.transp = 1;
+            gp.Q = X; gp.ldq = n1; gp.transq = 1;
+            gp.alpha = 1.0; gp.beta = 0.0;
+            gp.D = G; gp.ldd = r;
+            ALG_TRY(gemm_launch<T>(1, &gp, st, S));
+            hm_axpby_problem ap{};
+            ap.m = r; ap.n = r; ap.A = G; ap.lda = r; ap.dr = sk; ap.dc = sk; ap.alpha = 1.0; ap.beta = 0.0;
+            ap.D = H; ap.ldd = r;
+            ALG_TRY(axpby_launch<T>(1, &ap, st, S));
+        }
+
+        std::vector<int> leaves, inner;
+        subtree(g.right, leaves, inner);
+        int64_t nlmax = 0;
+        for (int L : leaves) nlmax = std::max(nlmax, in[L].n);
+        const size_t lsmem = (size_t)(2 * nlmax * r + r * r) * sizeof(T);
+        if (!leaves.empty() && r <= kGramMax && nlmax <= kLeafUpdMax && lsmem <= kCoreSmemBytes) {
+            std::vector<LeafUpd> ups(leaves.size());
+            for (size_t k = 0; k < leaves.size(); ++k) {
+                const int L = leaves[k];
+                const int64_t nl = in[L].n;
+                T *Dn = nullptr;
+                ALG_TRY(temp.get((size_t)(nl * nl), &Dn));
+                ups[k] = LeafUpd{nl, Vk + (nd[L].off - b0), n2, nd[L].D, nd[L].ldd, Dn, nl};
+                nd[L].D = Dn;
+                nd[L].ldd = nl;
+            }
+            ALG_TRY(set_smem(hchol_leaf_update<T>, lsmem));
+            LeafUpd *du = nullptr;
+            ALG_TRY(S.put(ups.data(), ups.size(), &du));
+            hchol_leaf_update<T><<<(unsigned)ups.size(), kThreads, lsmem, st>>>(du, H, r);
+            ALG_CK(cudaGetLastError());
+        } else if (!leaves.empty()) {
+            std::vector<hm_gemm_problem> p1(leaves.size()), p2(leaves.size());
+            for (size_t k = 0; k < leaves.size(); ++k) {
+                const int L = leaves[k];
+                const int64_t nl = in[L].n;
+                const T *Vp = Vk + (nd[L].off - b0);
+                T *TL = nullptr, *Dn = nullptr;
+                ALG_TRY(temp.get((size_t)(nl * r), &TL));
+                ALG_TRY(temp.get((size_t)(nl * nl), &Dn));
+                hm_gemm_problem &a = p1[k];
+                a = hm_gemm_problem{};
+                a.m = nl; a.n = r; a.k = r;
+                a.P = Vp; a.ldp = n2; a.Q = H; a.ldq = r;
+                a.alpha = 1.0; a.beta = 0.0; a.D = TL; a.ldd = nl;
+                hm_gemm_problem &b = p2[k];
+                b = hm_gemm_problem{};
+                b.m = nl; b.n = nl; b.k = r;
+                b.P = TL; b.ldp = nl; b.Q = Vp; b.ldq = n2;
+                b.alpha = -1.0; b.beta = 1.0; b.C = nd[L].D; b.ldc = nd[L].ldd;
+                b.D = Dn; b.ldd = nl;
+                nd[L].D = Dn;
+                nd[L].ldd = nl;
+            }
+            ALG_TRY(gemm_launch<T>((int)p1.size(), p1.data(), st, S));
+            ALG_TRY(gemm_launch<T>((int)p2.size(), p2.data(), st, S));
+        }
+        if (inner.empty()) return HM_OK;
+        const int np = (int)inner.size();
+        std::vector<LrJob> jobs(np);
+        for (int k = 0; k < np; ++k) {
+            const int M = inner[k];
+            const hm_hchol_node &gm = in[M];
+            const int64_t m1 = gm.n1, m2 = gm.n - gm.n1;
+            const int rm = nd[M].r;
+            const int cap = (int)std::min<int64_t>(std::min(m1, m2), rm + r);
+            T *Un = nullptr, *sn = nullptr, *Vn = nullptr;
+            ALG_TRY(temp.get((size_t)(m1 * cap), &Un));
+            ALG_TRY(temp.get((size_t)cap, &sn));
+            ALG_TRY(temp.get((size_t)(m2 * cap), &Vn));
+            hm_lr_problem p{};
+            p.m = m1; p.n = m2;
+            p.a1 = rm; p.a2 = r; p.b1 = rm; p.b2 = r;
+            p.qr_left = 1; p.qr_right = 1;
+            p.P1 = rm ? nd[M].U : nullptr; p.ldp1 = nd[M].ldu;
+            p.P2 = Vk + (nd[M].off - b0); p.ldp2 = n2;
+            p.Q1 = rm ? nd[M].V : nullptr; p.ldq1 = nd[M].ldv;
+            p.Q2 = Vk + (nd[M].off + m1 - b0); p.ldq2 = n2;
+            p.s1 = rm ? nd[M].s : nullptr;
+            p.sign2 = -1.0;
+            p.U = Un; p.s = sn; p.V = Vn;
+            jobs[k] = LrJob{p, H, r};
+            nd[M].U = Un; nd[M].ldu = std::max<int64_t>(m1, 1);
+            nd[M].s = sn;
+            nd[M].V = Vn; nd[M].ldv = std::max<int64_t>(m2, 1);
+        }
+        LrPlan pl;
+        ALG_TRY(lr_svd_plan<T>(np, jobs.data(), pl));
+        LrJob *dj = nullptr;
+        int64_t *doff = nullptr, *dcoff = nullptr;
+        T *dws = nullptr;
+        int *dr = nullptr;
+        ALG_TRY(S.put(jobs.data(), (size_t)np, &dj));
+        ALG_TRY(S.put(pl.off.data(), pl.off.size(), &doff));
+        ALG_TRY(S.put(pl.coff.data(), pl.coff.size(), &dcoff));
+        ALG_TRY(S.zeros((size_t)pl.ws, &dws));
+        ALG_TRY(S.zeros((size_t)np, &dr));
+        lr_svd_kernel<T><<<np, kThreads, pl.smem, st>>>(dj, doff, dcoff, dws, dr, pl.dmax);
+        ALG_CK(cudaGetLastError());
+        ALG_TRY(small_host(np));
+        ALG_CK(cudaMemcpyAsync(h_small, dr, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, st));
+        ALG_CK(cudaStreamSynchronize(st));
+        S.drained();
+        for (int k = 0; k < np; ++k) nd[inner[k]].r = h_small[k];
+        return HM_OK;
+    }
+
+    int node(int i)
+    {
+        const hm_hchol_node &g = in[i];
+        if (is_leaf(g)) return leaf(i);
+        ALG_TRY(node(g.left));
+        Node &N = nd[i];
+        const int r = N.r;
+        const int64_t n1 = g.n1, n2 = g.n - g.n1;
+        T *X = nullptr, *sk = nullptr, *Vk = nullptr;
+        ALG_TRY(res->keep.get((size_t)(n1 * r), &X));
+        ALG_TRY(res->keep.get((size_t)r, &sk));
+        ALG_TRY(res->keep.get((size_t)(n2 * r), &Vk));
+        if (r > 0) {
+            ALG_CK(cudaMemcpy2DAsync(X, n1 * sizeof(T), N.U, N.ldu * sizeof(T), n1 * sizeof(T), r,
+                                     cudaMemcpyDeviceToDevice, st));
+            ALG_CK(cudaMemcpyAsync(sk, N.s, r * sizeof(T), cudaMemcpyDeviceToDevice, st));
+            ALG_CK(cudaMemcpy2DAsync(Vk, n2 * sizeof(T), N.V, N.ldv * sizeof(T), n2 * sizeof(T), r,
+                                     cudaMemcpyDeviceToDevice, st));
+            const Node &L = nd[g.left];
+            solve_schedule<T><<<(unsigned)r, kThreads, 0, st>>>(d_ops + L.ob, L.oe - L.ob, X, n1, L.off);
+            ALG_CK(cudaGetLastError());
+        }
+        hm_hchol_out &o = res->out[i];
+        o.r = r;
+        o.U = X; o.ldu = std::max<int64_t>(n1, 1);
+        o.s = sk;
+        o.V = Vk; o.ldv = std::max<int64_t>(n2, 1);
+        hm_solve_op &op = h_ops[N.inord];
+        op.r = r;
+        if (r > 0) {
+            op.A = X;
+            op.s = sk;
+            op.B = Vk;
+            ALG_CK(cudaMemcpyAsync(d_ops + N.inord, &op, sizeof(hm_solve_op), cudaMemcpyHostToDevice, st));
+            ALG_TRY(update(i, X, sk, Vk, r));
+        }
+        return node(g.right);
+    }
+
+    // returns HM_OK, or HM_ERR_NOT_POSDEF with (node, pivot) of the first
+    // failing leaf in the reference's order
+    int run(int root, int32_t *fail)
+    {
+        ALG_TRY(setup(root));
+        ALG_TRY(node(root));
+        ALG_CK(cudaMemcpyAsync(h_small, d_info, sizeof(int32_t) * nleaves, cudaMemcpyDeviceToHost, st));
+        ALG_CK(cudaStreamSynchronize(st));
+        S.drained();
+        for (int i : inorder) {
+            if (!is_leaf(in[i])) continue;
+            const int w = h_small[nd[i].leaf];
+            if (w) {
+                if (fail) { fail[0] = i; fail[1] = w; }
+                set_last_error("PosDefException: leaf %d is not positive definite (pivot %d)", i, w);
+                return HM_ERR_NOT_POSDEF;
+            }
+        }
+        return HM_OK;
+    }
+};
+
+template <typename T>
+int hchol_factor(int nnodes, const hm_hchol_node *nodes, int32_t root, void **ctx, int32_t *fail, cudaStream_t st)
+{
+    HCholResult *res = new HCholResult();
+    int rc;
+    {
+        HChol<T> h(nodes, nnodes, st, res);
+        rc = h.run(root, fail);
+        if (rc) cudaStreamSynchronize(st);       // nothing in flight reads memory freed below
+    }
+    if (rc) {
+        delete res;
+        return rc;
+    }
+    *ctx = res;
     return HM_OK;
 }
 
@@ -1006,6 +1938,39 @@ int hm_trtri_batched(int dtype, int nprob, const hm_trtri_problem *probs, void *
     if (dtype == HM_F32) return trtri_run<float>(nprob, probs, st);
     set_last_error("unknown dtype %d", dtype);
     return HM_ERR_UNSUPPORTED;
+}
+
+int hm_hchol_factor(int dtype, int nnodes, const hm_hchol_node *nodes, int32_t root, void **ctx, int32_t *fail,
+                    void *stream)
+{
+    clear_last_error();
+    if (!ctx || nnodes < 1 || !nodes) { set_last_error("bad node list"); return HM_ERR_INVALID_ARG; }
+    *ctx = nullptr;
+    if (fail) fail[0] = fail[1] = -1;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dtype == HM_F64) return hchol_factor<double>(nnodes, nodes, root, ctx, fail, st);
+    if (dtype == HM_F32) return hchol_factor<float>(nnodes, nodes, root, ctx, fail, st);
+    set_last_error("unknown dtype %d", dtype);
+    return HM_ERR_UNSUPPORTED;
+}
+
+int hm_hchol_result(void *ctx, int32_t node, hm_hchol_out *out)
+{
+    clear_last_error();
+    HCholResult *res = static_cast<HCholResult *>(ctx);
+    if (!res || !out || node < 0 || node >= (int32_t)res->out.size()) {
+        set_last_error("bad context or node");
+        return HM_ERR_INVALID_ARG;
+    }
+    *out = res->out[node];
+    return HM_OK;
+}
+
+int hm_hchol_free(void *ctx)
+{
+    clear_last_error();
+    delete static_cast<HCholResult *>(ctx);
+    return HM_OK;
 }
 
 int hm_solve_transposed(int dtype, int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t ncols, void *stream)

@@ -20,6 +20,9 @@ void clear_last_error();
 // device_malloc_async means the legacy default stream, as in CUDA.
 cudaError_t device_malloc(void **p, size_t bytes);
 cudaError_t device_malloc_async(void **p, size_t bytes, cudaStream_t stream);
+// From the library's own stream-ordered pool, which keeps freed memory for
+// reuse instead of returning it to the driver at synchronisations.
+cudaError_t device_malloc_pooled(void **p, size_t bytes, cudaStream_t stream);
 
 // ---------------------------------------------------------------- numerics
 

@@ -79,7 +79,8 @@ EXPORTED = (
     "hm_mul_host", "hm_mul_noalloc", "hm_debug_fail_alloc", "hm_direct_rows", "hm_configure", "hm_autotune", "hm_autotune_choice", "hm_profile", "hm_profile_read", "hm_profile_timeline", "hm_free", "hm_plan_create", "hm_plan_table", "hm_plan_sizes",
     "hm_plan_free", "hm_batch_plan_create", "hm_hier_build", "hm_dense_mul", "hm_lowrank_mul",
     "hm_bary_factors", "hm_lr_svd", "hm_gemm_batched", "hm_axpby_batched", "hm_potrf_batched",
-    "hm_solve_transposed", "hm_potrf_batched_async", "hm_trtri_batched",
+    "hm_solve_transposed", "hm_potrf_batched_async", "hm_trtri_batched", "hm_hchol_factor", "hm_hchol_result",
+    "hm_hchol_free",
 )
 
 _d = ctypes.POINTER(ctypes.c_double)
@@ -129,6 +130,18 @@ class SolveOp(ctypes.Structure):
     """hm_solve_op of include/hmgpu.h."""
     _fields_ = [("kind", _c32), ("r", _c32), ("o1", _c64), ("n1", _c64), ("o2", _c64), ("n2", _c64),
                 ("ld", _c64), ("ld2", _c64), ("A", _vp), ("s", _vp), ("B", _vp)]
+
+
+class HcholNode(ctypes.Structure):
+    """hm_hchol_node of include/hmgpu.h."""
+    _fields_ = [("n", _c64), ("n1", _c64), ("left", _c32), ("right", _c32), ("D", _vp), ("ldd", _c64),
+                ("U", _vp), ("ldu", _c64), ("s", _vp), ("V", _vp), ("ldv", _c64), ("r", _c32)]
+
+
+class HcholOut(ctypes.Structure):
+    """hm_hchol_out of include/hmgpu.h."""
+    _fields_ = [("r", _c32), ("U", _vp), ("ldu", _c64), ("s", _vp), ("V", _vp), ("ldv", _c64),
+                ("R", _vp), ("ldr", _c64), ("W", _vp), ("ldw", _c64)]
 
 
 class HMError(RuntimeError):
@@ -194,6 +207,13 @@ def _load():
     L.hm_trtri_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(TrtriProblem), _vp]
     L.hm_solve_transposed.restype = ctypes.c_int
     L.hm_solve_transposed.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(SolveOp), _vp, _i64, _i64, _vp]
+    L.hm_hchol_factor.restype = ctypes.c_int
+    L.hm_hchol_factor.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(HcholNode), ctypes.c_int32,
+                                  ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int32), _vp]
+    L.hm_hchol_result.restype = ctypes.c_int
+    L.hm_hchol_result.argtypes = [_vp, ctypes.c_int32, ctypes.POINTER(HcholOut)]
+    L.hm_hchol_free.restype = ctypes.c_int
+    L.hm_hchol_free.argtypes = [_vp]
     L.hm_size.restype = ctypes.c_int
     L.hm_size.argtypes = [_vp, _pi64, _pi64]
     L.hm_storage.restype = ctypes.c_int

@@ -608,16 +608,29 @@ def _check_2x2(A):
     return t
 
 
-def hierarchicalcholesky(A):
+def hierarchicalcholesky(A, native=True):
     """hierarchicalcholesky(A) (src/cholesky.jl:12-92): the upper factor R with
     R'R = A of a symmetric positive definite 2 x 2 hierarchical matrix (or a
     dense matrix), in the reference's block order:
     R11 = chol(A11); R12 = R11^{-T} A12; R22 = chol(A22 - R12'R12).
-    The dense diagonal leaves are factored without waiting; their pivot checks
-    are read once at the end, and the first failing leaf (in the reference's
-    order) raises the PosDefException the reference would raise."""
+    A HODLR tree (every upper off-diagonal block a LowRankMatrix, diagonal
+    blocks hierarchical or dense) is factored by one hm_hchol_factor call,
+    which runs this recursion natively; other trees (dense off-diagonal
+    blocks), or native=False, take the recursion here, one batched call per
+    block operation.  The dense diagonal leaves are factored without waiting;
+    their pivot checks are read once at the end, and the first failing leaf
+    (in the reference's order) raises the PosDefException the reference would
+    raise."""
     if _is_dense(A) or not isinstance(A, AbstractHierarchical):
         return _hchol(A, None)
+    if native:
+        dtype = _tree_dtype(A)
+        try:
+            nodes = _hodlr_nodes(A, dtype)
+        except _NotHodlr:
+            nodes = None
+        if nodes is not None:
+            return _hchol_native(nodes, dtype)
     infos = []
     R = _hchol(A, infos)
     if infos:
@@ -627,6 +640,127 @@ def hierarchicalcholesky(A):
             raise np.linalg.LinAlgError(f"PosDefException: matrix is not positive definite; "
                                         f"Cholesky factorization failed at pivot {int(words[bad[0]])}")
     return R
+
+
+class _NotHodlr(Exception):
+    pass
+
+
+def _hodlr_nodes(A, dtype):
+    """The node list of hm_hchol_factor (pre-order, the root first), each
+    node a dict with the tree object and its device blocks; raises _NotHodlr
+    for trees the native driver does not take."""
+    nodes = []
+
+    def rec(B):
+        if _is_dense(B):
+            D = _dev(B, dtype)
+            if D.dim() != 2 or D.shape[0] != D.shape[1] or D.shape[0] == 0:
+                raise _NotHodlr
+            nodes.append(dict(obj=B, n=int(D.shape[0]), n1=0, left=-1, right=-1, D=D))
+            return len(nodes) - 1
+        if not isinstance(B, AbstractHierarchical) or B.blocksize() != (2, 2):
+            raise _NotHodlr
+        t = (int(B.assigned[0, 0]), int(B.assigned[0, 1]), int(B.assigned[1, 1]))
+        if t[0] not in _TAGS_DIAG or t[1] != 2 or t[2] not in _TAGS_DIAG:
+            raise _NotHodlr
+        i = len(nodes)
+        nodes.append(None)
+        left, right = rec(B.block(0, 0)), rec(B.block(1, 1))
+        U, sg, V = _lr_dev(B.block(0, 1), dtype)
+        n1, n2 = nodes[left]["n"], nodes[right]["n"]
+        if U.shape[0] != n1 or V.shape[0] != n2 or U.shape[1] != V.shape[1] or sg.shape[0] != U.shape[1]:
+            raise _NotHodlr
+        nodes[i] = dict(obj=B, n=n1 + n2, n1=n1, left=left, right=right, U=U, s=sg, V=V)
+        return i
+
+    rec(A)
+    return nodes
+
+
+class _HcholOwner:
+    """The memory of one hm_hchol_factor result; the factor's tensors are
+    views of it and keep this object alive, so it is freed with the last."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+
+    def __del__(self):
+        if self.ctx and lib is not None:
+            lib.hm_hchol_free(self.ctx)
+            self.ctx = None
+
+
+class _DeviceSpan:
+    """__cuda_array_interface__ of a column-major block owned by _HcholOwner."""
+
+    def __init__(self, owner, ptr, shape, strides, typestr):
+        self._owner = owner
+        self.__cuda_array_interface__ = {"shape": shape, "strides": strides, "typestr": typestr,
+                                         "data": (ptr, False), "version": 2}
+
+
+def _owned(owner, ptr, m, n, ld, dtype):
+    torch = _torch()
+    if m == 0 or n == 0 or not ptr:
+        return torch.empty(m, dtype=dtype, device="cuda") if n is None else _empty(m, n, dtype)
+    es = 8 if dtype == torch.float64 else 4
+    ts = "<f8" if es == 8 else "<f4"
+    if n is None:
+        span = _DeviceSpan(owner, ptr, (m,), (es,), ts)
+    else:
+        span = _DeviceSpan(owner, ptr, (m, n), (es, es * ld), ts)
+    return torch.as_tensor(span, device="cuda")
+
+
+def _hchol_native(nodes, dtype):
+    """hm_hchol_factor on the node list; the factor as a tree of the input's
+    types whose blocks are views of the call's result memory (each dense
+    leaf carries its inverse as ``_hm_inverse`` for solvetransposed)."""
+    torch = _torch()
+    arr = (_lib.HcholNode * len(nodes))()
+    for i, nd in enumerate(nodes):
+        pb = arr[i]
+        pb.n, pb.n1, pb.left, pb.right = nd["n"], nd["n1"], nd["left"], nd["right"]
+        if nd["left"] < 0:
+            pb.D, pb.ldd = _ptr(nd["D"]), _ld(nd["D"])
+        else:
+            U, sg, V = nd["U"], nd["s"], nd["V"]
+            pb.r = int(U.shape[1])
+            pb.U, pb.ldu, pb.s, pb.V, pb.ldv = _ptr(U), _ld(U), _ptr(sg), _ptr(V), _ld(V)
+    ctx = ctypes.c_void_p()
+    fail = (ctypes.c_int32 * 2)()
+    dt = _lib.HM_F64 if dtype == torch.float64 else _lib.HM_F32
+    st = lib.hm_hchol_factor(dt, len(nodes), arr, 0, ctypes.byref(ctx), fail, _stream())
+    if st == _lib.HM_ERR_NOT_POSDEF:
+        raise np.linalg.LinAlgError(f"PosDefException: matrix is not positive definite; "
+                                    f"Cholesky factorization failed at pivot {int(fail[1])}")
+    check(st)
+    owner = _HcholOwner(ctx.value)
+    outs = []
+    for i in range(len(nodes)):
+        o = _lib.HcholOut()
+        check(lib.hm_hchol_result(ctx, i, ctypes.byref(o)))
+        outs.append(o)
+
+    def build(i):
+        nd, o = nodes[i], outs[i]
+        if nd["left"] < 0:
+            n = nd["n"]
+            R = _owned(owner, o.R, n, n, o.ldr, dtype)
+            if o.W:
+                R._hm_inverse = _owned(owner, o.W, n, n, o.ldw, dtype)
+            return R
+        n1, n2, r = nd["n1"], nd["n"] - nd["n1"], int(o.r)
+        R = type(nd["obj"])(2, 2, dtype=nd["obj"].dtype)
+        R[_block(1), _block(1)] = build(nd["left"])
+        R[_block(1), _block(2)] = LowRankMatrix(_owned(owner, o.U, n1, r, o.ldu, dtype),
+                                                 _owned(owner, o.s, r, None, 0, dtype),
+                                                 _owned(owner, o.V, n2, r, o.ldv, dtype))
+        R[_block(2), _block(2)] = build(nd["right"])
+        return R
+
+    return build(0)
 
 
 def _hchol(A, infos):
@@ -695,6 +829,12 @@ def _invert_leaves(ops, keep):
     leaf's serial forward substitution on one warp is slow at GB300's FP64
     rate, its inverse's product runs on every warp of the CTA."""
     todo = [o for o in ops if o["kind"] == _lib.HM_SOLVE_TRSM and 0 < o["n1"] <= _INV_MAX]
+    for o in todo:                                # leaves of a native factor come with their inverse
+        W = getattr(o["A"], "_hm_inverse", None)
+        if W is not None:
+            keep.append(W)
+            o["kind"], o["A"], o["ld"] = _lib.HM_SOLVE_INV, W, _ld(W)
+    todo = [o for o in todo if o["kind"] == _lib.HM_SOLVE_TRSM]
     if not todo or any(o["A"].dtype != todo[0]["A"].dtype for o in todo):
         return                                    # nothing to do, or mixed storage: keep the substitutions
     dtype = todo[0]["A"].dtype

@@ -525,6 +525,45 @@ int hm_trtri_batched(int dtype, int nprob, const hm_trtri_problem *probs, void *
 int hm_solve_transposed(int dtype, int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t ncols,
                         void *stream);
 
+/* hierarchicalcholesky(A) (src/cholesky.jl:12-92) of a whole HODLR tree in
+   one call, the recursion run natively.  The tree is a node list: node i
+   covers n rows; a leaf (left = right = -1) holds its dense diagonal block D
+   (n x n, ld ldd; the upper triangle is read); an internal node splits its
+   rows n1 + (n - n1) between its children left and right and holds its upper
+   off-diagonal block A12 = U diag(s) V^T (U n1 x r, V (n - n1) x r, r >= 0).
+   Every block of A22 is updated when its ancestor is reached and the blocks
+   are factored in the reference's order; A12 - R12'R12 updates take
+   R12'R12 = V H V^T whole (H = diag(s) X^T X diag(s), X = R11^{-T} U) into
+   one truncated SVD per block.  The inputs are only read.  On success *ctx
+   owns the factor (free with hm_hchol_free): hm_hchol_result gives, per
+   node, R12 = U diag(s) V^T (rank r; U n1 x r, V (n - n1) x r) or the leaf's
+   upper factor R (n x n) and, for leaves up to 112 rows (FP64; 159 FP32),
+   W = R^{-1}.  A leaf that is not positive definite: HM_ERR_NOT_POSDEF with
+   fail = {node, pivot} of the first such leaf in the reference's order, no
+   context.  Synchronous (the host waits once per node whose A22 holds
+   LowRankMatrix blocks, for their new ranks). */
+typedef struct {
+    int64_t n, n1;
+    int32_t left, right;
+    const void *D; int64_t ldd;
+    const void *U; int64_t ldu;
+    const void *s;
+    const void *V; int64_t ldv;
+    int32_t r;
+} hm_hchol_node;
+typedef struct {
+    int32_t r;
+    void *U; int64_t ldu;
+    void *s;
+    void *V; int64_t ldv;
+    void *R; int64_t ldr;
+    void *W; int64_t ldw;
+} hm_hchol_out;
+int hm_hchol_factor(int dtype, int nnodes, const hm_hchol_node *nodes, int32_t root, void **ctx, int32_t *fail,
+                    void *stream);
+int hm_hchol_result(void *ctx, int32_t node, hm_hchol_out *out);
+int hm_hchol_free(void *ctx);
+
 #ifdef __cplusplus
 }
 #endif

@@ -184,6 +184,38 @@ def test_hierarchical_cholesky(dt, kernel, dense_below):
 
 
 @pytest.mark.parametrize("dt", DT)
+@pytest.mark.parametrize("n,leaf", [(1024, 64), (2000, 50), (4096, 128)])
+def test_native_cholesky_matches_recursion(dt, n, leaf):
+    """hm_hchol_factor (the recursion of src/cholesky.jl:12-92 run natively,
+    R12'R12 passed whole into the A22 updates) against the block-by-block
+    recursion and the oracle, on uneven and deeper trees."""
+    T, D = A.spd_hodlr(n, leaf, kernel="gauss", seed=n)
+    Td = tree_dev(T, dt)
+    Rn = G.hierarchicalcholesky(Td)
+    Rp = G.hierarchicalcholesky(Td, native=False)
+    Rdn, Rdp = A.todense(tree_host(Rn)), A.todense(tree_host(Rp))
+    tol = CHOL[dt]
+    assert np.allclose(np.tril(Rdn, -1), 0)
+    assert rel(Rdn, Rdp) <= tol["fwd"]
+    assert rel(Rdn.T @ Rdn, D) <= tol["bwd"]
+    if dt == torch.float64:
+        assert rel(Rdn, A.todense(A.cholesky(T))) <= tol["fwd"]
+    # the leaves carry their inverses, which solvetransposed applies
+    leaves = [b for b, _, _ in Rn.leaves() if G._is_dense(b)]
+    assert all(getattr(b, "_hm_inverse", None) is not None for b in leaves if b.shape[0] <= 112)
+    b = np.random.default_rng(n + 1).standard_normal(n)
+    x = host(G.solvetransposed(Rn, dev(b, dt)))
+    assert rel(Rdn.T @ x, b) <= tol["solve"]
+    # the factor's memory lives as long as its tensors do
+    U = [blk for blk, _, _ in Rn.leaves() if isinstance(blk, hm.LowRankMatrix)][0].U
+    del Rn
+    import gc
+    gc.collect()
+    torch.cuda.synchronize()
+    assert torch.isfinite(U).all()
+
+
+@pytest.mark.parametrize("dt", DT)
 def test_trtri_batched(dt):
     """hm_trtri_batched: W = R^{-1} of upper triangular blocks (the inverses
     solvetransposed applies to small diagonal leaves) against numpy's inverse."""
