@@ -1364,9 +1364,13 @@ int solve_run(int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t nc
 // drop only singular values below q eps(sigma_1)) and the update's SVD
 // truncates the sum.  R12 = R11^{-T} U runs through the left subtree's
 // forward-substitution schedule (its leaves as products with their inverses).
-// The host waits once per node whose A22 holds LowRankMatrix blocks (their
-// new ranks size the next problems); everything else is queued on the stream.
-// Problem descriptors go to the device from pinned host memory.
+// The A22 updates' truncated SVDs run on a second stream: a block updated at
+// node N is next needed when the factorisation reaches it, after N's whole
+// left part of A22, so the SVDs overlap with the chain of leaf factorisations
+// and solves.  The host reads a block's new rank (which sizes the problems
+// that use it) only when it next uses the block, waiting on that update's
+// event; nothing else waits until the end.  Problem descriptors go to the
+// device from pinned host memory.
 
 // Device memory handed out in 256-byte aligned pieces from chunks of at
 // least 32 MB, all released together.
@@ -1479,6 +1483,8 @@ struct HChol {
         int r = 0;
         const T *D = nullptr;                            // the current block (leaves)
         int64_t ldd = 1;
+        cudaEvent_t ev = nullptr;                        // r is pending: *slot once ev has completed
+        const int32_t *slot = nullptr;
     };
     const hm_hchol_node *in;
     int nn;
@@ -1491,14 +1497,58 @@ struct HChol {
     hm_solve_op *h_ops = nullptr, *d_ops = nullptr;
     int32_t *h_small = nullptr, *d_info = nullptr;       // h_small: pinned, ranks and pivot words read back
     unsigned *counter = nullptr;                         // hchol_gram's last-CTA counter
+    cudaStream_t su = nullptr;                           // the A22 updates' truncated SVDs
+    std::vector<cudaEvent_t> events;
+    std::vector<int32_t *> pinned_ints;                  // rank words read back by the side stream
+    size_t pinned_left = 0, pinned_cap = 0;
     int64_t h_small_n = 0;
     int nleaves = 0;
 
     HChol(const hm_hchol_node *nodes, int n, cudaStream_t s, HCholResult *r) : in(nodes), nn(n), st(s), res(r), S(s) {}
     ~HChol()
     {
+        if (su) {
+            cudaStreamSynchronize(su);                   // nothing in flight reads memory freed below
+            cudaStreamDestroy(su);
+        }
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+        for (int32_t *p : pinned_ints) cudaFreeHost(p);
         if (h_ops) cudaFreeHost(h_ops);
         if (h_small) cudaFreeHost(h_small);
+    }
+
+    int new_event(cudaEvent_t *e)
+    {
+        ALG_CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        events.push_back(*e);
+        return HM_OK;
+    }
+
+    int pinned_words(int n, int32_t **p)
+    {
+        if ((size_t)n > pinned_left) {
+            const size_t cnt = std::max<size_t>(n, 16384);
+            int32_t *h = nullptr;
+            ALG_CK(cudaMallocHost((void **)&h, cnt * sizeof(int32_t)));
+            pinned_ints.push_back(h);
+            pinned_cap = pinned_left = cnt;
+        }
+        *p = pinned_ints.back() + (pinned_cap - pinned_left);
+        pinned_left -= n;
+        return HM_OK;
+    }
+
+    // the rank of node i's current A12 on the host (waits for the update that made it)
+    int resolve(int i)
+    {
+        Node &N = nd[i];
+        if (!N.ev) return HM_OK;
+        ALG_CK(cudaEventSynchronize(N.ev));
+        ALG_CK(cudaStreamWaitEvent(st, N.ev, 0));
+        N.r = *N.slot;
+        N.ev = nullptr;
+        N.slot = nullptr;
+        return HM_OK;
     }
 
     static bool is_leaf(const hm_hchol_node &g) { return g.left < 0 && g.right < 0; }
@@ -1579,6 +1629,7 @@ struct HChol {
     int setup(int root)
     {
         ALG_TRY(layout(root));
+        ALG_CK(cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking));
         res->out.assign(nn, hm_hchol_out{});
         const int64_t tmax = trtri_max<T>();
         ALG_CK(cudaMallocHost((void **)&h_ops, sizeof(hm_solve_op) * inorder.size()));
@@ -1740,6 +1791,7 @@ struct HChol {
         }
         if (inner.empty()) return HM_OK;
         const int np = (int)inner.size();
+        for (int M : inner) ALG_TRY(resolve(M));
         std::vector<LrJob> jobs(np);
         for (int k = 0; k < np; ++k) {
             const int M = inner[k];
@@ -1767,24 +1819,38 @@ struct HChol {
             nd[M].s = sn;
             nd[M].V = Vn; nd[M].ldv = std::max<int64_t>(m2, 1);
         }
+        // the truncated SVDs run on the side stream once H and R12 are ready on
+        // the main one; the new ranks come back there too, and are waited for
+        // only where a block is next used (resolve)
         LrPlan pl;
         ALG_TRY(lr_svd_plan<T>(np, jobs.data(), pl));
+        cudaEvent_t eh = nullptr, es = nullptr;
+        ALG_TRY(new_event(&eh));
+        ALG_TRY(new_event(&es));
+        ALG_CK(cudaEventRecord(eh, st));
+        ALG_CK(cudaStreamWaitEvent(su, eh, 0));
         LrJob *dj = nullptr;
         int64_t *doff = nullptr, *dcoff = nullptr;
         T *dws = nullptr;
         int *dr = nullptr;
-        ALG_TRY(S.put(jobs.data(), (size_t)np, &dj));
-        ALG_TRY(S.put(pl.off.data(), pl.off.size(), &doff));
-        ALG_TRY(S.put(pl.coff.data(), pl.coff.size(), &dcoff));
+        S.st = su;
+        int rc = S.put(jobs.data(), (size_t)np, &dj);
+        if (!rc) rc = S.put(pl.off.data(), pl.off.size(), &doff);
+        if (!rc) rc = S.put(pl.coff.data(), pl.coff.size(), &dcoff);
+        S.st = st;
+        ALG_TRY(rc);
         ALG_TRY(S.zeros((size_t)pl.ws, &dws));
         ALG_TRY(S.zeros((size_t)np, &dr));
-        lr_svd_kernel<T><<<np, kThreads, pl.smem, st>>>(dj, doff, dcoff, dws, dr, pl.dmax);
+        lr_svd_kernel<T><<<np, kThreads, pl.smem, su>>>(dj, doff, dcoff, dws, dr, pl.dmax);
         ALG_CK(cudaGetLastError());
-        ALG_TRY(small_host(np));
-        ALG_CK(cudaMemcpyAsync(h_small, dr, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, st));
-        ALG_CK(cudaStreamSynchronize(st));
-        S.drained();
-        for (int k = 0; k < np; ++k) nd[inner[k]].r = h_small[k];
+        int32_t *slot = nullptr;
+        ALG_TRY(pinned_words(np, &slot));
+        ALG_CK(cudaMemcpyAsync(slot, dr, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, su));
+        ALG_CK(cudaEventRecord(es, su));
+        for (int k = 0; k < np; ++k) {
+            nd[inner[k]].ev = es;
+            nd[inner[k]].slot = slot + k;
+        }
         return HM_OK;
     }
 
@@ -1793,6 +1859,7 @@ struct HChol {
         const hm_hchol_node &g = in[i];
         if (is_leaf(g)) return leaf(i);
         ALG_TRY(node(g.left));
+        ALG_TRY(resolve(i));
         Node &N = nd[i];
         const int r = N.r;
         const int64_t n1 = g.n1, n2 = g.n - g.n1;
@@ -1834,6 +1901,7 @@ struct HChol {
         ALG_TRY(setup(root));
         ALG_TRY(node(root));
         ALG_CK(cudaMemcpyAsync(h_small, d_info, sizeof(int32_t) * nleaves, cudaMemcpyDeviceToHost, st));
+        ALG_CK(cudaStreamSynchronize(su));
         ALG_CK(cudaStreamSynchronize(st));
         S.drained();
         for (int i : inorder) {

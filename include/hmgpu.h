@@ -540,8 +540,9 @@ int hm_solve_transposed(int dtype, int nops, const hm_solve_op *ops, void *B, in
    upper factor R (n x n) and, for leaves up to 112 rows (FP64; 159 FP32),
    W = R^{-1}.  A leaf that is not positive definite: HM_ERR_NOT_POSDEF with
    fail = {node, pivot} of the first such leaf in the reference's order, no
-   context.  Synchronous (the host waits once per node whose A22 holds
-   LowRankMatrix blocks, for their new ranks). */
+   context.  Synchronous.  The A22 updates' truncated SVDs run on a second
+   stream of the library's and overlap with the leaf factorisations and solves
+   on `stream`; the host reads a block's new rank when it next uses it. */
 typedef struct {
     int64_t n, n1;
     int32_t left, right;
