@@ -29,7 +29,8 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kJacobiSweeps = 40;
 constexpr int kTkChunk = 128;       // coefficients per warp of a low-rank solve update
-constexpr int kInvMax = 256;        // largest block of an HM_SOLVE_INV op
+constexpr int kInvMax = 256;        // largest block of an HM_SOLVE_INV or HM_SOLVE_LTRSM op
+constexpr int kLtrsmSmem = 64;      // HM_SOLVE_LTRSM blocks up to this size are staged in shared memory
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v)
@@ -138,9 +139,10 @@ __device__ void apply_q(const T *A, int64_t m, int kk, const T *tau, T *y)
 // t = g / (2a) from the two mantissas with the exponents applied apart
 // (strongly graded columns give angles far below FP32's range).  Its
 // relative error, about 1e-7, only leaves an inner product of that relative
-// size for the next sweep.  c = (1 + t^2)^(-1/2) is then refined in T by two
-// Newton steps from the FP32 estimate, so c^2 + s^2 = 1 to T's rounding and
-// every rotation is orthogonal in T.  Returns false when t underflows.
+// size for the next sweep.  c = (1 + t^2)^(-1/2) is then refined in T from
+// the FP32 estimate, so c^2 + s^2 = 1 to T's rounding and
+// every rotation is orthogonal in T (c by one Halley step from the FP32
+// estimate).  Returns false when t underflows.
 __device__ __forceinline__ int exponent_of(double x) { return ((__double2hiint(x) >> 20) & 0x7ff) - 1023; }
 __device__ __forceinline__ int exponent_of(float x) { return ((__float_as_int(x) >> 23) & 0xff) - 127; }
 template <typename T> __device__ __forceinline__ T pow2(int e);
@@ -175,41 +177,50 @@ __device__ __forceinline__ bool jacobi_tangent(T al, T be, T ga, T &t)
     return t != T(0);
 }
 
-template <typename T>
-__device__ __forceinline__ bool jacobi_rotation(T al, T be, T ga, T &c, T &s)
+// d^(-1/2) for d > 0 from the FP32 estimate refined by Halley's iteration;
+// d outside FP32's range is first scaled to m in [1, 4) by an even power of
+// two.  (Subnormal d: the library square root.)
+__device__ __forceinline__ double rsqrt_halley(double d, double y0)
 {
-    T t;
-    if (!jacobi_tangent(al, be, ga, t)) return false;
-    const float tf = (float)t;
-    const T h = T(-0.5) * fma(t, t, T(1));
-    T cc = (T)rsqrtf(fmaf(tf, tf, 1.f));
-    cc = cc * fma(h, cc * cc, T(1.5));
-    cc = cc * fma(h, cc * cc, T(1.5));
-    c = cc;
-    s = cc * t;
-    return true;
+    // one step of Halley's iteration for d^(-1/2): with e = 1 - d y0^2,
+    // y = y0 (1 + e/2 + 3e^2/8) leaves 5e^3/16, below double rounding for
+    // the 2^-23 of an FP32 estimate; four dependent FP64 operations
+    const double e = fma(-d, y0 * y0, 1.0);
+    return fma(y0 * e, fma(0.375, e, 0.5), y0);
 }
-
-// d^(-1/2) for d > 0 by Newton's iteration y <- y (3 - d y^2) / 2 from the
-// FP32 estimate: d = m 2^e with e even and m in [1, 4), two steps take the
-// estimate's 2^-23 to T's precision.  (Subnormal d: the library square root.)
 __device__ __forceinline__ double rsqrt_pos(double d)
 {
+    if (d > 1e-30 && d < 1e30) return rsqrt_halley(d, (double)rsqrtf((float)d));
     if (d < 1e-300) return 1.0 / sqrt(d);
     int e = exponent_of(d);
     e -= e & 1;
     const double m = d * pow2<double>(-e);
-    double y = (double)rsqrtf((float)m);
-    const double h = -0.5 * m;
-    y = y * fma(h, y * y, 1.5);
-    y = y * fma(h, y * y, 1.5);
-    return y * pow2<double>(-e / 2);
+    return rsqrt_halley(m, (double)rsqrtf((float)m)) * pow2<double>(-e / 2);
 }
 __device__ __forceinline__ float rsqrt_pos(float d)
 {
     if (d < 1e-36f) return 1.f / sqrtf(d);
     const float y = rsqrtf(d);
     return y * fmaf(-0.5f * d, y * y, 1.5f);
+}
+
+template <typename T>
+__device__ __forceinline__ bool jacobi_rotation(T al, T be, T ga, T &c, T &s)
+{
+    T t;
+    if (!jacobi_tangent(al, be, ga, t)) return false;
+    const float tf = (float)t;
+    const T u = fma(t, t, T(1));
+    const T c0 = (T)rsqrtf(fmaf(tf, tf, 1.f));
+    T cc;
+    if constexpr (sizeof(T) == 8) {
+        cc = rsqrt_halley(u, c0);
+    } else {
+        cc = c0 * fmaf(-0.5f * u, c0 * c0, 1.5f);
+    }
+    c = cc;
+    s = cc * t;
+    return true;
 }
 
 // One problem of lr_svd as the kernel reads it: the public descriptor and,
@@ -457,10 +468,15 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const LrJob *jobs, con
         if (lane == 0) sig[j] = sv * invj * s_unscale;
     }
     __syncthreads();
+    // descending order, ties by index; a NaN ranks below everything (its key
+    // is -1), so that perm is a permutation whatever the values
     for (int j = tid; j < q; j += kThreads) {
         int pos = 0;
-        const T sj = sig[j];
-        for (int l = 0; l < q; ++l) pos += (sig[l] > sj) || (sig[l] == sj && l < j);
+        const T sj = sig[j] == sig[j] ? sig[j] : T(-1);
+        for (int l = 0; l < q; ++l) {
+            const T sl = sig[l] == sig[l] ? sig[l] : T(-1);
+            pos += (sl > sj) || (sl == sj && l < j);
+        }
         perm[pos] = j;
     }
     __syncthreads();
@@ -707,83 +723,84 @@ __device__ __forceinline__ void upper_pair(int p, int &i, int &j)
 }
 
 // A dense diagonal leaf of the hierarchical Cholesky: R = chol(A) (the upper
-// triangle of A read) and W = R^{-1}, one CTA, both in shared memory.  The
-// factorisation is right-looking: one warp forms each pivot (Newton's
-// reciprocal square root) and scales its row, then the trailing triangle is
-// updated with its entries spread evenly over all threads (an FP64 warp
-// instruction costs the same with idle lanes).  W comes from Gauss-Jordan
-// elimination on [R | I] from the last row up: step k scales row k of W by
-// 1/R_kk and subtracts R_ik times it from the rows i < k, k (n - k)
-// independent FMAs per step and no dot-product chain.
+// triangle of A read) and L = R^T, one CTA, in shared memory (ld n + 1).
+// Right-looking with lookahead: warp 0 applies step j to row j + 1 and forms
+// pivot j + 1 (a Halley reciprocal square root; the dependent FP64 chain is
+// the kernel's critical path on GB300, 64 cycles per operation) while the
+// other warps apply step j to the rows below, its entries spread evenly over
+// them (an FP64 warp instruction costs the same with idle lanes); one barrier
+// per step.  L is what the forward substitutions of the solves read (its
+// columns contiguous).
 struct LeafChol {
     int64_t n;
     const void *A; int64_t lda;
     void *R; int64_t ldr;
-    void *W; int64_t ldw;
+    void *L; int64_t ldl;
 };
+// largest leaf that leaf_chol keeps in shared memory
+template <typename T>
+int64_t leaf_chol_max()
+{
+    int64_t n = 0;
+    while (((n + 1) * (n + 2) + (n + 1)) * (int64_t)sizeof(T) <= 200 * 1024) ++n;
+    return n;
+}
 template <typename T>
 __global__ void __launch_bounds__(kThreads) leaf_chol(const LeafChol *probs, int *info)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const LeafChol g = probs[blockIdx.x];
-    const int n = (int)g.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    T *S = reinterpret_cast<T *>(smem_raw);            // n x n, ld n
-    T *Wm = S + (int64_t)n * n;                        // n x n, ld n
-    T *rinv = Wm + (int64_t)n * n;                     // n
+    const int n = (int)g.n, ls = n + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    T *S = reinterpret_cast<T *>(smem_raw);            // n x n, ld n + 1
     __shared__ int s_fail;
     const T *A = static_cast<const T *>(g.A);
     for (int e = tid; e < n * n; e += kThreads) {
         const int i = e % n, j = e / n;
-        S[e] = i <= j ? A[i + g.lda * j] : T(0);
-        Wm[e] = i == j ? T(1) : T(0);
+        S[i + ls * j] = i <= j ? A[i + g.lda * j] : T(0);
     }
     if (tid == 0) s_fail = 0;
     __syncthreads();
-    for (int j = 0; j < n; ++j) {
+    auto pivot = [&](int j) {
+        const T d = S[j + ls * j];
+        if (!(d > T(0))) {
+            if (lane == 0) s_fail = j + 1;
+            return;
+        }
+        const T y = rsqrt_pos(d);
+        for (int l = j + 1 + lane; l < n; l += 32) S[j + ls * l] *= y;
+        if (lane == 0) S[j + ls * j] = d * y;
+    };
+    if (warp == 0) pivot(0);
+    __syncthreads();
+    for (int j = 0; j < n && !s_fail; ++j) {
         if (warp == 0) {
-            const T d = S[j + n * j];
-            if (!(d > T(0))) {
-                if (lane == 0) s_fail = j + 1;
-            } else {
-                const T y = rsqrt_pos(d);
-                for (int l = j + 1 + lane; l < n; l += 32) S[j + n * l] *= y;
-                if (lane == 0) { S[j + n * j] = d * y; rinv[j] = y; }
+            if (j + 1 < n) {
+                const T a = S[j + ls * (j + 1)];
+                for (int l = j + 1 + lane; l < n; l += 32) S[j + 1 + ls * l] = fma(-a, S[j + ls * l], S[j + 1 + ls * l]);
+                __syncwarp();
+                pivot(j + 1);
+            }
+        } else {
+            const int m = n - j - 2, tj = m > 0 ? m * (m + 1) / 2 : 0;
+            for (int p = tid - 32; p < tj; p += kThreads - 32) {
+                int i, l;
+                upper_pair(p, i, l);
+                i += j + 2;
+                l += j + 2;
+                S[i + ls * l] = fma(-S[j + ls * i], S[j + ls * l], S[i + ls * l]);
             }
         }
         __syncthreads();
-        if (s_fail) break;
-        const int m = n - j - 1, tj = m * (m + 1) / 2;
-        for (int p = tid; p < tj; p += kThreads) {
-            int i, l;
-            upper_pair(p, i, l);
-            i += j + 1;
-            l += j + 1;
-            S[i + n * l] = fma(-S[j + n * i], S[j + n * l], S[i + n * l]);
-        }
-        __syncthreads();
     }
-    if (s_fail) {
-        if (tid == 0) info[blockIdx.x] = s_fail;
-        return;
-    }
-    for (int k = n - 1; k >= 0; --k) {
-        const T y = rinv[k];
-        for (int jj = k + tid; jj < n; jj += kThreads) Wm[k + n * jj] *= y;
-        __syncthreads();
-        const int cnt = k * (n - k);
-        for (int p = tid; p < cnt; p += kThreads) {
-            const int i = p % k, jj = k + p / k;
-            Wm[i + n * jj] = fma(-S[i + n * k], Wm[k + n * jj], Wm[i + n * jj]);
-        }
-        __syncthreads();
-    }
-    T *R = static_cast<T *>(g.R), *W = static_cast<T *>(g.W);
+    if (tid == 0) info[blockIdx.x] = s_fail;
+    // R and L are written also after a failed pivot (the partial factor, as
+    // potrf_batched leaves it): what follows reads finite values
+    T *R = static_cast<T *>(g.R), *Lo = static_cast<T *>(g.L);
     for (int e = tid; e < n * n; e += kThreads) {
         const int i = e % n, j = e / n;
-        R[i + g.ldr * j] = S[e];
-        W[i + g.ldw * j] = Wm[e];
+        R[i + g.ldr * j] = S[i + ls * j];
+        Lo[i + g.ldl * j] = i >= j ? S[j + ls * i] : T(0);
     }
-    if (tid == 0) info[blockIdx.x] = 0;
 }
 
 // H = diag(s) X^T X diag(s) for a tall X (rows x r, r <= kGramMax) by
@@ -889,6 +906,56 @@ __global__ void __launch_bounds__(kThreads) hchol_leaf_update(const LeafUpd *ups
     }
 }
 
+// x <- L^{-1} x for a lower triangular n x n block L (n <= 256) by one warp,
+// right-looking: lane l holds x[l + 32 t]; once x_i is final (its owner
+// multiplies by 1/L_ii, formed for all rows up front) a shuffle broadcasts it
+// and every lane subtracts L[l, i] x_i from its rows l > i.  Column i of L is
+// read contiguously (from shared memory when the caller staged L there) and
+// the next column is loaded while the current one is applied.  Per step: one
+// FP64 multiply, one shuffle and one FMA per 32 rows on the dependent path.
+template <typename T>
+__device__ void ltrsm_warp(const T *L, int64_t ld, int n, T *x)
+{
+    const int lane = threadIdx.x & 31, nt = (n + 31) >> 5;
+    T xr[8], rinv[8], col[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int i = lane + 32 * t;
+        xr[t] = t < nt && i < n ? x[i] : T(0);
+        rinv[t] = t < nt && i < n ? T(1) / L[i + ld * i] : T(0);
+        col[t] = t < nt && i > 0 && i < n ? L[i] : T(0);
+    }
+    for (int i = 0; i < n; ++i) {
+        T nxt[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int row = lane + 32 * t;
+            nxt[t] = t < nt && i + 1 < n && row > i + 1 && row < n ? L[row + ld * (i + 1)] : T(0);
+        }
+        const int owner = i & 31, ti = i >> 5;
+        T xs = xr[0], rs = rinv[0];
+#pragma unroll
+        for (int t = 1; t < 8; ++t)
+            if (t == ti) { xs = xr[t]; rs = rinv[t]; }
+        const T xi = __shfl_sync(0xffffffffu, xs * rs, owner);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            if (t >= nt) break;
+            const int row = lane + 32 * t;
+            if (row == i) xr[t] = xi;
+            else if (row > i) xr[t] = fma(-col[t], xi, xr[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) col[t] = nxt[t];
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int i = lane + 32 * t;
+        if (t < nt && i < n) x[i] = xr[t];
+    }
+    __syncwarp();
+}
+
 // W = R^{-1} for upper triangular n x n blocks, one CTA per block, R staged in
 // shared memory.  Column j of W is the back substitution R w = e_j, run by a
 // group of four lanes (partial sums over k = i+1+q, i+5+q, ... reduced by two
@@ -941,6 +1008,7 @@ __global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *op
 {
     __shared__ T tk[kTkChunk];
     __shared__ T xs[kInvMax];
+    __shared__ T ls[kLtrsmSmem * kLtrsmSmem];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     T *const xb = B + ldb * (int64_t)blockIdx.x;
     auto xat = [&](int64_t o) { return xb + (o - base); };    // row o of the schedule is row o - base of B
@@ -949,6 +1017,17 @@ __global__ void __launch_bounds__(kThreads) solve_schedule(const hm_solve_op *op
         const T *A = static_cast<const T *>(op.A);
         if (op.kind == HM_SOLVE_TRSM) {
             if (warp == 0) trsm_t_warp(A, op.ld, op.n1, xat(op.o1));
+        } else if (op.kind == HM_SOLVE_LTRSM) {
+            if (op.n1 <= kLtrsmSmem) {                  // L staged by all warps, then one warp substitutes
+                for (int e = tid; e < op.n1 * op.n1; e += kThreads) {
+                    const int i = e % (int)op.n1, j = e / (int)op.n1;
+                    ls[i + kLtrsmSmem * j] = i >= j ? A[i + op.ld * j] : T(0);
+                }
+                __syncthreads();
+                if (warp == 0) ltrsm_warp<T>(ls, kLtrsmSmem, (int)op.n1, xat(op.o1));
+            } else if (warp == 0) {
+                ltrsm_warp<T>(A, op.ld, (int)op.n1, xat(op.o1));
+            }
         } else if (op.kind == HM_SOLVE_INV) {
             // x1 <- W^T x1, W = R^{-1} upper: four lanes per output, all warps
             T *x1 = xat(op.o1);
@@ -1324,7 +1403,7 @@ int solve_run(int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t nc
     int64_t extent = 0;
     for (int i = 0; i < nops; ++i) {
         const hm_solve_op &o = ops[i];
-        if (o.kind < HM_SOLVE_TRSM || o.kind > HM_SOLVE_INV || (o.kind == HM_SOLVE_INV && o.n1 > kInvMax) || o.n1 < 0 || o.n2 < 0 || o.o1 < 0 || o.o2 < 0 ||
+        if (o.kind < HM_SOLVE_TRSM || o.kind > HM_SOLVE_LTRSM || ((o.kind == HM_SOLVE_INV || o.kind == HM_SOLVE_LTRSM) && o.n1 > kInvMax) || o.n1 < 0 || o.n2 < 0 || o.o1 < 0 || o.o2 < 0 ||
             !o.A || (o.kind == HM_SOLVE_LR && (o.r < 0 || (o.r && (!o.s || !o.B || o.ld < o.n1 || o.ld2 < o.n2)))) ||
             (o.kind != HM_SOLVE_LR && o.ld < o.n1)) {
             set_last_error("solve op %d: bad operation", i);
@@ -1494,10 +1573,13 @@ struct HChol {
     std::vector<int> inorder;
     Arena temp;
     PinnedStager S;
-    hm_solve_op *h_ops = nullptr, *d_ops = nullptr;
+    hm_solve_op *h_ops = nullptr;                        // the whole tree's schedule, in order
     int32_t *h_small = nullptr, *d_info = nullptr;       // h_small: pinned, ranks and pivot words read back
     unsigned *counter = nullptr;                         // hchol_gram's last-CTA counter
+    std::vector<T *> lts;                                // per leaf: R^T for the forward substitutions
     cudaStream_t su = nullptr;                           // the A22 updates' truncated SVDs
+    cudaStream_t sw = nullptr;                           // the leaves' inverses
+    std::vector<cudaEvent_t> wev;                        // per node: its leaf inverse is done
     std::vector<cudaEvent_t> events;
     std::vector<int32_t *> pinned_ints;                  // rank words read back by the side stream
     size_t pinned_left = 0, pinned_cap = 0;
@@ -1507,9 +1589,10 @@ struct HChol {
     HChol(const hm_hchol_node *nodes, int n, cudaStream_t s, HCholResult *r) : in(nodes), nn(n), st(s), res(r), S(s) {}
     ~HChol()
     {
-        if (su) {
-            cudaStreamSynchronize(su);                   // nothing in flight reads memory freed below
-            cudaStreamDestroy(su);
+        for (cudaStream_t x : {su, sw}) {
+            if (!x) continue;
+            cudaStreamSynchronize(x);                    // nothing in flight reads memory freed below
+            cudaStreamDestroy(x);
         }
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         for (int32_t *p : pinned_ints) cudaFreeHost(p);
@@ -1630,10 +1713,11 @@ struct HChol {
     {
         ALG_TRY(layout(root));
         ALG_CK(cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking));
+        ALG_CK(cudaStreamCreateWithFlags(&sw, cudaStreamNonBlocking));
         res->out.assign(nn, hm_hchol_out{});
-        const int64_t tmax = trtri_max<T>();
+        lts.assign(nn, nullptr);
+        wev.assign(nn, nullptr);
         ALG_CK(cudaMallocHost((void **)&h_ops, sizeof(hm_solve_op) * inorder.size()));
-        ALG_TRY(temp.get(inorder.size(), &d_ops));
         ALG_TRY(temp.get((size_t)nleaves, &d_info));
         ALG_TRY(temp.get(1, &counter));
         ALG_CK(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
@@ -1654,12 +1738,17 @@ struct HChol {
                 op.A = R;
                 op.ld = g.n;
                 op.kind = HM_SOLVE_TRSM;
-                if (g.n <= tmax && g.n <= kInvMax) {  // factored with its inverse by leaf_chol
+                if (g.n <= leaf_chol_max<T>() && g.n <= kInvMax) {  // leaf_chol, its transpose for the solves
+                    T *Lt = nullptr;
+                    ALG_TRY(temp.get((size_t)(g.n * g.n), &Lt));
+                    lts[i] = Lt;
+                    op.A = Lt;
+                    op.kind = HM_SOLVE_LTRSM;
+                }
+                if (g.n <= trtri_max<T>()) {          // the inverse, made on its own stream
                     ALG_TRY(res->keep.get((size_t)(g.n * g.n), &W));
                     o.W = W;
                     o.ldw = g.n;
-                    op.A = W;
-                    op.kind = HM_SOLVE_INV;
                 }
                 any = R;
             } else {
@@ -1672,7 +1761,6 @@ struct HChol {
         }
         for (int i : inorder)
             if (!h_ops[nd[i].inord].A) h_ops[nd[i].inord].A = any;
-        ALG_CK(cudaMemcpyAsync(d_ops, h_ops, sizeof(hm_solve_op) * inorder.size(), cudaMemcpyHostToDevice, st));
         return HM_OK;
     }
 
@@ -1681,15 +1769,15 @@ struct HChol {
         const hm_hchol_node &g = in[i];
         Node &N = nd[i];
         hm_hchol_out &o = res->out[i];
-        if (o.W) {
-            const LeafChol lc{g.n, N.D, N.ldd, o.R, o.ldr, o.W, o.ldw};
-            const size_t smem = (size_t)(2 * g.n * g.n + g.n) * sizeof(T);
+        if (lts[i]) {
+            const LeafChol lc{g.n, N.D, N.ldd, o.R, o.ldr, lts[i], g.n};
+            const size_t smem = (size_t)(g.n * (g.n + 1)) * sizeof(T);
             ALG_TRY(set_smem(leaf_chol<T>, smem));
             LeafChol *dl = nullptr;
             ALG_TRY(S.put(&lc, 1, &dl));
             leaf_chol<T><<<1, kThreads, smem, st>>>(dl, d_info + N.leaf);
             ALG_CK(cudaGetLastError());
-            return HM_OK;
+            return inverse(i);
         }
         const hm_potrf_problem pp{g.n, N.D, N.ldd, o.R, o.ldr};
         const int64_t nsmem = potrf_nsmem<T>(g.n);
@@ -1699,7 +1787,47 @@ struct HChol {
         ALG_TRY(S.put(&pp, 1, &dp));
         potrf_batched<T><<<1, kThreads, smem, st>>>(dp, d_info + N.leaf, nsmem);
         ALG_CK(cudaGetLastError());
+        return inverse(i);
+    }
+
+    // W = R^{-1} of leaf i on the inverses' stream; the solves use it once done
+    int inverse(int i)
+    {
+        hm_hchol_out &o = res->out[i];
+        if (!o.W) return HM_OK;
+        cudaEvent_t e = nullptr;
+        ALG_TRY(new_event(&e));
+        ALG_TRY(new_event(&wev[i]));
+        ALG_CK(cudaEventRecord(e, st));
+        ALG_CK(cudaStreamWaitEvent(sw, e, 0));
+        const hm_trtri_problem tp{in[i].n, o.R, o.ldr, o.W, o.ldw};
+        S.st = sw;
+        const int rc = trtri_launch<T>(1, &tp, sw, S);
+        S.st = st;
+        ALG_TRY(rc);
+        ALG_CK(cudaEventRecord(wev[i], sw));
         return HM_OK;
+    }
+
+    // the forward-substitution schedule of the subtree of node j: each leaf
+    // as a product with its inverse when that is already made, else by
+    // substitution (nothing waits for an inverse)
+    int schedule(int j, hm_solve_op **d)
+    {
+        const Node &J = nd[j];
+        std::vector<hm_solve_op> ops(h_ops + J.ob, h_ops + J.oe);
+        for (int k = J.ob; k < J.oe; ++k) {
+            const int i = inorder[k];
+            if (!is_leaf(in[i]) || !wev[i]) continue;
+            const cudaError_t q = cudaEventQuery(wev[i]);
+            if (q == cudaErrorNotReady) continue;
+            ALG_CK(q);
+            hm_solve_op &op = ops[k - J.ob];
+            op.kind = HM_SOLVE_INV;
+            op.A = res->out[i].W;
+            op.ld = res->out[i].ldw;
+        }
+        return S.put(ops.data(), ops.size(), d);
     }
 
     // every node and leaf below node j (j itself included)
@@ -1874,7 +2002,9 @@ struct HChol {
             ALG_CK(cudaMemcpy2DAsync(Vk, n2 * sizeof(T), N.V, N.ldv * sizeof(T), n2 * sizeof(T), r,
                                      cudaMemcpyDeviceToDevice, st));
             const Node &L = nd[g.left];
-            solve_schedule<T><<<(unsigned)r, kThreads, 0, st>>>(d_ops + L.ob, L.oe - L.ob, X, n1, L.off);
+            hm_solve_op *dops = nullptr;
+            ALG_TRY(schedule(g.left, &dops));
+            solve_schedule<T><<<(unsigned)r, kThreads, 0, st>>>(dops, L.oe - L.ob, X, n1, L.off);
             ALG_CK(cudaGetLastError());
         }
         hm_hchol_out &o = res->out[i];
@@ -1888,7 +2018,6 @@ struct HChol {
             op.A = X;
             op.s = sk;
             op.B = Vk;
-            ALG_CK(cudaMemcpyAsync(d_ops + N.inord, &op, sizeof(hm_solve_op), cudaMemcpyHostToDevice, st));
             ALG_TRY(update(i, X, sk, Vk, r));
         }
         return node(g.right);
@@ -1902,6 +2031,7 @@ struct HChol {
         ALG_TRY(node(root));
         ALG_CK(cudaMemcpyAsync(h_small, d_info, sizeof(int32_t) * nleaves, cudaMemcpyDeviceToHost, st));
         ALG_CK(cudaStreamSynchronize(su));
+        ALG_CK(cudaStreamSynchronize(sw));
         ALG_CK(cudaStreamSynchronize(st));
         S.drained();
         for (int i : inorder) {

@@ -24,7 +24,7 @@ HM_ERR_BOX = 8
 HM_ERR_DEGENERATE = 9
 HM_ERR_NOT_POSDEF = 10
 HM_LR_KMAX = 96
-HM_SOLVE_TRSM, HM_SOLVE_LR, HM_SOLVE_DENSE, HM_SOLVE_INV = 0, 1, 2, 3
+HM_SOLVE_TRSM, HM_SOLVE_LR, HM_SOLVE_DENSE, HM_SOLVE_INV, HM_SOLVE_LTRSM = 0, 1, 2, 3, 4
 
 HM_KERNEL_CAUCHY, HM_KERNEL_COULOMB, HM_KERNEL_COULOMB_PRIME, HM_KERNEL_LOG = 0, 1, 2, 3
 HM_F64, HM_F32, HM_DF64 = 0, 1, 2

@@ -501,10 +501,13 @@ int hm_potrf_batched_async(int dtype, int nprob, const hm_potrf_problem *probs, 
      HM_SOLVE_DENSE  x[o2 : o2+n2) -= M^T x[o1 : o1+n1)       (A = M n1 x n2, ld)
      HM_SOLVE_INV    x[o1 : o1+n1) <- W^T x[..], W = R^{-1}  (A = W, n1 x n1 upper, ld;
                                                               n1 <= 256; from hm_trtri_batched)
+     HM_SOLVE_LTRSM  x[o1 : o1+n1) <- L^{-1} x[..], L = R^T  (A = L, n1 x n1 lower, ld;
+                                                              n1 <= 256: forward substitution
+                                                              reading L's columns contiguously)
    One CTA per column of B runs the ops in order.  HM_SOLVE_INV turns the
    serial forward substitution of a diagonal block into one parallel product
    (GB300's FP64 rate makes a one-warp substitution slow). */
-enum { HM_SOLVE_TRSM = 0, HM_SOLVE_LR = 1, HM_SOLVE_DENSE = 2, HM_SOLVE_INV = 3 };
+enum { HM_SOLVE_TRSM = 0, HM_SOLVE_LR = 1, HM_SOLVE_DENSE = 2, HM_SOLVE_INV = 3, HM_SOLVE_LTRSM = 4 };
 typedef struct {
     int32_t kind, r;
     int64_t o1, n1, o2, n2, ld, ld2;

@@ -202,7 +202,8 @@ def test_native_cholesky_matches_recursion(dt, n, leaf):
         assert rel(Rdn, A.todense(A.cholesky(T))) <= tol["fwd"]
     # the leaves carry their inverses, which solvetransposed applies
     leaves = [b for b, _, _ in Rn.leaves() if G._is_dense(b)]
-    assert all(getattr(b, "_hm_inverse", None) is not None for b in leaves if b.shape[0] <= 112)
+    nmax = 112 if dt == torch.float64 else 159        # leaves whose inverse hm_trtri_batched makes
+    assert all(getattr(b, "_hm_inverse", None) is not None for b in leaves if b.shape[0] <= nmax)
     b = np.random.default_rng(n + 1).standard_normal(n)
     x = host(G.solvetransposed(Rn, dev(b, dt)))
     assert rel(Rdn.T @ x, b) <= tol["solve"]
