@@ -1443,10 +1443,12 @@ int solve_run(int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t nc
 // drop only singular values below q eps(sigma_1)) and the update's SVD
 // truncates the sum.  R12 = R11^{-T} U runs through the left subtree's
 // forward-substitution schedule (its leaves as products with their inverses).
-// The A22 updates' truncated SVDs run on a second stream: a block updated at
-// node N is next needed when the factorisation reaches it, after N's whole
-// left part of A22, so the SVDs overlap with the chain of leaf factorisations
-// and solves.  The host reads a block's new rank (which sizes the problems
+// The A22 updates' truncated SVDs run on a pool of other streams, one launch
+// per level of A22's tree (the deepest, needed first, first; blocks of one
+// depth in the tree always on the same stream): a block updated
+// at node N is next needed when the factorisation reaches it, after the part
+// of A22 before it, so the SVDs overlap with the chain of leaf factorisations
+// and solves, and a large block's SVD does not hold up the small ones.  The host reads a block's new rank (which sizes the problems
 // that use it) only when it next uses the block, waiting on that update's
 // event; nothing else waits until the end.  Problem descriptors go to the
 // device from pinned host memory.
@@ -1557,6 +1559,7 @@ struct HChol {
     struct Node {
         int64_t off = 0;
         int inord = -1, leaf = -1, ob = 0, oe = 0;      // in-order position, leaf number, subtree's op range
+        int depth = 0;
         const T *U = nullptr, *s = nullptr, *V = nullptr;   // the current A12 (internal nodes)
         int64_t ldu = 1, ldv = 1;
         int r = 0;
@@ -1577,7 +1580,8 @@ struct HChol {
     int32_t *h_small = nullptr, *d_info = nullptr;       // h_small: pinned, ranks and pivot words read back
     unsigned *counter = nullptr;                         // hchol_gram's last-CTA counter
     std::vector<T *> lts;                                // per leaf: R^T for the forward substitutions
-    cudaStream_t su = nullptr;                           // the A22 updates' truncated SVDs
+    static constexpr int kUpdStreams = 8;
+    cudaStream_t sup[kUpdStreams] = {};                 // the A22 updates' truncated SVDs
     cudaStream_t sw = nullptr;                           // the leaves' inverses
     std::vector<cudaEvent_t> wev;                        // per node: its leaf inverse is done
     std::vector<cudaEvent_t> events;
@@ -1589,10 +1593,14 @@ struct HChol {
     HChol(const hm_hchol_node *nodes, int n, cudaStream_t s, HCholResult *r) : in(nodes), nn(n), st(s), res(r), S(s) {}
     ~HChol()
     {
-        for (cudaStream_t x : {su, sw}) {
+        for (cudaStream_t &x : sup) {
             if (!x) continue;
             cudaStreamSynchronize(x);                    // nothing in flight reads memory freed below
             cudaStreamDestroy(x);
+        }
+        if (sw) {
+            cudaStreamSynchronize(sw);
+            cudaStreamDestroy(sw);
         }
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         for (int32_t *p : pinned_ints) cudaFreeHost(p);
@@ -1683,6 +1691,7 @@ struct HChol {
                 seen[g.left] = seen[g.right] = 1;
                 nd[g.left].off = N.off;
                 nd[g.right].off = N.off + n1;
+                nd[g.left].depth = nd[g.right].depth = N.depth + 1;
                 f.stage = 1;
                 stack.push_back({g.left, 0});
             } else if (f.stage == 1) {
@@ -1712,7 +1721,7 @@ struct HChol {
     int setup(int root)
     {
         ALG_TRY(layout(root));
-        ALG_CK(cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking));
+        for (cudaStream_t &x : sup) ALG_CK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
         ALG_CK(cudaStreamCreateWithFlags(&sw, cudaStreamNonBlocking));
         res->out.assign(nn, hm_hchol_out{});
         lts.assign(nn, nullptr);
@@ -1918,11 +1927,38 @@ struct HChol {
             ALG_TRY(gemm_launch<T>((int)p2.size(), p2.data(), st, S));
         }
         if (inner.empty()) return HM_OK;
-        const int np = (int)inner.size();
-        for (int M : inner) ALG_TRY(resolve(M));
+        for (int M : inner) ALG_TRY(resolve(M));         // their previous updates are done
+        // one batch per level of the subtree, the deepest first (needed first)
+        std::vector<int> depth(inner.size());
+        int dmax = 0;
+        for (size_t k = 0; k < inner.size(); ++k) {
+            int dd = 0;
+            for (int64_t w = in[inner[k]].n; w < in[g.right].n; w *= 2) ++dd;
+            depth[k] = dd;
+            dmax = std::max(dmax, dd);
+        }
+        cudaEvent_t eh = nullptr;
+        ALG_TRY(new_event(&eh));
+        ALG_CK(cudaEventRecord(eh, st));
+        for (int lev = dmax; lev >= 0; --lev) {
+            std::vector<int> grp;
+            for (size_t k = 0; k < inner.size(); ++k)
+                if (depth[k] == lev) grp.push_back(inner[k]);
+            if (grp.empty()) continue;
+            ALG_TRY(svd_batch(grp, H, Vk, r, n2, b0, eh));
+        }
+        return HM_OK;
+    }
+
+    // the truncated SVDs of [U_M | V_p] diag(s_M ; -H) [V_M | V_q]^T for the
+    // blocks M of one level, on the next update stream once H is ready
+    int svd_batch(const std::vector<int> &grp, const T *H, const T *Vk, int r, int64_t n2, int64_t b0,
+                  cudaEvent_t eh)
+    {
+        const int np = (int)grp.size();
         std::vector<LrJob> jobs(np);
         for (int k = 0; k < np; ++k) {
-            const int M = inner[k];
+            const int M = grp[k];
             const hm_hchol_node &gm = in[M];
             const int64_t m1 = gm.n1, m2 = gm.n - gm.n1;
             const int rm = nd[M].r;
@@ -1947,21 +1983,19 @@ struct HChol {
             nd[M].s = sn;
             nd[M].V = Vn; nd[M].ldv = std::max<int64_t>(m2, 1);
         }
-        // the truncated SVDs run on the side stream once H and R12 are ready on
-        // the main one; the new ranks come back there too, and are waited for
-        // only where a block is next used (resolve)
         LrPlan pl;
         ALG_TRY(lr_svd_plan<T>(np, jobs.data(), pl));
-        cudaEvent_t eh = nullptr, es = nullptr;
-        ALG_TRY(new_event(&eh));
+        // blocks of one depth (one size) share a stream: their updates run in the
+        // order the factorisation needs them, never behind a larger block's
+        cudaStream_t sx = sup[nd[grp[0]].depth % kUpdStreams];
+        cudaEvent_t es = nullptr;
         ALG_TRY(new_event(&es));
-        ALG_CK(cudaEventRecord(eh, st));
-        ALG_CK(cudaStreamWaitEvent(su, eh, 0));
+        ALG_CK(cudaStreamWaitEvent(sx, eh, 0));
         LrJob *dj = nullptr;
         int64_t *doff = nullptr, *dcoff = nullptr;
         T *dws = nullptr;
         int *dr = nullptr;
-        S.st = su;
+        S.st = sx;
         int rc = S.put(jobs.data(), (size_t)np, &dj);
         if (!rc) rc = S.put(pl.off.data(), pl.off.size(), &doff);
         if (!rc) rc = S.put(pl.coff.data(), pl.coff.size(), &dcoff);
@@ -1969,15 +2003,15 @@ struct HChol {
         ALG_TRY(rc);
         ALG_TRY(S.zeros((size_t)pl.ws, &dws));
         ALG_TRY(S.zeros((size_t)np, &dr));
-        lr_svd_kernel<T><<<np, kThreads, pl.smem, su>>>(dj, doff, dcoff, dws, dr, pl.dmax);
+        lr_svd_kernel<T><<<np, kThreads, pl.smem, sx>>>(dj, doff, dcoff, dws, dr, pl.dmax);
         ALG_CK(cudaGetLastError());
         int32_t *slot = nullptr;
         ALG_TRY(pinned_words(np, &slot));
-        ALG_CK(cudaMemcpyAsync(slot, dr, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, su));
-        ALG_CK(cudaEventRecord(es, su));
+        ALG_CK(cudaMemcpyAsync(slot, dr, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, sx));
+        ALG_CK(cudaEventRecord(es, sx));
         for (int k = 0; k < np; ++k) {
-            nd[inner[k]].ev = es;
-            nd[inner[k]].slot = slot + k;
+            nd[grp[k]].ev = es;
+            nd[grp[k]].slot = slot + k;
         }
         return HM_OK;
     }
@@ -2030,7 +2064,7 @@ struct HChol {
         ALG_TRY(setup(root));
         ALG_TRY(node(root));
         ALG_CK(cudaMemcpyAsync(h_small, d_info, sizeof(int32_t) * nleaves, cudaMemcpyDeviceToHost, st));
-        ALG_CK(cudaStreamSynchronize(su));
+        for (cudaStream_t x : sup) ALG_CK(cudaStreamSynchronize(x));
         ALG_CK(cudaStreamSynchronize(sw));
         ALG_CK(cudaStreamSynchronize(st));
         S.drained();
