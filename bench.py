@@ -398,6 +398,14 @@ def run_cholesky(hm, torch, dev, args, n=16384, leaf=64):
         R = algebra.hierarchicalcholesky(A)
     torch.cuda.synchronize()
     ms = (time.perf_counter() - t0) / reps * 1e3
+    # the same recursion driven block operation by block operation from Python
+    # (hierarchicalcholesky(A, native=False)), one run, for comparison
+    algebra.hierarchicalcholesky(A, native=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    algebra.hierarchicalcholesky(A, native=False)
+    torch.cuda.synchronize()
+    rec_ms = (time.perf_counter() - t0) * 1e3
     b = torch.randn(n, device=dev, dtype=torch.float64)
     algebra.solvetransposed(R, b)
     torch.cuda.synchronize()
@@ -415,7 +423,9 @@ def run_cholesky(hm, torch, dev, args, n=16384, leaf=64):
     return {"workload": f"hierarchicalcholesky of K + 1e-2 I, K Gaussian exp(-(x-y)^2/(2*0.15^2)) on n={n} sorted "
                         f"uniform points, leaf {leaf}, off-diagonal LowRankMatrix blocks at 1e-12, FP64; "
                         "then solvetransposed of one vector",
-            "n": n, "ms_per_factorization": ms, "factorizations_per_s": 1e3 / ms, "solve_ms": solve_ms,
+            "path": "hm_hchol_factor (native recursion, A22-update SVDs on a stream pool)",
+            "n": n, "ms_per_factorization": ms, "factorizations_per_s": 1e3 / ms,
+            "ms_block_by_block_from_python": rec_ms, "solve_ms": solve_ms,
             "max_rank_A": tree_ranks(A), "max_rank_R": tree_ranks(R), "solve_rel_residual_leading_2048": resid,
             "reps": reps, "cpu_baseline": cpu}
 

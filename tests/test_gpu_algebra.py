@@ -217,6 +217,40 @@ def test_native_cholesky_matches_recursion(dt, n, leaf):
 
 
 @pytest.mark.parametrize("dt", DT)
+def test_solve_ops_agree(dt):
+    """hm_solve_transposed with a diagonal leaf given four ways: R (HM_SOLVE_TRSM),
+    R^{-1} (HM_SOLVE_INV), R^T (HM_SOLVE_LTRSM, staged in shared memory up to 64
+    rows, read from global memory above) and against numpy's R^{-T} b; the
+    low-rank update between two leaves as in src/cholesky.jl:142-228."""
+    import ctypes
+    from hierarchicalmatrices import _lib
+    rng = np.random.default_rng(23)
+    tol = 1e-12 if dt == torch.float64 else 2e-5
+    for n1, n2 in ((40, 64), (100, 70)):
+        R1 = np.triu(rng.standard_normal((n1, n1))) + 4 * np.eye(n1)
+        R2 = np.triu(rng.standard_normal((n2, n2))) + 4 * np.eye(n2)
+        U, sg, V = rng.standard_normal((n1, 3)), rng.random(3), rng.standard_normal((n2, 3))
+        b = rng.standard_normal((n1 + n2, 2))
+        x1 = np.linalg.solve(R1.T, b[:n1])
+        x2 = np.linalg.solve(R2.T, b[n1:] - V @ (sg[:, None] * (U.T @ x1)))
+        ref = np.vstack([x1, x2])
+        keep = [dev(m, dt) for m in (R1, R2, np.linalg.inv(R1), np.linalg.inv(R2), R1.T.copy(), R2.T.copy(), U, sg, V)]
+        d = dict(zip(("R1", "R2", "W1", "W2", "L1", "L2", "U", "s", "V"), keep))
+        for kind, a1, a2 in ((_lib.HM_SOLVE_TRSM, "R1", "R2"), (_lib.HM_SOLVE_INV, "W1", "W2"),
+                             (_lib.HM_SOLVE_LTRSM, "L1", "L2")):
+            ops = (_lib.SolveOp * 3)()
+            ops[0].kind, ops[0].o1, ops[0].n1, ops[0].A, ops[0].ld = kind, 0, n1, d[a1].data_ptr(), n1
+            ops[1].kind, ops[1].r, ops[1].o1, ops[1].n1, ops[1].o2, ops[1].n2 = _lib.HM_SOLVE_LR, 3, 0, n1, n1, n2
+            ops[1].A, ops[1].ld, ops[1].s, ops[1].B, ops[1].ld2 = d["U"].data_ptr(), n1, d["s"].data_ptr(), d["V"].data_ptr(), n2
+            ops[2].kind, ops[2].o1, ops[2].n1, ops[2].A, ops[2].ld = kind, n1, n2, d[a2].data_ptr(), n2
+            X = dev(b, dt)
+            _lib.check(_lib.lib.hm_solve_transposed(_lib.HM_F64 if dt == torch.float64 else _lib.HM_F32, 3, ops,
+                                                     ctypes.c_void_p(X.data_ptr()), X.stride(1), 2, None))
+            torch.cuda.synchronize()
+            assert rel(host(X), ref) <= tol, (kind, n1)
+
+
+@pytest.mark.parametrize("dt", DT)
 def test_trtri_batched(dt):
     """hm_trtri_batched: W = R^{-1} of upper triangular blocks (the inverses
     solvetransposed applies to small diagonal leaves) against numpy's inverse."""
