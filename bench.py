@@ -336,14 +336,16 @@ def run_batch(hm, torch, dev, args, count=512, nrhs=8):
 
 # ----------------------------------------------------------------- gradients
 
-def spd_hodlr_gauss(hm, torch, dev, n, leaf, ell=0.15, shift=1e-2, tol=1e-12, seed=21):
+def spd_hodlr_gauss(hm, torch, dev, n, leaf, ell=0.15, shift=1e-2, tol=1e-12, seed=21, host_linalg=False):
     """A synthetic symmetric positive definite HierarchicalMatrix of the shape
     src/cholesky.jl factors: K(x_i, x_j) = exp(-(x_i - x_j)^2 / (2 ell^2)) +
     shift I on n sorted uniform points of [0, 1], halved recursively down to
     dense diagonal leaves of at most `leaf` rows, each upper off-diagonal
     block a LowRankMatrix (its singular values above tol times the largest,
     found on the device by a randomized range finder with two power steps),
-    the lower block unassigned.  FP64, built on the device (setup, untimed)."""
+    the lower block unassigned.  FP64, built on the device (setup, untimed);
+    host_linalg: the range finder's QR and SVD in numpy instead (torch.linalg
+    does not load under ncu)."""
     g = torch.Generator(device=dev).manual_seed(seed)
     x = torch.sort(torch.rand(n, generator=g, device=dev, dtype=torch.float64)).values
 
@@ -360,10 +362,22 @@ def spd_hodlr_gauss(hm, torch, dev, n, leaf, ell=0.15, shift=1e-2, tol=1e-12, se
         mid = (i0 + i1) // 2
         B = kblock(i0, mid, mid, i1)
         k = min(96, B.shape[0], B.shape[1])
-        Q = torch.linalg.qr(B @ torch.randn(B.shape[1], k, generator=g, device=dev, dtype=torch.float64))[0]
+        if host_linalg:
+            def qr(M):
+                return torch.tensor(np.linalg.qr(M.cpu().numpy())[0], device=dev)
+
+            def svd(M):
+                return [torch.tensor(t, device=dev) for t in np.linalg.svd(M.cpu().numpy(), full_matrices=False)]
+        else:
+            def qr(M):
+                return torch.linalg.qr(M)[0]
+
+            def svd(M):
+                return torch.linalg.svd(M, full_matrices=False)
+        Q = qr(B @ torch.randn(B.shape[1], k, generator=g, device=dev, dtype=torch.float64))
         for _ in range(2):
-            Q = torch.linalg.qr(B @ (B.t() @ Q))[0]
-        Uc, S, Vt = torch.linalg.svd(Q.t() @ B, full_matrices=False)
+            Q = qr(B @ (B.t() @ Q))
+        Uc, S, Vt = svd(Q.t() @ B)
         r = int((S > tol * S[0]).sum())
         H = hm.HierarchicalMatrix(2, 2)
         H[hm.Block(1), hm.Block(1)] = build(i0, mid)
@@ -515,7 +529,16 @@ def run_grad(hm, torch, dev, args, n=65536):
 
 
 def profile_case(hm, torch, args):
-    """Three products of one workload, for ncu captures (no timing)."""
+    """Three products of one workload, for ncu captures (no timing); the
+    hierarchical Cholesky case factors the bench's n = 16384 matrix twice."""
+    if args.profile_case == "cholesky":
+        from hierarchicalmatrices import algebra
+        A = spd_hodlr_gauss(hm, torch, "cuda", 16384, 64, host_linalg=True)
+        for _ in range(2):
+            algebra.hierarchicalcholesky(A)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "cholesky", "n": 16384, "ok": True}), flush=True)
+        return 0
     n = args.n
     x, y = grid_points(n)
     case = args.profile_case
@@ -565,11 +588,12 @@ def main():
     ap.add_argument("--autotune-reps", type=int, default=50,
                     help="products timed per candidate schedule by the autotuner (fewer for profiling runs)")
     ap.add_argument("--profile-case", default=None,
-                    choices=["headline", "fp64", "df64", "k8", "k32", "k256"],
+                    choices=["headline", "fp64", "df64", "k8", "k32", "k256", "cholesky"],
                     help="run three products of one workload at --n points and exit (for ncu captures): the "
                          "headline FP32 product with the autotuner's choice for it (near field after the leaf "
                          "stage, programmatic launches), the FP64 / FP64-double-float product, or FP32 with 8, 32 "
-                         "or 256 right-hand sides with every stage on one stream")
+                         "or 256 right-hand sides with every stage on one stream; or two hierarchical Cholesky "
+                         "factorisations of the bench's n = 16384 matrix")
     ap.add_argument("--wide-tree", default=None, choices=["off", "on", "all"],
                     help="HM_OPT_WIDE_TREE for --profile-case and --only-batch runs")
     args = ap.parse_args()
