@@ -216,6 +216,36 @@ def test_native_cholesky_matches_recursion(dt, n, leaf):
     assert torch.isfinite(U).all()
 
 
+def test_native_cholesky_edge_cases():
+    """hm_hchol_factor on trees the driver handles by its other paths: leaves
+    of 200 rows (beyond the fused leaf kernel: the batched Cholesky kernel and
+    substitution by R in the solves, no inverse) and blocks of rank 0 (R12 of
+    rank 0, no update), against the oracle's factor."""
+    dt = torch.float64
+    T, D = A.spd_hodlr(1600, 200, kernel="gauss", seed=31)
+    R = G.hierarchicalcholesky(tree_dev(T, dt))
+    Rd = A.todense(tree_host(R))
+    assert rel(Rd, A.todense(A.cholesky(T))) <= CHOL[dt]["fwd"]
+    assert rel(Rd.T @ Rd, D) <= CHOL[dt]["bwd"]
+    # rank 0: a block-diagonal SPD matrix whose upper blocks are empty LowRankMatrix
+    T, D = A.spd_hodlr(512, 64, kernel="gauss", seed=32)
+
+    def zero_blocks(B):
+        if isinstance(B, A.HB):
+            B.blocks[0][1] = A.LR(np.zeros((B.blocks[0][1].U.shape[0], 0)), np.zeros(0),
+                                  np.zeros((B.blocks[0][1].V.shape[0], 0)))
+            zero_blocks(B.blocks[0][0])
+            zero_blocks(B.blocks[1][1])
+    zero_blocks(T)
+    D = A.todense(T)
+    D = np.triu(D) + np.triu(D, 1).T
+    R = G.hierarchicalcholesky(tree_dev(T, dt))
+    Rd = A.todense(tree_host(R))
+    assert rel(Rd.T @ Rd, D) <= CHOL[dt]["bwd"]
+    assert rel(Rd, A.todense(A.cholesky(T))) <= CHOL[dt]["fwd"]
+    assert all(b.U.shape[1] == 0 for b, _, _ in R.leaves() if isinstance(b, hm.LowRankMatrix))
+
+
 @pytest.mark.parametrize("dt", DT)
 def test_solve_ops_agree(dt):
     """hm_solve_transposed with a diagonal leaf given four ways: R (HM_SOLVE_TRSM),
