@@ -242,7 +242,8 @@ struct LrJob {
 // when core_off < 0, else at ws + core_off for cores too large for it.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const LrJob *jobs, const int64_t *ws_off,
-                                                          const int64_t *core_off, T *ws, int *ranks, int64_t d_elems)
+                                                          const int64_t *core_off, T *ws, int *ranks, int64_t d_elems,
+                                                          int64_t xoff)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const hm_lr_problem pr = jobs[blockIdx.x].p;
@@ -398,8 +399,28 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const LrJob *jobs, con
             for (int64_t e = tid; e < (int64_t)p * q; e += kThreads) D[e] *= sc;
         __syncthreads();
     }
+    // QR preconditioning (cores in shared memory, q >= 4, formed from QR'd
+    // factors): D = Q R, and the Jacobi sweeps run on X = R^T, whose columns
+    // are far closer to orthogonal for the graded spectra of low-rank sums
+    // (about half the sweeps); then D = (Q J) Sigma U_x^T with X J = U_x Sigma.
+    // The Xm^T Ym cores of L1' * L2 gain fewer sweeps than the QR costs.
+    const bool pre = co < 0 && xoff >= 0 && q >= 4 && !pr.Xm;
+    T *Xs = nullptr, *Lf = nullptr, *tq = nullptr;
+    if (pre) {
+        Xs = reinterpret_cast<T *>(smem_raw) + xoff;   // q x q
+        Lf = Xs + (int64_t)q * q;                      // p x q
+        tq = Lf + (int64_t)p * q;                      // q
+        house_qr(D, (int64_t)p, q, tq);
+        for (int e = tid; e < q * q; e += kThreads) {
+            const int i = e % q, j = e / q;
+            Xs[e] = i >= j ? D[j + (int64_t)p * i] : T(0);
+        }
+        __syncthreads();
+    }
+    T *const Dj = pre ? Xs : D;
+    const int pj = pre ? q : p;
     const int qq = (q + 1) & ~1, npairs = qq / 2;
-    const int G = p <= 32 ? 8 : (p <= 64 ? 16 : 32);
+    const int G = pj <= 32 ? 8 : (pj <= 64 ? 16 : 32);
     const int gpw = 32 / G, lg = lane & (G - 1), grp = lane / G;
     const T eps2 = Lim<T>::eps * Lim<T>::eps;
     for (int sweep = 0; sweep < kJacobiSweeps; ++sweep) {
@@ -415,10 +436,10 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const LrJob *jobs, con
                     if (i > j) { const int tmp = i; i = j; j = tmp; }
                 }
                 const bool live = j < q;
-                T *di = D + (int64_t)p * i, *dj = D + (int64_t)p * (live ? j : i);
+                T *di = Dj + (int64_t)pj * i, *dj = Dj + (int64_t)pj * (live ? j : i);
                 T al = 0, be = 0, ga = 0;
                 if (live)
-                    for (int r = lg; r < p; r += G) {
+                    for (int r = lg; r < pj; r += G) {
                         const T u = di[r], v = dj[r];
                         al = fma(u, u, al); be = fma(v, v, be); ga = fma(u, v, ga);
                     }
@@ -430,7 +451,7 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const LrJob *jobs, con
                 if (!live || al == T(0) || be == T(0) || !(ga * ga > eps2 * al * be)) continue;
                 T c, sn;
                 if (!jacobi_rotation(al, be, ga, c, sn)) continue;
-                for (int r = lg; r < p; r += G) {
+                for (int r = lg; r < pj; r += G) {
                     const T u = di[r], v = dj[r];
                     di[r] = c * u - sn * v;
                     dj[r] = sn * u + c * v;
@@ -448,6 +469,27 @@ __global__ void __launch_bounds__(kThreads) lr_svd_kernel(const LrJob *jobs, con
         const int any = s_flag;
         __syncthreads();
         if (!any) break;
+    }
+    if (pre) {
+        // D's columns become Q [J_j; 0] sigma_j (sigma_j = |X_j|) and J's X_j / sigma_j,
+        // the form the unpreconditioned sweeps leave
+        for (int j = warp; j < q; j += kWarps) {
+            const T *xj = Xs + (int64_t)q * j;
+            T ss = 0;
+            for (int r = lane; r < q; r += 32) ss = fma(xj[r], xj[r], ss);
+            const T sgm = sqrt(warp_sum(ss));
+            T *y = Lf + (int64_t)p * j;
+            T *jc = J + (int64_t)q * j;
+            for (int i = lane; i < p; i += 32) y[i] = i < q ? jc[i] : T(0);
+            __syncwarp();
+            apply_q(D, (int64_t)p, q, tq, y);
+            for (int i = lane; i < p; i += 32) y[i] *= sgm;
+            const T inv = sgm > T(0) ? T(1) / sgm : T(0);
+            for (int r = lane; r < q; r += 32) jc[r] = sgm > T(0) ? xj[r] * inv : (r == j ? T(1) : T(0));
+        }
+        __syncthreads();
+        for (int e = tid; e < p * q; e += kThreads) D[e] = Lf[e];
+        __syncthreads();
     }
 
     // 4. singular values, descending order, getrank
@@ -1139,11 +1181,14 @@ int set_smem(K kernel, size_t bytes)
 
 // Cores whose storage exceeds this many bytes run from the global workspace.
 constexpr size_t kCoreSmemBytes = 200 * 1024;
+// Cores whose storage with the QR preconditioner's fits in this many bytes
+// are preconditioned.
+constexpr size_t kPreconSmemBytes = 224 * 1024;
 
 // Workspace layout and shared memory of one lr_svd launch.
 struct LrPlan {
     std::vector<int64_t> off, coff;
-    int64_t ws = 0, dmax = 1;
+    int64_t ws = 0, dmax = 1, xoff = -1;
     size_t smem = 0;
 };
 
@@ -1152,7 +1197,7 @@ int lr_svd_plan(int nprob, const LrJob *jobs, LrPlan &pl)
 {
     pl.off.assign(nprob, 0);
     pl.coff.assign(nprob, -1);
-    int64_t ws = 0, dmax = 1, jmax = 1;
+    int64_t ws = 0, dmax = 1, jmax = 1, xmax = 0;
     int qmax = 1;
     for (int i = 0; i < nprob; ++i) {
         const hm_lr_problem &p = jobs[i].p;
@@ -1201,6 +1246,7 @@ int lr_svd_plan(int nprob, const LrJob *jobs, LrPlan &pl)
             dmax = std::max(dmax, pp * q);
             jmax = std::max(jmax, jn);
             qmax = std::max<int>(qmax, (int)q);
+            xmax = std::max(xmax, q * q + pp * q + q);
         } else {
             pl.coff[i] = ws;
             ws += pp * q + jn + 2 * q;          // sigma (q values) and the order (q ints) after J
@@ -1209,8 +1255,14 @@ int lr_svd_plan(int nprob, const LrJob *jobs, LrPlan &pl)
     }
     pl.ws = std::max<int64_t>(ws, 1);
     pl.dmax = dmax;
-    // J also holds sigma (q values) and the sort order (q ints) after it
+    // J also holds sigma (q values) and the sort order (q ints) after it; then,
+    // when it fits, the QR preconditioner's area (R^T, Q J and the reflectors' tau)
     pl.smem = (size_t)(dmax + jmax + qmax) * sizeof(T) + (size_t)qmax * sizeof(int) + 64;
+    const int64_t xoff = (int64_t)((pl.smem + sizeof(T) - 1) / sizeof(T));
+    if (xmax > 0 && (size_t)(xoff + xmax) * sizeof(T) <= kPreconSmemBytes) {
+        pl.xoff = xoff;
+        pl.smem = (size_t)(xoff + xmax) * sizeof(T);
+    }
     return set_smem(lr_svd_kernel<T>, pl.smem);
 }
 
@@ -1232,7 +1284,7 @@ int lr_svd_run(int nprob, const hm_lr_problem *probs, int32_t *ranks, cudaStream
     ALG_TRY(S.put(pl.coff.data(), pl.coff.size(), &d_coff));
     ALG_TRY(S.zeros((size_t)pl.ws, &d_ws));
     ALG_TRY(S.zeros((size_t)nprob, &d_ranks));
-    lr_svd_kernel<T><<<nprob, kThreads, pl.smem, st>>>(d_jobs, d_off, d_coff, d_ws, d_ranks, pl.dmax);
+    lr_svd_kernel<T><<<nprob, kThreads, pl.smem, st>>>(d_jobs, d_off, d_coff, d_ws, d_ranks, pl.dmax, pl.xoff);
     ALG_CK(cudaGetLastError());
     std::vector<int> hr(nprob);
     ALG_CK(cudaMemcpyAsync(hr.data(), d_ranks, nprob * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -2003,7 +2055,7 @@ struct HChol {
         ALG_TRY(rc);
         ALG_TRY(S.zeros((size_t)pl.ws, &dws));
         ALG_TRY(S.zeros((size_t)np, &dr));
-        lr_svd_kernel<T><<<np, kThreads, pl.smem, sx>>>(dj, doff, dcoff, dws, dr, pl.dmax);
+        lr_svd_kernel<T><<<np, kThreads, pl.smem, sx>>>(dj, doff, dcoff, dws, dr, pl.dmax, pl.xoff);
         ALG_CK(cudaGetLastError());
         int32_t *slot = nullptr;
         ALG_TRY(pinned_words(np, &slot));
