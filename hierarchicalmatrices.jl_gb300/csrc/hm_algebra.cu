@@ -1497,13 +1497,13 @@ int solve_run(int nops, const hm_solve_op *ops, void *B, int64_t ldb, int64_t nc
 // forward-substitution schedule (its leaves as products with their inverses).
 // The A22 updates' truncated SVDs run on a pool of other streams, one launch
 // per level of A22's tree (the deepest, needed first, first; blocks of one
-// depth in the tree always on the same stream): a block updated
-// at node N is next needed when the factorisation reaches it, after the part
-// of A22 before it, so the SVDs overlap with the chain of leaf factorisations
-// and solves, and a large block's SVD does not hold up the small ones.  The host reads a block's new rank (which sizes the problems
-// that use it) only when it next uses the block, waiting on that update's
-// event; nothing else waits until the end.  Problem descriptors go to the
-// device from pinned host memory.
+// depth in the tree always on the same stream): a block updated at node N is
+// next needed when the factorisation reaches it, after the part of A22 before
+// it, so the SVDs overlap with the chain of leaf factorisations and solves,
+// and a large block's SVD does not hold up the small ones.  The host reads a
+// block's new rank (which sizes the problems that use it) only when it next
+// uses the block, waiting on that update's event; nothing else waits until the
+// end.  Problem descriptors go to the device from pinned host memory.
 
 // Device memory handed out in 256-byte aligned pieces from chunks of at
 // least 32 MB, all released together.
