@@ -885,9 +885,17 @@ int launch_tree_qc(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, A 
         if constexpr (std::is_same<S, double>::value && std::is_same<A, double>::value) {
             if (h->n_m2l_rows && h->storage == HM_DF64) {
                 // far-field blocks as double-float pairs: every right-hand side in one launch
-                HM_TRY(launch_k("m2l_df", m2l_df, dim3((unsigned)((h->n_m2l_rows + 7) / 8)), dim3(256), 0, st,
-                                pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents,
-                                static_cast<const float2 *>(h->d_F), h->fstride, t, s, r, k));
+                if (r == 20) {
+                    const size_t rsm = (size_t)kM2lDfWarps * kM2lDfStages * 400 * sizeof(float2);
+                    HM_TRY(launch_k("m2l_df_ring", m2l_df_ring<kM2lDfStages>,
+                                    dim3((unsigned)((h->n_m2l_rows + kM2lDfWarps - 1) / kM2lDfWarps)),
+                                    dim3(kM2lDfWarps * 32), rsm, st, pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows,
+                                    h->d_m2l_ents, static_cast<const float2 *>(h->d_F), t, s, k));
+                } else {
+                    HM_TRY(launch_k("m2l_df", m2l_df, dim3((unsigned)((h->n_m2l_rows + 7) / 8)), dim3(256), 0, st,
+                                    pdl_on && chain, h->d_m2l_rows, h->n_m2l_rows, h->d_m2l_ents,
+                                    static_cast<const float2 *>(h->d_F), h->fstride, t, s, r, k));
+                }
                 chain = true;
                 done = true;
             }

@@ -254,6 +254,74 @@ __device__ __forceinline__ void m2l_df_r20(const hm_m2l_row &R, const hm_m2l_ent
 }
 }  // namespace
 
+// Rank 20 with a per-warp ring of kM2lDfStages blocks of F in shared memory
+// filled by cp.async: a warp keeps two blocks (6.4 KB) in flight instead of
+// one in registers, and without the 40 registers of the register copy more
+// warps fit on an SM (four per CTA, 38.4 KB of ring per CTA).
+template <int NS>
+__global__ void __launch_bounds__(kM2lDfWarps * 32)
+    m2l_df_ring(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, const double *t,
+                double *s, int k)
+{
+    extern __shared__ __align__(16) unsigned char m2l_smem[];
+    __shared__ float2 tsh[kM2lDfWarps][32];
+    constexpr int R20 = 20, BLK = R20 * R20;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * kM2lDfWarps + wib;
+    pdl_trigger();
+    pdl_wait();                                                // the upward pass's coefficients are ready
+    if (w >= (int64_t)nrows) return;
+    float2 *ring = reinterpret_cast<float2 *>(m2l_smem) + (size_t)wib * NS * BLK;
+    float2 *ts = tsh[wib];
+    const hm_m2l_row R = rows[w];
+    const int ne = R.end - R.begin;
+    auto issue = [&](int i, int stage) {
+        const hm_m2l_ent E = ents[R.begin + i];
+        float2 *dst = ring + stage * BLK;
+        const float2 *src = F + E.foff;
+        if ((E.foff & 1) == 0) {
+            for (int c = lane; c < BLK / 2; c += 32) async_copy16(dst + 2 * c, src + 2 * c);
+        } else {
+            for (int c = lane; c < BLK; c += 32) async_copy<8>(dst + c, src + c);
+        }
+    };
+    for (int q = 0; q < k; ++q) {
+        float sh = 0.f, sl = 0.f;
+        double tc = 0.0;
+        if (ne > 0 && lane < R20) tc = t[((int64_t)ents[R.begin].yslot * k + q) * R20 + lane];
+#pragma unroll
+        for (int i = 0; i < NS - 1; ++i) {
+            if (i < ne) issue(i, i);
+            async_commit();
+        }
+        for (int e = 0; e < ne; ++e) {
+            const int ei = e + NS - 1;
+            if (ei < ne) issue(ei, ei % NS);
+            async_commit();
+            asm volatile("cp.async.wait_group %0;" ::"n"(NS - 1) : "memory");
+            if (lane < R20) ts[lane] = df_split(tc);
+            __syncwarp();                                      // block e and the coefficients visible
+            double tn = 0.0;
+            if (e + 1 < ne && lane < R20) tn = t[((int64_t)ents[R.begin + e + 1].yslot * k + q) * R20 + lane];
+            if (lane < R20) {
+                const float2 *f = ring + (e % NS) * BLK + lane;
+#pragma unroll
+                for (int n = 0; n < R20; ++n) {
+                    const float2 v = f[R20 * n];
+                    df_fma(sh, sl, v.x, v.y, ts[n].x, ts[n].y);
+                }
+            }
+            __syncwarp();                                      // the stage and ts are free again
+            tc = tn;
+        }
+        async_wait_all();
+        __syncwarp();
+        if (lane < R20) s[((int64_t)R.slot * k + q) * R20 + lane] = __dadd_rn((double)sh, (double)sl);
+    }
+}
+template __global__ void m2l_df_ring<kM2lDfStages>(const hm_m2l_row *, int, const hm_m2l_ent *, const float2 *,
+                                                   const double *, double *, int);
+
 __global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, int fstride,
                        const double *t, double *s, int r, int k)
 {

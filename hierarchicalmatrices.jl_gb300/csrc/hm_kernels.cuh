@@ -287,6 +287,12 @@ __global__ void leaf_up_df(MulArgs<double> ma, const hm_vpanel *vp, int npanels,
                            int cap);
 __global__ void m2l_df(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, int fstride,
                        const double *t, double *s, int r, int k);
+// m2l_df_ring: rank 20, kM2lDfWarps warps per CTA (one per row slot), each with
+// a ring of NS blocks of F in shared memory (NS * 3.2 KB per warp).
+constexpr int kM2lDfWarps = 4, kM2lDfStages = 3;
+template <int NS>
+__global__ void m2l_df_ring(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const float2 *F, const double *t,
+                            double *s, int k);
 // far_rows_df: far-field rows of right-hand side q0, one thread per row, four
 // segments of at most 64 rows per CTA of 256 threads (at most 64 far columns).
 __global__ void far_rows_df(MulArgs<double> ma, const hm_seg *segs, int nsegs, const hm_piece *pieces,
