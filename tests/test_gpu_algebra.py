@@ -246,6 +246,34 @@ def test_native_cholesky_edge_cases():
     assert all(b.U.shape[1] == 0 for b, _, _ in R.leaves() if isinstance(b, hm.LowRankMatrix))
 
 
+def test_native_cholesky_releases_memory():
+    """The factor's memory (held by its tensors) and the driver's temporary
+    arenas, streams and staging buffers are all released: device memory
+    returns to its level after repeated factorisations once the factors are
+    dropped, also after a factorisation that fails."""
+    import gc
+    dt = torch.float64
+    T, _ = A.spd_hodlr(2048, 64, kernel="gauss", seed=33)
+    Td = tree_dev(T, dt)
+    Tb, _ = A.spd_hodlr(512, 64, seed=34)
+    Tb.blocks[0][0].blocks[0][0].blocks[0][0][0, 0] = -1.0
+    Tbd = tree_dev(Tb, dt)                          # torch's own allocations before the baseline
+    R = G.hierarchicalcholesky(Td)                  # warm-up: modules, attributes
+    del R
+    gc.collect()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        R = G.hierarchicalcholesky(Td)
+        assert R.blocksize() == (2, 2)
+        del R
+    with pytest.raises(np.linalg.LinAlgError):
+        G.hierarchicalcholesky(Tbd)
+    gc.collect()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 @pytest.mark.parametrize("dt", DT)
 def test_solve_ops_agree(dt):
     """hm_solve_transposed with a diagonal leaf given four ways: R (HM_SOLVE_TRSM),
