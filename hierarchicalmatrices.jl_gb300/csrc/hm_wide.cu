@@ -8,7 +8,8 @@
 // a step (an R x R far-field block F, a transfer matrix, or R-value rows of a
 // basis panel) is read from shared memory as 16-byte broadcasts and the
 // right-hand side's own values as one 16-byte read per four, so about four of
-// five instructions are FMAs.  All are small GEMMs:
+// five FMA-or-load steps are FMAs; in FP32 each two adjacent FMAs go out as
+// one packed FP32x2 FMA.  All are small GEMMs:
 //   m2l_w:       s[slot][q][:] = sum_e F_e t[yslot_e][q][:]         (R x R times R)
 //   leaf_up_w:   t[slot][q][:] = V^T x[rows][q]                      (R x nrows times nrows)
 //   xfer_task_w: t[parent] = sum_c T_c^T t[child_c], s[child_c] += T_c s[parent]
@@ -35,6 +36,21 @@ __device__ __forceinline__ void ld4(const double *p, double *v)
     const double2 a = *reinterpret_cast<const double2 *>(p);
     const double2 b = *reinterpret_cast<const double2 *>(p + 2);
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+// acc[i] = fma(f[i], x, acc[i]) for i < 4.  FP32 runs it as two packed
+// FP32x2 FMAs (__ffma2_rn, each half rounded as fmaf: the same sums in half
+// the FMA instructions).
+__device__ __forceinline__ void axpy4(const float *f, float x, float *acc)
+{
+    const float2 xx = make_float2(x, x);
+    const float2 a = __ffma2_rn(make_float2(f[0], f[1]), xx, make_float2(acc[0], acc[1]));
+    const float2 b = __ffma2_rn(make_float2(f[2], f[3]), xx, make_float2(acc[2], acc[3]));
+    acc[0] = a.x; acc[1] = a.y; acc[2] = b.x; acc[3] = b.y;
+}
+__device__ __forceinline__ void axpy4(const double *f, double x, double *acc)
+{
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i] = fma(f[i], x, acc[i]);
 }
 template <typename A>
 __device__ __forceinline__ void st4(A *p, const A *v);
@@ -137,9 +153,7 @@ __global__ void __launch_bounds__(kWideWarps * 32)
                     A f[4];
                     ld4(col + m, f);
 #pragma unroll
-                    for (int p = 0; p < QPL; ++p)
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) acc[p][m + i] = fma(f[i], tv[p][u], acc[p][m + i]);
+                    for (int p = 0; p < QPL; ++p) axpy4(f, tv[p][u], acc[p] + m);
                 }
             }
         }
@@ -237,9 +251,7 @@ __global__ void __launch_bounds__(kWideWarps * 32)
                 A v[4];
                 ld4(row + m, v);
 #pragma unroll
-                for (int p = 0; p < QPL; ++p)
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) acc[p][m + i] = fma(v[i], xv[p][u], acc[p][m + i]);
+                for (int p = 0; p < QPL; ++p) axpy4(v, xv[p][u], acc[p] + m);
             }
         }
     }
@@ -335,8 +347,8 @@ __global__ void __launch_bounds__(kWideTaskThreads)
                             A t0[4], t1[4];
                             ld4(Ts + (mp + u) * R + m, t0);
                             ld4(Ts + R * R + (mp + u) * R + m, t1);
-#pragma unroll
-                            for (int i = 0; i < 4; ++i) acc[m + i] = fma(t1[i], b[u], fma(t0[i], a[u], acc[m + i]));
+                            axpy4(t0, a[u], acc + m);
+                            axpy4(t1, b[u], acc + m);
                         }
                     }
                 }
@@ -369,11 +381,8 @@ __global__ void __launch_bounds__(kWideTaskThreads)
                             A t0[4], t1[4];
                             ld4(Ts + (m + u) * R + mq, t0);
                             ld4(Ts + R * R + (m + u) * R + mq, t1);
-#pragma unroll
-                            for (int i = 0; i < 4; ++i) {
-                                a0[mq + i] = fma(t0[i], pv[u], a0[mq + i]);
-                                a1[mq + i] = fma(t1[i], pv[u], a1[mq + i]);
-                            }
+                            axpy4(t0, pv[u], a0 + mq);
+                            axpy4(t1, pv[u], a1 + mq);
                         }
                     }
                 }
