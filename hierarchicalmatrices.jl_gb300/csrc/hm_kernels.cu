@@ -1023,7 +1023,20 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int q = 0; q < KB; ++q) acc[q] = A(0);
     const S *pr = P + G.poff + row;
-    for (int c = 0; c < nfar; ++c) {
+    // eight columns' loads issued before their FMAs (eight loads in flight per
+    // thread), the sums in column order as one column at a time
+    constexpr int CU = 8;
+    int c = 0;
+    for (; c + CU <= nfar; c += CU) {
+        A u[CU];
+#pragma unroll
+        for (int i = 0; i < CU; ++i) u[i] = (A)__ldcs(pr + (int64_t)(c + i) * G.ld);
+#pragma unroll
+        for (int i = 0; i < CU; ++i)
+#pragma unroll
+            for (int q = 0; q < KB; ++q) acc[q] = fma(u[i], cs[ls][(c + i) * KB + q], acc[q]);
+    }
+    for (; c < nfar; ++c) {
         const A u = (A)__ldcs(pr + (int64_t)c * G.ld);
 #pragma unroll
         for (int q = 0; q < KB; ++q) acc[q] = fma(u, cs[ls][c * KB + q], acc[q]);
