@@ -60,9 +60,13 @@ enum {
    KernelMatrix builds only (not hm_hier_build). */
 enum { HM_F64 = 0, HM_F32 = 1, HM_DF64 = 2 };
 
+/* Error reporting (the reference raises Julia exceptions instead: BoundsError
+   from indsplit, src/BarycentricMatrix.jl:299-307, and AssertionError from
+   update!, :249-250).  Name of a status code. */
 const char *hm_status_string(int status);
 /* Message of the last failing call on this thread ("" if none). */
 const char *hm_last_error(void);
+/* Library version number (no reference counterpart). */
 int hm_version(void);
 
 /* BLOCKRANK(T) (src/HierarchicalMatrices.jl:5): rank for machine epsilon eps. */
@@ -146,10 +150,13 @@ int hm_bary_factors(int kernel, int rank, double a, double b, double c, double d
 
 /* size(H) (src/hierarchical.jl:33-47). */
 int hm_size(const hm_handle *h, int64_t *m, int64_t *n);
-/* Storage type of h (HM_F64 / HM_F32 / HM_DF64). */
+/* Storage type of h (HM_F64 / HM_F32 / HM_DF64): the element type T of the
+   KernelMatrix{T} type of src/KernelMatrix.jl:1, plus the DF64 form. */
 int hm_storage(const hm_handle *h);
 
-/* Statistics: out[0..] = barycentric blocks, dense blocks, tree depth, row slots,
+/* Statistics (no reference counterpart; the block counts are those of the
+   tree src/KernelMatrix.jl:47-116 builds):
+   out[0..] = barycentric blocks, dense blocks, tree depth, row slots,
    column slots, canonical stored values, reference-layout values, values this
    build stores, dense values, row segments, max panel width, device bytes,
    kernel launches per single-RHS hm_mul with the side stream on (the default).
@@ -204,21 +211,23 @@ int hm_mul_drow(hm_handle *h, int transposed, const void *v, int64_t ldv, void *
 int hm_mul_strided(hm_handle *h, const void *x, int64_t lenx, int64_t jstart, int64_t incx,
                    void *y, int64_t leny, int64_t istart, int64_t incy, void *stream);
 
-/* H * v with HOST arrays (u = H v or u += H v): copies v to the device, runs
-   hm_mul and brings the result back; synchronous.  When u is page-locked
-   (cudaHostAlloc / cudaHostRegister) and the product ends by combining its
-   near and far fields, that last kernel writes u directly; otherwise the
-   result is copied back.  When v is page-locked, the leaf panels cover every
-   row of v once and the near field starts after the leaf stage, the leaf
-   stage reads v from the host and stores it on the device as it goes,
-   instead of a copy before the product.  The launches are replayed from a CUDA graph from
-   the second call with the same right-hand-side count, accumulate flag and
-   destination. */
+/* H * v with HOST arrays (u = H v or u += H v; the reference's
+   mul!(u, K, v) and K * v on Julia arrays, src/KernelMatrix.jl:5-45):
+   copies v to the device, runs hm_mul and brings the result back;
+   synchronous.  When u is page-locked (cudaHostAlloc / cudaHostRegister)
+   and the product ends by combining its near and far fields, that last
+   kernel writes u directly; otherwise the result is copied back.  When v is
+   page-locked, the leaf panels cover every row of v once and the near field
+   starts after the leaf stage, the leaf stage reads v from the host and
+   stores it on the device as it goes, instead of a copy before the product.
+   The launches are replayed from a CUDA graph from the second call with the
+   same right-hand-side count, accumulate flag and destination. */
 int hm_mul_host(hm_handle *h, const void *v, void *u, int nrhs, int accumulate);
 
 /* Exact dense rows: out[q] = sum_j f(x[rows[q]], y[j]) b[j] evaluated in FP64
    with double-double accumulation, on the handle's points (DEVICE b, rows,
-   out).  Used to state the error of a compressed product. */
+   out).  Used to state the error of a compressed product (the reference's
+   own check multiplies the dense Matrix(K), examples/Kernel.jl:73-78). */
 int hm_direct_rows(hm_handle *h, const double *b, const int64_t *rows, int64_t nrows, double *out,
                    void *stream);
 
@@ -371,11 +380,13 @@ int hm_profile_read(hm_handle *h, double *ms, int64_t *launches, int n, int rese
    records (only the first nmax are written), or a negative status. */
 int hm_profile_timeline(hm_handle *h, double *out, int nmax);
 
+/* Releases a handle (Julia's garbage collector, in the reference). */
 void hm_free(hm_handle *h);
 
 /* --- host planner (no GPU needed) ------------------------------------------
-   The block tree and the flattened tables that hm_kernelmatrix_build uploads,
-   for inspection and host-side tests.  Same validation and status codes as
+   The block tree of KernelMatrix (src/KernelMatrix.jl:47-116, split by
+   indsplit, src/BarycentricMatrix.jl:299-307) and the flattened tables that
+   hm_kernelmatrix_build uploads, for inspection and host-side tests.  Same validation and status codes as
    hm_kernelmatrix_build. */
 typedef struct hm_plan hm_plan;
 int hm_plan_create(const double *x, int64_t nx, const double *y, int64_t ny, double a, double b,
