@@ -1053,7 +1053,8 @@ int launch_tree_wide(hm_handle *h, const MulArgs<S> &ma, cudaStream_t st, A *t, 
             // two right-hand sides per lane from 64 on (half the shared-memory reads per FMA)
             const int qpl = (G == 1 && k >= 64) ? 2 : 1;
             auto kern = qpl == 2 ? m2l_w<A, R, 2, G> : m2l_w<A, R, 1, G>;
-            const size_t smem = (size_t)kWideWarps * G * 2 * ((size_t)h->fstride + QL * qpl * R) * sizeof(A);
+            const size_t smem =
+                (size_t)kWideWarps * G * m2l_w_group_vals(h->fstride, QL * qpl, R, (int)sizeof(A)) * sizeof(A);
             HM_TRY(ensure_smem(kern, smem));
             const int64_t groups = (int64_t)h->n_m2l_rows * ((k + QL * qpl - 1) / (QL * qpl));
             HM_TRY(launch_k("m2l_w", kern, dim3(ctas(groups)), dim3(32 * kWideWarps), smem, st, pdl_on && chain,

@@ -257,7 +257,7 @@ __global__ void ring_part(MulArgs<float> ma, const hm_seg *segs, int nsegs, cons
 // Tree passes for 32 and more right-hand sides (hm_wide.cu): lane q of a
 // warp's group of QL = 32 / G lanes owns right-hand sides q + QL p (p < QPL)
 // of a chunk of QL QPL; R (the rank) a multiple of 4.  m2l_w: a group per
-// (row slot, chunk), shared memory kWideWarps * G * 2 * (fstride + QL QPL R)
+// (row slot, chunk), shared memory kWideWarps * G * m2l_w_group_vals(...)
 // values; leaf_up_w: a group per (panel, chunk), panels row-major with ld ==
 // width == R and at most cap rows (a multiple of 8), shared memory
 // kWideWarps * G * ((G == 1 ? cap R : 0) + QL QPL (cap + 4)) values;
@@ -266,6 +266,15 @@ __global__ void ring_part(MulArgs<float> ma, const hm_seg *segs, int nsegs, cons
 // (2 R^2 + locals * QL R) values.
 constexpr int kWideWarps = 4;
 constexpr int kWideTaskThreads = 256;
+// Values of one m2l_w group's buffer: two stages of (an F block, the chunk's
+// qw x r coefficients), then 16 bytes of padding.  Without the padding the
+// groups of a warp (2 x 560 floats apart for 8 right-hand sides, rank 20)
+// start on the same shared-memory bank, and their simultaneous 16-byte reads
+// of different F blocks would conflict.
+__host__ __device__ constexpr int m2l_w_group_vals(int fstride, int qw, int r, int esize)
+{
+    return 2 * (fstride + qw * r) + 16 / esize;
+}
 template <typename A, int R, int QPL, int G>
 __global__ void m2l_w(const hm_m2l_row *rows, int nrows, const hm_m2l_ent *ents, const A *F, int fstride, const A *t,
                       A *s, int k);

@@ -115,7 +115,8 @@ __global__ void __launch_bounds__(kWideWarps * 32)
     const hm_m2l_row Rw = rows[w / nq];
     const int q0 = (int)(w % nq) * QW, qc = min(QW, k - q0);
     const int stage_vals = fstride + QW * R;
-    A *buf = reinterpret_cast<A *>(wide_smem) + ((size_t)wib * G + g) * 2 * stage_vals;
+    A *buf = reinterpret_cast<A *>(wide_smem) +
+             ((size_t)wib * G + g) * m2l_w_group_vals(fstride, QW, R, (int)sizeof(A));
     auto fetch = [&](int e, int b) {
         const hm_m2l_ent E = ents[e];
         A *fb = buf + b * stage_vals;
